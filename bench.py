@@ -1,0 +1,392 @@
+#!/usr/bin/env python
+"""Throughput of the Taylor-Couette time step on GB300, in Mcell-steps/s.
+
+Workload (default, "C2"): 512 x 512 x 384 (theta x z x r) cells, radial
+tanh clustering at both walls (ISTR=4, STR3=4; the configuration's ISTR=1 is
+undefined in the reference grid generator and maps to 4), RINT=1, REXT=1.4,
+ALX3D=2*pi, 1/NU=5000, inner cylinder oscillating (VIROTINT=1, AMPL_PERT=0.1,
+FREQ_PERT=0.5), RK3, variable dt (CFLMAX=1.2, DTMIN=1e-5), seeded
+Couette-plus-noise start (amplitude 0.01).  One "step" is one full RK3 time
+step (three substeps) with the dt rule of main.F90, FP64 throughout.
+
+  value  : steps with the state resident in HBM (tc_run, one host sync)
+  e2e    : through the C ABI with host buffers: tc_set_state from pinned host
+           memory, one tc_run(1) per step (the host reads dt/time back each
+           step, as the reference's host loop does), tc_get_state at the end
+  roofline: the kernel class with the largest share of the timed region,
+           algorithmic HBM bytes per launch / its mean CUDA-event duration
+  cpu_baseline: the CPU oracle (C++ restatement of the reference's serial
+           algorithm) on the host cores, on a bounded sample of the workload
+
+Under torchrun (N > 1) every rank advances its own replica (the time step of
+one run does not shard without the reference's halo and transpose exchanges),
+so scaling is weak and value sums the replicas.
+``--impl reference`` times the CPU oracle alone on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "C2": dict(nthm=512, nzm=512, nrm=384, istr=4, str=4.0, ren=5000.0, sizepert=0.1, omegapert=0.5,
+               idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=1e-2),
+    "C1": dict(nthm=64, nzm=64, nrm=64, istr=0, ren=1000.0, idtv=1, limitCFL=1e3, dtmin=1e-3, dtmax=1e-3),
+    "C3": dict(nthm=1024, nzm=768, nrm=512, istr=4, str=4.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
+               dtmin=1e-5, dtmax=1e-2),
+}
+DESCR = {
+    "C2": "512x512x384 theta x z x r, ISTR=4 STR3=4, RINT=1 REXT=1.4, 1/NU=5000, AMPL_PERT=0.1 FREQ_PERT=0.5, "
+          "RK3, variable dt CFLMAX=1.2 DTMIN=1e-5, seeded Couette+noise 0.01",
+    "C1": "64x64x64, ISTR=0, RINT=1 REXT=1.4, 1/NU=1000, RK3, dt=1e-3, seeded Couette+noise 0.01",
+    "C3": "1024x768x512, ISTR=4 STR3=4, ROTP=0.1, 1/NU=2e4, RK3, variable dt CFLMAX=1.2 (FP64 form)",
+}
+
+# Algorithmic HBM bytes per cell and launch of each kernel class (FP64):
+# the compulsory reads and writes of the arrays the kernel's job needs, each
+# counted once (neighbour re-reads are not algorithmic).  P_SPEC is the
+# fraction of a real field the half spectrum occupies: (nthm/2+1)/nthm complex.
+def algorithmic_bytes(cls: str, nt: int, nz: int, nr: int, rk_substep_mix: float) -> float:
+    cells = nt * nz * nr
+    spec = (nt // 2 + 1) * 2 / nt          # complex doubles per cell, in doubles
+    per_cell = {
+        # read qt qr qz pr (+ ru1..3 on substeps with ro != 0), write rhs x3, ru x3
+        "momentum": 8 * (4 + 3 * rk_substep_mix + 6),
+        # read rhs x3 and q x3, write q x3
+        "radial_solve": 8 * 9,
+        # read qt qr qz, write half spectrum
+        "div_theta_fft": 8 * (3 + spec),
+        # read + write half spectrum
+        "z_fft": 8 * 2 * spec,
+        "pressure_tridiag": 8 * 2 * spec,
+        # read half spectrum, write phi
+        "theta_inverse_fft": 8 * (spec + 1),
+        # read phi q x3 pr, write q x3 pr
+        "correct": 8 * 9,
+    }
+    return per_cell.get(cls, 0.0) * cells
+
+
+def base_bou(**kw):
+    d = dict(nthm=64, nzm=64, nrm=64, nsst=3, idtv=1, nread=1, ntst=10 ** 8, tout=1.0e9, tmax=1.0e9,
+             ireset=0, walltimemax=1e9, alx3=2 * math.pi, rint=1.0, rext=1.4, istr=0, str=4.0, lamb=1.0,
+             virotint=1.0, virotext=0.0, sizepert=0.0, omegapert=0.0, ren=1000.0, romeg=0.0, resid=1e-2,
+             limitCFL=1.2, tsta=0.0, starea=0, dtmin=1e-5, dtmax=1e-3, limitVel=1e3, cfllim=1.0,
+             nslabr=0, dpthcut=0, dpstave=0, tframe2d=1.0, dpfullf=0, tframe3d=1.0,
+             minstrt=0, minstrz=0, multmin=0)
+    d.update(kw)
+    return d
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_sample(workload: str, seconds: float, threads: int):
+    """Time the CPU oracle on a bounded sample of the workload: the same theta
+    x z plane with the radial extent cut so one step takes a second or so."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tc_ref
+    import __graft_entry__ as entry
+    entry.load()
+    import tc_gb300.initial as ini
+    tc_ref.build()
+    tc_ref.set_threads(threads)
+    w = dict(WORKLOADS[workload])
+    nr_sample = min(w["nrm"], 48)
+    w["nrm"] = nr_sample
+    bou = base_bou(**w)
+    st = ini.couette_noise(bou, seed=1234)
+    o = tc_ref.CppOracle(bou)
+    o.set_state(*st)
+    cells = bou["nthm"] * bou["nzm"] * bou["nrm"]
+    o.run(0, 1, 0.0)                      # warm-up step (page faults, plans)
+    n, t0 = 0, time.perf_counter()
+    ntime, tsim = 1, 0.0
+    while True:
+        code, tsim, _ = o.run(ntime, 1, tsim)
+        ntime += 1
+        n += 1
+        el = time.perf_counter() - t0
+        if el > seconds or n >= 200:
+            break
+    return cells * n / el / 1e6, n, el, bou
+
+
+def run_reference(args, rank: int):
+    """--impl reference: the CPU restatement of the reference's serial algorithm
+    (the Fortran reference itself cannot be built here) on the host cores."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tc_ref
+    import __graft_entry__ as entry
+    entry.load()
+    import tc_gb300.initial as ini
+    tc_ref.build()
+    tc_ref.set_threads(threads)
+    w = dict(WORKLOADS[args.workload])
+    w["nrm"] = min(w["nrm"], 48)
+    bou = base_bou(**w)
+    st = ini.couette_noise(bou, seed=1234)
+    o = tc_ref.CppOracle(bou)
+    o.set_state(*st)
+    cells = bou["nthm"] * bou["nzm"] * bou["nrm"]
+    ntime, tsim = 0, 0.0
+    for _ in range(args.warmup):
+        _, tsim, _ = o.run(ntime, 1, tsim)
+        ntime += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, tsim, _ = o.run(ntime, 1, tsim)
+        ntime += 1
+    el = time.perf_counter() - t0
+    v = cells * args.steps / el / 1e6
+    sample = (f"{bou['nthm']}x{bou['nzm']}x{bou['nrm']} slab of the {args.workload} workload "
+              f"(radial extent cut from {WORKLOADS[args.workload]['nrm']} to {bou['nrm']}), "
+              f"{args.steps} steps after {args.warmup} warm-up")
+    line = {"impl": "reference", "metric": "Mcell-steps/s", "value": v, "unit": "Mcell-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {DESCR[args.workload]}", "cells_sample": cells},
+            "cpu_baseline": {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__ as entry
+    tc = entry.load()
+    import tc_gb300.build as tb
+    tb.build()
+    import tc_gb300.initial as ini
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    bou = base_bou(**WORKLOADS[args.workload])
+    nt, nz, nr = bou["nthm"], bou["nzm"], bou["nrm"]
+    cells = nt * nz * nr
+    stream = torch.cuda.current_stream()
+    g = tc.TaylorCouette(bou)
+    g.set_stream(stream.cuda_stream)
+
+    # seeded start in pinned host memory (reference layout)
+    st = ini.couette_noise(bou, seed=1234 + rank)
+    pinned = []
+    for a in st:
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = a
+        pinned.append(t.numpy())
+    del st
+    g.set_state(*pinned)
+
+    # warm-up
+    code, ntime, tsim, dt = g.run(args.warmup, 0, 0.0)
+    if code != 0:
+        raise SystemExit(f"warm-up stopped with error code {code}")
+
+    # ---- device-resident timed region --------------------------------------
+    clocks = Clocks(local) if rank == 0 else None
+    g.profile(True)
+    barrier()
+    n0 = g.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    code, ntime, tsim, dt = g.run(args.steps, ntime, tsim)
+    e1.record(stream)
+    barrier()
+    launches = g.launch_count - n0
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    prof = g.profile_read()
+    g.profile(False)
+    clk = clocks.stop() if clocks else None
+    if code != 0:
+        raise SystemExit(f"timed steps stopped with error code {code}")
+    value = world * cells * args.steps / (ms * 1e-3) / 1e6
+
+    # ---- end to end through the C ABI with host buffers ----------------------
+    e2e = None
+    if not args.no_e2e:
+        barrier()
+        e0.record(stream)
+        g.set_state(*pinned)
+        nt2, t2 = 0, 0.0
+        for _ in range(args.steps):
+            code, nt2, t2, _ = g.run(1, nt2, t2)
+        qt_o, qr_o, qz_o, pr_o = g.get_state()
+        e1.record(stream)
+        barrier()
+        ms_e2e = max_over_ranks(e0.elapsed_time(e1))
+        h2d = sum(a.nbytes for a in pinned)
+        d2h = h2d
+        e2e = {"value": world * cells * args.steps / (ms_e2e * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+               "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+               "ms_per_step": ms_e2e / args.steps,
+               "note": "state in (tc_set_state) and out (tc_get_state) once per timed run, amortised per step; "
+                       "dt/time read back every step"}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel class ------------------------------
+    peak_gbs, peak_kind = load_peaks()
+    fp64_peak = g.measure_fp64_peak()
+    dom = max((k for k in prof if k not in ("step_control", "reduction", "layout")), key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    rk_mix = 2.0 / 3.0   # ru read on 2 of the 3 RK3 substeps
+    bytes_launch = algorithmic_bytes(dom, nt, nz, nr, rk_mix)
+    achieved = bytes_launch / (dom_ms / dom_n * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tj = json.load(f)
+        ent = tj.get(args.workload, {}).get(dom)
+        if ent:
+            traffic = ent.get("bytes_per_launch")
+    total_ms = sum(v[0] for v in prof.values())
+    shares = {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}
+
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, n, el, sb = cpu_sample(args.workload, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{n} steps of a {sb['nthm']}x{sb['nzm']}x{sb['nrm']} slab of the workload "
+                         f"({el:.1f} s, C++ oracle, OpenMP on all host cores)"}
+
+    line = {
+        "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Couette+noise start)",
+        "config": {"workload": f"{args.workload}: {DESCR[args.workload]}", "grid": [nt, nz, nr],
+                   "cells": cells, "precision": "FP64 plain", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: every field is "
+                         f"{cells * 8 / 1e6:.0f} MB, 12 fields resident"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved / peak_gbs, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": bytes_launch,
+                     "ms_per_launch": dom_ms / dom_n, "launches": dom_n},
+        "fp64": {"probe_tflops": fp64_peak,
+                 "note": "FP64 FMA rate of the device measured by a probe kernel; the FP64 path is "
+                         "bounded by it rather than by HBM"},
+        "kernel_shares": shares,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "sim": {"time": tsim, "last_dt": dt},
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

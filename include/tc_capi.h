@@ -1,0 +1,198 @@
+/*
+ * tc_capi.h -- C ABI of the GB300 Taylor-Couette time step (libtcgb300.so).
+ *
+ * Drop-in for the time-step path of rodosti/Taylor-Couette-AFiD.  The
+ * reference has no plugin API: its routines take no arguments and talk
+ * through the Fortran modules `param` and `local_arrays` (param.F90:4-102).
+ * Each entry point below replaces the reference routine(s) named in its
+ * comment; a Fortran host binds them with ISO_C_BINDING (see INTEGRATION.md
+ * and taylor-couette-afid_gb300/fortran/tc_gpu_mod.F90).
+ *
+ * Conventions
+ *  - Every function returns an int status: 0 = OK.  165, 166, 169, 266, 333
+ *    and 555 are the reference's error codes (main.F90:148-259); 1000-1999 are
+ *    CUDA or allocation failures; 2000-2999 are invalid arguments or
+ *    configurations.  tc_last_error() returns a message for the last failure.
+ *  - Host arrays of 3-D fields use the reference layout: Fortran
+ *    q(1:nr, 0:nzm+1, 0:nthm+1), r fastest, one periodic halo cell in z and
+ *    theta (InitVariables.F90:26-35).  pr/qt/qz entries at k = nr are not
+ *    part of the step (never read by any routine of the path).
+ *  - All work is ordered on the handle's CUDA stream.  Calls that return
+ *    host scalars synchronise that stream.  A handle is used by one host
+ *    thread at a time; distinct handles are independent.
+ *  - All arithmetic is IEEE FP64.
+ */
+#ifndef TC_CAPI_H
+#define TC_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* bou.in values, in file order (ReadInputFile.F90:17-39, param.F90:9-27). */
+typedef struct tc_bou {
+    int nthm, nzm, nrm, nsst, idtv, nread;
+    int ntst; double tout, tmax; int ireset; double walltimemax;
+    double alx3, rint, rext; int istr; double str, lamb;
+    double virotint, virotext, sizepert, omegapert;
+    double ren, romeg, resid, limitCFL;
+    double tsta; int starea;
+    double dtmin, dtmax, limitVel, cfllim;
+    int nslabr, dpthcut, dpstave; double tframe2d;
+    int dpfullf; double tframe3d;
+    int minstrt, minstrz, multmin;
+} tc_bou;
+
+typedef struct tc_handle tc_handle;
+
+/* 1-D grid/coefficient arrays, 0-based (entry m = reference index m+1). */
+enum tc_grid_array {
+    TC_G_RC = 0, TC_G_RM, TC_G_G2RC, TC_G_G2RM, TC_G_USRC, TC_G_USRM,
+    TC_G_UDX1VIS1, TC_G_UDX1VIS2, TC_G_UDX1QM, TC_G_UDX2C, TC_G_UDX2M,
+    TC_G_RUDX2C, TC_G_UDX2RM,
+    TC_G_AP1J, TC_G_AM1J, TC_G_AC1J, TC_G_AP2J, TC_G_AM2J, TC_G_AC2J,
+    TC_G_AP2JE, TC_G_AM2JE, TC_G_AC2JE, TC_G_AP3J, TC_G_AM3J, TC_G_AC3J,
+    TC_G_APPH, TC_G_AMPH, TC_G_ACPH,
+    TC_G_AK1,  /* length nthm */
+    TC_G_AK3,  /* length nzm  */
+    TC_G_COUNT
+};
+
+/* 3-D arrays readable through tc_get_field (reference layout). */
+enum tc_field {
+    TC_F_QT = 0, TC_F_QR, TC_F_QZ, TC_F_PR, TC_F_DPH,       /* (nr, nzm+2, nthm+2) */
+    TC_F_RHS_T, TC_F_RHS_R, TC_F_RHS_Z,                    /* (nr, nzm, nthm): rhs of each component */
+    TC_F_RU1, TC_F_RU2, TC_F_RU3,                          /* (nr, nzm, nthm) */
+    TC_F_DQ, TC_F_HR, TC_F_QCAP,                           /* explicit terms of qt, qr, qz */
+    TC_F_COUNT
+};
+
+/* ---- host-only entry points (no GPU needed) ---------------------------- */
+
+/* ReadInputFile.F90:10-74: parse bou.in (list-directed, one header record
+ * before each value record).  Returns 0, or 2001 (cannot open) / 2002
+ * (malformed).  err (may be NULL) receives a message. */
+int tc_read_bou(const char* path, tc_bou* out, char* err, int errlen);
+
+/* CreateGrid.F90:24-324 and InitPressureSolver.F90:22-110 on the host:
+ * writes grid array `which` (enum tc_grid_array) into out[0..len-1] and
+ * returns its length, or a negative status on bad input. */
+int tc_grid_array(const tc_bou* cfg, int which, double* out, int len);
+
+/* Library version string. */
+const char* tc_version(void);
+
+/* ---- handle lifecycle --------------------------------------------------- */
+
+/* InitTimeMarchScheme + InitVariables + CreateGrid + InitPressureSolver
+ * (main.F90:70-94): validate cfg, build the grid and coefficients, allocate
+ * all device state on the current CUDA device, zero it.  Fields start at zero
+ * and time at 0; load a start with tc_set_state. */
+int tc_create(const tc_bou* cfg, tc_handle** out);
+void tc_destroy(tc_handle* h);
+const char* tc_last_error(const tc_handle* h);   /* h may be NULL */
+
+/* Order all later work of h on this CUDA stream (cudaStream_t, NULL = the
+ * legacy default stream). */
+int tc_set_stream(tc_handle* h, void* cuda_stream);
+
+/* ---- state transfer (ReadFlowField.F90:135-140 / WriteFlowField) -------- */
+
+/* Copy a start into the handle: host arrays in the reference layout; halo
+ * entries are ignored (the device keeps the fields periodic by index wrap).
+ * qr(1,:,:) and qr(nr,:,:) are forced to 0 (wall values).  pr may be NULL
+ * (zero pressure, as ReadFlowField leaves it).  Also zeroes ru1..ru3. */
+int tc_set_state(tc_handle* h, const double* qt, const double* qr,
+                 const double* qz, const double* pr);
+/* Copy the state back into host arrays in the reference layout with the
+ * periodic halo filled (the values update_halo would leave). */
+int tc_get_state(tc_handle* h, double* qt, double* qr, double* qz, double* pr);
+/* Copy any 3-D array (enum tc_field) back; see the shapes in the enum. */
+int tc_get_field(tc_handle* h, int which, double* out);
+/* Overwrite a 3-D array (enum tc_field) from the host, same shapes. */
+int tc_set_field(tc_handle* h, int which, const double* in);
+
+/* ---- the time step ------------------------------------------------------ */
+
+/* TimeMarcher.F90:12-67: one full time step of length dt from time `time`
+ * (all NSST substeps).  Asynchronous; returns after enqueueing. */
+int tc_time_marcher(tc_handle* h, double dt, double time);
+
+/* main.F90:152-226 restricted to the step path: for each of nsteps steps,
+ * CalcMaxCFL, the dt rule (variable dt: DTMIN for ntime <= 1, then
+ * min(CFLMAX/instCFL, DTMAX); IDTV=0 runs with dt = DTMAX because the
+ * reference never assigns dt in that branch), TimeMarcher, time += dt, and on
+ * output steps (ntime == 1 or mod(time,TOUT) < dt) the velocity-limit and
+ * divergence checks.  Step control lives on the device; the host reads it
+ * back only on output steps.  Returns the first error code raised (166, 165,
+ * 266, 169, 333, 555) or 0; *time, *dt and *ntime are updated. */
+int tc_run(tc_handle* h, int nsteps, int* ntime, double* time, double* dt);
+
+/* ---- routines of one substep, for parity bisection ---------------------- */
+
+/* TimeMarcher.F90:20-23: beta, InnerCylVelocity, SlipBCs for a step of
+ * length dt starting at time; then TimeMarcher.F90:27-29 for substep ns
+ * (1-based) is selected with tc_set_substep. */
+int tc_begin_step(tc_handle* h, double dt, double time);
+int tc_set_substep(tc_handle* h, int ns);
+/* ExplicitTermsQT/QR/QZ (ExplicitTermsQT.F90:22-129, ExplicitTermsQR.F90:159-280,
+ * ExplicitTermsQZ.F90:311-390): explicit terms into DQ, HR, QCAP. */
+int tc_explicit_terms(tc_handle* h);
+/* ImplicitAndUpdateQT/QR/QZ (ImplicitAndUpdateQT.F90:26-117,
+ * ImplicitAndUpdateQR.F90:152-195, ImplicitAndUpdateQZ.F90:223-312) with
+ * SolveImpEqnUpdate_QT/QR/QZ (SolveImpEqnUpdate_QT.F90:22-80,
+ * _QR.F90:109-151, _QZ.F90:177-225): rhs and ru from DQ/HR/QCAP, radial
+ * implicit solve, q += dq, qr walls reset. */
+int tc_implicit_and_update(tc_handle* h);
+/* Explicit terms fused with the rhs and ru update (no DQ/HR/QCAP arrays);
+ * equivalent to the explicit half of the two calls above. */
+int tc_explicit_and_rhs(tc_handle* h);
+/* SolveImpEqnUpdate_QT/QR/QZ alone, on the RHS_T/R/Z arrays. */
+int tc_solve_imp_eqn_update(tc_handle* h);
+/* CalcLocalDivergence.F90:19-40: DPH = div(q)/(al*dt). */
+int tc_calc_local_divergence(tc_handle* h);
+/* SolvePressureCorrection.F90:129-290: DPH <- phi.  The singular
+ * k_theta = k_z = 0 mode is solved with phi(nrm) = 0 (its last equation is
+ * the dependent one); LAPACK in the reference divides by a roundoff pivot
+ * there instead, which only moves phi by a radially constant offset. */
+int tc_solve_pressure_correction(tc_handle* h);
+/* CorrectVelocity.F90:302-340 and CorrectPressure.F90:352-393. */
+int tc_correct_velocity(tc_handle* h);
+int tc_correct_pressure(tc_handle* h);
+
+/* ---- reductions (host scalars; these synchronise) ------------------------ */
+
+/* CalcMaxCFL.F90:12-49 */
+int tc_calc_max_cfl(tc_handle* h, double* cflm);
+/* CheckDivergence.F90:60-95 */
+int tc_check_divergence(tc_handle* h, double* qmax);
+/* CalcTorque.F90:107-157 (the host writes torquenu.out itself). */
+int tc_calc_torque(tc_handle* h, double* inner, double* outer);
+/* CalcVelocityStats.F90:11-68: vmax(3) and the three rms values. */
+int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3);
+
+/* ---- measurement helpers ------------------------------------------------ */
+
+/* Number of kernels one tc_time_marcher call launches. */
+int tc_kernels_per_step(const tc_handle* h);
+/* Device bytes held by the handle. */
+long long tc_device_bytes(const tc_handle* h);
+/* Kernels launched by this handle so far (all entry points). */
+long long tc_launch_count(const tc_handle* h);
+/* Kernels one step of tc_run launches (step control and checks included). */
+int tc_kernels_per_run_step(const tc_handle* h);
+/* Per-kernel-class timing: enable (1) or disable (0) CUDA-event brackets
+ * around every launch on the handle's stream; enabling resets the totals. */
+int tc_profile(tc_handle* h, int enable);
+/* Totals since tc_profile(h, 1): ms[c] and launches[c] for class c; returns
+ * the number of classes.  tc_profile_name(c) names class c. */
+int tc_profile_read(tc_handle* h, double* ms, long long* launches, int cap);
+const char* tc_profile_name(int cls);
+/* FP64 FMA throughput of the device in TFLOP/s (a dedicated probe kernel on
+ * the handle's stream; used as the FP64 roofline denominator). */
+int tc_measure_fp64_peak(tc_handle* h, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TC_CAPI_H */

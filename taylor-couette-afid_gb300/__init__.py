@@ -1,0 +1,321 @@
+"""tc_gb300 -- GB300 (sm_103a) Taylor-Couette time step behind a C ABI.
+
+Host-side mirror of the reference routine interface (rodosti/Taylor-Couette-AFiD):
+the methods of :class:`TaylorCouette` carry the names of the Fortran routines
+they replace (TimeMarcher, CalcMaxCFL, CheckDivergence, CalcTorque, ...) and
+call ``libtcgb300.so`` through ctypes.  There is no CPU fallback: if the
+library or a CUDA device is missing, construction raises.
+
+Arrays exchanged with the host use the reference layout.  A NumPy array of
+shape ``(nthm+2, nzm+2, nr)`` in C order is the Fortran array
+``q(1:nr, 0:nzm+1, 0:nthm+1)`` (r fastest, periodic halo in z and theta).
+
+The package directory is ``taylor-couette-afid_gb300``; load it with
+``load()`` from ``__graft_entry__`` or ``tests/conftest.py``, which register it
+as ``tc_gb300``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtcgb300.so")
+
+# error codes of main.F90:148-259
+ERRORS = {165: "CFL above CFLLIM with fixed dt", 166: "dt below DTMIN", 169: "divergence above RESID",
+          266: "velocity above VMAX", 333: "time above TMAX", 555: "NTST steps done"}
+
+GRID_ARRAYS = ["rc", "rm", "g2rc", "g2rm", "usrc", "usrm", "udx1vis1", "udx1vis2", "udx1qm", "udx2c",
+               "udx2m", "rudx2c", "udx2rm", "ap1j", "am1j", "ac1j", "ap2j", "am2j", "ac2j", "ap2je",
+               "am2je", "ac2je", "ap3j", "am3j", "ac3j", "apph", "amph", "acph", "ak1", "ak3"]
+FIELDS = ["qt", "qr", "qz", "pr", "dph", "rhs_t", "rhs_r", "rhs_z", "ru1", "ru2", "ru3", "dq", "hr", "qcap"]
+_HALO_FIELDS = 5
+
+
+class Bou(ctypes.Structure):
+    """tc_bou: bou.in values in file order (ReadInputFile.F90:17-39)."""
+    _fields_ = [
+        ("nthm", ctypes.c_int), ("nzm", ctypes.c_int), ("nrm", ctypes.c_int), ("nsst", ctypes.c_int),
+        ("idtv", ctypes.c_int), ("nread", ctypes.c_int),
+        ("ntst", ctypes.c_int), ("tout", ctypes.c_double), ("tmax", ctypes.c_double),
+        ("ireset", ctypes.c_int), ("walltimemax", ctypes.c_double),
+        ("alx3", ctypes.c_double), ("rint", ctypes.c_double), ("rext", ctypes.c_double),
+        ("istr", ctypes.c_int), ("str", ctypes.c_double), ("lamb", ctypes.c_double),
+        ("virotint", ctypes.c_double), ("virotext", ctypes.c_double), ("sizepert", ctypes.c_double),
+        ("omegapert", ctypes.c_double),
+        ("ren", ctypes.c_double), ("romeg", ctypes.c_double), ("resid", ctypes.c_double),
+        ("limitCFL", ctypes.c_double),
+        ("tsta", ctypes.c_double), ("starea", ctypes.c_int),
+        ("dtmin", ctypes.c_double), ("dtmax", ctypes.c_double), ("limitVel", ctypes.c_double),
+        ("cfllim", ctypes.c_double),
+        ("nslabr", ctypes.c_int), ("dpthcut", ctypes.c_int), ("dpstave", ctypes.c_int),
+        ("tframe2d", ctypes.c_double),
+        ("dpfullf", ctypes.c_int), ("tframe3d", ctypes.c_double),
+        ("minstrt", ctypes.c_int), ("minstrz", ctypes.c_int), ("multmin", ctypes.c_int),
+    ]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Bou":
+        b = cls()
+        for name, typ in cls._fields_:
+            if name in d:
+                setattr(b, name, int(d[name]) if typ is ctypes.c_int else float(d[name]))
+        return b
+
+    def to_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class TCError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+# C ABI signatures: name -> (restype, argtypes)
+_vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+SIGNATURES = {
+    "tc_read_bou": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Bou), ctypes.c_char_p, ctypes.c_int]),
+    "tc_grid_array": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_int, _dp, ctypes.c_int]),
+    "tc_version": (ctypes.c_char_p, []),
+    "tc_create": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.POINTER(_vp)]),
+    "tc_destroy": (None, [_vp]),
+    "tc_last_error": (ctypes.c_char_p, [_vp]),
+    "tc_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "tc_set_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "tc_get_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "tc_get_field": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "tc_set_field": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "tc_time_marcher": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double]),
+    "tc_run": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp]),
+    "tc_begin_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double]),
+    "tc_set_substep": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tc_explicit_terms": (ctypes.c_int, [_vp]),
+    "tc_implicit_and_update": (ctypes.c_int, [_vp]),
+    "tc_explicit_and_rhs": (ctypes.c_int, [_vp]),
+    "tc_solve_imp_eqn_update": (ctypes.c_int, [_vp]),
+    "tc_calc_local_divergence": (ctypes.c_int, [_vp]),
+    "tc_solve_pressure_correction": (ctypes.c_int, [_vp]),
+    "tc_correct_velocity": (ctypes.c_int, [_vp]),
+    "tc_correct_pressure": (ctypes.c_int, [_vp]),
+    "tc_calc_max_cfl": (ctypes.c_int, [_vp, _dp]),
+    "tc_check_divergence": (ctypes.c_int, [_vp, _dp]),
+    "tc_calc_torque": (ctypes.c_int, [_vp, _dp, _dp]),
+    "tc_calc_velocity_stats": (ctypes.c_int, [_vp, _dp, _dp]),
+    "tc_kernels_per_step": (ctypes.c_int, [_vp]),
+    "tc_device_bytes": (ctypes.c_longlong, [_vp]),
+    "tc_launch_count": (ctypes.c_longlong, [_vp]),
+    "tc_kernels_per_run_step": (ctypes.c_int, [_vp]),
+    "tc_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tc_profile_read": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "tc_profile_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "tc_measure_fp64_peak": (ctypes.c_int, [_vp, _dp]),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """Load libtcgb300.so (build it first with ``tc_gb300.build.build()``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it (python {HERE}/build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def read_bou(path: str) -> dict:
+    """ReadInputFile.F90: parse a bou.in file into a dict of its values."""
+    b = Bou()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().tc_read_bou(path.encode(), ctypes.byref(b), err, 512)
+    if rc != 0:
+        raise TCError(rc, err.value.decode())
+    return b.to_dict()
+
+
+def grid_array(bou: dict, name: str) -> np.ndarray:
+    """CreateGrid / InitPressureSolver arrays computed on the host (no GPU)."""
+    b = Bou.from_dict(bou)
+    n = max(int(bou["nrm"]) + 1, int(bou["nthm"]), int(bou["nzm"]))
+    out = np.zeros(n)
+    rc = lib().tc_grid_array(ctypes.byref(b), GRID_ARRAYS.index(name), _dptr(out), n)
+    if rc < 0:
+        raise TCError(-rc, lib().tc_last_error(None).decode())
+    return out[:rc].copy()
+
+
+class TaylorCouette:
+    """One simulation instance resident on the current CUDA device."""
+
+    def __init__(self, bou: dict):
+        self.L = lib()
+        self.bou = dict(bou)
+        self._b = Bou.from_dict(bou)
+        h = ctypes.c_void_p()
+        rc = self.L.tc_create(ctypes.byref(self._b), ctypes.byref(h))
+        if rc != 0:
+            raise TCError(rc, self.L.tc_last_error(None).decode())
+        self.h = h
+        self.nthm, self.nzm, self.nrm = self._b.nthm, self._b.nzm, self._b.nrm
+        self.nr = self.nrm + 1
+        self.halo_shape = (self.nthm + 2, self.nzm + 2, self.nr)
+        self.plain_shape = (self.nthm, self.nzm, self.nr)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc: int):
+        if rc != 0:
+            raise TCError(rc, self.L.tc_last_error(self.h).decode())
+
+    # ---- state -----------------------------------------------------------
+    def set_stream(self, stream_ptr: int):
+        self._ck(self.L.tc_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def set_state(self, qt, qr, qz, pr=None):
+        """ReadFlowField: load a start (reference layout, halos ignored)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (qt, qr, qz)]
+        for a in arrs:
+            if a.shape != self.halo_shape:
+                raise ValueError(f"expected shape {self.halo_shape}, got {a.shape}")
+        p = None
+        if pr is not None:
+            p = np.ascontiguousarray(pr, dtype=np.float64)
+            if p.shape != self.halo_shape:
+                raise ValueError(f"expected shape {self.halo_shape}, got {p.shape}")
+        self._ck(self.L.tc_set_state(self.h, *[_dptr(a) for a in arrs], _dptr(p) if p is not None else None))
+
+    def get_state(self):
+        out = [np.empty(self.halo_shape) for _ in range(4)]
+        self._ck(self.L.tc_get_state(self.h, *[_dptr(a) for a in out]))
+        return tuple(out)
+
+    def get_field(self, name: str) -> np.ndarray:
+        w = FIELDS.index(name)
+        a = np.empty(self.halo_shape if w < _HALO_FIELDS else self.plain_shape)
+        self._ck(self.L.tc_get_field(self.h, w, _dptr(a)))
+        return a
+
+    def set_field(self, name: str, a: np.ndarray):
+        w = FIELDS.index(name)
+        shp = self.halo_shape if w < _HALO_FIELDS else self.plain_shape
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(shp)
+        self._ck(self.L.tc_set_field(self.h, w, _dptr(a)))
+
+    # ---- the step (TimeMarcher.F90, main.F90) -------------------------------
+    def time_marcher(self, dt: float, time: float):
+        self._ck(self.L.tc_time_marcher(self.h, float(dt), float(time)))
+
+    def run(self, nsteps: int, ntime: int, time: float, dt: float = 0.0):
+        """main.F90 loop: returns (errorcode, ntime, time, dt)."""
+        n, t, d = ctypes.c_int(ntime), ctypes.c_double(time), ctypes.c_double(dt)
+        rc = self.L.tc_run(self.h, int(nsteps), ctypes.byref(n), ctypes.byref(t), ctypes.byref(d))
+        if rc != 0 and rc not in ERRORS:
+            raise TCError(rc, self.L.tc_last_error(self.h).decode())
+        return rc, n.value, t.value, d.value
+
+    # per-routine entry points (parity bisection)
+    def begin_step(self, dt: float, time: float):
+        self._ck(self.L.tc_begin_step(self.h, float(dt), float(time)))
+
+    def set_substep(self, ns: int):
+        self._ck(self.L.tc_set_substep(self.h, int(ns)))
+
+    def explicit_terms(self):
+        self._ck(self.L.tc_explicit_terms(self.h))
+
+    def implicit_and_update(self):
+        self._ck(self.L.tc_implicit_and_update(self.h))
+
+    def explicit_and_rhs(self):
+        self._ck(self.L.tc_explicit_and_rhs(self.h))
+
+    def solve_imp_eqn_update(self):
+        self._ck(self.L.tc_solve_imp_eqn_update(self.h))
+
+    def calc_local_divergence(self):
+        self._ck(self.L.tc_calc_local_divergence(self.h))
+
+    def solve_pressure_correction(self):
+        self._ck(self.L.tc_solve_pressure_correction(self.h))
+
+    def correct_velocity(self):
+        self._ck(self.L.tc_correct_velocity(self.h))
+
+    def correct_pressure(self):
+        self._ck(self.L.tc_correct_pressure(self.h))
+
+    # ---- reductions ----------------------------------------------------------
+    def calc_max_cfl(self) -> float:
+        v = ctypes.c_double()
+        self._ck(self.L.tc_calc_max_cfl(self.h, ctypes.byref(v)))
+        return v.value
+
+    def check_divergence(self) -> float:
+        v = ctypes.c_double()
+        self._ck(self.L.tc_check_divergence(self.h, ctypes.byref(v)))
+        return v.value
+
+    def calc_torque(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._ck(self.L.tc_calc_torque(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def velocity_stats(self):
+        v, r = np.zeros(3), np.zeros(3)
+        self._ck(self.L.tc_calc_velocity_stats(self.h, _dptr(v), _dptr(r)))
+        return v, r
+
+    @property
+    def kernels_per_step(self) -> int:
+        return self.L.tc_kernels_per_step(self.h)
+
+    @property
+    def device_bytes(self) -> int:
+        return self.L.tc_device_bytes(self.h)
+
+    @property
+    def launch_count(self) -> int:
+        return self.L.tc_launch_count(self.h)
+
+    @property
+    def kernels_per_run_step(self) -> int:
+        return self.L.tc_kernels_per_run_step(self.h)
+
+    def profile(self, enable: bool):
+        self._ck(self.L.tc_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        ms = np.zeros(16)
+        n = np.zeros(16, dtype=np.int64)
+        cnt = self.L.tc_profile_read(self.h, _dptr(ms), n.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), 16)
+        if cnt < 0:
+            raise TCError(cnt, "profile read")
+        return {self.L.tc_profile_name(c).decode(): (float(ms[c]), int(n[c])) for c in range(cnt)}
+
+    def measure_fp64_peak(self) -> float:
+        v = ctypes.c_double()
+        self._ck(self.L.tc_measure_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value

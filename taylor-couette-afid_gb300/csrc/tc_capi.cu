@@ -1,0 +1,616 @@
+// tc_capi.cu -- the C ABI (include/tc_capi.h): handle, device memory, the
+// step sequence and the per-routine entry points.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tc_capi.h"
+#include "tc_grid.h"
+#include "tc_kernels.cuh"
+
+using namespace tcgb;
+
+struct tc_handle {
+    tc_bou bou;
+    Grid g;
+    Dims d;
+    Consts k;
+    Coef c;
+    Fields f;
+    Plans p;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    double* stage = nullptr;
+    StepState* st_host = nullptr;   // pinned mirror
+    int sub = 0;
+    long long bytes = 0;
+    std::string err;
+    // launch accounting and optional per-kernel event timing
+    long long launches = 0;
+    bool profiling = false;
+    struct Rec { int cls; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    size_t pool_used = 0;
+    double prof_ms[16] = {0};
+    long long prof_n[16] = {0};
+};
+
+namespace {
+
+std::string g_last_error;
+
+int fail(tc_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(tc_handle* h, cudaError_t e, const char* what) {
+    return fail(h, 1000 + (int)e, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_fail(h, e_, what); } while (0)
+
+template <typename T>
+cudaError_t dalloc(tc_handle* h, T** p, size_t count) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, count * sizeof(T));
+    if (e != cudaSuccess) return e;
+    h->allocs.push_back(v);
+    h->bytes += (long long)(count * sizeof(T));
+    e = cudaMemset(v, 0, count * sizeof(T));
+    *p = (T*)v;
+    return e;
+}
+
+// Radix plan: radix-4 stages first, then 2, 3, 5.
+bool make_plan(int n, FFTPlan& P) {
+    P.n = n;
+    P.nstages = 0;
+    int m = n;
+    for (int r : {4, 2, 3, 5})
+        while (m % r == 0 && m > 1) {
+            if (P.nstages >= kMaxStages) return false;
+            P.radix[P.nstages++] = r;
+            m /= r;
+        }
+    return m == 1;
+}
+
+std::vector<double2> twiddles(int n, int count) {
+    std::vector<double2> w(count);
+    const long double tpi = 6.283185307179586476925286766559L;
+    for (int j = 0; j < count; ++j) {
+        long double a = tpi * (long double)j / (long double)n;
+        w[j] = make_double2((double)cosl(a), -(double)sinl(a));
+    }
+    return w;
+}
+
+int check(tc_handle* h) {
+    if (!h) return fail(nullptr, 2000, "null handle");
+    return 0;
+}
+
+// Kernel classes reported by tc_profile_read.
+enum { K_MOMENTUM = 0, K_RADIAL, K_DIVFFT, K_ZFFT, K_PTRI, K_THINV, K_CORRECT, K_CONTROL, K_REDUCE,
+       K_LAYOUT, K_COUNT };
+const char* const kClassNames[K_COUNT] = {"momentum", "radial_solve", "div_theta_fft", "z_fft",
+                                          "pressure_tridiag", "theta_inverse_fft", "correct",
+                                          "step_control", "reduction", "layout"};
+
+cudaEvent_t next_event(tc_handle* h) {
+    if (h->pool_used == h->pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        h->pool.push_back(e);
+    }
+    return h->pool[h->pool_used++];
+}
+
+// Enqueue `n` kernel launches of class `cls` done by `fn`, counting them and,
+// when profiling, bracketing them with events on the handle's stream.
+template <typename Fn>
+void L(tc_handle* h, int cls, int n, Fn fn) {
+    if (h->profiling) {
+        cudaEvent_t a = next_event(h), b = next_event(h);
+        cudaEventRecord(a, h->stream);
+        fn();
+        cudaEventRecord(b, h->stream);
+        h->recs.push_back({cls, a, b});
+    } else {
+        fn();
+    }
+    h->launches += n;
+    if (h->profiling) h->prof_n[cls] += n;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tc_last_error(const tc_handle* h) {
+    if (h) return h->err.c_str();
+    return g_last_error.c_str();
+}
+
+int tc_create(const tc_bou* cfg, tc_handle** out) {
+    if (!cfg || !out) return fail(nullptr, 2000, "null argument");
+    *out = nullptr;
+    tc_handle* h = new tc_handle();
+    h->bou = *cfg;
+    std::string e = build_grid(*cfg, h->g);
+    if (!e.empty()) { int r = fail(nullptr, 2003, e); delete h; return r; }
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "no CUDA device"); delete h; return r; }
+
+    const Grid& g = h->g;
+    Dims& d = h->d;
+    d.nt = cfg->nthm; d.nz = cfg->nzm; d.nr = cfg->nrm;
+    d.M = d.nt / 2; d.PH = d.M + 1; d.nzh = d.nz / 2 + 1;
+    d.P = (long long)d.nz * d.nt;
+    d.PS = (long long)d.nz * d.PH;
+    const int nr = d.nr, nrr = nr + 1;
+
+    Consts& k = h->k;
+    std::memset(&k, 0, sizeof k);
+    k.dxt = g.dxt; k.dxz = g.dxz; k.dxtq = g.dxtq; k.dxzq = g.dxzq;
+    k.ren = cfg->ren; k.romeg = cfg->romeg; k.virotint = cfg->virotint; k.virotext = cfg->virotext;
+    k.ap1j_fs0 = g.ap1j_fs[0]; k.ac1j_fs0 = g.ac1j_fs[0]; k.am1j_fs0 = g.am1j_fs[0];
+    k.ap1j_fs1 = g.ap1j_fs[1]; k.ac1j_fs1 = g.ac1j_fs[1];
+    k.ap3j_fs0 = g.ap3j_fs[0]; k.ac3j_fs0 = g.ac3j_fs[0]; k.am3j_fs0 = g.am3j_fs[0];
+    k.ap3j_fs1 = g.ap3j_fs[1]; k.ac3j_fs1 = g.ac3j_fs[1];
+    k.sizepert = cfg->sizepert; k.omegapert = cfg->omegapert; k.pi = g.pi;
+    k.rint = cfg->rint; k.rext = cfg->rext; k.lamb = cfg->lamb;
+    k.dtmin = cfg->dtmin; k.dtmax = cfg->dtmax; k.limitCFL = cfg->limitCFL; k.tout = cfg->tout;
+    k.tmax = cfg->tmax; k.limitVel = cfg->limitVel; k.resid = cfg->resid;
+    time_march_scheme(cfg->nsst, k.gam, k.rom, k.alm);
+    k.nsst = cfg->nsst; k.idtv = cfg->idtv; k.ntst = cfg->ntst;
+    k.minstrt = cfg->minstrt; k.minstrz = cfg->minstrz; k.multmin = cfg->multmin;
+    k.patterned = (cfg->minstrt * cfg->multmin + cfg->minstrz * cfg->multmin) != 0;
+
+    // 1-D coefficient arrays, each padded to nrr entries
+    std::vector<const std::vector<double>*> src = {
+        &g.usrm, &g.usrc, &g.udx2rm, &g.udx1vis1, nullptr, nullptr,
+        &g.rc, &g.udx2c, &g.udx1vis2, nullptr, nullptr,
+        &g.ap1j, &g.ac1j, &g.am1j, &g.ap2je, &g.ac2je, &g.am2je, &g.ap3j, &g.ac3j, &g.am3j,
+        &g.ap2j, &g.ac2j, &g.am2j,
+        &g.udx2m, &g.rudx2c, &g.udx1qm, &g.apph, &g.acph, &g.amph, nullptr};
+    const int ncoef = (int)src.size();
+    const int lenK = std::max(std::max(nrr, d.nt), d.nz) + 1;
+    std::vector<double> host((size_t)(ncoef + 2) * lenK, 0.0);
+    for (int a = 0; a < ncoef; ++a) {
+        double* dst = host.data() + (size_t)a * lenK;
+        if (src[a]) for (size_t m = 0; m < src[a]->size(); ++m) dst[m] = (*src[a])[m];
+    }
+    for (int m = 0; m < nrr; ++m) {
+        double rm = g.rm[m], rc = g.rc[m];
+        host[(size_t)4 * lenK + m] = m < nr ? g.dxt * 0.25 * g.usrm[m] : 0.0;              // udxt_m
+        host[(size_t)5 * lenK + m] = m < nr ? g.dxtq / (cfg->ren * (rm * rm)) : 0.0;       // udxtq_m
+        host[(size_t)9 * lenK + m] = g.dxt * 0.25 * g.usrc[m];                             // udxt_c
+        host[(size_t)10 * lenK + m] = g.dxtq / (cfg->ren * (rc * rc));                      // udxtq_c
+        host[(size_t)29 * lenK + m] = g.usrm[m] * g.usrm[m];                                // usrm2
+    }
+    for (int i = 0; i < d.nt; ++i) host[(size_t)ncoef * lenK + i] = g.ak1[i];
+    for (int j = 0; j < d.nz; ++j) host[(size_t)(ncoef + 1) * lenK + j] = g.ak3[j];
+    double* dcoef = nullptr;
+    ce = dalloc(h, &dcoef, host.size());
+    if (ce == cudaSuccess) ce = cudaMemcpy(dcoef, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "coefficient upload"); tc_destroy(h); return r; }
+    const double** cp[] = {&h->c.usrm, &h->c.usrc, &h->c.udx2rm, &h->c.udx1vis1, &h->c.udxt_m, &h->c.udxtq_m,
+                           &h->c.rc, &h->c.udx2c, &h->c.udx1vis2, &h->c.udxt_c, &h->c.udxtq_c,
+                           &h->c.ap1j, &h->c.ac1j, &h->c.am1j, &h->c.ap2je, &h->c.ac2je, &h->c.am2je,
+                           &h->c.ap3j, &h->c.ac3j, &h->c.am3j, &h->c.ap2j, &h->c.ac2j, &h->c.am2j,
+                           &h->c.udx2m, &h->c.rudx2c, &h->c.udx1qm, &h->c.apph, &h->c.acph, &h->c.amph,
+                           &h->c.usrm2};
+    for (int a = 0; a < ncoef; ++a) *cp[a] = dcoef + (size_t)a * lenK;
+    h->c.ak1 = dcoef + (size_t)ncoef * lenK;
+    h->c.ak3 = dcoef + (size_t)(ncoef + 1) * lenK;
+
+    // fields
+    Fields& f = h->f;
+    std::memset(&f, 0, sizeof f);
+    const size_t cells = (size_t)d.P * nr, faces = (size_t)d.P * nrr;
+    ce = cudaSuccess;
+#define AL(ptr, n) if (ce == cudaSuccess) ce = dalloc(h, &(ptr), (n))
+    AL(f.qt, cells); AL(f.qr, faces); AL(f.qz, cells); AL(f.pr, cells); AL(f.phi, cells);
+    AL(f.ru1, cells); AL(f.ru2, faces); AL(f.ru3, cells);
+    AL(f.rhs_t, cells); AL(f.rhs_r, faces); AL(f.rhs_z, cells);
+    AL(f.spec, (size_t)d.PS * nr);
+    double *pl = nullptr, *pd = nullptr;
+    AL(pl, (size_t)d.nzh * d.PH * nr);
+    AL(pd, (size_t)d.nzh * d.PH * nr);
+    f.pf_l = pl; f.pf_dinv = pd;
+    AL(f.icyl, (size_t)d.P);
+    AL(f.st, 1);
+    AL(f.F.base, MomFactors::doubles(nrr));
+    f.F.stride = nrr;
+    AL(f.corr, (size_t)9 * nrr);
+    AL(f.red, (size_t)6 * reduction_blocks());
+    AL(h->stage, (size_t)nrr * (d.nz + 2) * (d.nt + 2));
+#undef AL
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "device allocation"); tc_destroy(h); return r; }
+    cudaMemset(f.icyl, 1, (size_t)d.P);
+
+    // FFT plans and twiddles
+    if (!make_plan(d.M, h->p.th) || !make_plan(d.nz, h->p.z)) {
+        int r = fail(nullptr, 2003, "FFT length does not factor into 2, 3, 5"); tc_destroy(h); return r;
+    }
+    std::vector<double2> wt = twiddles(d.M, d.M), wz = twiddles(d.nz, d.nz), wr = twiddles(d.nt, d.M + 1);
+    double2 *dwt = nullptr, *dwz = nullptr, *dwr = nullptr;
+    ce = dalloc(h, &dwt, wt.size());
+    if (ce == cudaSuccess) ce = dalloc(h, &dwz, wz.size());
+    if (ce == cudaSuccess) ce = dalloc(h, &dwr, wr.size());
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwt, wt.data(), wt.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwz, wz.data(), wz.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwr, wr.data(), wr.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "twiddle upload"); tc_destroy(h); return r; }
+    h->p.th.tw = dwt; h->p.z.tw = dwz; h->p.twr = dwr;
+
+    ce = cudaMallocHost((void**)&h->st_host, sizeof(StepState));
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pinned allocation"); tc_destroy(h); return r; }
+    std::memset(h->st_host, 0, sizeof(StepState));
+
+    launch_pressure_factors(h->stream, d, h->c, pl, pd);
+    ce = cudaStreamSynchronize(h->stream);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pressure factors"); tc_destroy(h); return r; }
+    *out = h;
+    return 0;
+}
+
+void tc_destroy(tc_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    else cudaDeviceSynchronize();
+    for (void* p : h->allocs) cudaFree(p);
+    for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
+    if (h->st_host) cudaFreeHost(h->st_host);
+    delete h;
+}
+
+int tc_set_stream(tc_handle* h, void* s) {
+    if (int r = check(h)) return r;
+    h->stream = (cudaStream_t)s;
+    return 0;
+}
+
+// ---- state transfer --------------------------------------------------------
+
+static int upload(tc_handle* h, const double* src, double* dst, int nk, int halo) {
+    const Dims& d = h->d;
+    size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
+    CK(cudaMemcpyAsync(h->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, h->stream), "H2D copy");
+    L(h, K_LAYOUT, 1, [&] { launch_to_device(h->stream, d, h->stage, dst, nk, halo); });
+    return 0;
+}
+
+static int download(tc_handle* h, const double* src, double* dst, int nk, int halo) {
+    const Dims& d = h->d;
+    size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
+    L(h, K_LAYOUT, 1, [&] { launch_to_host(h->stream, d, src, h->stage, nk, halo); });
+    CK(cudaMemcpyAsync(dst, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H copy");
+    CK(cudaStreamSynchronize(h->stream), "D2H sync");
+    return 0;
+}
+
+int tc_set_state(tc_handle* h, const double* qt, const double* qr, const double* qz, const double* pr) {
+    if (int r = check(h)) return r;
+    if (!qt || !qr || !qz) return fail(h, 2000, "null field");
+    const Dims& d = h->d;
+    const size_t cells = (size_t)d.P * d.nr, faces = (size_t)d.P * (d.nr + 1);
+    if (int r = upload(h, qt, h->f.qt, d.nr, 1)) return r;
+    if (int r = upload(h, qr, h->f.qr, d.nr + 1, 1)) return r;
+    if (int r = upload(h, qz, h->f.qz, d.nr, 1)) return r;
+    if (pr) { if (int r = upload(h, pr, h->f.pr, d.nr, 1)) return r; }
+    else CK(cudaMemsetAsync(h->f.pr, 0, cells * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(h->f.qr, 0, (size_t)d.P * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(h->f.qr + (size_t)d.nr * d.P, 0, (size_t)d.P * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(h->f.ru1, 0, cells * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(h->f.ru2, 0, faces * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(h->f.ru3, 0, cells * sizeof(double), h->stream), "memset");
+    CK(cudaStreamSynchronize(h->stream), "set_state sync");
+    return 0;
+}
+
+int tc_get_state(tc_handle* h, double* qt, double* qr, double* qz, double* pr) {
+    if (int r = check(h)) return r;
+    const Dims& d = h->d;
+    if (qt) if (int r = download(h, h->f.qt, qt, d.nr, 1)) return r;
+    if (qr) if (int r = download(h, h->f.qr, qr, d.nr + 1, 1)) return r;
+    if (qz) if (int r = download(h, h->f.qz, qz, d.nr, 1)) return r;
+    if (pr) if (int r = download(h, h->f.pr, pr, d.nr, 1)) return r;
+    return 0;
+}
+
+static int field_ptr(tc_handle* h, int which, double** p, int* nk, int* halo) {
+    const Dims& d = h->d;
+    Fields& f = h->f;
+    *halo = which <= TC_F_DPH ? 1 : 0;
+    switch (which) {
+        case TC_F_QT: *p = f.qt; *nk = d.nr; break;
+        case TC_F_QR: *p = f.qr; *nk = d.nr + 1; break;
+        case TC_F_QZ: *p = f.qz; *nk = d.nr; break;
+        case TC_F_PR: *p = f.pr; *nk = d.nr; break;
+        case TC_F_DPH: *p = f.phi; *nk = d.nr; break;
+        case TC_F_RHS_T: *p = f.rhs_t; *nk = d.nr; break;
+        case TC_F_RHS_R: *p = f.rhs_r; *nk = d.nr + 1; break;
+        case TC_F_RHS_Z: *p = f.rhs_z; *nk = d.nr; break;
+        case TC_F_RU1: *p = f.ru1; *nk = d.nr; break;
+        case TC_F_RU2: *p = f.ru2; *nk = d.nr + 1; break;
+        case TC_F_RU3: *p = f.ru3; *nk = d.nr; break;
+        case TC_F_DQ: *p = f.h_t; *nk = d.nr; break;
+        case TC_F_HR: *p = f.h_r; *nk = d.nr + 1; break;
+        case TC_F_QCAP: *p = f.h_z; *nk = d.nr; break;
+        default: return fail(h, 2004, "unknown field id");
+    }
+    if (!*p) return fail(h, 2005, "field not allocated (call tc_explicit_terms first)");
+    return 0;
+}
+
+int tc_get_field(tc_handle* h, int which, double* out) {
+    if (int r = check(h)) return r;
+    double* p; int nk, halo;
+    if (int r = field_ptr(h, which, &p, &nk, &halo)) return r;
+    return download(h, p, out, nk, halo);
+}
+
+int tc_set_field(tc_handle* h, int which, const double* in) {
+    if (int r = check(h)) return r;
+    double* p; int nk, halo;
+    if (int r = field_ptr(h, which, &p, &nk, &halo)) return r;
+    if (int r = upload(h, in, p, nk, halo)) return r;
+    CK(cudaStreamSynchronize(h->stream), "set_field sync");
+    return 0;
+}
+
+// ---- the step ----------------------------------------------------------------
+
+static void enqueue_substeps(tc_handle* h) {
+    cudaStream_t s = h->stream;
+    for (int sub = 0; sub < h->k.nsst; ++sub) {
+        L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_FUSED, h->d, h->c, h->k, h->f, sub); });
+        L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, h->f, sub); });
+        L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, h->c, h->k, h->f, h->p, sub, false); });
+        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, false); });
+        L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, h->f); });
+        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, true); });
+        L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, h->f, h->p); });
+        L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, h->f, sub, true, true); });
+    }
+}
+
+static void enqueue_begin(tc_handle* h, int mode, double dt, double time) {
+    L(h, K_CONTROL, 1, [&] { launch_begin_step(h->stream, h->k, h->f.st, mode, dt, time); });
+    if (h->k.patterned) L(h, K_CONTROL, 1, [&] { launch_slip(h->stream, h->d, h->k, h->f); });
+    L(h, K_CONTROL, 1, [&] { launch_factors(h->stream, h->d, h->c, h->k, h->f); });
+}
+
+int tc_time_marcher(tc_handle* h, double dt, double time) {
+    if (int r = check(h)) return r;
+    enqueue_begin(h, 0, dt, time);
+    enqueue_substeps(h);
+    CK(cudaGetLastError(), "tc_time_marcher launch");
+    return 0;
+}
+
+int tc_kernels_per_step(const tc_handle* h) {
+    if (!h) return 0;
+    return 2 + (h->k.patterned ? 1 : 0) + 8 * h->k.nsst;
+}
+
+long long tc_device_bytes(const tc_handle* h) { return h ? h->bytes : 0; }
+
+namespace {
+__global__ void set_clock_kernel(StepState* st, int ntime, double time) {
+    st->ntime = ntime;
+    st->time = time;
+    st->halt = 0;
+    st->errorcode = 0;
+}
+}  // namespace
+
+static int read_state(tc_handle* h) {
+    CK(cudaMemcpyAsync(h->st_host, h->f.st, sizeof(StepState), cudaMemcpyDeviceToHost, h->stream), "state read");
+    CK(cudaStreamSynchronize(h->stream), "state sync");
+    return 0;
+}
+
+int tc_run(tc_handle* h, int nsteps, int* ntime, double* time, double* dt) {
+    if (int r = check(h)) return r;
+    if (!ntime || !time || !dt) return fail(h, 2000, "null argument");
+    cudaStream_t s = h->stream;
+    const int nt0 = *ntime;
+    const double t0 = *time;
+    L(h, K_CONTROL, 1, [&] { set_clock_kernel<<<1, 1, 0, s>>>(h->f.st, nt0, t0); });
+    for (int n = 0; n < nsteps; ++n) {
+        L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, h->f); });
+        enqueue_begin(h, 1, 0.0, 0.0);
+        enqueue_substeps(h);
+        L(h, K_CONTROL, 1, [&] { launch_end_step(s, h->k, h->f.st); });
+        L(h, K_REDUCE, 4, [&] {
+            launch_velocity_stats(s, h->d, h->c, h->k, h->f, true);
+            launch_check_divergence(s, h->d, h->c, h->k, h->f, true);
+        });
+        L(h, K_CONTROL, 1, [&] { launch_finish_step(s, h->k, h->f.st); });
+    }
+    CK(cudaGetLastError(), "tc_run launch");
+    if (int r = read_state(h)) return r;
+    *ntime = h->st_host->ntime;
+    *time = h->st_host->time;
+    *dt = h->st_host->dt;
+    return h->st_host->halt ? h->st_host->errorcode : 0;
+}
+
+// ---- per-routine entry points ---------------------------------------------
+
+int tc_begin_step(tc_handle* h, double dt, double time) {
+    if (int r = check(h)) return r;
+    enqueue_begin(h, 0, dt, time);
+    h->sub = 0;
+    return 0;
+}
+
+int tc_set_substep(tc_handle* h, int ns) {
+    if (int r = check(h)) return r;
+    if (ns < 1 || ns > h->k.nsst) return fail(h, 2006, "substep out of range");
+    h->sub = ns - 1;
+    return 0;
+}
+
+static int ensure_h(tc_handle* h) {
+    const Dims& d = h->d;
+    cudaError_t ce = cudaSuccess;
+    if (!h->f.h_t) ce = dalloc(h, &h->f.h_t, (size_t)d.P * d.nr);
+    if (ce == cudaSuccess && !h->f.h_r) ce = dalloc(h, &h->f.h_r, (size_t)d.P * (d.nr + 1));
+    if (ce == cudaSuccess && !h->f.h_z) ce = dalloc(h, &h->f.h_z, (size_t)d.P * d.nr);
+    if (ce != cudaSuccess) return cuda_fail(h, ce, "explicit-term arrays");
+    return 0;
+}
+
+int tc_explicit_terms(tc_handle* h) {
+    if (int r = check(h)) return r;
+    if (int r = ensure_h(h)) return r;
+    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_EXPLICIT, h->d, h->c, h->k, h->f, h->sub); });
+    return 0;
+}
+
+int tc_implicit_and_update(tc_handle* h) {
+    if (int r = check(h)) return r;
+    if (int r = ensure_h(h)) return r;
+    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_IMPLICIT, h->d, h->c, h->k, h->f, h->sub); });
+    L(h, K_RADIAL, 1, [&] { launch_radial_solve(h->stream, h->d, h->f, h->sub); });
+    return 0;
+}
+
+int tc_explicit_and_rhs(tc_handle* h) {
+    if (int r = check(h)) return r;
+    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_FUSED, h->d, h->c, h->k, h->f, h->sub); });
+    return 0;
+}
+
+int tc_solve_imp_eqn_update(tc_handle* h) {
+    if (int r = check(h)) return r;
+    L(h, K_RADIAL, 1, [&] { launch_radial_solve(h->stream, h->d, h->f, h->sub); });
+    return 0;
+}
+
+int tc_calc_local_divergence(tc_handle* h) {
+    if (int r = check(h)) return r;
+    L(h, K_DIVFFT, 1, [&] { launch_divergence(h->stream, h->d, h->c, h->k, h->f, h->sub); });
+    return 0;
+}
+
+int tc_solve_pressure_correction(tc_handle* h) {
+    if (int r = check(h)) return r;
+    cudaStream_t s = h->stream;
+    L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, h->c, h->k, h->f, h->p, h->sub, true); });
+    L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, false); });
+    L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, h->f); });
+    L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, true); });
+    L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, h->f, h->p); });
+    return 0;
+}
+
+int tc_correct_velocity(tc_handle* h) {
+    if (int r = check(h)) return r;
+    L(h, K_CORRECT, 1, [&] { launch_correct(h->stream, h->d, h->c, h->k, h->f, h->sub, true, false); });
+    return 0;
+}
+
+int tc_correct_pressure(tc_handle* h) {
+    if (int r = check(h)) return r;
+    L(h, K_CORRECT, 1, [&] { launch_correct(h->stream, h->d, h->c, h->k, h->f, h->sub, false, true); });
+    return 0;
+}
+
+// ---- reductions ---------------------------------------------------------------
+
+int tc_calc_max_cfl(tc_handle* h, double* cflm) {
+    if (int r = check(h)) return r;
+    L(h, K_REDUCE, 2, [&] { launch_cfl(h->stream, h->d, h->c, h->k, h->f); });
+    if (int r = read_state(h)) return r;
+    if (cflm) *cflm = h->st_host->instcfl;
+    return 0;
+}
+
+int tc_check_divergence(tc_handle* h, double* qmax) {
+    if (int r = check(h)) return r;
+    L(h, K_REDUCE, 2, [&] { launch_check_divergence(h->stream, h->d, h->c, h->k, h->f, false); });
+    if (int r = read_state(h)) return r;
+    if (qmax) *qmax = h->st_host->dmax;
+    return 0;
+}
+
+int tc_calc_torque(tc_handle* h, double* inner, double* outer) {
+    if (int r = check(h)) return r;
+    L(h, K_REDUCE, 2, [&] { launch_torque(h->stream, h->d, h->c, h->k, h->f); });
+    if (int r = read_state(h)) return r;
+    if (inner) *inner = h->st_host->torque[0];
+    if (outer) *outer = h->st_host->torque[1];
+    return 0;
+}
+
+int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3) {
+    if (int r = check(h)) return r;
+    L(h, K_REDUCE, 2, [&] { launch_velocity_stats(h->stream, h->d, h->c, h->k, h->f, false); });
+    if (int r = read_state(h)) return r;
+    for (int q = 0; q < 3; ++q) {
+        if (vmax3) vmax3[q] = h->st_host->vmax[q];
+        if (rms3) rms3[q] = h->st_host->rms[q];
+    }
+    return 0;
+}
+
+// ---- measurement helpers ---------------------------------------------------
+
+long long tc_launch_count(const tc_handle* h) { return h ? h->launches : 0; }
+
+int tc_kernels_per_run_step(const tc_handle* h) {
+    if (!h) return 0;
+    return tc_kernels_per_step(h) + 2 + 1 + 4 + 1;
+}
+
+int tc_profile(tc_handle* h, int enable) {
+    if (int r = check(h)) return r;
+    CK(cudaStreamSynchronize(h->stream), "profile sync");
+    h->profiling = enable != 0;
+    h->recs.clear();
+    h->pool_used = 0;
+    for (int c = 0; c < 16; ++c) { h->prof_ms[c] = 0.0; h->prof_n[c] = 0; }
+    return 0;
+}
+
+int tc_profile_read(tc_handle* h, double* ms, long long* launches, int cap) {
+    if (int r = check(h)) return r;
+    CK(cudaStreamSynchronize(h->stream), "profile sync");
+    for (const auto& r : h->recs) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, r.a, r.b), "event time");
+        h->prof_ms[r.cls] += t;
+    }
+    h->recs.clear();
+    h->pool_used = 0;
+    for (int c = 0; c < K_COUNT && c < cap; ++c) {
+        if (ms) ms[c] = h->prof_ms[c];
+        if (launches) launches[c] = h->prof_n[c];
+    }
+    return K_COUNT;
+}
+
+int tc_measure_fp64_peak(tc_handle* h, double* tflops) {
+    if (int r = check(h)) return r;
+    double v = measure_fp64_peak(h->stream);
+    if (v < 0) return fail(h, 1002, "probe allocation failed");
+    if (tflops) *tflops = v;
+    return 0;
+}
+
+const char* tc_profile_name(int cls) { return (cls >= 0 && cls < K_COUNT) ? kClassNames[cls] : ""; }
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// tc_dev.h -- device-side data structures shared by the kernels and the C ABI.
+//
+// Device layout of every 3-D field: [k][j][i] with i = theta fastest
+// (contiguous), then j = z, then k = r; no halo cells (periodic neighbours are
+// found by index wrap).  k is the reference radial index minus one:
+//   qt, qz, pr, phi, ru1, ru3, rhs_t, rhs_z : k = 0 .. nrm-1   (cells)
+//   qr, ru2, rhs_r                          : k = 0 .. nrm     (faces; 0 and
+//                                             nrm are the walls, always 0)
+// The pressure spectrum is complex [k][kz][kt] with kt = 0..nthm/2 (the
+// half-spectrum of the real transform along theta) and kz = 0..nzm-1.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+namespace tcgb {
+
+constexpr int kMaxStages = 24;
+
+// Radix plan of one complex transform length (radices 2, 3, 4, 5).
+struct FFTPlan {
+    int n = 0;
+    int nstages = 0;
+    int radix[kMaxStages] = {0};
+    const double2* tw = nullptr;   // exp(-2 pi i j / n), j = 0..n-1
+};
+
+struct Dims {
+    int nt, nz, nr;        // nthm, nzm, nrm
+    int M, PH;             // nthm/2, nthm/2 + 1
+    int nzh;               // nzm/2 + 1
+    long long P;           // nz * nt (one r-plane of a real field)
+    long long PS;          // nz * PH (one r-plane of the spectrum)
+};
+
+// 1-D coefficient arrays on the device, 0-based (entry m = reference m+1).
+struct Coef {
+    const double *usrm, *usrc, *udx2rm, *udx1vis1, *udxt_m, *udxtq_m;
+    const double *rc, *udx2c, *udx1vis2, *udxt_c, *udxtq_c;
+    const double *ap1j, *ac1j, *am1j, *ap2je, *ac2je, *am2je, *ap3j, *ac3j, *am3j;
+    const double *ap2j, *ac2j, *am2j;
+    const double *udx2m, *rudx2c, *udx1qm, *apph, *acph, *amph, *usrm2;
+    const double *ak1, *ak3;
+};
+
+// Scalars of the configuration (param.F90).
+struct Consts {
+    double dxt, dxz, dxtq, dxzq, ren, romeg, virotint, virotext;
+    double ap1j_fs0, ac1j_fs0, am1j_fs0, ap1j_fs1, ac1j_fs1;
+    double ap3j_fs0, ac3j_fs0, am3j_fs0, ap3j_fs1, ac3j_fs1;
+    double sizepert, omegapert, pi, rint, rext, lamb;
+    double dtmin, dtmax, limitCFL, tout, tmax, limitVel, resid;
+    double gam[3], rom[3], alm[3];
+    int nsst, idtv, ntst;
+    int patterned;          // patterned slip active (SlipBCs.F90:520)
+    int minstrt, minstrz, multmin;
+};
+
+// Per-step state kept on the device (main.F90 / TimeMarcher.F90 scalars).
+struct StepState {
+    double time;        // start-of-step time
+    double dt;
+    double beta;        // dt / ren / 2
+    double vinner_t, dvinner_t;
+    double instcfl;     // last CalcMaxCFL result
+    double dmax;        // last CheckDivergence result
+    double vmax[3], rms[3];
+    double torque[2];
+    int ntime;          // step counter of main.F90
+    int errorcode;      // code raised by the last step
+    int halt;           // a step raised an error: later steps do nothing
+    int output;         // the last step was an output step
+};
+
+// Factors of the row-scaled momentum matrices of one step: for each substep
+// s (3), component c (0 = qt, 1 = qr, 2 = qz) and slip variant v (0 = no
+// slip at the inner wall, 1 = free slip), arrays of length nr+1:
+//   l    : multipliers of the LU factorisation (row k eliminates row k-1)
+//   dinv : 1 / pivot
+//   u    : super-diagonal
+// plus per (s, c) the right-hand-side scale 1/(1 - ac(k) beta al) and, per s,
+// the inner-wall forcing term of qt (SolveImpEqnUpdate_QT.F90:65-67).
+struct MomFactors {
+    double* base;
+    int stride;          // nr + 1
+    __host__ __device__ double* l(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 0) * (size_t)stride; }
+    __host__ __device__ double* dinv(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 1) * (size_t)stride; }
+    __host__ __device__ double* u(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 2) * (size_t)stride; }
+    __host__ __device__ double* scale(int s, int c) const { return base + ((((s * 3 + c) * 2 + 0) * 4) + 3) * (size_t)stride; }
+    __host__ __device__ double* extra(int s) const { return base + (size_t)(3 * 3 * 2 * 4) * stride + s; }
+    static size_t doubles(int stride) { return (size_t)(3 * 3 * 2 * 4) * stride + 8; }
+};
+
+}  // namespace tcgb

@@ -1,0 +1,1142 @@
+// tc_kernels.cu -- FP64 kernels of the Taylor-Couette time step for sm_103a.
+//
+// One substep (TimeMarcher.F90:27-54) is six kernels:
+//   momentum_kernel      ExplicitTermsQT/QR/QZ fused with the right-hand sides
+//                        and ru updates of ImplicitAndUpdateQT/QR/QZ
+//   radial_solve_kernel  SolveImpEqnUpdate_QT/QR/QZ: LU solves along r, q += dq
+//   div_fft_kernel       CalcLocalDivergence fused with the real FFT along theta
+//   zfft_kernel          complex FFT along z (forward)
+//   ptri_kernel          radial tridiagonal solve per (k_theta, k_z) mode
+//   zfft_kernel          complex FFT along z (inverse)
+//   theta_inv_kernel     inverse real FFT along theta -> phi
+//   correct_kernel       CorrectVelocity fused with CorrectPressure
+// The decomp_2d transposes of the reference disappear: every transform works
+// on the [k][j][i] layout in place (theta contiguous, z strided).  Halo
+// exchanges (update_halo) become periodic index wrap.
+
+#include <cstdio>
+
+#include "tc_fft.cuh"
+#include "tc_kernels.cuh"
+
+namespace tcgb {
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 304;   // 2 x 152 SMs
+constexpr int kZC = 4;            // lines per z-FFT block
+
+__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
+__device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
+
+// --------------------------------------------------------------------------
+// Step control
+// --------------------------------------------------------------------------
+
+// mode 0: dt and time given by the host (tc_time_marcher / tc_begin_step).
+// mode 1: main.F90:156-174 -- dt from the CFL number of the current field.
+__global__ void begin_step_kernel(Consts k, StepState* st, int mode, double dt_h, double time_h) {
+    if (threadIdx.x != 0) return;
+    double dt, time;
+    if (mode == 0) {
+        dt = dt_h;
+        time = time_h;
+        st->halt = 0;
+        st->errorcode = 0;
+    } else {
+        if (st->halt) return;
+        int err = 0;
+        double cfl = st->instcfl;
+        time = st->time;
+        if (k.idtv == 1) {
+            if (st->ntime > 1) {
+                dt = (cfl < 1.0e-8) ? k.dtmax : k.limitCFL / cfl;
+                if (dt > k.dtmax) dt = k.dtmax;
+            } else {
+                dt = k.dtmin;
+            }
+            if (dt < k.dtmin) err = 166;
+        } else {
+            // IDTV=0: the reference never assigns dt; run with dt = DTMAX.
+            dt = k.dtmax;
+            if (cfl * dt > k.limitCFL) err = 165;
+        }
+        st->errorcode = err;
+    }
+    st->dt = dt;
+    st->time = time;
+    st->beta = dt / k.ren * 0.5;                                   // TimeMarcher.F90:20
+    st->vinner_t = k.sizepert * sin(2.0 * k.pi * k.omegapert * time);          // InnerCylVelocity.F90:15
+    st->dvinner_t = 2.0 * k.pi * k.omegapert * k.sizepert * cos(2.0 * k.pi * k.omegapert * time) * dt;
+}
+
+// time = time + dt and the output-step test of main.F90:178-180.
+__global__ void end_step_kernel(Consts k, StepState* st) {
+    if (threadIdx.x != 0 || st->halt) return;
+    double t = st->time + st->dt;
+    st->time = t;
+    st->output = (st->ntime == 1 || fmod(t, k.tout) < st->dt) ? 1 : 0;
+}
+
+// Error codes raised after TimeMarcher (main.F90:182-226); the last assignment
+// wins, as in the reference.
+__global__ void finish_step_kernel(Consts k, StepState* st) {
+    if (threadIdx.x != 0 || st->halt) return;
+    int err = st->errorcode;
+    if (st->output) {
+        if (st->vmax[0] > k.limitVel && st->vmax[1] > k.limitVel) err = 266;
+        if (fabs(st->dmax) > k.resid) err = 169;
+    }
+    if (st->time > k.tmax) err = 333;
+    if (st->ntime == k.ntst) err = 555;
+    st->errorcode = err;
+    st->ntime += 1;
+    if (err != 0) st->halt = 1;
+}
+
+// SlipBCs.F90:495-555 for the rotated slip pattern (only launched when
+// MINSTRT*MULTMIN and MINSTRZ*MULTMIN are both non-zero).  One thread per
+// (z, theta) column decides whether any band covers it.
+__global__ void slip_kernel(Dims d, Consts k, StepState* st, signed char* icyl) {
+    int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= d.P || st->halt) return;
+    const int nthm = d.nt, nzm = d.nz;
+    int jz = col / nthm + 1;         // z index k of the reference loop (1-based)
+    int truej = col % nthm + 1;      // theta index (1-based)
+    int ntott = k.minstrt * k.multmin, ntotz = k.minstrz * k.multmin;
+    double perdist = __dmul_rn(2.0, k.pi) / k.lamb;
+    double wint = k.virotint / k.rint;
+    double anglemoved = fmod(__dmul_rn(wint, st->time), perdist);
+    int pm = (int)floor(__dmul_rn(anglemoved, k.dxt));
+    // thdispl(j) = mod(j + pm, nthm), 0 -> nthm: invert the rotation
+    int j = ((truej - 1 - pm) % nthm + nthm) % nthm + 1;
+    double m1 = __ddiv_rn(__dmul_rn(__ddiv_rn((double)k.minstrt, (double)k.minstrz), (double)nzm), (double)nthm);
+    double y1 = __ddiv_rn((double)nzm, (double)ntotz);
+    int on = 0;
+    for (int i = -ntott; i <= ntotz && !on; ++i) {
+        double a = __dsub_rn(__dsub_rn((double)jz, __dmul_rn(__dmul_rn(1.0, m1), (double)j)), __dmul_rn((double)i, y1));
+        if (a > 0.00001 && __dsub_rn(a, y1 / 2.0) < 0.00001) on = 1;
+    }
+    icyl[col] = (signed char)on;
+}
+
+// Row-scaled momentum matrices of SolveImpEqnUpdate_QT/QR/QZ and their LU
+// factors for every substep of the step (dgttrf without row interchanges:
+// the matrices are diagonally dominant), plus the per-substep correction
+// coefficients of CorrectVelocity.  One block.
+__global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFactors F, double* corr) {
+    if (st->halt) return;
+    const int nr = d.nr;
+    const double beta = st->beta, dt = st->dt;
+    const int nsub = k.nsst;
+    // phase 1: row entries (parallel over rows)
+    for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
+        int row = t % nr, chain = t / nr;        // chain: 0,1 = qt v0/v1; 2 = qr; 3,4 = qz v0/v1
+        int s = chain / 5, ch = chain % 5;
+        double betadx = beta * k.alm[s];
+        if (ch == 0 || ch == 1 || ch == 3 || ch == 4) {
+            bool qt = ch < 2;
+            int v = (ch == 1 || ch == 4) ? 1 : 0;
+            double fic = v == 0 ? 1.0 : 0.0, foc = 1.0;
+            const double* ac = qt ? c.ac1j : c.ac3j;
+            const double* am = qt ? c.am1j : c.am3j;
+            const double* ap = qt ? c.ap1j : c.ap3j;
+            double acfs0 = qt ? k.ac1j_fs0 : k.ac3j_fs0, acfs1 = qt ? k.ac1j_fs1 : k.ac3j_fs1;
+            double acr = ac[row];
+            if (row == 0) acr = ac[0] * fic + acfs0 * (1.0 - fic);
+            else if (row == nr - 1) acr = ac[nr - 1] * foc + acfs1 * (1.0 - foc);
+            double ackl_b = 1.0 / (1.0 - acr * betadx);
+            int cidx = qt ? 0 : 2;
+            F.l(s, cidx, v)[row] = row > 0 ? -am[row] * betadx * ackl_b : 0.0;        // amkl
+            F.u(s, cidx, v)[row] = row < nr - 1 ? -ap[row] * betadx * ackl_b : 0.0;   // apkl
+            if (v == 0) F.scale(s, cidx)[row] = 1.0 / (1.0 - ac[row] * betadx);
+        } else {
+            // qr faces 1..nr-1; rows 0 and nr are identity rows
+            double ackl_b = (row >= 1) ? 1.0 / (1.0 - c.ac2j[row] * betadx) : 1.0;
+            F.l(s, 1, 0)[row] = row >= 1 ? -c.am2j[row] * betadx * ackl_b : 0.0;
+            F.u(s, 1, 0)[row] = row >= 1 ? -c.ap2j[row] * betadx * ackl_b : 0.0;
+            F.scale(s, 1)[row] = ackl_b;
+        }
+        // CorrectVelocity.F90:325-330 coefficients
+        if (ch == 0) {
+            corr[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
+            corr[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
+            if (row == 0) corr[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
+        }
+    }
+    __syncthreads();
+    // phase 2: sequential elimination, one thread per chain
+    if (threadIdx.x < nsub * 5) {
+        int s = threadIdx.x / 5, ch = threadIdx.x % 5;
+        int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
+        int v = (ch == 1 || ch == 4) ? 1 : 0;
+        double* l = F.l(s, cidx, v);
+        double* u = F.u(s, cidx, v);
+        double* di = F.dinv(s, cidx, v);
+        int k0 = (cidx == 1) ? 1 : 0;
+        double dp = 1.0;
+        di[k0] = 1.0;
+        if (cidx == 1) l[1] = 0.0;   // couples to the wall value qr(1) = 0
+        for (int row = k0 + 1; row < nr; ++row) {
+            double fact = l[row] / dp;
+            l[row] = fact;
+            dp = 1.0 - fact * u[row - 1];
+            di[row] = dp;
+        }
+    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + nsub) {
+        int s = threadIdx.x - 32;
+        // SolveImpEqnUpdate_QT.F90:67
+        *F.extra(s) = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
+    }
+    __syncthreads();
+    // phase 3: reciprocals of the pivots
+    for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
+        int row = t % nr, chain = t / nr;
+        int s = chain / 5, ch = chain % 5;
+        int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
+        int v = (ch == 1 || ch == 4) ? 1 : 0;
+        if (cidx == 1 && row == 0) continue;
+        double* di = F.dinv(s, cidx, v);
+        di[row] = 1.0 / di[row];
+    }
+}
+
+// --------------------------------------------------------------------------
+// Momentum: explicit terms and implicit right-hand sides
+// --------------------------------------------------------------------------
+
+struct Stencil {
+    int i, j, k, im, ip, jm, jp;
+    size_t P, row;
+    int nt;
+    __device__ size_t at(int kk, int jj, int ii) const { return (size_t)kk * P + (size_t)jj * nt + ii; }
+};
+
+// ExplicitTermsQT.F90:40-125 at cell (i, j, k)
+__device__ double explicit_qt(const Stencil& S, int nr, const Coef& c, const Consts& K,
+                              const double* qt, const double* qr, const double* qz) {
+    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
+    double t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip)), t_im = ld(qt + S.at(k, S.j, S.im));
+    double t_jp = ld(qt + S.at(k, S.jp, S.i)), t_jm = ld(qt + S.at(k, S.jm, S.i));
+    double t_kp = ld(qt + S.at(kpp, S.j, S.i)), t_km = ld(qt + S.at(kmm, S.j, S.i));
+    double r_c = ld(qr + S.at(k, S.j, S.i)), r_im = ld(qr + S.at(k, S.j, S.im));
+    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_pim = ld(qr + S.at(kp, S.j, S.im));
+    double z_c = ld(qz + S.at(k, S.j, S.i)), z_im = ld(qz + S.at(k, S.j, S.im));
+    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
+    const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const double usrm = ld(c.usrm + k), usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
+    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    double h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
+    double h12d = ((r_p + r_pim) * (t_kp + t_c) - (r_c + r_im) * (t_c + t_km)) * 0.25 * ld(c.udx2rm + k);
+    double h12n = t_c * usrm * ((r_p + r_pim) * usrcp + (r_c + r_im) * usrc) * 0.25;
+    double h13 = ((z_jp + z_jpim) * (t_jp + t_c) - (z_c + z_im) * (t_c + t_jm)) * udxz;
+    double d11qt = (t_ip - 2.0 * t_c + t_im) * udxtq;
+    double d22qt = (t_jp - 2.0 * t_c + t_jm) * udxzq;
+    double qre = r_p * usrcp + r_c * usrc;
+    double qrw = r_pim * usrcp + r_im * usrc;
+    double d11qre = (qre - qrw) * ld(c.udx1vis1 + k) * 0.5;
+    double coriol = -((r_c + r_im) * usrc + (r_p + r_pim) * usrcp) * 0.25 * K.romeg;
+    return -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
+}
+
+// ExplicitTermsQR.F90:180-280 at face (i, j, k), 1 <= k <= nr-1
+__device__ double explicit_qr(const Stencil& S, const Coef& c, const Consts& K,
+                              const double* qt, const double* qr, const double* qz) {
+    const int k = S.k, km = k - 1, kp = k + 1;
+    double t_c = ld(qt + S.at(k, S.j, S.i)), t_m = ld(qt + S.at(km, S.j, S.i));
+    double t_ip = ld(qt + S.at(k, S.j, S.ip)), t_mip = ld(qt + S.at(km, S.j, S.ip));
+    double r_c = ld(qr + S.at(k, S.j, S.i)), r_ip = ld(qr + S.at(k, S.j, S.ip)), r_im = ld(qr + S.at(k, S.j, S.im));
+    double r_jp = ld(qr + S.at(k, S.jp, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_m = ld(qr + S.at(km, S.j, S.i));
+    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_mjp = ld(qz + S.at(km, S.jp, S.i));
+    double z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
+    const double udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
+    const double usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
+    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    double a = (t_ip + t_mip + t_c + t_m) * 0.25;
+    double h11n = a * a;
+    double h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
+    double h22 = ((r_p * usrcp + r_c * usrc) * (r_p + r_c) - (r_c * usrc + r_m * usrcm) * (r_c + r_m)) * ld(c.udx2c + k) * 0.25;
+    double h23 = ((z_jp + z_mjp) * (r_jp + r_c) - (z_c + z_m) * (r_c + r_jm)) * udxz;
+    double d11qre = -((t_ip + t_mip) - (t_c + t_m)) * ld(c.udx1vis2 + k);
+    double d11qr = (r_ip - 2.0 * r_c + r_im) * udxtq;
+    double d22qr = (r_jp - 2.0 * r_c + r_jm) * udxzq;
+    double coriol = (t_c + t_ip + t_m + t_mip) * 0.25 * ld(c.rc + k) * K.romeg;
+    return -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
+}
+
+// ExplicitTermsQZ.F90:328-390 at cell (i, j, k)
+__device__ double explicit_qz(const Stencil& S, int nr, const Coef& c, const Consts& K,
+                              const double* qt, const double* qr, const double* qz) {
+    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
+    double t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip));
+    double t_jm = ld(qt + S.at(k, S.jm, S.i)), t_jmip = ld(qt + S.at(k, S.jm, S.ip));
+    double z_c = ld(qz + S.at(k, S.j, S.i)), z_ip = ld(qz + S.at(k, S.j, S.ip)), z_im = ld(qz + S.at(k, S.j, S.im));
+    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jm = ld(qz + S.at(k, S.jm, S.i));
+    double z_kp = ld(qz + S.at(kpp, S.j, S.i)), z_km = ld(qz + S.at(kmm, S.j, S.i));
+    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
+    double r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    double h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
+    double h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.udx2rm + k) * 0.25;
+    double h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * udxz;
+    double dqz1 = (z_im - 2.0 * z_c + z_ip) * udxtq;
+    double dqz2 = (z_jm - 2.0 * z_c + z_jp) * udxzq;
+    return -(h31 + h32 + h33) + dqz1 + dqz2;
+}
+
+struct MomArgs {
+    const double *qt, *qr, *qz, *pr;
+    double *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
+    const signed char* icyl;
+    const StepState* st;
+    double al, ga, ro;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K, MomArgs a) {
+    if (a.st->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= d.nt || j >= d.nz) return;
+    const int nr = d.nr;
+    Stencil S;
+    S.i = i; S.j = j; S.k = k; S.nt = d.nt; S.P = (size_t)d.P;
+    S.im = wm(i, d.nt); S.ip = wp(i, d.nt); S.jm = wm(j, d.nz); S.jp = wp(j, d.nz);
+    const size_t o = S.at(k, j, i);
+    double ht = 0.0, hr = 0.0, hz = 0.0;
+    if (MODE != MODE_IMPLICIT) {
+        ht = explicit_qt(S, nr, c, K, a.qt, a.qr, a.qz);
+        if (k >= 1) hr = explicit_qr(S, c, K, a.qt, a.qr, a.qz);
+        hz = explicit_qz(S, nr, c, K, a.qt, a.qr, a.qz);
+        if (MODE == MODE_EXPLICIT) {
+            a.h_t[o] = ht;
+            if (k >= 1) a.h_r[o] = hr;
+            a.h_z[o] = hz;
+            return;
+        }
+    } else {
+        ht = a.h_t[o];
+        if (k >= 1) hr = a.h_r[o];
+        hz = a.h_z[o];
+    }
+    const double dt = a.st->dt, al = a.al, ga = a.ga, ro = a.ro, alre = al / K.ren;
+    const double fic = a.icyl ? (double)a.icyl[(size_t)j * d.nt + i] : 1.0, foc = 1.0;
+    const double* qt = a.qt;
+    const double* qr = a.qr;
+    const double* qz = a.qz;
+    const double* pr = a.pr;
+    const double p_c = ld(pr + o);
+    // ---- qt (ImplicitAndUpdateQT.F90:45-115)
+    {
+        double d33;
+        if (k == 0) {
+            double app = ld(c.ap1j);
+            double acc = ld(c.ac1j) * fic + K.ac1j_fs0 * (1.0 - fic);
+            double amm = ld(c.am1j) * fic + K.am1j_fs0 * (1.0 - fic);
+            d33 = ld(qt + S.at(1, j, i)) * app + ld(qt + o) * acc + (K.virotint + a.st->vinner_t) * amm;
+        } else if (k == nr - 1) {
+            double amm = ld(c.am1j + k);
+            double app = ld(c.ap1j + k) * foc + K.ap1j_fs1 * (1.0 - foc);
+            double acc = ld(c.ac1j + k) * foc + K.ac1j_fs1 * (1.0 - foc);
+            d33 = K.virotext * app + ld(qt + o) * acc + ld(qt + S.at(k - 1, j, i)) * amm;
+        } else {
+            d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
+                  ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
+        }
+        double dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * K.dxt * al * ld(c.usrm + k);
+        double old = ro != 0.0 ? a.ru1[o] : 0.0;
+        a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
+        a.ru1[o] = ht;
+    }
+    // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
+    if (k >= 1) {
+        double d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
+                     ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
+        double udx2 = ld(c.rc + k) * al * ld(c.udx2c + k);
+        double dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
+        double old = ro != 0.0 ? a.ru2[o] : 0.0;
+        a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
+        a.ru2[o] = hr;
+    }
+    // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
+    {
+        double d33;
+        if (k == 0) {
+            double app = ld(c.ap3j);
+            double acc = ld(c.ac3j) * fic + K.ac3j_fs0 * (1.0 - fic);
+            double amm = ld(c.am3j) * fic + K.am3j_fs0 * (1.0 - fic);
+            double q0 = ld(qz + o);
+            d33 = ld(qz + S.at(1, j, i)) * app + q0 * acc + q0 * amm;
+        } else if (k == nr - 1) {
+            double app = ld(c.ap3j + k) * foc + K.ap3j_fs1 * (1.0 - foc);
+            double acc = ld(c.ac3j + k) * foc + K.ac3j_fs1 * (1.0 - foc);
+            double q0 = ld(qz + o);
+            d33 = q0 * app + q0 * acc + ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+        } else {
+            d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
+                  ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+        }
+        double dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * (K.dxz * al);
+        // At the outer wall the reference has already replaced ru3(nrm) by
+        // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
+        double old = (k == nr - 1) ? hz : (ro != 0.0 ? a.ru3[o] : 0.0);
+        a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
+        a.ru3[o] = hz;
+    }
+}
+
+// --------------------------------------------------------------------------
+// Radial implicit solves, one thread per (z, theta) column
+// --------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, Fields f, int sub) {
+    if (f.st->halt) return;
+    const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= d.P) return;
+    const int nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
+    const MomFactors& F = f.F;
+    // qt: SolveImpEqnUpdate_QT.F90:65-78
+    {
+        const double *l = F.l(sub, 0, v), *di = F.dinv(sub, 0, v), *u = F.u(sub, 0, v), *sc = F.scale(sub, 0);
+        double* rhs = f.rhs_t + col;
+        double* q = f.qt + col;
+        double y = (rhs[0] + *F.extra(sub)) * ld(sc);
+        rhs[0] = y;
+        for (int k = 1; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        double x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 0; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+    // qr: SolveImpEqnUpdate_QR.F90:136-150, faces 1..nr-1
+    {
+        const double *l = F.l(sub, 1, 0), *di = F.dinv(sub, 1, 0), *u = F.u(sub, 1, 0), *sc = F.scale(sub, 1);
+        double* rhs = f.rhs_r + col;
+        double* q = f.qr + col;
+        double y = rhs[P] * ld(sc + 1);
+        rhs[P] = y;
+        for (int k = 2; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        double x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 1; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+    // qz: SolveImpEqnUpdate_QZ.F90:214-224
+    {
+        const double *l = F.l(sub, 2, v), *di = F.dinv(sub, 2, v), *u = F.u(sub, 2, v), *sc = F.scale(sub, 2);
+        double* rhs = f.rhs_z + col;
+        double* q = f.qz + col;
+        double y = rhs[0] * ld(sc);
+        rhs[0] = y;
+        for (int k = 1; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        double x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 0; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Pressure: divergence + real FFT along theta (forward), per block R rows
+// (row = k*nzm + j) of nthm reals packed as nthm/2 complex values.
+// --------------------------------------------------------------------------
+
+// CalcLocalDivergence.F90:27-40 for cells 2m and 2m+1 of row (k, j).
+__device__ __forceinline__ double2 div_pair(const Dims& d, const Coef& c, const Consts& K,
+                                            const double* qt, const double* qr, const double* qz,
+                                            int k, int j, int m) {
+    const size_t P = (size_t)d.P;
+    const int nt = d.nt;
+    const size_t row = (size_t)k * P + (size_t)j * nt;
+    const int i0 = 2 * m, i2 = (2 * m + 2 == nt) ? 0 : 2 * m + 2;
+    double2 t01 = __ldg(reinterpret_cast<const double2*>(qt + row + i0));
+    double t2 = ld(qt + row + i2);
+    double2 r0 = __ldg(reinterpret_cast<const double2*>(qr + row + i0));
+    double2 r1 = __ldg(reinterpret_cast<const double2*>(qr + row + P + i0));
+    const int jp = wp(j, d.nz);
+    double2 z0 = __ldg(reinterpret_cast<const double2*>(qz + row + i0));
+    double2 z1 = __ldg(reinterpret_cast<const double2*>(qz + (size_t)k * P + (size_t)jp * nt + i0));
+    const double udx2m = ld(c.udx2m + k), usrm = ld(c.usrm + k);
+    double a = ((t01.y - t01.x) * K.dxt + (r1.x - r0.x) * udx2m) * usrm + (z1.x - z0.x) * K.dxz;
+    double b = ((t2 - t01.y) * K.dxt + (r1.y - r0.y) * udx2m) * usrm + (z1.y - z0.y) * K.dxz;
+    return make_double2(a, b);
+}
+
+// Forward transform of R rows.  FROM_PHI: the rows come from the phi array
+// (CalcLocalDivergence already ran); otherwise the divergence is computed on
+// the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
+template <bool FROM_PHI, int R>
+__global__ void __launch_bounds__(128) div_fft_kernel(Dims d, Coef c, Consts K, Fields f, FFTPlan pl,
+                                                      const double2* twr, double al) {
+    if (f.st->halt) return;
+    extern __shared__ double2 smem[];
+    const int M = pl.n;
+    double2* a = smem;
+    double2* b = smem + (size_t)R * M;
+    const long long nrows = (long long)d.nr * d.nz;
+    const long long row0 = (long long)blockIdx.x * R;
+    // the 1/2 of the real-transform unpacking is folded into the scale
+    const double norm = 0.5 / ((double)d.nt * (double)d.nz);
+    const double scl = FROM_PHI ? norm : (1.0 / (al * f.st->dt)) * norm;
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, m = t - r * M;
+        const long long row = row0 + r;
+        double2 z = make_double2(0.0, 0.0);
+        if (row < nrows) {
+            const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
+            if (FROM_PHI) z = __ldg(reinterpret_cast<const double2*>(f.phi + (size_t)row * d.nt + 2 * m));
+            else z = div_pair(d, c, K, f.qt, f.qr, f.qz, k, j, m);
+            z.x *= scl;
+            z.y *= scl;
+        }
+        a[m * R + r] = z;
+    }
+    __syncthreads();
+    const double2* Z = fft_lines<R>(a, b, pl, false);
+    // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
+    const int PH = M + 1;
+    for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
+        const int r = t / PH, kt = t - r * PH;
+        const long long row = row0 + r;
+        if (row >= nrows) continue;
+        const int k1 = kt == M ? 0 : kt, k2 = kt == 0 ? 0 : M - kt;
+        double2 zk = Z[k1 * R + r], zc = cconj(Z[k2 * R + r]);
+        double2 e = cadd(zk, zc), o = csub(zk, zc);
+        double2 w = __ldg(twr + kt);
+        double2 wo = cmul(w, o);
+        // - i * wo = (wo.y, -wo.x)
+        f.spec[(size_t)row * PH + kt] = make_double2(e.x + wo.y, e.y - wo.x);
+    }
+}
+
+// Complex FFT along z of kZC consecutive kt columns of one r-plane.
+__global__ void __launch_bounds__(128) zfft_kernel(Dims d, Fields f, FFTPlan pl, int inv) {
+    if (f.st->halt) return;
+    extern __shared__ double2 smem[];
+    const int nz = pl.n, PH = d.PH;
+    double2* a = smem;
+    double2* b = smem + (size_t)kZC * nz;
+    const int kt0 = blockIdx.x * kZC;
+    double2* plane = f.spec + (size_t)blockIdx.y * d.PS;
+    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
+        const int c = t % kZC, j = t / kZC;
+        a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const double2* Z = fft_lines<kZC>(a, b, pl, inv != 0);
+    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
+        const int c = t % kZC, j = t / kZC;
+        if (kt0 + c < PH) plane[(size_t)j * PH + kt0 + c] = Z[t];
+    }
+}
+
+// SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
+// matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
+// right-hand side, with the precomputed LU factors.  One thread per pair of
+// modes (kz, nzm-kz) that share a matrix.
+__global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, Fields f) {
+    if (f.st->halt) return;
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nzh * PH) return;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const bool two = (kz != 0) && (2 * kz != d.nz);
+    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
+    double2* x1 = f.spec + (size_t)kz * PH + kt;
+    double2* x2 = f.spec + (size_t)(two ? d.nz - kz : kz) * PH + kt;
+    const double* L = f.pf_l + t;
+    const double* DI = f.pf_dinv + t;
+    double2 y1 = x1[0], y2 = two ? x2[0] : make_double2(0.0, 0.0);
+    for (int k = 1; k < nr; ++k) {
+        const double l = ld(L + k * FS);
+        double2 b1 = x1[k * PS];
+        y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
+        x1[k * PS] = y1;
+        if (two) {
+            double2 b2 = x2[k * PS];
+            y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
+            x2[k * PS] = y2;
+        }
+    }
+    double di = ld(DI + (size_t)(nr - 1) * FS);
+    double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
+    x1[(size_t)(nr - 1) * PS] = s1;
+    if (two) x2[(size_t)(nr - 1) * PS] = s2;
+    for (int k = nr - 2; k >= 0; --k) {
+        const double u = ld(c.apph + k);
+        di = ld(DI + k * FS);
+        double2 b1 = x1[k * PS];
+        s1 = make_double2((b1.x - u * s1.x) * di, (b1.y - u * s1.y) * di);
+        x1[k * PS] = s1;
+        if (two) {
+            double2 b2 = x2[k * PS];
+            s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
+            x2[k * PS] = s2;
+        }
+    }
+}
+
+// LU factors of every pressure mode matrix (time independent): thread per
+// (kz <= nzm/2, kt).  The k_theta = k_z = 0 matrix is singular (zero-flux
+// rows, kmc(1) = kpc(nrm) = 0); its last pivot is replaced so that the solve
+// returns phi(nrm) = 0 for that mode.
+__global__ void pfactor_kernel(Dims d, Coef c, double* fl, double* fdi) {
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nzh * PH) return;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const size_t FS = (size_t)nzh * PH;
+    const double a3 = c.ak3[kz], a1 = c.ak1[kt];
+    double dp = (c.acph[0] - a3) - a1 * c.usrm2[0];
+    fl[t] = 0.0;
+    fdi[t] = 1.0 / dp;
+    for (int k = 1; k < nr; ++k) {
+        double dk = (c.acph[k] - a3) - a1 * c.usrm2[k];
+        double fact = c.amph[k] / dp;
+        dp = dk - fact * c.apph[k - 1];
+        fl[k * FS + t] = fact;
+        fdi[k * FS + t] = 1.0 / dp;
+    }
+    if (kz == 0 && kt == 0) fdi[(size_t)(nr - 1) * FS + t] = 0.0;
+}
+
+// Inverse real FFT along theta: spec rows -> phi rows.
+template <int R>
+__global__ void __launch_bounds__(128) theta_inv_kernel(Dims d, Fields f, FFTPlan pl, const double2* twr) {
+    if (f.st->halt) return;
+    extern __shared__ double2 smem[];
+    const int M = pl.n, PH = M + 1;
+    double2* a = smem;
+    double2* b = smem + (size_t)R * M;
+    const long long nrows = (long long)d.nr * d.nz;
+    const long long row0 = (long long)blockIdx.x * R;
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, kt = t - r * M;
+        const long long row = row0 + r;
+        double2 z = make_double2(0.0, 0.0);
+        if (row < nrows) {
+            const double2* X = f.spec + (size_t)row * PH;
+            double2 xk = X[kt], xm = X[M - kt];
+            if (kt == 0) { xk.y = 0.0; xm.y = 0.0; }   // imaginary parts of the 0 and Nyquist bins
+            double2 xc = cconj(xm);
+            double2 e = cadd(xk, xc), o = csub(xk, xc);
+            double2 w = cconj(__ldg(twr + kt));
+            double2 wo = cmul(w, o);
+            // Z = e + i wo
+            z = make_double2(e.x - wo.y, e.y + wo.x);
+        }
+        a[kt * R + r] = z;
+    }
+    __syncthreads();
+    const double2* Z = fft_lines<R>(a, b, pl, true);
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, m = t - r * M;
+        const long long row = row0 + r;
+        if (row < nrows) *reinterpret_cast<double2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
+    }
+}
+
+// --------------------------------------------------------------------------
+// Projection: CorrectVelocity.F90:318-337 and CorrectPressure.F90:364-390
+// --------------------------------------------------------------------------
+
+template <bool VEL, bool PRES>
+__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, Consts K, Fields f, int sub) {
+    if (f.st->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= d.nt || j >= d.nz) return;
+    const int nt = d.nt, nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const int im = wm(i, nt), ip = wp(i, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
+    const size_t rowoff = (size_t)j * nt;
+    const size_t o = (size_t)k * P + rowoff + i;
+    const double* phi = f.phi;
+    const double loc = ld(phi + o);
+    const double pim = ld(phi + (size_t)k * P + rowoff + im);
+    const double pjm = ld(phi + (size_t)k * P + (size_t)jm * nt + i);
+    const double pkm = ld(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i);
+    if (VEL) {
+        const double* cf = f.corr + (size_t)sub * 3 * (nr + 1);
+        f.qt[o] -= (loc - pim) * ld(cf + k);
+        if (k >= 1) f.qr[o] -= (loc - pkm) * ld(cf + (nr + 1) + k);
+        f.qz[o] -= (loc - pjm) * ld(cf + 2 * (nr + 1));
+    }
+    if (PRES) {
+        const double pip = ld(phi + (size_t)k * P + rowoff + ip);
+        const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+        const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+        const double be = f.st->beta;
+        const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
+        f.pr[o] = f.pr[o] + loc - be * ((pip - 2.0 * loc + pim) * ld(c.udx1qm + k) +
+                                        (pjp - 2.0 * loc + pjm) * K.dxzq +
+                                        (pkp * app + loc * acc + pkm * amm));
+    }
+}
+
+// CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
+__global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts K, Fields f, double al) {
+    if (f.st->halt) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long half = (long long)d.nr * d.nz * (d.nt / 2);
+    if (t >= half) return;
+    const int M = d.nt / 2;
+    const long long row = t / M;
+    const int m = (int)(t - row * M);
+    const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
+    double2 z = div_pair(d, c, K, f.qt, f.qr, f.qz, k, j, m);
+    const double usdt = 1.0 / (al * f.st->dt);
+    *reinterpret_cast<double2*>(f.phi + (size_t)row * d.nt + 2 * m) = make_double2(z.x * usdt, z.y * usdt);
+}
+
+// --------------------------------------------------------------------------
+// Reductions: per-block partials in a fixed order, then one finishing block.
+// --------------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <bool MAX>
+__device__ double block_reduce(double v, double* sh) {
+    v = MAX ? warp_max(v) : warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (w == 0) {
+        v = (l < nw) ? sh[l] : (MAX ? -1.0e300 : 0.0);
+        v = MAX ? warp_max(v) : warp_sum(v);
+    }
+    return v;
+}
+
+// CalcMaxCFL.F90:30-43 (which = 0) and CheckDivergence.F90:77-89 (which = 1).
+__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Consts K, Fields f, int which,
+                                                               int only_on_output) {
+    __shared__ double sh[32];
+    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    const long long n = (long long)d.nr * d.P;
+    double best = which == 0 ? 0.00000001 : 0.0;
+    const size_t P = (size_t)d.P;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / d.P);
+        const long long cell = t - (long long)k * d.P;
+        const int j = (int)(cell / d.nt), i = (int)(cell - (long long)j * d.nt);
+        const int ip = wp(i, d.nt), jp = wp(j, d.nz);
+        const size_t o = (size_t)t;
+        const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
+        const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
+        const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
+        double v;
+        if (which == 0) {
+            v = fabs((t1 + t0) * 0.5 * K.dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
+                fabs((z1 + z0) * 0.5 * K.dxz);
+        } else {
+            v = fabs(((t1 - t0) * K.dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * K.dxz);
+        }
+        best = fmax(best, v);
+    }
+    best = block_reduce<true>(best, sh);
+    if (threadIdx.x == 0) f.red[blockIdx.x] = best;
+}
+
+__global__ void __launch_bounds__(kRedThreads) cellmax_finish(Fields f, int nblocks, int which, int only_on_output) {
+    __shared__ double sh[32];
+    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    double best = which == 0 ? 0.00000001 : 0.0;
+    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = fmax(best, f.red[t]);
+    best = block_reduce<true>(best, sh);
+    if (threadIdx.x == 0) {
+        if (which == 0) f.st->instcfl = best;
+        else f.st->dmax = best;
+    }
+}
+
+// CalcVelocityStats.F90:21-43: vmax and the pvol-weighted squares.
+__global__ void __launch_bounds__(kRedThreads) vstats_kernel(Dims d, Coef c, Consts K, Fields f, int only_on_output) {
+    __shared__ double sh[32];
+    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    const long long n = (long long)d.nr * d.P;
+    const size_t P = (size_t)d.P;
+    double vm[3] = {-100.0, -100.0, -100.0}, s[3] = {0.0, 0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / d.P);
+        const long long cell = t - (long long)k * d.P;
+        const int j = (int)(cell / d.nt), i = (int)(cell - (long long)j * d.nt);
+        const size_t o = (size_t)t;
+        const double t0 = ld(f.qt + o), r0 = ld(f.qr + o), z0 = ld(f.qz + o);
+        vm[0] = fmax(vm[0], fabs(t0));
+        vm[1] = fmax(vm[1], fabs(r0));
+        vm[2] = fmax(vm[2], fabs(z0));
+        const double pv = ld(c.rc + k + 1) * ld(c.rc + k + 1) - ld(c.rc + k) * ld(c.rc + k);
+        const double t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + wp(i, d.nt));
+        const double r1 = ld(f.qr + o + P);
+        const double z1 = ld(f.qz + (size_t)k * P + (size_t)wp(j, d.nz) * d.nt + i);
+        const double a = t0 + t1, b = r0 * ld(c.usrc + k) + r1 * ld(c.usrc + k + 1), e = z0 + z1;
+        s[0] += a * a * pv * K.pi * 0.25;
+        s[1] += b * b * pv * K.pi * 0.25;
+        s[2] += e * e * pv * K.pi * 0.25;
+    }
+    for (int q = 0; q < 3; ++q) {
+        double m = block_reduce<true>(vm[q], sh);
+        if (threadIdx.x == 0) f.red[(q) * gridDim.x + blockIdx.x] = m;
+        double v = block_reduce<false>(s[q], sh);
+        if (threadIdx.x == 0) f.red[(3 + q) * gridDim.x + blockIdx.x] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads) vstats_finish(Consts K, Fields f, int nblocks, double vol,
+                                                              int only_on_output) {
+    __shared__ double sh[32];
+    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    for (int q = 0; q < 3; ++q) {
+        double m = -100.0, s = 0.0;
+        for (int t = threadIdx.x; t < nblocks; t += blockDim.x) {
+            m = fmax(m, f.red[q * nblocks + t]);
+            s += f.red[(3 + q) * nblocks + t];
+        }
+        m = block_reduce<true>(m, sh);
+        s = block_reduce<false>(s, sh);
+        if (threadIdx.x == 0) {
+            f.st->vmax[q] = m;
+            f.st->rms[q] = s / vol;
+        }
+    }
+}
+
+// CalcTorque.F90:131-150: wall sums over (z, theta) columns.
+__global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, Consts K, Fields f) {
+    __shared__ double sh[32];
+    const int nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const double del = -1.0 / (ld(c.rc + 1) - ld(c.rc + 0));
+    const double deln = -1.0 / (ld(c.rc + nr) - ld(c.rc + nr - 1));
+    double lo = 0.0, up = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < d.P; t += (long long)gridDim.x * blockDim.x) {
+        const double fic = f.icyl ? (double)f.icyl[t] : 1.0;
+        double grtlow = ((ld(f.qt + P + t) * ld(c.usrm + 1) + ld(f.qt + t) * ld(c.usrm + 0)) * 0.5 -
+                         K.virotint * ld(c.usrc + 0)) * del;
+        lo = lo + grtlow * fic;
+        double grtup = (K.virotext * ld(c.usrc + nr) -
+                        (ld(f.qt + (size_t)(nr - 2) * P + t) * ld(c.usrm + nr - 2) +
+                         ld(f.qt + (size_t)(nr - 1) * P + t) * ld(c.usrm + nr - 1)) * 0.5) * deln;
+        up = up + grtup;   // ocylsl = 1
+    }
+    lo = block_reduce<false>(lo, sh);
+    if (threadIdx.x == 0) f.red[blockIdx.x] = lo;
+    up = block_reduce<false>(up, sh);
+    if (threadIdx.x == 0) f.red[gridDim.x + blockIdx.x] = up;
+}
+
+__global__ void __launch_bounds__(kRedThreads) torque_finish(Dims d, Coef c, Consts K, Fields f, int nblocks) {
+    __shared__ double sh[32];
+    double lo = 0.0, up = 0.0;
+    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) {
+        lo += f.red[t];
+        up += f.red[nblocks + t];
+    }
+    lo = block_reduce<false>(lo, sh);
+    up = block_reduce<false>(up, sh);
+    if (threadIdx.x == 0) {
+        const int nr = d.nr;
+        const double reninv = 1.0 / K.ren;
+        const double rint = K.rint, rext = K.rext;
+        const double jlam = 2.0 * rint * rint * rext * rext * (K.virotint / rint - K.virotext / rext) /
+                            (rext * rext - rint * rint) * reninv;
+        const double jlami = 1.0 / jlam;
+        const double r2 = ld(c.rc + 1), rn = ld(c.rc + nr - 1);
+        lo = lo * (r2 * r2 * r2) * reninv * jlami;
+        up = up * (rn * rn * rn) * reninv * jlami;
+        const double surf = 1.0 / ((double)d.nt * (double)d.nz);
+        f.st->torque[0] = lo * surf;
+        f.st->torque[1] = up * surf;
+    }
+}
+
+// --------------------------------------------------------------------------
+// Layout conversion.  Reference layout: stage[(k) + nr*(jh + (nzm+2)*ih)]
+// with jh, ih halo indices (0 and n+1 are ghosts); device: [k][j][i].
+// --------------------------------------------------------------------------
+
+__global__ void to_device_kernel(Dims d, const double* stage, double* dst, int nk, int halo) {
+    __shared__ double tile[32][33];
+    const int nrr = d.nr + 1;
+    const int NJ = d.nz + 2 * halo;
+    const int j = blockIdx.z;
+    const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    // read: k fastest
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        int i = i0 + y, k = k0 + threadIdx.x;
+        if (i < d.nt && k < nk)
+            tile[y][threadIdx.x] = stage[(size_t)k + (size_t)nrr * ((size_t)(j + halo) + (size_t)NJ * (size_t)(i + halo))];
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        int k = k0 + y, i = i0 + threadIdx.x;
+        if (i < d.nt && k < nk) dst[(size_t)k * d.P + (size_t)j * d.nt + i] = tile[threadIdx.x][y];
+    }
+}
+
+// halo = 1: output (nr, nzm+2, nthm+2) with periodic ghosts; halo = 0: (nr, nzm, nthm).
+__global__ void to_host_kernel(Dims d, const double* src, double* stage, int nk, int halo) {
+    __shared__ double tile[32][33];
+    const int nrr = d.nr + 1;
+    const int NJ = d.nz + 2 * halo, NI = d.nt + 2 * halo;
+    const int jh = blockIdx.z;
+    const int j = halo ? (jh == 0 ? d.nz - 1 : (jh == d.nz + 1 ? 0 : jh - 1)) : jh;
+    const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        int k = k0 + y, ih = i0 + threadIdx.x;
+        if (ih < NI && k < nrr) {
+            int i = halo ? (ih == 0 ? d.nt - 1 : (ih == d.nt + 1 ? 0 : ih - 1)) : ih;
+            tile[y][threadIdx.x] = (k < nk) ? src[(size_t)k * d.P + (size_t)j * d.nt + i] : 0.0;
+        }
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        int ih = i0 + y, k = k0 + threadIdx.x;
+        if (ih < NI && k < nrr) stage[(size_t)k + (size_t)nrr * ((size_t)jh + (size_t)NJ * (size_t)ih)] = tile[threadIdx.x][y];
+    }
+}
+
+// FP64 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void fp64_probe_kernel(double* out, int iters, double b, double c) {
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+    double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+    for (int it = 0; it < iters; ++it) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 123.456) out[threadIdx.x] = s;   // keeps the chains live
+}
+
+}  // namespace
+
+double measure_fp64_peak(cudaStream_t s) {
+    const int blocks = 152 * 8, threads = 256, iters = 8192;
+    double* out = nullptr;
+    if (cudaMalloc(&out, threads * sizeof(double)) != cudaSuccess) return -1.0;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);   // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a, s);
+        fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    double flops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads;
+    return flops / (best * 1e-3) / 1e12;
+}
+
+// ==========================================================================
+// Launchers
+// ==========================================================================
+
+#define TC_LAUNCH_CHECK() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) { \
+    std::fprintf(stderr, "tcgb300: launch failed at %s:%d: %s\n", __FILE__, __LINE__, cudaGetErrorString(e_)); } } while (0)
+
+int reduction_blocks() { return kRedBlocks; }
+
+void launch_begin_step(cudaStream_t s, const Consts& k, StepState* st, int mode, double dt, double time) {
+    begin_step_kernel<<<1, 32, 0, s>>>(k, st, mode, dt, time);
+}
+void launch_slip(cudaStream_t s, const Dims& d, const Consts& k, const Fields& f) {
+    slip_kernel<<<(unsigned)((d.P + 255) / 256), 256, 0, s>>>(d, k, f.st, f.icyl);
+}
+void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
+    factors_kernel<<<1, 512, 0, s>>>(d, c, k, f.st, f.F, f.corr);
+}
+void launch_end_step(cudaStream_t s, const Consts& k, StepState* st) { end_step_kernel<<<1, 32, 0, s>>>(k, st); }
+void launch_finish_step(cudaStream_t s, const Consts& k, StepState* st) { finish_step_kernel<<<1, 32, 0, s>>>(k, st); }
+
+static dim3 cell_grid(const Dims& d, dim3& blk) {
+    blk = dim3(d.nt >= 64 ? 64 : 32, d.nt >= 64 ? 2 : 4, 1);
+    return dim3((d.nt + blk.x - 1) / blk.x, (d.nz + blk.y - 1) / blk.y, d.nr);
+}
+
+void launch_momentum(cudaStream_t s, int mode, const Dims& d, const Coef& c, const Consts& k,
+                     const Fields& f, int sub) {
+    MomArgs a;
+    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.pr;
+    a.ru1 = f.ru1; a.ru2 = f.ru2; a.ru3 = f.ru3;
+    a.rhs_t = f.rhs_t; a.rhs_r = f.rhs_r; a.rhs_z = f.rhs_z;
+    a.h_t = f.h_t; a.h_r = f.h_r; a.h_z = f.h_z;
+    a.icyl = k.patterned ? f.icyl : nullptr;
+    a.st = f.st;
+    a.al = k.alm[sub]; a.ga = k.gam[sub]; a.ro = k.rom[sub];
+    dim3 blk;
+    dim3 g = cell_grid(d, blk);
+    if (mode == MODE_FUSED) momentum_kernel<MODE_FUSED><<<g, blk, 0, s>>>(d, c, k, a);
+    else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT><<<g, blk, 0, s>>>(d, c, k, a);
+    else momentum_kernel<MODE_IMPLICIT><<<g, blk, 0, s>>>(d, c, k, a);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_radial_solve(cudaStream_t s, const Dims& d, const Fields& f, int sub) {
+    radial_solve_kernel<<<(unsigned)((d.P + 127) / 128), 128, 0, s>>>(d, f, sub);
+    TC_LAUNCH_CHECK();
+}
+
+template <bool FP, int R>
+static void div_fft_R(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+                      const Plans& p, double al) {
+    size_t sm = (size_t)2 * R * p.th.n * sizeof(double2);
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(div_fft_kernel<FP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    long long nrows = (long long)d.nr * d.nz;
+    div_fft_kernel<FP, R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, c, k, f, p.th, p.twr, al);
+}
+
+int theta_rows(int M) {
+    int R = 1;
+    while (R < 32 && (R * 2) * M <= 512) R *= 2;
+    return R;
+}
+
+void launch_div_fft(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+                    const Plans& p, int sub, bool from_phi) {
+    double al = k.alm[sub];
+    int R = theta_rows(p.th.n);
+#define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR>(s, d, c, k, f, p, al); else div_fft_R<false, RR>(s, d, c, k, f, p, al); break;
+    switch (R) { TC_DF(1) TC_DF(2) TC_DF(4) TC_DF(8) TC_DF(16) TC_DF(32) }
+#undef TC_DF
+    TC_LAUNCH_CHECK();
+}
+
+void launch_zfft(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p, bool inv) {
+    size_t sm = (size_t)2 * kZC * p.z.n * sizeof(double2);
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(zfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    dim3 g((d.PH + kZC - 1) / kZC, d.nr);
+    zfft_kernel<<<g, 128, sm, s>>>(d, f, p.z, inv ? 1 : 0);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const Fields& f) {
+    long long n = (long long)d.nzh * d.PH;
+    ptri_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f);
+    TC_LAUNCH_CHECK();
+}
+
+template <int R>
+static void theta_inv_R(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p) {
+    size_t sm = (size_t)2 * R * p.th.n * sizeof(double2);
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(theta_inv_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    long long nrows = (long long)d.nr * d.nz;
+    theta_inv_kernel<R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, f, p.th, p.twr);
+}
+
+void launch_theta_inverse(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p) {
+    int R = theta_rows(p.th.n);
+    switch (R) {
+        case 1: theta_inv_R<1>(s, d, f, p); break;
+        case 2: theta_inv_R<2>(s, d, f, p); break;
+        case 4: theta_inv_R<4>(s, d, f, p); break;
+        case 8: theta_inv_R<8>(s, d, f, p); break;
+        case 16: theta_inv_R<16>(s, d, f, p); break;
+        default: theta_inv_R<32>(s, d, f, p); break;
+    }
+    TC_LAUNCH_CHECK();
+}
+
+void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+                    int sub, bool vel, bool pres) {
+    dim3 blk;
+    dim3 g = cell_grid(d, blk);
+    if (vel && pres) correct_kernel<true, true><<<g, blk, 0, s>>>(d, c, k, f, sub);
+    else if (vel) correct_kernel<true, false><<<g, blk, 0, s>>>(d, c, k, f, sub);
+    else correct_kernel<false, true><<<g, blk, 0, s>>>(d, c, k, f, sub);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+                       int sub) {
+    long long n = (long long)d.nr * d.nz * (d.nt / 2);
+    divergence_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, k, f, k.alm[sub]);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, double* l, double* dinv) {
+    long long n = (long long)d.nzh * d.PH;
+    pfactor_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, l, dinv);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
+    cellmax_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, 0, 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f, kRedBlocks, 0, 0);
+    TC_LAUNCH_CHECK();
+}
+void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
+                             const Fields& f, bool only_on_output) {
+    cellmax_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, 1, only_on_output ? 1 : 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f, kRedBlocks, 1, only_on_output ? 1 : 0);
+    TC_LAUNCH_CHECK();
+}
+void launch_velocity_stats(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
+                           const Fields& f, bool only_on_output) {
+    vstats_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, only_on_output ? 1 : 0);
+    // CalcVelocityStats.F90:47-50: divide by nthm*nzm*pi*(rext^2 - rint^2)
+    double volt = k.pi * (k.rext * k.rext - k.rint * k.rint);
+    double vol = (double)d.nt * (double)d.nz * volt;
+    vstats_finish<<<1, kRedThreads, 0, s>>>(k, f, kRedBlocks, vol, only_on_output ? 1 : 0);
+    TC_LAUNCH_CHECK();
+}
+void launch_torque(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
+    torque_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f);
+    torque_finish<<<1, kRedThreads, 0, s>>>(d, c, k, f, kRedBlocks);
+    TC_LAUNCH_CHECK();
+}
+
+void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, double* dst, int nk, int halo) {
+    dim3 g((d.nt + 31) / 32, (nk + 31) / 32, d.nz);
+    to_device_kernel<<<g, dim3(32, 8), 0, s>>>(d, stage, dst, nk, halo);
+    TC_LAUNCH_CHECK();
+}
+void launch_to_host(cudaStream_t s, const Dims& d, const double* src, double* stage, int nk, int halo) {
+    dim3 g((d.nt + 2 * halo + 31) / 32, (d.nr + 1 + 31) / 32, d.nz + 2 * halo);
+    to_host_kernel<<<g, dim3(32, 8), 0, s>>>(d, src, stage, nk, halo);
+    TC_LAUNCH_CHECK();
+}
+
+}  // namespace tcgb

@@ -1,0 +1,186 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+The oracle (oracle/tc_ref.cpp) restates the reference Fortran routines; both
+solve the singular k_theta = k_z = 0 pressure mode with phi(nrm) = 0, so every
+field, pressure included, is compared directly.
+
+Tolerances (relative to the max-norm of the oracle field):
+  * one routine on the same input: 1e-12;
+  * one full time step: 1e-12;
+  * 20 RK3 steps: 1e-10 (velocities and pressure), torques 1e-10.
+"""
+import numpy as np
+import pytest
+
+from conftest import make_bou, rel_err, tc
+
+import tc_gb300.initial as ini
+
+pytestmark = pytest.mark.gpu
+
+TOL_ROUTINE = 1e-12
+TOL_STEP = 1e-12
+TOL_20 = 1e-10
+
+
+def pair(oracle, bou, seed=5, amp=0.01):
+    st = ini.couette_noise(bou, seed=seed, amp=amp)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*st)
+    o = oracle.CppOracle(bou)
+    o.set_state(*st)
+    return g, o, st
+
+
+def compare_state(g, o, tol, nrm):
+    gs, os_ = g.get_state(), o.state()
+    errs = {}
+    for name, a, b, nk in zip(("qt", "qr", "qz", "pr"), gs, os_, (nrm, nrm + 1, nrm, nrm)):
+        errs[name] = rel_err(a, b, nk=nk)
+    assert max(errs.values()) < tol, errs
+    return errs
+
+
+@pytest.mark.parametrize("case", [
+    dict(),
+    dict(nthm=48, nzm=40, nrm=24, istr=4, str=3.0, sizepert=0.1, omegapert=0.5, romeg=0.1, dtmin=1e-4, dtmax=1e-4),
+    dict(nthm=32, nzm=96, nrm=20, istr=6, str=3.0),
+    dict(nthm=20, nzm=30, nrm=12, nsst=1),
+], ids=["uniform64", "tanh-osc-rot", "cheb-radix3", "ab2-radix5"])
+def test_routines_one_substep(gpu_lib, oracle, case):
+    """Each routine of substep 1 (then 2) on identical input."""
+    bou = make_bou(**case)
+    g, o, _ = pair(oracle, bou)
+    dt = bou["dtmax"]
+    nrm = bou["nrm"]
+    g.begin_step(dt, 0.37)
+    o.call("begin_step", dt, 0.37)
+    for ns in range(1, bou["nsst"] + 1):
+        g.set_substep(ns)
+        o.call("set_substep", ns)
+        g.explicit_terms()
+        for f in ("explicit_terms_qt", "explicit_terms_qr", "explicit_terms_qz"):
+            o.call(f)
+        assert rel_err(g.get_field("dq"), o.get(oracle.DQ), interior=False, nk=nrm) < TOL_ROUTINE
+        assert rel_err(g.get_field("qcap"), o.get(oracle.QCAP), interior=False, nk=nrm) < TOL_ROUTINE
+        hr_o = o.get(oracle.DPH)[1:-1, 1:-1, 1:nrm]
+        assert rel_err(g.get_field("hr")[..., 1:nrm], hr_o, interior=False) < TOL_ROUTINE
+        g.implicit_and_update()
+        for f in ("implicit_rhs_qt", "solve_imp_eqn_update_qt", "implicit_rhs_qr", "solve_imp_eqn_update_qr",
+                  "implicit_rhs_qz", "solve_imp_eqn_update_qz"):
+            o.call(f)
+        for w in (oracle.QT, oracle.QR, oracle.QZ):
+            o.call("update_halo", w)
+        for name, w in (("ru1", oracle.RU1), ("ru2", oracle.RU2), ("ru3", oracle.RU3)):
+            lo = 1 if name == "ru2" else 0
+            hi = nrm
+            assert rel_err(g.get_field(name)[..., lo:hi], o.get(w)[..., lo:hi], interior=False) < TOL_ROUTINE, name
+        compare_state(g, o, TOL_ROUTINE, nrm)
+        g.calc_local_divergence()
+        o.call("calc_local_divergence")
+        assert rel_err(g.get_field("dph"), o.get(oracle.DPH), nk=nrm) < TOL_ROUTINE
+        g.solve_pressure_correction()
+        o.call("solve_pressure_correction")
+        o.call("update_halo", oracle.DPH)
+        assert rel_err(g.get_field("dph"), o.get(oracle.DPH), nk=nrm) < TOL_ROUTINE
+        g.correct_velocity()
+        o.call("correct_velocity")
+        g.correct_pressure()
+        o.call("correct_pressure")
+        for w in (oracle.QT, oracle.QR, oracle.QZ, oracle.PR):
+            o.call("update_halo", w)
+        compare_state(g, o, TOL_ROUTINE, nrm)
+    g.close()
+
+
+def test_fused_step_matches_routines(gpu_lib, oracle):
+    """tc_time_marcher (fused kernels) equals the oracle's TimeMarcher."""
+    bou = make_bou(nthm=32, nzm=48, nrm=32)
+    g, o, _ = pair(oracle, bou)
+    g.time_marcher(1e-3, 0.0)
+    o.time_marcher(1e-3, 0.0)
+    compare_state(g, o, TOL_STEP, bou["nrm"])
+    g.close()
+
+
+@pytest.mark.parametrize("case", [
+    dict(),
+    dict(nthm=64, nzm=48, nrm=48, istr=4, str=4.0, sizepert=0.1, omegapert=0.5, romeg=0.1, ren=5000.0,
+         dtmin=1e-5, dtmax=1e-3, limitCFL=1.2),
+], ids=["C1-64cubed-fixed-dt", "tanh-variable-dt"])
+def test_twenty_steps(gpu_lib, oracle, case):
+    """20 steps (NTST = 19 in the reference's 0..NTST loop) through tc_run."""
+    bou = make_bou(**case)
+    g, o, _ = pair(oracle, bou)
+    code_g, n_g, t_g, dt_g = g.run(20, 0, 0.0)
+    code_o, t_o, dt_o = o.run(0, 20, 0.0)
+    assert code_g == code_o == 0
+    assert n_g == 20
+    assert abs(t_g - t_o) <= 1e-12 * abs(t_o)
+    errs = compare_state(g, o, TOL_20, bou["nrm"])
+    ti_g, to_g = g.calc_torque()
+    ti_o, to_o = o.calc_torque()
+    assert abs(ti_g - ti_o) <= TOL_20 * abs(ti_o)
+    assert abs(to_g - to_o) <= TOL_20 * abs(to_o)
+    assert g.check_divergence() < bou["resid"]
+    print(case, errs, (ti_g, to_g))
+    g.close()
+
+
+def test_reductions(gpu_lib, oracle):
+    bou = make_bou(nthm=48, nzm=64, nrm=40, istr=4)
+    g, o, _ = pair(oracle, bou, amp=0.05)
+    assert abs(g.calc_max_cfl() - o.calc_max_cfl()) <= 1e-13 * o.calc_max_cfl()
+    assert abs(g.check_divergence() - o.check_divergence()) <= 1e-12 * o.check_divergence()
+    ti, to = g.calc_torque()
+    ri, ro = o.calc_torque()
+    assert abs(ti - ri) <= 1e-12 * abs(ri) and abs(to - ro) <= 1e-12 * abs(ro)
+    vg, rg = g.velocity_stats()
+    vo, ro_ = o.velocity_stats()
+    np.testing.assert_allclose(vg, vo, rtol=1e-14)
+    np.testing.assert_allclose(rg, ro_, rtol=1e-12)
+    g.close()
+
+
+def test_patterned_slip(gpu_lib, oracle):
+    """SlipBCs with MINSTRT, MINSTRZ, MULTMIN non-zero (rotating free-slip bands)."""
+    bou = make_bou(nthm=32, nzm=32, nrm=24, minstrt=2, minstrz=1, multmin=2)
+    g, o, _ = pair(oracle, bou)
+    t = 0.0
+    for n in range(3):
+        g.time_marcher(1e-3, t)
+        o.time_marcher(1e-3, t)
+        t += 0.25   # rotate the pattern between steps
+    compare_state(g, o, 1e-11, bou["nrm"])
+    ti, to = g.calc_torque()
+    ri, ro = o.calc_torque()
+    assert abs(ti - ri) <= 1e-11 * abs(ri)
+    g.close()
+
+
+def test_state_round_trip(gpu_lib):
+    bou = make_bou(nthm=24, nzm=18, nrm=10)
+    st = ini.couette_noise(bou, seed=3)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*st)
+    back = g.get_state()
+    for a, b in zip(back[:3], st[:3]):
+        np.testing.assert_array_equal(a[..., :bou["nrm"]], b[..., :bou["nrm"]])
+    np.testing.assert_array_equal(back[1], st[1])
+    g.close()
+
+
+def test_error_codes(gpu_lib, oracle):
+    """main.F90 exits: 166 (dt < DTMIN), 333 (time > TMAX), 555 (NTST)."""
+    cases = [dict(dtmin=1e-2, dtmax=1e-3, nthm=16, nzm=16, nrm=12),
+             dict(tmax=2.5e-3, nthm=16, nzm=16, nrm=12),
+             dict(ntst=3, nthm=16, nzm=16, nrm=12)]
+    for c in cases:
+        bou = make_bou(**c)
+        g, o, _ = pair(oracle, bou)
+        code_g, n_g, t_g, _ = g.run(10, 0, 0.0)
+        code_o, t_o, _ = o.run(0, 10, 0.0)
+        assert code_g == code_o != 0, (c, code_g, code_o)
+        assert abs(t_g - t_o) < 1e-15
+        compare_state(g, o, 1e-11, bou["nrm"])
+        g.close()

@@ -1,0 +1,118 @@
+"""The CPU oracle (test infrastructure) checked against an independent
+restatement that calls the real LAPACK ?gttrf/?gttrs (scipy) and numpy.fft, and
+against physics known-answer tests.  The reference ships no golden vectors, so
+this is how the oracle is pinned."""
+import numpy as np
+import pytest
+
+from conftest import make_bou, rel_err
+
+import tc_gb300.initial as ini
+import tc_np
+
+
+def run_both(oracle, bou, nsteps, dt, pin=True, seed=7):
+    st = ini.couette_noise(bou, seed=seed)
+    c = oracle.CppOracle(bou, oracle.MODE00_PIN if pin else oracle.MODE00_LAPACK)
+    n = tc_np.NpOracle(bou, pin_mode00=pin)
+    c.set_state(*st)
+    n.set_state(*st)
+    t = 0.0
+    for _ in range(nsteps):
+        c.time_marcher(dt, t)
+        n.time_marcher(dt, t)
+        t += dt
+    return c, n
+
+
+@pytest.mark.parametrize("case,dt", [
+    (dict(nthm=16, nzm=24, nrm=16), 1e-3),
+    (dict(nthm=16, nzm=24, nrm=20, istr=4, sizepert=0.1, omegapert=0.5, romeg=0.1), 2e-5),
+    (dict(nthm=12, nzm=18, nrm=16, istr=6, str=3.0), 1e-3),
+    (dict(nthm=12, nzm=10, nrm=8, nsst=1), 1e-3),
+], ids=["uniform", "tanh-osc-rot", "cheb", "ab2"])
+def test_cpp_matches_lapack_numpy(oracle, case, dt):
+    bou = make_bou(**case)
+    c, n = run_both(oracle, bou, 5, dt)
+    nrm = bou["nrm"]
+    for w, a, nk in ((oracle.QT, n.qt, nrm), (oracle.QR, n.qr, nrm + 1), (oracle.QZ, n.qz, nrm), (oracle.PR, n.pr, nrm)):
+        assert rel_err(c.get(w), a, nk=nk) < 1e-11, w
+    ti, to = c.calc_torque()
+    ni, no = n.calc_torque()
+    assert abs(ti - ni) < 1e-12 * abs(ni) and abs(to - no) < 1e-12 * abs(no)
+    assert abs(c.calc_max_cfl() - n.calc_max_cfl()) < 1e-12 * n.calc_max_cfl()
+
+
+def test_mode00_only_moves_pressure(oracle):
+    """The singular k=0 pressure mode: LAPACK's roundoff pivot (real LAPACK in
+    numpy) versus the pinned solve changes velocities only at roundoff."""
+    bou = make_bou(nthm=16, nzm=16, nrm=16)
+    st = ini.couette_noise(bou, seed=2)
+    c = oracle.CppOracle(bou, oracle.MODE00_PIN)
+    n = tc_np.NpOracle(bou, pin_mode00=False)
+    c.set_state(*st)
+    n.set_state(*st)
+    for s in range(10):
+        c.time_marcher(1e-3, s * 1e-3)
+        n.time_marcher(1e-3, s * 1e-3)
+    for w, a, nk in ((oracle.QT, n.qt, 16), (oracle.QR, n.qr, 17), (oracle.QZ, n.qz, 16)):
+        assert rel_err(c.get(w), a, nk=nk) < 1e-12
+
+
+def test_laminar_couette_torque(oracle):
+    """CalcTorque normalises by the laminar torque: circular Couette flow gives
+    torque -> 1 at both walls as the radial grid is refined (the wall gradient
+    of CalcTorque.F90:133-137 is first-order accurate)."""
+    errs = []
+    for nrm in (32, 64, 128):
+        bou = make_bou(nthm=8, nzm=8, nrm=nrm)
+        st = ini.couette_noise(bou, seed=1, amp=0.0)
+        c = oracle.CppOracle(bou)
+        c.set_state(*st)
+        for s in range(3):
+            c.time_marcher(1e-3, s * 1e-3)
+        ti, to = c.calc_torque()
+        errs.append(max(abs(ti - 1.0), abs(to - 1.0)))
+        assert c.check_divergence() < 1e-12
+    assert errs[1] < 0.02
+    assert errs[1] < errs[0] / 1.8 and errs[2] < errs[1] / 1.8, errs
+
+
+def test_projection_is_divergence_free(oracle):
+    bou = make_bou(nthm=16, nzm=16, nrm=16, istr=4)
+    st = ini.couette_noise(bou, seed=4, amp=0.05)
+    c = oracle.CppOracle(bou)
+    c.set_state(*st)
+    d0 = c.check_divergence()
+    c.time_marcher(1e-4, 0.0)
+    assert d0 > 1.0
+    assert c.check_divergence() < 1e-11 * d0
+
+
+def test_run_error_codes(oracle):
+    bou = make_bou(nthm=8, nzm=8, nrm=8, tmax=2.5e-3)
+    st = ini.couette_noise(bou, seed=1)
+    c = oracle.CppOracle(bou)
+    c.set_state(*st)
+    code, t, dt = c.run(0, 10, 0.0)
+    assert code == 333 and abs(t - 3e-3) < 1e-15
+    bou = make_bou(nthm=8, nzm=8, nrm=8, ntst=2)
+    c = oracle.CppOracle(bou)
+    c.set_state(*st)
+    code, t, dt = c.run(0, 10, 0.0)
+    assert code == 555 and abs(t - 3e-3) < 1e-15
+
+
+def test_thread_count_does_not_change_results(oracle):
+    bou = make_bou(nthm=16, nzm=16, nrm=16)
+    st = ini.couette_noise(bou, seed=9)
+    res = []
+    for th in (1, 4):
+        oracle.set_threads(th)
+        c = oracle.CppOracle(bou)
+        c.set_state(*st)
+        c.time_marcher(1e-3, 0.0)
+        res.append(c.state())
+    oracle.set_threads(0)
+    for a, b in zip(*res):
+        np.testing.assert_array_equal(a, b)
