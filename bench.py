@@ -2,10 +2,12 @@
 """Throughput of the Taylor-Couette time step on GB300, in Mcell-steps/s.
 
 Workload (default, "C2"): 512 x 512 x 384 (theta x z x r) cells, radial
-tanh clustering at both walls (ISTR=4, STR3=4; the configuration's ISTR=1 is
-undefined in the reference grid generator and maps to 4), RINT=1, REXT=1.4,
-ALX3D=2*pi, 1/NU=5000, inner cylinder oscillating (VIROTINT=1, AMPL_PERT=0.1,
-FREQ_PERT=0.5), RK3, variable dt (CFLMAX=1.2, DTMIN=1e-5), seeded
+clustering at both walls with the reference's own bou.in grid (ISTR=6,
+STR3=20: the configuration's ISTR=1 is undefined in the reference grid
+generator, and the tanh grid ISTR=4 with STR3=4 is numerically unstable in the
+reference algorithm at 384 radial cells), RINT=1, REXT=1.4, ALX3D=2*pi,
+1/NU=5000, inner cylinder oscillating (VIROTINT=1, AMPL_PERT=0.1,
+FREQ_PERT=0.5), RK3, variable dt (CFLMAX=1.2, DTMIN=1e-5, DTMAX=1e-3), seeded
 Couette-plus-noise start (amplitude 0.01).  One "step" is one full RK3 time
 step (three substeps) with the dt rule of main.F90, FP64 throughout.
 
@@ -41,17 +43,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    "C2": dict(nthm=512, nzm=512, nrm=384, istr=4, str=4.0, ren=5000.0, sizepert=0.1, omegapert=0.5,
-               idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=1e-2),
+    "C2": dict(nthm=512, nzm=512, nrm=384, istr=6, str=20.0, ren=5000.0, sizepert=0.1, omegapert=0.5,
+               idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=1e-3),
     "C1": dict(nthm=64, nzm=64, nrm=64, istr=0, ren=1000.0, idtv=1, limitCFL=1e3, dtmin=1e-3, dtmax=1e-3),
-    "C3": dict(nthm=1024, nzm=768, nrm=512, istr=4, str=4.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
-               dtmin=1e-5, dtmax=1e-2),
+    # profiling size: the C2 theta-z plane with a third of the radial cells (a few GB on the device)
+    "P2": dict(nthm=512, nzm=512, nrm=128, istr=6, str=20.0, ren=5000.0, sizepert=0.1, omegapert=0.5,
+               idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=1e-3),
+    "C3": dict(nthm=1024, nzm=768, nrm=512, istr=6, str=20.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
+               dtmin=1e-5, dtmax=1e-3),
 }
 DESCR = {
-    "C2": "512x512x384 theta x z x r, ISTR=4 STR3=4, RINT=1 REXT=1.4, 1/NU=5000, AMPL_PERT=0.1 FREQ_PERT=0.5, "
-          "RK3, variable dt CFLMAX=1.2 DTMIN=1e-5, seeded Couette+noise 0.01",
+    "C2": "512x512x384 theta x z x r, wall-clustered radial grid ISTR=6 STR3=20, RINT=1 REXT=1.4, 1/NU=5000, "
+          "AMPL_PERT=0.1 FREQ_PERT=0.5, RK3, variable dt CFLMAX=1.2 DTMIN=1e-5 DTMAX=1e-3, seeded Couette+noise 0.01",
     "C1": "64x64x64, ISTR=0, RINT=1 REXT=1.4, 1/NU=1000, RK3, dt=1e-3, seeded Couette+noise 0.01",
-    "C3": "1024x768x512, ISTR=4 STR3=4, ROTP=0.1, 1/NU=2e4, RK3, variable dt CFLMAX=1.2 (FP64 form)",
+    "P2": "512x512x128 (profiling size of C2), ISTR=6 STR3=20, 1/NU=5000, RK3, variable dt",
+    "C3": "1024x768x512, ISTR=6 STR3=20, ROTP=0.1, 1/NU=2e4, RK3, variable dt CFLMAX=1.2 DTMAX=1e-3 (FP64 form)",
 }
 
 # Algorithmic HBM bytes per cell and launch of each kernel class (FP64):

@@ -116,3 +116,20 @@ def test_thread_count_does_not_change_results(oracle):
     oracle.set_threads(0)
     for a, b in zip(*res):
         np.testing.assert_array_equal(a, b)
+
+
+def test_tanh_grid_with_str4_is_unstable_in_the_reference_algorithm(oracle):
+    """Why the production workload uses the ISTR=6, STR3=20 radial grid of the
+    reference's bou.in: with the tanh grid ISTR=4, STR3=4 at 384 radial cells
+    (wall cell 5.7e-6 wide, 700 times smaller than the widest) the reference
+    algorithm blows up within a few steps even at dt = 1e-4 (velocity limited
+    by CFL, not by this), while ISTR=6 with STR3=20 stays bounded."""
+    def vmax_after(istr, st, nsteps=4, dt=1e-4):
+        bou = make_bou(nthm=16, nzm=16, nrm=384, istr=istr, str=st, ren=5000.0, sizepert=0.1, omegapert=0.5)
+        c = oracle.CppOracle(bou)
+        c.set_state(*ini.couette_noise(bou, seed=1234))
+        for s in range(nsteps):
+            c.time_marcher(dt, s * dt)
+        return float(c.velocity_stats()[0].max())
+    assert vmax_after(4, 4.0) > 1e3
+    assert vmax_after(6, 20.0) < 2.0
