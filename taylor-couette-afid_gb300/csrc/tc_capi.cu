@@ -171,6 +171,14 @@ int tc_create(const tc_bou* cfg, tc_handle** out) {
     k.dtmin = cfg->dtmin; k.dtmax = cfg->dtmax; k.limitCFL = cfg->limitCFL; k.tout = cfg->tout;
     k.tmax = cfg->tmax; k.limitVel = cfg->limitVel; k.resid = cfg->resid;
     time_march_scheme(cfg->nsst, k.gam, k.rom, k.alm);
+    k.udxz = g.dxz * 0.25;
+    k.udxzq = g.dxzq / cfg->ren;
+    for (int s = 0; s < 3; ++s) {
+        k.alre[s] = k.alm[s] / cfg->ren;
+        k.dxz_al[s] = g.dxz * k.alm[s];
+        k.dxt_al[s] = g.dxt * k.alm[s];
+    }
+    k.fft_norm = 0.5 / ((double)cfg->nthm * (double)cfg->nzm);
     k.nsst = cfg->nsst; k.idtv = cfg->idtv; k.ntst = cfg->ntst;
     k.minstrt = cfg->minstrt; k.minstrz = cfg->minstrz; k.multmin = cfg->multmin;
     k.patterned = (cfg->minstrt * cfg->multmin + cfg->minstrz * cfg->multmin) != 0;
@@ -231,7 +239,7 @@ int tc_create(const tc_bou* cfg, tc_handle** out) {
     AL(f.st, 1);
     AL(f.F.base, MomFactors::doubles(nrr));
     f.F.stride = nrr;
-    AL(f.corr, (size_t)9 * nrr);
+    AL(f.corr, (size_t)9 * nrr + 8);
     AL(f.red, (size_t)6 * reduction_blocks());
     AL(h->stage, (size_t)nrr * (d.nz + 2) * (d.nt + 2));
 #undef AL

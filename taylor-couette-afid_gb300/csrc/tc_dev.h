@@ -51,6 +51,11 @@ struct Consts {
     double sizepert, omegapert, pi, rint, rext, lamb;
     double dtmin, dtmax, limitCFL, tout, tmax, limitVel, resid;
     double gam[3], rom[3], alm[3];
+    // scalars hoisted out of the kernels (host-computed, time independent)
+    double udxz, udxzq;          // dxz*0.25 (ExplicitTerms*), dxzq/ren
+    double alre[3];              // al/ren per substep
+    double dxz_al[3], dxt_al[3]; // dxz*al, dxt*al per substep
+    double fft_norm;             // 0.5/(nthm*nzm): FFT normalisation and real-unpacking 1/2
     int nsst, idtv, ntst;
     int patterned;          // patterned slip active (SlipBCs.F90:520)
     int minstrt, minstrz, multmin;

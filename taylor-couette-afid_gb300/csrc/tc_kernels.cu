@@ -189,6 +189,10 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
         int s = threadIdx.x - 32;
         // SolveImpEqnUpdate_QT.F90:67
         *F.extra(s) = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
+        // CalcLocalDivergence.F90:19 usdt, alone and times the FFT normalisation
+        const double usdt = 1.0 / (k.alm[s] * dt);
+        corr[9 * (nr + 1) + s] = usdt * k.fft_norm;
+        corr[9 * (nr + 1) + 3 + s] = usdt;
     }
     __syncthreads();
     // phase 3: reciprocals of the pivots
@@ -227,7 +231,7 @@ __device__ double explicit_qt(const Stencil& S, int nr, const Coef& c, const Con
     double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
     const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
     const double usrm = ld(c.usrm + k), usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
-    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    const double udxz = K.udxz, udxzq = K.udxzq;
     double h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
     double h12d = ((r_p + r_pim) * (t_kp + t_c) - (r_c + r_im) * (t_c + t_km)) * 0.25 * ld(c.udx2rm + k);
     double h12n = t_c * usrm * ((r_p + r_pim) * usrcp + (r_c + r_im) * usrc) * 0.25;
@@ -254,7 +258,7 @@ __device__ double explicit_qr(const Stencil& S, const Coef& c, const Consts& K,
     double z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
     const double udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
     const double usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
-    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    const double udxz = K.udxz, udxzq = K.udxzq;
     double a = (t_ip + t_mip + t_c + t_m) * 0.25;
     double h11n = a * a;
     double h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
@@ -279,7 +283,7 @@ __device__ double explicit_qz(const Stencil& S, int nr, const Coef& c, const Con
     double r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
     double r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
     const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-    const double udxz = K.dxz * 0.25, udxzq = K.dxzq / K.ren;
+    const double udxz = K.udxz, udxzq = K.udxzq;
     double h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
     double h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.udx2rm + k) * 0.25;
     double h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * udxz;
@@ -293,7 +297,7 @@ struct MomArgs {
     double *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
     const signed char* icyl;
     const StepState* st;
-    double al, ga, ro;
+    double al, ga, ro, alre, dxt_al, dxz_al;
 };
 
 template <int MODE>
@@ -324,7 +328,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
         if (k >= 1) hr = a.h_r[o];
         hz = a.h_z[o];
     }
-    const double dt = a.st->dt, al = a.al, ga = a.ga, ro = a.ro, alre = al / K.ren;
+    const double dt = a.st->dt, ga = a.ga, ro = a.ro, alre = a.alre;
     const double fic = a.icyl ? (double)a.icyl[(size_t)j * d.nt + i] : 1.0, foc = 1.0;
     const double* qt = a.qt;
     const double* qr = a.qr;
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
             d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
                   ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
         }
-        double dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * K.dxt * al * ld(c.usrm + k);
+        double dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
         double old = ro != 0.0 ? a.ru1[o] : 0.0;
         a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
         a.ru1[o] = ht;
@@ -357,7 +361,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
     if (k >= 1) {
         double d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
                      ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
-        double udx2 = ld(c.rc + k) * al * ld(c.udx2c + k);
+        double udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
         double dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
         double old = ro != 0.0 ? a.ru2[o] : 0.0;
         a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
             d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
                   ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
         }
-        double dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * (K.dxz * al);
+        double dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
         double old = (k == nr - 1) ? hz : (ro != 0.0 ? a.ru3[o] : 0.0);
@@ -489,7 +493,7 @@ __device__ __forceinline__ double2 div_pair(const Dims& d, const Coef& c, const 
 // the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
 template <bool FROM_PHI, int R>
 __global__ void __launch_bounds__(128) div_fft_kernel(Dims d, Coef c, Consts K, Fields f, FFTPlan pl,
-                                                      const double2* twr, double al) {
+                                                      const double2* twr, int sub) {
     if (f.st->halt) return;
     extern __shared__ double2 smem[];
     const int M = pl.n;
@@ -497,9 +501,9 @@ __global__ void __launch_bounds__(128) div_fft_kernel(Dims d, Coef c, Consts K, 
     double2* b = smem + (size_t)R * M;
     const long long nrows = (long long)d.nr * d.nz;
     const long long row0 = (long long)blockIdx.x * R;
-    // the 1/2 of the real-transform unpacking is folded into the scale
-    const double norm = 0.5 / ((double)d.nt * (double)d.nz);
-    const double scl = FROM_PHI ? norm : (1.0 / (al * f.st->dt)) * norm;
+    // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in;
+    // the factors kernel stores it per substep behind the correction coefficients
+    const double scl = FROM_PHI ? K.fft_norm : f.corr[9 * (d.nr + 1) + sub];
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = t / M, m = t - r * M;
         const long long row = row0 + r;
@@ -698,7 +702,7 @@ __global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, Consts K, 
 }
 
 // CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
-__global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts K, Fields f, double al) {
+__global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts K, Fields f, int sub) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long half = (long long)d.nr * d.nz * (d.nt / 2);
@@ -708,7 +712,7 @@ __global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts 
     const int m = (int)(t - row * M);
     const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
     double2 z = div_pair(d, c, K, f.qt, f.qr, f.qz, k, j, m);
-    const double usdt = 1.0 / (al * f.st->dt);
+    const double usdt = f.corr[9 * (d.nr + 1) + 3 + sub];
     *reinterpret_cast<double2*>(f.phi + (size_t)row * d.nt + 2 * m) = make_double2(z.x * usdt, z.y * usdt);
 }
 
@@ -1003,6 +1007,7 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const Coef& c, con
     a.icyl = k.patterned ? f.icyl : nullptr;
     a.st = f.st;
     a.al = k.alm[sub]; a.ga = k.gam[sub]; a.ro = k.rom[sub];
+    a.alre = k.alre[sub]; a.dxt_al = k.dxt_al[sub]; a.dxz_al = k.dxz_al[sub];
     dim3 blk;
     dim3 g = cell_grid(d, blk);
     if (mode == MODE_FUSED) momentum_kernel<MODE_FUSED><<<g, blk, 0, s>>>(d, c, k, a);
@@ -1018,12 +1023,12 @@ void launch_radial_solve(cudaStream_t s, const Dims& d, const Fields& f, int sub
 
 template <bool FP, int R>
 static void div_fft_R(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
-                      const Plans& p, double al) {
+                      const Plans& p, int sub) {
     size_t sm = (size_t)2 * R * p.th.n * sizeof(double2);
     static bool attr = false;
     if (!attr) { cudaFuncSetAttribute(div_fft_kernel<FP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
     long long nrows = (long long)d.nr * d.nz;
-    div_fft_kernel<FP, R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, c, k, f, p.th, p.twr, al);
+    div_fft_kernel<FP, R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, c, k, f, p.th, p.twr, sub);
 }
 
 int theta_rows(int M) {
@@ -1034,9 +1039,8 @@ int theta_rows(int M) {
 
 void launch_div_fft(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
                     const Plans& p, int sub, bool from_phi) {
-    double al = k.alm[sub];
     int R = theta_rows(p.th.n);
-#define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR>(s, d, c, k, f, p, al); else div_fft_R<false, RR>(s, d, c, k, f, p, al); break;
+#define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR>(s, d, c, k, f, p, sub); else div_fft_R<false, RR>(s, d, c, k, f, p, sub); break;
     switch (R) { TC_DF(1) TC_DF(2) TC_DF(4) TC_DF(8) TC_DF(16) TC_DF(32) }
 #undef TC_DF
     TC_LAUNCH_CHECK();
@@ -1092,7 +1096,7 @@ void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& 
 void launch_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
                        int sub) {
     long long n = (long long)d.nr * d.nz * (d.nt / 2);
-    divergence_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, k, f, k.alm[sub]);
+    divergence_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, k, f, sub);
     TC_LAUNCH_CHECK();
 }
 
