@@ -235,6 +235,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed FP32/FP64 leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -333,6 +334,54 @@ def main():
                "ms_per_step": ms_e2e / args.steps,
                "note": "state in (tc_set_state) and out (tc_get_state) once per timed run, amortised per step; "
                        "dt/time read back every step"}
+        ref_state = (qt_o, qr_o, qz_o)
+        ref_torque = g.calc_torque()
+
+    # ---- the mixed FP32/FP64 form on the same start ---------------------------
+    mixed = None
+    if not args.no_mixed:
+        gm = tc.TaylorCouette(bou, precision="mixed")
+        gm.set_stream(stream.cuda_stream)
+        gm.set_state(*pinned)
+        code_m, ntm, tm, _ = gm.run(args.warmup, 0, 0.0)
+        gm.profile(True)
+        barrier()
+        e0.record(stream)
+        code_m, ntm, tm, _ = gm.run(args.steps, ntm, tm)
+        e1.record(stream)
+        barrier()
+        ms_m = max_over_ranks(e0.elapsed_time(e1))
+        prof_m = gm.profile_read()
+        gm.profile(False)
+        mixed = {"value": world * cells * args.steps / (ms_m * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                 "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m, "status": code_m}
+        tot_m = sum(v[0] for v in prof_m.values())
+        mixed["kernel_shares"] = {k: round(v[0] / tot_m, 4) for k, v in prof_m.items() if v[1]}
+        if e2e is not None:
+            barrier()
+            e0.record(stream)
+            gm.set_state(*pinned)
+            nt3, t3 = 0, 0.0
+            for _ in range(args.steps):
+                code_m, nt3, t3, _ = gm.run(1, nt3, t3)
+            mstate = gm.get_state()
+            e1.record(stream)
+            barrier()
+            ms_me = max_over_ranks(e0.elapsed_time(e1))
+            mixed["e2e"] = {"value": world * cells * args.steps / (ms_me * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                            "ms_per_step": ms_me / args.steps}
+            # error against the FP64 path after the same K steps from the same start
+            errs = {}
+            for name, a, b, nk in zip(("qt", "qr", "qz"), mstate[:3], ref_state, (nr, nr + 1, nr)):
+                a, b = a[1:-1, 1:-1, :nk], b[1:-1, 1:-1, :nk]
+                errs[name] = float(np.abs(a - b).max() / np.abs(b).max())
+            ti, to = gm.calc_torque()
+            errs["torque_inner"] = abs(ti - ref_torque[0]) / abs(ref_torque[0])
+            errs["torque_outer"] = abs(to - ref_torque[1]) / abs(ref_torque[1])
+            errs["max_divergence"] = gm.check_divergence()
+            errs["steps"] = args.steps
+            mixed["err_vs_fp64"] = errs
+        gm.close()
 
     if rank != 0:
         if dist is not None:
@@ -385,6 +434,7 @@ def main():
         "kernel_shares": shares,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "mixed": mixed,
         "gpu_launches": launches,
         "clocks": clk,
         "sim": {"time": tsim, "last_dt": dt},

@@ -20,7 +20,8 @@
  *  - All work is ordered on the handle's CUDA stream.  Calls that return
  *    host scalars synchronise that stream.  A handle is used by one host
  *    thread at a time; distinct handles are independent.
- *  - All arithmetic is IEEE FP64.
+ *  - Handles made by tc_create compute in IEEE FP64; tc_create_ex can make a
+ *    mixed FP32/FP64 handle (see enum tc_precision_mode).
  */
 #ifndef TC_CAPI_H
 #define TC_CAPI_H
@@ -44,6 +45,14 @@ typedef struct tc_bou {
 } tc_bou;
 
 typedef struct tc_handle tc_handle;
+
+/* Precision of a handle.  TC_PREC_FP64: the plain path, every operation in
+ * IEEE FP64 (the drop-in).  TC_PREC_MIXED: velocity fields, explicit terms,
+ * implicit momentum sweeps and FFTs in FP32 with FP32 accumulation; the
+ * radial pressure tridiagonals, the pressure accumulation of CorrectPressure
+ * and the CFL/divergence/torque reductions in FP64.  Host arrays are FP64
+ * in both. */
+enum tc_precision_mode { TC_PREC_FP64 = 0, TC_PREC_MIXED = 1 };
 
 /* 1-D grid/coefficient arrays, 0-based (entry m = reference index m+1). */
 enum tc_grid_array {
@@ -89,6 +98,11 @@ const char* tc_version(void);
  * all device state on the current CUDA device, zero it.  Fields start at zero
  * and time at 0; load a start with tc_set_state. */
 int tc_create(const tc_bou* cfg, tc_handle** out);
+/* tc_create with a precision (enum tc_precision_mode); tc_create is
+ * tc_create_ex(cfg, TC_PREC_FP64, out).  No counterpart in the reference,
+ * which is FP64 only. */
+int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out);
+int tc_precision(const tc_handle* h);
 void tc_destroy(tc_handle* h);
 const char* tc_last_error(const tc_handle* h);   /* h may be NULL */
 

@@ -84,6 +84,8 @@ SIGNATURES = {
     "tc_grid_array": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_int, _dp, ctypes.c_int]),
     "tc_version": (ctypes.c_char_p, []),
     "tc_create": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.POINTER(_vp)]),
+    "tc_create_ex": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_int, ctypes.POINTER(_vp)]),
+    "tc_precision": (ctypes.c_int, [_vp]),
     "tc_destroy": (None, [_vp]),
     "tc_last_error": (ctypes.c_char_p, [_vp]),
     "tc_set_stream": (ctypes.c_int, [_vp, _vp]),
@@ -158,15 +160,26 @@ def grid_array(bou: dict, name: str) -> np.ndarray:
     return out[:rc].copy()
 
 
-class TaylorCouette:
-    """One simulation instance resident on the current CUDA device."""
+PREC_FP64, PREC_MIXED = 0, 1
 
-    def __init__(self, bou: dict):
+
+class TaylorCouette:
+    """One simulation instance resident on the current CUDA device.
+
+    precision: "fp64" (plain path, the drop-in) or "mixed" (FP32 velocities,
+    explicit terms, momentum sweeps and FFTs; FP64 pressure solve, pressure
+    accumulation and reductions)."""
+
+    def __init__(self, bou: dict, precision: str = "fp64"):
         self.L = lib()
         self.bou = dict(bou)
         self._b = Bou.from_dict(bou)
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
         h = ctypes.c_void_p()
-        rc = self.L.tc_create(ctypes.byref(self._b), ctypes.byref(h))
+        rc = self.L.tc_create_ex(ctypes.byref(self._b), PREC_MIXED if precision == "mixed" else PREC_FP64,
+                                 ctypes.byref(h))
         if rc != 0:
             raise TCError(rc, self.L.tc_last_error(None).decode())
         self.h = h

@@ -1,11 +1,13 @@
 // tc_capi.cu -- the C ABI (include/tc_capi.h): handle, device memory, the
-// step sequence and the per-routine entry points.
+// step sequence and the per-routine entry points, for the plain FP64 path
+// and the mixed FP32/FP64 path.
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/tc_capi.h"
@@ -16,15 +18,20 @@ using namespace tcgb;
 
 struct tc_handle {
     tc_bou bou;
+    int mixed = 0;          // 0: plain FP64, 1: mixed FP32/FP64
     Grid g;
     Dims d;
     Consts k;
-    Coef c;
-    Fields f;
-    Plans p;
+    Coef c;                 // FP64 coefficients (pressure, reductions, factors)
+    CoefT<float> cf;        // FP32 copies (mixed path velocity kernels)
+    FieldsT<double> fd;     // plain path state
+    FieldsT<float> ff;      // mixed path state
+    PlansT<double> pd;
+    PlansT<float> pf;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     double* stage = nullptr;
+    StepState* st = nullptr;        // device
     StepState* st_host = nullptr;   // pinned mirror
     int sub = 0;
     long long bytes = 0;
@@ -82,12 +89,15 @@ bool make_plan(int n, FFTPlan& P) {
     return m == 1;
 }
 
-std::vector<double2> twiddles(int n, int count) {
-    std::vector<double2> w(count);
+// exp(-2 pi i j / n), j = 0..count-1, rounded once into the element type.
+template <typename C2>
+std::vector<C2> twiddles(int n, int count) {
+    std::vector<C2> w(count);
     const long double tpi = 6.283185307179586476925286766559L;
     for (int j = 0; j < count; ++j) {
         long double a = tpi * (long double)j / (long double)n;
-        w[j] = make_double2((double)cosl(a), -(double)sinl(a));
+        w[j].x = (decltype(w[j].x))cosl(a);
+        w[j].y = -(decltype(w[j].y))sinl(a);
     }
     return w;
 }
@@ -130,20 +140,95 @@ void L(tc_handle* h, int cls, int n, Fn fn) {
     if (h->profiling) h->prof_n[cls] += n;
 }
 
+template <typename T> FieldsT<T>& F(tc_handle* h);
+template <> FieldsT<double>& F<double>(tc_handle* h) { return h->fd; }
+template <> FieldsT<float>& F<float>(tc_handle* h) { return h->ff; }
+template <typename T> const CoefT<T>& CF(tc_handle* h);
+template <> const CoefT<double>& CF<double>(tc_handle* h) { return h->c; }
+template <> const CoefT<float>& CF<float>(tc_handle* h) { return h->cf; }
+template <typename T> const PlansT<T>& PL(tc_handle* h);
+template <> const PlansT<double>& PL<double>(tc_handle* h) { return h->pd; }
+template <> const PlansT<float>& PL<float>(tc_handle* h) { return h->pf; }
+
+// Allocate the velocity-side state of element type T.
+template <typename T>
+cudaError_t alloc_fields(tc_handle* h, FieldsT<T>& f) {
+    const Dims& d = h->d;
+    const int nr = d.nr, nrr = nr + 1;
+    const size_t cells = (size_t)d.P * nr, faces = (size_t)d.P * nrr;
+    cudaError_t ce = cudaSuccess;
+#define AL(ptr, n) if (ce == cudaSuccess) ce = dalloc(h, &(ptr), (n))
+    AL(f.qt, cells); AL(f.qr, faces); AL(f.qz, cells); AL(f.pr, cells); AL(f.phi, cells);
+    AL(f.ru1, cells); AL(f.ru2, faces); AL(f.ru3, cells);
+    AL(f.rhs_t, cells); AL(f.rhs_r, faces); AL(f.rhs_z, cells);
+    AL(f.spec, (size_t)d.PS * nr);
+    AL(f.F.base, MomFactorsT<T>::count(nrr));
+    f.F.stride = nrr;
+    AL(f.corr, (size_t)9 * nrr);
+    AL(f.scal, 8);
+    AL(f.red, (size_t)6 * reduction_blocks());
+    if (std::is_same<T, double>::value) {
+        f.Fd.base = reinterpret_cast<double*>(f.F.base);
+        f.Fd.stride = nrr;
+        f.corrd = reinterpret_cast<double*>(f.corr);
+        f.ws = nullptr;
+    } else {
+        AL(f.Fd.base, MomFactorsT<double>::count(nrr));
+        f.Fd.stride = nrr;
+        AL(f.corrd, (size_t)9 * nrr);
+        AL(f.ws, (size_t)d.PS * nr);
+    }
+#undef AL
+    return ce;
+}
+
+template <typename T>
+cudaError_t upload_plans(tc_handle* h, PlansT<T>& p) {
+    typedef typename V2<T>::type C2;
+    const Dims& d = h->d;
+    std::vector<C2> wt = twiddles<C2>(d.M, d.M), wz = twiddles<C2>(d.nz, d.nz), wr = twiddles<C2>(d.nt, d.M + 1);
+    C2 *dwt = nullptr, *dwz = nullptr, *dwr = nullptr;
+    cudaError_t ce = dalloc(h, &dwt, wt.size());
+    if (ce == cudaSuccess) ce = dalloc(h, &dwz, wz.size());
+    if (ce == cudaSuccess) ce = dalloc(h, &dwr, wr.size());
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwt, wt.data(), wt.size() * sizeof(C2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwz, wz.data(), wz.size() * sizeof(C2), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dwr, wr.data(), wr.size() * sizeof(C2), cudaMemcpyHostToDevice);
+    p.tw_th = dwt; p.tw_z = dwz; p.twr = dwr;
+    return ce;
+}
+
+template <typename T>
+void set_coef_ptrs(CoefT<T>& c, const T* base, int lenK) {
+    const T** cp[] = {&c.usrm, &c.usrc, &c.udx2rm, &c.udx1vis1, &c.udxt_m, &c.udxtq_m,
+                      &c.rc, &c.udx2c, &c.udx1vis2, &c.udxt_c, &c.udxtq_c,
+                      &c.ap1j, &c.ac1j, &c.am1j, &c.ap2je, &c.ac2je, &c.am2je,
+                      &c.ap3j, &c.ac3j, &c.am3j, &c.ap2j, &c.ac2j, &c.am2j,
+                      &c.udx2m, &c.rudx2c, &c.udx1qm, &c.apph, &c.acph, &c.amph,
+                      &c.usrm2, &c.q_udx2rm, &c.q_usrm, &c.h_udx1vis1, &c.q_udx2c,
+                      &c.q_rc_romeg};
+    for (int a = 0; a < kCoefArrays; ++a) *cp[a] = base + (size_t)a * lenK;
+    c.ak1 = base + (size_t)kCoefArrays * lenK;
+    c.ak3 = base + (size_t)(kCoefArrays + 1) * lenK;
+}
+
 }  // namespace
 
-extern "C" {
+// The exported functions below are declared extern "C" in tc_capi.h, which
+// gives these definitions C linkage.
 
 const char* tc_last_error(const tc_handle* h) {
     if (h) return h->err.c_str();
     return g_last_error.c_str();
 }
 
-int tc_create(const tc_bou* cfg, tc_handle** out) {
+int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     if (!cfg || !out) return fail(nullptr, 2000, "null argument");
+    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED) return fail(nullptr, 2007, "unknown precision");
     *out = nullptr;
     tc_handle* h = new tc_handle();
     h->bou = *cfg;
+    h->mixed = precision == TC_PREC_MIXED;
     std::string e = build_grid(*cfg, h->g);
     if (!e.empty()) { int r = fail(nullptr, 2003, e); delete h; return r; }
     int dev = 0;
@@ -173,6 +258,7 @@ int tc_create(const tc_bou* cfg, tc_handle** out) {
     time_march_scheme(cfg->nsst, k.gam, k.rom, k.alm);
     k.udxz = g.dxz * 0.25;
     k.udxzq = g.dxzq / cfg->ren;
+    k.q_romeg = 0.25 * cfg->romeg;
     for (int s = 0; s < 3; ++s) {
         k.alre[s] = k.alm[s] / cfg->ren;
         k.dxz_al[s] = g.dxz * k.alm[s];
@@ -183,17 +269,17 @@ int tc_create(const tc_bou* cfg, tc_handle** out) {
     k.minstrt = cfg->minstrt; k.minstrz = cfg->minstrz; k.multmin = cfg->multmin;
     k.patterned = (cfg->minstrt * cfg->multmin + cfg->minstrz * cfg->multmin) != 0;
 
-    // 1-D coefficient arrays, each padded to nrr entries
+    // 1-D coefficient arrays, each padded to lenK entries
     std::vector<const std::vector<double>*> src = {
         &g.usrm, &g.usrc, &g.udx2rm, &g.udx1vis1, nullptr, nullptr,
         &g.rc, &g.udx2c, &g.udx1vis2, nullptr, nullptr,
         &g.ap1j, &g.ac1j, &g.am1j, &g.ap2je, &g.ac2je, &g.am2je, &g.ap3j, &g.ac3j, &g.am3j,
         &g.ap2j, &g.ac2j, &g.am2j,
-        &g.udx2m, &g.rudx2c, &g.udx1qm, &g.apph, &g.acph, &g.amph, nullptr};
-    const int ncoef = (int)src.size();
+        &g.udx2m, &g.rudx2c, &g.udx1qm, &g.apph, &g.acph, &g.amph, nullptr,
+        nullptr, nullptr, nullptr, nullptr, nullptr};
     const int lenK = std::max(std::max(nrr, d.nt), d.nz) + 1;
-    std::vector<double> host((size_t)(ncoef + 2) * lenK, 0.0);
-    for (int a = 0; a < ncoef; ++a) {
+    std::vector<double> host((size_t)(kCoefArrays + 2) * lenK, 0.0);
+    for (int a = 0; a < kCoefArrays; ++a) {
         double* dst = host.data() + (size_t)a * lenK;
         if (src[a]) for (size_t m = 0; m < src[a]->size(); ++m) dst[m] = (*src[a])[m];
     }
@@ -204,73 +290,71 @@ int tc_create(const tc_bou* cfg, tc_handle** out) {
         host[(size_t)9 * lenK + m] = g.dxt * 0.25 * g.usrc[m];                             // udxt_c
         host[(size_t)10 * lenK + m] = g.dxtq / (cfg->ren * (rc * rc));                      // udxtq_c
         host[(size_t)29 * lenK + m] = g.usrm[m] * g.usrm[m];                                // usrm2
+        host[(size_t)30 * lenK + m] = 0.25 * g.udx2rm[m];
+        host[(size_t)31 * lenK + m] = 0.25 * g.usrm[m];
+        host[(size_t)32 * lenK + m] = 0.5 * g.udx1vis1[m];
+        host[(size_t)33 * lenK + m] = 0.25 * g.udx2c[m];
+        host[(size_t)34 * lenK + m] = 0.25 * g.rc[m] * cfg->romeg;
     }
-    for (int i = 0; i < d.nt; ++i) host[(size_t)ncoef * lenK + i] = g.ak1[i];
-    for (int j = 0; j < d.nz; ++j) host[(size_t)(ncoef + 1) * lenK + j] = g.ak3[j];
+    for (int i = 0; i < d.nt; ++i) host[(size_t)kCoefArrays * lenK + i] = g.ak1[i];
+    for (int j = 0; j < d.nz; ++j) host[(size_t)(kCoefArrays + 1) * lenK + j] = g.ak3[j];
     double* dcoef = nullptr;
     ce = dalloc(h, &dcoef, host.size());
     if (ce == cudaSuccess) ce = cudaMemcpy(dcoef, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "coefficient upload"); tc_destroy(h); return r; }
-    const double** cp[] = {&h->c.usrm, &h->c.usrc, &h->c.udx2rm, &h->c.udx1vis1, &h->c.udxt_m, &h->c.udxtq_m,
-                           &h->c.rc, &h->c.udx2c, &h->c.udx1vis2, &h->c.udxt_c, &h->c.udxtq_c,
-                           &h->c.ap1j, &h->c.ac1j, &h->c.am1j, &h->c.ap2je, &h->c.ac2je, &h->c.am2je,
-                           &h->c.ap3j, &h->c.ac3j, &h->c.am3j, &h->c.ap2j, &h->c.ac2j, &h->c.am2j,
-                           &h->c.udx2m, &h->c.rudx2c, &h->c.udx1qm, &h->c.apph, &h->c.acph, &h->c.amph,
-                           &h->c.usrm2};
-    for (int a = 0; a < ncoef; ++a) *cp[a] = dcoef + (size_t)a * lenK;
-    h->c.ak1 = dcoef + (size_t)ncoef * lenK;
-    h->c.ak3 = dcoef + (size_t)(ncoef + 1) * lenK;
+    set_coef_ptrs(h->c, (const double*)dcoef, lenK);
+    if (h->mixed) {
+        std::vector<float> hostf(host.size());
+        for (size_t m = 0; m < host.size(); ++m) hostf[m] = (float)host[m];
+        float* fcoef = nullptr;
+        ce = dalloc(h, &fcoef, hostf.size());
+        if (ce == cudaSuccess) ce = cudaMemcpy(fcoef, hostf.data(), hostf.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "coefficient upload"); tc_destroy(h); return r; }
+        set_coef_ptrs(h->cf, (const float*)fcoef, lenK);
+    }
 
-    // fields
-    Fields& f = h->f;
-    std::memset(&f, 0, sizeof f);
-    const size_t cells = (size_t)d.P * nr, faces = (size_t)d.P * nrr;
-    ce = cudaSuccess;
-#define AL(ptr, n) if (ce == cudaSuccess) ce = dalloc(h, &(ptr), (n))
-    AL(f.qt, cells); AL(f.qr, faces); AL(f.qz, cells); AL(f.pr, cells); AL(f.phi, cells);
-    AL(f.ru1, cells); AL(f.ru2, faces); AL(f.ru3, cells);
-    AL(f.rhs_t, cells); AL(f.rhs_r, faces); AL(f.rhs_z, cells);
-    AL(f.spec, (size_t)d.PS * nr);
-    double *pl = nullptr, *pd = nullptr;
-    AL(pl, (size_t)d.nzh * d.PH * nr);
-    AL(pd, (size_t)d.nzh * d.PH * nr);
-    f.pf_l = pl; f.pf_dinv = pd;
-    AL(f.icyl, (size_t)d.P);
-    AL(f.st, 1);
-    AL(f.F.base, MomFactors::doubles(nrr));
-    f.F.stride = nrr;
-    AL(f.corr, (size_t)9 * nrr + 8);
-    AL(f.red, (size_t)6 * reduction_blocks());
-    AL(h->stage, (size_t)nrr * (d.nz + 2) * (d.nt + 2));
-#undef AL
+    // state shared by both paths
+    double *pl = nullptr, *pdv = nullptr;
+    signed char* icyl = nullptr;
+    ce = dalloc(h, &pl, (size_t)d.nzh * d.PH * nr);
+    if (ce == cudaSuccess) ce = dalloc(h, &pdv, (size_t)d.nzh * d.PH * nr);
+    if (ce == cudaSuccess) ce = dalloc(h, &icyl, (size_t)d.P);
+    if (ce == cudaSuccess) ce = dalloc(h, &h->st, 1);
+    if (ce == cudaSuccess) ce = dalloc(h, &h->stage, (size_t)nrr * (d.nz + 2) * (d.nt + 2));
+    if (ce == cudaSuccess) ce = cudaMemset(icyl, 1, (size_t)d.P);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "device allocation"); tc_destroy(h); return r; }
-    cudaMemset(f.icyl, 1, (size_t)d.P);
+
+    std::memset(&h->fd, 0, sizeof h->fd);
+    std::memset(&h->ff, 0, sizeof h->ff);
+    if (h->mixed) ce = alloc_fields(h, h->ff);
+    else ce = alloc_fields(h, h->fd);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "device allocation"); tc_destroy(h); return r; }
+    h->fd.pf_l = pl; h->fd.pf_dinv = pdv; h->fd.icyl = icyl; h->fd.st = h->st;
+    h->ff.pf_l = pl; h->ff.pf_dinv = pdv; h->ff.icyl = icyl; h->ff.st = h->st;
 
     // FFT plans and twiddles
-    if (!make_plan(d.M, h->p.th) || !make_plan(d.nz, h->p.z)) {
+    FFTPlan pth, pz;
+    if (!make_plan(d.M, pth) || !make_plan(d.nz, pz)) {
         int r = fail(nullptr, 2003, "FFT length does not factor into 2, 3, 5"); tc_destroy(h); return r;
     }
-    std::vector<double2> wt = twiddles(d.M, d.M), wz = twiddles(d.nz, d.nz), wr = twiddles(d.nt, d.M + 1);
-    double2 *dwt = nullptr, *dwz = nullptr, *dwr = nullptr;
-    ce = dalloc(h, &dwt, wt.size());
-    if (ce == cudaSuccess) ce = dalloc(h, &dwz, wz.size());
-    if (ce == cudaSuccess) ce = dalloc(h, &dwr, wr.size());
-    if (ce == cudaSuccess) ce = cudaMemcpy(dwt, wt.data(), wt.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(dwz, wz.data(), wz.size() * sizeof(double2), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(dwr, wr.data(), wr.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    h->pd.th = pth; h->pd.z = pz; h->pf.th = pth; h->pf.z = pz;
+    ce = h->mixed ? upload_plans(h, h->pf) : upload_plans(h, h->pd);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "twiddle upload"); tc_destroy(h); return r; }
-    h->p.th.tw = dwt; h->p.z.tw = dwz; h->p.twr = dwr;
 
     ce = cudaMallocHost((void**)&h->st_host, sizeof(StepState));
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pinned allocation"); tc_destroy(h); return r; }
     std::memset(h->st_host, 0, sizeof(StepState));
 
-    launch_pressure_factors(h->stream, d, h->c, pl, pd);
+    launch_pressure_factors(h->stream, d, h->c, pl, pdv);
     ce = cudaStreamSynchronize(h->stream);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pressure factors"); tc_destroy(h); return r; }
     *out = h;
     return 0;
 }
+
+int tc_create(const tc_bou* cfg, tc_handle** out) { return tc_create_ex(cfg, TC_PREC_FP64, out); }
+
+int tc_precision(const tc_handle* h) { return h ? (h->mixed ? TC_PREC_MIXED : TC_PREC_FP64) : -1; }
 
 void tc_destroy(tc_handle* h) {
     if (!h) return;
@@ -290,15 +374,17 @@ int tc_set_stream(tc_handle* h, void* s) {
 
 // ---- state transfer --------------------------------------------------------
 
-static int upload(tc_handle* h, const double* src, double* dst, int nk, int halo) {
+template <typename T>
+static int upload(tc_handle* h, const double* src, T* dst, int nk, int halo) {
     const Dims& d = h->d;
     size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
     CK(cudaMemcpyAsync(h->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, h->stream), "H2D copy");
-    L(h, K_LAYOUT, 1, [&] { launch_to_device(h->stream, d, h->stage, dst, nk, halo); });
+    L(h, K_LAYOUT, 1, [&] { launch_to_device(h->stream, d, (const double*)h->stage, dst, nk, halo); });
     return 0;
 }
 
-static int download(tc_handle* h, const double* src, double* dst, int nk, int halo) {
+template <typename T>
+static int download(tc_handle* h, const T* src, double* dst, int nk, int halo) {
     const Dims& d = h->d;
     size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
     L(h, K_LAYOUT, 1, [&] { launch_to_host(h->stream, d, src, h->stage, nk, halo); });
@@ -307,102 +393,122 @@ static int download(tc_handle* h, const double* src, double* dst, int nk, int ha
     return 0;
 }
 
+template <typename T>
+static int set_state_t(tc_handle* h, const double* qt, const double* qr, const double* qz, const double* pr) {
+    const Dims& d = h->d;
+    FieldsT<T>& f = F<T>(h);
+    const size_t cells = (size_t)d.P * d.nr, faces = (size_t)d.P * (d.nr + 1);
+    if (int r = upload(h, qt, f.qt, d.nr, 1)) return r;
+    if (int r = upload(h, qr, f.qr, d.nr + 1, 1)) return r;
+    if (int r = upload(h, qz, f.qz, d.nr, 1)) return r;
+    if (pr) { if (int r = upload(h, pr, f.pr, d.nr, 1)) return r; }
+    else CK(cudaMemsetAsync(f.pr, 0, cells * sizeof(double), h->stream), "memset");
+    CK(cudaMemsetAsync(f.qr, 0, (size_t)d.P * sizeof(T), h->stream), "memset");
+    CK(cudaMemsetAsync(f.qr + (size_t)d.nr * d.P, 0, (size_t)d.P * sizeof(T), h->stream), "memset");
+    CK(cudaMemsetAsync(f.ru1, 0, cells * sizeof(T), h->stream), "memset");
+    CK(cudaMemsetAsync(f.ru2, 0, faces * sizeof(T), h->stream), "memset");
+    CK(cudaMemsetAsync(f.ru3, 0, cells * sizeof(T), h->stream), "memset");
+    CK(cudaStreamSynchronize(h->stream), "set_state sync");
+    return 0;
+}
+
 int tc_set_state(tc_handle* h, const double* qt, const double* qr, const double* qz, const double* pr) {
     if (int r = check(h)) return r;
     if (!qt || !qr || !qz) return fail(h, 2000, "null field");
+    return h->mixed ? set_state_t<float>(h, qt, qr, qz, pr) : set_state_t<double>(h, qt, qr, qz, pr);
+}
+
+template <typename T>
+static int get_state_t(tc_handle* h, double* qt, double* qr, double* qz, double* pr) {
     const Dims& d = h->d;
-    const size_t cells = (size_t)d.P * d.nr, faces = (size_t)d.P * (d.nr + 1);
-    if (int r = upload(h, qt, h->f.qt, d.nr, 1)) return r;
-    if (int r = upload(h, qr, h->f.qr, d.nr + 1, 1)) return r;
-    if (int r = upload(h, qz, h->f.qz, d.nr, 1)) return r;
-    if (pr) { if (int r = upload(h, pr, h->f.pr, d.nr, 1)) return r; }
-    else CK(cudaMemsetAsync(h->f.pr, 0, cells * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(h->f.qr, 0, (size_t)d.P * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(h->f.qr + (size_t)d.nr * d.P, 0, (size_t)d.P * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(h->f.ru1, 0, cells * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(h->f.ru2, 0, faces * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(h->f.ru3, 0, cells * sizeof(double), h->stream), "memset");
-    CK(cudaStreamSynchronize(h->stream), "set_state sync");
+    FieldsT<T>& f = F<T>(h);
+    if (qt) if (int r = download(h, (const T*)f.qt, qt, d.nr, 1)) return r;
+    if (qr) if (int r = download(h, (const T*)f.qr, qr, d.nr + 1, 1)) return r;
+    if (qz) if (int r = download(h, (const T*)f.qz, qz, d.nr, 1)) return r;
+    if (pr) if (int r = download(h, (const double*)f.pr, pr, d.nr, 1)) return r;
     return 0;
 }
 
 int tc_get_state(tc_handle* h, double* qt, double* qr, double* qz, double* pr) {
     if (int r = check(h)) return r;
-    const Dims& d = h->d;
-    if (qt) if (int r = download(h, h->f.qt, qt, d.nr, 1)) return r;
-    if (qr) if (int r = download(h, h->f.qr, qr, d.nr + 1, 1)) return r;
-    if (qz) if (int r = download(h, h->f.qz, qz, d.nr, 1)) return r;
-    if (pr) if (int r = download(h, h->f.pr, pr, d.nr, 1)) return r;
-    return 0;
+    return h->mixed ? get_state_t<float>(h, qt, qr, qz, pr) : get_state_t<double>(h, qt, qr, qz, pr);
 }
 
-static int field_ptr(tc_handle* h, int which, double** p, int* nk, int* halo) {
+template <typename T>
+static int field_io(tc_handle* h, int which, double* out, const double* in) {
     const Dims& d = h->d;
-    Fields& f = h->f;
-    *halo = which <= TC_F_DPH ? 1 : 0;
+    FieldsT<T>& f = F<T>(h);
+    int halo = which <= TC_F_DPH ? 1 : 0, nk = d.nr;
+    T* p = nullptr;
+    double* pp = nullptr;
     switch (which) {
-        case TC_F_QT: *p = f.qt; *nk = d.nr; break;
-        case TC_F_QR: *p = f.qr; *nk = d.nr + 1; break;
-        case TC_F_QZ: *p = f.qz; *nk = d.nr; break;
-        case TC_F_PR: *p = f.pr; *nk = d.nr; break;
-        case TC_F_DPH: *p = f.phi; *nk = d.nr; break;
-        case TC_F_RHS_T: *p = f.rhs_t; *nk = d.nr; break;
-        case TC_F_RHS_R: *p = f.rhs_r; *nk = d.nr + 1; break;
-        case TC_F_RHS_Z: *p = f.rhs_z; *nk = d.nr; break;
-        case TC_F_RU1: *p = f.ru1; *nk = d.nr; break;
-        case TC_F_RU2: *p = f.ru2; *nk = d.nr + 1; break;
-        case TC_F_RU3: *p = f.ru3; *nk = d.nr; break;
-        case TC_F_DQ: *p = f.h_t; *nk = d.nr; break;
-        case TC_F_HR: *p = f.h_r; *nk = d.nr + 1; break;
-        case TC_F_QCAP: *p = f.h_z; *nk = d.nr; break;
+        case TC_F_QT: p = f.qt; break;
+        case TC_F_QR: p = f.qr; nk = d.nr + 1; break;
+        case TC_F_QZ: p = f.qz; break;
+        case TC_F_PR: pp = f.pr; break;
+        case TC_F_DPH: p = f.phi; break;
+        case TC_F_RHS_T: p = f.rhs_t; break;
+        case TC_F_RHS_R: p = f.rhs_r; nk = d.nr + 1; break;
+        case TC_F_RHS_Z: p = f.rhs_z; break;
+        case TC_F_RU1: p = f.ru1; break;
+        case TC_F_RU2: p = f.ru2; nk = d.nr + 1; break;
+        case TC_F_RU3: p = f.ru3; break;
+        case TC_F_DQ: p = f.h_t; break;
+        case TC_F_HR: p = f.h_r; nk = d.nr + 1; break;
+        case TC_F_QCAP: p = f.h_z; break;
         default: return fail(h, 2004, "unknown field id");
     }
-    if (!*p) return fail(h, 2005, "field not allocated (call tc_explicit_terms first)");
+    if (!p && !pp) return fail(h, 2005, "field not allocated (call tc_explicit_terms first)");
+    if (out) return pp ? download(h, (const double*)pp, out, nk, halo) : download(h, (const T*)p, out, nk, halo);
+    int r = pp ? upload(h, in, pp, nk, halo) : upload(h, in, p, nk, halo);
+    if (r) return r;
+    CK(cudaStreamSynchronize(h->stream), "set_field sync");
     return 0;
 }
 
 int tc_get_field(tc_handle* h, int which, double* out) {
     if (int r = check(h)) return r;
-    double* p; int nk, halo;
-    if (int r = field_ptr(h, which, &p, &nk, &halo)) return r;
-    return download(h, p, out, nk, halo);
+    if (!out) return fail(h, 2000, "null output");
+    return h->mixed ? field_io<float>(h, which, out, nullptr) : field_io<double>(h, which, out, nullptr);
 }
 
 int tc_set_field(tc_handle* h, int which, const double* in) {
     if (int r = check(h)) return r;
-    double* p; int nk, halo;
-    if (int r = field_ptr(h, which, &p, &nk, &halo)) return r;
-    if (int r = upload(h, in, p, nk, halo)) return r;
-    CK(cudaStreamSynchronize(h->stream), "set_field sync");
-    return 0;
+    if (!in) return fail(h, 2000, "null input");
+    return h->mixed ? field_io<float>(h, which, nullptr, in) : field_io<double>(h, which, nullptr, in);
 }
 
 // ---- the step ----------------------------------------------------------------
 
+template <typename T>
 static void enqueue_substeps(tc_handle* h) {
     cudaStream_t s = h->stream;
+    const FieldsT<T>& f = F<T>(h);
+    const CoefT<T>& cv = CF<T>(h);
+    const PlansT<T>& p = PL<T>(h);
     for (int sub = 0; sub < h->k.nsst; ++sub) {
-        L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_FUSED, h->d, h->c, h->k, h->f, sub); });
-        L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, h->f, sub); });
-        L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, h->c, h->k, h->f, h->p, sub, false); });
-        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, false); });
-        L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, h->f); });
-        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, true); });
-        L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, h->f, h->p); });
-        L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, h->f, sub, true, true); });
+        L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_FUSED, h->d, cv, h->k, f, sub); });
+        L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub); });
+        L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, cv, h->k, f, p, sub, false); });
+        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, f, p, false); });
+        L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, f); });
+        L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, f, p, true); });
+        L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, f, p); });
+        L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, true, true); });
     }
 }
 
+template <typename T>
 static void enqueue_begin(tc_handle* h, int mode, double dt, double time) {
-    L(h, K_CONTROL, 1, [&] { launch_begin_step(h->stream, h->k, h->f.st, mode, dt, time); });
-    if (h->k.patterned) L(h, K_CONTROL, 1, [&] { launch_slip(h->stream, h->d, h->k, h->f); });
-    L(h, K_CONTROL, 1, [&] { launch_factors(h->stream, h->d, h->c, h->k, h->f); });
+    L(h, K_CONTROL, 1, [&] { launch_begin_step(h->stream, h->k, h->st, mode, dt, time); });
+    if (h->k.patterned) L(h, K_CONTROL, 1, [&] { launch_slip(h->stream, h->d, h->k, F<T>(h)); });
+    L(h, K_CONTROL, 1, [&] { launch_factors(h->stream, h->d, h->c, h->k, F<T>(h)); });
 }
 
 int tc_time_marcher(tc_handle* h, double dt, double time) {
     if (int r = check(h)) return r;
-    enqueue_begin(h, 0, dt, time);
-    enqueue_substeps(h);
+    if (h->mixed) { enqueue_begin<float>(h, 0, dt, time); enqueue_substeps<float>(h); }
+    else { enqueue_begin<double>(h, 0, dt, time); enqueue_substeps<double>(h); }
     CK(cudaGetLastError(), "tc_time_marcher launch");
     return 0;
 }
@@ -424,29 +530,34 @@ __global__ void set_clock_kernel(StepState* st, int ntime, double time) {
 }  // namespace
 
 static int read_state(tc_handle* h) {
-    CK(cudaMemcpyAsync(h->st_host, h->f.st, sizeof(StepState), cudaMemcpyDeviceToHost, h->stream), "state read");
+    CK(cudaMemcpyAsync(h->st_host, h->st, sizeof(StepState), cudaMemcpyDeviceToHost, h->stream), "state read");
     CK(cudaStreamSynchronize(h->stream), "state sync");
     return 0;
+}
+
+template <typename T>
+static void enqueue_run(tc_handle* h, int nsteps, int nt0, double t0) {
+    cudaStream_t s = h->stream;
+    const FieldsT<T>& f = F<T>(h);
+    L(h, K_CONTROL, 1, [&] { set_clock_kernel<<<1, 1, 0, s>>>(h->st, nt0, t0); });
+    for (int n = 0; n < nsteps; ++n) {
+        L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, f); });
+        enqueue_begin<T>(h, 1, 0.0, 0.0);
+        enqueue_substeps<T>(h);
+        L(h, K_CONTROL, 1, [&] { launch_end_step(s, h->k, h->st); });
+        L(h, K_REDUCE, 4, [&] {
+            launch_velocity_stats(s, h->d, h->c, h->k, f, true);
+            launch_check_divergence(s, h->d, h->c, h->k, f, true);
+        });
+        L(h, K_CONTROL, 1, [&] { launch_finish_step(s, h->k, h->st); });
+    }
 }
 
 int tc_run(tc_handle* h, int nsteps, int* ntime, double* time, double* dt) {
     if (int r = check(h)) return r;
     if (!ntime || !time || !dt) return fail(h, 2000, "null argument");
-    cudaStream_t s = h->stream;
-    const int nt0 = *ntime;
-    const double t0 = *time;
-    L(h, K_CONTROL, 1, [&] { set_clock_kernel<<<1, 1, 0, s>>>(h->f.st, nt0, t0); });
-    for (int n = 0; n < nsteps; ++n) {
-        L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, h->f); });
-        enqueue_begin(h, 1, 0.0, 0.0);
-        enqueue_substeps(h);
-        L(h, K_CONTROL, 1, [&] { launch_end_step(s, h->k, h->f.st); });
-        L(h, K_REDUCE, 4, [&] {
-            launch_velocity_stats(s, h->d, h->c, h->k, h->f, true);
-            launch_check_divergence(s, h->d, h->c, h->k, h->f, true);
-        });
-        L(h, K_CONTROL, 1, [&] { launch_finish_step(s, h->k, h->f.st); });
-    }
+    if (h->mixed) enqueue_run<float>(h, nsteps, *ntime, *time);
+    else enqueue_run<double>(h, nsteps, *ntime, *time);
     CK(cudaGetLastError(), "tc_run launch");
     if (int r = read_state(h)) return r;
     *ntime = h->st_host->ntime;
@@ -459,7 +570,8 @@ int tc_run(tc_handle* h, int nsteps, int* ntime, double* time, double* dt) {
 
 int tc_begin_step(tc_handle* h, double dt, double time) {
     if (int r = check(h)) return r;
-    enqueue_begin(h, 0, dt, time);
+    if (h->mixed) enqueue_begin<float>(h, 0, dt, time);
+    else enqueue_begin<double>(h, 0, dt, time);
     h->sub = 0;
     return 0;
 }
@@ -471,103 +583,118 @@ int tc_set_substep(tc_handle* h, int ns) {
     return 0;
 }
 
+template <typename T>
 static int ensure_h(tc_handle* h) {
     const Dims& d = h->d;
+    FieldsT<T>& f = F<T>(h);
     cudaError_t ce = cudaSuccess;
-    if (!h->f.h_t) ce = dalloc(h, &h->f.h_t, (size_t)d.P * d.nr);
-    if (ce == cudaSuccess && !h->f.h_r) ce = dalloc(h, &h->f.h_r, (size_t)d.P * (d.nr + 1));
-    if (ce == cudaSuccess && !h->f.h_z) ce = dalloc(h, &h->f.h_z, (size_t)d.P * d.nr);
+    if (!f.h_t) ce = dalloc(h, &f.h_t, (size_t)d.P * d.nr);
+    if (ce == cudaSuccess && !f.h_r) ce = dalloc(h, &f.h_r, (size_t)d.P * (d.nr + 1));
+    if (ce == cudaSuccess && !f.h_z) ce = dalloc(h, &f.h_z, (size_t)d.P * d.nr);
     if (ce != cudaSuccess) return cuda_fail(h, ce, "explicit-term arrays");
     return 0;
 }
 
-int tc_explicit_terms(tc_handle* h) {
-    if (int r = check(h)) return r;
-    if (int r = ensure_h(h)) return r;
-    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_EXPLICIT, h->d, h->c, h->k, h->f, h->sub); });
-    return 0;
-}
-
-int tc_implicit_and_update(tc_handle* h) {
-    if (int r = check(h)) return r;
-    if (int r = ensure_h(h)) return r;
-    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_IMPLICIT, h->d, h->c, h->k, h->f, h->sub); });
-    L(h, K_RADIAL, 1, [&] { launch_radial_solve(h->stream, h->d, h->f, h->sub); });
-    return 0;
-}
-
-int tc_explicit_and_rhs(tc_handle* h) {
-    if (int r = check(h)) return r;
-    L(h, K_MOMENTUM, 1, [&] { launch_momentum(h->stream, MODE_FUSED, h->d, h->c, h->k, h->f, h->sub); });
-    return 0;
-}
-
-int tc_solve_imp_eqn_update(tc_handle* h) {
-    if (int r = check(h)) return r;
-    L(h, K_RADIAL, 1, [&] { launch_radial_solve(h->stream, h->d, h->f, h->sub); });
-    return 0;
-}
-
-int tc_calc_local_divergence(tc_handle* h) {
-    if (int r = check(h)) return r;
-    L(h, K_DIVFFT, 1, [&] { launch_divergence(h->stream, h->d, h->c, h->k, h->f, h->sub); });
-    return 0;
-}
-
-int tc_solve_pressure_correction(tc_handle* h) {
-    if (int r = check(h)) return r;
+template <typename T>
+static int routine(tc_handle* h, int which) {
     cudaStream_t s = h->stream;
-    L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, h->c, h->k, h->f, h->p, h->sub, true); });
-    L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, false); });
-    L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, h->f); });
-    L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, h->f, h->p, true); });
-    L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, h->f, h->p); });
+    if (which <= 1) {
+        if (int r = ensure_h<T>(h)) return r;
+    }
+    const FieldsT<T>& f = F<T>(h);
+    const CoefT<T>& cv = CF<T>(h);
+    const PlansT<T>& p = PL<T>(h);
+    const int sub = h->sub;
+    switch (which) {
+        case 0:  // ExplicitTermsQT/QR/QZ
+            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_EXPLICIT, h->d, cv, h->k, f, sub); });
+            break;
+        case 1:  // ImplicitAndUpdateQ* with SolveImpEqnUpdate_Q*
+            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_IMPLICIT, h->d, cv, h->k, f, sub); });
+            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub); });
+            break;
+        case 2:
+            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_FUSED, h->d, cv, h->k, f, sub); });
+            break;
+        case 3:
+            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub); });
+            break;
+        case 4:
+            L(h, K_DIVFFT, 1, [&] { launch_divergence(s, h->d, cv, h->k, f, sub); });
+            break;
+        case 5:
+            L(h, K_DIVFFT, 1, [&] { launch_div_fft(s, h->d, cv, h->k, f, p, sub, true); });
+            L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, f, p, false); });
+            L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, f); });
+            L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, f, p, true); });
+            L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, f, p); });
+            break;
+        case 6:
+            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, true, false); });
+            break;
+        default:
+            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, false, true); });
+            break;
+    }
     return 0;
 }
 
-int tc_correct_velocity(tc_handle* h) {
+static int run_routine(tc_handle* h, int which) {
     if (int r = check(h)) return r;
-    L(h, K_CORRECT, 1, [&] { launch_correct(h->stream, h->d, h->c, h->k, h->f, h->sub, true, false); });
-    return 0;
+    return h->mixed ? routine<float>(h, which) : routine<double>(h, which);
 }
 
-int tc_correct_pressure(tc_handle* h) {
-    if (int r = check(h)) return r;
-    L(h, K_CORRECT, 1, [&] { launch_correct(h->stream, h->d, h->c, h->k, h->f, h->sub, false, true); });
-    return 0;
-}
+int tc_explicit_terms(tc_handle* h) { return run_routine(h, 0); }
+int tc_implicit_and_update(tc_handle* h) { return run_routine(h, 1); }
+int tc_explicit_and_rhs(tc_handle* h) { return run_routine(h, 2); }
+int tc_solve_imp_eqn_update(tc_handle* h) { return run_routine(h, 3); }
+int tc_calc_local_divergence(tc_handle* h) { return run_routine(h, 4); }
+int tc_solve_pressure_correction(tc_handle* h) { return run_routine(h, 5); }
+int tc_correct_velocity(tc_handle* h) { return run_routine(h, 6); }
+int tc_correct_pressure(tc_handle* h) { return run_routine(h, 7); }
 
 // ---- reductions ---------------------------------------------------------------
 
-int tc_calc_max_cfl(tc_handle* h, double* cflm) {
+template <typename T>
+static void enqueue_reduce(tc_handle* h, int which) {
+    cudaStream_t s = h->stream;
+    const FieldsT<T>& f = F<T>(h);
+    switch (which) {
+        case 0: L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, f); }); break;
+        case 1: L(h, K_REDUCE, 2, [&] { launch_check_divergence(s, h->d, h->c, h->k, f, false); }); break;
+        case 2: L(h, K_REDUCE, 2, [&] { launch_torque(s, h->d, h->c, h->k, f); }); break;
+        default: L(h, K_REDUCE, 2, [&] { launch_velocity_stats(s, h->d, h->c, h->k, f, false); }); break;
+    }
+}
+
+static int reduce(tc_handle* h, int which) {
     if (int r = check(h)) return r;
-    L(h, K_REDUCE, 2, [&] { launch_cfl(h->stream, h->d, h->c, h->k, h->f); });
-    if (int r = read_state(h)) return r;
+    if (h->mixed) enqueue_reduce<float>(h, which);
+    else enqueue_reduce<double>(h, which);
+    return read_state(h);
+}
+
+int tc_calc_max_cfl(tc_handle* h, double* cflm) {
+    if (int r = reduce(h, 0)) return r;
     if (cflm) *cflm = h->st_host->instcfl;
     return 0;
 }
 
 int tc_check_divergence(tc_handle* h, double* qmax) {
-    if (int r = check(h)) return r;
-    L(h, K_REDUCE, 2, [&] { launch_check_divergence(h->stream, h->d, h->c, h->k, h->f, false); });
-    if (int r = read_state(h)) return r;
+    if (int r = reduce(h, 1)) return r;
     if (qmax) *qmax = h->st_host->dmax;
     return 0;
 }
 
 int tc_calc_torque(tc_handle* h, double* inner, double* outer) {
-    if (int r = check(h)) return r;
-    L(h, K_REDUCE, 2, [&] { launch_torque(h->stream, h->d, h->c, h->k, h->f); });
-    if (int r = read_state(h)) return r;
+    if (int r = reduce(h, 2)) return r;
     if (inner) *inner = h->st_host->torque[0];
     if (outer) *outer = h->st_host->torque[1];
     return 0;
 }
 
 int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3) {
-    if (int r = check(h)) return r;
-    L(h, K_REDUCE, 2, [&] { launch_velocity_stats(h->stream, h->d, h->c, h->k, h->f, false); });
-    if (int r = read_state(h)) return r;
+    if (int r = reduce(h, 3)) return r;
     for (int q = 0; q < 3; ++q) {
         if (vmax3) vmax3[q] = h->st_host->vmax[q];
         if (rms3) rms3[q] = h->st_host->rms[q];
@@ -620,5 +747,3 @@ int tc_measure_fp64_peak(tc_handle* h, double* tflops) {
 }
 
 const char* tc_profile_name(int cls) { return (cls >= 0 && cls < K_COUNT) ? kClassNames[cls] : ""; }
-
-}  // extern "C"

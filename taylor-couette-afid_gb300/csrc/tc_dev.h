@@ -8,6 +8,11 @@
 //                                             nrm are the walls, always 0)
 // The pressure spectrum is complex [k][kz][kt] with kt = 0..nthm/2 (the
 // half-spectrum of the real transform along theta) and kz = 0..nzm-1.
+//
+// Precision: the element type T of the velocity-side arrays (q, ru, rhs,
+// explicit terms, phi, spectrum, momentum factors) is double for the plain
+// FP64 path and float for the mixed path.  The pressure pr, the pressure LU
+// factors and the reductions are double in both.
 #pragma once
 
 #include <cstddef>
@@ -17,12 +22,15 @@ namespace tcgb {
 
 constexpr int kMaxStages = 24;
 
+template <typename T> struct V2;
+template <> struct V2<double> { typedef double2 type; };
+template <> struct V2<float> { typedef float2 type; };
+
 // Radix plan of one complex transform length (radices 2, 3, 4, 5).
 struct FFTPlan {
     int n = 0;
     int nstages = 0;
     int radix[kMaxStages] = {0};
-    const double2* tw = nullptr;   // exp(-2 pi i j / n), j = 0..n-1
 };
 
 struct Dims {
@@ -34,14 +42,20 @@ struct Dims {
 };
 
 // 1-D coefficient arrays on the device, 0-based (entry m = reference m+1).
-struct Coef {
-    const double *usrm, *usrc, *udx2rm, *udx1vis1, *udxt_m, *udxtq_m;
-    const double *rc, *udx2c, *udx1vis2, *udxt_c, *udxtq_c;
-    const double *ap1j, *ac1j, *am1j, *ap2je, *ac2je, *am2je, *ap3j, *ac3j, *am3j;
-    const double *ap2j, *ac2j, *am2j;
-    const double *udx2m, *rudx2c, *udx1qm, *apph, *acph, *amph, *usrm2;
-    const double *ak1, *ak3;
+template <typename T>
+struct CoefT {
+    const T *usrm, *usrc, *udx2rm, *udx1vis1, *udxt_m, *udxtq_m;
+    const T *rc, *udx2c, *udx1vis2, *udxt_c, *udxtq_c;
+    const T *ap1j, *ac1j, *am1j, *ap2je, *ac2je, *am2je, *ap3j, *ac3j, *am3j;
+    const T *ap2j, *ac2j, *am2j;
+    const T *udx2m, *rudx2c, *udx1qm, *apph, *acph, *amph, *usrm2;
+    // products with powers of two folded in (exact): 0.25*udx2rm, 0.25*usrm,
+    // 0.5*udx1vis1, 0.25*udx2c; and 0.25*rc*romeg
+    const T *q_udx2rm, *q_usrm, *h_udx1vis1, *q_udx2c, *q_rc_romeg;
+    const T *ak1, *ak3;
 };
+typedef CoefT<double> Coef;
+constexpr int kCoefArrays = 35;   // arrays before ak1, ak3
 
 // Scalars of the configuration (param.F90).
 struct Consts {
@@ -53,6 +67,7 @@ struct Consts {
     double gam[3], rom[3], alm[3];
     // scalars hoisted out of the kernels (host-computed, time independent)
     double udxz, udxzq;          // dxz*0.25 (ExplicitTerms*), dxzq/ren
+    double q_romeg;              // 0.25*romeg
     double alre[3];              // al/ren per substep
     double dxz_al[3], dxt_al[3]; // dxz*al, dxt*al per substep
     double fft_norm;             // 0.5/(nthm*nzm): FFT normalisation and real-unpacking 1/2
@@ -85,15 +100,16 @@ struct StepState {
 //   u    : super-diagonal
 // plus per (s, c) the right-hand-side scale 1/(1 - ac(k) beta al) and, per s,
 // the inner-wall forcing term of qt (SolveImpEqnUpdate_QT.F90:65-67).
-struct MomFactors {
-    double* base;
+template <typename T>
+struct MomFactorsT {
+    T* base;
     int stride;          // nr + 1
-    __host__ __device__ double* l(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 0) * (size_t)stride; }
-    __host__ __device__ double* dinv(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 1) * (size_t)stride; }
-    __host__ __device__ double* u(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 2) * (size_t)stride; }
-    __host__ __device__ double* scale(int s, int c) const { return base + ((((s * 3 + c) * 2 + 0) * 4) + 3) * (size_t)stride; }
-    __host__ __device__ double* extra(int s) const { return base + (size_t)(3 * 3 * 2 * 4) * stride + s; }
-    static size_t doubles(int stride) { return (size_t)(3 * 3 * 2 * 4) * stride + 8; }
+    __host__ __device__ T* l(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 0) * (size_t)stride; }
+    __host__ __device__ T* dinv(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 1) * (size_t)stride; }
+    __host__ __device__ T* u(int s, int c, int v) const { return base + ((((s * 3 + c) * 2 + v) * 4) + 2) * (size_t)stride; }
+    __host__ __device__ T* scale(int s, int c) const { return base + ((((s * 3 + c) * 2 + 0) * 4) + 3) * (size_t)stride; }
+    __host__ __device__ T* extra(int s) const { return base + (size_t)(3 * 3 * 2 * 4) * stride + s; }
+    __host__ __device__ static size_t count(int stride) { return (size_t)(3 * 3 * 2 * 4) * stride + 8; }
 };
 
 }  // namespace tcgb

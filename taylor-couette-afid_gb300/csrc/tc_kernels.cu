@@ -1,20 +1,26 @@
-// tc_kernels.cu -- FP64 kernels of the Taylor-Couette time step for sm_103a.
+// tc_kernels.cu -- kernels of the Taylor-Couette time step for sm_103a.
 //
-// One substep (TimeMarcher.F90:27-54) is six kernels:
+// One substep (TimeMarcher.F90:27-54) is eight kernels:
 //   momentum_kernel      ExplicitTermsQT/QR/QZ fused with the right-hand sides
 //                        and ru updates of ImplicitAndUpdateQT/QR/QZ
 //   radial_solve_kernel  SolveImpEqnUpdate_QT/QR/QZ: LU solves along r, q += dq
 //   div_fft_kernel       CalcLocalDivergence fused with the real FFT along theta
 //   zfft_kernel          complex FFT along z (forward)
-//   ptri_kernel          radial tridiagonal solve per (k_theta, k_z) mode
+//   ptri_kernel          radial tridiagonal solve per (k_theta, k_z) mode (FP64)
 //   zfft_kernel          complex FFT along z (inverse)
 //   theta_inv_kernel     inverse real FFT along theta -> phi
-//   correct_kernel       CorrectVelocity fused with CorrectPressure
+//   correct_kernel       CorrectVelocity fused with CorrectPressure (pr in FP64)
 // The decomp_2d transposes of the reference disappear: every transform works
 // on the [k][j][i] layout in place (theta contiguous, z strided).  Halo
 // exchanges (update_halo) become periodic index wrap.
+//
+// Velocity-side kernels are templates on the element type T: double gives
+// the plain FP64 path, float the mixed path (velocities, explicit terms,
+// momentum sweeps and FFTs in FP32; pressure tridiagonals, pressure
+// accumulation and reductions in FP64).
 
 #include <cstdio>
+#include <type_traits>
 
 #include "tc_fft.cuh"
 #include "tc_kernels.cuh"
@@ -29,7 +35,7 @@ constexpr int kZC = 4;            // lines per z-FFT block
 
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
-__device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
+template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
 
 // --------------------------------------------------------------------------
 // Step control
@@ -67,8 +73,8 @@ __global__ void begin_step_kernel(Consts k, StepState* st, int mode, double dt_h
     }
     st->dt = dt;
     st->time = time;
-    st->beta = dt / k.ren * 0.5;                                   // TimeMarcher.F90:20
-    st->vinner_t = k.sizepert * sin(2.0 * k.pi * k.omegapert * time);          // InnerCylVelocity.F90:15
+    st->beta = dt / k.ren * 0.5;                                                  // TimeMarcher.F90:20
+    st->vinner_t = k.sizepert * sin(2.0 * k.pi * k.omegapert * time);             // InnerCylVelocity.F90:15
     st->dvinner_t = 2.0 * k.pi * k.omegapert * k.sizepert * cos(2.0 * k.pi * k.omegapert * time) * dt;
 }
 
@@ -125,8 +131,12 @@ __global__ void slip_kernel(Dims d, Consts k, StepState* st, signed char* icyl) 
 // Row-scaled momentum matrices of SolveImpEqnUpdate_QT/QR/QZ and their LU
 // factors for every substep of the step (dgttrf without row interchanges:
 // the matrices are diagonally dominant), plus the per-substep correction
-// coefficients of CorrectVelocity.  One block.
-__global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFactors F, double* corr) {
+// coefficients of CorrectVelocity and the CalcLocalDivergence scale.  All in
+// FP64 (Fd, corrd); for the mixed path the results are then rounded into the
+// FP32 copies F, corr.  One block.
+template <typename T>
+__global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFactorsT<double> Fd, double* corrd,
+                               double* scal, MomFactorsT<T> F, T* corr) {
     if (st->halt) return;
     const int nr = d.nr;
     const double beta = st->beta, dt = st->dt;
@@ -149,21 +159,21 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
             else if (row == nr - 1) acr = ac[nr - 1] * foc + acfs1 * (1.0 - foc);
             double ackl_b = 1.0 / (1.0 - acr * betadx);
             int cidx = qt ? 0 : 2;
-            F.l(s, cidx, v)[row] = row > 0 ? -am[row] * betadx * ackl_b : 0.0;        // amkl
-            F.u(s, cidx, v)[row] = row < nr - 1 ? -ap[row] * betadx * ackl_b : 0.0;   // apkl
-            if (v == 0) F.scale(s, cidx)[row] = 1.0 / (1.0 - ac[row] * betadx);
+            Fd.l(s, cidx, v)[row] = row > 0 ? -am[row] * betadx * ackl_b : 0.0;        // amkl
+            Fd.u(s, cidx, v)[row] = row < nr - 1 ? -ap[row] * betadx * ackl_b : 0.0;   // apkl
+            if (v == 0) Fd.scale(s, cidx)[row] = 1.0 / (1.0 - ac[row] * betadx);
         } else {
             // qr faces 1..nr-1; rows 0 and nr are identity rows
             double ackl_b = (row >= 1) ? 1.0 / (1.0 - c.ac2j[row] * betadx) : 1.0;
-            F.l(s, 1, 0)[row] = row >= 1 ? -c.am2j[row] * betadx * ackl_b : 0.0;
-            F.u(s, 1, 0)[row] = row >= 1 ? -c.ap2j[row] * betadx * ackl_b : 0.0;
-            F.scale(s, 1)[row] = ackl_b;
+            Fd.l(s, 1, 0)[row] = row >= 1 ? -c.am2j[row] * betadx * ackl_b : 0.0;
+            Fd.u(s, 1, 0)[row] = row >= 1 ? -c.ap2j[row] * betadx * ackl_b : 0.0;
+            Fd.scale(s, 1)[row] = ackl_b;
         }
         // CorrectVelocity.F90:325-330 coefficients
         if (ch == 0) {
-            corr[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
-            corr[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
-            if (row == 0) corr[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
+            corrd[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
+            corrd[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
+            if (row == 0) corrd[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
         }
     }
     __syncthreads();
@@ -172,9 +182,9 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
         int s = threadIdx.x / 5, ch = threadIdx.x % 5;
         int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
         int v = (ch == 1 || ch == 4) ? 1 : 0;
-        double* l = F.l(s, cidx, v);
-        double* u = F.u(s, cidx, v);
-        double* di = F.dinv(s, cidx, v);
+        double* l = Fd.l(s, cidx, v);
+        double* u = Fd.u(s, cidx, v);
+        double* di = Fd.dinv(s, cidx, v);
         int k0 = (cidx == 1) ? 1 : 0;
         double dp = 1.0;
         di[k0] = 1.0;
@@ -188,11 +198,11 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
     } else if (threadIdx.x >= 32 && threadIdx.x < 32 + nsub) {
         int s = threadIdx.x - 32;
         // SolveImpEqnUpdate_QT.F90:67
-        *F.extra(s) = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
+        *Fd.extra(s) = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
         // CalcLocalDivergence.F90:19 usdt, alone and times the FFT normalisation
         const double usdt = 1.0 / (k.alm[s] * dt);
-        corr[9 * (nr + 1) + s] = usdt * k.fft_norm;
-        corr[9 * (nr + 1) + 3 + s] = usdt;
+        scal[s] = usdt * k.fft_norm;
+        scal[3 + s] = usdt;
     }
     __syncthreads();
     // phase 3: reciprocals of the pivots
@@ -202,8 +212,15 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
         int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
         int v = (ch == 1 || ch == 4) ? 1 : 0;
         if (cidx == 1 && row == 0) continue;
-        double* di = F.dinv(s, cidx, v);
+        double* di = Fd.dinv(s, cidx, v);
         di[row] = 1.0 / di[row];
+    }
+    // phase 4 (mixed path): round the factors into the FP32 copies
+    if (!std::is_same<T, double>::value) {
+        __syncthreads();
+        const int nF = (int)MomFactorsT<T>::count(F.stride), nC = 9 * (nr + 1);
+        for (int t = threadIdx.x; t < nF; t += blockDim.x) F.base[t] = (T)Fd.base[t];
+        for (int t = threadIdx.x; t < nC; t += blockDim.x) corr[t] = (T)corrd[t];
     }
 }
 
@@ -213,95 +230,105 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
 
 struct Stencil {
     int i, j, k, im, ip, jm, jp;
-    size_t P, row;
+    size_t P;
     int nt;
     __device__ size_t at(int kk, int jj, int ii) const { return (size_t)kk * P + (size_t)jj * nt + ii; }
 };
 
+// Scalars of the momentum kernel in the element type T.
+template <typename T>
+struct MomArgs {
+    const T *qt, *qr, *qz;
+    const double* pr;
+    T *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
+    const signed char* icyl;
+    const StepState* st;
+    T al, ga, ro, alre, dxt_al, dxz_al;
+    T udxz, udxzq, q_romeg, virotint, virotext;
+    T ac1j_fs0, am1j_fs0, ap1j_fs1, ac1j_fs1, ac3j_fs0, am3j_fs0, ap3j_fs1, ac3j_fs1;
+    int use_ru;
+};
+
 // ExplicitTermsQT.F90:40-125 at cell (i, j, k)
-__device__ double explicit_qt(const Stencil& S, int nr, const Coef& c, const Consts& K,
-                              const double* qt, const double* qr, const double* qz) {
+template <typename T>
+__device__ T explicit_qt(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
     const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
-    double t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip)), t_im = ld(qt + S.at(k, S.j, S.im));
-    double t_jp = ld(qt + S.at(k, S.jp, S.i)), t_jm = ld(qt + S.at(k, S.jm, S.i));
-    double t_kp = ld(qt + S.at(kpp, S.j, S.i)), t_km = ld(qt + S.at(kmm, S.j, S.i));
-    double r_c = ld(qr + S.at(k, S.j, S.i)), r_im = ld(qr + S.at(k, S.j, S.im));
-    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_pim = ld(qr + S.at(kp, S.j, S.im));
-    double z_c = ld(qz + S.at(k, S.j, S.i)), z_im = ld(qz + S.at(k, S.j, S.im));
-    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
-    const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-    const double usrm = ld(c.usrm + k), usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
-    const double udxz = K.udxz, udxzq = K.udxzq;
-    double h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
-    double h12d = ((r_p + r_pim) * (t_kp + t_c) - (r_c + r_im) * (t_c + t_km)) * 0.25 * ld(c.udx2rm + k);
-    double h12n = t_c * usrm * ((r_p + r_pim) * usrcp + (r_c + r_im) * usrc) * 0.25;
-    double h13 = ((z_jp + z_jpim) * (t_jp + t_c) - (z_c + z_im) * (t_c + t_jm)) * udxz;
-    double d11qt = (t_ip - 2.0 * t_c + t_im) * udxtq;
-    double d22qt = (t_jp - 2.0 * t_c + t_jm) * udxzq;
-    double qre = r_p * usrcp + r_c * usrc;
-    double qrw = r_pim * usrcp + r_im * usrc;
-    double d11qre = (qre - qrw) * ld(c.udx1vis1 + k) * 0.5;
-    double coriol = -((r_c + r_im) * usrc + (r_p + r_pim) * usrcp) * 0.25 * K.romeg;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip)), t_im = ld(qt + S.at(k, S.j, S.im));
+    T t_jp = ld(qt + S.at(k, S.jp, S.i)), t_jm = ld(qt + S.at(k, S.jm, S.i));
+    T t_kp = ld(qt + S.at(kpp, S.j, S.i)), t_km = ld(qt + S.at(kmm, S.j, S.i));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_im = ld(qr + S.at(k, S.j, S.im));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pim = ld(qr + S.at(kp, S.j, S.im));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_im = ld(qz + S.at(k, S.j, S.im));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
+    const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
+    const T two = (T)2.0;
+    T h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
+    const T rp2 = r_p + r_pim, rc2 = r_c + r_im;
+    T h12d = (rp2 * (t_kp + t_c) - rc2 * (t_c + t_km)) * ld(c.q_udx2rm + k);
+    T h12n = t_c * ld(c.q_usrm + k) * (rp2 * usrcp + rc2 * usrc);
+    T h13 = ((z_jp + z_jpim) * (t_jp + t_c) - (z_c + z_im) * (t_c + t_jm)) * A.udxz;
+    T d11qt = (t_ip - two * t_c + t_im) * udxtq;
+    T d22qt = (t_jp - two * t_c + t_jm) * A.udxzq;
+    T qre = r_p * usrcp + r_c * usrc;
+    T qrw = r_pim * usrcp + r_im * usrc;
+    T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
+    T coriol = -(rc2 * usrc + rp2 * usrcp) * A.q_romeg;
     return -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
 }
 
 // ExplicitTermsQR.F90:180-280 at face (i, j, k), 1 <= k <= nr-1
-__device__ double explicit_qr(const Stencil& S, const Coef& c, const Consts& K,
-                              const double* qt, const double* qr, const double* qz) {
+template <typename T>
+__device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
     const int k = S.k, km = k - 1, kp = k + 1;
-    double t_c = ld(qt + S.at(k, S.j, S.i)), t_m = ld(qt + S.at(km, S.j, S.i));
-    double t_ip = ld(qt + S.at(k, S.j, S.ip)), t_mip = ld(qt + S.at(km, S.j, S.ip));
-    double r_c = ld(qr + S.at(k, S.j, S.i)), r_ip = ld(qr + S.at(k, S.j, S.ip)), r_im = ld(qr + S.at(k, S.j, S.im));
-    double r_jp = ld(qr + S.at(k, S.jp, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
-    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_m = ld(qr + S.at(km, S.j, S.i));
-    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_mjp = ld(qz + S.at(km, S.jp, S.i));
-    double z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
-    const double udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
-    const double usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
-    const double udxz = K.udxz, udxzq = K.udxzq;
-    double a = (t_ip + t_mip + t_c + t_m) * 0.25;
-    double h11n = a * a;
-    double h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
-    double h22 = ((r_p * usrcp + r_c * usrc) * (r_p + r_c) - (r_c * usrc + r_m * usrcm) * (r_c + r_m)) * ld(c.udx2c + k) * 0.25;
-    double h23 = ((z_jp + z_mjp) * (r_jp + r_c) - (z_c + z_m) * (r_c + r_jm)) * udxz;
-    double d11qre = -((t_ip + t_mip) - (t_c + t_m)) * ld(c.udx1vis2 + k);
-    double d11qr = (r_ip - 2.0 * r_c + r_im) * udxtq;
-    double d22qr = (r_jp - 2.0 * r_c + r_jm) * udxzq;
-    double coriol = (t_c + t_ip + t_m + t_mip) * 0.25 * ld(c.rc + k) * K.romeg;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_m = ld(qt + S.at(km, S.j, S.i));
+    T t_ip = ld(qt + S.at(k, S.j, S.ip)), t_mip = ld(qt + S.at(km, S.j, S.ip));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_ip = ld(qr + S.at(k, S.j, S.ip)), r_im = ld(qr + S.at(k, S.j, S.im));
+    T r_jp = ld(qr + S.at(k, S.jp, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_m = ld(qr + S.at(km, S.j, S.i));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_mjp = ld(qz + S.at(km, S.jp, S.i));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
+    const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
+    const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
+    const T two = (T)2.0;
+    T a = (t_ip + t_mip + t_c + t_m) * (T)0.25;
+    T h11n = a * a;
+    T h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
+    T h22 = ((r_p * usrcp + r_c * usrc) * (r_p + r_c) - (r_c * usrc + r_m * usrcm) * (r_c + r_m)) * ld(c.q_udx2c + k);
+    T h23 = ((z_jp + z_mjp) * (r_jp + r_c) - (z_c + z_m) * (r_c + r_jm)) * A.udxz;
+    T d11qre = -((t_ip + t_mip) - (t_c + t_m)) * ld(c.udx1vis2 + k);
+    T d11qr = (r_ip - two * r_c + r_im) * udxtq;
+    T d22qr = (r_jp - two * r_c + r_jm) * A.udxzq;
+    T coriol = (t_c + t_ip + t_m + t_mip) * ld(c.q_rc_romeg + k);
     return -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
 }
 
 // ExplicitTermsQZ.F90:328-390 at cell (i, j, k)
-__device__ double explicit_qz(const Stencil& S, int nr, const Coef& c, const Consts& K,
-                              const double* qt, const double* qr, const double* qz) {
+template <typename T>
+__device__ T explicit_qz(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
     const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
-    double t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip));
-    double t_jm = ld(qt + S.at(k, S.jm, S.i)), t_jmip = ld(qt + S.at(k, S.jm, S.ip));
-    double z_c = ld(qz + S.at(k, S.j, S.i)), z_ip = ld(qz + S.at(k, S.j, S.ip)), z_im = ld(qz + S.at(k, S.j, S.im));
-    double z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jm = ld(qz + S.at(k, S.jm, S.i));
-    double z_kp = ld(qz + S.at(kpp, S.j, S.i)), z_km = ld(qz + S.at(kmm, S.j, S.i));
-    double r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
-    double r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
-    const double udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-    const double udxz = K.udxz, udxzq = K.udxzq;
-    double h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
-    double h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.udx2rm + k) * 0.25;
-    double h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * udxz;
-    double dqz1 = (z_im - 2.0 * z_c + z_ip) * udxtq;
-    double dqz2 = (z_jm - 2.0 * z_c + z_jp) * udxzq;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip));
+    T t_jm = ld(qt + S.at(k, S.jm, S.i)), t_jmip = ld(qt + S.at(k, S.jm, S.ip));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_ip = ld(qz + S.at(k, S.j, S.ip)), z_im = ld(qz + S.at(k, S.j, S.im));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jm = ld(qz + S.at(k, S.jm, S.i));
+    T z_kp = ld(qz + S.at(kpp, S.j, S.i)), z_km = ld(qz + S.at(kmm, S.j, S.i));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const T two = (T)2.0;
+    T h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
+    T h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.q_udx2rm + k);
+    T h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * A.udxz;
+    T dqz1 = (z_im - two * z_c + z_ip) * udxtq;
+    T dqz2 = (z_jm - two * z_c + z_jp) * A.udxzq;
     return -(h31 + h32 + h33) + dqz1 + dqz2;
 }
 
-struct MomArgs {
-    const double *qt, *qr, *qz, *pr;
-    double *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
-    const signed char* icyl;
-    const StepState* st;
-    double al, ga, ro, alre, dxt_al, dxz_al;
-};
-
-template <int MODE>
-__global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K, MomArgs a) {
+template <int MODE, typename T>
+__global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
     if (a.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -312,11 +339,11 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
     S.i = i; S.j = j; S.k = k; S.nt = d.nt; S.P = (size_t)d.P;
     S.im = wm(i, d.nt); S.ip = wp(i, d.nt); S.jm = wm(j, d.nz); S.jp = wp(j, d.nz);
     const size_t o = S.at(k, j, i);
-    double ht = 0.0, hr = 0.0, hz = 0.0;
+    T ht = 0, hr = 0, hz = 0;
     if (MODE != MODE_IMPLICIT) {
-        ht = explicit_qt(S, nr, c, K, a.qt, a.qr, a.qz);
-        if (k >= 1) hr = explicit_qr(S, c, K, a.qt, a.qr, a.qz);
-        hz = explicit_qz(S, nr, c, K, a.qt, a.qr, a.qz);
+        ht = explicit_qt(S, nr, c, a);
+        if (k >= 1) hr = explicit_qr(S, c, a);
+        hz = explicit_qz(S, nr, c, a);
         if (MODE == MODE_EXPLICIT) {
             a.h_t[o] = ht;
             if (k >= 1) a.h_r[o] = hr;
@@ -328,67 +355,68 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
         if (k >= 1) hr = a.h_r[o];
         hz = a.h_z[o];
     }
-    const double dt = a.st->dt, ga = a.ga, ro = a.ro, alre = a.alre;
-    const double fic = a.icyl ? (double)a.icyl[(size_t)j * d.nt + i] : 1.0, foc = 1.0;
-    const double* qt = a.qt;
-    const double* qr = a.qr;
-    const double* qz = a.qz;
+    const T dt = (T)a.st->dt, ga = a.ga, ro = a.ro, alre = a.alre;
+    const T one = (T)1.0;
+    const T fic = a.icyl ? (T)a.icyl[(size_t)j * d.nt + i] : one, foc = one;
+    const T* qt = a.qt;
+    const T* qr = a.qr;
+    const T* qz = a.qz;
     const double* pr = a.pr;
     const double p_c = ld(pr + o);
     // ---- qt (ImplicitAndUpdateQT.F90:45-115)
     {
-        double d33;
+        T d33;
         if (k == 0) {
-            double app = ld(c.ap1j);
-            double acc = ld(c.ac1j) * fic + K.ac1j_fs0 * (1.0 - fic);
-            double amm = ld(c.am1j) * fic + K.am1j_fs0 * (1.0 - fic);
-            d33 = ld(qt + S.at(1, j, i)) * app + ld(qt + o) * acc + (K.virotint + a.st->vinner_t) * amm;
+            T app = ld(c.ap1j);
+            T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
+            T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
+            d33 = ld(qt + S.at(1, j, i)) * app + ld(qt + o) * acc + (a.virotint + (T)a.st->vinner_t) * amm;
         } else if (k == nr - 1) {
-            double amm = ld(c.am1j + k);
-            double app = ld(c.ap1j + k) * foc + K.ap1j_fs1 * (1.0 - foc);
-            double acc = ld(c.ac1j + k) * foc + K.ac1j_fs1 * (1.0 - foc);
-            d33 = K.virotext * app + ld(qt + o) * acc + ld(qt + S.at(k - 1, j, i)) * amm;
+            T amm = ld(c.am1j + k);
+            T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
+            T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
+            d33 = a.virotext * app + ld(qt + o) * acc + ld(qt + S.at(k - 1, j, i)) * amm;
         } else {
             d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
                   ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
         }
-        double dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
-        double old = ro != 0.0 ? a.ru1[o] : 0.0;
+        T dpx11 = (T)(p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
+        T old = a.use_ru ? a.ru1[o] : (T)0;
         a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
         a.ru1[o] = ht;
     }
     // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
     if (k >= 1) {
-        double d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
-                     ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
-        double udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
-        double dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
-        double old = ro != 0.0 ? a.ru2[o] : 0.0;
+        T d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
+                ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
+        T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
+        T dpx22 = (T)(p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
+        T old = a.use_ru ? a.ru2[o] : (T)0;
         a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
         a.ru2[o] = hr;
     }
     // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
     {
-        double d33;
+        T d33;
         if (k == 0) {
-            double app = ld(c.ap3j);
-            double acc = ld(c.ac3j) * fic + K.ac3j_fs0 * (1.0 - fic);
-            double amm = ld(c.am3j) * fic + K.am3j_fs0 * (1.0 - fic);
-            double q0 = ld(qz + o);
+            T app = ld(c.ap3j);
+            T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
+            T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
+            T q0 = ld(qz + o);
             d33 = ld(qz + S.at(1, j, i)) * app + q0 * acc + q0 * amm;
         } else if (k == nr - 1) {
-            double app = ld(c.ap3j + k) * foc + K.ap3j_fs1 * (1.0 - foc);
-            double acc = ld(c.ac3j + k) * foc + K.ac3j_fs1 * (1.0 - foc);
-            double q0 = ld(qz + o);
+            T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
+            T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
+            T q0 = ld(qz + o);
             d33 = q0 * app + q0 * acc + ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
         } else {
             d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
                   ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
         }
-        double dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
+        T dpx33 = (T)(p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
-        double old = (k == nr - 1) ? hz : (ro != 0.0 ? a.ru3[o] : 0.0);
+        T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
         a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
         a.ru3[o] = hz;
     }
@@ -398,26 +426,27 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, Coef c, Consts K,
 // Radial implicit solves, one thread per (z, theta) column
 // --------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, Fields f, int sub) {
+template <typename T>
+__global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= d.P) return;
     const int nr = d.nr;
     const size_t P = (size_t)d.P;
     const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
-    const MomFactors& F = f.F;
+    const MomFactorsT<T>& F = f.F;
     // qt: SolveImpEqnUpdate_QT.F90:65-78
     {
-        const double *l = F.l(sub, 0, v), *di = F.dinv(sub, 0, v), *u = F.u(sub, 0, v), *sc = F.scale(sub, 0);
-        double* rhs = f.rhs_t + col;
-        double* q = f.qt + col;
-        double y = (rhs[0] + *F.extra(sub)) * ld(sc);
+        const T *l = F.l(sub, 0, v), *di = F.dinv(sub, 0, v), *u = F.u(sub, 0, v), *sc = F.scale(sub, 0);
+        T* rhs = f.rhs_t + col;
+        T* q = f.qt + col;
+        T y = (rhs[0] + *F.extra(sub)) * ld(sc);
         rhs[0] = y;
         for (int k = 1; k < nr; ++k) {
             y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
             rhs[k * P] = y;
         }
-        double x = y * ld(di + nr - 1);
+        T x = y * ld(di + nr - 1);
         q[(nr - 1) * P] += x;
         for (int k = nr - 2; k >= 0; --k) {
             x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
@@ -426,16 +455,16 @@ __global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, Fields f, int
     }
     // qr: SolveImpEqnUpdate_QR.F90:136-150, faces 1..nr-1
     {
-        const double *l = F.l(sub, 1, 0), *di = F.dinv(sub, 1, 0), *u = F.u(sub, 1, 0), *sc = F.scale(sub, 1);
-        double* rhs = f.rhs_r + col;
-        double* q = f.qr + col;
-        double y = rhs[P] * ld(sc + 1);
+        const T *l = F.l(sub, 1, 0), *di = F.dinv(sub, 1, 0), *u = F.u(sub, 1, 0), *sc = F.scale(sub, 1);
+        T* rhs = f.rhs_r + col;
+        T* q = f.qr + col;
+        T y = rhs[P] * ld(sc + 1);
         rhs[P] = y;
         for (int k = 2; k < nr; ++k) {
             y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
             rhs[k * P] = y;
         }
-        double x = y * ld(di + nr - 1);
+        T x = y * ld(di + nr - 1);
         q[(nr - 1) * P] += x;
         for (int k = nr - 2; k >= 1; --k) {
             x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
@@ -444,16 +473,16 @@ __global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, Fields f, int
     }
     // qz: SolveImpEqnUpdate_QZ.F90:214-224
     {
-        const double *l = F.l(sub, 2, v), *di = F.dinv(sub, 2, v), *u = F.u(sub, 2, v), *sc = F.scale(sub, 2);
-        double* rhs = f.rhs_z + col;
-        double* q = f.qz + col;
-        double y = rhs[0] * ld(sc);
+        const T *l = F.l(sub, 2, v), *di = F.dinv(sub, 2, v), *u = F.u(sub, 2, v), *sc = F.scale(sub, 2);
+        T* rhs = f.rhs_z + col;
+        T* q = f.qz + col;
+        T y = rhs[0] * ld(sc);
         rhs[0] = y;
         for (int k = 1; k < nr; ++k) {
             y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
             rhs[k * P] = y;
         }
-        double x = y * ld(di + nr - 1);
+        T x = y * ld(di + nr - 1);
         q[(nr - 1) * P] += x;
         for (int k = nr - 2; k >= 0; --k) {
             x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
@@ -467,58 +496,64 @@ __global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, Fields f, int
 // (row = k*nzm + j) of nthm reals packed as nthm/2 complex values.
 // --------------------------------------------------------------------------
 
+__device__ __forceinline__ double2 ld2(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }
+__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+
 // CalcLocalDivergence.F90:27-40 for cells 2m and 2m+1 of row (k, j).
-__device__ __forceinline__ double2 div_pair(const Dims& d, const Coef& c, const Consts& K,
-                                            const double* qt, const double* qr, const double* qz,
-                                            int k, int j, int m) {
+template <typename T>
+__device__ __forceinline__ typename V2<T>::type div_pair(const Dims& d, const CoefT<T>& c, T dxt, T dxz,
+                                                         const T* qt, const T* qr, const T* qz,
+                                                         int k, int j, int m) {
     const size_t P = (size_t)d.P;
     const int nt = d.nt;
     const size_t row = (size_t)k * P + (size_t)j * nt;
     const int i0 = 2 * m, i2 = (2 * m + 2 == nt) ? 0 : 2 * m + 2;
-    double2 t01 = __ldg(reinterpret_cast<const double2*>(qt + row + i0));
-    double t2 = ld(qt + row + i2);
-    double2 r0 = __ldg(reinterpret_cast<const double2*>(qr + row + i0));
-    double2 r1 = __ldg(reinterpret_cast<const double2*>(qr + row + P + i0));
+    auto t01 = ld2(qt + row + i0);
+    T t2 = ld(qt + row + i2);
+    auto r0 = ld2(qr + row + i0);
+    auto r1 = ld2(qr + row + P + i0);
     const int jp = wp(j, d.nz);
-    double2 z0 = __ldg(reinterpret_cast<const double2*>(qz + row + i0));
-    double2 z1 = __ldg(reinterpret_cast<const double2*>(qz + (size_t)k * P + (size_t)jp * nt + i0));
-    const double udx2m = ld(c.udx2m + k), usrm = ld(c.usrm + k);
-    double a = ((t01.y - t01.x) * K.dxt + (r1.x - r0.x) * udx2m) * usrm + (z1.x - z0.x) * K.dxz;
-    double b = ((t2 - t01.y) * K.dxt + (r1.y - r0.y) * udx2m) * usrm + (z1.y - z0.y) * K.dxz;
-    return make_double2(a, b);
+    auto z0 = ld2(qz + row + i0);
+    auto z1 = ld2(qz + (size_t)k * P + (size_t)jp * nt + i0);
+    const T udx2m = ld(c.udx2m + k), usrm = ld(c.usrm + k);
+    T a = ((t01.y - t01.x) * dxt + (r1.x - r0.x) * udx2m) * usrm + (z1.x - z0.x) * dxz;
+    T b = ((t2 - t01.y) * dxt + (r1.y - r0.y) * udx2m) * usrm + (z1.y - z0.y) * dxz;
+    return mk2(a, b);
 }
 
 // Forward transform of R rows.  FROM_PHI: the rows come from the phi array
 // (CalcLocalDivergence already ran); otherwise the divergence is computed on
 // the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
-template <bool FROM_PHI, int R>
-__global__ void __launch_bounds__(128) div_fft_kernel(Dims d, Coef c, Consts K, Fields f, FFTPlan pl,
-                                                      const double2* twr, int sub) {
+template <bool FROM_PHI, int R, typename T>
+__global__ void __launch_bounds__(128) div_fft_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, FFTPlan pl,
+                                                      const typename V2<T>::type* tw,
+                                                      const typename V2<T>::type* twr, double fft_norm, int sub) {
+    typedef typename V2<T>::type C2;
     if (f.st->halt) return;
-    extern __shared__ double2 smem[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2* smem = reinterpret_cast<C2*>(smem_raw);
     const int M = pl.n;
-    double2* a = smem;
-    double2* b = smem + (size_t)R * M;
+    C2* a = smem;
+    C2* b = smem + (size_t)R * M;
     const long long nrows = (long long)d.nr * d.nz;
     const long long row0 = (long long)blockIdx.x * R;
-    // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in;
-    // the factors kernel stores it per substep behind the correction coefficients
-    const double scl = FROM_PHI ? K.fft_norm : f.corr[9 * (d.nr + 1) + sub];
+    // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in
+    const T scl = (T)(FROM_PHI ? fft_norm : f.scal[sub]);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = t / M, m = t - r * M;
         const long long row = row0 + r;
-        double2 z = make_double2(0.0, 0.0);
+        C2 z = mk2((T)0, (T)0);
         if (row < nrows) {
             const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
-            if (FROM_PHI) z = __ldg(reinterpret_cast<const double2*>(f.phi + (size_t)row * d.nt + 2 * m));
-            else z = div_pair(d, c, K, f.qt, f.qr, f.qz, k, j, m);
+            if (FROM_PHI) z = ld2(f.phi + (size_t)row * d.nt + 2 * m);
+            else z = div_pair(d, c, dxt, dxz, f.qt, f.qr, f.qz, k, j, m);
             z.x *= scl;
             z.y *= scl;
         }
         a[m * R + r] = z;
     }
     __syncthreads();
-    const double2* Z = fft_lines<R>(a, b, pl, false);
+    const C2* Z = fft_lines<R>(a, b, pl, tw, false);
     // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
     const int PH = M + 1;
     for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
@@ -526,41 +561,54 @@ __global__ void __launch_bounds__(128) div_fft_kernel(Dims d, Coef c, Consts K, 
         const long long row = row0 + r;
         if (row >= nrows) continue;
         const int k1 = kt == M ? 0 : kt, k2 = kt == 0 ? 0 : M - kt;
-        double2 zk = Z[k1 * R + r], zc = cconj(Z[k2 * R + r]);
-        double2 e = cadd(zk, zc), o = csub(zk, zc);
-        double2 w = __ldg(twr + kt);
-        double2 wo = cmul(w, o);
+        C2 zk = Z[k1 * R + r], zc = cconj(Z[k2 * R + r]);
+        C2 e = cadd(zk, zc), o = csub(zk, zc);
+        C2 w = __ldg(twr + kt);
+        C2 wo = cmul(w, o);
         // - i * wo = (wo.y, -wo.x)
-        f.spec[(size_t)row * PH + kt] = make_double2(e.x + wo.y, e.y - wo.x);
+        f.spec[(size_t)row * PH + kt] = mk2(e.x + wo.y, e.y - wo.x);
     }
 }
 
 // Complex FFT along z of kZC consecutive kt columns of one r-plane.
-__global__ void __launch_bounds__(128) zfft_kernel(Dims d, Fields f, FFTPlan pl, int inv) {
+template <typename T>
+__global__ void __launch_bounds__(128) zfft_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
+                                                   const typename V2<T>::type* tw, int inv) {
+    typedef typename V2<T>::type C2;
     if (f.st->halt) return;
-    extern __shared__ double2 smem[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2* smem = reinterpret_cast<C2*>(smem_raw);
     const int nz = pl.n, PH = d.PH;
-    double2* a = smem;
-    double2* b = smem + (size_t)kZC * nz;
+    C2* a = smem;
+    C2* b = smem + (size_t)kZC * nz;
     const int kt0 = blockIdx.x * kZC;
-    double2* plane = f.spec + (size_t)blockIdx.y * d.PS;
+    C2* plane = f.spec + (size_t)blockIdx.y * d.PS;
     for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
         const int c = t % kZC, j = t / kZC;
-        a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : make_double2(0.0, 0.0);
+        a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
     }
     __syncthreads();
-    const double2* Z = fft_lines<kZC>(a, b, pl, inv != 0);
+    const C2* Z = fft_lines<kZC>(a, b, pl, tw, inv != 0);
     for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
         const int c = t % kZC, j = t / kZC;
         if (kt0 + c < PH) plane[(size_t)j * PH + kt0 + c] = Z[t];
     }
 }
 
+__device__ __forceinline__ double2 to_d2(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ void st2(double2* p, double x, double y) { *p = make_double2(x, y); }
+__device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_float2((float)x, (float)y); }
+
 // SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
 // matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
-// right-hand side, with the precomputed LU factors.  One thread per pair of
-// modes (kz, nzm-kz) that share a matrix.
-__global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, Fields f) {
+// right-hand side, with the precomputed LU factors, in FP64.  One thread per
+// pair of modes (kz, nzm-kz) that share a matrix.  The forward-sweep partial
+// results go to the FP64 array ws: the spectrum itself for the FP64 path, a
+// separate scratch for the mixed path, so the FP32 spectrum is rounded once.
+template <typename T>
+__global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, FieldsT<T> f, double2* ws) {
+    typedef typename V2<T>::type C2;
     if (f.st->halt) return;
     const int PH = d.PH, nzh = d.nzh, nr = d.nr;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -568,36 +616,41 @@ __global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, Fields f) {
     const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
     const bool two = (kz != 0) && (2 * kz != d.nz);
     const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
-    double2* x1 = f.spec + (size_t)kz * PH + kt;
-    double2* x2 = f.spec + (size_t)(two ? d.nz - kz : kz) * PH + kt;
+    const size_t o1 = (size_t)kz * PH + kt, o2 = (size_t)(two ? d.nz - kz : kz) * PH + kt;
+    C2* x1 = f.spec + o1;
+    C2* x2 = f.spec + o2;
+    double2* w1 = ws + o1;
+    double2* w2 = ws + o2;
     const double* L = f.pf_l + t;
     const double* DI = f.pf_dinv + t;
-    double2 y1 = x1[0], y2 = two ? x2[0] : make_double2(0.0, 0.0);
+    double2 y1 = to_d2(x1[0]), y2 = two ? to_d2(x2[0]) : make_double2(0.0, 0.0);
+    w1[0] = y1;
+    if (two) w2[0] = y2;
     for (int k = 1; k < nr; ++k) {
         const double l = ld(L + k * FS);
-        double2 b1 = x1[k * PS];
+        double2 b1 = to_d2(x1[k * PS]);
         y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
-        x1[k * PS] = y1;
+        w1[k * PS] = y1;
         if (two) {
-            double2 b2 = x2[k * PS];
+            double2 b2 = to_d2(x2[k * PS]);
             y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
-            x2[k * PS] = y2;
+            w2[k * PS] = y2;
         }
     }
     double di = ld(DI + (size_t)(nr - 1) * FS);
     double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
-    x1[(size_t)(nr - 1) * PS] = s1;
-    if (two) x2[(size_t)(nr - 1) * PS] = s2;
+    st2(x1 + (size_t)(nr - 1) * PS, s1.x, s1.y);
+    if (two) st2(x2 + (size_t)(nr - 1) * PS, s2.x, s2.y);
     for (int k = nr - 2; k >= 0; --k) {
         const double u = ld(c.apph + k);
         di = ld(DI + k * FS);
-        double2 b1 = x1[k * PS];
+        double2 b1 = w1[k * PS];
         s1 = make_double2((b1.x - u * s1.x) * di, (b1.y - u * s1.y) * di);
-        x1[k * PS] = s1;
+        st2(x1 + k * PS, s1.x, s1.y);
         if (two) {
-            double2 b2 = x2[k * PS];
+            double2 b2 = w2[k * PS];
             s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
-            x2[k * PS] = s2;
+            st2(x2 + k * PS, s2.x, s2.y);
         }
     }
 }
@@ -627,47 +680,52 @@ __global__ void pfactor_kernel(Dims d, Coef c, double* fl, double* fdi) {
 }
 
 // Inverse real FFT along theta: spec rows -> phi rows.
-template <int R>
-__global__ void __launch_bounds__(128) theta_inv_kernel(Dims d, Fields f, FFTPlan pl, const double2* twr) {
+template <int R, typename T>
+__global__ void __launch_bounds__(128) theta_inv_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
+                                                        const typename V2<T>::type* tw,
+                                                        const typename V2<T>::type* twr) {
+    typedef typename V2<T>::type C2;
     if (f.st->halt) return;
-    extern __shared__ double2 smem[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2* smem = reinterpret_cast<C2*>(smem_raw);
     const int M = pl.n, PH = M + 1;
-    double2* a = smem;
-    double2* b = smem + (size_t)R * M;
+    C2* a = smem;
+    C2* b = smem + (size_t)R * M;
     const long long nrows = (long long)d.nr * d.nz;
     const long long row0 = (long long)blockIdx.x * R;
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = t / M, kt = t - r * M;
         const long long row = row0 + r;
-        double2 z = make_double2(0.0, 0.0);
+        C2 z = mk2((T)0, (T)0);
         if (row < nrows) {
-            const double2* X = f.spec + (size_t)row * PH;
-            double2 xk = X[kt], xm = X[M - kt];
-            if (kt == 0) { xk.y = 0.0; xm.y = 0.0; }   // imaginary parts of the 0 and Nyquist bins
-            double2 xc = cconj(xm);
-            double2 e = cadd(xk, xc), o = csub(xk, xc);
-            double2 w = cconj(__ldg(twr + kt));
-            double2 wo = cmul(w, o);
+            const C2* X = f.spec + (size_t)row * PH;
+            C2 xk = X[kt], xm = X[M - kt];
+            if (kt == 0) { xk.y = 0; xm.y = 0; }   // imaginary parts of the 0 and Nyquist bins
+            C2 xc = cconj(xm);
+            C2 e = cadd(xk, xc), o = csub(xk, xc);
+            C2 w = cconj(__ldg(twr + kt));
+            C2 wo = cmul(w, o);
             // Z = e + i wo
-            z = make_double2(e.x - wo.y, e.y + wo.x);
+            z = mk2(e.x - wo.y, e.y + wo.x);
         }
         a[kt * R + r] = z;
     }
     __syncthreads();
-    const double2* Z = fft_lines<R>(a, b, pl, true);
+    const C2* Z = fft_lines<R>(a, b, pl, tw, true);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = t / M, m = t - r * M;
         const long long row = row0 + r;
-        if (row < nrows) *reinterpret_cast<double2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
+        if (row < nrows) *reinterpret_cast<C2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
     }
 }
 
 // --------------------------------------------------------------------------
-// Projection: CorrectVelocity.F90:318-337 and CorrectPressure.F90:364-390
+// Projection: CorrectVelocity.F90:318-337 (element type T) and
+// CorrectPressure.F90:364-390 (FP64: pr += phi - beta lap(phi))
 // --------------------------------------------------------------------------
 
-template <bool VEL, bool PRES>
-__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, Consts K, Fields f, int sub) {
+template <bool VEL, bool PRES, typename T>
+__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, double dxzq, FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -678,13 +736,13 @@ __global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, Consts K, 
     const int im = wm(i, nt), ip = wp(i, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
     const size_t rowoff = (size_t)j * nt;
     const size_t o = (size_t)k * P + rowoff + i;
-    const double* phi = f.phi;
-    const double loc = ld(phi + o);
-    const double pim = ld(phi + (size_t)k * P + rowoff + im);
-    const double pjm = ld(phi + (size_t)k * P + (size_t)jm * nt + i);
-    const double pkm = ld(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i);
+    const T* phi = f.phi;
+    const T loc = ld(phi + o);
+    const T pim = ld(phi + (size_t)k * P + rowoff + im);
+    const T pjm = ld(phi + (size_t)k * P + (size_t)jm * nt + i);
+    const T pkm = ld(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i);
     if (VEL) {
-        const double* cf = f.corr + (size_t)sub * 3 * (nr + 1);
+        const T* cf = f.corr + (size_t)sub * 3 * (nr + 1);
         f.qt[o] -= (loc - pim) * ld(cf + k);
         if (k >= 1) f.qr[o] -= (loc - pkm) * ld(cf + (nr + 1) + k);
         f.qz[o] -= (loc - pjm) * ld(cf + 2 * (nr + 1));
@@ -693,16 +751,18 @@ __global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, Consts K, 
         const double pip = ld(phi + (size_t)k * P + rowoff + ip);
         const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
         const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+        const double l0 = loc, im_ = pim, jm_ = pjm, km_ = pkm;
         const double be = f.st->beta;
         const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
-        f.pr[o] = f.pr[o] + loc - be * ((pip - 2.0 * loc + pim) * ld(c.udx1qm + k) +
-                                        (pjp - 2.0 * loc + pjm) * K.dxzq +
-                                        (pkp * app + loc * acc + pkm * amm));
+        f.pr[o] = f.pr[o] + l0 - be * ((pip - 2.0 * l0 + im_) * ld(c.udx1qm + k) +
+                                       (pjp - 2.0 * l0 + jm_) * dxzq +
+                                       (pkp * app + l0 * acc + km_ * amm));
     }
 }
 
 // CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
-__global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts K, Fields f, int sub) {
+template <typename T>
+__global__ void __launch_bounds__(128) divergence_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long half = (long long)d.nr * d.nz * (d.nt / 2);
@@ -711,13 +771,14 @@ __global__ void __launch_bounds__(128) divergence_kernel(Dims d, Coef c, Consts 
     const long long row = t / M;
     const int m = (int)(t - row * M);
     const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
-    double2 z = div_pair(d, c, K, f.qt, f.qr, f.qz, k, j, m);
-    const double usdt = f.corr[9 * (d.nr + 1) + 3 + sub];
-    *reinterpret_cast<double2*>(f.phi + (size_t)row * d.nt + 2 * m) = make_double2(z.x * usdt, z.y * usdt);
+    auto z = div_pair(d, c, dxt, dxz, f.qt, f.qr, f.qz, k, j, m);
+    const T usdt = (T)f.scal[3 + sub];
+    *reinterpret_cast<typename V2<T>::type*>(f.phi + (size_t)row * d.nt + 2 * m) = mk2(z.x * usdt, z.y * usdt);
 }
 
 // --------------------------------------------------------------------------
-// Reductions: per-block partials in a fixed order, then one finishing block.
+// Reductions (FP64 arithmetic): per-block partials in a fixed order, then one
+// finishing block.
 // --------------------------------------------------------------------------
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -744,8 +805,9 @@ __device__ double block_reduce(double v, double* sh) {
 }
 
 // CalcMaxCFL.F90:30-43 (which = 0) and CheckDivergence.F90:77-89 (which = 1).
-__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Consts K, Fields f, int which,
-                                                               int only_on_output) {
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, double dxt, double dxz, FieldsT<T> f,
+                                                               int which, int only_on_output) {
     __shared__ double sh[32];
     if (only_on_output && (f.st->halt || !f.st->output)) return;
     const long long n = (long long)d.nr * d.P;
@@ -762,10 +824,10 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Co
         const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
         double v;
         if (which == 0) {
-            v = fabs((t1 + t0) * 0.5 * K.dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
-                fabs((z1 + z0) * 0.5 * K.dxz);
+            v = fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
+                fabs((z1 + z0) * 0.5 * dxz);
         } else {
-            v = fabs(((t1 - t0) * K.dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * K.dxz);
+            v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * dxz);
         }
         best = fmax(best, v);
     }
@@ -773,20 +835,22 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Co
     if (threadIdx.x == 0) f.red[blockIdx.x] = best;
 }
 
-__global__ void __launch_bounds__(kRedThreads) cellmax_finish(Fields f, int nblocks, int which, int only_on_output) {
+__global__ void __launch_bounds__(kRedThreads) cellmax_finish(const double* red, StepState* st, int nblocks,
+                                                               int which, int only_on_output) {
     __shared__ double sh[32];
-    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    if (only_on_output && (st->halt || !st->output)) return;
     double best = which == 0 ? 0.00000001 : 0.0;
-    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = fmax(best, f.red[t]);
+    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = fmax(best, red[t]);
     best = block_reduce<true>(best, sh);
     if (threadIdx.x == 0) {
-        if (which == 0) f.st->instcfl = best;
-        else f.st->dmax = best;
+        if (which == 0) st->instcfl = best;
+        else st->dmax = best;
     }
 }
 
 // CalcVelocityStats.F90:21-43: vmax and the pvol-weighted squares.
-__global__ void __launch_bounds__(kRedThreads) vstats_kernel(Dims d, Coef c, Consts K, Fields f, int only_on_output) {
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) vstats_kernel(Dims d, Coef c, double pi, FieldsT<T> f, int only_on_output) {
     __shared__ double sh[32];
     if (only_on_output && (f.st->halt || !f.st->output)) return;
     const long long n = (long long)d.nr * d.P;
@@ -806,9 +870,9 @@ __global__ void __launch_bounds__(kRedThreads) vstats_kernel(Dims d, Coef c, Con
         const double r1 = ld(f.qr + o + P);
         const double z1 = ld(f.qz + (size_t)k * P + (size_t)wp(j, d.nz) * d.nt + i);
         const double a = t0 + t1, b = r0 * ld(c.usrc + k) + r1 * ld(c.usrc + k + 1), e = z0 + z1;
-        s[0] += a * a * pv * K.pi * 0.25;
-        s[1] += b * b * pv * K.pi * 0.25;
-        s[2] += e * e * pv * K.pi * 0.25;
+        s[0] += a * a * pv * pi * 0.25;
+        s[1] += b * b * pv * pi * 0.25;
+        s[2] += e * e * pv * pi * 0.25;
     }
     for (int q = 0; q < 3; ++q) {
         double m = block_reduce<true>(vm[q], sh);
@@ -818,27 +882,29 @@ __global__ void __launch_bounds__(kRedThreads) vstats_kernel(Dims d, Coef c, Con
     }
 }
 
-__global__ void __launch_bounds__(kRedThreads) vstats_finish(Consts K, Fields f, int nblocks, double vol,
+__global__ void __launch_bounds__(kRedThreads) vstats_finish(const double* red, StepState* st, int nblocks, double vol,
                                                               int only_on_output) {
     __shared__ double sh[32];
-    if (only_on_output && (f.st->halt || !f.st->output)) return;
+    if (only_on_output && (st->halt || !st->output)) return;
     for (int q = 0; q < 3; ++q) {
         double m = -100.0, s = 0.0;
         for (int t = threadIdx.x; t < nblocks; t += blockDim.x) {
-            m = fmax(m, f.red[q * nblocks + t]);
-            s += f.red[(3 + q) * nblocks + t];
+            m = fmax(m, red[q * nblocks + t]);
+            s += red[(3 + q) * nblocks + t];
         }
         m = block_reduce<true>(m, sh);
         s = block_reduce<false>(s, sh);
         if (threadIdx.x == 0) {
-            f.st->vmax[q] = m;
-            f.st->rms[q] = s / vol;
+            st->vmax[q] = m;
+            st->rms[q] = s / vol;
         }
     }
 }
 
 // CalcTorque.F90:131-150: wall sums over (z, theta) columns.
-__global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, Consts K, Fields f) {
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, double virotint, double virotext,
+                                                              FieldsT<T> f) {
     __shared__ double sh[32];
     const int nr = d.nr;
     const size_t P = (size_t)d.P;
@@ -847,12 +913,12 @@ __global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, Con
     double lo = 0.0, up = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < d.P; t += (long long)gridDim.x * blockDim.x) {
         const double fic = f.icyl ? (double)f.icyl[t] : 1.0;
-        double grtlow = ((ld(f.qt + P + t) * ld(c.usrm + 1) + ld(f.qt + t) * ld(c.usrm + 0)) * 0.5 -
-                         K.virotint * ld(c.usrc + 0)) * del;
+        double grtlow = (((double)ld(f.qt + P + t) * ld(c.usrm + 1) + (double)ld(f.qt + t) * ld(c.usrm + 0)) * 0.5 -
+                         virotint * ld(c.usrc + 0)) * del;
         lo = lo + grtlow * fic;
-        double grtup = (K.virotext * ld(c.usrc + nr) -
-                        (ld(f.qt + (size_t)(nr - 2) * P + t) * ld(c.usrm + nr - 2) +
-                         ld(f.qt + (size_t)(nr - 1) * P + t) * ld(c.usrm + nr - 1)) * 0.5) * deln;
+        double grtup = (virotext * ld(c.usrc + nr) -
+                        ((double)ld(f.qt + (size_t)(nr - 2) * P + t) * ld(c.usrm + nr - 2) +
+                         (double)ld(f.qt + (size_t)(nr - 1) * P + t) * ld(c.usrm + nr - 1)) * 0.5) * deln;
         up = up + grtup;   // ocylsl = 1
     }
     lo = block_reduce<false>(lo, sh);
@@ -861,12 +927,13 @@ __global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, Con
     if (threadIdx.x == 0) f.red[gridDim.x + blockIdx.x] = up;
 }
 
-__global__ void __launch_bounds__(kRedThreads) torque_finish(Dims d, Coef c, Consts K, Fields f, int nblocks) {
+__global__ void __launch_bounds__(kRedThreads) torque_finish(Dims d, Coef c, Consts K, const double* red,
+                                                              StepState* st, int nblocks) {
     __shared__ double sh[32];
     double lo = 0.0, up = 0.0;
     for (int t = threadIdx.x; t < nblocks; t += blockDim.x) {
-        lo += f.red[t];
-        up += f.red[nblocks + t];
+        lo += red[t];
+        up += red[nblocks + t];
     }
     lo = block_reduce<false>(lo, sh);
     up = block_reduce<false>(up, sh);
@@ -881,8 +948,8 @@ __global__ void __launch_bounds__(kRedThreads) torque_finish(Dims d, Coef c, Con
         lo = lo * (r2 * r2 * r2) * reninv * jlami;
         up = up * (rn * rn * rn) * reninv * jlami;
         const double surf = 1.0 / ((double)d.nt * (double)d.nz);
-        f.st->torque[0] = lo * surf;
-        f.st->torque[1] = up * surf;
+        st->torque[0] = lo * surf;
+        st->torque[1] = up * surf;
     }
 }
 
@@ -891,7 +958,8 @@ __global__ void __launch_bounds__(kRedThreads) torque_finish(Dims d, Coef c, Con
 // with jh, ih halo indices (0 and n+1 are ghosts); device: [k][j][i].
 // --------------------------------------------------------------------------
 
-__global__ void to_device_kernel(Dims d, const double* stage, double* dst, int nk, int halo) {
+template <typename T>
+__global__ void to_device_kernel(Dims d, const double* stage, T* dst, int nk, int halo) {
     __shared__ double tile[32][33];
     const int nrr = d.nr + 1;
     const int NJ = d.nz + 2 * halo;
@@ -906,12 +974,13 @@ __global__ void to_device_kernel(Dims d, const double* stage, double* dst, int n
     __syncthreads();
     for (int y = threadIdx.y; y < 32; y += blockDim.y) {
         int k = k0 + y, i = i0 + threadIdx.x;
-        if (i < d.nt && k < nk) dst[(size_t)k * d.P + (size_t)j * d.nt + i] = tile[threadIdx.x][y];
+        if (i < d.nt && k < nk) dst[(size_t)k * d.P + (size_t)j * d.nt + i] = (T)tile[threadIdx.x][y];
     }
 }
 
 // halo = 1: output (nr, nzm+2, nthm+2) with periodic ghosts; halo = 0: (nr, nzm, nthm).
-__global__ void to_host_kernel(Dims d, const double* src, double* stage, int nk, int halo) {
+template <typename T>
+__global__ void to_host_kernel(Dims d, const T* src, double* stage, int nk, int halo) {
     __shared__ double tile[32][33];
     const int nrr = d.nr + 1;
     const int NJ = d.nz + 2 * halo, NI = d.nt + 2 * halo;
@@ -922,7 +991,7 @@ __global__ void to_host_kernel(Dims d, const double* src, double* stage, int nk,
         int k = k0 + y, ih = i0 + threadIdx.x;
         if (ih < NI && k < nrr) {
             int i = halo ? (ih == 0 ? d.nt - 1 : (ih == d.nt + 1 ? 0 : ih - 1)) : ih;
-            tile[y][threadIdx.x] = (k < nk) ? src[(size_t)k * d.P + (size_t)j * d.nt + i] : 0.0;
+            tile[y][threadIdx.x] = (k < nk) ? (double)src[(size_t)k * d.P + (size_t)j * d.nt + i] : 0.0;
         }
     }
     __syncthreads();
@@ -980,123 +1049,153 @@ double measure_fp64_peak(cudaStream_t s) {
 
 int reduction_blocks() { return kRedBlocks; }
 
-void launch_begin_step(cudaStream_t s, const Consts& k, StepState* st, int mode, double dt, double time) {
-    begin_step_kernel<<<1, 32, 0, s>>>(k, st, mode, dt, time);
-}
-void launch_slip(cudaStream_t s, const Dims& d, const Consts& k, const Fields& f) {
-    slip_kernel<<<(unsigned)((d.P + 255) / 256), 256, 0, s>>>(d, k, f.st, f.icyl);
-}
-void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
-    factors_kernel<<<1, 512, 0, s>>>(d, c, k, f.st, f.F, f.corr);
-}
-void launch_end_step(cudaStream_t s, const Consts& k, StepState* st) { end_step_kernel<<<1, 32, 0, s>>>(k, st); }
-void launch_finish_step(cudaStream_t s, const Consts& k, StepState* st) { finish_step_kernel<<<1, 32, 0, s>>>(k, st); }
-
-static dim3 cell_grid(const Dims& d, dim3& blk) {
-    blk = dim3(d.nt >= 64 ? 64 : 32, d.nt >= 64 ? 2 : 4, 1);
-    return dim3((d.nt + blk.x - 1) / blk.x, (d.nz + blk.y - 1) / blk.y, d.nr);
-}
-
-void launch_momentum(cudaStream_t s, int mode, const Dims& d, const Coef& c, const Consts& k,
-                     const Fields& f, int sub) {
-    MomArgs a;
-    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.pr;
-    a.ru1 = f.ru1; a.ru2 = f.ru2; a.ru3 = f.ru3;
-    a.rhs_t = f.rhs_t; a.rhs_r = f.rhs_r; a.rhs_z = f.rhs_z;
-    a.h_t = f.h_t; a.h_r = f.h_r; a.h_z = f.h_z;
-    a.icyl = k.patterned ? f.icyl : nullptr;
-    a.st = f.st;
-    a.al = k.alm[sub]; a.ga = k.gam[sub]; a.ro = k.rom[sub];
-    a.alre = k.alre[sub]; a.dxt_al = k.dxt_al[sub]; a.dxz_al = k.dxz_al[sub];
-    dim3 blk;
-    dim3 g = cell_grid(d, blk);
-    if (mode == MODE_FUSED) momentum_kernel<MODE_FUSED><<<g, blk, 0, s>>>(d, c, k, a);
-    else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT><<<g, blk, 0, s>>>(d, c, k, a);
-    else momentum_kernel<MODE_IMPLICIT><<<g, blk, 0, s>>>(d, c, k, a);
-    TC_LAUNCH_CHECK();
-}
-
-void launch_radial_solve(cudaStream_t s, const Dims& d, const Fields& f, int sub) {
-    radial_solve_kernel<<<(unsigned)((d.P + 127) / 128), 128, 0, s>>>(d, f, sub);
-    TC_LAUNCH_CHECK();
-}
-
-template <bool FP, int R>
-static void div_fft_R(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
-                      const Plans& p, int sub) {
-    size_t sm = (size_t)2 * R * p.th.n * sizeof(double2);
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(div_fft_kernel<FP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-    long long nrows = (long long)d.nr * d.nz;
-    div_fft_kernel<FP, R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, c, k, f, p.th, p.twr, sub);
-}
-
 int theta_rows(int M) {
     int R = 1;
     while (R < 32 && (R * 2) * M <= 512) R *= 2;
     return R;
 }
 
-void launch_div_fft(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
-                    const Plans& p, int sub, bool from_phi) {
+void launch_begin_step(cudaStream_t s, const Consts& k, StepState* st, int mode, double dt, double time) {
+    begin_step_kernel<<<1, 32, 0, s>>>(k, st, mode, dt, time);
+}
+void launch_end_step(cudaStream_t s, const Consts& k, StepState* st) { end_step_kernel<<<1, 32, 0, s>>>(k, st); }
+void launch_finish_step(cudaStream_t s, const Consts& k, StepState* st) { finish_step_kernel<<<1, 32, 0, s>>>(k, st); }
+
+template <typename T>
+void launch_slip(cudaStream_t s, const Dims& d, const Consts& k, const FieldsT<T>& f) {
+    slip_kernel<<<(unsigned)((d.P + 255) / 256), 256, 0, s>>>(d, k, f.st, f.icyl);
+}
+
+template <typename T>
+void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f) {
+    factors_kernel<T><<<1, 512, 0, s>>>(d, c, k, f.st, f.Fd, f.corrd, f.scal, f.F, f.corr);
+    TC_LAUNCH_CHECK();
+}
+
+static dim3 cell_grid(const Dims& d, dim3& blk) {
+    blk = dim3(d.nt >= 64 ? 64 : 32, d.nt >= 64 ? 2 : 4, 1);
+    return dim3((d.nt + blk.x - 1) / blk.x, (d.nz + blk.y - 1) / blk.y, d.nr);
+}
+
+template <typename T>
+void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c, const Consts& k,
+                     const FieldsT<T>& f, int sub) {
+    MomArgs<T> a;
+    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.pr;
+    a.ru1 = f.ru1; a.ru2 = f.ru2; a.ru3 = f.ru3;
+    a.rhs_t = f.rhs_t; a.rhs_r = f.rhs_r; a.rhs_z = f.rhs_z;
+    a.h_t = f.h_t; a.h_r = f.h_r; a.h_z = f.h_z;
+    a.icyl = k.patterned ? f.icyl : nullptr;
+    a.st = f.st;
+    a.al = (T)k.alm[sub]; a.ga = (T)k.gam[sub]; a.ro = (T)k.rom[sub];
+    a.alre = (T)k.alre[sub]; a.dxt_al = (T)k.dxt_al[sub]; a.dxz_al = (T)k.dxz_al[sub];
+    a.udxz = (T)k.udxz; a.udxzq = (T)k.udxzq; a.q_romeg = (T)k.q_romeg;
+    a.virotint = (T)k.virotint; a.virotext = (T)k.virotext;
+    a.ac1j_fs0 = (T)k.ac1j_fs0; a.am1j_fs0 = (T)k.am1j_fs0; a.ap1j_fs1 = (T)k.ap1j_fs1; a.ac1j_fs1 = (T)k.ac1j_fs1;
+    a.ac3j_fs0 = (T)k.ac3j_fs0; a.am3j_fs0 = (T)k.am3j_fs0; a.ap3j_fs1 = (T)k.ap3j_fs1; a.ac3j_fs1 = (T)k.ac3j_fs1;
+    a.use_ru = k.rom[sub] != 0.0;
+    dim3 blk;
+    dim3 g = cell_grid(d, blk);
+    if (mode == MODE_FUSED) momentum_kernel<MODE_FUSED, T><<<g, blk, 0, s>>>(d, c, a);
+    else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
+    else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
+    TC_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub) {
+    radial_solve_kernel<T><<<(unsigned)((d.P + 127) / 128), 128, 0, s>>>(d, f, sub);
+    TC_LAUNCH_CHECK();
+}
+
+template <bool FP, int R, typename T>
+static void div_fft_R(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
+                      const PlansT<T>& p, int sub) {
+    size_t sm = (size_t)2 * R * p.th.n * sizeof(typename V2<T>::type);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(div_fft_kernel<FP, R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    long long nrows = (long long)d.nr * d.nz;
+    div_fft_kernel<FP, R, T><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(
+        d, c, (T)k.dxt, (T)k.dxz, f, p.th, p.tw_th, p.twr, k.fft_norm, sub);
+}
+
+template <typename T>
+void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
+                    const PlansT<T>& p, int sub, bool from_phi) {
     int R = theta_rows(p.th.n);
-#define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR>(s, d, c, k, f, p, sub); else div_fft_R<false, RR>(s, d, c, k, f, p, sub); break;
+#define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR, T>(s, d, c, k, f, p, sub); \
+                           else div_fft_R<false, RR, T>(s, d, c, k, f, p, sub); break;
     switch (R) { TC_DF(1) TC_DF(2) TC_DF(4) TC_DF(8) TC_DF(16) TC_DF(32) }
 #undef TC_DF
     TC_LAUNCH_CHECK();
 }
 
-void launch_zfft(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p, bool inv) {
-    size_t sm = (size_t)2 * kZC * p.z.n * sizeof(double2);
+template <typename T>
+void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p, bool inv) {
+    size_t sm = (size_t)2 * kZC * p.z.n * sizeof(typename V2<T>::type);
     static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(zfft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    if (!attr) {
+        cudaFuncSetAttribute(zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
     dim3 g((d.PH + kZC - 1) / kZC, d.nr);
-    zfft_kernel<<<g, 128, sm, s>>>(d, f, p.z, inv ? 1 : 0);
+    zfft_kernel<T><<<g, 128, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
 
-void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const Fields& f) {
+template <typename T>
+void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f) {
     long long n = (long long)d.nzh * d.PH;
-    ptri_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f);
+    double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(f.spec) : f.ws;
+    ptri_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f, ws);
     TC_LAUNCH_CHECK();
 }
 
-template <int R>
-static void theta_inv_R(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p) {
-    size_t sm = (size_t)2 * R * p.th.n * sizeof(double2);
+template <int R, typename T>
+static void theta_inv_R(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
+    size_t sm = (size_t)2 * R * p.th.n * sizeof(typename V2<T>::type);
     static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(theta_inv_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    if (!attr) {
+        cudaFuncSetAttribute(theta_inv_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
     long long nrows = (long long)d.nr * d.nz;
-    theta_inv_kernel<R><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, f, p.th, p.twr);
+    theta_inv_kernel<R, T><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, f, p.th, p.tw_th, p.twr);
 }
 
-void launch_theta_inverse(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p) {
+template <typename T>
+void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
     int R = theta_rows(p.th.n);
     switch (R) {
-        case 1: theta_inv_R<1>(s, d, f, p); break;
-        case 2: theta_inv_R<2>(s, d, f, p); break;
-        case 4: theta_inv_R<4>(s, d, f, p); break;
-        case 8: theta_inv_R<8>(s, d, f, p); break;
-        case 16: theta_inv_R<16>(s, d, f, p); break;
-        default: theta_inv_R<32>(s, d, f, p); break;
+        case 1: theta_inv_R<1, T>(s, d, f, p); break;
+        case 2: theta_inv_R<2, T>(s, d, f, p); break;
+        case 4: theta_inv_R<4, T>(s, d, f, p); break;
+        case 8: theta_inv_R<8, T>(s, d, f, p); break;
+        case 16: theta_inv_R<16, T>(s, d, f, p); break;
+        default: theta_inv_R<32, T>(s, d, f, p); break;
     }
     TC_LAUNCH_CHECK();
 }
 
-void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+template <typename T>
+void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f,
                     int sub, bool vel, bool pres) {
     dim3 blk;
     dim3 g = cell_grid(d, blk);
-    if (vel && pres) correct_kernel<true, true><<<g, blk, 0, s>>>(d, c, k, f, sub);
-    else if (vel) correct_kernel<true, false><<<g, blk, 0, s>>>(d, c, k, f, sub);
-    else correct_kernel<false, true><<<g, blk, 0, s>>>(d, c, k, f, sub);
+    if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
+    else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
+    else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
     TC_LAUNCH_CHECK();
 }
 
-void launch_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+template <typename T>
+void launch_divergence(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                        int sub) {
     long long n = (long long)d.nr * d.nz * (d.nt / 2);
-    divergence_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, k, f, sub);
+    divergence_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, (T)k.dxt, (T)k.dxz, f, sub);
     TC_LAUNCH_CHECK();
 }
 
@@ -1106,41 +1205,74 @@ void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, doubl
     TC_LAUNCH_CHECK();
 }
 
-void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
-    cellmax_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, 0, 0);
-    cellmax_finish<<<1, kRedThreads, 0, s>>>(f, kRedBlocks, 0, 0);
+template <typename T>
+void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f) {
+    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.dxt, k.dxz, f, 0, 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 0, 0);
     TC_LAUNCH_CHECK();
 }
+template <typename T>
 void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
-                             const Fields& f, bool only_on_output) {
-    cellmax_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, 1, only_on_output ? 1 : 0);
-    cellmax_finish<<<1, kRedThreads, 0, s>>>(f, kRedBlocks, 1, only_on_output ? 1 : 0);
+                             const FieldsT<T>& f, bool only_on_output) {
+    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.dxt, k.dxz, f, 1, only_on_output ? 1 : 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 1, only_on_output ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
+template <typename T>
 void launch_velocity_stats(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
-                           const Fields& f, bool only_on_output) {
-    vstats_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f, only_on_output ? 1 : 0);
+                           const FieldsT<T>& f, bool only_on_output) {
+    vstats_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.pi, f, only_on_output ? 1 : 0);
     // CalcVelocityStats.F90:47-50: divide by nthm*nzm*pi*(rext^2 - rint^2)
     double volt = k.pi * (k.rext * k.rext - k.rint * k.rint);
     double vol = (double)d.nt * (double)d.nz * volt;
-    vstats_finish<<<1, kRedThreads, 0, s>>>(k, f, kRedBlocks, vol, only_on_output ? 1 : 0);
+    vstats_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, vol, only_on_output ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
-void launch_torque(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f) {
-    torque_kernel<<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k, f);
-    torque_finish<<<1, kRedThreads, 0, s>>>(d, c, k, f, kRedBlocks);
+template <typename T>
+void launch_torque(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f) {
+    torque_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.virotint, k.virotext, f);
+    torque_finish<<<1, kRedThreads, 0, s>>>(d, c, k, f.red, f.st, kRedBlocks);
     TC_LAUNCH_CHECK();
 }
 
-void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, double* dst, int nk, int halo) {
+template <typename T>
+void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, T* dst, int nk, int halo) {
     dim3 g((d.nt + 31) / 32, (nk + 31) / 32, d.nz);
-    to_device_kernel<<<g, dim3(32, 8), 0, s>>>(d, stage, dst, nk, halo);
+    to_device_kernel<T><<<g, dim3(32, 8), 0, s>>>(d, stage, dst, nk, halo);
     TC_LAUNCH_CHECK();
 }
-void launch_to_host(cudaStream_t s, const Dims& d, const double* src, double* stage, int nk, int halo) {
+template <typename T>
+void launch_to_host(cudaStream_t s, const Dims& d, const T* src, double* stage, int nk, int halo) {
     dim3 g((d.nt + 2 * halo + 31) / 32, (d.nr + 1 + 31) / 32, d.nz + 2 * halo);
-    to_host_kernel<<<g, dim3(32, 8), 0, s>>>(d, src, stage, nk, halo);
+    to_host_kernel<T><<<g, dim3(32, 8), 0, s>>>(d, src, stage, nk, halo);
     TC_LAUNCH_CHECK();
 }
+
+#define TC_INSTANTIATE(T)                                                                                      \
+    template void launch_slip<T>(cudaStream_t, const Dims&, const Consts&, const FieldsT<T>&);                 \
+    template void launch_factors<T>(cudaStream_t, const Dims&, const Coef&, const Consts&, const FieldsT<T>&); \
+    template void launch_momentum<T>(cudaStream_t, int, const Dims&, const CoefT<T>&, const Consts&,           \
+                                     const FieldsT<T>&, int);                                                 \
+    template void launch_radial_solve<T>(cudaStream_t, const Dims&, const FieldsT<T>&, int);                  \
+    template void launch_div_fft<T>(cudaStream_t, const Dims&, const CoefT<T>&, const Consts&,                \
+                                    const FieldsT<T>&, const PlansT<T>&, int, bool);                          \
+    template void launch_zfft<T>(cudaStream_t, const Dims&, const FieldsT<T>&, const PlansT<T>&, bool);       \
+    template void launch_pressure_tridiag<T>(cudaStream_t, const Dims&, const Coef&, const FieldsT<T>&);      \
+    template void launch_theta_inverse<T>(cudaStream_t, const Dims&, const FieldsT<T>&, const PlansT<T>&);    \
+    template void launch_correct<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,                    \
+                                    const FieldsT<T>&, int, bool, bool);                                      \
+    template void launch_divergence<T>(cudaStream_t, const Dims&, const CoefT<T>&, const Consts&,             \
+                                       const FieldsT<T>&, int);                                               \
+    template void launch_cfl<T>(cudaStream_t, const Dims&, const Coef&, const Consts&, const FieldsT<T>&);    \
+    template void launch_check_divergence<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,           \
+                                             const FieldsT<T>&, bool);                                        \
+    template void launch_velocity_stats<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,             \
+                                           const FieldsT<T>&, bool);                                          \
+    template void launch_torque<T>(cudaStream_t, const Dims&, const Coef&, const Consts&, const FieldsT<T>&); \
+    template void launch_to_device<T>(cudaStream_t, const Dims&, const double*, T*, int, int);                \
+    template void launch_to_host<T>(cudaStream_t, const Dims&, const T*, double*, int, int);
+
+TC_INSTANTIATE(double)
+TC_INSTANTIATE(float)
 
 }  // namespace tcgb

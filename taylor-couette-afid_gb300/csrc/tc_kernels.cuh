@@ -1,4 +1,8 @@
 // tc_kernels.cuh -- launch interface of the step kernels (tc_kernels.cu).
+//
+// Every velocity-side kernel is a template on the element type T (double:
+// plain FP64 path; float: mixed path).  The launchers are instantiated for
+// both.
 #pragma once
 
 #include "tc_dev.h"
@@ -7,65 +11,88 @@ namespace tcgb {
 
 enum { MODE_FUSED = 0, MODE_EXPLICIT = 1, MODE_IMPLICIT = 2 };
 
-struct Fields {
-    double *qt, *qr, *qz, *pr, *phi;
-    double *ru1, *ru2, *ru3;
-    double *rhs_t, *rhs_r, *rhs_z;
-    double *h_t, *h_r, *h_z;          // explicit-term arrays (per-routine entry points only)
-    double2* spec;
-    const double *pf_l, *pf_dinv;     // pressure LU factors [k][kz <= nzm/2][kt]
+template <typename T>
+struct FieldsT {
+    T *qt, *qr, *qz;
+    double* pr;                       // pressure is FP64 in both paths
+    T* phi;
+    T *ru1, *ru2, *ru3;
+    T *rhs_t, *rhs_r, *rhs_z;
+    T *h_t, *h_r, *h_z;               // explicit-term arrays (per-routine entry points only)
+    typename V2<T>::type* spec;
+    const double *pf_l, *pf_dinv;     // pressure LU factors [k][kz <= nzm/2][kt] (FP64)
     signed char* icyl;                // inner-wall slip mask per column (1 = no slip)
     StepState* st;
-    MomFactors F;
-    double* corr;                     // per-substep correction coefficients [s][3][nr+1]
+    MomFactorsT<T> F;                 // momentum LU factors of the step
+    T* corr;                          // CorrectVelocity coefficients [s][3][nr+1]
+    MomFactorsT<double> Fd;           // the same in FP64 (aliases F, corr when T = double)
+    double* corrd;
+    double* scal;                     // per substep: [s] usdt*fft_norm, [3+s] usdt
     double* red;                      // reduction partials
+    double2* ws;                      // FP64 forward-sweep scratch of the pressure solve (T = float)
 };
 
-struct Plans {
+template <typename T>
+struct PlansT {
     FFTPlan th;        // complex length nthm/2 (real transform along theta)
     FFTPlan z;         // complex length nzm
-    const double2* twr;  // exp(-2 pi i k / nthm), k = 0..nthm/2
+    const typename V2<T>::type* tw_th;   // exp(-2 pi i j / (nthm/2))
+    const typename V2<T>::type* tw_z;    // exp(-2 pi i j / nzm)
+    const typename V2<T>::type* twr;     // exp(-2 pi i k / nthm), k = 0..nthm/2
 };
 
 int reduction_blocks();
+int theta_rows(int M);
 
-// Step control.
+// Step control (precision independent).
 void launch_begin_step(cudaStream_t s, const Consts& k, StepState* st, int mode, double dt, double time);
-void launch_slip(cudaStream_t s, const Dims& d, const Consts& k, const Fields& f);
-void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f);
 void launch_end_step(cudaStream_t s, const Consts& k, StepState* st);
 void launch_finish_step(cudaStream_t s, const Consts& k, StepState* st);
+template <typename T> void launch_slip(cudaStream_t s, const Dims& d, const Consts& k, const FieldsT<T>& f);
+template <typename T>
+void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f);
 
 // Substep kernels.
-void launch_momentum(cudaStream_t s, int mode, const Dims& d, const Coef& c, const Consts& k,
-                     const Fields& f, int sub);
-void launch_radial_solve(cudaStream_t s, const Dims& d, const Fields& f, int sub);
-void launch_div_fft(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
-                    const Plans& p, int sub, bool from_phi);
-void launch_zfft(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p, bool inv);
-void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const Fields& f);
-void launch_theta_inverse(cudaStream_t s, const Dims& d, const Fields& f, const Plans& p);
-void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+template <typename T>
+void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c, const Consts& k,
+                     const FieldsT<T>& f, int sub);
+template <typename T> void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub);
+template <typename T>
+void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
+                    const PlansT<T>& p, int sub, bool from_phi);
+template <typename T> void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p, bool inv);
+template <typename T>
+void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f);
+template <typename T> void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p);
+template <typename T>
+void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f,
                     int sub, bool vel, bool pres);
-void launch_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f,
+template <typename T>
+void launch_divergence(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                        int sub);
 
 // One-time set-up.
 void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, double* l, double* dinv);
 
-// Reductions (results land in StepState).
-void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f);
+// Reductions (FP64 arithmetic; results land in StepState).
+template <typename T>
+void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f);
+template <typename T>
 void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
-                             const Fields& f, bool only_on_output);
+                             const FieldsT<T>& f, bool only_on_output);
+template <typename T>
 void launch_velocity_stats(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
-                           const Fields& f, bool only_on_output);
-void launch_torque(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const Fields& f);
+                           const FieldsT<T>& f, bool only_on_output);
+template <typename T>
+void launch_torque(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f);
 
-// Layout conversion between the reference layout (with halo) and the device.
-// nk device planes; halo = 1 for (nr, nzm+2, nthm+2) arrays, 0 for (nr, nzm, nthm).
-void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, double* dst, int nk, int halo);
-void launch_to_host(cudaStream_t s, const Dims& d, const double* src, double* stage, int nk, int halo);
-int theta_rows(int M);
+// Layout conversion between the reference layout (FP64 host arrays, with or
+// without halo) and a device array of element type T.  nk device planes;
+// halo = 1 for (nr, nzm+2, nthm+2) arrays, 0 for (nr, nzm, nthm).
+template <typename T>
+void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, T* dst, int nk, int halo);
+template <typename T>
+void launch_to_host(cudaStream_t s, const Dims& d, const T* src, double* stage, int nk, int halo);
 
 // Dense FP64 FMA rate of the current device in TFLOP/s (measurement helper).
 double measure_fp64_peak(cudaStream_t s);
