@@ -167,6 +167,8 @@ cudaError_t alloc_fields(tc_handle* h, FieldsT<T>& f) {
     AL(f.corr, (size_t)9 * nrr);
     AL(f.scal, 8);
     AL(f.red, (size_t)6 * reduction_blocks());
+    if (std::is_same<T, double>::value) f.prf = reinterpret_cast<T*>(f.pr);
+    else AL(f.prf, cells);
     if (std::is_same<T, double>::value) {
         f.Fd.base = reinterpret_cast<double*>(f.F.base);
         f.Fd.stride = nrr;
@@ -393,6 +395,13 @@ static int download(tc_handle* h, const T* src, double* dst, int nk, int halo) {
     return 0;
 }
 
+// The mixed path keeps an FP32 copy of the FP64 pressure for the momentum rhs.
+static void refresh_prf(tc_handle*, FieldsT<double>&) {}
+static void refresh_prf(tc_handle* h, FieldsT<float>& f) {
+    const long long n = (long long)h->d.P * h->d.nr;
+    L(h, K_LAYOUT, 1, [&] { launch_round_to_float(h->stream, f.pr, f.prf, n); });
+}
+
 template <typename T>
 static int set_state_t(tc_handle* h, const double* qt, const double* qr, const double* qz, const double* pr) {
     const Dims& d = h->d;
@@ -408,6 +417,7 @@ static int set_state_t(tc_handle* h, const double* qt, const double* qr, const d
     CK(cudaMemsetAsync(f.ru1, 0, cells * sizeof(T), h->stream), "memset");
     CK(cudaMemsetAsync(f.ru2, 0, faces * sizeof(T), h->stream), "memset");
     CK(cudaMemsetAsync(f.ru3, 0, cells * sizeof(T), h->stream), "memset");
+    refresh_prf(h, f);
     CK(cudaStreamSynchronize(h->stream), "set_state sync");
     return 0;
 }
@@ -462,6 +472,7 @@ static int field_io(tc_handle* h, int which, double* out, const double* in) {
     if (out) return pp ? download(h, (const double*)pp, out, nk, halo) : download(h, (const T*)p, out, nk, halo);
     int r = pp ? upload(h, in, pp, nk, halo) : upload(h, in, p, nk, halo);
     if (r) return r;
+    if (pp) refresh_prf(h, f);
     CK(cudaStreamSynchronize(h->stream), "set_field sync");
     return 0;
 }

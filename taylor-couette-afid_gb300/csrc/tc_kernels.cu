@@ -239,7 +239,7 @@ struct Stencil {
 template <typename T>
 struct MomArgs {
     const T *qt, *qr, *qz;
-    const double* pr;
+    const T* pr;            // pressure in the element type (FP32 copy on the mixed path)
     T *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
     const signed char* icyl;
     const StepState* st;
@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
     const T* qt = a.qt;
     const T* qr = a.qr;
     const T* qz = a.qz;
-    const double* pr = a.pr;
-    const double p_c = ld(pr + o);
+    const T* pr = a.pr;
+    const T p_c = ld(pr + o);
     // ---- qt (ImplicitAndUpdateQT.F90:45-115)
     {
         T d33;
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
             d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
                   ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
         }
-        T dpx11 = (T)(p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
+        T dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
         T old = a.use_ru ? a.ru1[o] : (T)0;
         a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
         a.ru1[o] = ht;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
         T d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
                 ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
         T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
-        T dpx22 = (T)(p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
+        T dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
         T old = a.use_ru ? a.ru2[o] : (T)0;
         a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
         a.ru2[o] = hr;
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
             d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
                   ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
         }
-        T dpx33 = (T)(p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
+        T dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
         T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
@@ -626,6 +626,7 @@ __global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, FieldsT<T> f,
     double2 y1 = to_d2(x1[0]), y2 = two ? to_d2(x2[0]) : make_double2(0.0, 0.0);
     w1[0] = y1;
     if (two) w2[0] = y2;
+#pragma unroll 4
     for (int k = 1; k < nr; ++k) {
         const double l = ld(L + k * FS);
         double2 b1 = to_d2(x1[k * PS]);
@@ -641,6 +642,7 @@ __global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, FieldsT<T> f,
     double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
     st2(x1 + (size_t)(nr - 1) * PS, s1.x, s1.y);
     if (two) st2(x2 + (size_t)(nr - 1) * PS, s2.x, s2.y);
+#pragma unroll 4
     for (int k = nr - 2; k >= 0; --k) {
         const double u = ld(c.apph + k);
         di = ld(DI + k * FS);
@@ -748,15 +750,33 @@ __global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, double dxz
         f.qz[o] -= (loc - pjm) * ld(cf + 2 * (nr + 1));
     }
     if (PRES) {
-        const double pip = ld(phi + (size_t)k * P + rowoff + ip);
-        const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
-        const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
-        const double l0 = loc, im_ = pim, jm_ = pjm, km_ = pkm;
-        const double be = f.st->beta;
-        const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
-        f.pr[o] = f.pr[o] + l0 - be * ((pip - 2.0 * l0 + im_) * ld(c.udx1qm + k) +
-                                       (pjp - 2.0 * l0 + jm_) * dxzq +
-                                       (pkp * app + l0 * acc + km_ * amm));
+        if (std::is_same<T, double>::value) {
+            const double pip = ld(phi + (size_t)k * P + rowoff + ip);
+            const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+            const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+            const double l0 = loc, im_ = pim, jm_ = pjm, km_ = pkm;
+            const double be = f.st->beta;
+            const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
+            f.pr[o] = f.pr[o] + l0 - be * ((pip - 2.0 * l0 + im_) * ld(c.udx1qm + k) +
+                                           (pjp - 2.0 * l0 + jm_) * dxzq +
+                                           (pkp * app + l0 * acc + km_ * amm));
+        } else {
+            // mixed path: the increment phi - beta lap(phi) from the FP32 phi in
+            // FP32, accumulated into the FP64 pressure; the FP32 copy used by
+            // the momentum rhs is refreshed from the FP64 sum
+            const T pip = ld(phi + (size_t)k * P + rowoff + ip);
+            const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+            const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+            const T be = (T)f.st->beta;
+            const T app = (T)ld(c.apph + k), acc = (T)ld(c.acph + k), amm = app;   // amm = apph(kc)
+            const T two = (T)2.0;
+            const T inc = loc - be * ((pip - two * loc + pim) * (T)ld(c.udx1qm + k) +
+                                      (pjp - two * loc + pjm) * (T)dxzq +
+                                      (pkp * app + loc * acc + pkm * amm));
+            const double p = f.pr[o] + (double)inc;
+            f.pr[o] = p;
+            f.prf[o] = (T)p;
+        }
     }
 }
 
@@ -823,7 +843,14 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, do
         const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
         const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
         double v;
-        if (which == 0) {
+        if (which == 0 && !std::is_same<T, double>::value) {
+            // CalcMaxCFL of the mixed path in FP32 (the max itself is exact)
+            const T h = (T)0.5;
+            const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * (T)ld(c.usrm + k)));
+            const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * (T)ld(c.udx2rm + k)));
+            const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
+            v = (double)(vt + vr + vz);
+        } else if (which == 0) {
             v = fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
                 fabs((z1 + z0) * 0.5 * dxz);
         } else {
@@ -1001,6 +1028,11 @@ __global__ void to_host_kernel(Dims d, const T* src, double* stage, int nk, int 
     }
 }
 
+__global__ void round_kernel(const double* src, float* dst, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = (float)src[t];
+}
+
 // FP64 FMA throughput probe: 8 independent FMA chains per thread.
 __global__ void fp64_probe_kernel(double* out, int iters, double b, double c) {
     double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
@@ -1049,6 +1081,11 @@ double measure_fp64_peak(cudaStream_t s) {
 
 int reduction_blocks() { return kRedBlocks; }
 
+void launch_round_to_float(cudaStream_t s, const double* src, float* dst, long long n) {
+    round_kernel<<<1216, 256, 0, s>>>(src, dst, n);
+    TC_LAUNCH_CHECK();
+}
+
 int theta_rows(int M) {
     int R = 1;
     while (R < 32 && (R * 2) * M <= 512) R *= 2;
@@ -1081,7 +1118,7 @@ template <typename T>
 void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c, const Consts& k,
                      const FieldsT<T>& f, int sub) {
     MomArgs<T> a;
-    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.pr;
+    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.prf;
     a.ru1 = f.ru1; a.ru2 = f.ru2; a.ru3 = f.ru3;
     a.rhs_t = f.rhs_t; a.rhs_r = f.rhs_r; a.rhs_z = f.rhs_z;
     a.h_t = f.h_t; a.h_r = f.h_r; a.h_z = f.h_z;

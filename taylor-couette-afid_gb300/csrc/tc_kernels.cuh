@@ -15,6 +15,7 @@ template <typename T>
 struct FieldsT {
     T *qt, *qr, *qz;
     double* pr;                       // pressure is FP64 in both paths
+    T* prf;                           // pr rounded to T for the momentum rhs (aliases pr when T = double)
     T* phi;
     T *ru1, *ru2, *ru3;
     T *rhs_t, *rhs_r, *rhs_z;
@@ -93,6 +94,9 @@ template <typename T>
 void launch_to_device(cudaStream_t s, const Dims& d, const double* stage, T* dst, int nk, int halo);
 template <typename T>
 void launch_to_host(cudaStream_t s, const Dims& d, const T* src, double* stage, int nk, int halo);
+
+// dst[i] = (float)src[i], i < n.
+void launch_round_to_float(cudaStream_t s, const double* src, float* dst, long long n);
 
 // Dense FP64 FMA rate of the current device in TFLOP/s (measurement helper).
 double measure_fp64_peak(cudaStream_t s);
