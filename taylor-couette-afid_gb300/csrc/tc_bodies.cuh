@@ -1,0 +1,674 @@
+// tc_bodies.cuh -- device bodies of the step kernels, written against
+// explicit indices so that the single-instance kernels (tc_kernels.cu) and the
+// grouped ensemble kernels (tc_batch.cu) run the same arithmetic.
+//
+// Velocity-side bodies are templates on the element type T: double gives the
+// plain FP64 path, float the mixed path (velocities, explicit terms, momentum
+// sweeps and FFTs in FP32; pressure tridiagonals, pressure accumulation and
+// reductions in FP64).
+#pragma once
+
+#include <type_traits>
+
+#include "tc_fft.cuh"
+#include "tc_kernels.cuh"
+
+namespace tcgb {
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 304;   // 2 x 152 SMs
+constexpr int kZC = 4;            // lines per z-FFT block
+
+__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
+template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
+
+
+// --------------------------------------------------------------------------
+// Step control
+// --------------------------------------------------------------------------
+
+// mode 0: dt and time given by the host (tc_time_marcher / tc_begin_step).
+// mode 1: main.F90:156-174 -- dt from the CFL number of the current field.
+__device__ void begin_step_body(const Consts& k, StepState* st, int mode, double dt_h, double time_h) {
+    double dt, time;
+    if (mode == 0) {
+        dt = dt_h;
+        time = time_h;
+        st->halt = 0;
+        st->errorcode = 0;
+    } else {
+        if (st->halt) return;
+        int err = 0;
+        double cfl = st->instcfl;
+        time = st->time;
+        if (k.idtv == 1) {
+            if (st->ntime > 1) {
+                dt = (cfl < 1.0e-8) ? k.dtmax : k.limitCFL / cfl;
+                if (dt > k.dtmax) dt = k.dtmax;
+            } else {
+                dt = k.dtmin;
+            }
+            if (dt < k.dtmin) err = 166;
+        } else {
+            // IDTV=0: the reference never assigns dt; run with dt = DTMAX.
+            dt = k.dtmax;
+            if (cfl * dt > k.limitCFL) err = 165;
+        }
+        st->errorcode = err;
+    }
+    st->dt = dt;
+    st->time = time;
+    st->beta = dt / k.ren * 0.5;                                                  // TimeMarcher.F90:20
+    st->vinner_t = k.sizepert * sin(2.0 * k.pi * k.omegapert * time);             // InnerCylVelocity.F90:15
+    st->dvinner_t = 2.0 * k.pi * k.omegapert * k.sizepert * cos(2.0 * k.pi * k.omegapert * time) * dt;
+}
+
+// Row-scaled momentum matrices of SolveImpEqnUpdate_QT/QR/QZ and their LU
+// factors for every substep of the step (dgttrf without row interchanges:
+// the matrices are diagonally dominant), plus the per-substep correction
+// coefficients of CorrectVelocity and the CalcLocalDivergence scale.  All in
+// FP64 (Fd, corrd); for the mixed path the results are then rounded into the
+// FP32 copies F, corr.  One block.
+template <typename T>
+__device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, const StepState* st,
+                             const MomFactorsT<double>& Fd, double* corrd, double* scal, const MomFactorsT<T>& F,
+                             T* corr) {
+    const int nr = d.nr;
+    const double beta = st->beta, dt = st->dt;
+    const int nsub = k.nsst;
+    // phase 1: row entries (parallel over rows)
+    for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
+        int row = t % nr, chain = t / nr;        // chain: 0,1 = qt v0/v1; 2 = qr; 3,4 = qz v0/v1
+        int s = chain / 5, ch = chain % 5;
+        double betadx = beta * k.alm[s];
+        if (ch == 0 || ch == 1 || ch == 3 || ch == 4) {
+            bool qt = ch < 2;
+            int v = (ch == 1 || ch == 4) ? 1 : 0;
+            double fic = v == 0 ? 1.0 : 0.0, foc = 1.0;
+            const double* ac = qt ? c.ac1j : c.ac3j;
+            const double* am = qt ? c.am1j : c.am3j;
+            const double* ap = qt ? c.ap1j : c.ap3j;
+            double acfs0 = qt ? k.ac1j_fs0 : k.ac3j_fs0, acfs1 = qt ? k.ac1j_fs1 : k.ac3j_fs1;
+            double acr = ac[row];
+            if (row == 0) acr = ac[0] * fic + acfs0 * (1.0 - fic);
+            else if (row == nr - 1) acr = ac[nr - 1] * foc + acfs1 * (1.0 - foc);
+            double ackl_b = 1.0 / (1.0 - acr * betadx);
+            int cidx = qt ? 0 : 2;
+            Fd.l(s, cidx, v)[row] = row > 0 ? -am[row] * betadx * ackl_b : 0.0;        // amkl
+            Fd.u(s, cidx, v)[row] = row < nr - 1 ? -ap[row] * betadx * ackl_b : 0.0;   // apkl
+            if (v == 0) Fd.scale(s, cidx)[row] = 1.0 / (1.0 - ac[row] * betadx);
+        } else {
+            // qr faces 1..nr-1; rows 0 and nr are identity rows
+            double ackl_b = (row >= 1) ? 1.0 / (1.0 - c.ac2j[row] * betadx) : 1.0;
+            Fd.l(s, 1, 0)[row] = row >= 1 ? -c.am2j[row] * betadx * ackl_b : 0.0;
+            Fd.u(s, 1, 0)[row] = row >= 1 ? -c.ap2j[row] * betadx * ackl_b : 0.0;
+            Fd.scale(s, 1)[row] = ackl_b;
+        }
+        // CorrectVelocity.F90:325-330 coefficients
+        if (ch == 0) {
+            corrd[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
+            corrd[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
+            if (row == 0) corrd[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
+        }
+    }
+    __syncthreads();
+    // phase 2: sequential elimination, one thread per chain
+    if (threadIdx.x < nsub * 5) {
+        int s = threadIdx.x / 5, ch = threadIdx.x % 5;
+        int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
+        int v = (ch == 1 || ch == 4) ? 1 : 0;
+        double* l = Fd.l(s, cidx, v);
+        double* u = Fd.u(s, cidx, v);
+        double* di = Fd.dinv(s, cidx, v);
+        int k0 = (cidx == 1) ? 1 : 0;
+        double dp = 1.0;
+        di[k0] = 1.0;
+        if (cidx == 1) l[1] = 0.0;   // couples to the wall value qr(1) = 0
+        for (int row = k0 + 1; row < nr; ++row) {
+            double fact = l[row] / dp;
+            l[row] = fact;
+            dp = 1.0 - fact * u[row - 1];
+            di[row] = dp;
+        }
+    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + nsub) {
+        int s = threadIdx.x - 32;
+        // SolveImpEqnUpdate_QT.F90:67
+        *Fd.extra(s) = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
+        // CalcLocalDivergence.F90:19 usdt, alone and times the FFT normalisation
+        const double usdt = 1.0 / (k.alm[s] * dt);
+        scal[s] = usdt * k.fft_norm;
+        scal[3 + s] = usdt;
+    }
+    __syncthreads();
+    // phase 3: reciprocals of the pivots
+    for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
+        int row = t % nr, chain = t / nr;
+        int s = chain / 5, ch = chain % 5;
+        int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
+        int v = (ch == 1 || ch == 4) ? 1 : 0;
+        if (cidx == 1 && row == 0) continue;
+        double* di = Fd.dinv(s, cidx, v);
+        di[row] = 1.0 / di[row];
+    }
+    // phase 4 (mixed path): round the factors into the FP32 copies
+    if (!std::is_same<T, double>::value) {
+        __syncthreads();
+        const int nF = (int)MomFactorsT<T>::count(F.stride), nC = 9 * (nr + 1);
+        for (int t = threadIdx.x; t < nF; t += blockDim.x) F.base[t] = (T)Fd.base[t];
+        for (int t = threadIdx.x; t < nC; t += blockDim.x) corr[t] = (T)corrd[t];
+    }
+}
+
+struct Stencil {
+    int i, j, k, im, ip, jm, jp;
+    size_t P;
+    int nt;
+    __device__ size_t at(int kk, int jj, int ii) const { return (size_t)kk * P + (size_t)jj * nt + ii; }
+};
+
+// Scalars of the momentum kernel in the element type T.
+template <typename T>
+struct MomArgs {
+    const T *qt, *qr, *qz;
+    const T* pr;            // pressure in the element type (FP32 copy on the mixed path)
+    T *ru1, *ru2, *ru3, *rhs_t, *rhs_r, *rhs_z, *h_t, *h_r, *h_z;
+    const signed char* icyl;
+    const StepState* st;
+    T al, ga, ro, alre, dxt_al, dxz_al;
+    T udxz, udxzq, q_romeg, virotint, virotext;
+    T ac1j_fs0, am1j_fs0, ap1j_fs1, ac1j_fs1, ac3j_fs0, am3j_fs0, ap3j_fs1, ac3j_fs1;
+    int use_ru;
+};
+
+// ExplicitTermsQT.F90:40-125 at cell (i, j, k)
+template <typename T>
+__device__ T explicit_qt(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
+    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip)), t_im = ld(qt + S.at(k, S.j, S.im));
+    T t_jp = ld(qt + S.at(k, S.jp, S.i)), t_jm = ld(qt + S.at(k, S.jm, S.i));
+    T t_kp = ld(qt + S.at(kpp, S.j, S.i)), t_km = ld(qt + S.at(kmm, S.j, S.i));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_im = ld(qr + S.at(k, S.j, S.im));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pim = ld(qr + S.at(kp, S.j, S.im));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_im = ld(qz + S.at(k, S.j, S.im));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
+    const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
+    const T two = (T)2.0;
+    T h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
+    const T rp2 = r_p + r_pim, rc2 = r_c + r_im;
+    T h12d = (rp2 * (t_kp + t_c) - rc2 * (t_c + t_km)) * ld(c.q_udx2rm + k);
+    T h12n = t_c * ld(c.q_usrm + k) * (rp2 * usrcp + rc2 * usrc);
+    T h13 = ((z_jp + z_jpim) * (t_jp + t_c) - (z_c + z_im) * (t_c + t_jm)) * A.udxz;
+    T d11qt = (t_ip - two * t_c + t_im) * udxtq;
+    T d22qt = (t_jp - two * t_c + t_jm) * A.udxzq;
+    T qre = r_p * usrcp + r_c * usrc;
+    T qrw = r_pim * usrcp + r_im * usrc;
+    T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
+    T coriol = -(rc2 * usrc + rp2 * usrcp) * A.q_romeg;
+    return -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
+}
+
+// ExplicitTermsQR.F90:180-280 at face (i, j, k), 1 <= k <= nr-1
+template <typename T>
+__device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
+    const int k = S.k, km = k - 1, kp = k + 1;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_m = ld(qt + S.at(km, S.j, S.i));
+    T t_ip = ld(qt + S.at(k, S.j, S.ip)), t_mip = ld(qt + S.at(km, S.j, S.ip));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_ip = ld(qr + S.at(k, S.j, S.ip)), r_im = ld(qr + S.at(k, S.j, S.im));
+    T r_jp = ld(qr + S.at(k, S.jp, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_m = ld(qr + S.at(km, S.j, S.i));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_mjp = ld(qz + S.at(km, S.jp, S.i));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
+    const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
+    const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
+    const T two = (T)2.0;
+    T a = (t_ip + t_mip + t_c + t_m) * (T)0.25;
+    T h11n = a * a;
+    T h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
+    T h22 = ((r_p * usrcp + r_c * usrc) * (r_p + r_c) - (r_c * usrc + r_m * usrcm) * (r_c + r_m)) * ld(c.q_udx2c + k);
+    T h23 = ((z_jp + z_mjp) * (r_jp + r_c) - (z_c + z_m) * (r_c + r_jm)) * A.udxz;
+    T d11qre = -((t_ip + t_mip) - (t_c + t_m)) * ld(c.udx1vis2 + k);
+    T d11qr = (r_ip - two * r_c + r_im) * udxtq;
+    T d22qr = (r_jp - two * r_c + r_jm) * A.udxzq;
+    T coriol = (t_c + t_ip + t_m + t_mip) * ld(c.q_rc_romeg + k);
+    return -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
+}
+
+// ExplicitTermsQZ.F90:328-390 at cell (i, j, k)
+template <typename T>
+__device__ T explicit_qz(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
+    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
+    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
+    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip));
+    T t_jm = ld(qt + S.at(k, S.jm, S.i)), t_jmip = ld(qt + S.at(k, S.jm, S.ip));
+    T z_c = ld(qz + S.at(k, S.j, S.i)), z_ip = ld(qz + S.at(k, S.j, S.ip)), z_im = ld(qz + S.at(k, S.j, S.im));
+    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jm = ld(qz + S.at(k, S.jm, S.i));
+    T z_kp = ld(qz + S.at(kpp, S.j, S.i)), z_km = ld(qz + S.at(kmm, S.j, S.i));
+    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
+    T r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+    const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+    const T two = (T)2.0;
+    T h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
+    T h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.q_udx2rm + k);
+    T h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * A.udxz;
+    T dqz1 = (z_im - two * z_c + z_ip) * udxtq;
+    T dqz2 = (z_jm - two * z_c + z_jp) * A.udxzq;
+    return -(h31 + h32 + h33) + dqz1 + dqz2;
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
+                                              int k) {
+    const int nr = d.nr;
+    Stencil S;
+    S.i = i; S.j = j; S.k = k; S.nt = d.nt; S.P = (size_t)d.P;
+    S.im = wm(i, d.nt); S.ip = wp(i, d.nt); S.jm = wm(j, d.nz); S.jp = wp(j, d.nz);
+    const size_t o = S.at(k, j, i);
+    T ht = 0, hr = 0, hz = 0;
+    if (MODE != MODE_IMPLICIT) {
+        ht = explicit_qt(S, nr, c, a);
+        if (k >= 1) hr = explicit_qr(S, c, a);
+        hz = explicit_qz(S, nr, c, a);
+        if (MODE == MODE_EXPLICIT) {
+            a.h_t[o] = ht;
+            if (k >= 1) a.h_r[o] = hr;
+            a.h_z[o] = hz;
+            return;
+        }
+    } else {
+        ht = a.h_t[o];
+        if (k >= 1) hr = a.h_r[o];
+        hz = a.h_z[o];
+    }
+    const T dt = (T)a.st->dt, ga = a.ga, ro = a.ro, alre = a.alre;
+    const T one = (T)1.0;
+    const T fic = a.icyl ? (T)a.icyl[(size_t)j * d.nt + i] : one, foc = one;
+    const T* qt = a.qt;
+    const T* qr = a.qr;
+    const T* qz = a.qz;
+    const T* pr = a.pr;
+    const T p_c = ld(pr + o);
+    // ---- qt (ImplicitAndUpdateQT.F90:45-115)
+    {
+        T d33;
+        if (k == 0) {
+            T app = ld(c.ap1j);
+            T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
+            T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
+            d33 = ld(qt + S.at(1, j, i)) * app + ld(qt + o) * acc + (a.virotint + (T)a.st->vinner_t) * amm;
+        } else if (k == nr - 1) {
+            T amm = ld(c.am1j + k);
+            T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
+            T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
+            d33 = a.virotext * app + ld(qt + o) * acc + ld(qt + S.at(k - 1, j, i)) * amm;
+        } else {
+            d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
+                  ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
+        }
+        T dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
+        T old = a.use_ru ? a.ru1[o] : (T)0;
+        a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
+        a.ru1[o] = ht;
+    }
+    // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
+    if (k >= 1) {
+        T d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
+                ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
+        T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
+        T dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
+        T old = a.use_ru ? a.ru2[o] : (T)0;
+        a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
+        a.ru2[o] = hr;
+    }
+    // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
+    {
+        T d33;
+        if (k == 0) {
+            T app = ld(c.ap3j);
+            T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
+            T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
+            T q0 = ld(qz + o);
+            d33 = ld(qz + S.at(1, j, i)) * app + q0 * acc + q0 * amm;
+        } else if (k == nr - 1) {
+            T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
+            T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
+            T q0 = ld(qz + o);
+            d33 = q0 * app + q0 * acc + ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+        } else {
+            d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
+                  ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+        }
+        T dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
+        // At the outer wall the reference has already replaced ru3(nrm) by
+        // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
+        T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
+        a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
+        a.ru3[o] = hz;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f, int sub, long long col) {
+    const int nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
+    const MomFactorsT<T>& F = f.F;
+    // qt: SolveImpEqnUpdate_QT.F90:65-78
+    {
+        const T *l = F.l(sub, 0, v), *di = F.dinv(sub, 0, v), *u = F.u(sub, 0, v), *sc = F.scale(sub, 0);
+        T* rhs = f.rhs_t + col;
+        T* q = f.qt + col;
+        T y = (rhs[0] + *F.extra(sub)) * ld(sc);
+        rhs[0] = y;
+        for (int k = 1; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        T x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 0; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+    // qr: SolveImpEqnUpdate_QR.F90:136-150, faces 1..nr-1
+    {
+        const T *l = F.l(sub, 1, 0), *di = F.dinv(sub, 1, 0), *u = F.u(sub, 1, 0), *sc = F.scale(sub, 1);
+        T* rhs = f.rhs_r + col;
+        T* q = f.qr + col;
+        T y = rhs[P] * ld(sc + 1);
+        rhs[P] = y;
+        for (int k = 2; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        T x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 1; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+    // qz: SolveImpEqnUpdate_QZ.F90:214-224
+    {
+        const T *l = F.l(sub, 2, v), *di = F.dinv(sub, 2, v), *u = F.u(sub, 2, v), *sc = F.scale(sub, 2);
+        T* rhs = f.rhs_z + col;
+        T* q = f.qz + col;
+        T y = rhs[0] * ld(sc);
+        rhs[0] = y;
+        for (int k = 1; k < nr; ++k) {
+            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
+            rhs[k * P] = y;
+        }
+        T x = y * ld(di + nr - 1);
+        q[(nr - 1) * P] += x;
+        for (int k = nr - 2; k >= 0; --k) {
+            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
+            q[k * P] += x;
+        }
+    }
+}
+
+__device__ __forceinline__ double2 ld2(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }
+__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+
+// CalcLocalDivergence.F90:27-40 for cells 2m and 2m+1 of row (k, j).
+template <typename T>
+__device__ __forceinline__ typename V2<T>::type div_pair(const Dims& d, const CoefT<T>& c, T dxt, T dxz,
+                                                         const T* qt, const T* qr, const T* qz,
+                                                         int k, int j, int m) {
+    const size_t P = (size_t)d.P;
+    const int nt = d.nt;
+    const size_t row = (size_t)k * P + (size_t)j * nt;
+    const int i0 = 2 * m, i2 = (2 * m + 2 == nt) ? 0 : 2 * m + 2;
+    auto t01 = ld2(qt + row + i0);
+    T t2 = ld(qt + row + i2);
+    auto r0 = ld2(qr + row + i0);
+    auto r1 = ld2(qr + row + P + i0);
+    const int jp = wp(j, d.nz);
+    auto z0 = ld2(qz + row + i0);
+    auto z1 = ld2(qz + (size_t)k * P + (size_t)jp * nt + i0);
+    const T udx2m = ld(c.udx2m + k), usrm = ld(c.usrm + k);
+    T a = ((t01.y - t01.x) * dxt + (r1.x - r0.x) * udx2m) * usrm + (z1.x - z0.x) * dxz;
+    T b = ((t2 - t01.y) * dxt + (r1.y - r0.y) * udx2m) * usrm + (z1.y - z0.y) * dxz;
+    return mk2(a, b);
+}
+
+// Forward transform of R rows.  FROM_PHI: the rows come from the phi array
+// (CalcLocalDivergence already ran); otherwise the divergence is computed on
+// the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
+template <bool FROM_PHI, int R, typename T>
+__device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f, const FFTPlan& pl,
+                             const typename V2<T>::type* tw, const typename V2<T>::type* twr, double fft_norm,
+                             int sub, long long row0, typename V2<T>::type* smem) {
+    typedef typename V2<T>::type C2;
+    const int M = pl.n;
+    C2* a = smem;
+    C2* b = smem + (size_t)R * M;
+    const long long nrows = (long long)d.nr * d.nz;
+    // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in
+    const T scl = (T)(FROM_PHI ? fft_norm : f.scal[sub]);
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, m = t - r * M;
+        const long long row = row0 + r;
+        C2 z = mk2((T)0, (T)0);
+        if (row < nrows) {
+            const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
+            if (FROM_PHI) z = ld2(f.phi + (size_t)row * d.nt + 2 * m);
+            else z = div_pair(d, c, dxt, dxz, f.qt, f.qr, f.qz, k, j, m);
+            z.x *= scl;
+            z.y *= scl;
+        }
+        a[m * R + r] = z;
+    }
+    __syncthreads();
+    const C2* Z = fft_lines<R>(a, b, pl, tw, false);
+    // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
+    const int PH = M + 1;
+    for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
+        const int r = t / PH, kt = t - r * PH;
+        const long long row = row0 + r;
+        if (row >= nrows) continue;
+        const int k1 = kt == M ? 0 : kt, k2 = kt == 0 ? 0 : M - kt;
+        C2 zk = Z[k1 * R + r], zc = cconj(Z[k2 * R + r]);
+        C2 e = cadd(zk, zc), o = csub(zk, zc);
+        C2 w = __ldg(twr + kt);
+        C2 wo = cmul(w, o);
+        // - i * wo = (wo.y, -wo.x)
+        f.spec[(size_t)row * PH + kt] = mk2(e.x + wo.y, e.y - wo.x);
+    }
+}
+
+// Complex FFT along z of kZC consecutive kt columns of one r-plane.
+template <typename T>
+__device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
+                          int inv, int kt0, int kplane, typename V2<T>::type* smem) {
+    typedef typename V2<T>::type C2;
+    const int nz = pl.n, PH = d.PH;
+    C2* a = smem;
+    C2* b = smem + (size_t)kZC * nz;
+    C2* plane = f.spec + (size_t)kplane * d.PS;
+    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
+        const int c = t % kZC, j = t / kZC;
+        a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
+    }
+    __syncthreads();
+    const C2* Z = fft_lines<kZC>(a, b, pl, tw, inv != 0);
+    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
+        const int c = t % kZC, j = t / kZC;
+        if (kt0 + c < PH) plane[(size_t)j * PH + kt0 + c] = Z[t];
+    }
+}
+
+__device__ __forceinline__ double2 to_d2(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ void st2(double2* p, double x, double y) { *p = make_double2(x, y); }
+__device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_float2((float)x, (float)y); }
+
+// SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
+// matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
+// right-hand side, with the precomputed LU factors, in FP64.  One thread per
+// pair of modes (kz, nzm-kz) that share a matrix.  The forward-sweep partial
+// results go to the FP64 array ws: the spectrum itself for the FP64 path, a
+// separate scratch for the mixed path, so the FP32 spectrum is rounded once.
+template <typename T>
+__device__ __forceinline__ void ptri_mode(const Dims& d, const Coef& c, const FieldsT<T>& f, double2* ws, long long t) {
+    typedef typename V2<T>::type C2;
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const bool two = (kz != 0) && (2 * kz != d.nz);
+    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
+    const size_t o1 = (size_t)kz * PH + kt, o2 = (size_t)(two ? d.nz - kz : kz) * PH + kt;
+    C2* x1 = f.spec + o1;
+    C2* x2 = f.spec + o2;
+    double2* w1 = ws + o1;
+    double2* w2 = ws + o2;
+    const double* L = f.pf_l + t;
+    const double* DI = f.pf_dinv + t;
+    double2 y1 = to_d2(x1[0]), y2 = two ? to_d2(x2[0]) : make_double2(0.0, 0.0);
+    w1[0] = y1;
+    if (two) w2[0] = y2;
+#pragma unroll 4
+    for (int k = 1; k < nr; ++k) {
+        const double l = ld(L + k * FS);
+        double2 b1 = to_d2(x1[k * PS]);
+        y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
+        w1[k * PS] = y1;
+        if (two) {
+            double2 b2 = to_d2(x2[k * PS]);
+            y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
+            w2[k * PS] = y2;
+        }
+    }
+    double di = ld(DI + (size_t)(nr - 1) * FS);
+    double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
+    st2(x1 + (size_t)(nr - 1) * PS, s1.x, s1.y);
+    if (two) st2(x2 + (size_t)(nr - 1) * PS, s2.x, s2.y);
+#pragma unroll 4
+    for (int k = nr - 2; k >= 0; --k) {
+        const double u = ld(c.apph + k);
+        di = ld(DI + k * FS);
+        double2 b1 = w1[k * PS];
+        s1 = make_double2((b1.x - u * s1.x) * di, (b1.y - u * s1.y) * di);
+        st2(x1 + k * PS, s1.x, s1.y);
+        if (two) {
+            double2 b2 = w2[k * PS];
+            s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
+            st2(x2 + k * PS, s2.x, s2.y);
+        }
+    }
+}
+
+// Inverse real FFT along theta: spec rows -> phi rows.
+template <int R, typename T>
+__device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
+                           const typename V2<T>::type* twr, long long row0, typename V2<T>::type* smem) {
+    typedef typename V2<T>::type C2;
+    const int M = pl.n, PH = M + 1;
+    C2* a = smem;
+    C2* b = smem + (size_t)R * M;
+    const long long nrows = (long long)d.nr * d.nz;
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, kt = t - r * M;
+        const long long row = row0 + r;
+        C2 z = mk2((T)0, (T)0);
+        if (row < nrows) {
+            const C2* X = f.spec + (size_t)row * PH;
+            C2 xk = X[kt], xm = X[M - kt];
+            if (kt == 0) { xk.y = 0; xm.y = 0; }   // imaginary parts of the 0 and Nyquist bins
+            C2 xc = cconj(xm);
+            C2 e = cadd(xk, xc), o = csub(xk, xc);
+            C2 w = cconj(__ldg(twr + kt));
+            C2 wo = cmul(w, o);
+            // Z = e + i wo
+            z = mk2(e.x - wo.y, e.y + wo.x);
+        }
+        a[kt * R + r] = z;
+    }
+    __syncthreads();
+    const C2* Z = fft_lines<R>(a, b, pl, tw, true);
+    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+        const int r = t / M, m = t - r * M;
+        const long long row = row0 + r;
+        if (row < nrows) *reinterpret_cast<C2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
+    }
+}
+
+template <bool VEL, bool PRES, typename T>
+__device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, double dxzq, const FieldsT<T>& f, int sub,
+                                             int i, int j, int k) {
+    const int nt = d.nt, nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const int im = wm(i, nt), ip = wp(i, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
+    const size_t rowoff = (size_t)j * nt;
+    const size_t o = (size_t)k * P + rowoff + i;
+    const T* phi = f.phi;
+    const T loc = ld(phi + o);
+    const T pim = ld(phi + (size_t)k * P + rowoff + im);
+    const T pjm = ld(phi + (size_t)k * P + (size_t)jm * nt + i);
+    const T pkm = ld(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i);
+    if (VEL) {
+        const T* cf = f.corr + (size_t)sub * 3 * (nr + 1);
+        f.qt[o] -= (loc - pim) * ld(cf + k);
+        if (k >= 1) f.qr[o] -= (loc - pkm) * ld(cf + (nr + 1) + k);
+        f.qz[o] -= (loc - pjm) * ld(cf + 2 * (nr + 1));
+    }
+    if (PRES) {
+        if (std::is_same<T, double>::value) {
+            const double pip = ld(phi + (size_t)k * P + rowoff + ip);
+            const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+            const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+            const double l0 = loc, im_ = pim, jm_ = pjm, km_ = pkm;
+            const double be = f.st->beta;
+            const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
+            f.pr[o] = f.pr[o] + l0 - be * ((pip - 2.0 * l0 + im_) * ld(c.udx1qm + k) +
+                                           (pjp - 2.0 * l0 + jm_) * dxzq +
+                                           (pkp * app + l0 * acc + km_ * amm));
+        } else {
+            // mixed path: the increment phi - beta lap(phi) from the FP32 phi in
+            // FP32, accumulated into the FP64 pressure; the FP32 copy used by
+            // the momentum rhs is refreshed from the FP64 sum
+            const T pip = ld(phi + (size_t)k * P + rowoff + ip);
+            const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+            const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+            const T be = (T)f.st->beta;
+            const T app = (T)ld(c.apph + k), acc = (T)ld(c.acph + k), amm = app;   // amm = apph(kc)
+            const T two = (T)2.0;
+            const T inc = loc - be * ((pip - two * loc + pim) * (T)ld(c.udx1qm + k) +
+                                      (pjp - two * loc + pjm) * (T)dxzq +
+                                      (pkp * app + loc * acc + pkm * amm));
+            const double p = f.pr[o] + (double)inc;
+            f.pr[o] = p;
+            f.prf[o] = (T)p;
+        }
+    }
+}
+
+
+// Scalars of the momentum kernel for substep `sub`, in the element type T.
+template <typename T>
+inline MomArgs<T> make_mom_args(const Consts& k, const FieldsT<T>& f, int sub) {
+    MomArgs<T> a;
+    a.qt = f.qt; a.qr = f.qr; a.qz = f.qz; a.pr = f.prf;
+    a.ru1 = f.ru1; a.ru2 = f.ru2; a.ru3 = f.ru3;
+    a.rhs_t = f.rhs_t; a.rhs_r = f.rhs_r; a.rhs_z = f.rhs_z;
+    a.h_t = f.h_t; a.h_r = f.h_r; a.h_z = f.h_z;
+    a.icyl = k.patterned ? f.icyl : nullptr;
+    a.st = f.st;
+    a.al = (T)k.alm[sub]; a.ga = (T)k.gam[sub]; a.ro = (T)k.rom[sub];
+    a.alre = (T)k.alre[sub]; a.dxt_al = (T)k.dxt_al[sub]; a.dxz_al = (T)k.dxz_al[sub];
+    a.udxz = (T)k.udxz; a.udxzq = (T)k.udxzq; a.q_romeg = (T)k.q_romeg;
+    a.virotint = (T)k.virotint; a.virotext = (T)k.virotext;
+    a.ac1j_fs0 = (T)k.ac1j_fs0; a.am1j_fs0 = (T)k.am1j_fs0; a.ap1j_fs1 = (T)k.ap1j_fs1; a.ac1j_fs1 = (T)k.ac1j_fs1;
+    a.ac3j_fs0 = (T)k.ac3j_fs0; a.am3j_fs0 = (T)k.am3j_fs0; a.ap3j_fs1 = (T)k.ap3j_fs1; a.ac3j_fs1 = (T)k.ac3j_fs1;
+    a.use_ru = k.rom[sub] != 0.0;
+    return a;
+}
+
+}  // namespace
+}  // namespace tcgb

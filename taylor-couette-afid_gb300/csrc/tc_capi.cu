@@ -12,40 +12,10 @@
 
 #include "../../include/tc_capi.h"
 #include "tc_grid.h"
+#include "tc_handle.h"
 #include "tc_kernels.cuh"
 
 using namespace tcgb;
-
-struct tc_handle {
-    tc_bou bou;
-    int mixed = 0;          // 0: plain FP64, 1: mixed FP32/FP64
-    Grid g;
-    Dims d;
-    Consts k;
-    Coef c;                 // FP64 coefficients (pressure, reductions, factors)
-    CoefT<float> cf;        // FP32 copies (mixed path velocity kernels)
-    FieldsT<double> fd;     // plain path state
-    FieldsT<float> ff;      // mixed path state
-    PlansT<double> pd;
-    PlansT<float> pf;
-    cudaStream_t stream = nullptr;
-    std::vector<void*> allocs;
-    double* stage = nullptr;
-    StepState* st = nullptr;        // device
-    StepState* st_host = nullptr;   // pinned mirror
-    int sub = 0;
-    long long bytes = 0;
-    std::string err;
-    // launch accounting and optional per-kernel event timing
-    long long launches = 0;
-    bool profiling = false;
-    struct Rec { int cls; cudaEvent_t a, b; };
-    std::vector<Rec> recs;
-    std::vector<cudaEvent_t> pool;
-    size_t pool_used = 0;
-    double prof_ms[16] = {0};
-    long long prof_n[16] = {0};
-};
 
 namespace {
 

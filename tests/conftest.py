@@ -31,13 +31,14 @@ def make_bou(**kw):
     return d
 
 
-def rel_err(a, b, interior=True, nk=None):
-    """max |a-b| / max |b| over the interior (no halo) cells."""
+def rel_err(a, b, interior=True, nk=None, scale=None):
+    """max |a-b| / max |b| over the interior (no halo) cells; with `scale`,
+    max |a-b| / scale instead."""
     if interior:
         a, b = a[1:-1, 1:-1], b[1:-1, 1:-1]
     if nk is not None:
         a, b = a[..., :nk], b[..., :nk]
-    den = float(np.abs(b).max())
+    den = float(np.abs(b).max()) if scale is None else float(scale)
     return float(np.abs(a - b).max()) / (den if den > 0 else 1.0)
 
 

@@ -53,9 +53,14 @@ def test_mixed_routines(gpu_lib, oracle):
     o.call("correct_velocity")
     g.correct_pressure()
     o.call("correct_pressure")
+    # The correction is the gradient of phi; its FP32 error is set by the
+    # azimuthal velocity (O(1)) that dominates the divergence, not by the
+    # small radial and axial noise, so every component is measured against
+    # the largest velocity.
     gs, os_ = g.get_state(), o.state()
+    u = float(np.abs(os_[0][1:-1, 1:-1, :32]).max())
     for a, b, nk in zip(gs[:3], os_[:3], (32, 33, 32)):
-        assert rel_err(a, b, nk=nk) < 1e-4
+        assert rel_err(a, b, nk=nk, scale=u) < 1e-4
     g.close()
 
 
