@@ -185,6 +185,30 @@ int tc_calc_torque(tc_handle* h, double* inner, double* outer);
 /* CalcVelocityStats.F90:11-68: vmax(3) and the three rms values. */
 int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3);
 
+/* CheckDivergence.F90:60-95 on velocity arrays the caller keeps on the
+ * current CUDA device, without a handle and without allocating device
+ * memory.  No counterpart in the reference.
+ *  - qt, qr, qz: device arrays in the reference layout
+ *    q(1:nrm+1, 0:nzm+1, 0:nthm+1), r fastest, periodic halos current (as
+ *    after update_halo); cells k = 1..nrm, j = 1..nzm, i = 1..nthm are read.
+ *  - udx2m, usrm: HOST arrays, entries 0..nrm-1 = udx2m(1:nrm), usrm(1:nrm)
+ *    (tc_grid_array TC_G_UDX2M, TC_G_USRM); dxt = nthm*LAMB/(2 pi),
+ *    dxz = nzm/ALX3 (dx1, dx3 of CreateGrid.F90:28-34).
+ *  - stream: cudaStream_t the work is ordered on (NULL = legacy default);
+ *    the call synchronises it and returns the maximum |div| in *qmax.
+ * Its scratch (coefficients, per-block maxima, result) is one static
+ * 130 KB device array per device, not memory of the caller's: nrm above
+ * 8192 is rejected with 2016.  Nothing in it must start at zero; every
+ * call writes what it later reads.  The first call with a device current
+ * looks the array's address up (cudaGetSymbolAddress), so make it before
+ * any stream capture.  Calls on one device share the array: calls that
+ * overlap (other streams, other host threads) race and may return each
+ * other's values; issue them one at a time. */
+int tc_check_divergence_noalloc(const double* qt, const double* qr, const double* qz,
+                                int nthm, int nzm, int nrm,
+                                const double* udx2m, const double* usrm,
+                                double dxt, double dxz, void* stream, double* qmax);
+
 /* ---- measurement helpers ------------------------------------------------ */
 
 /* Number of kernels one tc_time_marcher call launches. */

@@ -107,6 +107,8 @@ SIGNATURES = {
     "tc_correct_pressure": (ctypes.c_int, [_vp]),
     "tc_calc_max_cfl": (ctypes.c_int, [_vp, _dp]),
     "tc_check_divergence": (ctypes.c_int, [_vp, _dp]),
+    "tc_check_divergence_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                    _dp, _dp, ctypes.c_double, ctypes.c_double, _vp, _dp]),
     "tc_calc_torque": (ctypes.c_int, [_vp, _dp, _dp]),
     "tc_calc_velocity_stats": (ctypes.c_int, [_vp, _dp, _dp]),
     "tc_kernels_per_step": (ctypes.c_int, [_vp]),
@@ -158,6 +160,23 @@ def grid_array(bou: dict, name: str) -> np.ndarray:
     if rc < 0:
         raise TCError(-rc, lib().tc_last_error(None).decode())
     return out[:rc].copy()
+
+
+def check_divergence_noalloc(qt: int, qr: int, qz: int, nthm: int, nzm: int, nrm: int, udx2m: np.ndarray,
+                             usrm: np.ndarray, dxt: float, dxz: float, stream: int = 0) -> float:
+    """CheckDivergence on caller-owned device arrays (addresses of FP64
+    arrays in the reference layout, periodic halos current) with no handle
+    and no device allocation; udx2m and usrm are host arrays of nrm
+    entries.  Calls on one device must not overlap."""
+    u = np.ascontiguousarray(udx2m[:nrm], dtype=np.float64)
+    m = np.ascontiguousarray(usrm[:nrm], dtype=np.float64)
+    v = ctypes.c_double()
+    L = lib()
+    rc = L.tc_check_divergence_noalloc(qt, qr, qz, nthm, nzm, nrm, _dptr(u), _dptr(m), dxt, dxz, stream,
+                                       ctypes.byref(v))
+    if rc != 0:
+        raise TCError(rc, L.tc_last_error(None).decode())
+    return v.value
 
 
 PREC_FP64, PREC_MIXED = 0, 1

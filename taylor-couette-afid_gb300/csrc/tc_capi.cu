@@ -186,6 +186,11 @@ void set_coef_ptrs(CoefT<T>& c, const T* base, int lenK) {
 
 }  // namespace
 
+// Message for tc_last_error(NULL) from the other translation units.
+namespace tcgb {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace tcgb
+
 // The exported functions below are declared extern "C" in tc_capi.h, which
 // gives these definitions C linkage.
 

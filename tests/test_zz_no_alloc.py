@@ -1,0 +1,66 @@
+"""tc_check_divergence_noalloc: the divergence check on caller-owned device
+arrays, with its scratch in a static device array, against the handle's
+tc_check_divergence on the same state, two calls in a row.  This file is
+collected last so that it also runs after every other GPU test."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import make_bou, tc
+
+import tc_gb300.initial as ini
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_copy(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda:0")
+
+
+@pytest.mark.parametrize("case", [
+    dict(nthm=48, nzm=40, nrm=32, istr=6, str=3.0),
+    dict(nthm=64, nzm=48, nrm=96, istr=6, str=20.0),
+], ids=["48x40x32", "64x48x96"])
+def test_noalloc_divergence_matches_handle(gpu_lib, case):
+    import torch
+    bou = make_bou(**case)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*ini.couette_noise(bou, seed=11))
+    g.run(3, 0, 0.0)                       # a projected, nearly solenoidal field
+    qt, qr, qz, _ = g.get_state()          # reference layout, halos filled
+    want = g.check_divergence()
+    nthm, nzm, nrm = bou["nthm"], bou["nzm"], bou["nrm"]
+    udx2m, usrm = tc.grid_array(bou, "udx2m"), tc.grid_array(bou, "usrm")
+    dxt = nthm * bou["lamb"] / (2.0 * math.pi)
+    dxz = nzm / bou["alx3"]
+    dq = [_device_copy(a) for a in (qt, qr, qz)]
+    torch.cuda.synchronize()
+    got = [tc.check_divergence_noalloc(dq[0].data_ptr(), dq[1].data_ptr(), dq[2].data_ptr(), nthm, nzm, nrm,
+                                       udx2m, usrm, dxt, dxz) for _ in range(2)]
+    assert want > 0.0
+    for v in got:
+        assert abs(v - want) <= 1e-12 * want
+    # a raw, unprojected field: large divergence, same agreement
+    st = ini.couette_noise(bou, seed=12, amp=0.5)
+    g.set_state(*st)
+    want = g.check_divergence()
+    qt, qr, qz, _ = g.get_state()
+    dq = [_device_copy(a) for a in (qt, qr, qz)]
+    torch.cuda.synchronize()
+    got = [tc.check_divergence_noalloc(dq[0].data_ptr(), dq[1].data_ptr(), dq[2].data_ptr(), nthm, nzm, nrm,
+                                       udx2m, usrm, dxt, dxz) for _ in range(2)]
+    for v in got:
+        assert abs(v - want) <= 1e-12 * want
+    g.close()
+
+
+def test_noalloc_rejects_too_many_radial_cells(gpu_lib):
+    import torch
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda:0")
+    coef = np.ones(8193)
+    with pytest.raises(tc.TCError) as e:
+        tc.check_divergence_noalloc(buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), 4, 4, 8193, coef, coef,
+                                    1.0, 1.0)
+    assert e.value.code == 2016 and "8192" in str(e.value)
