@@ -51,6 +51,7 @@ WORKLOADS = {
                idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=1e-3),
     "C3": dict(nthm=1024, nzm=768, nrm=512, istr=6, str=20.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
                dtmin=1e-5, dtmax=1e-3),
+    "C5": {},     # serving loop (run_serving)
 }
 DESCR = {
     "C2": "512x512x384 theta x z x r, wall-clustered radial grid ISTR=6 STR3=20, RINT=1 REXT=1.4, 1/NU=5000, "
@@ -58,6 +59,7 @@ DESCR = {
     "C1": "64x64x64, ISTR=0, RINT=1 REXT=1.4, 1/NU=1000, RK3, dt=1e-3, seeded Couette+noise 0.01",
     "P2": "512x512x128 (profiling size of C2), ISTR=6 STR3=20, 1/NU=5000, RK3, variable dt",
     "C3": "1024x768x512, ISTR=6 STR3=20, ROTP=0.1, 1/NU=2e4, RK3, variable dt CFLMAX=1.2 DTMAX=1e-3 (FP64 form)",
+    "C5": "serving loop",
 }
 
 # Algorithmic HBM bytes per cell and launch of each kernel class (FP64):
@@ -225,6 +227,126 @@ def run_reference(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+def ensemble_legs(tc, torch, stream, steps: int, warmup: int, n_inst: int = 96, seed: int = 2024):
+    """The batched-ensemble workload: n_inst instances with grids drawn from
+    {32,48,64,96,128}^3, radius ratio in [0.5, 0.9], 1/NU log-uniform in
+    [500, 5000], fixed dt at CFL 0.8 of the start; FP64 and mixed ensembles
+    advanced by one CUDA graph of grouped launches per step, tile shapes from
+    the autotuner.  Both forms use the FP64 form's dt per instance, so the
+    mixed torque is compared with the FP64 torque after the same steps."""
+    import tc_gb300.autotune as at
+    import tc_gb300.initial as ini
+    import tc_gb300.serving as sv
+    bous = sv.draw_ensemble(n_inst, seed)
+    states = [ini.couette_noise(b, seed=seed + i) for i, b in enumerate(bous)]
+    out = {"instances": n_inst, "cells": int(sum(b["nthm"] * b["nzm"] * b["nrm"] for b in bous)),
+           "grids": "drawn from {32,48,64,96,128}^3", "steps_timed": steps, "warmup": warmup}
+    dts = None
+    torques = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        (thr, rows), table = at.tune(prec, bous, states, steps=2)
+        tune_s = time.perf_counter() - t0
+        ens = tc.Ensemble(prec)
+        ens.set_stream(stream.cuda_stream)
+        ens.tune(thr, rows)
+        slots = [ens.add(b, st, nsteps=300, dt=(dts[i] if dts else 0.0)) for i, (b, st) in
+                 enumerate(zip(bous, states))]
+        if dts is None:
+            dts = [ens.status_full(sl)[2] for sl in slots]
+        ens.step(warmup)
+        torch.cuda.synchronize()
+        n0 = ens.launch_count
+        e0.record(stream)
+        ens.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        torques[prec] = [ens.member(sl).calc_torque() for sl in slots]
+        codes = [ens.status_full(sl)[3] for sl in slots]
+        out[prec] = {"value": out["cells"] * steps / (ms * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                     "ms_per_step": ms / steps, "tile": {"threads": thr, "rows": rows},
+                     "tune_seconds": round(tune_s, 2), "tune_table_ms": {k: round(v * 1e3, 3) for k, v in
+                                                                          table.items()},
+                     "launches_per_step": ens.launches_per_step, "gpu_launches": ens.launch_count - n0,
+                     "device_bytes": ens.device_bytes, "errorcodes_nonzero": sum(1 for c in codes if c)}
+        ens.close()
+    errs = []
+    for a, b in zip(torques["mixed"], torques["fp64"]):
+        errs.append(max(abs(a[0] - b[0]) / abs(b[0]), abs(a[1] - b[1]) / max(abs(b[1]), 1e-300)))
+    out["torque_err_mixed_vs_fp64"] = {"max": max(errs), "median": statistics.median(errs),
+                                       "steps": warmup + steps}
+    out["speedup_mixed_vs_fp64_ensemble"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def run_serving(args):
+    """The serving workload: seeded Poisson arrivals swept over rates, runs of
+    64^3 .. 256x256x128 cells and 100..2000 RK3 steps (variable dt, CFLMAX
+    0.8), admitted against a 150 GB HBM budget into one mixed-precision
+    ensemble (continuous batching).  Beside it: the same runs one after
+    another on the plain FP64 single-run path (tc_run), for the aggregate
+    throughput and each run's torque."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as entry
+    tc = entry.load()
+    import tc_gb300.build as tb
+    tb.build()
+    import tc_gb300.autotune as at
+    import tc_gb300.initial as ini
+    import tc_gb300.serving as sv
+    n = args.requests
+    rates = [float(x) for x in args.rates.split(",")]
+    base = sv.draw_requests(n, rates[0], seed=7)
+    states = {r.rid: ini.couette_noise(r.bou, seed=r.seed) for r in base}
+    # sequential plain FP64 (the drop-in path), one run at a time
+    seq_t0 = time.perf_counter()
+    fp64_torque, fp64_cell_steps = {}, 0
+    for r in base:
+        g = tc.TaylorCouette(r.bou)
+        g.set_state(*states[r.rid])
+        code, _, _, _ = g.run(r.nsteps, 0, 0.0)
+        fp64_torque[r.rid] = g.calc_torque()
+        g.close()
+        fp64_cell_steps += r.bou["nthm"] * r.bou["nzm"] * r.bou["nrm"] * r.nsteps
+    seq_s = time.perf_counter() - seq_t0
+    seq = {"value": fp64_cell_steps / seq_s / 1e6, "unit": "Mcell-steps/s", "wall_s": seq_s,
+           "note": "same runs, one after another, tc_run on the plain FP64 path, host states in, torque out"}
+    tile, _ = at.tune("mixed", [r.bou for r in base[:8]], [states[r.rid] for r in base[:8]], steps=2)
+    sweep = []
+    clocks = Clocks(0)
+    for rate in rates:
+        reqs = sv.with_rate(base, rate, seed=7)
+        srv = sv.Server("mixed", hbm_budget=args.hbm_budget, chunk=args.chunk, tune=tile)
+        res, stats = srv.run(reqs, lambda r: states[r.rid])
+        lat = [x.latency for x in res]
+        terr = []
+        for x in res:
+            w = fp64_torque[x.rid]
+            terr.append(max(abs(x.torque[0] - w[0]) / abs(w[0]), abs(x.torque[1] - w[1]) / abs(w[1])))
+        sweep.append({"rate_runs_per_s": rate, "requests": len(res), "p50_s": sv.percentile(lat, 0.5),
+                      "p99_s": sv.percentile(lat, 0.99), "mean_s": sum(lat) / len(lat),
+                      "value": stats["cell_steps"] / stats["wall_s"] / 1e6, "unit": "Mcell-steps/s",
+                      "wall_s": stats["wall_s"], "peak_resident_runs": stats["peak_active"],
+                      "peak_bytes": stats["peak_bytes"],
+                      "torque_err_vs_fp64": {"max": max(terr), "median": statistics.median(terr)},
+                      "errorcodes_nonzero": sum(1 for x in res if x.errorcode)})
+    clk = clocks.stop()
+    best = max(sweep, key=lambda x: x["value"])
+    line = {"metric": "Mcell-steps/s", "value": best["value"], "unit": "Mcell-steps/s", "n_gpus": 1,
+            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/f64 mixed", "data": "synthetic (seeded Couette+noise starts, seeded Poisson arrivals)",
+            "config": {"workload": "C5: serving loop, Poisson arrivals, grids 64^3..256x256x128, 100..2000 RK3 "
+                                   "steps, radius ratio 0.5..0.9, 1/NU 500..1e4, variable dt CFLMAX 0.8, "
+                                   f"{args.hbm_budget / 1e9:.0f} GB HBM budget, chunk {args.chunk} steps",
+                       "requests_per_rate": n, "tile": {"threads": tile[0], "rows": tile[1]}},
+            "serving": sweep, "sequential_fp64": seq,
+            "speedup_served_mixed_vs_sequential_fp64": best["value"] / seq["value"], "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,6 +358,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed FP32/FP64 leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble legs")
+    ap.add_argument("--ens-steps", type=int, default=20, help="timed steps of each ensemble leg")
+    ap.add_argument("--ens-instances", type=int, default=96)
+    ap.add_argument("--requests", type=int, default=16, help="C5: runs per arrival rate")
+    ap.add_argument("--rates", default="0.5,2,8,20", help="C5: arrival rates, runs/s")
+    ap.add_argument("--chunk", type=int, default=25, help="C5: steps between admissions")
+    ap.add_argument("--hbm-budget", type=float, default=150e9)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -245,6 +374,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "C5":
+        if rank == 0:
+            run_serving(args)
         return
 
     import torch
@@ -383,6 +516,12 @@ def main():
             mixed["err_vs_fp64"] = errs
         gm.close()
 
+    # ---- batched ensembles (FP64 and mixed) ----------------------------------
+    ensemble = None
+    if not args.no_ensemble:
+        ensemble = ensemble_legs(tc, torch, stream, args.ens_steps, args.warmup, args.ens_instances)
+        ensemble["speedup_mixed_ensemble_vs_plain_fp64"] = ensemble["mixed"]["value"] / value
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -435,6 +574,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "mixed": mixed,
+        "ensemble": ensemble,
         "gpu_launches": launches,
         "clocks": clk,
         "sim": {"time": tsim, "last_dt": dt},

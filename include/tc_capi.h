@@ -45,6 +45,7 @@ typedef struct tc_bou {
 } tc_bou;
 
 typedef struct tc_handle tc_handle;
+typedef struct tc_ensemble tc_ensemble;
 
 /* Precision of a handle.  TC_PREC_FP64: the plain path, every operation in
  * IEEE FP64 (the drop-in).  TC_PREC_MIXED: velocity fields, explicit terms,
@@ -208,6 +209,63 @@ int tc_check_divergence_noalloc(const double* qt, const double* qr, const double
                                 int nthm, int nzm, int nrm,
                                 const double* udx2m, const double* usrm,
                                 double dxt, double dxz, void* stream, double* qmax);
+
+/* ---- ensembles (no counterpart in the reference) -------------------------
+ * Many independent runs of different sizes, Re and radius ratio resident on
+ * one device and advanced together: each step of the ensemble is one CUDA
+ * graph of grouped launches, each launch covering every member (a flat list
+ * of (member, tile) items).  A member's arithmetic is the single-run path's,
+ * so its result does not depend on which other members share the launches.
+ * One ensemble has one precision; all members use the same NSST; patterned
+ * slip (MINSTRT/MINSTRZ > 0) is not supported; no output-step checks run
+ * (read a member's reductions through its handle between steps). */
+
+int tc_ensemble_create(int precision, tc_ensemble** out);
+/* Waits for the ensemble's stream, frees every member and the tables. */
+void tc_ensemble_destroy(tc_ensemble* e);
+const char* tc_ensemble_last_error(const tc_ensemble* e);
+/* Stream of all later ensemble work (members included). */
+int tc_ensemble_set_stream(tc_ensemble* e, void* cuda_stream);
+/* Admit a run: build its handle (tc_create_ex), load the start (tc_set_state
+ * arrays, pr may be NULL) and choose its time step:
+ *   dt > 0             fixed dt;
+ *   dt <= 0, IDTV = 1  the reference's variable dt every step
+ *                      (main.F90:156-174: CalcMaxCFL of the current field,
+ *                      DTMIN on the first steps, errors 165/166 stop the
+ *                      member);
+ *   dt <= 0, IDTV = 0  fixed dt = min(LIMITCFL / CFL(start), DTMAX).
+ * nsteps is the run's requested length,
+ * kept for the caller (tc_ensemble_status); the ensemble does not stop a
+ * member by itself.  *slot receives the member's slot (reused after
+ * tc_ensemble_remove).  Synchronises the ensemble's stream. */
+int tc_ensemble_add(tc_ensemble* e, const tc_bou* cfg, double dt, const double* qt,
+                    const double* qr, const double* qz, const double* pr, int nsteps,
+                    int* slot);
+/* Retire a member and free its device memory (waits for the stream). */
+int tc_ensemble_remove(tc_ensemble* e, int slot);
+/* The member's handle, for tc_get_state / tc_calc_torque / ... (owned by
+ * the ensemble: do not tc_destroy it). */
+int tc_ensemble_member(tc_ensemble* e, int slot, tc_handle** h);
+int tc_ensemble_count(const tc_ensemble* e);
+/* Tile shapes: threads per cell/column/mode tile (64, 128 or 256) and rows
+ * per theta-FFT block (0 = the single-run choice for the largest member,
+ * else 1..32, a power of two); schedule 0 = one graph of grouped launches
+ * per step.  Takes effect at the next tc_ensemble_step. */
+int tc_ensemble_tune(tc_ensemble* e, int threads, int rows);
+/* Enqueue nsteps steps of every member (graph replays; asynchronous). */
+int tc_ensemble_step(tc_ensemble* e, int nsteps);
+int tc_ensemble_sync(tc_ensemble* e);
+/* Steps done, simulated time, last dt and error code (165/166 for a
+ * variable-dt member, which then stops) of a member (synchronises). */
+int tc_ensemble_status(tc_ensemble* e, int slot, int* steps_done, double* time,
+                       double* dt, int* errorcode);
+/* Requested length given to tc_ensemble_add. */
+int tc_ensemble_target(const tc_ensemble* e, int slot);
+long long tc_ensemble_launch_count(const tc_ensemble* e);
+int tc_ensemble_launches_per_step(const tc_ensemble* e);
+long long tc_ensemble_device_bytes(const tc_ensemble* e);
+/* Cells of all members: sum of nthm * nzm * nrm. */
+long long tc_ensemble_cells(const tc_ensemble* e);
 
 /* ---- measurement helpers ------------------------------------------------ */
 

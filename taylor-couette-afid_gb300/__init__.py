@@ -119,6 +119,24 @@ SIGNATURES = {
     "tc_profile_read": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "tc_profile_name": (ctypes.c_char_p, [ctypes.c_int]),
     "tc_measure_fp64_peak": (ctypes.c_int, [_vp, _dp]),
+    "tc_ensemble_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    "tc_ensemble_destroy": (None, [_vp]),
+    "tc_ensemble_last_error": (ctypes.c_char_p, [_vp]),
+    "tc_ensemble_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "tc_ensemble_add": (ctypes.c_int, [_vp, ctypes.POINTER(Bou), ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                       _ip]),
+    "tc_ensemble_remove": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tc_ensemble_member": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "tc_ensemble_count": (ctypes.c_int, [_vp]),
+    "tc_ensemble_tune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tc_ensemble_step": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tc_ensemble_sync": (ctypes.c_int, [_vp]),
+    "tc_ensemble_status": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip]),
+    "tc_ensemble_target": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tc_ensemble_launch_count": (ctypes.c_longlong, [_vp]),
+    "tc_ensemble_launches_per_step": (ctypes.c_int, [_vp]),
+    "tc_ensemble_device_bytes": (ctypes.c_longlong, [_vp]),
+    "tc_ensemble_cells": (ctypes.c_longlong, [_vp]),
 }
 
 
@@ -189,18 +207,22 @@ class TaylorCouette:
     explicit terms, momentum sweeps and FFTs; FP64 pressure solve, pressure
     accumulation and reductions)."""
 
-    def __init__(self, bou: dict, precision: str = "fp64"):
+    def __init__(self, bou: dict, precision: str = "fp64", _handle=None):
         self.L = lib()
         self.bou = dict(bou)
         self._b = Bou.from_dict(bou)
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
-        h = ctypes.c_void_p()
-        rc = self.L.tc_create_ex(ctypes.byref(self._b), PREC_MIXED if precision == "mixed" else PREC_FP64,
-                                 ctypes.byref(h))
-        if rc != 0:
-            raise TCError(rc, self.L.tc_last_error(None).decode())
+        self._owned = _handle is None
+        if _handle is None:
+            h = ctypes.c_void_p()
+            rc = self.L.tc_create_ex(ctypes.byref(self._b), PREC_MIXED if precision == "mixed" else PREC_FP64,
+                                     ctypes.byref(h))
+            if rc != 0:
+                raise TCError(rc, self.L.tc_last_error(None).decode())
+        else:
+            h = _handle
         self.h = h
         self.nthm, self.nzm, self.nrm = self._b.nthm, self._b.nzm, self._b.nrm
         self.nr = self.nrm + 1
@@ -209,7 +231,8 @@ class TaylorCouette:
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.tc_destroy(self.h)
+            if self._owned:
+                self.L.tc_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -351,3 +374,115 @@ class TaylorCouette:
         v = ctypes.c_double()
         self._ck(self.L.tc_measure_fp64_peak(self.h, ctypes.byref(v)))
         return v.value
+
+
+class Ensemble:
+    """Many independent runs resident on one device, stepped together (one
+    CUDA graph of grouped launches per step).  Members are admitted and
+    retired between steps; each keeps the single-run arithmetic.
+
+    precision: "fp64" or "mixed" for every member."""
+
+    def __init__(self, precision: str = "mixed"):
+        self.L = lib()
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+        e = ctypes.c_void_p()
+        rc = self.L.tc_ensemble_create(PREC_MIXED if precision == "mixed" else PREC_FP64, ctypes.byref(e))
+        if rc != 0:
+            raise TCError(rc, "tc_ensemble_create")
+        self.e = e
+        self.bous = {}
+
+    def close(self):
+        if getattr(self, "e", None):
+            self.L.tc_ensemble_destroy(self.e)
+            self.e = None
+            self.bous = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc: int):
+        if rc != 0:
+            raise TCError(rc, (self.L.tc_ensemble_last_error(self.e) or b"").decode())
+
+    def set_stream(self, stream_ptr: int):
+        self._ck(self.L.tc_ensemble_set_stream(self.e, ctypes.c_void_p(stream_ptr)))
+
+    def add(self, bou: dict, state, nsteps: int = 0, dt: float = 0.0) -> int:
+        """Admit a run with start `state` = (qt, qr, qz[, pr]) in the reference
+        layout.  dt > 0: fixed dt; dt <= 0 with IDTV = 1: the reference's
+        variable dt every step; dt <= 0 with IDTV = 0: fixed dt from the
+        start's CFL number (LIMITCFL / CFL, capped at DTMAX)."""
+        b = Bou.from_dict(bou)
+        shp = (b.nthm + 2, b.nzm + 2, b.nrm + 1)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in state[:3]]
+        for a in arrs:
+            if a.shape != shp:
+                raise ValueError(f"expected shape {shp}, got {a.shape}")
+        pr = None
+        if len(state) > 3 and state[3] is not None:
+            pr = np.ascontiguousarray(state[3], dtype=np.float64)
+        slot = ctypes.c_int()
+        self._ck(self.L.tc_ensemble_add(self.e, ctypes.byref(b), float(dt), *[_dptr(a) for a in arrs],
+                                        _dptr(pr) if pr is not None else None, int(nsteps), ctypes.byref(slot)))
+        self.bous[slot.value] = dict(bou)
+        return slot.value
+
+    def remove(self, slot: int):
+        self._ck(self.L.tc_ensemble_remove(self.e, slot))
+        self.bous.pop(slot, None)
+
+    def member(self, slot: int) -> TaylorCouette:
+        """A non-owning view of the member (get_state, calc_torque, ...)."""
+        h = ctypes.c_void_p()
+        self._ck(self.L.tc_ensemble_member(self.e, slot, ctypes.byref(h)))
+        return TaylorCouette(self.bous[slot], self.precision, _handle=h)
+
+    def tune(self, threads: int = 128, rows: int = 0):
+        self._ck(self.L.tc_ensemble_tune(self.e, threads, rows))
+
+    def step(self, nsteps: int = 1):
+        self._ck(self.L.tc_ensemble_step(self.e, int(nsteps)))
+
+    def sync(self):
+        self._ck(self.L.tc_ensemble_sync(self.e))
+
+    def status(self, slot: int):
+        """(steps done, simulated time) of a member."""
+        return self.status_full(slot)[:2]
+
+    def status_full(self, slot: int):
+        """(steps done, simulated time, last dt, error code) of a member."""
+        n, t, d, c = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self._ck(self.L.tc_ensemble_status(self.e, slot, ctypes.byref(n), ctypes.byref(t), ctypes.byref(d),
+                                           ctypes.byref(c)))
+        return n.value, t.value, d.value, c.value
+
+    def target(self, slot: int) -> int:
+        return self.L.tc_ensemble_target(self.e, slot)
+
+    @property
+    def count(self) -> int:
+        return self.L.tc_ensemble_count(self.e)
+
+    @property
+    def cells(self) -> int:
+        return self.L.tc_ensemble_cells(self.e)
+
+    @property
+    def launch_count(self) -> int:
+        return self.L.tc_ensemble_launch_count(self.e)
+
+    @property
+    def launches_per_step(self) -> int:
+        return self.L.tc_ensemble_launches_per_step(self.e)
+
+    @property
+    def device_bytes(self) -> int:
+        return self.L.tc_ensemble_device_bytes(self.e)

@@ -1,0 +1,607 @@
+// tc_batch.cu -- ensembles: many independent, unevenly sized instances
+// advanced together (include/tc_capi.h, tc_ensemble_*).
+//
+// Each member is an ordinary handle (tc_create_ex); its device state, grid
+// and coefficients are reused as they are.  One step of the ensemble is a
+// fixed sequence of grouped launches, each covering every active member: the
+// launch's blocks form a flat work list of (member, tile) items, a block
+// finds its member by binary search in a prefix table of item counts and then
+// runs the same device body as the single-instance kernel (tc_bodies.cuh), so
+// a member's arithmetic is identical alone and in the mix.  Per step:
+//   begin (dt, beta, inner-wall forcing per member), factors (one block per
+//   member), then per RK substep: momentum, radial solve, divergence + theta
+//   FFT, z FFT, pressure tridiagonal, inverse z FFT, inverse theta FFT,
+//   correction; then end (time += dt).
+// The whole step is captured once in a CUDA graph and replayed; it is
+// re-captured only when members join or leave.  Members run with a fixed dt
+// (the ensemble configurations fix dt per member from its initial CFL).
+//
+// Tile shapes (threads per cell tile, rows per theta-FFT block) are tuning
+// knobs, chosen per ensemble by the project's autotuner
+// (taylor-couette-afid_gb300/autotune.py) through tc_ensemble_tune.
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tc_bodies.cuh"
+#include "tc_handle.h"
+
+namespace tcgb {
+namespace ens {
+
+template <typename T>
+struct InstT {
+    Dims d;
+    CoefT<T> cv;
+    Coef c;
+    Consts k;
+    FieldsT<T> f;
+    PlansT<T> p;
+    MomArgs<T> ma[3];
+    int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
+};
+
+enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };
+
+constexpr double kCflFloor = 0.00000001;   // CalcMaxCFL.F90 starts its maximum here
+
+__device__ __forceinline__ int find_member(const int* prefix, int n, long long item) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (prefix[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---- per-step control ----------------------------------------------------
+
+// Fixed-dt members: TimeMarcher with the member's dt (mode 0).  Variable-dt
+// members: main.F90:156-174 from the CFL number the CFL kernel just reduced
+// (mode 1), which may raise 165/166.
+template <typename T>
+__global__ void ens_begin_kernel(const InstT<T>* inst, int n) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    StepState* st = inst[m].f.st;
+    if (st->halt) return;
+    begin_step_body(inst[m].k, st, inst[m].vdt, st->dt, st->time);
+}
+
+// time = time + dt; a variable-dt member that raised an error stops here,
+// as the reference's run would (main.F90:229-259).
+template <typename T>
+__global__ void ens_end_kernel(const InstT<T>* inst, int n) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    StepState* st = inst[m].f.st;
+    if (st->halt) return;
+    st->time = st->time + st->dt;
+    st->ntime += 1;
+    if (st->errorcode != 0) st->halt = 1;
+    st->instcfl = kCflFloor;
+}
+
+template <typename T>
+__global__ void ens_factors_kernel(const InstT<T>* inst) {
+    const InstT<T>& I = inst[blockIdx.x];
+    if (I.f.st->halt) return;
+    factors_body(I.d, I.c, I.k, I.f.st, I.f.Fd, I.f.corrd, I.f.scal, I.f.F, I.f.corr);
+}
+
+__global__ void ens_init_kernel(StepState* st, double dt, double time, int ntime) {
+    st->dt = dt;
+    st->time = time;
+    st->ntime = ntime;
+    st->halt = 0;
+    st->errorcode = 0;
+    st->instcfl = kCflFloor;
+}
+
+// CalcMaxCFL of the variable-dt members: item = (k, tile of cells); block
+// maximum, then an atomic maximum on the bits of the member's instcfl (the
+// order of non-negative doubles is the order of their bit patterns).
+template <typename T>
+__global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, const int* prefix, int n) {
+    __shared__ double sh[32];
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const long long local = item - prefix[m];
+    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const int k = (int)(local / tiles);
+    const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (flat < I.d.P) {
+        const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+        v = cfl_cell(I.d, I.c, I.k.dxt, I.k.dxz, I.f, i, j, k);
+    }
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (l == 0)
+            atomicMax(reinterpret_cast<unsigned long long*>(&I.f.st->instcfl), (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// ---- grouped substep phases ---------------------------------------------------
+
+// cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)
+template <typename T>
+__global__ void __launch_bounds__(256) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const long long local = item - prefix[m];
+    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const int k = (int)(local / tiles);
+    const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
+    if (flat >= I.d.P) return;
+    const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+    momentum_cell<MODE_FUSED>(I.d, I.cv, I.ma[sub], i, j, k);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const long long local = item - prefix[m];
+    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const int k = (int)(local / tiles);
+    const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
+    if (flat >= I.d.P) return;
+    const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+    correct_cell<true, true, T>(I.d, I.c, I.k.dxzq, I.f, sub, i, j, k);
+}
+
+// column-wise: item = TPB consecutive (z, theta) columns
+template <typename T>
+__global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const long long col = (item - prefix[m]) * blockDim.x + threadIdx.x;
+    if (col >= I.d.P) return;
+    radial_column(I.d, I.f, sub, col);
+}
+
+// mode-pair-wise: item = TPB consecutive (kz <= nzm/2, kt) mode pairs
+template <typename T>
+__global__ void __launch_bounds__(256) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const long long t = (item - prefix[m]) * blockDim.x + threadIdx.x;
+    if (t >= (long long)I.d.nzh * I.d.PH) return;
+    double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(I.f.spec) : I.f.ws;
+    ptri_mode(I.d, I.c, I.f, ws, t);
+}
+
+// row-wise FFT phases: item = R consecutive (k, j) rows
+template <int R, typename T>
+__global__ void __launch_bounds__(128) ens_divfft_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    div_fft_rows<false, R, T>(I.d, I.cv, (T)I.k.dxt, (T)I.k.dxz, I.f, I.p.th, I.p.tw_th, I.p.twr, I.k.fft_norm, sub,
+                              (item - prefix[m]) * R, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+}
+
+template <int R, typename T>
+__global__ void __launch_bounds__(128) ens_thinv_kernel(const InstT<T>* inst, const int* prefix, int n) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    thinv_rows<R, T>(I.d, I.f, I.p.th, I.p.tw_th, I.p.twr, (item - prefix[m]) * R,
+                     reinterpret_cast<typename V2<T>::type*>(smem_raw));
+}
+
+// z FFT: item = (plane k, kZC consecutive kt columns)
+template <typename T>
+__global__ void __launch_bounds__(128) ens_zfft_kernel(const InstT<T>* inst, const int* prefix, int n, int inv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const long long item = blockIdx.x;
+    const int m = find_member(prefix, n, item);
+    const InstT<T>& I = inst[m];
+    if (I.f.st->halt) return;
+    const int local = (int)(item - prefix[m]);
+    const int groups = (I.d.PH + kZC - 1) / kZC;
+    const int kplane = local / groups, g = local - kplane * groups;
+    zfft_tile(I.d, I.f, I.p.z, I.p.tw_z, inv, g * kZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+}
+
+int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace ens
+}  // namespace tcgb
+
+struct tc_ensemble {
+    int mixed = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<tc_handle*> members;     // slot -> member (nullptr = free)
+    std::vector<int> target;             // requested step count per slot (informational)
+    std::vector<int> vdt;                // per slot: 1 = variable dt (CFL rule every step)
+    std::vector<int> active;             // slots in the current work list
+    void* inst_dev = nullptr;            // InstT<T>[active]
+    int* prefix_dev = nullptr;           // PH_COUNT tables of (n+1) ints
+    int threads = 128;                   // threads per cell/column/mode tile
+    int rows = 0;                        // rows per theta-FFT block (0: from the largest member)
+    int rows_used = 0;
+    size_t smem_div = 0, smem_z = 0;
+    int items[tcgb::ens::PH_COUNT] = {0};
+    bool dirty = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+    int launches_per_step = 0;
+    std::string err;
+};
+
+namespace tcgb {
+namespace ens {
+
+int efail(tc_ensemble* e, int code, const std::string& msg) {
+    if (e) e->err = msg;
+    return code;
+}
+
+int ecuda(tc_ensemble* e, cudaError_t c, const char* what) {
+    return efail(e, 1000 + (int)c, std::string(what) + ": " + cudaGetErrorString(c));
+}
+
+template <typename T> FieldsT<T>& MF(tc_handle* h);
+template <> FieldsT<double>& MF<double>(tc_handle* h) { return h->fd; }
+template <> FieldsT<float>& MF<float>(tc_handle* h) { return h->ff; }
+template <typename T> const CoefT<T>& MC(tc_handle* h);
+template <> const CoefT<double>& MC<double>(tc_handle* h) { return h->c; }
+template <> const CoefT<float>& MC<float>(tc_handle* h) { return h->cf; }
+template <typename T> const PlansT<T>& MP(tc_handle* h);
+template <> const PlansT<double>& MP<double>(tc_handle* h) { return h->pd; }
+template <> const PlansT<float>& MP<float>(tc_handle* h) { return h->pf; }
+
+template <int R, typename T>
+void set_smem_attrs() {
+    cudaFuncSetAttribute(ens_divfft_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(ens_thinv_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template <typename T>
+int rebuild(tc_ensemble* e) {
+    const int n = (int)e->active.size();
+    if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+    if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+    if (e->inst_dev) { cudaFree(e->inst_dev); e->inst_dev = nullptr; }
+    if (e->prefix_dev) { cudaFree(e->prefix_dev); e->prefix_dev = nullptr; }
+    e->dirty = false;
+    if (n == 0) return 0;
+    std::vector<InstT<T>> inst(n);
+    std::vector<int> prefix((size_t)PH_COUNT * (n + 1), 0);
+    int maxM = 1, maxNz = 1;
+    for (int a = 0; a < n; ++a) maxM = std::max(maxM, e->members[e->active[a]]->d.M);
+    int R = e->rows > 0 ? e->rows : theta_rows(maxM);
+    e->rows_used = R;
+    const int TPB = e->threads;
+    for (int a = 0; a < n; ++a) {
+        tc_handle* h = e->members[e->active[a]];
+        InstT<T>& I = inst[a];
+        I.d = h->d; I.cv = MC<T>(h); I.c = h->c; I.k = h->k; I.f = MF<T>(h); I.p = MP<T>(h);
+        for (int s = 0; s < 3; ++s) I.ma[s] = make_mom_args(h->k, I.f, s);
+        I.vdt = e->vdt[e->active[a]];
+        const Dims& d = h->d;
+        maxNz = std::max(maxNz, d.nz);
+        long long cnt[PH_COUNT];
+        cnt[PH_MOM] = (long long)d.nr * ceil_div(d.P, TPB);
+        cnt[PH_CORR] = cnt[PH_MOM];
+        cnt[PH_RAD] = ceil_div(d.P, TPB);
+        cnt[PH_PTRI] = ceil_div((long long)d.nzh * d.PH, TPB);
+        cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
+        cnt[PH_THINV] = cnt[PH_DIV];
+        cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, kZC);
+        cnt[PH_FACT] = 1;
+        cnt[PH_CFL] = I.vdt ? cnt[PH_MOM] : 0;
+        for (int p = 0; p < PH_COUNT; ++p) {
+            long long v = (long long)prefix[(size_t)p * (n + 1) + a] + cnt[p];
+            if (v > 2000000000LL) return efail(e, 2010, "ensemble work list exceeds 2^31 items");
+            prefix[(size_t)p * (n + 1) + a + 1] = (int)v;
+        }
+    }
+    for (int p = 0; p < PH_COUNT; ++p) e->items[p] = prefix[(size_t)p * (n + 1) + n];
+    typedef typename V2<T>::type C2;
+    e->smem_div = (size_t)2 * R * maxM * sizeof(C2);
+    e->smem_z = (size_t)2 * kZC * maxNz * sizeof(C2);
+    if (e->smem_div > 200 * 1024 || e->smem_z > 200 * 1024) return efail(e, 2011, "ensemble FFT tile exceeds shared memory");
+    cudaError_t c = cudaMalloc(&e->inst_dev, sizeof(InstT<T>) * n);
+    if (c == cudaSuccess) c = cudaMalloc(&e->prefix_dev, sizeof(int) * prefix.size());
+    if (c == cudaSuccess) c = cudaMemcpy(e->inst_dev, inst.data(), sizeof(InstT<T>) * n, cudaMemcpyHostToDevice);
+    if (c == cudaSuccess) c = cudaMemcpy(e->prefix_dev, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice);
+    if (c != cudaSuccess) return ecuda(e, c, "ensemble tables");
+    switch (R) {
+        case 1: set_smem_attrs<1, T>(); break;
+        case 2: set_smem_attrs<2, T>(); break;
+        case 4: set_smem_attrs<4, T>(); break;
+        case 8: set_smem_attrs<8, T>(); break;
+        case 16: set_smem_attrs<16, T>(); break;
+        default: set_smem_attrs<32, T>(); break;
+    }
+    cudaFuncSetAttribute(ens_zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return 0;
+}
+
+template <int R, typename T>
+void launch_div(tc_ensemble* e, const InstT<T>* I, const int* pre, int n, int sub) {
+    ens_divfft_kernel<R, T><<<e->items[PH_DIV], 128, e->smem_div, e->stream>>>(I, pre, n, sub);
+}
+template <int R, typename T>
+void launch_thinv(tc_ensemble* e, const InstT<T>* I, const int* pre, int n) {
+    ens_thinv_kernel<R, T><<<e->items[PH_THINV], 128, e->smem_div, e->stream>>>(I, pre, n);
+}
+
+// Enqueue one step of every active member on e->stream.
+template <typename T>
+int enqueue_step(tc_ensemble* e) {
+    const int n = (int)e->active.size();
+    const InstT<T>* I = (const InstT<T>*)e->inst_dev;
+    const int* pre = e->prefix_dev;
+    auto P = [&](int p) { return pre + (size_t)p * (n + 1); };
+    cudaStream_t s = e->stream;
+    const int TPB = e->threads;
+    int count = 0;
+    if (e->items[PH_CFL] > 0) {
+        ens_cfl_kernel<T><<<e->items[PH_CFL], TPB, 0, s>>>(I, P(PH_CFL), n);
+        ++count;
+    }
+    ens_begin_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(I, n); ++count;
+    ens_factors_kernel<T><<<n, 256, 0, s>>>(I); ++count;
+    const int nsst = e->members[e->active[0]]->k.nsst;
+    for (int sub = 0; sub < nsst; ++sub) {
+        ens_momentum_kernel<T><<<e->items[PH_MOM], TPB, 0, s>>>(I, P(PH_MOM), n, sub);
+        ens_radial_kernel<T><<<e->items[PH_RAD], TPB, 0, s>>>(I, P(PH_RAD), n, sub);
+        switch (e->rows_used) {
+            case 1: launch_div<1, T>(e, I, P(PH_DIV), n, sub); break;
+            case 2: launch_div<2, T>(e, I, P(PH_DIV), n, sub); break;
+            case 4: launch_div<4, T>(e, I, P(PH_DIV), n, sub); break;
+            case 8: launch_div<8, T>(e, I, P(PH_DIV), n, sub); break;
+            case 16: launch_div<16, T>(e, I, P(PH_DIV), n, sub); break;
+            default: launch_div<32, T>(e, I, P(PH_DIV), n, sub); break;
+        }
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], 128, e->smem_z, s>>>(I, P(PH_ZFFT), n, 0);
+        ens_ptri_kernel<T><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], 128, e->smem_z, s>>>(I, P(PH_ZFFT), n, 1);
+        switch (e->rows_used) {
+            case 1: launch_thinv<1, T>(e, I, P(PH_THINV), n); break;
+            case 2: launch_thinv<2, T>(e, I, P(PH_THINV), n); break;
+            case 4: launch_thinv<4, T>(e, I, P(PH_THINV), n); break;
+            case 8: launch_thinv<8, T>(e, I, P(PH_THINV), n); break;
+            case 16: launch_thinv<16, T>(e, I, P(PH_THINV), n); break;
+            default: launch_thinv<32, T>(e, I, P(PH_THINV), n); break;
+        }
+        ens_correct_kernel<T><<<e->items[PH_CORR], TPB, 0, s>>>(I, P(PH_CORR), n, sub);
+        count += 8;
+    }
+    ens_end_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(I, n); ++count;
+    e->launches_per_step = count;
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return ecuda(e, c, "ensemble launch");
+    return 0;
+}
+
+template <typename T>
+int capture(tc_ensemble* e) {
+    cudaStream_t cap = nullptr;
+    cudaError_t c = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (c != cudaSuccess) return ecuda(e, c, "capture stream");
+    cudaStream_t saved = e->stream;
+    e->stream = cap;
+    c = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int r = 0;
+    if (c == cudaSuccess) {
+        r = enqueue_step<T>(e);
+        cudaError_t c2 = cudaStreamEndCapture(cap, &e->graph);
+        if (c2 != cudaSuccess && r == 0) r = ecuda(e, c2, "end capture");
+    } else {
+        r = ecuda(e, c, "begin capture");
+    }
+    e->stream = saved;
+    cudaStreamDestroy(cap);
+    if (r) return r;
+    c = cudaGraphInstantiate(&e->exec, e->graph, 0);
+    if (c != cudaSuccess) return ecuda(e, c, "graph instantiate");
+    return 0;
+}
+
+int prepare(tc_ensemble* e) {
+    if (!e->dirty && (e->exec || e->active.empty())) return 0;
+    int r = e->mixed ? rebuild<float>(e) : rebuild<double>(e);
+    if (r) return r;
+    if (e->active.empty()) return 0;
+    return e->mixed ? capture<float>(e) : capture<double>(e);
+}
+
+}  // namespace ens
+}  // namespace tcgb
+
+using namespace tcgb;
+using namespace tcgb::ens;
+
+// The exported functions below are declared extern "C" in tc_capi.h.
+
+int tc_ensemble_create(int precision, tc_ensemble** out) {
+    if (!out) return 2000;
+    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED) return 2007;
+    tc_ensemble* e = new tc_ensemble();
+    e->mixed = precision == TC_PREC_MIXED;
+    *out = e;
+    return 0;
+}
+
+void tc_ensemble_destroy(tc_ensemble* e) {
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    else cudaDeviceSynchronize();
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    if (e->inst_dev) cudaFree(e->inst_dev);
+    if (e->prefix_dev) cudaFree(e->prefix_dev);
+    for (tc_handle* h : e->members) if (h) tc_destroy(h);
+    delete e;
+}
+
+const char* tc_ensemble_last_error(const tc_ensemble* e) { return e ? e->err.c_str() : ""; }
+
+int tc_ensemble_set_stream(tc_ensemble* e, void* stream) {
+    if (!e) return 2000;
+    e->stream = (cudaStream_t)stream;
+    for (tc_handle* h : e->members) if (h) tc_set_stream(h, stream);
+    return 0;
+}
+
+int tc_ensemble_add(tc_ensemble* e, const tc_bou* cfg, double dt, const double* qt, const double* qr,
+                    const double* qz, const double* pr, int nsteps, int* slot) {
+    if (!e || !cfg || !slot) return 2000;
+    if (cfg->minstrt > 0 || cfg->minstrz > 0)
+        return efail(e, 2012, "patterned slip (MINSTRT/MINSTRZ > 0) cannot run in an ensemble");
+    for (int s : e->active)
+        if (e->members[s]->k.nsst != cfg->nsst)
+            return efail(e, 2012, "every member of an ensemble needs the same NSST");
+    tc_handle* h = nullptr;
+    int r = tc_create_ex(cfg, e->mixed ? TC_PREC_MIXED : TC_PREC_FP64, &h);
+    if (r) return efail(e, r, tc_last_error(nullptr));
+    tc_set_stream(h, e->stream);
+    r = tc_set_state(h, qt, qr, qz, pr);
+    if (r) { std::string m = tc_last_error(h); tc_destroy(h); return efail(e, r, m); }
+    int variable = 0;
+    if (!(dt > 0.0) && cfg->idtv == 1) {
+        variable = 1;                   // begin computes dt from the CFL of each step
+        dt = cfg->dtmin;
+    } else if (!(dt > 0.0)) {
+        // main.F90:160-166 once, on the start
+        double cfl = 0.0;
+        r = tc_calc_max_cfl(h, &cfl);
+        if (r) { std::string m = tc_last_error(h); tc_destroy(h); return efail(e, r, m); }
+        dt = (cfl < 1.0e-8) ? cfg->dtmax : cfg->limitCFL / cfl;
+        if (dt > cfg->dtmax) dt = cfg->dtmax;
+    }
+    ens_init_kernel<<<1, 1, 0, e->stream>>>(h->st, dt, 0.0, 0);
+    cudaError_t c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) { tc_destroy(h); return ecuda(e, c, "member init"); }
+    int s = -1;
+    for (size_t i = 0; i < e->members.size(); ++i)
+        if (!e->members[i]) { s = (int)i; break; }
+    if (s < 0) {
+        s = (int)e->members.size();
+        e->members.push_back(nullptr);
+        e->target.push_back(0);
+        e->vdt.push_back(0);
+    }
+    e->members[s] = h;
+    e->target[s] = nsteps;
+    e->vdt[s] = variable;
+    e->active.push_back(s);
+    std::sort(e->active.begin(), e->active.end());
+    e->dirty = true;
+    *slot = s;
+    return 0;
+}
+
+int tc_ensemble_remove(tc_ensemble* e, int slot) {
+    if (!e || slot < 0 || slot >= (int)e->members.size() || !e->members[slot]) return 2000;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    else cudaDeviceSynchronize();
+    tc_destroy(e->members[slot]);
+    e->members[slot] = nullptr;
+    e->active.erase(std::remove(e->active.begin(), e->active.end(), slot), e->active.end());
+    e->dirty = true;
+    return 0;
+}
+
+int tc_ensemble_member(tc_ensemble* e, int slot, tc_handle** h) {
+    if (!e || !h || slot < 0 || slot >= (int)e->members.size() || !e->members[slot]) return 2000;
+    *h = e->members[slot];
+    return 0;
+}
+
+int tc_ensemble_count(const tc_ensemble* e) { return e ? (int)e->active.size() : 0; }
+
+int tc_ensemble_target(const tc_ensemble* e, int slot) {
+    if (!e || slot < 0 || slot >= (int)e->members.size() || !e->members[slot]) return -1;
+    return e->target[slot];
+}
+
+int tc_ensemble_tune(tc_ensemble* e, int threads, int rows) {
+    if (!e) return 2000;
+    if (threads != 64 && threads != 128 && threads != 256) return efail(e, 2013, "threads must be 64, 128 or 256");
+    if (rows != 0 && rows != 1 && rows != 2 && rows != 4 && rows != 8 && rows != 16 && rows != 32)
+        return efail(e, 2013, "rows must be 0 (automatic) or a power of two up to 32");
+    e->threads = threads;
+    e->rows = rows;
+    e->dirty = true;
+    return 0;
+}
+
+int tc_ensemble_step(tc_ensemble* e, int nsteps) {
+    if (!e) return 2000;
+    if (int r = prepare(e)) return r;
+    if (e->active.empty()) return 0;
+    for (int n = 0; n < nsteps; ++n) {
+        cudaError_t c = cudaGraphLaunch(e->exec, e->stream);
+        if (c != cudaSuccess) return ecuda(e, c, "graph launch");
+        e->launches += e->launches_per_step;
+    }
+    return 0;
+}
+
+int tc_ensemble_sync(tc_ensemble* e) {
+    if (!e) return 2000;
+    cudaError_t c = e->stream ? cudaStreamSynchronize(e->stream) : cudaDeviceSynchronize();
+    if (c != cudaSuccess) return ecuda(e, c, "ensemble sync");
+    return 0;
+}
+
+int tc_ensemble_status(tc_ensemble* e, int slot, int* steps_done, double* time, double* dt, int* errorcode) {
+    tc_handle* h = nullptr;
+    if (int r = tc_ensemble_member(e, slot, &h)) return r;
+    StepState st;
+    cudaError_t c = cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess) c = e->stream ? cudaStreamSynchronize(e->stream) : cudaDeviceSynchronize();
+    if (c != cudaSuccess) return ecuda(e, c, "status read");
+    if (steps_done) *steps_done = st.ntime;
+    if (time) *time = st.time;
+    if (dt) *dt = st.dt;
+    if (errorcode) *errorcode = st.errorcode;
+    return 0;
+}
+
+long long tc_ensemble_launch_count(const tc_ensemble* e) { return e ? e->launches : 0; }
+int tc_ensemble_launches_per_step(const tc_ensemble* e) { return e ? e->launches_per_step : 0; }
+
+long long tc_ensemble_device_bytes(const tc_ensemble* e) {
+    if (!e) return 0;
+    long long b = 0;
+    for (tc_handle* h : e->members) if (h) b += tc_device_bytes(h);
+    return b;
+}
+
+long long tc_ensemble_cells(const tc_ensemble* e) {
+    if (!e) return 0;
+    long long c = 0;
+    for (int s : e->active) c += e->members[s]->d.P * e->members[s]->d.nr;
+    return c;
+}

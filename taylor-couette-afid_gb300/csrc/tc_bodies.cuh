@@ -649,6 +649,27 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, doubl
     }
 }
 
+// CalcMaxCFL.F90:30-43 at cell (i, j, k); in FP32 on the mixed path (the
+// maximum itself is exact in any precision).
+template <typename T>
+__device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, double dxt, double dxz, const FieldsT<T>& f,
+                                           int i, int j, int k) {
+    const size_t P = (size_t)d.P;
+    const int ip = wp(i, d.nt), jp = wp(j, d.nz);
+    const size_t o = (size_t)k * P + (size_t)j * d.nt + i;
+    if (!std::is_same<T, double>::value) {
+        const T h = (T)0.5;
+        const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * (T)ld(c.usrm + k)));
+        const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * (T)ld(c.udx2rm + k)));
+        const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
+        return (double)(vt + vr + vz);
+    }
+    const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
+    const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
+    const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
+    return fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
+           fabs((z1 + z0) * 0.5 * dxz);
+}
 
 // Scalars of the momentum kernel for substep `sub`, in the element type T.
 template <typename T>

@@ -267,16 +267,8 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, do
         const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
         const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
         double v;
-        if (which == 0 && !std::is_same<T, double>::value) {
-            // CalcMaxCFL of the mixed path in FP32 (the max itself is exact)
-            const T h = (T)0.5;
-            const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * (T)ld(c.usrm + k)));
-            const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * (T)ld(c.udx2rm + k)));
-            const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
-            v = (double)(vt + vr + vz);
-        } else if (which == 0) {
-            v = fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
-                fabs((z1 + z0) * 0.5 * dxz);
+        if (which == 0) {
+            v = cfl_cell(d, c, dxt, dxz, f, i, j, k);
         } else {
             v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * dxz);
         }
