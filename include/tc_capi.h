@@ -287,6 +287,12 @@ const char* tc_profile_name(int cls);
 /* FP64 FMA throughput of the device in TFLOP/s (a dedicated probe kernel on
  * the handle's stream; used as the FP64 roofline denominator). */
 int tc_measure_fp64_peak(tc_handle* h, double* tflops);
+/* Self-check of the integer-pipe float <-> double conversions the mixed
+ * path uses: n operands (random bit patterns, the binary32 exponent range
+ * and rounding halfway cases) converted both ways and compared bit for bit
+ * with the hardware conversions on the current device; *mismatches receives
+ * the count (0 expected).  No counterpart in the reference. */
+int tc_selftest_conversions(long long n, long long* mismatches);
 
 #ifdef __cplusplus
 }

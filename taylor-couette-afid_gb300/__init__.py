@@ -119,6 +119,7 @@ SIGNATURES = {
     "tc_profile_read": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "tc_profile_name": (ctypes.c_char_p, [ctypes.c_int]),
     "tc_measure_fp64_peak": (ctypes.c_int, [_vp, _dp]),
+    "tc_selftest_conversions": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "tc_ensemble_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
     "tc_ensemble_destroy": (None, [_vp]),
     "tc_ensemble_last_error": (ctypes.c_char_p, [_vp]),
@@ -194,6 +195,16 @@ def check_divergence_noalloc(qt: int, qr: int, qz: int, nthm: int, nzm: int, nrm
                                        ctypes.byref(v))
     if rc != 0:
         raise TCError(rc, L.tc_last_error(None).decode())
+    return v.value
+
+
+def selftest_conversions(n: int = 1 << 24) -> int:
+    """Mismatches of the integer-pipe float <-> double conversions against the
+    hardware conversions over n operands (0 expected)."""
+    v = ctypes.c_longlong()
+    rc = lib().tc_selftest_conversions(int(n), ctypes.byref(v))
+    if rc != 0:
+        raise TCError(rc, "tc_selftest_conversions")
     return v.value
 
 

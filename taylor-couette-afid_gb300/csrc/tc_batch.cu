@@ -42,6 +42,7 @@ struct InstT {
     PlansT<T> p;
     MomArgs<T> ma[3];
     int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
+    T dxzq_t;         // dxzq in the element type
 };
 
 enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
     double v = 0.0;
     if (flat < I.d.P) {
         const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
-        v = cfl_cell(I.d, I.c, I.k.dxt, I.k.dxz, I.f, i, j, k);
+        v = cfl_cell(I.d, I.c, I.cv, I.k.dxt, I.k.dxz, I.f, i, j, k);
     }
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
     const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
     if (flat >= I.d.P) return;
     const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
-    correct_cell<true, true, T>(I.d, I.c, I.k.dxzq, I.f, sub, i, j, k);
+    correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, k);
 }
 
 // column-wise: item = TPB consecutive (z, theta) columns
@@ -223,9 +224,10 @@ __global__ void __launch_bounds__(128) ens_zfft_kernel(const InstT<T>* inst, con
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const int local = (int)(item - prefix[m]);
-    const int groups = (I.d.PH + kZC - 1) / kZC;
+    constexpr int ZC = ZCols<T>::value;
+    const int groups = (I.d.PH + ZC - 1) / ZC;
     const int kplane = local / groups, g = local - kplane * groups;
-    zfft_tile(I.d, I.f, I.p.z, I.p.tw_z, inv, g * kZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    zfft_tile(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
 int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
@@ -305,6 +307,7 @@ int rebuild(tc_ensemble* e) {
         I.d = h->d; I.cv = MC<T>(h); I.c = h->c; I.k = h->k; I.f = MF<T>(h); I.p = MP<T>(h);
         for (int s = 0; s < 3; ++s) I.ma[s] = make_mom_args(h->k, I.f, s);
         I.vdt = e->vdt[e->active[a]];
+        I.dxzq_t = (T)h->k.dxzq;
         const Dims& d = h->d;
         maxNz = std::max(maxNz, d.nz);
         long long cnt[PH_COUNT];
@@ -314,7 +317,7 @@ int rebuild(tc_ensemble* e) {
         cnt[PH_PTRI] = ceil_div((long long)d.nzh * d.PH, TPB);
         cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
         cnt[PH_THINV] = cnt[PH_DIV];
-        cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, kZC);
+        cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, ZCols<T>::value);
         cnt[PH_FACT] = 1;
         cnt[PH_CFL] = I.vdt ? cnt[PH_MOM] : 0;
         for (int p = 0; p < PH_COUNT; ++p) {
@@ -326,7 +329,7 @@ int rebuild(tc_ensemble* e) {
     for (int p = 0; p < PH_COUNT; ++p) e->items[p] = prefix[(size_t)p * (n + 1) + n];
     typedef typename V2<T>::type C2;
     e->smem_div = (size_t)2 * R * maxM * sizeof(C2);
-    e->smem_z = (size_t)2 * kZC * maxNz * sizeof(C2);
+    e->smem_z = (size_t)2 * ZCols<T>::value * maxNz * sizeof(C2);
     if (e->smem_div > 200 * 1024 || e->smem_z > 200 * 1024) return efail(e, 2011, "ensemble FFT tile exceeds shared memory");
     cudaError_t c = cudaMalloc(&e->inst_dev, sizeof(InstT<T>) * n);
     if (c == cudaSuccess) c = cudaMalloc(&e->prefix_dev, sizeof(int) * prefix.size());

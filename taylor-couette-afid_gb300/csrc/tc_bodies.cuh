@@ -10,6 +10,7 @@
 
 #include <type_traits>
 
+#include "tc_convert.cuh"
 #include "tc_fft.cuh"
 #include "tc_kernels.cuh"
 
@@ -19,7 +20,9 @@ namespace {
 
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 304;   // 2 x 152 SMs
-constexpr int kZC = 4;            // lines per z-FFT block
+// Columns (kt) per z-FFT block (8 columns measured slower for FP32: twice
+// the shared memory per block halves the resident blocks).
+template <typename T> struct ZCols { static constexpr int value = 4; };
 
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
@@ -64,7 +67,18 @@ __device__ void begin_step_body(const Consts& k, StepState* st, int mode, double
     st->beta = dt / k.ren * 0.5;                                                  // TimeMarcher.F90:20
     st->vinner_t = k.sizepert * sin(2.0 * k.pi * k.omegapert * time);             // InnerCylVelocity.F90:15
     st->dvinner_t = 2.0 * k.pi * k.omegapert * k.sizepert * cos(2.0 * k.pi * k.omegapert * time) * dt;
+    st->dt_f = (float)dt;
+    st->beta_f = (float)st->beta;
+    st->vinner_f = (float)st->vinner_t;
 }
+
+// dt and vinner_t in the element type T (FP32 copies made once per step).
+template <typename T> __device__ __forceinline__ T step_dt(const StepState* st);
+template <> __device__ __forceinline__ double step_dt<double>(const StepState* st) { return st->dt; }
+template <> __device__ __forceinline__ float step_dt<float>(const StepState* st) { return st->dt_f; }
+template <typename T> __device__ __forceinline__ T step_vinner(const StepState* st);
+template <> __device__ __forceinline__ double step_vinner<double>(const StepState* st) { return st->vinner_t; }
+template <> __device__ __forceinline__ float step_vinner<float>(const StepState* st) { return st->vinner_f; }
 
 // Row-scaled momentum matrices of SolveImpEqnUpdate_QT/QR/QZ and their LU
 // factors for every substep of the step (dgttrf without row interchanges:
@@ -162,12 +176,30 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, cons
     }
 }
 
+// Neighbour offsets of cell (i, j, k) relative to its own index o, in
+// elements (32-bit): the periodic wraps in theta and z are folded into dim,
+// dip, djm, djp; radial neighbours are +-P.  Loads then cost one address add
+// each instead of a 64-bit index product.
 struct Stencil {
-    int i, j, k, im, ip, jm, jp;
-    size_t P;
-    int nt;
-    __device__ size_t at(int kk, int jj, int ii) const { return (size_t)kk * P + (size_t)jj * nt + ii; }
+    size_t o;
+    int dim, dip, djm, djp, P;
+    int k, kmm, kpp;          // radial index and its clamped neighbours (kmv/kpv)
 };
+
+__device__ __forceinline__ Stencil make_stencil(const Dims& d, int i, int j, int k) {
+    Stencil S;
+    const int nt = d.nt, nz = d.nz;
+    S.P = (int)d.P;
+    S.o = (size_t)k * (size_t)d.P + (size_t)j * nt + i;
+    S.dim = i == 0 ? nt - 1 : -1;
+    S.dip = i == nt - 1 ? 1 - nt : 1;
+    S.djm = j == 0 ? (nz - 1) * nt : -nt;
+    S.djp = j == nz - 1 ? -(nz - 1) * nt : nt;
+    S.k = k;
+    S.kmm = k > 0 ? k - 1 : 0;
+    S.kpp = k < d.nr - 1 ? k + 1 : d.nr - 1;
+    return S;
+}
 
 // Scalars of the momentum kernel in the element type T.
 template <typename T>
@@ -183,18 +215,18 @@ struct MomArgs {
     int use_ru;
 };
 
-// ExplicitTermsQT.F90:40-125 at cell (i, j, k)
+// ExplicitTermsQT.F90:40-125 at cell (i, j, k); qt, qr, qz point at the cell.
 template <typename T>
-__device__ T explicit_qt(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
-    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
-    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
-    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip)), t_im = ld(qt + S.at(k, S.j, S.im));
-    T t_jp = ld(qt + S.at(k, S.jp, S.i)), t_jm = ld(qt + S.at(k, S.jm, S.i));
-    T t_kp = ld(qt + S.at(kpp, S.j, S.i)), t_km = ld(qt + S.at(kmm, S.j, S.i));
-    T r_c = ld(qr + S.at(k, S.j, S.i)), r_im = ld(qr + S.at(k, S.j, S.im));
-    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pim = ld(qr + S.at(kp, S.j, S.im));
-    T z_c = ld(qz + S.at(k, S.j, S.i)), z_im = ld(qz + S.at(k, S.j, S.im));
-    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jpim = ld(qz + S.at(k, S.jp, S.im));
+__device__ T explicit_qt(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A, const T* qt, const T* qr,
+                         const T* qz) {
+    const int k = S.k, kp = k + 1, P = S.P;
+    T t_c = ld(qt), t_ip = ld(qt + S.dip), t_im = ld(qt + S.dim);
+    T t_jp = ld(qt + S.djp), t_jm = ld(qt + S.djm);
+    T t_kp = ld(qt + (S.kpp - k) * P), t_km = ld(qt + (S.kmm - k) * P);
+    T r_c = ld(qr), r_im = ld(qr + S.dim);
+    T r_p = ld(qr + P), r_pim = ld(qr + P + S.dim);
+    T z_c = ld(qz), z_im = ld(qz + S.dim);
+    T z_jp = ld(qz + S.djp), z_jpim = ld(qz + S.djp + S.dim);
     const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
     const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
     const T two = (T)2.0;
@@ -214,16 +246,16 @@ __device__ T explicit_qt(const Stencil& S, int nr, const CoefT<T>& c, const MomA
 
 // ExplicitTermsQR.F90:180-280 at face (i, j, k), 1 <= k <= nr-1
 template <typename T>
-__device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A) {
-    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
-    const int k = S.k, km = k - 1, kp = k + 1;
-    T t_c = ld(qt + S.at(k, S.j, S.i)), t_m = ld(qt + S.at(km, S.j, S.i));
-    T t_ip = ld(qt + S.at(k, S.j, S.ip)), t_mip = ld(qt + S.at(km, S.j, S.ip));
-    T r_c = ld(qr + S.at(k, S.j, S.i)), r_ip = ld(qr + S.at(k, S.j, S.ip)), r_im = ld(qr + S.at(k, S.j, S.im));
-    T r_jp = ld(qr + S.at(k, S.jp, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
-    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_m = ld(qr + S.at(km, S.j, S.i));
-    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_mjp = ld(qz + S.at(km, S.jp, S.i));
-    T z_c = ld(qz + S.at(k, S.j, S.i)), z_m = ld(qz + S.at(km, S.j, S.i));
+__device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A, const T* qt, const T* qr,
+                         const T* qz) {
+    const int k = S.k, km = k - 1, kp = k + 1, P = S.P;
+    T t_c = ld(qt), t_m = ld(qt - P);
+    T t_ip = ld(qt + S.dip), t_mip = ld(qt - P + S.dip);
+    T r_c = ld(qr), r_ip = ld(qr + S.dip), r_im = ld(qr + S.dim);
+    T r_jp = ld(qr + S.djp), r_jm = ld(qr + S.djm);
+    T r_p = ld(qr + P), r_m = ld(qr - P);
+    T z_jp = ld(qz + S.djp), z_mjp = ld(qz - P + S.djp);
+    T z_c = ld(qz), z_m = ld(qz - P);
     const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
     const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
     const T two = (T)2.0;
@@ -241,16 +273,16 @@ __device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
 
 // ExplicitTermsQZ.F90:328-390 at cell (i, j, k)
 template <typename T>
-__device__ T explicit_qz(const Stencil& S, int nr, const CoefT<T>& c, const MomArgs<T>& A) {
-    const T *qt = A.qt, *qr = A.qr, *qz = A.qz;
-    const int k = S.k, kmm = k > 0 ? k - 1 : 0, kpp = k < nr - 1 ? k + 1 : nr - 1, kp = k + 1;
-    T t_c = ld(qt + S.at(k, S.j, S.i)), t_ip = ld(qt + S.at(k, S.j, S.ip));
-    T t_jm = ld(qt + S.at(k, S.jm, S.i)), t_jmip = ld(qt + S.at(k, S.jm, S.ip));
-    T z_c = ld(qz + S.at(k, S.j, S.i)), z_ip = ld(qz + S.at(k, S.j, S.ip)), z_im = ld(qz + S.at(k, S.j, S.im));
-    T z_jp = ld(qz + S.at(k, S.jp, S.i)), z_jm = ld(qz + S.at(k, S.jm, S.i));
-    T z_kp = ld(qz + S.at(kpp, S.j, S.i)), z_km = ld(qz + S.at(kmm, S.j, S.i));
-    T r_p = ld(qr + S.at(kp, S.j, S.i)), r_pjm = ld(qr + S.at(kp, S.jm, S.i));
-    T r_c = ld(qr + S.at(k, S.j, S.i)), r_jm = ld(qr + S.at(k, S.jm, S.i));
+__device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A, const T* qt, const T* qr,
+                         const T* qz) {
+    const int k = S.k, P = S.P;
+    T t_c = ld(qt), t_ip = ld(qt + S.dip);
+    T t_jm = ld(qt + S.djm), t_jmip = ld(qt + S.djm + S.dip);
+    T z_c = ld(qz), z_ip = ld(qz + S.dip), z_im = ld(qz + S.dim);
+    T z_jp = ld(qz + S.djp), z_jm = ld(qz + S.djm);
+    T z_kp = ld(qz + (S.kpp - k) * P), z_km = ld(qz + (S.kmm - k) * P);
+    T r_p = ld(qr + P), r_pjm = ld(qr + P + S.djm);
+    T r_c = ld(qr), r_jm = ld(qr + S.djm);
     const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
     const T two = (T)2.0;
     T h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
@@ -265,15 +297,17 @@ template <int MODE, typename T>
 __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
                                               int k) {
     const int nr = d.nr;
-    Stencil S;
-    S.i = i; S.j = j; S.k = k; S.nt = d.nt; S.P = (size_t)d.P;
-    S.im = wm(i, d.nt); S.ip = wp(i, d.nt); S.jm = wm(j, d.nz); S.jp = wp(j, d.nz);
-    const size_t o = S.at(k, j, i);
+    const Stencil S = make_stencil(d, i, j, k);
+    const size_t o = S.o;
+    const int P = S.P;
+    const T* qt = a.qt + o;
+    const T* qr = a.qr + o;
+    const T* qz = a.qz + o;
     T ht = 0, hr = 0, hz = 0;
     if (MODE != MODE_IMPLICIT) {
-        ht = explicit_qt(S, nr, c, a);
-        if (k >= 1) hr = explicit_qr(S, c, a);
-        hz = explicit_qz(S, nr, c, a);
+        ht = explicit_qt(S, c, a, qt, qr, qz);
+        if (k >= 1) hr = explicit_qr(S, c, a, qt, qr, qz);
+        hz = explicit_qz(S, c, a, qt, qr, qz);
         if (MODE == MODE_EXPLICIT) {
             a.h_t[o] = ht;
             if (k >= 1) a.h_r[o] = hr;
@@ -285,14 +319,11 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
         if (k >= 1) hr = a.h_r[o];
         hz = a.h_z[o];
     }
-    const T dt = (T)a.st->dt, ga = a.ga, ro = a.ro, alre = a.alre;
+    const T dt = step_dt<T>(a.st), ga = a.ga, ro = a.ro, alre = a.alre;
     const T one = (T)1.0;
     const T fic = a.icyl ? (T)a.icyl[(size_t)j * d.nt + i] : one, foc = one;
-    const T* qt = a.qt;
-    const T* qr = a.qr;
-    const T* qz = a.qz;
-    const T* pr = a.pr;
-    const T p_c = ld(pr + o);
+    const T* pr = a.pr + o;
+    const T p_c = ld(pr);
     // ---- qt (ImplicitAndUpdateQT.F90:45-115)
     {
         T d33;
@@ -300,27 +331,25 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
             T app = ld(c.ap1j);
             T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
             T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
-            d33 = ld(qt + S.at(1, j, i)) * app + ld(qt + o) * acc + (a.virotint + (T)a.st->vinner_t) * amm;
+            d33 = ld(qt + P) * app + ld(qt) * acc + (a.virotint + step_vinner<T>(a.st)) * amm;
         } else if (k == nr - 1) {
             T amm = ld(c.am1j + k);
             T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
             T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
-            d33 = a.virotext * app + ld(qt + o) * acc + ld(qt + S.at(k - 1, j, i)) * amm;
+            d33 = a.virotext * app + ld(qt) * acc + ld(qt - P) * amm;
         } else {
-            d33 = ld(qt + S.at(k + 1, j, i)) * ld(c.ap1j + k) + ld(qt + o) * ld(c.ac1j + k) +
-                  ld(qt + S.at(k - 1, j, i)) * ld(c.am1j + k);
+            d33 = ld(qt + P) * ld(c.ap1j + k) + ld(qt) * ld(c.ac1j + k) + ld(qt - P) * ld(c.am1j + k);
         }
-        T dpx11 = (p_c - ld(pr + S.at(k, j, S.im))) * a.dxt_al * ld(c.usrm + k);
+        T dpx11 = (p_c - ld(pr + S.dim)) * a.dxt_al * ld(c.usrm + k);
         T old = a.use_ru ? a.ru1[o] : (T)0;
         a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
         a.ru1[o] = ht;
     }
     // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
     if (k >= 1) {
-        T d33 = ld(qr + S.at(k + 1, j, i)) * ld(c.ap2je + k) + ld(qr + o) * ld(c.ac2je + k) +
-                ld(qr + S.at(k - 1, j, i)) * ld(c.am2je + k);
+        T d33 = ld(qr + P) * ld(c.ap2je + k) + ld(qr) * ld(c.ac2je + k) + ld(qr - P) * ld(c.am2je + k);
         T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
-        T dpx22 = (p_c - ld(pr + S.at(k - 1, j, i))) * udx2;
+        T dpx22 = (p_c - ld(pr - P)) * udx2;
         T old = a.use_ru ? a.ru2[o] : (T)0;
         a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
         a.ru2[o] = hr;
@@ -332,18 +361,17 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
             T app = ld(c.ap3j);
             T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
             T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
-            T q0 = ld(qz + o);
-            d33 = ld(qz + S.at(1, j, i)) * app + q0 * acc + q0 * amm;
+            T q0 = ld(qz);
+            d33 = ld(qz + P) * app + q0 * acc + q0 * amm;
         } else if (k == nr - 1) {
             T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
             T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
-            T q0 = ld(qz + o);
-            d33 = q0 * app + q0 * acc + ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+            T q0 = ld(qz);
+            d33 = q0 * app + q0 * acc + ld(qz - P) * ld(c.am3j + k);
         } else {
-            d33 = ld(qz + S.at(k + 1, j, i)) * ld(c.ap3j + k) + ld(qz + o) * ld(c.ac3j + k) +
-                  ld(qz + S.at(k - 1, j, i)) * ld(c.am3j + k);
+            d33 = ld(qz + P) * ld(c.ap3j + k) + ld(qz) * ld(c.ac3j + k) + ld(qz - P) * ld(c.am3j + k);
         }
-        T dpx33 = (p_c - ld(pr + S.at(k, S.jm, i))) * a.dxz_al;
+        T dpx33 = (p_c - ld(pr + S.djm)) * a.dxz_al;
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
         T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
@@ -352,66 +380,69 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
     }
 }
 
+// One LU-factored tridiagonal along r for one column: forward elimination
+// into rhs (y_k0 = (rhs_k0 + extra) sc_k0, y_k = rhs_k sc_k - l_k y_k-1),
+// then back substitution adding the solution to q.  Planes are loaded in
+// batches of kRB ahead of the dependent arithmetic, so that each thread keeps
+// several loads in flight (the recurrence itself is sequential).
+constexpr int kRB = 8;
+
+template <bool EXTRA, typename T>
+__device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
+                                          const T* l, const T* di, const T* u, const T* sc, T extra) {
+    T y = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
+    rhs[(size_t)k0 * P] = y;
+    int k = k0 + 1;
+    for (; k + kRB <= nr; k += kRB) {
+        T r[kRB];
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) r[b] = rhs[(size_t)(k + b) * P];
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
+            rhs[(size_t)(k + b) * P] = y;
+        }
+    }
+    for (; k < nr; ++k) {
+        y = rhs[(size_t)k * P] * ld(sc + k) - ld(l + k) * y;
+        rhs[(size_t)k * P] = y;
+    }
+    T x = y * ld(di + nr - 1);
+    q[(size_t)(nr - 1) * P] += x;
+    k = nr - 2;
+    for (; k - (kRB - 1) >= k0; k -= kRB) {
+        T r[kRB], v[kRB];
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            r[b] = rhs[(size_t)(k - b) * P];
+            v[b] = q[(size_t)(k - b) * P];
+        }
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            x = (r[b] - ld(u + k - b) * x) * ld(di + k - b);
+            q[(size_t)(k - b) * P] = v[b] + x;
+        }
+    }
+    for (; k >= k0; --k) {
+        x = (rhs[(size_t)k * P] - ld(u + k) * x) * ld(di + k);
+        q[(size_t)k * P] += x;
+    }
+}
+
+// SolveImpEqnUpdate_QT.F90:65-78, _QR.F90:136-150 (faces 1..nr-1),
+// _QZ.F90:214-224 for the column `col`.
 template <typename T>
 __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f, int sub, long long col) {
     const int nr = d.nr;
     const size_t P = (size_t)d.P;
     const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
     const MomFactorsT<T>& F = f.F;
-    // qt: SolveImpEqnUpdate_QT.F90:65-78
-    {
-        const T *l = F.l(sub, 0, v), *di = F.dinv(sub, 0, v), *u = F.u(sub, 0, v), *sc = F.scale(sub, 0);
-        T* rhs = f.rhs_t + col;
-        T* q = f.qt + col;
-        T y = (rhs[0] + *F.extra(sub)) * ld(sc);
-        rhs[0] = y;
-        for (int k = 1; k < nr; ++k) {
-            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
-            rhs[k * P] = y;
-        }
-        T x = y * ld(di + nr - 1);
-        q[(nr - 1) * P] += x;
-        for (int k = nr - 2; k >= 0; --k) {
-            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
-            q[k * P] += x;
-        }
-    }
-    // qr: SolveImpEqnUpdate_QR.F90:136-150, faces 1..nr-1
-    {
-        const T *l = F.l(sub, 1, 0), *di = F.dinv(sub, 1, 0), *u = F.u(sub, 1, 0), *sc = F.scale(sub, 1);
-        T* rhs = f.rhs_r + col;
-        T* q = f.qr + col;
-        T y = rhs[P] * ld(sc + 1);
-        rhs[P] = y;
-        for (int k = 2; k < nr; ++k) {
-            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
-            rhs[k * P] = y;
-        }
-        T x = y * ld(di + nr - 1);
-        q[(nr - 1) * P] += x;
-        for (int k = nr - 2; k >= 1; --k) {
-            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
-            q[k * P] += x;
-        }
-    }
-    // qz: SolveImpEqnUpdate_QZ.F90:214-224
-    {
-        const T *l = F.l(sub, 2, v), *di = F.dinv(sub, 2, v), *u = F.u(sub, 2, v), *sc = F.scale(sub, 2);
-        T* rhs = f.rhs_z + col;
-        T* q = f.qz + col;
-        T y = rhs[0] * ld(sc);
-        rhs[0] = y;
-        for (int k = 1; k < nr; ++k) {
-            y = rhs[k * P] * ld(sc + k) - ld(l + k) * y;
-            rhs[k * P] = y;
-        }
-        T x = y * ld(di + nr - 1);
-        q[(nr - 1) * P] += x;
-        for (int k = nr - 2; k >= 0; --k) {
-            x = (rhs[k * P] - ld(u + k) * x) * ld(di + k);
-            q[k * P] += x;
-        }
-    }
+    lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
+                    F.scale(sub, 0), *F.extra(sub));
+    lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0),
+                     F.scale(sub, 1), (T)0);
+    lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v),
+                     F.scale(sub, 2), (T)0);
 }
 
 __device__ __forceinline__ double2 ld2(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }
@@ -454,11 +485,12 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
     // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in
     const T scl = (T)(FROM_PHI ? fft_norm : f.scal[sub]);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
-        const int r = t / M, m = t - r * M;
+        const int r = fdiv(t, pl.mn), m = t - r * M;
         const long long row = row0 + r;
         C2 z = mk2((T)0, (T)0);
         if (row < nrows) {
-            const int k = (int)(row / d.nz), j = (int)(row - (long long)k * d.nz);
+            const int k = d.mnz ? fdiv((int)row, d.mnz) : (int)(row / d.nz);
+            const int j = (int)(row - (long long)k * d.nz);
             if (FROM_PHI) z = ld2(f.phi + (size_t)row * d.nt + 2 * m);
             else z = div_pair(d, c, dxt, dxz, f.qt, f.qr, f.qz, k, j, m);
             z.x *= scl;
@@ -471,7 +503,7 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
     // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
     const int PH = M + 1;
     for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
-        const int r = t / PH, kt = t - r * PH;
+        const int r = fdiv(t, pl.mn1), kt = t - r * PH;
         const long long row = row0 + r;
         if (row >= nrows) continue;
         const int k1 = kt == M ? 0 : kt, k2 = kt == 0 ? 0 : M - kt;
@@ -489,26 +521,27 @@ template <typename T>
 __device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
                           int inv, int kt0, int kplane, typename V2<T>::type* smem) {
     typedef typename V2<T>::type C2;
+    constexpr int ZC = ZCols<T>::value;
     const int nz = pl.n, PH = d.PH;
     C2* a = smem;
-    C2* b = smem + (size_t)kZC * nz;
+    C2* b = smem + (size_t)ZC * nz;
     C2* plane = f.spec + (size_t)kplane * d.PS;
-    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
-        const int c = t % kZC, j = t / kZC;
+    for (int t = threadIdx.x; t < ZC * nz; t += blockDim.x) {
+        const int c = t % ZC, j = t / ZC;
         a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
     }
     __syncthreads();
-    const C2* Z = fft_lines<kZC>(a, b, pl, tw, inv != 0);
-    for (int t = threadIdx.x; t < kZC * nz; t += blockDim.x) {
-        const int c = t % kZC, j = t / kZC;
+    const C2* Z = fft_lines<ZC>(a, b, pl, tw, inv != 0);
+    for (int t = threadIdx.x; t < ZC * nz; t += blockDim.x) {
+        const int c = t % ZC, j = t / ZC;
         if (kt0 + c < PH) plane[(size_t)j * PH + kt0 + c] = Z[t];
     }
 }
 
 __device__ __forceinline__ double2 to_d2(double2 v) { return v; }
-__device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_d2(float2 v) { return f2d(v); }
 __device__ __forceinline__ void st2(double2* p, double x, double y) { *p = make_double2(x, y); }
-__device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_float2((float)x, (float)y); }
+__device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_float2(d2f(x), d2f(y)); }
 
 // SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
 // matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
@@ -530,36 +563,79 @@ __device__ __forceinline__ void ptri_mode(const Dims& d, const Coef& c, const Fi
     double2* w2 = ws + o2;
     const double* L = f.pf_l + t;
     const double* DI = f.pf_dinv + t;
+    // forward sweep, planes loaded kRB at a time ahead of the recurrence
     double2 y1 = to_d2(x1[0]), y2 = two ? to_d2(x2[0]) : make_double2(0.0, 0.0);
     w1[0] = y1;
     if (two) w2[0] = y2;
-#pragma unroll 4
-    for (int k = 1; k < nr; ++k) {
-        const double l = ld(L + k * FS);
-        double2 b1 = to_d2(x1[k * PS]);
-        y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
-        w1[k * PS] = y1;
-        if (two) {
-            double2 b2 = to_d2(x2[k * PS]);
-            y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
-            w2[k * PS] = y2;
+    int k = 1;
+    for (; k + kRB <= nr; k += kRB) {
+        C2 b1[kRB], b2[kRB];
+        double l[kRB];
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            l[b] = ld(L + (size_t)(k + b) * FS);
+            b1[b] = x1[(size_t)(k + b) * PS];
+            if (two) b2[b] = x2[(size_t)(k + b) * PS];
+        }
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            const double2 v1 = to_d2(b1[b]);
+            y1 = make_double2(v1.x - l[b] * y1.x, v1.y - l[b] * y1.y);
+            w1[(size_t)(k + b) * PS] = y1;
+            if (two) {
+                const double2 v2 = to_d2(b2[b]);
+                y2 = make_double2(v2.x - l[b] * y2.x, v2.y - l[b] * y2.y);
+                w2[(size_t)(k + b) * PS] = y2;
+            }
         }
     }
+    for (; k < nr; ++k) {
+        const double l = ld(L + (size_t)k * FS);
+        double2 b1 = to_d2(x1[(size_t)k * PS]);
+        y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
+        w1[(size_t)k * PS] = y1;
+        if (two) {
+            double2 b2 = to_d2(x2[(size_t)k * PS]);
+            y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
+            w2[(size_t)k * PS] = y2;
+        }
+    }
+    // back substitution
     double di = ld(DI + (size_t)(nr - 1) * FS);
     double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
     st2(x1 + (size_t)(nr - 1) * PS, s1.x, s1.y);
     if (two) st2(x2 + (size_t)(nr - 1) * PS, s2.x, s2.y);
-#pragma unroll 4
-    for (int k = nr - 2; k >= 0; --k) {
+    k = nr - 2;
+    for (; k - (kRB - 1) >= 0; k -= kRB) {
+        double2 b1[kRB], b2[kRB];
+        double u[kRB], dv[kRB];
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            u[b] = ld(c.apph + k - b);
+            dv[b] = ld(DI + (size_t)(k - b) * FS);
+            b1[b] = w1[(size_t)(k - b) * PS];
+            if (two) b2[b] = w2[(size_t)(k - b) * PS];
+        }
+#pragma unroll
+        for (int b = 0; b < kRB; ++b) {
+            s1 = make_double2((b1[b].x - u[b] * s1.x) * dv[b], (b1[b].y - u[b] * s1.y) * dv[b]);
+            st2(x1 + (size_t)(k - b) * PS, s1.x, s1.y);
+            if (two) {
+                s2 = make_double2((b2[b].x - u[b] * s2.x) * dv[b], (b2[b].y - u[b] * s2.y) * dv[b]);
+                st2(x2 + (size_t)(k - b) * PS, s2.x, s2.y);
+            }
+        }
+    }
+    for (; k >= 0; --k) {
         const double u = ld(c.apph + k);
-        di = ld(DI + k * FS);
-        double2 b1 = w1[k * PS];
+        di = ld(DI + (size_t)k * FS);
+        double2 b1 = w1[(size_t)k * PS];
         s1 = make_double2((b1.x - u * s1.x) * di, (b1.y - u * s1.y) * di);
-        st2(x1 + k * PS, s1.x, s1.y);
+        st2(x1 + (size_t)k * PS, s1.x, s1.y);
         if (two) {
-            double2 b2 = w2[k * PS];
+            double2 b2 = w2[(size_t)k * PS];
             s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
-            st2(x2 + k * PS, s2.x, s2.y);
+            st2(x2 + (size_t)k * PS, s2.x, s2.y);
         }
     }
 }
@@ -574,7 +650,7 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
     C2* b = smem + (size_t)R * M;
     const long long nrows = (long long)d.nr * d.nz;
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
-        const int r = t / M, kt = t - r * M;
+        const int r = fdiv(t, pl.mn), kt = t - r * M;
         const long long row = row0 + r;
         C2 z = mk2((T)0, (T)0);
         if (row < nrows) {
@@ -593,15 +669,15 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
     __syncthreads();
     const C2* Z = fft_lines<R>(a, b, pl, tw, true);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
-        const int r = t / M, m = t - r * M;
+        const int r = fdiv(t, pl.mn), m = t - r * M;
         const long long row = row0 + r;
         if (row < nrows) *reinterpret_cast<C2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
     }
 }
 
 template <bool VEL, bool PRES, typename T>
-__device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, double dxzq, const FieldsT<T>& f, int sub,
-                                             int i, int j, int k) {
+__device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxzq, T dxzq_t,
+                                             const FieldsT<T>& f, int sub, int i, int j, int k) {
     const int nt = d.nt, nr = d.nr;
     const size_t P = (size_t)d.P;
     const int im = wm(i, nt), ip = wp(i, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
@@ -633,18 +709,19 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, doubl
             // mixed path: the increment phi - beta lap(phi) from the FP32 phi in
             // FP32, accumulated into the FP64 pressure; the FP32 copy used by
             // the momentum rhs is refreshed from the FP64 sum
+            // (coefficients from the FP32 copies, conversions on the integer pipes)
             const T pip = ld(phi + (size_t)k * P + rowoff + ip);
             const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
             const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
-            const T be = (T)f.st->beta;
-            const T app = (T)ld(c.apph + k), acc = (T)ld(c.acph + k), amm = app;   // amm = apph(kc)
+            const float be = f.st->beta_f;
+            const T app = ld(cv.apph + k), acc = ld(cv.acph + k), amm = app;   // amm = apph(kc)
             const T two = (T)2.0;
-            const T inc = loc - be * ((pip - two * loc + pim) * (T)ld(c.udx1qm + k) +
-                                      (pjp - two * loc + pjm) * (T)dxzq +
+            const T inc = loc - be * ((pip - two * loc + pim) * ld(cv.udx1qm + k) +
+                                      (pjp - two * loc + pjm) * dxzq_t +
                                       (pkp * app + loc * acc + pkm * amm));
-            const double p = f.pr[o] + (double)inc;
+            const double p = f.pr[o] + f2d((float)inc);
             f.pr[o] = p;
-            f.prf[o] = (T)p;
+            f.prf[o] = (T)d2f(p);
         }
     }
 }
@@ -652,17 +729,17 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, doubl
 // CalcMaxCFL.F90:30-43 at cell (i, j, k); in FP32 on the mixed path (the
 // maximum itself is exact in any precision).
 template <typename T>
-__device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, double dxt, double dxz, const FieldsT<T>& f,
-                                           int i, int j, int k) {
+__device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxt, double dxz,
+                                           const FieldsT<T>& f, int i, int j, int k) {
     const size_t P = (size_t)d.P;
     const int ip = wp(i, d.nt), jp = wp(j, d.nz);
     const size_t o = (size_t)k * P + (size_t)j * d.nt + i;
     if (!std::is_same<T, double>::value) {
         const T h = (T)0.5;
-        const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * (T)ld(c.usrm + k)));
-        const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * (T)ld(c.udx2rm + k)));
+        const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * ld(cv.usrm + k)));
+        const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * ld(cv.udx2rm + k)));
         const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
-        return (double)(vt + vr + vz);
+        return f2d((float)(vt + vr + vz));
     }
     const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
     const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);

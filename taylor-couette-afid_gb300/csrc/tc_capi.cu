@@ -47,6 +47,7 @@ cudaError_t dalloc(tc_handle* h, T** p, size_t count) {
 
 // Radix plan: radix-4 stages first, then 2, 3, 5.
 bool make_plan(int n, FFTPlan& P) {
+    if (n < 1 || n > 65536) return false;
     P.n = n;
     P.nstages = 0;
     int m = n;
@@ -56,6 +57,14 @@ bool make_plan(int n, FFTPlan& P) {
             P.radix[P.nstages++] = r;
             m /= r;
         }
+    int L = 1;
+    for (int st = 0; st < P.nstages; ++st) {
+        L *= P.radix[st];
+        P.rp[st] = n / L;
+        P.mrp[st] = div_magic((unsigned)P.rp[st]);
+    }
+    P.mn = div_magic((unsigned)n);
+    P.mn1 = div_magic((unsigned)n + 1u);
     return m == 1;
 }
 
@@ -218,6 +227,7 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     d.M = d.nt / 2; d.PH = d.M + 1; d.nzh = d.nz / 2 + 1;
     d.P = (long long)d.nz * d.nt;
     d.PS = (long long)d.nz * d.PH;
+    d.mnz = ((unsigned long long)d.nr * d.nz * d.nz < (1ull << 32)) ? div_magic((unsigned)d.nz) : 0u;
     const int nr = d.nr, nrr = nr + 1;
 
     Consts& k = h->k;
@@ -480,7 +490,7 @@ static void enqueue_substeps(tc_handle* h) {
         L(h, K_PTRI, 1, [&] { launch_pressure_tridiag(s, h->d, h->c, f); });
         L(h, K_ZFFT, 1, [&] { launch_zfft(s, h->d, f, p, true); });
         L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, f, p); });
-        L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, true, true); });
+        L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, CF<T>(h), h->k, f, sub, true, true); });
     }
 }
 
@@ -527,13 +537,13 @@ static void enqueue_run(tc_handle* h, int nsteps, int nt0, double t0) {
     const FieldsT<T>& f = F<T>(h);
     L(h, K_CONTROL, 1, [&] { set_clock_kernel<<<1, 1, 0, s>>>(h->st, nt0, t0); });
     for (int n = 0; n < nsteps; ++n) {
-        L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, f); });
+        L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, CF<T>(h), h->k, f); });
         enqueue_begin<T>(h, 1, 0.0, 0.0);
         enqueue_substeps<T>(h);
         L(h, K_CONTROL, 1, [&] { launch_end_step(s, h->k, h->st); });
         L(h, K_REDUCE, 4, [&] {
             launch_velocity_stats(s, h->d, h->c, h->k, f, true);
-            launch_check_divergence(s, h->d, h->c, h->k, f, true);
+            launch_check_divergence(s, h->d, h->c, CF<T>(h), h->k, f, true);
         });
         L(h, K_CONTROL, 1, [&] { launch_finish_step(s, h->k, h->st); });
     }
@@ -616,10 +626,10 @@ static int routine(tc_handle* h, int which) {
             L(h, K_THINV, 1, [&] { launch_theta_inverse(s, h->d, f, p); });
             break;
         case 6:
-            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, true, false); });
+            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, CF<T>(h), h->k, f, sub, true, false); });
             break;
         default:
-            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, h->k, f, sub, false, true); });
+            L(h, K_CORRECT, 1, [&] { launch_correct(s, h->d, h->c, CF<T>(h), h->k, f, sub, false, true); });
             break;
     }
     return 0;
@@ -646,8 +656,8 @@ static void enqueue_reduce(tc_handle* h, int which) {
     cudaStream_t s = h->stream;
     const FieldsT<T>& f = F<T>(h);
     switch (which) {
-        case 0: L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, h->k, f); }); break;
-        case 1: L(h, K_REDUCE, 2, [&] { launch_check_divergence(s, h->d, h->c, h->k, f, false); }); break;
+        case 0: L(h, K_REDUCE, 2, [&] { launch_cfl(s, h->d, h->c, CF<T>(h), h->k, f); }); break;
+        case 1: L(h, K_REDUCE, 2, [&] { launch_check_divergence(s, h->d, h->c, CF<T>(h), h->k, f, false); }); break;
         case 2: L(h, K_REDUCE, 2, [&] { launch_torque(s, h->d, h->c, h->k, f); }); break;
         default: L(h, K_REDUCE, 2, [&] { launch_velocity_stats(s, h->d, h->c, h->k, f, false); }); break;
     }

@@ -26,12 +26,23 @@ template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 type; };
 template <> struct V2<float> { typedef float2 type; };
 
-// Radix plan of one complex transform length (radices 2, 3, 4, 5).
+// Radix plan of one complex transform length (radices 2, 3, 4, 5), with the
+// stride rp = n / (L p) of every Stockham stage and the multipliers that turn
+// the kernels' divisions by rp, n and n + 1 into a multiply-high:
+// x / d = umulhi(x, ceil(2^32 / d)) exactly when x * d < 2^32 (n <= 65536);
+// a multiplier of 0 stands for d = 1.
 struct FFTPlan {
     int n = 0;
     int nstages = 0;
     int radix[kMaxStages] = {0};
+    int rp[kMaxStages] = {0};
+    unsigned mrp[kMaxStages] = {0};
+    unsigned mn = 0, mn1 = 0;
 };
+
+inline unsigned div_magic(unsigned d) {
+    return d <= 1 ? 0u : (unsigned)(((1ull << 32) + d - 1) / d);
+}
 
 struct Dims {
     int nt, nz, nr;        // nthm, nzm, nrm
@@ -39,6 +50,7 @@ struct Dims {
     int nzh;               // nzm/2 + 1
     long long P;           // nz * nt (one r-plane of a real field)
     long long PS;          // nz * PH (one r-plane of the spectrum)
+    unsigned mnz;          // row / nz multiplier for rows < nr * nz (0: divide in hardware)
 };
 
 // 1-D coefficient arrays on the device, 0-based (entry m = reference m+1).
@@ -90,6 +102,9 @@ struct StepState {
     int errorcode;      // code raised by the last step
     int halt;           // a step raised an error: later steps do nothing
     int output;         // the last step was an output step
+    // dt, beta and vinner_t rounded once per step for the FP32 kernels of the
+    // mixed path (so that they do not convert per cell)
+    float dt_f, beta_f, vinner_f, pad_f;
 };
 
 // Factors of the row-scaled momentum matrices of one step: for each substep

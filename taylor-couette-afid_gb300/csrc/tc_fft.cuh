@@ -91,15 +91,18 @@ template <typename C2> __device__ __forceinline__ void dft5(C2* v, bool inv) {
 
 // One Stockham stage of radix p (compile time) over C interleaved lines:
 // sub-DFTs of length L become length L*p.
+// x / d with the plan's multiplier m (m = 0: d = 1).
+__device__ __forceinline__ int fdiv(int x, unsigned m) { return m ? (int)__umulhi((unsigned)x, m) : x; }
+
 template <int C, int p, typename C2>
-__device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restrict__ b, int n, int L,
-                                          const C2* __restrict__ tw, bool inv) {
-    const int Lp = L * p, rp = n / Lp, r = rp * p;
+__device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restrict__ b, int n, int L, int rp,
+                                          unsigned mrp, const C2* __restrict__ tw, bool inv) {
+    const int r = rp * p;
     const int nb = (n / p) * C;
     const int istep = rp * C, ostep = rp * L * C;
     for (int t = threadIdx.x; t < nb; t += blockDim.x) {
         const int c = t % C, bf = t / C;
-        const int q = bf % rp, s = bf / rp;
+        const int s = fdiv(bf, mrp), q = bf - s * rp;
         const C2* in = a + (size_t)(q + r * s) * C + c;
         C2* out = b + (size_t)(q + rp * s) * C + c;
         C2 v[p];
@@ -126,11 +129,12 @@ __device__ C2* fft_lines(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv)
     const int n = P.n;
     int L = 1;
     for (int st = 0; st < P.nstages; ++st) {
-        const int p = P.radix[st];
-        if (p == 4) fft_stage<C, 4>(a, b, n, L, tw, inv);
-        else if (p == 2) fft_stage<C, 2>(a, b, n, L, tw, inv);
-        else if (p == 3) fft_stage<C, 3>(a, b, n, L, tw, inv);
-        else fft_stage<C, 5>(a, b, n, L, tw, inv);
+        const int p = P.radix[st], rp = P.rp[st];
+        const unsigned m = P.mrp[st];
+        if (p == 4) fft_stage<C, 4>(a, b, n, L, rp, m, tw, inv);
+        else if (p == 2) fft_stage<C, 2>(a, b, n, L, rp, m, tw, inv);
+        else if (p == 3) fft_stage<C, 3>(a, b, n, L, rp, m, tw, inv);
+        else fft_stage<C, 5>(a, b, n, L, rp, m, tw, inv);
         __syncthreads();
         C2* t = a; a = b; b = t;
         L *= p;

@@ -144,7 +144,8 @@ __global__ void __launch_bounds__(128) zfft_kernel(Dims d, FieldsT<T> f, FFTPlan
                                                    const typename V2<T>::type* tw, int inv) {
     if (f.st->halt) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    zfft_tile(d, f, pl, tw, inv, blockIdx.x * kZC, blockIdx.y, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    zfft_tile(d, f, pl, tw, inv, blockIdx.x * ZCols<T>::value, blockIdx.y,
+              reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
 template <typename T>
@@ -195,13 +196,14 @@ __global__ void __launch_bounds__(128) theta_inv_kernel(Dims d, FieldsT<T> f, FF
 // --------------------------------------------------------------------------
 
 template <bool VEL, bool PRES, typename T>
-__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, double dxzq, FieldsT<T> f, int sub) {
+__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, CoefT<T> cv, double dxzq, T dxzq_t,
+                                                      FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= d.nt || j >= d.nz) return;
-    correct_cell<VEL, PRES, T>(d, c, dxzq, f, sub, i, j, k);
+    correct_cell<VEL, PRES, T>(d, c, cv, dxzq, dxzq_t, f, sub, i, j, k);
 }
 
 // CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
@@ -250,7 +252,7 @@ __device__ double block_reduce(double v, double* sh) {
 
 // CalcMaxCFL.F90:30-43 (which = 0) and CheckDivergence.F90:77-89 (which = 1).
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, double dxt, double dxz, FieldsT<T> f,
+__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, CoefT<T> cv, double dxt, double dxz, FieldsT<T> f,
                                                                int which, int only_on_output) {
     __shared__ double sh[32];
     if (only_on_output && (f.st->halt || !f.st->output)) return;
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, do
         const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
         double v;
         if (which == 0) {
-            v = cfl_cell(d, c, dxt, dxz, f, i, j, k);
+            v = cfl_cell(d, c, cv, dxt, dxz, f, i, j, k);
         } else {
             v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * dxz);
         }
@@ -575,13 +577,14 @@ void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Cons
 
 template <typename T>
 void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p, bool inv) {
-    size_t sm = (size_t)2 * kZC * p.z.n * sizeof(typename V2<T>::type);
+    constexpr int ZC = ZCols<T>::value;
+    size_t sm = (size_t)2 * ZC * p.z.n * sizeof(typename V2<T>::type);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    dim3 g((d.PH + kZC - 1) / kZC, d.nr);
+    dim3 g((d.PH + ZC - 1) / ZC, d.nr);
     zfft_kernel<T><<<g, 128, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
@@ -621,13 +624,14 @@ void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, co
 }
 
 template <typename T>
-void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f,
+void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k, const FieldsT<T>& f,
                     int sub, bool vel, bool pres) {
     dim3 blk;
     dim3 g = cell_grid(d, blk);
-    if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
-    else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
-    else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, c, k.dxzq, f, sub);
+    const T dxzq_t = (T)k.dxzq;
+    if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
+    else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
+    else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
     TC_LAUNCH_CHECK();
 }
 
@@ -646,15 +650,15 @@ void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, doubl
 }
 
 template <typename T>
-void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f) {
-    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.dxt, k.dxz, f, 0, 0);
+void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k, const FieldsT<T>& f) {
+    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, 0, 0);
     cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 0, 0);
     TC_LAUNCH_CHECK();
 }
 template <typename T>
-void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
+void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k,
                              const FieldsT<T>& f, bool only_on_output) {
-    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, k.dxt, k.dxz, f, 1, only_on_output ? 1 : 0);
+    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, 1, only_on_output ? 1 : 0);
     cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 1, only_on_output ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
@@ -699,12 +703,12 @@ void launch_to_host(cudaStream_t s, const Dims& d, const T* src, double* stage, 
     template void launch_zfft<T>(cudaStream_t, const Dims&, const FieldsT<T>&, const PlansT<T>&, bool);       \
     template void launch_pressure_tridiag<T>(cudaStream_t, const Dims&, const Coef&, const FieldsT<T>&);      \
     template void launch_theta_inverse<T>(cudaStream_t, const Dims&, const FieldsT<T>&, const PlansT<T>&);    \
-    template void launch_correct<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,                    \
+    template void launch_correct<T>(cudaStream_t, const Dims&, const Coef&, const CoefT<T>&, const Consts&,                    \
                                     const FieldsT<T>&, int, bool, bool);                                      \
     template void launch_divergence<T>(cudaStream_t, const Dims&, const CoefT<T>&, const Consts&,             \
                                        const FieldsT<T>&, int);                                               \
-    template void launch_cfl<T>(cudaStream_t, const Dims&, const Coef&, const Consts&, const FieldsT<T>&);    \
-    template void launch_check_divergence<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,           \
+    template void launch_cfl<T>(cudaStream_t, const Dims&, const Coef&, const CoefT<T>&, const Consts&, const FieldsT<T>&);    \
+    template void launch_check_divergence<T>(cudaStream_t, const Dims&, const Coef&, const CoefT<T>&, const Consts&,           \
                                              const FieldsT<T>&, bool);                                        \
     template void launch_velocity_stats<T>(cudaStream_t, const Dims&, const Coef&, const Consts&,             \
                                            const FieldsT<T>&, bool);                                          \

@@ -66,7 +66,7 @@ template <typename T>
 void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f);
 template <typename T> void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p);
 template <typename T>
-void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f,
+void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k, const FieldsT<T>& f,
                     int sub, bool vel, bool pres);
 template <typename T>
 void launch_divergence(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
@@ -77,9 +77,9 @@ void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, doubl
 
 // Reductions (FP64 arithmetic; results land in StepState).
 template <typename T>
-void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f);
+void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k, const FieldsT<T>& f);
 template <typename T>
-void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,
+void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k,
                              const FieldsT<T>& f, bool only_on_output);
 template <typename T>
 void launch_velocity_stats(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k,

@@ -98,3 +98,9 @@ def test_mixed_state_round_trip_is_fp32(gpu_lib):
     np.testing.assert_array_equal(back[0][..., :10], st[0][..., :10].astype(np.float32).astype(np.float64))
     np.testing.assert_array_equal(back[3], st[3])   # pressure stays FP64
     g.close()
+
+
+def test_integer_pipe_conversions_match_hardware(gpu_lib):
+    """The mixed path converts float <-> double on the integer pipes; every
+    result must equal the hardware conversion bit for bit."""
+    assert tc.selftest_conversions(1 << 24) == 0
