@@ -136,7 +136,9 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
 
 // ---- grouped substep phases ---------------------------------------------------
 
-// cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)
+// momentum: item = (chunk of kMomChunk radial levels, tile of TPB
+// consecutive (j, i) columns), each thread marching its column in r; for
+// FP64 (no marching) a chunk is one level and a thread one cell
 template <typename T>
 __global__ void __launch_bounds__(256) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;
@@ -145,12 +147,19 @@ __global__ void __launch_bounds__(256) ens_momentum_kernel(const InstT<T>* inst,
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int k = (int)(local / tiles);
-    const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
+    const int chunk = (int)(local / tiles);
+    const long long flat = (local - (long long)chunk * tiles) * blockDim.x + threadIdx.x;
     if (flat >= I.d.P) return;
     const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
-    momentum_cell<MODE_FUSED>(I.d, I.cv, I.ma[sub], i, j, k);
+    if (MomMarch<T>::value) {
+        const int k0 = chunk * kMomChunk, k1 = min(k0 + kMomChunk, I.d.nr);
+        momentum_column(I.d, I.cv, I.ma[sub], i, j, k0, k1);
+    } else {
+        momentum_cell<MODE_FUSED>(I.d, I.cv, I.ma[sub], i, j, chunk);
+    }
 }
+
+// cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)
 
 template <typename T>
 __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
@@ -167,16 +176,19 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
     correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, k);
 }
 
-// column-wise: item = TPB consecutive (z, theta) columns
+// column-wise: item = (component, TPB consecutive (z, theta) columns)
 template <typename T>
 __global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
-    const long long col = (item - prefix[m]) * blockDim.x + threadIdx.x;
+    const long long local = item - prefix[m];
+    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const int comp = (int)(local / tiles);
+    const long long col = (local - (long long)comp * tiles) * blockDim.x + threadIdx.x;
     if (col >= I.d.P) return;
-    radial_column(I.d, I.f, sub, col);
+    radial_column(I.d, I.f, sub, col, comp);
 }
 
 // mode-pair-wise: item = TPB consecutive (kz <= nzm/2, kt) mode pairs
@@ -311,15 +323,15 @@ int rebuild(tc_ensemble* e) {
         const Dims& d = h->d;
         maxNz = std::max(maxNz, d.nz);
         long long cnt[PH_COUNT];
-        cnt[PH_MOM] = (long long)d.nr * ceil_div(d.P, TPB);
-        cnt[PH_CORR] = cnt[PH_MOM];
-        cnt[PH_RAD] = ceil_div(d.P, TPB);
+        cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) * ceil_div(d.P, TPB);
+        cnt[PH_CORR] = (long long)d.nr * ceil_div(d.P, TPB);
+        cnt[PH_RAD] = 3LL * ceil_div(d.P, TPB);
         cnt[PH_PTRI] = ceil_div((long long)d.nzh * d.PH, TPB);
         cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
         cnt[PH_THINV] = cnt[PH_DIV];
         cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, ZCols<T>::value);
         cnt[PH_FACT] = 1;
-        cnt[PH_CFL] = I.vdt ? cnt[PH_MOM] : 0;
+        cnt[PH_CFL] = I.vdt ? cnt[PH_CORR] : 0;
         for (int p = 0; p < PH_COUNT; ++p) {
             long long v = (long long)prefix[(size_t)p * (n + 1) + a] + cnt[p];
             if (v > 2000000000LL) return efail(e, 2010, "ensemble work list exceeds 2^31 items");

@@ -19,7 +19,7 @@ namespace tcgb {
 namespace {
 
 constexpr int kRedThreads = 256;
-constexpr int kRedBlocks = 304;   // 2 x 152 SMs
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs: enough resident warps to cover load latency
 // Columns (kt) per z-FFT block (8 columns measured slower for FP32: twice
 // the shared memory per block halves the resident blocks).
 template <typename T> struct ZCols { static constexpr int value = 4; };
@@ -380,6 +380,182 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
     }
 }
 
+// The fused momentum work (explicit terms and implicit right-hand sides of
+// all three components, as momentum_cell with MODE_FUSED) for the cells
+// k0 <= k < k1 of column (i, j), marching outwards in r.  Values of planes
+// k-1 and k that the next level needs again stay in registers, and so do the
+// radial fluxes of the face between two levels: the lower-face flux of h12d,
+// h22 and h32 at level k is the upper-face flux of level k-1, the same
+// products of the same sums.  The arithmetic of every term is otherwise
+// momentum_cell's.
+constexpr int kMomChunk = 32;   // radial levels per thread
+
+// The fused momentum form each element type uses: the FP32 kernels are bound
+// by instruction issue and gain from the marching (fewer loads and address
+// computations); the FP64 kernels are bound by the FP64 pipe, and the
+// marching kernel's larger register footprint (128 vs 72) costs them more
+// occupancy than its few saved FP64 operations give back, so FP64 keeps one
+// thread per cell.
+template <typename T> struct MomMarch { static constexpr bool value = false; };
+template <> struct MomMarch<float> { static constexpr bool value = true; };
+
+template <typename T>
+__device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
+                                                int k0, int k1) {
+    const int nr = d.nr, nt = d.nt, nz = d.nz;
+    const int P = (int)d.P;
+    const int dim = i == 0 ? nt - 1 : -1, dip = i == nt - 1 ? 1 - nt : 1;
+    const int djm = j == 0 ? (nz - 1) * nt : -nt, djp = j == nz - 1 ? -(nz - 1) * nt : nt;
+    const size_t col = (size_t)j * nt + i;
+    const T one = (T)1.0, two = (T)2.0;
+    const T dt = step_dt<T>(a.st), ga = a.ga, ro = a.ro, alre = a.alre;
+    const T fic = a.icyl ? (T)a.icyl[col] : one, foc = one;
+    const T udxz = a.udxz, udxzq = a.udxzq;
+
+    // level k0 and its lower neighbours
+    size_t o = (size_t)k0 * P + col;
+    const int km0 = k0 > 0 ? k0 - 1 : 0;
+    const size_t om = (size_t)km0 * P + col;
+    T qt_c = ld(a.qt + o), qt_m = ld(a.qt + om), qt_mip = ld(a.qt + om + dip);
+    T qr_c = ld(a.qr + o), qr_im = ld(a.qr + o + dim), qr_jm = ld(a.qr + o + djm);
+    T qr_m = k0 > 0 ? ld(a.qr + om) : (T)0;
+    T qz_c = ld(a.qz + o), qz_m = ld(a.qz + om), qz_mjp = ld(a.qz + om + djp);
+    T pr_m = k0 > 0 ? ld(a.pr + om) : (T)0;
+    // fluxes through the lower face of level k0 (recomputed at a chunk start)
+    T U12, Uz, Gup;
+    {
+        const T rc2 = qr_c + qr_im;
+        U12 = rc2 * (qt_c + qt_m);                         // D12(k0): t_km = qt(kmm)
+        Uz = (qr_c + qr_jm) * (qz_c + qz_m);                // Dz(k0)
+        const T usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : (T)0;
+        Gup = (qr_c * usrc + qr_m * usrcm) * (qr_c + qr_m);   // Gdn(k0), used for k0 >= 1
+    }
+    for (int k = k0; k < k1; ++k, o += P) {
+        const bool top = k == nr - 1;
+        const int kp = k + 1;
+        // fresh loads of level k (neighbours) and k+1 (column)
+        const T qt_ip = ld(a.qt + o + dip), qt_im = ld(a.qt + o + dim);
+        const T qt_jp = ld(a.qt + o + djp), qt_jm = ld(a.qt + o + djm), qt_jmip = ld(a.qt + o + djm + dip);
+        const T qt_p = top ? qt_c : ld(a.qt + o + P);
+        const T qr_ip = ld(a.qr + o + dip), qr_jp = ld(a.qr + o + djp);
+        const T qr_p = ld(a.qr + o + P), qr_pim = ld(a.qr + o + P + dim), qr_pjm = ld(a.qr + o + P + djm);
+        const T qz_ip = ld(a.qz + o + dip), qz_im = ld(a.qz + o + dim);
+        const T qz_jp = ld(a.qz + o + djp), qz_jm = ld(a.qz + o + djm), qz_jpim = ld(a.qz + o + djp + dim);
+        const T qz_p = top ? qz_c : ld(a.qz + o + P);
+        const T p_c = ld(a.pr + o), p_im = ld(a.pr + o + dim), p_jm = ld(a.pr + o + djm);
+
+        const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
+        // ---- ExplicitTermsQT (momentum_cell / explicit_qt)
+        T ht;
+        {
+            const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+            const T h11 = ((qt_ip + qt_c) * (qt_ip + qt_c) - (qt_c + qt_im) * (qt_c + qt_im)) * udxt;
+            const T rp2 = qr_p + qr_pim, rc2 = qr_c + qr_im;
+            const T up = rp2 * (qt_p + qt_c);
+            const T h12d = (up - U12) * ld(c.q_udx2rm + k);
+            U12 = up;
+            const T h12n = qt_c * ld(c.q_usrm + k) * (rp2 * usrcp + rc2 * usrc);
+            const T h13 = ((qz_jp + qz_jpim) * (qt_jp + qt_c) - (qz_c + qz_im) * (qt_c + qt_jm)) * udxz;
+            const T d11qt = (qt_ip - two * qt_c + qt_im) * udxtq;
+            const T d22qt = (qt_jp - two * qt_c + qt_jm) * udxzq;
+            const T qre = qr_p * usrcp + qr_c * usrc;
+            const T qrw = qr_pim * usrcp + qr_im * usrc;
+            const T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
+            const T coriol = -(rc2 * usrc + rp2 * usrcp) * a.q_romeg;
+            ht = -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
+        }
+        // ---- ExplicitTermsQR at face k (1 <= k)
+        T hr = 0;
+        {
+            const T rup = (qr_p * usrcp + qr_c * usrc) * (qr_p + qr_c);
+            if (k >= 1) {
+                const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
+                const T qr_im_ = qr_im;
+                const T aa = (qt_ip + qt_mip + qt_c + qt_m) * (T)0.25;
+                const T h11n = aa * aa;
+                const T h21 = ((qt_ip + qt_mip) * (qr_ip + qr_c) - (qt_c + qt_m) * (qr_c + qr_im_)) * udxt;
+                const T h22 = (rup - Gup) * ld(c.q_udx2c + k);
+                const T h23 = ((qz_jp + qz_mjp) * (qr_jp + qr_c) - (qz_c + qz_m) * (qr_c + qr_jm)) * udxz;
+                const T d11qre = -((qt_ip + qt_mip) - (qt_c + qt_m)) * ld(c.udx1vis2 + k);
+                const T d11qr = (qr_ip - two * qr_c + qr_im_) * udxtq;
+                const T d22qr = (qr_jp - two * qr_c + qr_jm) * udxzq;
+                const T coriol = (qt_c + qt_ip + qt_m + qt_mip) * ld(c.q_rc_romeg + k);
+                hr = -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
+            }
+            Gup = rup;
+        }
+        // ---- ExplicitTermsQZ
+        T hz;
+        {
+            const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+            const T h31 = ((qt_ip + qt_jmip) * (qz_ip + qz_c) - (qt_c + qt_jm) * (qz_c + qz_im)) * udxt;
+            const T upz = (qr_p + qr_pjm) * (qz_p + qz_c);
+            const T h32 = (upz - Uz) * ld(c.q_udx2rm + k);
+            Uz = upz;
+            const T h33 = ((qz_jp + qz_c) * (qz_jp + qz_c) - (qz_c + qz_jm) * (qz_c + qz_jm)) * udxz;
+            const T dqz1 = (qz_im - two * qz_c + qz_ip) * udxtq;
+            const T dqz2 = (qz_jm - two * qz_c + qz_jp) * udxzq;
+            hz = -(h31 + h32 + h33) + dqz1 + dqz2;
+        }
+        // ---- ImplicitAndUpdateQT
+        {
+            T d33;
+            if (k == 0) {
+                const T app = ld(c.ap1j);
+                const T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
+                const T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
+                d33 = qt_p * app + qt_c * acc + (a.virotint + step_vinner<T>(a.st)) * amm;
+            } else if (top) {
+                const T amm = ld(c.am1j + k);
+                const T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
+                const T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
+                d33 = a.virotext * app + qt_c * acc + qt_m * amm;
+            } else {
+                d33 = qt_p * ld(c.ap1j + k) + qt_c * ld(c.ac1j + k) + qt_m * ld(c.am1j + k);
+            }
+            const T dpx11 = (p_c - p_im) * a.dxt_al * ld(c.usrm + k);
+            const T old = a.use_ru ? a.ru1[o] : (T)0;
+            a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
+            a.ru1[o] = ht;
+        }
+        // ---- ImplicitAndUpdateQR, faces 1..nr-1
+        if (k >= 1) {
+            const T d33 = qr_p * ld(c.ap2je + k) + qr_c * ld(c.ac2je + k) + qr_m * ld(c.am2je + k);
+            const T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
+            const T dpx22 = (p_c - pr_m) * udx2;
+            const T old = a.use_ru ? a.ru2[o] : (T)0;
+            a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
+            a.ru2[o] = hr;
+        }
+        // ---- ImplicitAndUpdateQZ
+        {
+            T d33;
+            if (k == 0) {
+                const T app = ld(c.ap3j);
+                const T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
+                const T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
+                d33 = qz_p * app + qz_c * acc + qz_c * amm;
+            } else if (top) {
+                const T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
+                const T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
+                d33 = qz_c * app + qz_c * acc + qz_m * ld(c.am3j + k);
+            } else {
+                d33 = qz_p * ld(c.ap3j + k) + qz_c * ld(c.ac3j + k) + qz_m * ld(c.am3j + k);
+            }
+            const T dpx33 = (p_c - p_jm) * a.dxz_al;
+            // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
+            const T old = top ? hz : (a.use_ru ? a.ru3[o] : (T)0);
+            a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
+            a.ru3[o] = hz;
+        }
+        // march: level k becomes the lower neighbour of level k+1
+        qt_m = qt_c; qt_mip = qt_ip; qt_c = qt_p;
+        qr_m = qr_c; qr_c = qr_p; qr_im = qr_pim; qr_jm = qr_pjm;
+        qz_m = qz_c; qz_mjp = qz_jp; qz_c = qz_p;
+        pr_m = p_c;
+    }
+}
+
 // One LU-factored tridiagonal along r for one column: forward elimination
 // into rhs (y_k0 = (rhs_k0 + extra) sc_k0, y_k = rhs_k sc_k - l_k y_k-1),
 // then back substitution adding the solution to q.  Planes are loaded in
@@ -429,20 +605,24 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
     }
 }
 
-// SolveImpEqnUpdate_QT.F90:65-78, _QR.F90:136-150 (faces 1..nr-1),
-// _QZ.F90:214-224 for the column `col`.
+// SolveImpEqnUpdate_QT.F90:65-78 (comp 0), _QR.F90:136-150 (comp 1, faces
+// 1..nr-1), _QZ.F90:214-224 (comp 2) for the column `col`.  The three
+// components are independent, so each gets its own thread.
 template <typename T>
-__device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f, int sub, long long col) {
+__device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f, int sub, long long col, int comp) {
     const int nr = d.nr;
     const size_t P = (size_t)d.P;
     const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
     const MomFactorsT<T>& F = f.F;
-    lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
-                    F.scale(sub, 0), *F.extra(sub));
-    lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0),
-                     F.scale(sub, 1), (T)0);
-    lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v),
-                     F.scale(sub, 2), (T)0);
+    if (comp == 0)
+        lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
+                        F.scale(sub, 0), *F.extra(sub));
+    else if (comp == 1)
+        lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0),
+                         F.scale(sub, 1), (T)0);
+    else
+        lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v),
+                         F.scale(sub, 2), (T)0);
 }
 
 __device__ __forceinline__ double2 ld2(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }

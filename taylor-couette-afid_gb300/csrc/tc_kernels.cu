@@ -111,8 +111,20 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
     momentum_cell<MODE>(d, c, a, i, j, k);
 }
 
+// The fused form: one thread per (theta, z) column and chunk of kMomChunk
+// radial levels, marching in r (momentum_column).
+template <typename T>
+__global__ void __launch_bounds__(128) momentum_march_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
+    if (a.st->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.nt || j >= d.nz) return;
+    const int k0 = blockIdx.z * kMomChunk, k1 = min(k0 + kMomChunk, d.nr);
+    momentum_column(d, c, a, i, j, k0, k1);
+}
+
 // --------------------------------------------------------------------------
-// Radial implicit solves, one thread per (z, theta) column
+// Radial implicit solves, one thread per (z, theta) column and component
 // --------------------------------------------------------------------------
 
 template <typename T>
@@ -120,7 +132,7 @@ __global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, FieldsT<T> f,
     if (f.st->halt) return;
     const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= d.P) return;
-    radial_column(d, f, sub, col);
+    radial_column(d, f, sub, col, blockIdx.y);
 }
 
 // --------------------------------------------------------------------------
@@ -538,7 +550,12 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
     MomArgs<T> a = make_mom_args(k, f, sub);
     dim3 blk;
     dim3 g = cell_grid(d, blk);
-    if (mode == MODE_FUSED) momentum_kernel<MODE_FUSED, T><<<g, blk, 0, s>>>(d, c, a);
+    if (mode == MODE_FUSED && MomMarch<T>::value) {
+        g.z = (d.nr + kMomChunk - 1) / kMomChunk;
+        momentum_march_kernel<T><<<g, blk, 0, s>>>(d, c, a);
+    } else if (mode == MODE_FUSED) {
+        momentum_kernel<MODE_FUSED, T><<<g, blk, 0, s>>>(d, c, a);
+    }
     else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
     else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
     TC_LAUNCH_CHECK();
@@ -546,7 +563,7 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
 
 template <typename T>
 void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub) {
-    radial_solve_kernel<T><<<(unsigned)((d.P + 127) / 128), 128, 0, s>>>(d, f, sub);
+    radial_solve_kernel<T><<<dim3((unsigned)((d.P + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
     TC_LAUNCH_CHECK();
 }
 
