@@ -104,6 +104,8 @@ int tc_create(const tc_bou* cfg, tc_handle** out);
  * which is FP64 only. */
 int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out);
 int tc_precision(const tc_handle* h);
+/* The configuration the handle was created with. */
+int tc_get_bou(const tc_handle* h, tc_bou* out);
 void tc_destroy(tc_handle* h);
 const char* tc_last_error(const tc_handle* h);   /* h may be NULL */
 
@@ -126,6 +128,35 @@ int tc_get_state(tc_handle* h, double* qt, double* qr, double* qz, double* pr);
 int tc_get_field(tc_handle* h, int which, double* out);
 /* Overwrite a 3-D array (enum tc_field) from the host, same shapes. */
 int tc_set_field(tc_handle* h, int which, const double* in);
+
+/* ---- restart files (HDF5, without libhdf5) --------------------------------
+ * The reference's continuation files in the layout its HDF5 routines use
+ * (HdfRoutines.F90:388-477): continua_qt.h5, continua_qr.h5, continua_qz.h5
+ * with one float64 dataset "var" of dataspace [nthm][nzm][nr] (Fortran
+ * q(1:nr, 1:nzm, 1:nthm), r fastest), and continua_master.h5 with the
+ * scalars nr, nth, nz, istr (int32) and time, rint, rext, str, alx3, lamb
+ * (float64).  Files are written in the HDF5 1.8 format subset that library
+ * writes by default (superblock 0, symbol-table groups, contiguous storage)
+ * and read back from it; chunked, compressed and new-style-group files are
+ * rejected with 2022.  dir may be NULL (current directory). */
+
+/* WriteFlowField.F90:17-47: the state of h at simulated time `time`. */
+int tc_h5_write_continua(tc_handle* h, const char* dir, double time);
+/* ReadFlowField.F90:31-149 for an unchanged grid: load the files into h
+ * (tc_set_state; pr = 0) and return their time.  Files of another grid fail
+ * with 2024 (the reference would interpolate, interp.F90). */
+int tc_h5_read_continua(tc_handle* h, const char* dir, double* time);
+/* WriteGridInfo.F90:22-33: cordin_info.h5 with rm(1:nrm), rc(1:nr),
+ * tm(1:nthm), zm(1:nzm) (host only). */
+int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir);
+/* One float64 dataset `name` of the given shape (C order) in a new file. */
+int tc_h5_write_dataset(const char* path, const char* name, int rank,
+                        const long long* dims, const double* data);
+/* Dataset `name` of an HDF5 file as doubles (float64/32 and int32/64 are
+ * converted): *rank and dims[0..rank-1] receive the shape (up to 8 axes);
+ * out (may be NULL to query the shape) receives up to cap values. */
+int tc_h5_read_dataset(const char* path, const char* name, double* out, long long cap,
+                       int* rank, long long* dims);
 
 /* ---- the time step ------------------------------------------------------ */
 

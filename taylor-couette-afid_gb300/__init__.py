@@ -120,6 +120,14 @@ SIGNATURES = {
     "tc_profile_name": (ctypes.c_char_p, [ctypes.c_int]),
     "tc_measure_fp64_peak": (ctypes.c_int, [_vp, _dp]),
     "tc_selftest_conversions": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
+    "tc_get_bou": (ctypes.c_int, [_vp, ctypes.POINTER(Bou)]),
+    "tc_h5_write_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
+    "tc_h5_read_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, _dp]),
+    "tc_h5_write_grid_info": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_char_p]),
+    "tc_h5_write_dataset": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_longlong), _dp]),
+    "tc_h5_read_dataset": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _dp, ctypes.c_longlong, _ip,
+                                          ctypes.POINTER(ctypes.c_longlong)]),
     "tc_ensemble_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
     "tc_ensemble_destroy": (None, [_vp]),
     "tc_ensemble_last_error": (ctypes.c_char_p, [_vp]),
@@ -208,6 +216,39 @@ def selftest_conversions(n: int = 1 << 24) -> int:
     return v.value
 
 
+def h5_write(path: str, name: str, data: np.ndarray):
+    """One float64 dataset in a new HDF5 file (C order shape of `data`)."""
+    a = np.ascontiguousarray(data, dtype=np.float64)
+    dims = (ctypes.c_longlong * a.ndim)(*a.shape)
+    rc = lib().tc_h5_write_dataset(path.encode(), name.encode(), a.ndim, dims, _dptr(a))
+    if rc != 0:
+        raise TCError(rc, lib().tc_last_error(None).decode())
+
+
+def h5_read(path: str, name: str) -> np.ndarray:
+    """Dataset `name` of an HDF5 file as a float64 array of its shape."""
+    L = lib()
+    rank = ctypes.c_int()
+    dims = (ctypes.c_longlong * 8)()
+    rc = L.tc_h5_read_dataset(path.encode(), name.encode(), None, 0, ctypes.byref(rank), dims)
+    if rc != 0:
+        raise TCError(rc, L.tc_last_error(None).decode())
+    shape = tuple(dims[i] for i in range(rank.value))
+    out = np.empty(shape)
+    rc = L.tc_h5_read_dataset(path.encode(), name.encode(), _dptr(out), out.size, ctypes.byref(rank), dims)
+    if rc != 0:
+        raise TCError(rc, L.tc_last_error(None).decode())
+    return out
+
+
+def h5_write_grid_info(bou: dict, directory: str = "."):
+    """WriteGridInfo: cordin_info.h5 with rm, rc, tm, zm."""
+    b = Bou.from_dict(bou)
+    rc = lib().tc_h5_write_grid_info(ctypes.byref(b), directory.encode())
+    if rc != 0:
+        raise TCError(rc, lib().tc_last_error(None).decode())
+
+
 PREC_FP64, PREC_MIXED = 0, 1
 
 
@@ -277,6 +318,16 @@ class TaylorCouette:
         out = [np.empty(self.halo_shape) for _ in range(4)]
         self._ck(self.L.tc_get_state(self.h, *[_dptr(a) for a in out]))
         return tuple(out)
+
+    def write_continua(self, directory: str = ".", time: float = 0.0):
+        """WriteFlowField: continua_q{t,r,z}.h5 and continua_master.h5."""
+        self._ck(self.L.tc_h5_write_continua(self.h, directory.encode(), float(time)))
+
+    def read_continua(self, directory: str = ".") -> float:
+        """ReadFlowField (same grid): load the continuation files, return their time."""
+        t = ctypes.c_double()
+        self._ck(self.L.tc_h5_read_continua(self.h, directory.encode(), ctypes.byref(t)))
+        return t.value
 
     def get_field(self, name: str) -> np.ndarray:
         w = FIELDS.index(name)

@@ -341,6 +341,12 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
 
 int tc_create(const tc_bou* cfg, tc_handle** out) { return tc_create_ex(cfg, TC_PREC_FP64, out); }
 
+int tc_get_bou(const tc_handle* h, tc_bou* out) {
+    if (!h || !out) return 2000;
+    *out = h->bou;
+    return 0;
+}
+
 int tc_precision(const tc_handle* h) { return h ? (h->mixed ? TC_PREC_MIXED : TC_PREC_FP64) : -1; }
 
 void tc_destroy(tc_handle* h) {

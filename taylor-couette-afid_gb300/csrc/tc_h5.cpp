@@ -1,0 +1,621 @@
+// tc_h5.cpp -- the HDF5 files of the reference's restart path, without
+// libhdf5: continua_q{t,r,z}.h5 (dataset "var", the interior of one velocity
+// field), continua_master.h5 (grid and time scalars) and cordin_info.h5
+// (coordinates), as WriteFlowField.F90:17-47, ReadFlowField.F90:31-149 and
+// WriteGridInfo.F90:22-33 read and write them through HdfRoutines.F90.
+//
+// The subset of the HDF5 file format written and read here is the one the
+// HDF5 1.8 library produces with its default properties:
+//   superblock version 0 (or 1 on reading), 8-byte offsets and lengths;
+//   groups as symbol tables: a version-1 B-tree of group nodes over symbol
+//   table nodes, names in a local heap;
+//   version-1 object headers (with continuation blocks on reading);
+//   datasets with a simple dataspace (message versions 1 and 2), a fixed-
+//   point or IEEE floating-point little-endian datatype, and contiguous (or,
+//   on reading, compact) storage.
+// Writing uses one symbol table node for all the names of a file (its group
+// leaf K is raised to fit them), contiguous storage and no fill value.
+//
+// Layout of the reference's arrays: Fortran q(1:nr, 1:nzm, 1:nthm) is the
+// HDF5 dataspace [nthm][nzm][nr] (the Fortran API lists dimensions in
+// reverse), r fastest.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tc_capi.h"
+
+namespace tcgb {
+void set_last_error(const std::string& msg);
+}
+
+namespace {
+
+constexpr uint64_t kUndef = ~0ull;
+
+// ---------------------------------------------------------------------------
+// writing
+
+struct WDataset {
+    std::string name;
+    bool is_int;                 // int32 (H5T_NATIVE_INTEGER) or float64
+    std::vector<uint64_t> dims;
+    std::vector<uint8_t> bytes;  // little-endian element data
+};
+
+struct Buf {
+    std::vector<uint8_t> b;
+    void u8(uint8_t v) { b.push_back(v); }
+    void u16(uint16_t v) { for (int i = 0; i < 2; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void u32(uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void u64(uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+    void zeros(size_t n) { b.insert(b.end(), n, 0); }
+    void pad8() { while (b.size() % 8) b.push_back(0); }
+    size_t size() const { return b.size(); }
+};
+
+// One object-header message: type, payload padded to 8 bytes.
+void message(Buf& o, uint16_t type, uint8_t flags, const Buf& payload) {
+    Buf p = payload;
+    p.pad8();
+    o.u16(type);
+    o.u16((uint16_t)p.size());
+    o.u8(flags);
+    o.zeros(3);
+    o.b.insert(o.b.end(), p.b.begin(), p.b.end());
+}
+
+// Version-1 object header holding `msgs` (already encoded messages).
+void object_header(Buf& out, const Buf& msgs, int nmsgs) {
+    out.u8(1);                       // version
+    out.u8(0);
+    out.u16((uint16_t)nmsgs);
+    out.u32(1);                      // reference count
+    out.u32((uint32_t)msgs.size());  // header data size
+    out.zeros(4);                    // align the messages to 8 bytes
+    out.b.insert(out.b.end(), msgs.b.begin(), msgs.b.end());
+}
+
+Buf dataset_messages(const WDataset& d, uint64_t data_addr, int* nmsgs) {
+    Buf m;
+    {   // dataspace, version 1
+        Buf p;
+        p.u8(1);
+        p.u8((uint8_t)d.dims.size());
+        p.u8(0);                     // no maximum dimensions
+        p.zeros(5);
+        for (uint64_t x : d.dims) p.u64(x);
+        message(m, 0x0001, 0, p);
+    }
+    {   // datatype, version 1
+        Buf p;
+        if (d.is_int) {
+            p.u8(0x10);              // class 0: fixed point
+            p.u8(0x08); p.u8(0); p.u8(0);   // little endian, signed
+            p.u32(4);
+            p.u16(0); p.u16(32);     // bit offset, precision
+        } else {
+            p.u8(0x11);              // class 1: floating point
+            p.u8(0x20); p.u8(63); p.u8(0);  // little endian, implied msb, sign bit 63
+            p.u32(8);
+            p.u16(0); p.u16(64);     // bit offset, precision
+            p.u8(52); p.u8(11);      // exponent location, size
+            p.u8(0); p.u8(52);       // mantissa location, size
+            p.u32(1023);             // exponent bias
+        }
+        message(m, 0x0003, 1, p);
+    }
+    {   // fill value, version 2: allocation late, written if set, undefined
+        Buf p;
+        p.u8(2); p.u8(2); p.u8(2); p.u8(0);
+        message(m, 0x0005, 1, p);
+    }
+    {   // data layout, version 3, contiguous
+        Buf p;
+        p.u8(3);
+        p.u8(1);
+        p.u64(data_addr);
+        p.u64((uint64_t)d.bytes.size());
+        message(m, 0x0008, 0, p);
+    }
+    *nmsgs = 4;
+    return m;
+}
+
+bool write_file(const std::string& path, std::vector<WDataset> ds, std::string& err) {
+    std::sort(ds.begin(), ds.end(), [](const WDataset& a, const WDataset& b) { return a.name < b.name; });
+    const int n = (int)ds.size();
+    const int leafK = std::max(4, (n + 1) / 2);      // a symbol table node holds 2K entries
+    const int nodeK = 16;                            // group B-tree node: 2K children
+    // local heap data: "" at 0, then the names, each padded to 8 bytes
+    Buf heap;
+    heap.zeros(8);
+    std::vector<uint64_t> name_off(n);
+    for (int i = 0; i < n; ++i) {
+        name_off[i] = heap.size();
+        heap.b.insert(heap.b.end(), ds[i].name.begin(), ds[i].name.end());
+        heap.u8(0);
+        heap.pad8();
+    }
+    // addresses
+    const uint64_t a_root = 96;                      // after the 96-byte superblock
+    const uint64_t root_size = 16 + 8 + 16;
+    const uint64_t a_heap = a_root + root_size;
+    const uint64_t a_heapdata = a_heap + 32;
+    const uint64_t a_btree = a_heapdata + heap.size();
+    const uint64_t btree_size = 24 + (2 * nodeK + 1) * 8 + 2 * nodeK * 8;
+    const uint64_t a_snod = a_btree + btree_size;
+    const uint64_t snod_size = 8 + 2 * (uint64_t)leafK * 40;
+    uint64_t a = a_snod + snod_size;
+    std::vector<uint64_t> a_oh(n), a_data(n);
+    std::vector<Buf> ohs(n);
+    for (int i = 0; i < n; ++i) {   // header sizes do not depend on the data address
+        int nm = 0;
+        Buf msgs = dataset_messages(ds[i], 0, &nm);
+        a_oh[i] = a;
+        a += 16 + msgs.size();
+    }
+    for (int i = 0; i < n; ++i) {
+        a_data[i] = a;
+        a += ds[i].bytes.size();
+        a = (a + 7) & ~7ull;
+    }
+    const uint64_t eof = a;
+    for (int i = 0; i < n; ++i) {
+        int nm = 0;
+        Buf msgs = dataset_messages(ds[i], a_data[i], &nm);
+        object_header(ohs[i], msgs, nm);
+    }
+
+    Buf f;
+    // superblock version 0
+    const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+    f.b.insert(f.b.end(), sig, sig + 8);
+    f.u8(0); f.u8(0); f.u8(0); f.u8(0);   // superblock, free space, root entry versions; reserved
+    f.u8(0); f.u8(8); f.u8(8); f.u8(0);   // shared header version, offset size, length size, reserved
+    f.u16((uint16_t)leafK);
+    f.u16((uint16_t)nodeK);
+    f.u32(0);                            // consistency flags
+    f.u64(0);                            // base address
+    f.u64(kUndef);                       // free-space info
+    f.u64(eof);
+    f.u64(kUndef);                       // driver information block
+    // root group symbol table entry, scratch pad caching the group's tables
+    f.u64(0);
+    f.u64(a_root);
+    f.u32(1);
+    f.u32(0);
+    f.u64(a_btree);
+    f.u64(a_heap);
+    // root group object header: one symbol table message
+    {
+        Buf p;
+        p.u64(a_btree);
+        p.u64(a_heap);
+        Buf msgs;
+        message(msgs, 0x0011, 0, p);
+        object_header(f, msgs, 1);
+    }
+    // local heap
+    f.b.insert(f.b.end(), {'H', 'E', 'A', 'P'});
+    f.u8(0); f.zeros(3);
+    f.u64(heap.size());
+    f.u64(kUndef);                       // no free block
+    f.u64(a_heapdata);
+    f.b.insert(f.b.end(), heap.b.begin(), heap.b.end());
+    // group B-tree: one leaf node with one child, the symbol table node
+    f.b.insert(f.b.end(), {'T', 'R', 'E', 'E'});
+    f.u8(0);                             // group node
+    f.u8(0);                             // level 0
+    f.u16(n > 0 ? 1 : 0);
+    f.u64(kUndef);
+    f.u64(kUndef);
+    f.u64(0);                            // key 0: the empty name
+    f.u64(a_snod);                       // child 0
+    f.u64(n > 0 ? name_off[n - 1] : 0);  // key 1: the last name in child 0
+    f.zeros((size_t)(btree_size - 24 - 3 * 8));
+    // symbol table node
+    f.b.insert(f.b.end(), {'S', 'N', 'O', 'D'});
+    f.u8(1); f.u8(0);
+    f.u16((uint16_t)n);
+    for (int i = 0; i < n; ++i) {
+        f.u64(name_off[i]);
+        f.u64(a_oh[i]);
+        f.u32(0); f.u32(0);
+        f.zeros(16);
+    }
+    f.zeros((size_t)(2 * leafK - n) * 40);
+    for (int i = 0; i < n; ++i) {
+        if (f.size() != a_oh[i]) { err = "internal layout error"; return false; }
+        f.b.insert(f.b.end(), ohs[i].b.begin(), ohs[i].b.end());
+    }
+    for (int i = 0; i < n; ++i) {
+        while (f.size() < a_data[i]) f.u8(0);
+        f.b.insert(f.b.end(), ds[i].bytes.begin(), ds[i].bytes.end());
+    }
+    while (f.size() < eof) f.u8(0);
+    FILE* fp = std::fopen(path.c_str(), "wb");
+    if (!fp) { err = "cannot create " + path; return false; }
+    const size_t w = std::fwrite(f.b.data(), 1, f.size(), fp);
+    const bool ok = std::fclose(fp) == 0 && w == f.size();
+    if (!ok) err = "write failed: " + path;
+    return ok;
+}
+
+WDataset f64_dataset(const std::string& name, std::vector<uint64_t> dims, const double* v) {
+    WDataset d{name, false, dims, {}};
+    uint64_t n = 1;
+    for (uint64_t x : dims) n *= x;
+    d.bytes.resize(n * 8);
+    for (uint64_t i = 0; i < n; ++i) {
+        uint64_t u;
+        std::memcpy(&u, v + i, 8);
+        for (int b = 0; b < 8; ++b) d.bytes[i * 8 + b] = (uint8_t)(u >> (8 * b));
+    }
+    return d;
+}
+
+WDataset i32_dataset(const std::string& name, int32_t v) {
+    WDataset d{name, true, {1}, {}};
+    const uint32_t u = (uint32_t)v;
+    for (int b = 0; b < 4; ++b) d.bytes.push_back((uint8_t)(u >> (8 * b)));
+    return d;
+}
+
+// ---------------------------------------------------------------------------
+// reading
+
+struct Reader {
+    std::vector<uint8_t> f;
+    std::string err;
+    int leafK = 4, nodeK = 16;
+
+    bool load(const std::string& path) {
+        FILE* fp = std::fopen(path.c_str(), "rb");
+        if (!fp) { err = "cannot open " + path; return false; }
+        std::fseek(fp, 0, SEEK_END);
+        long sz = std::ftell(fp);
+        std::fseek(fp, 0, SEEK_SET);
+        if (sz < 0) { std::fclose(fp); err = "cannot size " + path; return false; }
+        f.resize((size_t)sz);
+        size_t r = sz > 0 ? std::fread(f.data(), 1, (size_t)sz, fp) : 0;
+        std::fclose(fp);
+        if (r != (size_t)sz) { err = "short read: " + path; return false; }
+        return true;
+    }
+    bool have(uint64_t at, uint64_t n) {
+        if (at > f.size() || n > f.size() - at) { err = "truncated or corrupt file"; return false; }
+        return true;
+    }
+    uint64_t le(uint64_t at, int n) const {
+        uint64_t v = 0;
+        for (int i = 0; i < n; ++i) v |= (uint64_t)f[at + i] << (8 * i);
+        return v;
+    }
+
+    // superblock -> root group (B-tree, heap) addresses
+    bool root(uint64_t* btree, uint64_t* heap) {
+        static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+        if (!have(0, 8) || std::memcmp(f.data(), sig, 8) != 0) { err = "not an HDF5 file (no signature at 0)"; return false; }
+        if (!have(8, 16)) return false;
+        const int ver = f[8];
+        if (ver > 1) { err = "superblock version " + std::to_string(ver) + " is not supported"; return false; }
+        if (f[13] != 8 || f[14] != 8) { err = "only 8-byte offsets and lengths are supported"; return false; }
+        leafK = (int)le(16, 2);
+        nodeK = (int)le(18, 2);
+        uint64_t p = 24;
+        if (ver == 1) p += 4;
+        p += 32;                        // base, free space, eof, driver
+        if (!have(p, 40)) return false;
+        const uint64_t oh = le(p + 8, 8);
+        return group_tables(oh, btree, heap);
+    }
+
+    // Walk the messages of a version-1 object header (with continuations).
+    template <typename F>
+    bool messages(uint64_t oh, F fn) {
+        if (!have(oh, 16)) return false;
+        if (f[oh] != 1) {
+            err = (f[oh] == 'O') ? "version-2 object headers are not supported" : "bad object header";
+            return false;
+        }
+        const int nmsg = (int)le(oh + 2, 2);
+        std::vector<std::pair<uint64_t, uint64_t>> blocks{{oh + 16, le(oh + 8, 4)}};
+        int seen = 0;
+        for (size_t bi = 0; bi < blocks.size() && seen < nmsg; ++bi) {
+            uint64_t p = blocks[bi].first, end = p + blocks[bi].second;
+            if (!have(p, blocks[bi].second)) return false;
+            while (p + 8 <= end && seen < nmsg) {
+                const int type = (int)le(p, 2), size = (int)le(p + 2, 2);
+                const uint64_t data = p + 8;
+                if (!have(data, (uint64_t)size)) return false;
+                ++seen;
+                if (type == 0x0010) {
+                    blocks.push_back({le(data, 8), le(data + 8, 8)});
+                } else if (!fn(type, data, size)) {
+                    return false;
+                }
+                p = data + size;
+            }
+        }
+        return true;
+    }
+
+    bool group_tables(uint64_t oh, uint64_t* btree, uint64_t* heap) {
+        bool found = false;
+        if (!messages(oh, [&](int type, uint64_t d, int) {
+                if (type == 0x0011) {
+                    *btree = le(d, 8);
+                    *heap = le(d + 8, 8);
+                    found = true;
+                }
+                return true;
+            }))
+            return false;
+        if (!found) { err = "the root group has no symbol table (new-style groups are not supported)"; return false; }
+        return true;
+    }
+
+    // name -> object header address through the group B-tree
+    bool lookup(uint64_t btree, uint64_t heap, const std::string& name, uint64_t* oh) {
+        if (!have(heap, 32) || std::memcmp(&f[heap], "HEAP", 4) != 0) { err = "bad local heap"; return false; }
+        const uint64_t hdata = le(heap + 24, 8), hsize = le(heap + 8, 8);
+        if (!have(hdata, hsize)) return false;
+        return search(btree, hdata, hsize, name, oh, 0);
+    }
+
+    bool search(uint64_t node, uint64_t hdata, uint64_t hsize, const std::string& name, uint64_t* oh, int depth) {
+        if (depth > 32) { err = "B-tree too deep"; return false; }
+        if (!have(node, 24)) return false;
+        if (std::memcmp(&f[node], "TREE", 4) == 0) {
+            if (f[node + 4] != 0) { err = "not a group B-tree"; return false; }
+            const int n = (int)le(node + 6, 2);
+            if (!have(node + 24, (uint64_t)(2 * n + 1) * 8)) return false;
+            for (int c = 0; c < n; ++c) {
+                const uint64_t child = le(node + 24 + 8 + 16 * (uint64_t)c, 8);
+                if (search(child, hdata, hsize, name, oh, depth + 1)) return true;
+                if (!err.empty()) return false;
+            }
+            return false;
+        }
+        if (std::memcmp(&f[node], "SNOD", 4) == 0) {
+            const int n = (int)le(node + 6, 2);
+            if (!have(node + 8, (uint64_t)n * 40)) return false;
+            for (int e = 0; e < n; ++e) {
+                const uint64_t ent = node + 8 + 40 * (uint64_t)e;
+                const uint64_t off = le(ent, 8);
+                if (off >= hsize) { err = "bad name offset"; return false; }
+                const char* s = (const char*)&f[hdata + off];
+                const size_t len = strnlen(s, (size_t)(hsize - off));
+                if (name == std::string(s, len)) {
+                    *oh = le(ent + 8, 8);
+                    return true;
+                }
+            }
+            return false;
+        }
+        err = "bad B-tree node";
+        return false;
+    }
+
+    // a dataset as doubles
+    bool dataset(uint64_t oh, std::vector<double>& out, std::vector<uint64_t>& dims) {
+        int cls = -1, size = 0, order = 0;
+        bool sgn = true;
+        bool have_space = false, have_layout = false;
+        uint64_t addr = kUndef, bytes = 0, compact = 0;
+        bool is_compact = false;
+        if (!messages(oh, [&](int type, uint64_t d, int) {
+                if (type == 0x0001) {
+                    const int ver = f[d], rank = f[d + 1];
+                    const uint64_t p = d + (ver == 1 ? 8 : 4);
+                    dims.clear();
+                    for (int r = 0; r < rank; ++r) dims.push_back(le(p + 8 * (uint64_t)r, 8));
+                    have_space = true;
+                } else if (type == 0x0003) {
+                    cls = f[d] & 0x0f;
+                    order = f[d + 1] & 1;
+                    sgn = (f[d + 1] & 0x08) != 0;
+                    size = (int)le(d + 4, 4);
+                } else if (type == 0x0008) {
+                    const int ver = f[d];
+                    if (ver != 3) { err = "data layout message version " + std::to_string(ver) + " is not supported"; return false; }
+                    const int lc = f[d + 1];
+                    if (lc == 1) {
+                        addr = le(d + 2, 8);
+                        bytes = le(d + 10, 8);
+                    } else if (lc == 0) {
+                        bytes = le(d + 2, 2);
+                        compact = d + 4;
+                        is_compact = true;
+                    } else {
+                        err = "chunked storage is not supported";
+                        return false;
+                    }
+                    have_layout = true;
+                } else if (type == 0x000B) {
+                    err = "filtered (compressed) datasets are not supported";
+                    return false;
+                }
+                return true;
+            }))
+            return false;
+        if (!have_space || !have_layout || cls < 0) { err = "incomplete dataset header"; return false; }
+        if (order != 0) { err = "big-endian data is not supported"; return false; }
+        uint64_t n = 1;
+        for (uint64_t x : dims) n *= x;
+        if (!((cls == 1 && (size == 8 || size == 4)) || (cls == 0 && (size == 4 || size == 8)))) {
+            err = "unsupported datatype (class " + std::to_string(cls) + ", size " + std::to_string(size) + ")";
+            return false;
+        }
+        if (bytes < n * (uint64_t)size) { err = "dataset storage smaller than its dataspace"; return false; }
+        const uint64_t src = is_compact ? compact : addr;
+        if (!is_compact && addr == kUndef) { err = "dataset has no storage allocated"; return false; }
+        if (!have(src, n * (uint64_t)size)) return false;
+        out.resize(n);
+        for (uint64_t i = 0; i < n; ++i) {
+            const uint64_t u = le(src + i * size, size);
+            if (cls == 1 && size == 8) { double v; std::memcpy(&v, &u, 8); out[i] = v; }
+            else if (cls == 1) { uint32_t w = (uint32_t)u; float v; std::memcpy(&v, &w, 4); out[i] = v; }
+            else if (size == 4) out[i] = sgn ? (double)(int32_t)(uint32_t)u : (double)(uint32_t)u;
+            else out[i] = sgn ? (double)(int64_t)u : (double)u;
+        }
+        return true;
+    }
+};
+
+bool read_named(const std::string& path, const std::string& name, std::vector<double>& out,
+                std::vector<uint64_t>& dims, std::string& err) {
+    Reader r;
+    uint64_t bt = 0, hp = 0, oh = 0;
+    if (!r.load(path) || !r.root(&bt, &hp)) { err = r.err; return false; }
+    if (!r.lookup(bt, hp, name, &oh)) {
+        err = r.err.empty() ? "no dataset '" + name + "' in " + path : r.err;
+        return false;
+    }
+    if (!r.dataset(oh, out, dims)) { err = r.err; return false; }
+    return true;
+}
+
+int fail(int code, const std::string& msg) {
+    tcgb::set_last_error(msg);
+    return code;
+}
+
+std::string join(const char* dir, const char* file) {
+    std::string d = dir ? dir : ".";
+    if (d.empty()) d = ".";
+    if (d.back() != '/') d += '/';
+    return d + file;
+}
+
+}  // namespace
+
+// ---- exported (declared extern "C" in tc_capi.h) ---------------------------
+
+int tc_h5_write_dataset(const char* path, const char* name, int rank, const long long* dims, const double* data) {
+    if (!path || !name || !dims || !data || rank < 1 || rank > 8) return fail(2000, "tc_h5_write_dataset: bad argument");
+    std::vector<uint64_t> d;
+    for (int r = 0; r < rank; ++r) {
+        if (dims[r] < 1) return fail(2000, "tc_h5_write_dataset: dimensions must be positive");
+        d.push_back((uint64_t)dims[r]);
+    }
+    std::string err;
+    if (!write_file(path, {f64_dataset(name, d, data)}, err)) return fail(2021, err);
+    return 0;
+}
+
+int tc_h5_read_dataset(const char* path, const char* name, double* out, long long cap, int* rank, long long* dims) {
+    if (!path || !name) return fail(2000, "tc_h5_read_dataset: bad argument");
+    std::vector<double> v;
+    std::vector<uint64_t> d;
+    std::string err;
+    if (!read_named(path, name, v, d, err)) return fail(2022, err);
+    if (rank) *rank = (int)d.size();
+    if (dims) for (size_t r = 0; r < d.size() && r < 8; ++r) dims[r] = (long long)d[r];
+    if (out) {
+        if ((long long)v.size() > cap) return fail(2023, "tc_h5_read_dataset: output buffer too small");
+        std::memcpy(out, v.data(), v.size() * sizeof(double));
+    }
+    return 0;
+}
+
+int tc_h5_write_continua(tc_handle* h, const char* dir, double time) {
+    tc_bou b;
+    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_write_continua: null handle");
+    const tc_bou* cfg = &b;
+    const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
+    const size_t halo = (size_t)(nthm + 2) * (nzm + 2) * nr;
+    std::vector<double> q[3];
+    for (auto& a : q) a.resize(halo);
+    if (int r = tc_get_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr)) return r;
+    // interior q(1:nr, 1:nzm, 1:nthm) of q(1:nr, 0:nzm+1, 0:nthm+1)
+    const char* files[3] = {"continua_qt.h5", "continua_qr.h5", "continua_qz.h5"};
+    std::vector<double> in((size_t)nthm * nzm * nr);
+    for (int c = 0; c < 3; ++c) {
+        for (int i = 0; i < nthm; ++i)
+            for (int j = 0; j < nzm; ++j)
+                std::memcpy(&in[((size_t)i * nzm + j) * nr], &q[c][((size_t)(i + 1) * (nzm + 2) + (j + 1)) * nr],
+                            sizeof(double) * nr);
+        std::string err;
+        if (!write_file(join(dir, files[c]), {f64_dataset("var", {(uint64_t)nthm, (uint64_t)nzm, (uint64_t)nr}, in.data())}, err))
+            return fail(2021, err);
+    }
+    std::vector<WDataset> m;
+    m.push_back(i32_dataset("nr", nr));
+    m.push_back(i32_dataset("nth", nthm + 1));
+    m.push_back(i32_dataset("nz", nzm + 1));
+    m.push_back(f64_dataset("time", {1}, &time));
+    m.push_back(f64_dataset("rint", {1}, &cfg->rint));
+    m.push_back(f64_dataset("rext", {1}, &cfg->rext));
+    m.push_back(i32_dataset("istr", cfg->istr));
+    m.push_back(f64_dataset("str", {1}, &cfg->str));
+    m.push_back(f64_dataset("alx3", {1}, &cfg->alx3));
+    m.push_back(f64_dataset("lamb", {1}, &cfg->lamb));
+    std::string err;
+    if (!write_file(join(dir, "continua_master.h5"), m, err)) return fail(2021, err);
+    return 0;
+}
+
+int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
+    tc_bou b;
+    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_read_continua: null handle");
+    const tc_bou* cfg = &b;
+    const std::string master = join(dir, "continua_master.h5");
+    std::vector<double> v;
+    std::vector<uint64_t> d;
+    std::string err;
+    double s[6];
+    const char* names[6] = {"nth", "nr", "nz", "time", "istr", "str"};
+    for (int i = 0; i < 6; ++i) {
+        if (!read_named(master, names[i], v, d, err)) return fail(2022, err);
+        if (v.size() != 1) return fail(2022, std::string("master scalar '") + names[i] + "' is not a scalar");
+        s[i] = v[0];
+    }
+    const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
+    if ((int)s[0] != nthm + 1 || (int)s[1] != nr || (int)s[2] != nzm + 1 || (int)s[4] != cfg->istr || s[5] != cfg->str)
+        return fail(2024, "the continuation files hold another grid (nth " + std::to_string((int)s[0]) + ", nr " +
+                              std::to_string((int)s[1]) + ", nz " + std::to_string((int)s[2]) +
+                              "): restart interpolation (interp.F90) is not supported");
+    const size_t halo = (size_t)(nthm + 2) * (nzm + 2) * nr;
+    std::vector<double> q[3];
+    const char* files[3] = {"continua_qt.h5", "continua_qr.h5", "continua_qz.h5"};
+    for (int c = 0; c < 3; ++c) {
+        if (!read_named(join(dir, files[c]), "var", v, d, err)) return fail(2022, err);
+        if (d.size() != 3 || d[0] != (uint64_t)nthm || d[1] != (uint64_t)nzm || d[2] != (uint64_t)nr)
+            return fail(2024, std::string(files[c]) + ": dataset 'var' has the wrong shape");
+        q[c].assign(halo, 0.0);
+        for (int i = 0; i < nthm; ++i)
+            for (int j = 0; j < nzm; ++j)
+                std::memcpy(&q[c][((size_t)(i + 1) * (nzm + 2) + (j + 1)) * nr], &v[((size_t)i * nzm + j) * nr],
+                            sizeof(double) * nr);
+    }
+    if (int r = tc_set_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr)) return r;
+    if (time) *time = s[3];
+    return 0;
+}
+
+int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir) {
+    if (!cfg) return fail(2000, "tc_h5_write_grid_info: null argument");
+    const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
+    std::vector<double> rm(nr), rc(nr), tm(nthm), zm(nzm);
+    if (tc_grid_array(cfg, TC_G_RM, rm.data(), nr) < 0 || tc_grid_array(cfg, TC_G_RC, rc.data(), nr) < 0)
+        return fail(2001, "tc_h5_write_grid_info: invalid configuration");
+    // CreateGrid.F90:61,72: tm(i) = (i - 1/2)/dxt, zm(j) = (j - 1/2)/dxz
+    const double pi = 2.0 * std::asin(1.0);
+    const double dxt = ((double)nthm * cfg->lamb) / (2.0 * pi), dxz = (double)nzm / cfg->alx3;
+    for (int i = 0; i < nthm; ++i) tm[i] = ((double)i + 0.5) / dxt;
+    for (int j = 0; j < nzm; ++j) zm[j] = ((double)j + 0.5) / dxz;
+    std::string err;
+    if (!write_file(join(dir, "cordin_info.h5"),
+                    {f64_dataset("rm", {(uint64_t)nrm}, rm.data()), f64_dataset("rc", {(uint64_t)nr}, rc.data()),
+                     f64_dataset("tm", {(uint64_t)nthm}, tm.data()), f64_dataset("zm", {(uint64_t)nzm}, zm.data())},
+                    err))
+        return fail(2021, err);
+    return 0;
+}

@@ -1,0 +1,58 @@
+"""Restart files through a handle: WriteFlowField then ReadFlowField give back
+the same velocities, the master file carries the reference's scalars, and a
+run restarted from the files equals a run loaded from the same arrays."""
+import numpy as np
+import pytest
+
+from conftest import make_bou, tc
+
+import tc_gb300.initial as ini
+
+from test_h5 import walk
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_continua_round_trip(gpu_lib, tmp_path, precision):
+    bou = make_bou(nthm=48, nzm=40, nrm=32, istr=6, str=3.0)
+    g = tc.TaylorCouette(bou, precision=precision)
+    g.set_state(*ini.couette_noise(bou, seed=4))
+    code, n, t, dt = g.run(3, 0, 0.0)
+    g.write_continua(str(tmp_path), t)
+    want = g.get_state()
+    master = walk(str(tmp_path / "continua_master.h5"))
+    assert sorted(master) == sorted(["nr", "nth", "nz", "time", "rint", "rext", "istr", "str", "alx3", "lamb"])
+    assert master["nr"][2][0] == 33 and master["nth"][2][0] == 49 and master["nz"][2][0] == 41
+    assert master["time"][2][0] == t and master["istr"][2][0] == 6 and master["str"][2][0] == 3.0
+    var = walk(str(tmp_path / "continua_qt.h5"))["var"]
+    assert var[0] == [48, 40, 33]
+    assert np.array_equal(var[2][:, :, :32], want[0][1:-1, 1:-1, :32])
+    h = tc.TaylorCouette(bou, precision=precision)
+    t2 = h.read_continua(str(tmp_path))
+    assert t2 == t
+    got = h.get_state()
+    for a, b, nk in zip(got[:3], want[:3], (32, 33, 32)):
+        assert np.array_equal(a[..., :nk], b[..., :nk])
+    # a restart from the files equals a start from the same arrays
+    ref = tc.TaylorCouette(bou, precision=precision)
+    ref.set_state(*want[:3])
+    h.run(2, 3, t2)
+    ref.run(2, 3, t)
+    for a, b in zip(h.get_state()[:3], ref.get_state()[:3]):
+        assert np.array_equal(a, b)
+    for x in (g, h, ref):
+        x.close()
+
+
+def test_continua_of_another_grid_is_rejected(gpu_lib, tmp_path):
+    bou = make_bou(nthm=24, nzm=20, nrm=16)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*ini.couette_noise(bou, seed=1))
+    g.write_continua(str(tmp_path), 0.5)
+    other = tc.TaylorCouette(make_bou(nthm=24, nzm=20, nrm=20))
+    with pytest.raises(tc.TCError) as e:
+        other.read_continua(str(tmp_path))
+    assert e.value.code == 2024 and "interpolation" in str(e.value)
+    g.close()
+    other.close()
