@@ -63,6 +63,7 @@ enum tc_grid_array {
     TC_G_AP1J, TC_G_AM1J, TC_G_AC1J, TC_G_AP2J, TC_G_AM2J, TC_G_AC2J,
     TC_G_AP2JE, TC_G_AM2JE, TC_G_AC2JE, TC_G_AP3J, TC_G_AM3J, TC_G_AC3J,
     TC_G_APPH, TC_G_AMPH, TC_G_ACPH,
+    TC_G_PVOL, TC_G_UDX2MM, TC_G_UDX2CC,   /* statistics metrics (CreateGrid.F90:141-173) */
     TC_G_AK1,  /* length nthm */
     TC_G_AK3,  /* length nzm  */
     TC_G_COUNT
@@ -297,6 +298,33 @@ int tc_ensemble_launches_per_step(const tc_ensemble* e);
 long long tc_ensemble_device_bytes(const tc_ensemble* e);
 /* Cells of all members: sum of nthm * nzm * nrm. */
 long long tc_ensemble_cells(const tc_ensemble* e);
+
+/* ---- statistics of the output steps (main.F90:188-190) -------------------
+ * Theta averages accumulated per (r, z) row in FP64 on the device, the
+ * reference's stat_arrays: (nrm, nzm) arrays, r fastest. */
+enum tc_stat {
+    TC_ST_VT_MEAN = 0, TC_ST_VR_MEAN, TC_ST_VZ_MEAN, TC_ST_WT_MEAN, TC_ST_WR_MEAN, TC_ST_WZ_MEAN,
+    TC_ST_VT_RMS, TC_ST_VR_RMS, TC_ST_VZ_RMS, TC_ST_WT_RMS, TC_ST_WR_RMS, TC_ST_WZ_RMS,
+    TC_ST_VTVR_MEAN, TC_ST_VTVZ_MEAN, TC_ST_VRVZ_MEAN, TC_ST_PR_MEAN, TC_ST_PR_RMS,
+    TC_ST_DISSTE, TC_ST_COUNT
+};
+/* CalcStats (StatRoutines.F90:13-76, with CalcVorticity.F90:30-70): one
+ * sample of every statistic but disste. */
+int tc_calc_stats(tc_handle* h);
+/* CalcDissipation.F90:22-74: accumulate disste and return the normalised
+ * volume dissipation nute (the value the reference writes to unit 92). */
+int tc_calc_dissipation(tc_handle* h, double* nute);
+/* Statistic `which` (enum tc_stat) into out[nrm * nzm] (r fastest). */
+int tc_get_stat(tc_handle* h, int which, double* out);
+/* Samples taken by tc_calc_stats since creation or tc_reset_stats. */
+int tc_stat_samples(const tc_handle* h);
+int tc_reset_stats(tc_handle* h);
+/* WriteStats (StatRoutines.F90:82-177): <dir>/<name>.h5 with dataset <name>
+ * of shape (nrm, nzm) for every statistic, and <dir>/stafield_master.h5
+ * with averaging_time, R_cordin, Th_cordin, Z_cordin, "Reynolds Number"
+ * and R_Omega.  readstats = 1 adds the values already in the files
+ * (StatReadReduceWrite.F90:27-33). */
+int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats);
 
 /* ---- measurement helpers ------------------------------------------------ */
 

@@ -182,6 +182,11 @@ struct TCRef {
     // pressure-solver work: complex spectrum (1:nrm, 1:nzm/2+1, 1:nthm)
     std::vector<cd> spec;
     FFTPlan plan_z, plan_t;
+    // statistics (stat_arrays): TCREF_ST_COUNT arrays (1:nrm, 1:nzm), the
+    // vorticity (1:nrm, 1:nzm, 1:nthm) and the sample count
+    std::vector<double> stats, vortt, vortr, vortz;
+    int nstatsamples = 0;
+    double& st(int which, int k, int j) { return stats[(size_t)which * nrm * nzm + (size_t)(k - 1) + (size_t)nrm * (j - 1)]; }
 
     size_t H(int k, int j, int i) const { return (size_t)(k - 1) + (size_t)nr * ((size_t)j + (size_t)(nzm + 2) * (size_t)i); }
     size_t N(int k, int j, int i) const { return (size_t)(k - 1) + (size_t)nr * ((size_t)(j - 1) + (size_t)nzm * (size_t)(i - 1)); }
@@ -530,6 +535,8 @@ int tcref_get_grid(void* h, int which, double* dst) {
         case TCREF_G_AM3J: v = &r->am3j; break; case TCREF_G_AC3J: v = &r->ac3j; break;
         case TCREF_G_APPH: v = &r->apph; break; case TCREF_G_AMPH: v = &r->amph; break;
         case TCREF_G_ACPH: v = &r->acph; break;
+        case TCREF_G_PVOL: v = &r->pvol; break; case TCREF_G_UDX2MM: v = &r->udx2mm; break;
+        case TCREF_G_UDX2CC: v = &r->udx2cc; break;
         case TCREF_G_AK1: {
             for (int i = 1; i <= r->nthm; ++i) dst[i - 1] = r->ak1[i];
             return r->nthm;
@@ -1193,6 +1200,135 @@ void tcref_calc_velocity_stats(void* h, double* vmax, double* rms) {
     }
     double den = (double)R.nthm * (double)R.nzm * volt;
     rms[0] = qt2 / den; rms[1] = qr2 / den; rms[2] = qz2 / den;
+}
+
+// CalcVorticity.F90:30-70 into vortt, vortr, vortz (k = 1..nrm).
+static void calc_vorticity(TCRef& R) {
+    const int nrm = R.nrm;
+    R.vortt.assign((size_t)nrm * R.nzm * R.nthm, 0.0);
+    R.vortr.assign(R.vortt.size(), 0.0);
+    R.vortz.assign(R.vortt.size(), 0.0);
+    auto V = [&](int k, int j, int i) { return (size_t)(k - 1) + (size_t)nrm * ((size_t)(j - 1) + (size_t)R.nzm * (i - 1)); };
+    for (int ic = 1; ic <= R.nthm; ++ic) {
+        const int im = ic - 1, ip = ic + 1;
+        for (int jc = 1; jc <= R.nzm; ++jc) {
+            const int jm = jc - 1, jp = jc + 1;
+            for (int kc = 1; kc <= nrm; ++kc) {
+                const int kmm = R.kmv[kc], kpp = R.kpv[kc], kp = kc + 1;
+                const double durdz = ((R.qr[R.H(kp, jp, ic)] * R.usrc[kp] + R.qr[R.H(kc, jp, ic)] * R.usrc[kc])
+                                      - (R.qr[R.H(kp, jm, ic)] * R.usrc[kp] + R.qr[R.H(kc, jm, ic)] * R.usrc[kc])) * R.dxz * 0.25;
+                const double duzdr = ((R.qz[R.H(kpp, jc, ic)] + R.qz[R.H(kpp, jp, ic)])
+                                      - (R.qz[R.H(kmm, jc, ic)] + R.qz[R.H(kmm, jp, ic)])) * 0.5 * R.udx2mm[kc];
+                R.vortt[V(kc, jc, ic)] = durdz - duzdr;
+                const double duzdt = ((R.qz[R.H(kc, jc, ip)] + R.qz[R.H(kc, jp, ip)])
+                                      - (R.qz[R.H(kc, jc, im)] + R.qz[R.H(kc, jp, im)])) * 0.25 * R.dxt * R.usrm[kc];
+                const double dutdz = ((R.qt[R.H(kc, jp, ic)] + R.qt[R.H(kc, jp, ip)])
+                                      - (R.qt[R.H(kc, jm, ic)] + R.qt[R.H(kc, jm, ip)])) * 0.25 * R.dxz;
+                R.vortr[V(kc, jc, ic)] = duzdt - dutdz;
+                const double dutdr = ((R.qt[R.H(kpp, jc, ic)] + R.qt[R.H(kpp, jc, ip)]) * R.rm[kpp]
+                                      - (R.qt[R.H(kmm, jc, ic)] + R.qt[R.H(kmm, jc, ip)]) * R.rm[kmm])
+                                     * 0.5 * R.udx2mm[kc] * R.usrm[kc];
+                const double durdt = ((R.qr[R.H(kc, jc, ip)] * R.usrc[kc] + R.qr[R.H(kp, jc, ip)] * R.usrc[kp])
+                                      - (R.qr[R.H(kc, jc, im)] * R.usrc[kc] + R.qr[R.H(kp, jc, im)] * R.usrc[kp])) * R.dxt * 0.25;
+                R.vortz[V(kc, jc, ic)] = dutdr - durdt;
+            }
+        }
+    }
+}
+
+static void ensure_stats(TCRef& R) {
+    if (R.stats.empty()) R.stats.assign((size_t)TCREF_ST_COUNT * R.nrm * R.nzm, 0.0);
+}
+
+// StatRoutines.F90:13-76 (CalcStats): theta averages accumulated per (k, j).
+void tcref_calc_stats(void* h) {
+    TCRef& R = *(TCRef*)h;
+    ensure_stats(R);
+    R.nstatsamples = R.nstatsamples + 1;
+    const double usnthm = 1.0 / R.nthm;
+    calc_vorticity(R);
+    const int nrm = R.nrm;
+    auto V = [&](int k, int j, int i) { return (size_t)(k - 1) + (size_t)nrm * ((size_t)(j - 1) + (size_t)R.nzm * (i - 1)); };
+    for (int i = 1; i <= R.nthm; ++i) {
+        for (int j = 1; j <= R.nzm; ++j) {
+            for (int k = 1; k <= nrm; ++k) {
+                const int kp = R.kpv[k];          // clamped (StatRoutines.F90:33)
+                const double qt = R.qt[R.H(k, j, i)], qr = R.qr[R.H(k, j, i)], qz = R.qz[R.H(k, j, i)];
+                const double wt = R.vortt[V(k, j, i)], wr = R.vortr[V(k, j, i)], wz = R.vortz[V(k, j, i)];
+                const double prv = R.pr[R.H(k, j, i)];
+                R.st(TCREF_ST_VT_MEAN, k, j) = R.st(TCREF_ST_VT_MEAN, k, j) + qt * usnthm;
+                R.st(TCREF_ST_VR_MEAN, k, j) = R.st(TCREF_ST_VR_MEAN, k, j) + qr * usnthm * R.usrc[k];
+                R.st(TCREF_ST_VZ_MEAN, k, j) = R.st(TCREF_ST_VZ_MEAN, k, j) + qz * usnthm;
+                R.st(TCREF_ST_WT_MEAN, k, j) = R.st(TCREF_ST_WT_MEAN, k, j) + wt * usnthm;
+                R.st(TCREF_ST_WR_MEAN, k, j) = R.st(TCREF_ST_WR_MEAN, k, j) + wr * usnthm;
+                R.st(TCREF_ST_WZ_MEAN, k, j) = R.st(TCREF_ST_WZ_MEAN, k, j) + wz * usnthm;
+                R.st(TCREF_ST_VT_RMS, k, j) = R.st(TCREF_ST_VT_RMS, k, j) + sq(qt) * usnthm;
+                R.st(TCREF_ST_VR_RMS, k, j) = R.st(TCREF_ST_VR_RMS, k, j) + sq(qr * R.usrc[k]) * usnthm;
+                R.st(TCREF_ST_VZ_RMS, k, j) = R.st(TCREF_ST_VZ_RMS, k, j) + sq(qz) * usnthm;
+                R.st(TCREF_ST_WT_RMS, k, j) = R.st(TCREF_ST_WT_RMS, k, j) + sq(wt) * usnthm;
+                R.st(TCREF_ST_WR_RMS, k, j) = R.st(TCREF_ST_WR_RMS, k, j) + sq(wr) * usnthm;
+                R.st(TCREF_ST_WZ_RMS, k, j) = R.st(TCREF_ST_WZ_RMS, k, j) + sq(wz) * usnthm;
+                R.st(TCREF_ST_PR_MEAN, k, j) = R.st(TCREF_ST_PR_MEAN, k, j) + prv * usnthm;
+                R.st(TCREF_ST_PR_RMS, k, j) = R.st(TCREF_ST_PR_RMS, k, j) + sq(prv) * usnthm;
+                const double qr_kp = R.qr[R.H(kp, j, i)];
+                R.st(TCREF_ST_VTVR_MEAN, k, j) = R.st(TCREF_ST_VTVR_MEAN, k, j) +
+                    (qt + R.qt[R.H(k, j, i + 1)]) * (qr * R.usrc[k] + qr_kp * R.usrc[kp]) * usnthm * 0.25;
+                // StatRoutines.F90:58: the second factor sums qz(k,j,i) and qr(k,j+1,i)
+                R.st(TCREF_ST_VTVZ_MEAN, k, j) = R.st(TCREF_ST_VTVZ_MEAN, k, j) +
+                    (qt + R.qt[R.H(k, j, i + 1)]) * (qz + R.qr[R.H(k, j + 1, i)]) * usnthm * 0.25;
+                R.st(TCREF_ST_VRVZ_MEAN, k, j) = R.st(TCREF_ST_VRVZ_MEAN, k, j) +
+                    (qz + R.qz[R.H(k, j + 1, i)]) * (qr * R.usrc[k] + qr_kp * R.usrc[kp]) * usnthm * 0.25;
+            }
+        }
+    }
+}
+
+// CalcDissipation.F90:22-74: accumulates disste, returns nute.
+double tcref_calc_dissipation(void* h) {
+    TCRef& R = *(TCRef*)h;
+    ensure_stats(R);
+    double my_dissipte = 0.0;
+    for (int i = 1; i <= R.nthm; ++i) {
+        const int imm = i - 1, ipp = i + 1;
+        for (int j = 1; j <= R.nzm; ++j) {
+            const int jmm = j - 1, jpp = j + 1;
+            for (int k = 1; k <= R.nrm; ++k) {
+                const int kp = k + 1, kpp = R.kpv[k], kmm = R.kmv[k];
+                const double e11 = (R.qt[R.H(k, j, ipp)] - R.qt[R.H(k, j, imm)]) * R.dxt * R.usrm[k] * 0.5
+                                   + R.qr[R.H(k, j, i)] * sq(R.usrc[k]);
+                const double e12 = (R.qt[R.H(kpp, j, i)] * R.usrm[kpp] - R.qt[R.H(kmm, j, i)] * R.usrm[kmm]) * R.udx2mm[k] * R.rm[k]
+                                   + (R.qr[R.H(k, j, ipp)] - R.qr[R.H(k, j, imm)]) * R.usrc[k] * R.dxt * 0.5;
+                const double e13 = (R.qt[R.H(k, jpp, i)] - R.qt[R.H(k, jmm, i)]) * 0.5 * R.dxz
+                                   + (R.qz[R.H(k, j, ipp)] - R.qz[R.H(k, j, imm)]) * 0.5 * R.dxt * R.usrm[k];
+                const double e22 = (R.qr[R.H(kp, j, i)] * R.usrc[kp] - R.qr[R.H(kmm, j, i)] * R.usrc[kmm]) * R.udx2cc[k];
+                const double e23 = (R.qz[R.H(kpp, j, i)] - R.qz[R.H(kmm, j, i)]) * R.udx2mm[k]
+                                   + (R.qr[R.H(k, jpp, i)] - R.qr[R.H(k, jmm, i)]) * R.usrc[k] * R.dxz * 0.5;
+                const double e33 = (R.qz[R.H(k, jpp, i)] - R.qz[R.H(k, jmm, i)]) * R.dxz * 0.5;
+                const double dissipte = 2.0 * (sq(e11) + sq(e22) + sq(e33)) + sq(e12) + sq(e13) + sq(e23);
+                my_dissipte = my_dissipte + dissipte * R.pvol[k] * R.pi;
+                R.st(TCREF_ST_DISSTE, k, j) = R.st(TCREF_ST_DISSTE, k, j) + dissipte / R.b.ren / (double)R.nthm;
+            }
+        }
+    }
+    const double volt = R.pi * (sq(R.b.rext) - sq(R.b.rint));
+    const double lamdissip = 4.0 * sq(R.b.rext) * sq(R.b.rint) / sq(R.b.rext + R.b.rint) *
+                             sq((R.b.virotint / R.b.rint - R.b.virotext / R.b.rext) / (R.b.rext - R.b.rint));
+    return my_dissipte / ((double)R.nthm * (double)R.nzm * volt * lamdissip);
+}
+
+void tcref_get_stat(void* h, int which, double* out) {
+    TCRef& R = *(TCRef*)h;
+    ensure_stats(R);
+    std::memcpy(out, &R.stats[(size_t)which * R.nrm * R.nzm], sizeof(double) * R.nrm * R.nzm);
+}
+
+int tcref_stat_samples(void* h) { return ((TCRef*)h)->nstatsamples; }
+
+void tcref_get_vorticity(void* h, int comp, double* out) {
+    TCRef& R = *(TCRef*)h;
+    calc_vorticity(R);
+    const std::vector<double>& v = comp == 0 ? R.vortt : (comp == 1 ? R.vortr : R.vortz);
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
 }
 
 // main.F90:152-226, step semantics only (no I/O).  IDTV=0 runs with

@@ -60,6 +60,7 @@ enum {
     TCREF_G_AP1J, TCREF_G_AM1J, TCREF_G_AC1J, TCREF_G_AP2J, TCREF_G_AM2J, TCREF_G_AC2J,
     TCREF_G_AP2JE, TCREF_G_AM2JE, TCREF_G_AC2JE, TCREF_G_AP3J, TCREF_G_AM3J, TCREF_G_AC3J,
     TCREF_G_APPH, TCREF_G_AMPH, TCREF_G_ACPH,
+    TCREF_G_PVOL, TCREF_G_UDX2MM, TCREF_G_UDX2CC,
     TCREF_G_AK1, /* length nthm */
     TCREF_G_AK3, /* length nzm  */
     TCREF_G_COUNT
@@ -107,6 +108,19 @@ double tcref_check_divergence(void* h);
 void   tcref_calc_torque(void* h, double* inner, double* outer);
 /* CalcVelocityStats.F90:21-65: vmax(3) and rms(3). */
 void   tcref_calc_velocity_stats(void* h, double* vmax3, double* rms3);
+
+/* statistics (StatRoutines.F90, CalcVorticity.F90, CalcDissipation.F90) */
+enum tcref_stat {
+    TCREF_ST_VT_MEAN = 0, TCREF_ST_VR_MEAN, TCREF_ST_VZ_MEAN, TCREF_ST_WT_MEAN, TCREF_ST_WR_MEAN,
+    TCREF_ST_WZ_MEAN, TCREF_ST_VT_RMS, TCREF_ST_VR_RMS, TCREF_ST_VZ_RMS, TCREF_ST_WT_RMS,
+    TCREF_ST_WR_RMS, TCREF_ST_WZ_RMS, TCREF_ST_VTVR_MEAN, TCREF_ST_VTVZ_MEAN, TCREF_ST_VRVZ_MEAN,
+    TCREF_ST_PR_MEAN, TCREF_ST_PR_RMS, TCREF_ST_DISSTE, TCREF_ST_COUNT
+};
+void   tcref_calc_stats(void* h);
+double tcref_calc_dissipation(void* h);
+void   tcref_get_stat(void* h, int which, double* out);     /* (nrm, nzm), k fastest */
+int    tcref_stat_samples(void* h);
+void   tcref_get_vorticity(void* h, int comp, double* out); /* (nrm, nzm, nthm), k fastest */
 
 /* main.F90:152-226 time loop restricted to the step semantics: dt control,
  * TimeMarcher, time advance and the error codes it can raise (165, 166, 169,

@@ -23,7 +23,12 @@ LIB = os.path.join(BUILD, "libtcref.so")
 QT, QR, QZ, PR, DPH, RHS, RU1, RU2, RU3, DQ, QCAP = range(11)
 GRID_NAMES = ["rc", "rm", "g2rc", "g2rm", "usrc", "usrm", "udx1vis1", "udx1vis2", "udx1qm",
               "udx2c", "udx2m", "rudx2c", "udx2rm", "ap1j", "am1j", "ac1j", "ap2j", "am2j", "ac2j",
-              "ap2je", "am2je", "ac2je", "ap3j", "am3j", "ac3j", "apph", "amph", "acph", "ak1", "ak3"]
+              "ap2je", "am2je", "ac2je", "ap3j", "am3j", "ac3j", "apph", "amph", "acph", "pvol", "udx2mm", "udx2cc",
+              "ak1", "ak3"]
+# statistics of StatRoutines.F90 / CalcDissipation.F90, in the order of the
+# tcref_stat enum and of the file names WriteStats uses
+STAT_NAMES = ["vt_mean", "vr_mean", "vz_mean", "wt_mean", "wr_mean", "wz_mean", "vt_rms", "vr_rms", "vz_rms",
+              "wt_rms", "wr_rms", "wz_rms", "vtvr_mean", "vtvz_mean", "vrvz_mean", "pr_mean", "pr_rms", "disste"]
 MODE00_LAPACK, MODE00_PIN = 0, 1
 
 
@@ -106,6 +111,13 @@ def lib():
         L.tcref_calc_max_cfl.restype = ctypes.c_double
         L.tcref_check_divergence.argtypes = [vp]
         L.tcref_check_divergence.restype = ctypes.c_double
+        L.tcref_calc_stats.argtypes = [vp]
+        L.tcref_calc_dissipation.argtypes = [vp]
+        L.tcref_calc_dissipation.restype = ctypes.c_double
+        L.tcref_get_stat.argtypes = [vp, ctypes.c_int, dp]
+        L.tcref_stat_samples.argtypes = [vp]
+        L.tcref_stat_samples.restype = ctypes.c_int
+        L.tcref_get_vorticity.argtypes = [vp, ctypes.c_int, dp]
         L.tcref_calc_torque.argtypes = [vp, dp, dp]
         L.tcref_calc_velocity_stats.argtypes = [vp, dp, dp]
         L.tcref_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
@@ -195,6 +207,29 @@ class CppOracle:
         a, b = ctypes.c_double(), ctypes.c_double()
         self.L.tcref_calc_torque(self.h, ctypes.byref(a), ctypes.byref(b))
         return a.value, b.value
+
+    def calc_stats(self):
+        """CalcStats: accumulate the theta averages."""
+        self.L.tcref_calc_stats(self.h)
+
+    def calc_dissipation(self) -> float:
+        """CalcDissipation: accumulate disste, return nute."""
+        return self.L.tcref_calc_dissipation(self.h)
+
+    def stat(self, which: int) -> np.ndarray:
+        """Statistic `which` as an (nzm, nrm) array (Fortran (nrm, nzm))."""
+        out = np.zeros((self.nzm, self.nrm))
+        self.L.tcref_get_stat(self.h, which, _dp(out))
+        return out
+
+    def stat_samples(self) -> int:
+        return self.L.tcref_stat_samples(self.h)
+
+    def vorticity(self, comp: int) -> np.ndarray:
+        """CalcVorticity component (0 theta, 1 r, 2 z) as (nthm, nzm, nrm)."""
+        out = np.zeros((self.nthm, self.nzm, self.nrm))
+        self.L.tcref_get_vorticity(self.h, comp, _dp(out))
+        return out
 
     def velocity_stats(self):
         v, r = np.zeros(3), np.zeros(3)

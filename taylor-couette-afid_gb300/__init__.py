@@ -30,7 +30,10 @@ ERRORS = {165: "CFL above CFLLIM with fixed dt", 166: "dt below DTMIN", 169: "di
 
 GRID_ARRAYS = ["rc", "rm", "g2rc", "g2rm", "usrc", "usrm", "udx1vis1", "udx1vis2", "udx1qm", "udx2c",
                "udx2m", "rudx2c", "udx2rm", "ap1j", "am1j", "ac1j", "ap2j", "am2j", "ac2j", "ap2je",
-               "am2je", "ac2je", "ap3j", "am3j", "ac3j", "apph", "amph", "acph", "ak1", "ak3"]
+               "am2je", "ac2je", "ap3j", "am3j", "ac3j", "apph", "amph", "acph", "pvol", "udx2mm", "udx2cc", "ak1",
+               "ak3"]
+STATS = ["vt_mean", "vr_mean", "vz_mean", "wt_mean", "wr_mean", "wz_mean", "vt_rms", "vr_rms", "vz_rms",
+         "wt_rms", "wr_rms", "wz_rms", "vtvr_mean", "vtvz_mean", "vrvz_mean", "pr_mean", "pr_rms", "disste"]
 FIELDS = ["qt", "qr", "qz", "pr", "dph", "rhs_t", "rhs_r", "rhs_z", "ru1", "ru2", "ru3", "dq", "hr", "qcap"]
 _HALO_FIELDS = 5
 
@@ -121,6 +124,12 @@ SIGNATURES = {
     "tc_measure_fp64_peak": (ctypes.c_int, [_vp, _dp]),
     "tc_selftest_conversions": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "tc_get_bou": (ctypes.c_int, [_vp, ctypes.POINTER(Bou)]),
+    "tc_calc_stats": (ctypes.c_int, [_vp]),
+    "tc_calc_dissipation": (ctypes.c_int, [_vp, _dp]),
+    "tc_get_stat": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "tc_stat_samples": (ctypes.c_int, [_vp]),
+    "tc_reset_stats": (ctypes.c_int, [_vp]),
+    "tc_h5_write_stats": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
     "tc_h5_write_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
     "tc_h5_read_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, _dp]),
     "tc_h5_write_grid_info": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_char_p]),
@@ -318,6 +327,34 @@ class TaylorCouette:
         out = [np.empty(self.halo_shape) for _ in range(4)]
         self._ck(self.L.tc_get_state(self.h, *[_dptr(a) for a in out]))
         return tuple(out)
+
+    # ---- statistics (StatRoutines.F90, CalcDissipation.F90) -----------------
+    def calc_stats(self):
+        """CalcStats: accumulate one sample of the theta averages."""
+        self._ck(self.L.tc_calc_stats(self.h))
+
+    def calc_dissipation(self) -> float:
+        """CalcDissipation: accumulate disste, return nute."""
+        v = ctypes.c_double()
+        self._ck(self.L.tc_calc_dissipation(self.h, ctypes.byref(v)))
+        return v.value
+
+    def stat(self, name: str) -> np.ndarray:
+        """Statistic `name` as an (nzm, nrm) array (Fortran (nrm, nzm))."""
+        out = np.empty((self.nzm, self.nrm))
+        self._ck(self.L.tc_get_stat(self.h, STATS.index(name), _dptr(out)))
+        return out
+
+    @property
+    def stat_samples(self) -> int:
+        return self.L.tc_stat_samples(self.h)
+
+    def reset_stats(self):
+        self._ck(self.L.tc_reset_stats(self.h))
+
+    def write_stats(self, directory: str = ".", readstats: bool = False):
+        """WriteStats: one HDF5 file per statistic plus stafield_master.h5."""
+        self._ck(self.L.tc_h5_write_stats(self.h, directory.encode(), 1 if readstats else 0))
 
     def write_continua(self, directory: str = ".", time: float = 0.0):
         """WriteFlowField: continua_q{t,r,z}.h5 and continua_master.h5."""

@@ -187,7 +187,7 @@ void set_coef_ptrs(CoefT<T>& c, const T* base, int lenK) {
                       &c.ap3j, &c.ac3j, &c.am3j, &c.ap2j, &c.ac2j, &c.am2j,
                       &c.udx2m, &c.rudx2c, &c.udx1qm, &c.apph, &c.acph, &c.amph,
                       &c.usrm2, &c.q_udx2rm, &c.q_usrm, &c.h_udx1vis1, &c.q_udx2c,
-                      &c.q_rc_romeg};
+                      &c.q_rc_romeg, &c.rm, &c.udx2mm, &c.udx2cc, &c.pvol};
     for (int a = 0; a < kCoefArrays; ++a) *cp[a] = base + (size_t)a * lenK;
     c.ak1 = base + (size_t)kCoefArrays * lenK;
     c.ak3 = base + (size_t)(kCoefArrays + 1) * lenK;
@@ -263,7 +263,8 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
         &g.ap1j, &g.ac1j, &g.am1j, &g.ap2je, &g.ac2je, &g.am2je, &g.ap3j, &g.ac3j, &g.am3j,
         &g.ap2j, &g.ac2j, &g.am2j,
         &g.udx2m, &g.rudx2c, &g.udx1qm, &g.apph, &g.acph, &g.amph, nullptr,
-        nullptr, nullptr, nullptr, nullptr, nullptr};
+        nullptr, nullptr, nullptr, nullptr, nullptr,
+        &g.rm, &g.udx2mm, &g.udx2cc, &g.pvol};
     const int lenK = std::max(std::max(nrr, d.nt), d.nz) + 1;
     std::vector<double> host((size_t)(kCoefArrays + 2) * lenK, 0.0);
     for (int a = 0; a < kCoefArrays; ++a) {

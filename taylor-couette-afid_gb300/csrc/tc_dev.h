@@ -64,10 +64,12 @@ struct CoefT {
     // products with powers of two folded in (exact): 0.25*udx2rm, 0.25*usrm,
     // 0.5*udx1vis1, 0.25*udx2c; and 0.25*rc*romeg
     const T *q_udx2rm, *q_usrm, *h_udx1vis1, *q_udx2c, *q_rc_romeg;
+    // statistics metrics (CreateGrid.F90:136-173)
+    const T *rm, *udx2mm, *udx2cc, *pvol;
     const T *ak1, *ak3;
 };
 typedef CoefT<double> Coef;
-constexpr int kCoefArrays = 35;   // arrays before ak1, ak3
+constexpr int kCoefArrays = 39;   // arrays before ak1, ak3
 
 // Scalars of the configuration (param.F90).
 struct Consts {

@@ -17,7 +17,7 @@ struct Grid {
     double pi = 0, dxt = 0, dxz = 0, dxr = 0, dxtq = 0, dxzq = 0, dxrq = 0;
     // radial metrics, length nr
     std::vector<double> rc, rm, g2rc, g2rm, usrc, usrm, udx1vis1, udx1vis2, udx1qm,
-        udx2c, udx2m, rudx2c, udx2rm, pvol;
+        udx2c, udx2m, rudx2c, udx2rm, pvol, udx2mm, udx2cc;
     // momentum operators (CreateGrid.F90:194-322), length nr
     std::vector<double> ap1j, am1j, ac1j, ap2j, am2j, ac2j, ap2je, am2je, ac2je,
         ap3j, am3j, ac3j;

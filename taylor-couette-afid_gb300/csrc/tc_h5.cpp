@@ -619,3 +619,47 @@ int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir) {
         return fail(2021, err);
     return 0;
 }
+
+int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats) {
+    tc_bou b;
+    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_write_stats: null handle");
+    static const char* const names[TC_ST_COUNT] = {
+        "vt_mean", "vr_mean", "vz_mean", "wt_mean", "wr_mean", "wz_mean", "vt_rms", "vr_rms", "vz_rms",
+        "wt_rms", "wr_rms", "wz_rms", "vtvr_mean", "vtvz_mean", "vrvz_mean", "pr_mean", "pr_rms", "disste"};
+    const int nthm = b.nthm, nzm = b.nzm, nrm = b.nrm, nr = nrm + 1;
+    const size_t ns = (size_t)nrm * nzm;
+    std::vector<double> v(ns), old;
+    std::vector<uint64_t> d;
+    std::string err;
+    for (int a = 0; a < TC_ST_COUNT; ++a) {
+        if (int r = tc_get_stat(h, a, v.data())) return r;
+        const std::string path = join(dir, (std::string(names[a]) + ".h5").c_str());
+        if (readstats) {
+            if (!read_named(path, names[a], old, d, err)) return fail(2022, err);
+            if (old.size() != ns) return fail(2024, path + ": statistics of another grid");
+            for (size_t t = 0; t < ns; ++t) v[t] = v[t] + old[t];
+        }
+        // HdfWriteSerialReal2D: Fortran (nrm, nzm) is the dataspace [nzm][nrm]
+        if (!write_file(path, {f64_dataset(names[a], {(uint64_t)nzm, (uint64_t)nrm}, v.data())}, err))
+            return fail(2021, err);
+    }
+    const std::string master = join(dir, "stafield_master.h5");
+    int samples = tc_stat_samples(h);
+    if (readstats) {
+        if (!read_named(master, "averaging_time", old, d, err)) return fail(2022, err);
+        samples += (int)old.at(0);
+    }
+    std::vector<double> rm(nr), tm(nthm), zm(nzm);
+    if (tc_grid_array(&b, TC_G_RM, rm.data(), nr) < 0) return fail(2001, "tc_h5_write_stats: grid");
+    const double pi = 2.0 * std::asin(1.0);
+    const double dxt = ((double)nthm * b.lamb) / (2.0 * pi), dxz = (double)nzm / b.alx3;
+    for (int i = 0; i < nthm; ++i) tm[i] = ((double)i + 0.5) / dxt;
+    for (int j = 0; j < nzm; ++j) zm[j] = ((double)j + 0.5) / dxz;
+    if (!write_file(master, {i32_dataset("averaging_time", samples), f64_dataset("R_cordin", {(uint64_t)nrm}, rm.data()),
+                             f64_dataset("Th_cordin", {(uint64_t)nthm}, tm.data()),
+                             f64_dataset("Z_cordin", {(uint64_t)nzm}, zm.data()),
+                             f64_dataset("Reynolds Number", {1}, &b.ren), f64_dataset("R_Omega", {1}, &b.romeg)},
+                    err))
+        return fail(2021, err);
+    return 0;
+}

@@ -37,4 +37,9 @@ struct tc_handle {
     size_t pool_used = 0;
     double prof_ms[16] = {0};
     long long prof_n[16] = {0};
+    // statistics (StatRoutines.F90 stat_arrays), allocated at the first use:
+    // TC_ST_COUNT arrays of (nrm, nzm), r fastest, plus per-row dissipation
+    double* stats = nullptr;
+    double* stat_rows = nullptr;
+    int nstatsamples = 0;
 };

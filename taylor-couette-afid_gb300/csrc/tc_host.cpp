@@ -125,7 +125,8 @@ std::string build_grid(const tc_bou& b, Grid& g) {
     const int nthm = b.nthm, nzm = b.nzm, nrm = b.nrm, nr = nrm + 1;
     g.nthm = nthm; g.nzm = nzm; g.nrm = nrm; g.nr = nr;
     for (auto* a : {&g.rc, &g.rm, &g.g2rc, &g.g2rm, &g.usrc, &g.usrm, &g.udx1vis1, &g.udx1vis2,
-                    &g.udx1qm, &g.udx2c, &g.udx2m, &g.rudx2c, &g.udx2rm, &g.pvol, &g.ap1j, &g.am1j,
+                    &g.udx1qm, &g.udx2c, &g.udx2m, &g.rudx2c, &g.udx2rm, &g.pvol, &g.udx2mm, &g.udx2cc,
+                    &g.ap1j, &g.am1j,
                     &g.ac1j, &g.ap2j, &g.am2j, &g.ac2j, &g.ap2je, &g.am2je, &g.ac2je, &g.ap3j,
                     &g.am3j, &g.ac3j, &g.apph, &g.amph, &g.acph})
         a->assign(nr, 0.0);
@@ -178,6 +179,20 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         R(g.pvol, k) = sq(R(rc, k + 1)) - sq(R(rc, k));
     }
     R(g.udx2c, nr) = dxr / R(g.g2rc, nr);                         // :167
+    {   // :141-153,160,173: g2rmm and g2rcc (statistics only).  rm(nr) is never
+        // set by CreateGrid and stays 0, so g2rmm(nrm) and udx2mm(nrm) use it.
+        std::vector<double> g2rmm(nr, 0.0), g2rcc(nr, 0.0);
+        R(g2rmm, 1) = (R(g.rm, 2) - R(g.rm, 1)) * dxr;
+        R(g2rcc, 1) = (R(rc, 2) - R(rc, 1)) * dxr;
+        for (int k = 2; k <= nrm; ++k) {
+            R(g2rmm, k) = (R(g.rm, k + 1) - R(g.rm, k - 1)) * dxr;
+            R(g2rcc, k) = (R(rc, k + 1) - R(rc, k - 1)) * dxr;
+        }
+        R(g2rmm, nr) = (R(g.rm, nr) - R(g.rm, nrm)) * dxr;
+        R(g2rcc, nr) = (R(rc, nr) - R(rc, nrm)) * dxr;
+        for (int k = 1; k <= nrm; ++k) R(g.udx2mm, k) = dxr / R(g2rmm, k);
+        for (int k = 1; k <= nr; ++k) R(g.udx2cc, k) = dxr / R(g2rcc, k);
+    }
     for (int k = 1; k <= nr; ++k) {                               // :169-174
         R(g.udx1vis2, k) = g.dxt / (R(rc, k) * b.ren);
         R(g.usrc, k) = 1.0 / R(rc, k);
@@ -295,6 +310,7 @@ const std::vector<double>* grid_array(const Grid& g, int which) {
         case TC_G_AP2JE: return &g.ap2je; case TC_G_AM2JE: return &g.am2je; case TC_G_AC2JE: return &g.ac2je;
         case TC_G_AP3J: return &g.ap3j; case TC_G_AM3J: return &g.am3j; case TC_G_AC3J: return &g.ac3j;
         case TC_G_APPH: return &g.apph; case TC_G_AMPH: return &g.amph; case TC_G_ACPH: return &g.acph;
+        case TC_G_PVOL: return &g.pvol; case TC_G_UDX2MM: return &g.udx2mm; case TC_G_UDX2CC: return &g.udx2cc;
         case TC_G_AK1: return &g.ak1;   case TC_G_AK3: return &g.ak3;
         default: return nullptr;
     }

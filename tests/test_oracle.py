@@ -133,3 +133,69 @@ def test_tanh_grid_with_str4_is_unstable_in_the_reference_algorithm(oracle):
         return float(c.velocity_stats()[0].max())
     assert vmax_after(4, 4.0) > 1e3
     assert vmax_after(6, 20.0) < 2.0
+
+
+# ---- statistics (StatRoutines.F90, CalcVorticity.F90, CalcDissipation.F90) ----
+
+def _couette(oracle_mod, bou):
+    import tc_gb300.initial as ini
+    st = ini.couette_noise(bou, seed=1, amp=0.0)
+    o = oracle_mod.CppOracle(bou)
+    o.set_state(*st)
+    o.call("update_halo", oracle_mod.QT)
+    return o
+
+
+def test_stats_of_laminar_couette(oracle):
+    """Circular Couette flow: the theta mean of qt is the profile itself, its
+    rms equals the mean squared, the axial vorticity is 2A in the interior
+    (A r + B/r has curl 2A), and the normalised dissipation nute -> 1 as the
+    radial grid is refined."""
+    from conftest import make_bou
+    errs = []
+    for nrm in (16, 32, 64):
+        bou = make_bou(nthm=16, nzm=8, nrm=nrm, istr=0, virotint=1.0, virotext=0.0)
+        o = _couette(oracle, bou)
+        o.calc_stats()
+        nute = o.calc_dissipation()
+        assert o.stat_samples() == 1
+        qt = o.state()[0]
+        vt = o.stat(oracle.STAT_NAMES.index("vt_mean"))
+        assert np.allclose(vt, qt[1, 1:-1, :nrm], rtol=1e-14, atol=1e-15)
+        vt2 = o.stat(oracle.STAT_NAMES.index("vt_rms"))
+        assert np.allclose(vt2, vt ** 2, rtol=1e-13)
+        eta = bou["rint"] / bou["rext"]
+        A = (bou["virotext"] - eta * eta * bou["virotint"]) / (1 - eta * eta)
+        wz = o.vorticity(2)
+        assert np.allclose(wz[:, :, 1:-1], 2 * A, rtol=1e-9)
+        errs.append(abs(nute - 1.0))
+    # first order in the radial spacing (the outer-wall cell's gradients are one-sided)
+    assert 1.8 < errs[0] / errs[1] < 2.4 and 1.8 < errs[1] / errs[2] < 2.4 and errs[2] < 0.011
+
+
+def test_stats_accumulate_and_quirks(oracle):
+    """Two samples of one field are twice one sample; vtvz_mean uses qr(k,j+1)
+    as StatRoutines.F90:58 does (not qz), checked against a direct sum."""
+    from conftest import make_bou
+    import tc_gb300.initial as ini
+    bou = make_bou(nthm=12, nzm=10, nrm=8, istr=6, str=3.0)
+    st = ini.couette_noise(bou, seed=3, amp=0.3)
+    o = oracle.CppOracle(bou)
+    o.set_state(*st)
+    for a in (oracle.QT, oracle.QR, oracle.QZ, oracle.PR):
+        o.call("update_halo", a)
+    o.calc_stats()
+    one = [o.stat(w).copy() for w in range(len(oracle.STAT_NAMES))]
+    o.calc_stats()
+    for w in range(len(oracle.STAT_NAMES) - 1):
+        assert np.allclose(o.stat(w), 2 * one[w], rtol=1e-13, atol=1e-300)
+    qt, qr, qz, _ = o.state()
+    usrc = o.grid("usrc")
+    nthm, nzm, nrm = 12, 10, 8
+    want = np.zeros((nzm, nrm))
+    for i in range(1, nthm + 1):
+        for j in range(1, nzm + 1):
+            for k in range(1, nrm + 1):
+                want[j - 1, k - 1] += (qt[i, j, k - 1] + qt[i + 1, j, k - 1]) * (qz[i, j, k - 1] + qr[i, j + 1, k - 1]) \
+                    / nthm * 0.25
+    assert np.allclose(one[oracle.STAT_NAMES.index("vtvz_mean")], want, rtol=1e-12, atol=1e-15)
