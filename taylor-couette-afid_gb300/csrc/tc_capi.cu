@@ -198,6 +198,10 @@ void set_coef_ptrs(CoefT<T>& c, const T* base, int lenK) {
 // Message for tc_last_error(NULL) from the other translation units.
 namespace tcgb {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+void set_handle_error(tc_handle* h, const std::string& msg) {
+    if (h) h->err = msg;
+    g_last_error = msg;
+}
 }  // namespace tcgb
 
 // The exported functions below are declared extern "C" in tc_capi.h, which

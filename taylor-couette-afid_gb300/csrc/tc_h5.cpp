@@ -32,6 +32,7 @@
 
 namespace tcgb {
 void set_last_error(const std::string& msg);
+void set_handle_error(tc_handle* h, const std::string& msg);
 }
 
 namespace {
@@ -487,6 +488,11 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
+int hfail(tc_handle* h, int code, const std::string& msg) {
+    tcgb::set_handle_error(h, msg);
+    return code;
+}
+
 std::string join(const char* dir, const char* file) {
     std::string d = dir ? dir : ".";
     if (d.empty()) d = ".";
@@ -527,7 +533,7 @@ int tc_h5_read_dataset(const char* path, const char* name, double* out, long lon
 
 int tc_h5_write_continua(tc_handle* h, const char* dir, double time) {
     tc_bou b;
-    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_write_continua: null handle");
+    if (!h || tc_get_bou(h, &b)) return hfail(h, 2000, "tc_h5_write_continua: null handle");
     const tc_bou* cfg = &b;
     const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
     const size_t halo = (size_t)(nthm + 2) * (nzm + 2) * nr;
@@ -544,7 +550,7 @@ int tc_h5_write_continua(tc_handle* h, const char* dir, double time) {
                             sizeof(double) * nr);
         std::string err;
         if (!write_file(join(dir, files[c]), {f64_dataset("var", {(uint64_t)nthm, (uint64_t)nzm, (uint64_t)nr}, in.data())}, err))
-            return fail(2021, err);
+            return hfail(h, 2021, err);
     }
     std::vector<WDataset> m;
     m.push_back(i32_dataset("nr", nr));
@@ -558,13 +564,13 @@ int tc_h5_write_continua(tc_handle* h, const char* dir, double time) {
     m.push_back(f64_dataset("alx3", {1}, &cfg->alx3));
     m.push_back(f64_dataset("lamb", {1}, &cfg->lamb));
     std::string err;
-    if (!write_file(join(dir, "continua_master.h5"), m, err)) return fail(2021, err);
+    if (!write_file(join(dir, "continua_master.h5"), m, err)) return hfail(h, 2021, err);
     return 0;
 }
 
 int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
     tc_bou b;
-    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_read_continua: null handle");
+    if (!h || tc_get_bou(h, &b)) return hfail(h, 2000, "tc_h5_read_continua: null handle");
     const tc_bou* cfg = &b;
     const std::string master = join(dir, "continua_master.h5");
     std::vector<double> v;
@@ -573,22 +579,22 @@ int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
     double s[6];
     const char* names[6] = {"nth", "nr", "nz", "time", "istr", "str"};
     for (int i = 0; i < 6; ++i) {
-        if (!read_named(master, names[i], v, d, err)) return fail(2022, err);
-        if (v.size() != 1) return fail(2022, std::string("master scalar '") + names[i] + "' is not a scalar");
+        if (!read_named(master, names[i], v, d, err)) return hfail(h, 2022, err);
+        if (v.size() != 1) return hfail(h, 2022, std::string("master scalar '") + names[i] + "' is not a scalar");
         s[i] = v[0];
     }
     const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
     if ((int)s[0] != nthm + 1 || (int)s[1] != nr || (int)s[2] != nzm + 1 || (int)s[4] != cfg->istr || s[5] != cfg->str)
-        return fail(2024, "the continuation files hold another grid (nth " + std::to_string((int)s[0]) + ", nr " +
+        return hfail(h, 2024, "the continuation files hold another grid (nth " + std::to_string((int)s[0]) + ", nr " +
                               std::to_string((int)s[1]) + ", nz " + std::to_string((int)s[2]) +
                               "): restart interpolation (interp.F90) is not supported");
     const size_t halo = (size_t)(nthm + 2) * (nzm + 2) * nr;
     std::vector<double> q[3];
     const char* files[3] = {"continua_qt.h5", "continua_qr.h5", "continua_qz.h5"};
     for (int c = 0; c < 3; ++c) {
-        if (!read_named(join(dir, files[c]), "var", v, d, err)) return fail(2022, err);
+        if (!read_named(join(dir, files[c]), "var", v, d, err)) return hfail(h, 2022, err);
         if (d.size() != 3 || d[0] != (uint64_t)nthm || d[1] != (uint64_t)nzm || d[2] != (uint64_t)nr)
-            return fail(2024, std::string(files[c]) + ": dataset 'var' has the wrong shape");
+            return hfail(h, 2024, std::string(files[c]) + ": dataset 'var' has the wrong shape");
         q[c].assign(halo, 0.0);
         for (int i = 0; i < nthm; ++i)
             for (int j = 0; j < nzm; ++j)
@@ -622,7 +628,7 @@ int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir) {
 
 int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats) {
     tc_bou b;
-    if (!h || tc_get_bou(h, &b)) return fail(2000, "tc_h5_write_stats: null handle");
+    if (!h || tc_get_bou(h, &b)) return hfail(h, 2000, "tc_h5_write_stats: null handle");
     static const char* const names[TC_ST_COUNT] = {
         "vt_mean", "vr_mean", "vz_mean", "wt_mean", "wr_mean", "wz_mean", "vt_rms", "vr_rms", "vz_rms",
         "wt_rms", "wr_rms", "wz_rms", "vtvr_mean", "vtvz_mean", "vrvz_mean", "pr_mean", "pr_rms", "disste"};
@@ -635,22 +641,22 @@ int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats) {
         if (int r = tc_get_stat(h, a, v.data())) return r;
         const std::string path = join(dir, (std::string(names[a]) + ".h5").c_str());
         if (readstats) {
-            if (!read_named(path, names[a], old, d, err)) return fail(2022, err);
-            if (old.size() != ns) return fail(2024, path + ": statistics of another grid");
+            if (!read_named(path, names[a], old, d, err)) return hfail(h, 2022, err);
+            if (old.size() != ns) return hfail(h, 2024, path + ": statistics of another grid");
             for (size_t t = 0; t < ns; ++t) v[t] = v[t] + old[t];
         }
         // HdfWriteSerialReal2D: Fortran (nrm, nzm) is the dataspace [nzm][nrm]
         if (!write_file(path, {f64_dataset(names[a], {(uint64_t)nzm, (uint64_t)nrm}, v.data())}, err))
-            return fail(2021, err);
+            return hfail(h, 2021, err);
     }
     const std::string master = join(dir, "stafield_master.h5");
     int samples = tc_stat_samples(h);
     if (readstats) {
-        if (!read_named(master, "averaging_time", old, d, err)) return fail(2022, err);
+        if (!read_named(master, "averaging_time", old, d, err)) return hfail(h, 2022, err);
         samples += (int)old.at(0);
     }
     std::vector<double> rm(nr), tm(nthm), zm(nzm);
-    if (tc_grid_array(&b, TC_G_RM, rm.data(), nr) < 0) return fail(2001, "tc_h5_write_stats: grid");
+    if (tc_grid_array(&b, TC_G_RM, rm.data(), nr) < 0) return hfail(h, 2001, "tc_h5_write_stats: grid");
     const double pi = 2.0 * std::asin(1.0);
     const double dxt = ((double)nthm * b.lamb) / (2.0 * pi), dxz = (double)nzm / b.alx3;
     for (int i = 0; i < nthm; ++i) tm[i] = ((double)i + 0.5) / dxt;
@@ -660,6 +666,6 @@ int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats) {
                              f64_dataset("Z_cordin", {(uint64_t)nzm}, zm.data()),
                              f64_dataset("Reynolds Number", {1}, &b.ren), f64_dataset("R_Omega", {1}, &b.romeg)},
                     err))
-        return fail(2021, err);
+        return hfail(h, 2021, err);
     return 0;
 }
