@@ -150,6 +150,23 @@ int tc_h5_read_continua(tc_handle* h, const char* dir, double* time);
 /* WriteGridInfo.F90:22-33: cordin_info.h5 with rm(1:nrm), rc(1:nr),
  * tm(1:nthm), zm(1:nzm) (host only). */
 int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir);
+/* Dumps of the output steps (main.F90:191-198), files named with
+ * itime = nint(1000 time + 0.005) as %08d, written into dir:
+ * DumpFlowField.F90: qt_, qr_, qz_<itime>.h5 ("var", as the continua) and
+ *   ms_<itime>.h5 (time, rint, rext, istr, str, alx3, lamb);
+ * DumpRCuts.F90: slab<m>vt_, slab<m>vr_, slab<m>vz_<itime>.h5, the cylinder
+ *   surfaces at the radii rslab[0..nslab-1] (at most 9; cell k with
+ *   rm(k-1) < rslab < rm(k), InitDumpRCuts), shape (nzm, nthm);
+ * DumpThCuts.F90: the theta = 1 plane, shape (nrm, nzm), into slabvt_ and
+ *   slabvz_<itime>.h5 (the reference writes its vr plane to the slabvt_
+ *   name too, replacing vt there; kept);
+ * DumpStreamwiseAvg.F90: theta averages into slabvt_ax_, slabvr_ax_,
+ *   slabvz_ax_<itime>.h5, shape (nrm, nzm).
+ * The fields are read back from the device (tc_get_state). */
+int tc_h5_dump_flow_field(tc_handle* h, const char* dir, double time);
+int tc_h5_dump_rcuts(tc_handle* h, const char* dir, double time, const double* rslab, int nslab);
+int tc_h5_dump_thcuts(tc_handle* h, const char* dir, double time);
+int tc_h5_dump_streamwise_avg(tc_handle* h, const char* dir, double time);
 /* One float64 dataset `name` of the given shape (C order) in a new file. */
 int tc_h5_write_dataset(const char* path, const char* name, int rank,
                         const long long* dims, const double* data);

@@ -130,6 +130,10 @@ SIGNATURES = {
     "tc_stat_samples": (ctypes.c_int, [_vp]),
     "tc_reset_stats": (ctypes.c_int, [_vp]),
     "tc_h5_write_stats": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
+    "tc_h5_dump_flow_field": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
+    "tc_h5_dump_rcuts": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _dp, ctypes.c_int]),
+    "tc_h5_dump_thcuts": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
+    "tc_h5_dump_streamwise_avg": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
     "tc_h5_write_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
     "tc_h5_read_continua": (ctypes.c_int, [_vp, ctypes.c_char_p, _dp]),
     "tc_h5_write_grid_info": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_char_p]),
@@ -355,6 +359,20 @@ class TaylorCouette:
     def write_stats(self, directory: str = ".", readstats: bool = False):
         """WriteStats: one HDF5 file per statistic plus stafield_master.h5."""
         self._ck(self.L.tc_h5_write_stats(self.h, directory.encode(), 1 if readstats else 0))
+
+    # ---- dumps (DumpFlowField, DumpRCuts, DumpThCuts, DumpStreamwiseAvg) ----
+    def dump_flow_field(self, directory: str, time: float):
+        self._ck(self.L.tc_h5_dump_flow_field(self.h, directory.encode(), float(time)))
+
+    def dump_rcuts(self, directory: str, time: float, radii):
+        r = np.ascontiguousarray(radii, dtype=np.float64)
+        self._ck(self.L.tc_h5_dump_rcuts(self.h, directory.encode(), float(time), _dptr(r), len(r)))
+
+    def dump_thcuts(self, directory: str, time: float):
+        self._ck(self.L.tc_h5_dump_thcuts(self.h, directory.encode(), float(time)))
+
+    def dump_streamwise_avg(self, directory: str, time: float):
+        self._ck(self.L.tc_h5_dump_streamwise_avg(self.h, directory.encode(), float(time)))
 
     def write_continua(self, directory: str = ".", time: float = 0.0):
         """WriteFlowField: continua_q{t,r,z}.h5 and continua_master.h5."""

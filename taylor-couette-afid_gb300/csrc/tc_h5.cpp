@@ -669,3 +669,140 @@ int tc_h5_write_stats(tc_handle* h, const char* dir, int readstats) {
         return hfail(h, 2021, err);
     return 0;
 }
+
+// ---- dumps of the output steps (main.F90:191-198) ---------------------------
+
+namespace {
+
+// itime = nint(1000 time + 0.005), written i8.8 (Dump*.F90)
+std::string time_tag(double time) {
+    char buf[32];
+    std::snprintf(buf, sizeof buf, "%08ld", std::lround(1000.0 * time + 0.005));
+    return buf;
+}
+
+struct HostState {
+    tc_bou b;
+    int nthm, nzm, nrm, nr;
+    std::vector<double> q[3];
+    size_t H(int k, int j, int i) const { return (size_t)(k - 1) + (size_t)nr * ((size_t)j + (size_t)(nzm + 2) * i); }
+};
+
+int load_state(tc_handle* h, HostState& s) {
+    if (!h || tc_get_bou(h, &s.b)) return fail(2000, "null handle");
+    s.nthm = s.b.nthm; s.nzm = s.b.nzm; s.nrm = s.b.nrm; s.nr = s.nrm + 1;
+    for (auto& a : s.q) a.assign((size_t)(s.nthm + 2) * (s.nzm + 2) * s.nr, 0.0);
+    return tc_get_state(h, s.q[0].data(), s.q[1].data(), s.q[2].data(), nullptr);
+}
+
+}  // namespace
+
+int tc_h5_dump_flow_field(tc_handle* h, const char* dir, double time) {
+    HostState s;
+    if (int r = load_state(h, s)) return r;
+    const std::string tag = time_tag(time);
+    const char* pre[3] = {"qt_", "qr_", "qz_"};
+    std::vector<double> in((size_t)s.nthm * s.nzm * s.nr);
+    std::string err;
+    for (int c = 0; c < 3; ++c) {   // HdfWriteRealHalo3D: q(1:nr, 1:nzm, 1:nthm)
+        for (int i = 1; i <= s.nthm; ++i)
+            for (int j = 1; j <= s.nzm; ++j)
+                std::memcpy(&in[((size_t)(i - 1) * s.nzm + (j - 1)) * s.nr], &s.q[c][s.H(1, j, i)], sizeof(double) * s.nr);
+        if (!write_file(join(dir, (pre[c] + tag + ".h5").c_str()),
+                        {f64_dataset("var", {(uint64_t)s.nthm, (uint64_t)s.nzm, (uint64_t)s.nr}, in.data())}, err))
+            return hfail(h, 2021, err);
+    }
+    const tc_bou& b = s.b;
+    if (!write_file(join(dir, ("ms_" + tag + ".h5").c_str()),
+                    {f64_dataset("time", {1}, &time), f64_dataset("rint", {1}, &b.rint), f64_dataset("rext", {1}, &b.rext),
+                     i32_dataset("istr", b.istr), f64_dataset("str", {1}, &b.str), f64_dataset("alx3", {1}, &b.alx3),
+                     f64_dataset("lamb", {1}, &b.lamb)},
+                    err))
+        return hfail(h, 2021, err);
+    return 0;
+}
+
+int tc_h5_dump_rcuts(tc_handle* h, const char* dir, double time, const double* rslab, int nslab) {
+    HostState s;
+    if (int r = load_state(h, s)) return r;
+    if (nslab < 0 || (nslab > 0 && !rslab)) return hfail(h, 2000, "tc_h5_dump_rcuts: bad slab list");
+    if (nslab > 9) nslab = 9;   // InitDumpRCuts: at most 9 slabs
+    std::vector<double> rm(s.nr), usrc(s.nr);
+    if (tc_grid_array(&s.b, TC_G_RM, rm.data(), s.nr) < 0 || tc_grid_array(&s.b, TC_G_USRC, usrc.data(), s.nr) < 0)
+        return hfail(h, 2001, "tc_h5_dump_rcuts: grid");
+    const std::string tag = time_tag(time);
+    std::vector<double> vt((size_t)s.nthm * s.nzm), vr(vt.size()), vz(vt.size());
+    std::string err;
+    for (int m = 1; m <= nslab; ++m) {
+        // InitDumpRCuts: kslab = the k with rm(k-1) < rslab < rm(k), else 1
+        int ks = 1;
+        for (int k = 2; k <= s.nrm; ++k)
+            if (rm[k - 1] > rslab[m - 1] && rm[k - 2] < rslab[m - 1]) ks = k;
+        for (int i = 1; i <= s.nthm; ++i)
+            for (int j = 1; j <= s.nzm; ++j) {
+                const size_t o = (size_t)(i - 1) * s.nzm + (j - 1);   // Fortran (nzm, nthm): [nthm][nzm]
+                vz[o] = s.q[2][s.H(ks, j, i)];
+                vt[o] = s.q[0][s.H(ks, j, i)];
+                vr[o] = (s.q[1][s.H(ks, j, i)] * usrc[ks - 1] + s.q[1][s.H(ks + 1, j, i)] * usrc[ks]) * 0.5;
+            }
+        const std::string sm = "slab" + std::to_string(m);
+        const std::vector<uint64_t> dims{(uint64_t)s.nthm, (uint64_t)s.nzm};
+        if (!write_file(join(dir, (sm + "vt_" + tag + ".h5").c_str()), {f64_dataset("vt", dims, vt.data())}, err) ||
+            !write_file(join(dir, (sm + "vr_" + tag + ".h5").c_str()), {f64_dataset("vr", dims, vr.data())}, err) ||
+            !write_file(join(dir, (sm + "vz_" + tag + ".h5").c_str()), {f64_dataset("vz", dims, vz.data())}, err))
+            return hfail(h, 2021, err);
+    }
+    return 0;
+}
+
+int tc_h5_dump_thcuts(tc_handle* h, const char* dir, double time) {
+    HostState s;
+    if (int r = load_state(h, s)) return r;
+    std::vector<double> usrc(s.nr);
+    if (tc_grid_array(&s.b, TC_G_USRC, usrc.data(), s.nr) < 0) return hfail(h, 2001, "tc_h5_dump_thcuts: grid");
+    const size_t ns = (size_t)s.nrm * s.nzm;
+    std::vector<double> vt(ns), vr(ns), vz(ns);
+    for (int j = 1; j <= s.nzm; ++j)        // the theta = 1 plane (DumpThCuts.F90:33-43)
+        for (int k = 1; k <= s.nrm; ++k) {
+            const size_t o = (size_t)(k - 1) + (size_t)s.nrm * (j - 1);
+            vt[o] = s.q[0][s.H(k, j, 1)];
+            vr[o] = s.q[1][s.H(k, j, 1)] * usrc[k - 1];
+            vz[o] = s.q[2][s.H(k, j, 1)];
+        }
+    const std::string tag = time_tag(time);
+    const std::vector<uint64_t> dims{(uint64_t)s.nzm, (uint64_t)s.nrm};
+    std::string err;
+    // DumpThCuts.F90:55-63 names the vr file slabvt_ too, so the vr dataset
+    // replaces the vt one in that file, as in the reference
+    if (!write_file(join(dir, ("slabvt_" + tag + ".h5").c_str()), {f64_dataset("vt", dims, vt.data())}, err) ||
+        !write_file(join(dir, ("slabvt_" + tag + ".h5").c_str()), {f64_dataset("vr", dims, vr.data())}, err) ||
+        !write_file(join(dir, ("slabvz_" + tag + ".h5").c_str()), {f64_dataset("vz", dims, vz.data())}, err))
+        return hfail(h, 2021, err);
+    return 0;
+}
+
+int tc_h5_dump_streamwise_avg(tc_handle* h, const char* dir, double time) {
+    HostState s;
+    if (int r = load_state(h, s)) return r;
+    std::vector<double> usrc(s.nr);
+    if (tc_grid_array(&s.b, TC_G_USRC, usrc.data(), s.nr) < 0) return hfail(h, 2001, "tc_h5_dump_streamwise_avg: grid");
+    const size_t ns = (size_t)s.nrm * s.nzm;
+    std::vector<double> vt(ns, 0.0), vr(ns, 0.0), vz(ns, 0.0);
+    const double usnthm = 1.0 / (double)s.nthm;
+    for (int i = 1; i <= s.nthm; ++i)       // DumpStreamwiseAvg.F90:33-42
+        for (int j = 1; j <= s.nzm; ++j)
+            for (int k = 1; k <= s.nrm; ++k) {
+                const size_t o = (size_t)(k - 1) + (size_t)s.nrm * (j - 1);
+                vt[o] = vt[o] + s.q[0][s.H(k, j, i)] * usnthm;
+                vr[o] = vr[o] + s.q[1][s.H(k, j, i)] * usrc[k - 1] * usnthm;
+                vz[o] = vz[o] + s.q[2][s.H(k, j, i)] * usnthm;
+            }
+    const std::string tag = time_tag(time);
+    const std::vector<uint64_t> dims{(uint64_t)s.nzm, (uint64_t)s.nrm};
+    std::string err;
+    if (!write_file(join(dir, ("slabvt_ax_" + tag + ".h5").c_str()), {f64_dataset("vt", dims, vt.data())}, err) ||
+        !write_file(join(dir, ("slabvr_ax_" + tag + ".h5").c_str()), {f64_dataset("vr", dims, vr.data())}, err) ||
+        !write_file(join(dir, ("slabvz_ax_" + tag + ".h5").c_str()), {f64_dataset("vz", dims, vz.data())}, err))
+        return hfail(h, 2021, err);
+    return 0;
+}

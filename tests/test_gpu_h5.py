@@ -56,3 +56,35 @@ def test_continua_of_another_grid_is_rejected(gpu_lib, tmp_path):
     assert e.value.code == 2024 and "interpolation" in str(e.value)
     g.close()
     other.close()
+
+
+def test_output_dumps(gpu_lib, tmp_path):
+    """DumpFlowField, DumpRCuts, DumpThCuts and DumpStreamwiseAvg against
+    the same quantities computed here from the state."""
+    bou = make_bou(nthm=24, nzm=20, nrm=16, istr=6, str=3.0)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*ini.couette_noise(bou, seed=6, amp=0.1))
+    code, n, t, dt = g.run(2, 0, 0.0)
+    qt, qr, qz, _ = g.get_state()
+    usrc, rm = tc.grid_array(bou, "usrc"), tc.grid_array(bou, "rm")
+    tag = "%08d" % int(np.floor(1000.0 * t + 0.005 + 0.5))
+    d = str(tmp_path)
+    g.dump_flow_field(d, t)
+    assert np.array_equal(walk(f"{d}/qz_{tag}.h5")["var"][2], qz[1:-1, 1:-1, :])
+    assert walk(f"{d}/ms_{tag}.h5")["time"][2][0] == t
+    radii = [0.5 * (rm[3] + rm[4]), rm[10] - 1e-9]
+    g.dump_rcuts(d, t, radii)
+    for m, ks in ((1, 5), (2, 11)):                      # reference k (1-based) of each slab
+        vr = walk(f"{d}/slab{m}vr_{tag}.h5")["vr"][2]
+        want = (qr[1:-1, 1:-1, ks - 1] * usrc[ks - 1] + qr[1:-1, 1:-1, ks] * usrc[ks]) * 0.5
+        assert vr.shape == (24, 20) and np.allclose(vr, want, rtol=1e-15, atol=0)
+        assert np.array_equal(walk(f"{d}/slab{m}vt_{tag}.h5")["vt"][2], qt[1:-1, 1:-1, ks - 1])
+    g.dump_thcuts(d, t)
+    th = walk(f"{d}/slabvt_{tag}.h5")
+    assert list(th) == ["vr"]                            # the reference's file name collision, kept
+    assert np.array_equal(th["vr"][2], (qr[1, 1:-1, :16] * usrc[:16]))
+    assert np.array_equal(walk(f"{d}/slabvz_{tag}.h5")["vz"][2], qz[1, 1:-1, :16])
+    g.dump_streamwise_avg(d, t)
+    ax = walk(f"{d}/slabvt_ax_{tag}.h5")["vt"][2]
+    assert ax.shape == (20, 16) and np.allclose(ax, qt[1:-1, 1:-1, :16].mean(axis=0), rtol=1e-13)
+    g.close()
