@@ -77,7 +77,8 @@ def test_output_dumps(gpu_lib, tmp_path):
     for m, ks in ((1, 5), (2, 11)):                      # reference k (1-based) of each slab
         vr = walk(f"{d}/slab{m}vr_{tag}.h5")["vr"][2]
         want = (qr[1:-1, 1:-1, ks - 1] * usrc[ks - 1] + qr[1:-1, 1:-1, ks] * usrc[ks]) * 0.5
-        assert vr.shape == (24, 20) and np.allclose(vr, want, rtol=1e-15, atol=0)
+        # (the host compiler may contract the products into fused multiply-adds)
+        assert vr.shape == (24, 20) and np.allclose(vr, want, rtol=1e-13, atol=1e-18)
         assert np.array_equal(walk(f"{d}/slab{m}vt_{tag}.h5")["vt"][2], qt[1:-1, 1:-1, ks - 1])
     g.dump_thcuts(d, t)
     th = walk(f"{d}/slabvt_{tag}.h5")
