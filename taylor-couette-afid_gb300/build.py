@@ -47,7 +47,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         if src.endswith(".cu"):
             cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", path, "-o", obj]
         else:
-            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", obj,
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-c", path, "-o", obj,
                    "-I", os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode != 0:
