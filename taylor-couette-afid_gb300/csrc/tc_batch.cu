@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, c
     radial_column(I.d, I.f, sub, col, comp);
 }
 
-// mode-pair-wise: item = TPB consecutive (kz <= nzm/2, kt) mode pairs
+// mode-wise: item = TPB consecutive (kz, kt) modes
 template <typename T>
 __global__ void __launch_bounds__(256) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
     const long long item = blockIdx.x;
@@ -199,9 +199,9 @@ __global__ void __launch_bounds__(256) ens_ptri_kernel(const InstT<T>* inst, con
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long t = (item - prefix[m]) * blockDim.x + threadIdx.x;
-    if (t >= (long long)I.d.nzh * I.d.PH) return;
+    if (t >= (long long)I.d.nz * I.d.PH) return;
     double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(I.f.spec) : I.f.ws;
-    ptri_mode(I.d, I.c, I.f, ws, t);
+    ptri_one(I.d, I.c, I.f, ws, t);
 }
 
 // row-wise FFT phases: item = R consecutive (k, j) rows
@@ -326,7 +326,7 @@ int rebuild(tc_ensemble* e) {
         cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) * ceil_div(d.P, TPB);
         cnt[PH_CORR] = (long long)d.nr * ceil_div(d.P, TPB);
         cnt[PH_RAD] = 3LL * ceil_div(d.P, TPB);
-        cnt[PH_PTRI] = ceil_div((long long)d.nzh * d.PH, TPB);
+        cnt[PH_PTRI] = ceil_div((long long)d.nz * d.PH, TPB);
         cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
         cnt[PH_THINV] = cnt[PH_DIV];
         cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, ZCols<T>::value);

@@ -24,6 +24,7 @@ constexpr int kRedBlocks = 1216;  // 8 x 152 SMs: enough resident warps to cover
 // the shared memory per block halves the resident blocks).
 template <typename T> struct ZCols { static constexpr int value = 4; };
 
+
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
 template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
@@ -562,6 +563,7 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
 // batches of kRB ahead of the dependent arithmetic, so that each thread keeps
 // several loads in flight (the recurrence itself is sequential).
 constexpr int kRB = 8;
+constexpr int kRBr = 16;   // planes per batch in the radial momentum sweeps
 
 template <bool EXTRA, typename T>
 __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
@@ -569,12 +571,12 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
     T y = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
     rhs[(size_t)k0 * P] = y;
     int k = k0 + 1;
-    for (; k + kRB <= nr; k += kRB) {
-        T r[kRB];
+    for (; k + kRBr <= nr; k += kRBr) {
+        T r[kRBr];
 #pragma unroll
-        for (int b = 0; b < kRB; ++b) r[b] = rhs[(size_t)(k + b) * P];
+        for (int b = 0; b < kRBr; ++b) r[b] = rhs[(size_t)(k + b) * P];
 #pragma unroll
-        for (int b = 0; b < kRB; ++b) {
+        for (int b = 0; b < kRBr; ++b) {
             y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
             rhs[(size_t)(k + b) * P] = y;
         }
@@ -586,15 +588,15 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
     T x = y * ld(di + nr - 1);
     q[(size_t)(nr - 1) * P] += x;
     k = nr - 2;
-    for (; k - (kRB - 1) >= k0; k -= kRB) {
-        T r[kRB], v[kRB];
+    for (; k - (kRBr - 1) >= k0; k -= kRBr) {
+        T r[kRBr], v[kRBr];
 #pragma unroll
-        for (int b = 0; b < kRB; ++b) {
+        for (int b = 0; b < kRBr; ++b) {
             r[b] = rhs[(size_t)(k - b) * P];
             v[b] = q[(size_t)(k - b) * P];
         }
 #pragma unroll
-        for (int b = 0; b < kRB; ++b) {
+        for (int b = 0; b < kRBr; ++b) {
             x = (r[b] - ld(u + k - b) * x) * ld(di + k - b);
             q[(size_t)(k - b) * P] = v[b] + x;
         }
@@ -817,6 +819,75 @@ __device__ __forceinline__ void ptri_mode(const Dims& d, const Coef& c, const Fi
             s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
             st2(x2 + (size_t)k * PS, s2.x, s2.y);
         }
+    }
+}
+
+// One mode (kz, kt) of the full spectrum, kz = 0..nzm-1: the solve of
+// ptri_mode for one member of a pair (the factors of mode kz and nzm-kz are
+// shared: index min(kz, nzm-kz)).  Twice the threads of the paired form
+// with half the registers each, which keeps more warps resident on the FP64
+// pipe; the arithmetic of each mode is ptri_mode's.
+template <typename T>
+__device__ __forceinline__ void ptri_one(const Dims& d, const Coef& c, const FieldsT<T>& f, double2* ws, long long t) {
+    typedef typename V2<T>::type C2;
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const int kf = kz < nzh ? kz : d.nz - kz;          // factor row of the pair
+    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
+    const size_t o = (size_t)kz * PH + kt;
+    C2* x = f.spec + o;
+    double2* w = ws + o;
+    const double* L = f.pf_l + (size_t)kf * PH + kt;
+    const double* DI = f.pf_dinv + (size_t)kf * PH + kt;
+    double2 y = to_d2(x[0]);
+    w[0] = y;
+    int k = 1;
+    for (; k + kRB <= nr; k += kRB) {
+        C2 b[kRB];
+        double l[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; ++q) {
+            l[q] = ld(L + (size_t)(k + q) * FS);
+            b[q] = x[(size_t)(k + q) * PS];
+        }
+#pragma unroll
+        for (int q = 0; q < kRB; ++q) {
+            const double2 v = to_d2(b[q]);
+            y = make_double2(v.x - l[q] * y.x, v.y - l[q] * y.y);
+            w[(size_t)(k + q) * PS] = y;
+        }
+    }
+    for (; k < nr; ++k) {
+        const double l = ld(L + (size_t)k * FS);
+        const double2 v = to_d2(x[(size_t)k * PS]);
+        y = make_double2(v.x - l * y.x, v.y - l * y.y);
+        w[(size_t)k * PS] = y;
+    }
+    double di = ld(DI + (size_t)(nr - 1) * FS);
+    double2 s = make_double2(y.x * di, y.y * di);
+    st2(x + (size_t)(nr - 1) * PS, s.x, s.y);
+    k = nr - 2;
+    for (; k - (kRB - 1) >= 0; k -= kRB) {
+        double2 b[kRB];
+        double u[kRB], dv[kRB];
+#pragma unroll
+        for (int q = 0; q < kRB; ++q) {
+            u[q] = ld(c.apph + k - q);
+            dv[q] = ld(DI + (size_t)(k - q) * FS);
+            b[q] = w[(size_t)(k - q) * PS];
+        }
+#pragma unroll
+        for (int q = 0; q < kRB; ++q) {
+            s = make_double2((b[q].x - u[q] * s.x) * dv[q], (b[q].y - u[q] * s.y) * dv[q]);
+            st2(x + (size_t)(k - q) * PS, s.x, s.y);
+        }
+    }
+    for (; k >= 0; --k) {
+        const double u = ld(c.apph + k);
+        di = ld(DI + (size_t)k * FS);
+        const double2 b = w[(size_t)k * PS];
+        s = make_double2((b.x - u * s.x) * di, (b.y - u * s.y) * di);
+        st2(x + (size_t)k * PS, s.x, s.y);
     }
 }
 

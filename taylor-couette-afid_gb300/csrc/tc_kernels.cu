@@ -164,8 +164,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, FieldsT<T> f, double2* ws) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)d.nzh * d.PH) return;
-    ptri_mode(d, c, f, ws, t);
+    if (t >= (long long)d.nz * d.PH) return;
+    ptri_one(d, c, f, ws, t);
 }
 
 // LU factors of every pressure mode matrix (time independent): thread per
@@ -608,7 +608,7 @@ void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const Plans
 
 template <typename T>
 void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f) {
-    long long n = (long long)d.nzh * d.PH;
+    long long n = (long long)d.nz * d.PH;      // one thread per mode
     double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(f.spec) : f.ws;
     ptri_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f, ws);
     TC_LAUNCH_CHECK();
