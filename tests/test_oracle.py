@@ -199,3 +199,22 @@ def test_stats_accumulate_and_quirks(oracle):
                 want[j - 1, k - 1] += (qt[i, j, k - 1] + qt[i + 1, j, k - 1]) * (qz[i, j, k - 1] + qr[i, j + 1, k - 1]) \
                     / nthm * 0.25
     assert np.allclose(one[oracle.STAT_NAMES.index("vtvz_mean")], want, rtol=1e-12, atol=1e-15)
+
+
+def test_clustered_grid_needs_small_dt_in_the_reference_algorithm(oracle):
+    """On the C2 radial grid (nrm = 384, ISTR = 6, STR3 = 20, smallest cell
+    2.3e-4) an unperturbed Couette flow grows an axial mode from roundoff at
+    dt = 1e-3 (U dt / dr_min = 4.3) although its CFL number allows it, and
+    stays at roundoff at dt = 3e-4: the reason the clustered bench workloads
+    cap DTMAX."""
+    from conftest import make_bou
+    import tc_gb300.initial as ini
+    out = {}
+    for dt in (1e-3, 3e-4):
+        bou = make_bou(nthm=16, nzm=16, nrm=384, istr=6, str=20.0, ren=5000.0, idtv=1, limitCFL=1.2,
+                       dtmin=1e-5, dtmax=dt)
+        o = oracle.CppOracle(bou)
+        o.set_state(*ini.couette_noise(bou, seed=1, amp=0.0))
+        code, t, d = o.run(0, 40, 0.0)
+        out[dt] = o.velocity_stats()[0][2]
+    assert out[1e-3] > 1e-10 and out[3e-4] < 1e-15
