@@ -143,10 +143,23 @@ int tc_set_field(tc_handle* h, int which, const double* in);
 
 /* WriteFlowField.F90:17-47: the state of h at simulated time `time`. */
 int tc_h5_write_continua(tc_handle* h, const char* dir, double time);
-/* ReadFlowField.F90:31-149 for an unchanged grid: load the files into h
- * (tc_set_state; pr = 0) and return their time.  Files of another grid fail
- * with 2024 (the reference would interpolate, interp.F90). */
+/* ReadFlowField.F90:31-149: load the files into h (tc_set_state; pr = 0)
+ * and return their time.  Files of another grid (nth, nz, nr, istr or str
+ * differ) are interpolated onto h's grid as interp.F90 does (its quirks
+ * kept: the old field's halos are linear extrapolations, qr and qz are
+ * placed at (tm, zc, rm) and (tm, zm, rc), the radial direction takes the
+ * lower plane, istr = 0 grids are built as rext x + rint); a grid more than
+ * twice as fine in any direction, or ISTR other than 0 and 6, fails with
+ * 2024. */
 int tc_h5_read_continua(tc_handle* h, const char* dir, double* time);
+/* The same as host arrays, without a handle (no GPU): qt, qr, qz receive
+ * the fields in the reference layout of cfg's grid (halos 0). */
+int tc_h5_load_continua(const tc_bou* cfg, const char* dir, double* qt, double* qr, double* qz,
+                        double* time);
+/* Scalar datasets (int32 where is_int[i], else float64) in a new file, as
+ * HdfSerialWrite{Int,Real}Scalar write them. */
+int tc_h5_write_scalars(const char* path, int n, const char* const* names, const double* values,
+                        const int* is_int);
 /* WriteGridInfo.F90:22-33: cordin_info.h5 with rm(1:nrm), rc(1:nr),
  * tm(1:nthm), zm(1:nzm) (host only). */
 int tc_h5_write_grid_info(const tc_bou* cfg, const char* dir);

@@ -130,6 +130,9 @@ SIGNATURES = {
     "tc_stat_samples": (ctypes.c_int, [_vp]),
     "tc_reset_stats": (ctypes.c_int, [_vp]),
     "tc_h5_write_stats": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
+    "tc_h5_load_continua": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_char_p, _dp, _dp, _dp, _dp]),
+    "tc_h5_write_scalars": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _dp,
+                                           _ip]),
     "tc_h5_dump_flow_field": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
     "tc_h5_dump_rcuts": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _dp, ctypes.c_int]),
     "tc_h5_dump_thcuts": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
@@ -252,6 +255,31 @@ def h5_read(path: str, name: str) -> np.ndarray:
     if rc != 0:
         raise TCError(rc, L.tc_last_error(None).decode())
     return out
+
+
+def h5_write_scalars(path: str, values: dict, ints=()):
+    """Scalar datasets in a new HDF5 file; names in `ints` are int32."""
+    names = list(values)
+    arr = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+    v = np.array([float(values[n]) for n in names])
+    flags = np.array([1 if n in ints else 0 for n in names], dtype=np.int32)
+    rc = lib().tc_h5_write_scalars(path.encode(), len(names), arr, _dptr(v),
+                                   flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if rc != 0:
+        raise TCError(rc, lib().tc_last_error(None).decode())
+
+
+def h5_load_continua(bou: dict, directory: str = "."):
+    """ReadFlowField on the host: (qt, qr, qz, time) on bou's grid, reference
+    layout, interpolated when the files hold another grid (interp.F90)."""
+    b = Bou.from_dict(bou)
+    shape = (b.nthm + 2, b.nzm + 2, b.nrm + 1)
+    q = [np.zeros(shape) for _ in range(3)]
+    t = ctypes.c_double()
+    rc = lib().tc_h5_load_continua(ctypes.byref(b), directory.encode(), *[_dptr(a) for a in q], ctypes.byref(t))
+    if rc != 0:
+        raise TCError(rc, lib().tc_last_error(None).decode())
+    return q[0], q[1], q[2], t.value
 
 
 def h5_write_grid_info(bou: dict, directory: str = "."):

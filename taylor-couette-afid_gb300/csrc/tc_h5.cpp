@@ -568,10 +568,134 @@ int tc_h5_write_continua(tc_handle* h, const char* dir, double time) {
     return 0;
 }
 
-int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
-    tc_bou b;
-    if (!h || tc_get_bou(h, &b)) return hfail(h, 2000, "tc_h5_read_continua: null handle");
-    const tc_bou* cfg = &b;
+// ---- restart interpolation (interp.F90), for ReadFlowField's grid change ----
+
+namespace {
+
+// interp.F90:262-303 (gridnew): n points rc(1:n) and mid points rm(1:n),
+// 1-based in out vectors of size n + 2 (index 0 and n + 1 are filled later).
+// For istr = 0 it computes rc = rext x + rint, not (rext - rint) x + rint;
+// kept, as the reference interpolates between grids built the same way.
+bool gridnew(int n, double rint, double rext, int istr, double str, std::vector<double>& rc, std::vector<double>& rm) {
+    rc.assign(n + 2, 0.0);
+    rm.assign(n + 2, 0.0);
+    if (istr == 0) {
+        for (int i = 1; i <= n; ++i) {
+            const double x3 = (double)(i - 1) / (double)(n - 1);
+            rc[i] = rext * x3 + rint;
+        }
+    } else if (istr == 6) {
+        const double pi = 2.0 * std::asin(1.0);
+        const int nclip = (int)str;
+        const int nrmo = n + nclip + nclip;
+        std::vector<double> etazm(nrmo + 1), etaz(n + 1);
+        for (int i = 1; i <= nrmo; ++i) etazm[i] = +std::cos(pi * ((double)i - 0.5) / (double)nrmo);
+        for (int i = 1; i <= n; ++i) etaz[i] = etazm[i + nclip];
+        const double delet = etaz[1] - etaz[n];
+        for (int i = 1; i <= n; ++i) etaz[i] = etaz[i] / (0.5 * delet);
+        rc[1] = rint;
+        for (int i = 2; i <= n - 1; ++i) rc[i] = (rext - rint) * (1. - etaz[i]) * 0.5 + rint;
+        rc[n] = rext;
+    } else {
+        return false;
+    }
+    for (int i = 1; i <= n - 1; ++i) rm[i] = (rc[i] + rc[i + 1]) * 0.5;
+    rm[n] = 2 * rc[n] - rm[n - 1];
+    return true;
+}
+
+// interp.F90:1-215 for one field: `old` holds q(1:nro, 1:nzom, 1:nthom)
+// (r fastest); the result q(1:nr, 1:nzm, 1:nthm) goes to `out`.
+// Reference behaviour kept: the field is placed at (tc, zm, rm) for intvar 1
+// (qt), (tm, zc, rm) for 2 (qr) and (tm, zm, rc) for 3 (qz); the halos of the
+// old field are linear extrapolations; the radial "upper" corner values are
+// taken from the lower plane bifk (interp.F90:166-169), so the radial
+// direction is not interpolated.
+void interp_field(const std::vector<double>& old, int ntho, int nzo, int nro, int istro, double stro, int intvar,
+                  const tc_bou& b, std::vector<double>& out) {
+    const int nthom = ntho - 1, nzom = nzo - 1;
+    const int nthm = b.nthm, nzm = b.nzm, nr = b.nrm + 1;
+    const double pi = 2.0 * std::asin(1.0);
+    const double thmax = 2.0 * pi / b.lamb;
+    std::vector<double> tcold, tmold, zcold, zmold, rcold, rmold, tcnew, tmnew, zcnew, zmnew, rcnew, rmnew;
+    gridnew(ntho, 0.0, thmax, 0, 1.0, tcold, tmold);
+    gridnew(nzo, 0.0, b.alx3, 0, 1.0, zcold, zmold);
+    gridnew(nro, b.rint, b.rext, istro, stro, rcold, rmold);
+    auto ends = [](std::vector<double>& a, int n) {
+        a[0] = 2 * a[1] - a[2];
+        a[n + 1] = 2 * a[n] - a[n - 1];
+    };
+    ends(tcold, ntho); ends(tmold, ntho); ends(zcold, nzo); ends(zmold, nzo); ends(rcold, nro); ends(rmold, nro);
+    gridnew(nthm + 1, 0.0, thmax, 0, 1.0, tcnew, tmnew);
+    gridnew(nzm + 1, 0.0, b.alx3, 0, 1.0, zcnew, zmnew);
+    gridnew(nr, b.rint, b.rext, b.istr, b.str, rcnew, rmnew);
+    const std::vector<double>*xo, *yo, *zo, *xn, *yn, *zn;
+    switch (intvar) {
+        case 1: xo = &tcold; yo = &zmold; zo = &rmold; xn = &tcnew; yn = &zmnew; zn = &rmnew; break;
+        case 2: xo = &tmold; yo = &zcold; zo = &rmold; xn = &tmnew; yn = &zcnew; zn = &rmnew; break;
+        default: xo = &tmold; yo = &zmold; zo = &rcold; xn = &tmnew; yn = &zmnew; zn = &rcnew; break;
+    }
+    // arrold(0:nro+1, 0:nzom+1, 0:nthom+1); corners never set stay 0
+    const size_t sk = 1, sj = (size_t)nro + 2, si = sj * (size_t)(nzom + 2);
+    std::vector<double> a(si * (size_t)(nthom + 2), 0.0);
+    auto A = [&](int k, int j, int i) -> double& { return a[(size_t)k * sk + (size_t)j * sj + (size_t)i * si]; };
+    for (int i = 1; i <= nthom; ++i)
+        for (int j = 1; j <= nzom; ++j)
+            for (int k = 1; k <= nro; ++k) A(k, j, i) = old[(size_t)(k - 1) + (size_t)nro * ((size_t)(j - 1) + (size_t)nzom * (i - 1))];
+    for (int i = 1; i <= nthom; ++i)                     // interp.F90:99-104
+        for (int j = 1; j <= nzom; ++j) {
+            A(0, j, i) = 2.0 * A(1, j, i) - A(2, j, i);
+            A(nro + 1, j, i) = 2.0 * A(nro, j, i) - A(nro - 1, j, i);
+        }
+    for (int j = 1; j <= nzom; ++j)                      // :105-110
+        for (int k = 1; k <= nro; ++k) {
+            A(k, j, 0) = 2.0 * A(k, j, 1) - A(k, j, 2);
+            A(k, j, nthom + 1) = 2.0 * A(k, j, nthom) - A(k, j, nthom - 1);
+        }
+    for (int i = 1; i <= nthom; ++i)                     // :111-116
+        for (int k = 1; k <= nro; ++k) {
+            A(k, 0, i) = 2.0 * A(k, 1, i) - A(k, 2, i);
+            A(k, nzom + 1, i) = 2.0 * A(k, nzom, i) - A(k, nzom - 1, i);
+        }
+    auto bracket = [](const std::vector<double>& g, int n, double x, int& lo, int& hi) {
+        lo = n - 1; hi = n;
+        for (int l = 1; l <= n; ++l)
+            if (g[l] >= x) { lo = l - 1; hi = l; return; }
+    };
+    out.assign((size_t)nr * nzm * nthm, 0.0);
+    for (int i = 1; i <= nthm; ++i)
+        for (int j = 1; j <= nzm; ++j)
+            for (int k = 1; k <= nr; ++k) {
+                const double bix = (*xn)[i], biy = (*yn)[j], biz = (*zn)[k];
+                int bifi, bici, bifj, bicj, bifk, bick;
+                bracket(*xo, ntho, bix, bifi, bici);
+                bracket(*yo, nzo, biy, bifj, bicj);
+                bracket(*zo, nro, biz, bifk, bick);
+                const double bix1 = (*xo)[bifi], bix2 = (*xo)[bici];
+                const double biy1 = (*yo)[bifj], biy2 = (*yo)[bicj];
+                const double biz1 = (*zo)[bifk], biz2 = (*zo)[bick];
+                const double sfcf = A(bifk, bicj, bifi), sfff = A(bifk, bifj, bifi);
+                const double sccf = A(bifk, bicj, bici), scff = A(bifk, bifj, bici);
+                const double sfcc = A(bifk, bicj, bifi), sffc = A(bifk, bifj, bifi);
+                const double sccc = A(bifk, bicj, bici), scfc = A(bifk, bifj, bici);
+                // interptrilin (interp.F90:218-258)
+                const double dxdydz = 1.0 / ((bix2 - bix1) * (biy2 - biy1) * (biz2 - biz1));
+                const double ans = (sfcf * (bix2 - bix) * (biy - biy1) * (biz2 - biz)
+                                    + sfff * (bix2 - bix) * (biy2 - biy) * (biz2 - biz)
+                                    + sccf * (bix - bix1) * (biy - biy1) * (biz2 - biz)
+                                    + scff * (bix - bix1) * (biy2 - biy) * (biz2 - biz)
+                                    + sfcc * (bix2 - bix) * (biy - biy1) * (biz - biz1)
+                                    + sffc * (bix2 - bix) * (biy2 - biy) * (biz - biz1)
+                                    + sccc * (bix - bix1) * (biy - biy1) * (biz - biz1)
+                                    + scfc * (bix - bix1) * (biy2 - biy) * (biz - biz1)) * dxdydz;
+                out[(size_t)(k - 1) + (size_t)nr * ((size_t)(j - 1) + (size_t)nzm * (i - 1))] = ans;
+            }
+}
+
+}  // namespace
+
+int tc_h5_load_continua(const tc_bou* cfg, const char* dir, double* qt, double* qr, double* qz, double* time) {
+    if (!cfg || !qt || !qr || !qz) return fail(2000, "tc_h5_load_continua: null argument");
     const std::string master = join(dir, "continua_master.h5");
     std::vector<double> v;
     std::vector<uint64_t> d;
@@ -579,30 +703,67 @@ int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
     double s[6];
     const char* names[6] = {"nth", "nr", "nz", "time", "istr", "str"};
     for (int i = 0; i < 6; ++i) {
-        if (!read_named(master, names[i], v, d, err)) return hfail(h, 2022, err);
-        if (v.size() != 1) return hfail(h, 2022, std::string("master scalar '") + names[i] + "' is not a scalar");
+        if (!read_named(master, names[i], v, d, err)) return fail(2022, err);
+        if (v.size() != 1) return fail(2022, std::string("master scalar '") + names[i] + "' is not a scalar");
         s[i] = v[0];
     }
     const int nthm = cfg->nthm, nzm = cfg->nzm, nrm = cfg->nrm, nr = nrm + 1;
-    if ((int)s[0] != nthm + 1 || (int)s[1] != nr || (int)s[2] != nzm + 1 || (int)s[4] != cfg->istr || s[5] != cfg->str)
-        return hfail(h, 2024, "the continuation files hold another grid (nth " + std::to_string((int)s[0]) + ", nr " +
-                              std::to_string((int)s[1]) + ", nz " + std::to_string((int)s[2]) +
-                              "): restart interpolation (interp.F90) is not supported");
+    const int ntho = (int)s[0], nro = (int)s[1], nzo = (int)s[2], istro = (int)s[4];
+    const double stro = s[5];
+    // ReadFlowField.F90:64-116: another grid is interpolated (interp.F90)
+    const bool other = ntho != nthm + 1 || nro != nr || nzo != nzm + 1 || istro != cfg->istr || stro != cfg->str;
+    if (other) {
+        if (nthm + 1 > ntho * 2 || nzm + 1 > nzo * 2 || nr > nro * 2)
+            return fail(2024, "New grid resolution cannot be more than twice the old resolution");
+        if (ntho < 3 || nzo < 3 || nro < 3) return fail(2024, "the continuation files hold a degenerate grid");
+        std::vector<double> rc, rm;
+        if (!gridnew(nro, cfg->rint, cfg->rext, istro, stro, rc, rm) || !gridnew(nr, cfg->rint, cfg->rext, cfg->istr, cfg->str, rc, rm))
+            return fail(2024, "restart interpolation supports ISTR 0 and 6 only (interp.F90:267-274)");
+    }
+    const int fth = other ? ntho - 1 : nthm, fz = other ? nzo - 1 : nzm, fr = other ? nro : nr;
     const size_t halo = (size_t)(nthm + 2) * (nzm + 2) * nr;
-    std::vector<double> q[3];
+    double* q[3] = {qt, qr, qz};
+    std::vector<double> tmp;
     const char* files[3] = {"continua_qt.h5", "continua_qr.h5", "continua_qz.h5"};
     for (int c = 0; c < 3; ++c) {
-        if (!read_named(join(dir, files[c]), "var", v, d, err)) return hfail(h, 2022, err);
-        if (d.size() != 3 || d[0] != (uint64_t)nthm || d[1] != (uint64_t)nzm || d[2] != (uint64_t)nr)
-            return hfail(h, 2024, std::string(files[c]) + ": dataset 'var' has the wrong shape");
-        q[c].assign(halo, 0.0);
+        if (!read_named(join(dir, files[c]), "var", v, d, err)) return fail(2022, err);
+        if (d.size() != 3 || d[0] != (uint64_t)fth || d[1] != (uint64_t)fz || d[2] != (uint64_t)fr)
+            return fail(2024, std::string(files[c]) + ": dataset 'var' does not match continua_master.h5");
+        if (other) {
+            interp_field(v, ntho, nzo, nro, istro, stro, c + 1, *cfg, tmp);
+            v.swap(tmp);
+        }
+        std::fill(q[c], q[c] + halo, 0.0);
         for (int i = 0; i < nthm; ++i)
             for (int j = 0; j < nzm; ++j)
                 std::memcpy(&q[c][((size_t)(i + 1) * (nzm + 2) + (j + 1)) * nr], &v[((size_t)i * nzm + j) * nr],
                             sizeof(double) * nr);
     }
-    if (int r = tc_set_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr)) return r;
     if (time) *time = s[3];
+    return 0;
+}
+
+int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
+    tc_bou b;
+    if (!h || tc_get_bou(h, &b)) return hfail(h, 2000, "tc_h5_read_continua: null handle");
+    const size_t halo = (size_t)(b.nthm + 2) * (b.nzm + 2) * (b.nrm + 1);
+    std::vector<double> q[3];
+    for (auto& a : q) a.resize(halo);
+    if (int r = tc_h5_load_continua(&b, dir, q[0].data(), q[1].data(), q[2].data(), time))
+        return hfail(h, r, tc_last_error(nullptr));
+    return tc_set_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr);
+}
+
+int tc_h5_write_scalars(const char* path, int n, const char* const* names, const double* values, const int* is_int) {
+    if (!path || n < 1 || !names || !values) return fail(2000, "tc_h5_write_scalars: bad argument");
+    std::vector<WDataset> ds;
+    for (int i = 0; i < n; ++i) {
+        if (!names[i]) return fail(2000, "tc_h5_write_scalars: null name");
+        ds.push_back(is_int && is_int[i] ? i32_dataset(names[i], (int32_t)std::lround(values[i]))
+                                         : f64_dataset(names[i], {1}, &values[i]));
+    }
+    std::string err;
+    if (!write_file(path, ds, err)) return fail(2021, err);
     return 0;
 }
 

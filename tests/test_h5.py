@@ -199,3 +199,72 @@ def test_reader_follows_multi_node_group_trees(tmp_path):
     path.write_bytes(bytes(blob[:p]))
     for n in names:
         assert tc.h5_read(str(path), n)[0] == vals[n]
+
+
+def _write_continua(d, nthm, nzm, nrm, fields, time=0.25, istr=0, str_=1.0):
+    nr = nrm + 1
+    tc.h5_write_scalars(str(d / "continua_master.h5"),
+                        dict(nr=nr, nth=nthm + 1, nz=nzm + 1, time=time, rint=1.0, rext=1.4, istr=istr, str=str_,
+                             alx3=2 * math.pi, lamb=1.0), ints=("nr", "nth", "nz", "istr"))
+    for name, f in zip(("qt", "qr", "qz"), fields):
+        tc.h5_write(str(d / f"continua_{name}.h5"), "var", f)
+
+
+def _gridnew(n, rint, rext):
+    # interp.F90 gridnew for istr = 0: rc = rext x + rint (kept as in the reference)
+    rc = np.array([rext * (i / (n - 1)) + rint for i in range(n)])
+    rm = np.empty(n)
+    rm[:-1] = 0.5 * (rc[:-1] + rc[1:])
+    rm[-1] = 2 * rc[-1] - rm[-2]
+    return rc, rm
+
+
+def test_continua_load_same_grid(tmp_path):
+    from conftest import make_bou
+    bou = make_bou(nthm=8, nzm=6, nrm=5)
+    rng = np.random.default_rng(0)
+    f = [rng.standard_normal((8, 6, 6)) for _ in range(3)]
+    _write_continua(tmp_path, 8, 6, 5, f, time=0.75, istr=bou["istr"], str_=bou["str"])
+    qt, qr, qz, t = tc.h5_load_continua(bou, str(tmp_path))
+    assert t == 0.75
+    for a, b in zip((qt, qr, qz), f):
+        assert np.array_equal(a[1:-1, 1:-1, :], b)
+
+
+def test_continua_interpolated_onto_a_finer_grid(tmp_path):
+    """interp.F90: bilinear in theta and z between the old points (a field
+    linear in theta and z comes back exactly away from the corners), no
+    interpolation in r, qt placed at (tc, zm), qz at (tm, zm)."""
+    from conftest import make_bou
+    old = dict(nthm=8, nzm=6, nrm=6)
+    new = make_bou(nthm=12, nzm=10, nrm=6, istr=0)
+    thmax, alx3 = 2 * math.pi, 2 * math.pi
+    tco, tmo = _gridnew(old["nthm"] + 1, 0.0, thmax)
+    zco, zmo = _gridnew(old["nzm"] + 1, 0.0, alx3)
+    tcn, tmn = _gridnew(13, 0.0, thmax)
+    zcn, zmn = _gridnew(11, 0.0, alx3)
+    a, b, c = 0.3, -0.7, 1.25
+
+    def field(xs, ys, nth, nz, nr):
+        f = np.empty((nth, nz, nr))
+        for i in range(nth):
+            for j in range(nz):
+                f[i, j, :] = a * xs[i] + b * ys[j] + c
+        return f
+
+    f_qt = field(tco, zmo, 8, 6, 7)
+    f_qz = field(tmo, zmo, 8, 6, 7)
+    _write_continua(tmp_path, 8, 6, 6, [f_qt, f_qt * 0, f_qz])
+    qt, qr, qz, t = tc.h5_load_continua(new, str(tmp_path))
+    want_qt = field(tcn, zmn, 12, 10, 7)
+    want_qz = field(tmn, zmn, 12, 10, 7)
+    # away from the old field's unset corner halos (first and last new points)
+    sl = (slice(2, 11), slice(2, 9), slice(1, 6))
+    got_qt = qt[1:-1, 1:-1, :][sl]
+    got_qz = qz[1:-1, 1:-1, :][sl]
+    assert np.allclose(got_qt, want_qt[sl], rtol=0, atol=1e-12)
+    assert np.allclose(got_qz, want_qz[sl], rtol=0, atol=1e-12)
+    # more than twice as fine is refused
+    with pytest.raises(tc.TCError) as e:
+        tc.h5_load_continua(make_bou(nthm=24, nzm=10, nrm=6), str(tmp_path))
+    assert e.value.code == 2024
