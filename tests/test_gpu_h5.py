@@ -45,17 +45,25 @@ def test_continua_round_trip(gpu_lib, tmp_path, precision):
         x.close()
 
 
-def test_continua_of_another_grid_is_rejected(gpu_lib, tmp_path):
+def test_continua_of_another_grid(gpu_lib, tmp_path):
+    """A finer grid is interpolated (interp.F90, as the host loader does);
+    one more than twice as fine is refused."""
     bou = make_bou(nthm=24, nzm=20, nrm=16)
     g = tc.TaylorCouette(bou)
     g.set_state(*ini.couette_noise(bou, seed=1))
     g.write_continua(str(tmp_path), 0.5)
-    other = tc.TaylorCouette(make_bou(nthm=24, nzm=20, nrm=20))
+    finer = make_bou(nthm=32, nzm=24, nrm=20)
+    other = tc.TaylorCouette(finer)
+    assert other.read_continua(str(tmp_path)) == 0.5
+    want = tc.h5_load_continua(finer, str(tmp_path))
+    got = other.get_state()
+    assert np.array_equal(got[0][1:-1, 1:-1, :20], want[0][1:-1, 1:-1, :20])
+    too_fine = tc.TaylorCouette(make_bou(nthm=24, nzm=20, nrm=40))
     with pytest.raises(tc.TCError) as e:
-        other.read_continua(str(tmp_path))
-    assert e.value.code == 2024 and "interpolation" in str(e.value)
-    g.close()
-    other.close()
+        too_fine.read_continua(str(tmp_path))
+    assert e.value.code == 2024 and "twice" in str(e.value)
+    for x in (g, other, too_fine):
+        x.close()
 
 
 def test_output_dumps(gpu_lib, tmp_path):
