@@ -276,8 +276,9 @@ def ensemble_legs(tc, torch, stream, steps: int, warmup: int, n_inst: int = 96, 
     """The batched-ensemble workload: n_inst instances with grids drawn from
     {32,48,64,96,128}^3, radius ratio in [0.5, 0.9], 1/NU log-uniform in
     [500, 5000], RK3 at CFL <= 0.8 (the reference's dt rule each step); FP64
-    and mixed ensembles advanced by one CUDA graph of grouped launches per
-    step, tile shapes from the autotuner.  The mixed torque of every instance
+    and mixed ensembles advanced by one CUDA graph per step, the schedule
+    (grouped launches per phase, or one persistent launch per RK substep)
+    and tile shape from the autotuner.  The mixed torque of every instance
     is compared with its FP64 torque after the same number of steps."""
     import tc_gb300.autotune as at
     import tc_gb300.initial as ini
@@ -290,11 +291,11 @@ def ensemble_legs(tc, torch, stream, steps: int, warmup: int, n_inst: int = 96, 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for prec in ("fp64", "mixed"):
         t0 = time.perf_counter()
-        (thr, rows), table = at.tune(prec, bous, states, steps=2)
+        (thr, rows, sched, bps), table = at.tune(prec, bous, states, steps=2)
         tune_s = time.perf_counter() - t0
         ens = tc.Ensemble(prec)
         ens.set_stream(stream.cuda_stream)
-        ens.tune(thr, rows)
+        ens.tune(thr, rows, sched, bps)
         slots = [ens.add(b, st, nsteps=300, dt=0.0) for b, st in zip(bous, states)]
         ens.step(warmup)
         torch.cuda.synchronize()
@@ -307,7 +308,10 @@ def ensemble_legs(tc, torch, stream, steps: int, warmup: int, n_inst: int = 96, 
         torques[prec] = [ens.member(sl).calc_torque() for sl in slots]
         codes = [ens.status_full(sl)[3] for sl in slots]
         out[prec] = {"value": out["cells"] * steps / (ms * 1e-3) / 1e6, "unit": "Mcell-steps/s",
-                     "ms_per_step": ms / steps, "tile": {"threads": thr, "rows": rows},
+                     "ms_per_step": ms / steps, "tile": {"threads": thr, "rows": rows, "schedule": sched, "blocks_per_sm": bps},
+                     "best_ms_by_schedule": {s: round(min(v for k, v in table.items() if k.startswith(s)) * 1e3, 3)
+                                             for s in ("grouped", "persistent")
+                                             if any(k.startswith(s) for k in table)},
                      "tune_seconds": round(tune_s, 2), "tune_table_ms": {k: round(v * 1e3, 3) for k, v in
                                                                           table.items()},
                      "launches_per_step": ens.launches_per_step, "gpu_launches": ens.launch_count - n0,

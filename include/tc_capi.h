@@ -12,7 +12,9 @@
  *  - Every function returns an int status: 0 = OK.  165, 166, 169, 266, 333
  *    and 555 are the reference's error codes (main.F90:148-259); 1000-1999 are
  *    CUDA or allocation failures; 2000-2999 are invalid arguments or
- *    configurations.  tc_last_error() returns a message for the last failure.
+ *    configurations; 3000-3999 are failures the kernels report (3001: a
+ *    bounded wait gave up).  tc_last_error() returns a message for the last
+ *    failure.
  *  - Host arrays of 3-D fields use the reference layout: Fortran
  *    q(1:nr, 0:nzm+1, 0:nthm+1), r fastest, one periodic halo cell in z and
  *    theta (InitVariables.F90:26-35).  pr/qt/qz entries at k = nr are not
@@ -311,11 +313,43 @@ int tc_ensemble_member(tc_ensemble* e, int slot, tc_handle** h);
 int tc_ensemble_count(const tc_ensemble* e);
 /* Tile shapes: threads per cell/column/mode tile (64, 128 or 256) and rows
  * per theta-FFT block (0 = the single-run choice for the largest member,
- * else 1..32, a power of two); schedule 0 = one graph of grouped launches
- * per step.  Takes effect at the next tc_ensemble_step. */
+ * else 1..32, a power of two).  Takes effect at the next tc_ensemble_step.
+ * The persistent schedule uses 128 threads and at most 8 rows. */
 int tc_ensemble_tune(tc_ensemble* e, int threads, int rows);
+/* Schedule of a step:
+ *   TC_SCHED_GROUPED     one CUDA graph of grouped launches per step (a
+ *                        launch per phase and RK substep, each over every
+ *                        member: 27 or, with variable-dt members, 28);
+ *   TC_SCHED_PERSISTENT  one CUDA graph of one cooperative launch per RK
+ *                        substep, each running all phases of the substep for
+ *                        every member with grid-wide barriers between them
+ *                        (the first also CFL, dt and the momentum factors,
+ *                        the last also time += dt).
+ * Both run the same device bodies on the same work lists: a member's results
+ * are the same under either.  A barrier wait in the persistent kernel is
+ * bounded; if one gives up, tc_ensemble_sync returns 3001.  blocks_per_sm
+ * caps the persistent launch's blocks per SM (0 = the occupancy limit; fewer
+ * blocks make the barriers cheaper and leave fewer warps per phase).  Takes
+ * effect at the next tc_ensemble_step. */
+enum tc_schedule { TC_SCHED_GROUPED = 0, TC_SCHED_PERSISTENT = 1 };
+int tc_ensemble_schedule(tc_ensemble* e, int schedule, int blocks_per_sm);
+int tc_ensemble_get_schedule(const tc_ensemble* e);
+/* Blocks of the persistent launch (occupancy limit x SMs; 0 before the first
+ * persistent step). */
+int tc_ensemble_persistent_blocks(const tc_ensemble* e);
+/* Bound on one grid-barrier wait of the persistent kernel (default 10 s,
+ * measured by the device's global timer). */
+int tc_ensemble_set_barrier_timeout(tc_ensemble* e, double seconds);
+/* Failure-path test: make the next persistent barrier unreachable (its
+ * arrival count can no longer reach the grid size), so that every block's
+ * wait runs out after the barrier timeout; the next tc_ensemble_sync or
+ * tc_ensemble_status returns 3001 and resets the barrier.  Steps enqueued
+ * before that synchronisation do nothing. */
+int tc_ensemble_stall_next_barrier(tc_ensemble* e);
 /* Enqueue nsteps steps of every member (graph replays; asynchronous). */
 int tc_ensemble_step(tc_ensemble* e, int nsteps);
+/* Wait for the enqueued steps; 3001 if a persistent barrier wait gave up
+ * (those steps then did nothing from the failed barrier on). */
 int tc_ensemble_sync(tc_ensemble* e);
 /* Steps done, simulated time, last dt and error code (165/166 for a
  * variable-dt member, which then stops) of a member (synchronises). */

@@ -154,6 +154,11 @@ SIGNATURES = {
     "tc_ensemble_member": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
     "tc_ensemble_count": (ctypes.c_int, [_vp]),
     "tc_ensemble_tune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tc_ensemble_schedule": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tc_ensemble_get_schedule": (ctypes.c_int, [_vp]),
+    "tc_ensemble_persistent_blocks": (ctypes.c_int, [_vp]),
+    "tc_ensemble_set_barrier_timeout": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "tc_ensemble_stall_next_barrier": (ctypes.c_int, [_vp]),
     "tc_ensemble_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tc_ensemble_sync": (ctypes.c_int, [_vp]),
     "tc_ensemble_status": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip]),
@@ -521,10 +526,14 @@ class TaylorCouette:
         return v.value
 
 
+SCHEDULES = {"grouped": 0, "persistent": 1}
+
+
 class Ensemble:
     """Many independent runs resident on one device, stepped together (one
-    CUDA graph of grouped launches per step).  Members are admitted and
-    retired between steps; each keeps the single-run arithmetic.
+    CUDA graph per step: grouped launches per phase, or one persistent
+    cooperative launch per RK substep).  Members are admitted and retired
+    between steps; each keeps the single-run arithmetic.
 
     precision: "fp64" or "mixed" for every member."""
 
@@ -589,8 +598,36 @@ class Ensemble:
         self._ck(self.L.tc_ensemble_member(self.e, slot, ctypes.byref(h)))
         return TaylorCouette(self.bous[slot], self.precision, _handle=h)
 
-    def tune(self, threads: int = 128, rows: int = 0):
+    def tune(self, threads: int = 128, rows: int = 0, schedule: str | None = None, blocks_per_sm: int = 0):
+        """Tile shape (threads per tile, rows per theta-FFT item) and, if
+        given, the schedule ("grouped" or "persistent", with its cap on
+        blocks per SM, 0 = occupancy limit)."""
         self._ck(self.L.tc_ensemble_tune(self.e, threads, rows))
+        if schedule is not None:
+            self.set_schedule(schedule, blocks_per_sm)
+
+    def set_schedule(self, schedule: str, blocks_per_sm: int = 0):
+        if schedule not in SCHEDULES:
+            raise ValueError(f"schedule must be one of {sorted(SCHEDULES)}")
+        self._ck(self.L.tc_ensemble_schedule(self.e, SCHEDULES[schedule], int(blocks_per_sm)))
+
+    @property
+    def schedule(self) -> str:
+        v = self.L.tc_ensemble_get_schedule(self.e)
+        return {i: k for k, i in SCHEDULES.items()}[v]
+
+    @property
+    def persistent_blocks(self) -> int:
+        return self.L.tc_ensemble_persistent_blocks(self.e)
+
+    def set_barrier_timeout(self, seconds: float):
+        """Bound on one grid-barrier wait of the persistent kernel."""
+        self._ck(self.L.tc_ensemble_set_barrier_timeout(self.e, float(seconds)))
+
+    def stall_next_barrier(self):
+        """Failure-path test: the next persistent barrier cannot complete, its
+        waits run out and the next sync raises TCError(3001)."""
+        self._ck(self.L.tc_ensemble_stall_next_barrier(self.e))
 
     def step(self, nsteps: int = 1):
         self._ck(self.L.tc_ensemble_step(self.e, int(nsteps)))

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtcgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["tc_capi.cu", "tc_kernels.cu", "tc_host.cpp", "tc_noalloc.cu", "tc_batch.cu", "tc_selftest.cu", "tc_h5.cpp", "tc_stats.cu"]
+SOURCES = ["tc_capi.cu", "tc_kernels.cu", "tc_host.cpp", "tc_noalloc.cu", "tc_batch.cu", "tc_selftest.cu", "tc_h5.cpp", "tc_stats.cu", "tc_persist.cu"]
 
 
 def _nvcc() -> str:

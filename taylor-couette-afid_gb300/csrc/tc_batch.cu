@@ -14,11 +14,16 @@
 //   correction; then end (time += dt).
 // The whole step is captured once in a CUDA graph and replayed; it is
 // re-captured only when members join or leave.  Members run with a fixed dt
-// (the ensemble configurations fix dt per member from its initial CFL).
+// (from their initial CFL) or recompute dt from their CFL every step.
 //
-// Tile shapes (threads per cell tile, rows per theta-FFT block) are tuning
-// knobs, chosen per ensemble by the project's autotuner
-// (taylor-couette-afid_gb300/autotune.py) through tc_ensemble_tune.
+// The persistent schedule (tc_persist.cu, tc_ensemble_schedule) replaces the
+// grouped launches by one cooperative launch per RK substep over the same
+// work lists and device bodies, with grid-wide barriers between the phases.
+//
+// The schedule and the tile shapes (threads per cell tile, rows per
+// theta-FFT block) are tuning knobs, chosen per ensemble by the project's
+// autotuner (taylor-couette-afid_gb300/autotune.py) through
+// tc_ensemble_schedule and tc_ensemble_tune.
 
 #include <algorithm>
 #include <cstdio>
@@ -26,38 +31,11 @@
 #include <string>
 #include <vector>
 
-#include "tc_bodies.cuh"
+#include "tc_ens.cuh"
 #include "tc_handle.h"
 
 namespace tcgb {
 namespace ens {
-
-template <typename T>
-struct InstT {
-    Dims d;
-    CoefT<T> cv;
-    Coef c;
-    Consts k;
-    FieldsT<T> f;
-    PlansT<T> p;
-    MomArgs<T> ma[3];
-    int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
-    T dxzq_t;         // dxzq in the element type
-};
-
-enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };
-
-constexpr double kCflFloor = 0.00000001;   // CalcMaxCFL.F90 starts its maximum here
-
-__device__ __forceinline__ int find_member(const int* prefix, int n, long long item) {
-    int lo = 0, hi = n;
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= item) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
 
 // ---- per-step control ----------------------------------------------------
 
@@ -261,6 +239,12 @@ struct tc_ensemble {
     int rows_used = 0;
     size_t smem_div = 0, smem_z = 0;
     int items[tcgb::ens::PH_COUNT] = {0};
+    int schedule = TC_SCHED_GROUPED;
+    int persist_blocks = 0;              // resident blocks of the persistent kernel
+    int persist_per_sm = 0;              // cap on its blocks per SM (0: occupancy limit)
+    size_t persist_smem = 0;
+    unsigned* bar = nullptr;             // persistent barrier: count, generation, error flag, spare
+    double barrier_timeout = 10.0;       // seconds one persistent barrier wait may last
     bool dirty = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -310,9 +294,11 @@ int rebuild(tc_ensemble* e) {
     std::vector<int> prefix((size_t)PH_COUNT * (n + 1), 0);
     int maxM = 1, maxNz = 1;
     for (int a = 0; a < n; ++a) maxM = std::max(maxM, e->members[e->active[a]]->d.M);
+    const bool persistent = e->schedule == TC_SCHED_PERSISTENT;
     int R = e->rows > 0 ? e->rows : theta_rows(maxM);
+    if (persistent) R = std::min(R, kPersistMaxRows);
     e->rows_used = R;
-    const int TPB = e->threads;
+    const int TPB = persistent ? kPersistThreads : e->threads;
     for (int a = 0; a < n; ++a) {
         tc_handle* h = e->members[e->active[a]];
         InstT<T>& I = inst[a];
@@ -348,6 +334,17 @@ int rebuild(tc_ensemble* e) {
     if (c == cudaSuccess) c = cudaMemcpy(e->inst_dev, inst.data(), sizeof(InstT<T>) * n, cudaMemcpyHostToDevice);
     if (c == cudaSuccess) c = cudaMemcpy(e->prefix_dev, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice);
     if (c != cudaSuccess) return ecuda(e, c, "ensemble tables");
+    if (persistent) {
+        e->persist_smem = std::max(e->smem_div, e->smem_z);
+        if (!e->bar) {
+            c = cudaMalloc(&e->bar, 4 * sizeof(unsigned));
+            if (c != cudaSuccess) return ecuda(e, c, "persistent barrier");
+        }
+        c = cudaMemset(e->bar, 0, 4 * sizeof(unsigned));
+        if (c == cudaSuccess) c = prepare_persistent<T>(R, e->persist_smem, e->persist_per_sm, &e->persist_blocks);
+        if (c != cudaSuccess) return ecuda(e, c, "persistent kernel setup");
+        return 0;
+    }
     switch (R) {
         case 1: set_smem_attrs<1, T>(); break;
         case 2: set_smem_attrs<2, T>(); break;
@@ -377,6 +374,29 @@ int enqueue_step(tc_ensemble* e) {
     const int* pre = e->prefix_dev;
     auto P = [&](int p) { return pre + (size_t)p * (n + 1); };
     cudaStream_t s = e->stream;
+    const int nsst = e->members[e->active[0]]->k.nsst;
+    if (e->schedule == TC_SCHED_PERSISTENT) {
+        // one cooperative launch per substep; the first also runs CFL, begin
+        // and factors, the last also end
+        PersistArgs a;
+        a.prefix = pre;
+        a.n = n;
+        for (int p = 0; p < PH_COUNT; ++p) a.items[p] = e->items[p];
+        a.bar_count = e->bar;
+        a.bar_gen = e->bar + 1;
+        a.err = reinterpret_cast<int*>(e->bar + 2);
+        a.timeout_ns = (unsigned long long)(e->barrier_timeout * 1e9);
+        for (int sub = 0; sub < nsst; ++sub) {
+            a.sub = sub;
+            a.flags = 0;
+            if (sub == 0) a.flags |= (e->items[PH_CFL] > 0 ? PF_CFL : 0) | PF_BEGIN | PF_FACT;
+            if (sub == nsst - 1) a.flags |= PF_END;
+            cudaError_t c = launch_persistent<T>(s, I, a, e->rows_used, e->persist_smem, e->persist_blocks);
+            if (c != cudaSuccess) return ecuda(e, c, "persistent launch");
+        }
+        e->launches_per_step = nsst;
+        return 0;
+    }
     const int TPB = e->threads;
     int count = 0;
     if (e->items[PH_CFL] > 0) {
@@ -385,7 +405,6 @@ int enqueue_step(tc_ensemble* e) {
     }
     ens_begin_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(I, n); ++count;
     ens_factors_kernel<T><<<n, 256, 0, s>>>(I); ++count;
-    const int nsst = e->members[e->active[0]]->k.nsst;
     for (int sub = 0; sub < nsst; ++sub) {
         ens_momentum_kernel<T><<<e->items[PH_MOM], TPB, 0, s>>>(I, P(PH_MOM), n, sub);
         ens_radial_kernel<T><<<e->items[PH_RAD], TPB, 0, s>>>(I, P(PH_RAD), n, sub);
@@ -442,6 +461,20 @@ int capture(tc_ensemble* e) {
     return 0;
 }
 
+// After the stream has drained: 3001 if a persistent barrier wait gave up
+// since the last check (the barrier is reset for the next steps).
+int check_barrier(tc_ensemble* e) {
+    if (!e->bar) return 0;
+    unsigned flag = 0;
+    cudaError_t c = cudaMemcpy(&flag, e->bar + 2, sizeof flag, cudaMemcpyDeviceToHost);
+    if (c != cudaSuccess) return ecuda(e, c, "barrier flag read");
+    if (!flag) return 0;
+    c = cudaMemset(e->bar, 0, 4 * sizeof(unsigned));
+    if (c != cudaSuccess) return ecuda(e, c, "barrier reset");
+    return efail(e, 3001, "persistent ensemble step: a grid barrier wait gave up; the steps since the last "
+                          "synchronisation did not complete");
+}
+
 int prepare(tc_ensemble* e) {
     if (!e->dirty && (e->exec || e->active.empty())) return 0;
     int r = e->mixed ? rebuild<float>(e) : rebuild<double>(e);
@@ -475,6 +508,7 @@ void tc_ensemble_destroy(tc_ensemble* e) {
     if (e->graph) cudaGraphDestroy(e->graph);
     if (e->inst_dev) cudaFree(e->inst_dev);
     if (e->prefix_dev) cudaFree(e->prefix_dev);
+    if (e->bar) cudaFree(e->bar);
     for (tc_handle* h : e->members) if (h) tc_destroy(h);
     delete e;
 }
@@ -571,6 +605,45 @@ int tc_ensemble_tune(tc_ensemble* e, int threads, int rows) {
     return 0;
 }
 
+int tc_ensemble_schedule(tc_ensemble* e, int schedule, int blocks_per_sm) {
+    if (!e) return 2000;
+    if (schedule != TC_SCHED_GROUPED && schedule != TC_SCHED_PERSISTENT)
+        return efail(e, 2013, "schedule must be TC_SCHED_GROUPED or TC_SCHED_PERSISTENT");
+    if (blocks_per_sm < 0 || blocks_per_sm > 32) return efail(e, 2013, "blocks_per_sm must be 0..32");
+    if (schedule != e->schedule || blocks_per_sm != e->persist_per_sm) {
+        e->schedule = schedule;
+        e->persist_per_sm = blocks_per_sm;
+        e->dirty = true;
+    }
+    return 0;
+}
+
+int tc_ensemble_get_schedule(const tc_ensemble* e) { return e ? e->schedule : -1; }
+
+int tc_ensemble_set_barrier_timeout(tc_ensemble* e, double seconds) {
+    if (!e) return 2000;
+    if (!(seconds > 0.0) || seconds > 3600.0) return efail(e, 2013, "barrier timeout must be in (0, 3600] s");
+    e->barrier_timeout = seconds;
+    e->dirty = true;                     // the timeout is an argument of the captured launches
+    return 0;
+}
+
+int tc_ensemble_stall_next_barrier(tc_ensemble* e) {
+    if (!e) return 2000;
+    if (e->schedule != TC_SCHED_PERSISTENT) return efail(e, 2013, "the ensemble does not use the persistent schedule");
+    if (int r = prepare(e)) return r;
+    if (!e->bar) return efail(e, 2013, "the ensemble has no persistent barrier yet (no members)");
+    // an arrival count that no number of arrivals brings to the grid size:
+    // the next barrier's generation never changes and every wait runs out
+    const unsigned stuck = 0x80000000u;
+    cudaError_t c = cudaMemcpyAsync(e->bar, &stuck, sizeof stuck, cudaMemcpyHostToDevice, e->stream);
+    if (c == cudaSuccess) c = e->stream ? cudaStreamSynchronize(e->stream) : cudaDeviceSynchronize();
+    if (c != cudaSuccess) return ecuda(e, c, "barrier stall");
+    return 0;
+}
+
+int tc_ensemble_persistent_blocks(const tc_ensemble* e) { return e ? e->persist_blocks : 0; }
+
 int tc_ensemble_step(tc_ensemble* e, int nsteps) {
     if (!e) return 2000;
     if (int r = prepare(e)) return r;
@@ -587,7 +660,7 @@ int tc_ensemble_sync(tc_ensemble* e) {
     if (!e) return 2000;
     cudaError_t c = e->stream ? cudaStreamSynchronize(e->stream) : cudaDeviceSynchronize();
     if (c != cudaSuccess) return ecuda(e, c, "ensemble sync");
-    return 0;
+    return check_barrier(e);
 }
 
 int tc_ensemble_status(tc_ensemble* e, int slot, int* steps_done, double* time, double* dt, int* errorcode) {
@@ -597,6 +670,7 @@ int tc_ensemble_status(tc_ensemble* e, int slot, int* steps_done, double* time, 
     cudaError_t c = cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, e->stream);
     if (c == cudaSuccess) c = e->stream ? cudaStreamSynchronize(e->stream) : cudaDeviceSynchronize();
     if (c != cudaSuccess) return ecuda(e, c, "status read");
+    if (int r = check_barrier(e)) return r;
     if (steps_done) *steps_done = st.ntime;
     if (time) *time = st.time;
     if (dt) *dt = st.dt;

@@ -27,7 +27,16 @@ template <typename T> struct ZCols { static constexpr int value = 4; };
 
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
+// Loads of fields and coefficients.  Kernels that run several dependent
+// phases in one launch (tc_persist.cu) define TC_COHERENT_LOADS: their loads
+// are then ordinary global loads, which the memory model orders after the
+// grid barrier's fences; the read-only path (ld.global.nc) carries no such
+// guarantee for lines another block rewrote earlier in the same launch.
+#ifdef TC_COHERENT_LOADS
+template <typename T> __device__ __forceinline__ T ld(const T* p) { return *p; }
+#else
 template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
+#endif
 
 
 // --------------------------------------------------------------------------
@@ -627,8 +636,8 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
                          F.scale(sub, 2), (T)0);
 }
 
-__device__ __forceinline__ double2 ld2(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }
-__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+__device__ __forceinline__ double2 ld2(const double* p) { return ld(reinterpret_cast<const double2*>(p)); }
+__device__ __forceinline__ float2 ld2(const float* p) { return ld(reinterpret_cast<const float2*>(p)); }
 
 // CalcLocalDivergence.F90:27-40 for cells 2m and 2m+1 of row (k, j).
 template <typename T>

@@ -1,0 +1,77 @@
+// tc_ens.cuh -- what the ensemble kernels share (tc_batch.cu: grouped launches
+// per phase; tc_persist.cu: one persistent launch per substep): the
+// per-member parameter block, the phase enumeration and the lookup of a work
+// item's member in a prefix table of item counts.
+#pragma once
+
+#include "tc_bodies.cuh"
+
+namespace tcgb {
+namespace ens {
+
+template <typename T>
+struct InstT {
+    Dims d;
+    CoefT<T> cv;
+    Coef c;
+    Consts k;
+    FieldsT<T> f;
+    PlansT<T> p;
+    MomArgs<T> ma[3];
+    int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
+    T dxzq_t;         // dxzq in the element type
+};
+
+enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };
+
+constexpr double kCflFloor = 0.00000001;   // CalcMaxCFL.F90 starts its maximum here
+
+__device__ __forceinline__ int find_member(const int* prefix, int n, long long item) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (prefix[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The persistent schedule: one cooperative launch per RK substep.  The
+// first substep's launch also reduces the CFL numbers of variable-dt members,
+// sets each member's dt, beta and inner-wall forcing and factors the momentum
+// matrices; the last one also advances time.  Between phases the blocks meet
+// at a grid-wide barrier.  Tables are those of the grouped kernels, built
+// with kPersistThreads threads per tile and R <= kPersistMaxRows rows per
+// theta-FFT item.
+constexpr int kPersistThreads = 128;
+constexpr int kPersistMaxRows = 8;
+
+enum { PF_CFL = 1, PF_BEGIN = 2, PF_FACT = 4, PF_END = 8 };
+
+struct PersistArgs {
+    const int* prefix;           // PH_COUNT tables of n + 1 entries
+    int n;
+    int items[PH_COUNT];
+    int sub;
+    int flags;                   // PF_* phases around the substep
+    unsigned* bar_count;         // barrier arrival counter (0 between barriers)
+    unsigned* bar_gen;           // barrier generation
+    int* err;                    // set to 1 when a barrier wait gives up
+    unsigned long long timeout_ns;   // bound on one barrier wait (device global timer)
+};
+
+// Blocks of the persistent kernel for R rows and `smem` bytes of dynamic
+// shared memory: SMs x the occupancy limit, or x per_sm_cap if that is
+// smaller and positive (fewer blocks: cheaper barriers, fewer warps).  Sets
+// the kernel's shared memory attribute; call outside stream capture.
+template <typename T>
+cudaError_t prepare_persistent(int R, size_t smem, int per_sm_cap, int* blocks);
+
+// Enqueue one persistent substep on `s` (cooperative launch of `blocks`
+// blocks, as prepare_persistent returned); returns the launch's status.
+template <typename T>
+cudaError_t launch_persistent(cudaStream_t s, const InstT<T>* inst, const PersistArgs& a, int R, size_t smem,
+                              int blocks);
+
+}  // namespace ens
+}  // namespace tcgb
