@@ -93,11 +93,11 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int k = (int)(local / tiles);
+    const int k = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
     double v = 0.0;
     if (flat < I.d.P) {
-        const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+        const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
         v = cfl_cell(I.d, I.c, I.cv, I.k.dxt, I.k.dxz, I.f, i, j, k);
     }
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -125,10 +125,10 @@ __global__ void __launch_bounds__(256) ens_momentum_kernel(const InstT<T>* inst,
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int chunk = (int)(local / tiles);
+    const int chunk = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)chunk * tiles) * blockDim.x + threadIdx.x;
     if (flat >= I.d.P) return;
-    const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+    const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
     if (MomMarch<T>::value) {
         const int k0 = chunk * kMomChunk, k1 = min(k0 + kMomChunk, I.d.nr);
         momentum_column(I.d, I.cv, I.ma[sub], i, j, k0, k1);
@@ -147,10 +147,10 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int k = (int)(local / tiles);
+    const int k = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
     if (flat >= I.d.P) return;
-    const int j = (int)(flat / I.d.nt), i = (int)(flat - (long long)j * I.d.nt);
+    const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
     correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, k);
 }
 
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, c
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int comp = (int)(local / tiles);
+    const int comp = (int)((unsigned)local / (unsigned)tiles);
     const long long col = (local - (long long)comp * tiles) * blockDim.x + threadIdx.x;
     if (col >= I.d.P) return;
     radial_column(I.d, I.f, sub, col, comp);

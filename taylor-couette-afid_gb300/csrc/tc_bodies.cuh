@@ -39,6 +39,23 @@ template <typename T> __device__ __forceinline__ T ld(const T* p) { return __ldg
 #endif
 
 
+// Stage a tile in shared memory: a[at(t)] = get(t) for t in [0, n), with U
+// values (and their global loads) in flight per thread; a plain loop would
+// wait for each load before issuing the next.
+template <int U, typename C2, typename G, typename A>
+__device__ __forceinline__ void stage_tile(C2* a, int n, G get, A at) {
+    const int bd = blockDim.x;
+    int t = threadIdx.x;
+    for (; t + (U - 1) * bd < n; t += U * bd) {
+        C2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = get(t + u * bd);
+#pragma unroll
+        for (int u = 0; u < U; ++u) a[at(t + u * bd)] = v[u];
+    }
+    for (; t < n; t += bd) a[at(t)] = get(t);
+}
+
 // --------------------------------------------------------------------------
 // Step control
 // --------------------------------------------------------------------------
@@ -675,7 +692,7 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
     const long long nrows = (long long)d.nr * d.nz;
     // usdt/(nthm nzm) with the 1/2 of the real-transform unpacking folded in
     const T scl = (T)(FROM_PHI ? fft_norm : f.scal[sub]);
-    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+    stage_tile<4>(a, R * M, [&](int t) {
         const int r = fdiv(t, pl.mn), m = t - r * M;
         const long long row = row0 + r;
         C2 z = mk2((T)0, (T)0);
@@ -687,8 +704,8 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
             z.x *= scl;
             z.y *= scl;
         }
-        a[m * R + r] = z;
-    }
+        return z;
+    }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
     const C2* Z = fft_lines<R>(a, b, pl, tw, false);
     // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
@@ -717,10 +734,10 @@ __device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl,
     C2* a = smem;
     C2* b = smem + (size_t)ZC * nz;
     C2* plane = f.spec + (size_t)kplane * d.PS;
-    for (int t = threadIdx.x; t < ZC * nz; t += blockDim.x) {
+    stage_tile<8>(a, ZC * nz, [&](int t) {
         const int c = t % ZC, j = t / ZC;
-        a[t] = (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
-    }
+        return (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
+    }, [](int t) { return t; });
     __syncthreads();
     const C2* Z = fft_lines<ZC>(a, b, pl, tw, inv != 0);
     for (int t = threadIdx.x; t < ZC * nz; t += blockDim.x) {
@@ -909,7 +926,7 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
     C2* a = smem;
     C2* b = smem + (size_t)R * M;
     const long long nrows = (long long)d.nr * d.nz;
-    for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+    stage_tile<4>(a, R * M, [&](int t) {
         const int r = fdiv(t, pl.mn), kt = t - r * M;
         const long long row = row0 + r;
         C2 z = mk2((T)0, (T)0);
@@ -924,8 +941,8 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
             // Z = e + i wo
             z = mk2(e.x - wo.y, e.y + wo.x);
         }
-        a[kt * R + r] = z;
-    }
+        return z;
+    }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
     const C2* Z = fft_lines<R>(a, b, pl, tw, true);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
@@ -986,11 +1003,12 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, const
     }
 }
 
-// CalcMaxCFL.F90:30-43 at cell (i, j, k); in FP32 on the mixed path (the
-// maximum itself is exact in any precision).
+// CalcMaxCFL.F90:30-43 at cell (i, j, k), in the element type: FP32 on the
+// mixed path (a maximum is exact in any precision, so the reduction over
+// cells can stay in FP32 too).
 template <typename T>
-__device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxt, double dxz,
-                                           const FieldsT<T>& f, int i, int j, int k) {
+__device__ __forceinline__ T cfl_value(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxt, double dxz,
+                                       const FieldsT<T>& f, int i, int j, int k) {
     const size_t P = (size_t)d.P;
     const int ip = wp(i, d.nt), jp = wp(j, d.nz);
     const size_t o = (size_t)k * P + (size_t)j * d.nt + i;
@@ -999,13 +1017,22 @@ __device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, const C
         const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * ld(cv.usrm + k)));
         const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * ld(cv.udx2rm + k)));
         const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
-        return f2d((float)(vt + vr + vz));
+        return vt + vr + vz;
     }
     const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
     const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
     const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
-    return fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
-           fabs((z1 + z0) * 0.5 * dxz);
+    return (T)(fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
+               fabs((z1 + z0) * 0.5 * dxz));
+}
+
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return f2d(v); }
+
+template <typename T>
+__device__ __forceinline__ double cfl_cell(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxt, double dxz,
+                                           const FieldsT<T>& f, int i, int j, int k) {
+    return to_double(cfl_value(d, c, cv, dxt, dxz, f, i, j, k));
 }
 
 // Scalars of the momentum kernel for substep `sub`, in the element type T.

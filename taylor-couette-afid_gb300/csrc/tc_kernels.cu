@@ -262,34 +262,49 @@ __device__ double block_reduce(double v, double* sh) {
     return v;
 }
 
-// CalcMaxCFL.F90:30-43 (which = 0) and CheckDivergence.F90:77-89 (which = 1).
-template <typename T>
-__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, CoefT<T> cv, double dxt, double dxz, FieldsT<T> f,
-                                                               int which, int only_on_output) {
+// CalcMaxCFL.F90:30-43 (WHICH = 0) and CheckDivergence.F90:77-89 (WHICH = 1):
+// blockIdx.y strides over radial levels, the x blocks over the cells of a
+// level (32-bit index arithmetic).  The CFL maximum is kept in the element
+// type (exact); the divergence in FP64.
+template <int WHICH, typename T>
+__global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, CoefT<T> cv, double dxt, double dxz,
+                                                               FieldsT<T> f, int only_on_output) {
     __shared__ double sh[32];
     if (only_on_output && (f.st->halt || !f.st->output)) return;
-    const long long n = (long long)d.nr * d.P;
-    double best = which == 0 ? 0.00000001 : 0.0;
+    typedef typename std::conditional<WHICH == 0, T, double>::type A;
+    A best = WHICH == 0 ? (A)0.00000001 : (A)0.0;
     const size_t P = (size_t)d.P;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(t / d.P);
-        const long long cell = t - (long long)k * d.P;
-        const int j = (int)(cell / d.nt), i = (int)(cell - (long long)j * d.nt);
-        const int ip = wp(i, d.nt), jp = wp(j, d.nz);
-        const size_t o = (size_t)t;
-        const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
-        const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
-        const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
-        double v;
-        if (which == 0) {
-            v = cfl_cell(d, c, cv, dxt, dxz, f, i, j, k);
-        } else {
-            v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) + (z1 - z0) * dxz);
+    const int nt = d.nt, Pi = (int)d.P;
+    for (int k = blockIdx.y; k < d.nr; k += gridDim.y) {
+        for (int flat = blockIdx.x * blockDim.x + threadIdx.x; flat < Pi; flat += gridDim.x * blockDim.x) {
+            const int j = (int)((unsigned)flat / (unsigned)nt), i = flat - j * nt;
+            if (WHICH == 0) {
+                best = fmax(best, cfl_value(d, c, cv, dxt, dxz, f, i, j, k));
+            } else {
+                const int ip = wp(i, nt), jp = wp(j, d.nz);
+                const size_t o = (size_t)k * P + (size_t)flat;
+                const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * nt + ip);
+                const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
+                const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * nt + i);
+                const double v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) +
+                                      (z1 - z0) * dxz);
+                best = fmax(best, (A)v);
+            }
         }
-        best = fmax(best, v);
     }
-    best = block_reduce<true>(best, sh);
-    if (threadIdx.x == 0) f.red[blockIdx.x] = best;
+    double b = to_double(best);
+    b = block_reduce<true>(b, sh);
+    if (threadIdx.x == 0) f.red[blockIdx.y * gridDim.x + blockIdx.x] = b;
+}
+
+// Grid of the cell reductions: at most kRedBlocks blocks, levels on y.
+inline dim3 cellmax_grid(const Dims& d) {
+    const long long tiles = ((long long)d.P + kRedThreads - 1) / kRedThreads;
+    const int gx = (int)(tiles < kRedBlocks ? tiles : kRedBlocks);
+    int gy = kRedBlocks / gx;
+    if (gy > d.nr) gy = d.nr;
+    if (gy < 1) gy = 1;
+    return dim3(gx, gy);
 }
 
 __global__ void __launch_bounds__(kRedThreads) cellmax_finish(const double* red, StepState* st, int nblocks,
@@ -668,15 +683,17 @@ void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, doubl
 
 template <typename T>
 void launch_cfl(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k, const FieldsT<T>& f) {
-    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, 0, 0);
-    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 0, 0);
+    const dim3 g = cellmax_grid(d);
+    cellmax_kernel<0, T><<<g, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, (int)(g.x * g.y), 0, 0);
     TC_LAUNCH_CHECK();
 }
 template <typename T>
 void launch_check_divergence(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>& cv, const Consts& k,
                              const FieldsT<T>& f, bool only_on_output) {
-    cellmax_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, 1, only_on_output ? 1 : 0);
-    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, kRedBlocks, 1, only_on_output ? 1 : 0);
+    const dim3 g = cellmax_grid(d);
+    cellmax_kernel<1, T><<<g, kRedThreads, 0, s>>>(d, c, cv, k.dxt, k.dxz, f, only_on_output ? 1 : 0);
+    cellmax_finish<<<1, kRedThreads, 0, s>>>(f.red, f.st, (int)(g.x * g.y), 1, only_on_output ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
 template <typename T>

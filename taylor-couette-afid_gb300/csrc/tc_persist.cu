@@ -77,7 +77,7 @@ struct CellItem {
 __device__ __forceinline__ CellItem cell_item(long long local, size_t P) {
     const int tiles = (int)((P + kPersistThreads - 1) / kPersistThreads);
     CellItem c;
-    c.outer = (int)(local / tiles);
+    c.outer = (int)((unsigned)local / (unsigned)tiles);
     c.flat = (local - (long long)c.outer * tiles) * kPersistThreads + threadIdx.x;
     return c;
 }
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
             const CellItem ci = cell_item(item - table(PH_CFL)[m], I.d.P);
             double v = 0.0;
             if (ci.flat < (long long)I.d.P) {
-                const int j = (int)(ci.flat / I.d.nt), i = (int)(ci.flat - (long long)j * I.d.nt);
+                const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
                 v = cfl_cell(I.d, I.c, I.cv, I.k.dxt, I.k.dxz, I.f, i, j, ci.outer);
             }
             for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         if (I.f.st->halt) continue;
         const CellItem ci = cell_item(item - table(PH_MOM)[m], I.d.P);
         if (ci.flat < (long long)I.d.P) {
-            const int j = (int)(ci.flat / I.d.nt), i = (int)(ci.flat - (long long)j * I.d.nt);
+            const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
             if (MomMarch<T>::value) {
                 const int k0 = ci.outer * kMomChunk;
                 momentum_column(I.d, I.cv, I.ma[sub], i, j, k0, min(k0 + kMomChunk, I.d.nr));
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         if (I.f.st->halt) continue;
         const CellItem ci = cell_item(item - table(PH_CORR)[m], I.d.P);
         if (ci.flat < (long long)I.d.P) {
-            const int j = (int)(ci.flat / I.d.nt), i = (int)(ci.flat - (long long)j * I.d.nt);
+            const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
             correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, ci.outer);
         }
     }
