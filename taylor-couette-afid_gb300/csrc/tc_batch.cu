@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(128) ens_zfft_kernel(const InstT<T>* inst, con
     constexpr int ZC = ZCols<T>::value;
     const int groups = (I.d.PH + ZC - 1) / ZC;
     const int kplane = local / groups, g = local - kplane * groups;
-    zfft_tile(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    zfft_tile<ZC>(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
 int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }

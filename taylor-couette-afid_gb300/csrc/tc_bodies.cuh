@@ -20,9 +20,15 @@ namespace {
 
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 1216;  // 8 x 152 SMs: enough resident warps to cover load latency
-// Columns (kt) per z-FFT block (8 columns measured slower for FP32: twice
-// the shared memory per block halves the resident blocks).
+// Columns (kt) per z-FFT block of the ensemble kernels (128 threads).
 template <typename T> struct ZCols { static constexpr int value = 4; };
+// Columns and threads of the single-run z-FFT block.  Measured on the
+// 512x512x128 grid: FP32 8 columns of 512 threads 0.106 ms a launch against
+// 0.157 ms for 4 columns of 128 (4 x 256: 0.137, 8 x 1024: 0.125, 16 x 512:
+// 0.153); FP64 is bound by the FP64 pipe and keeps 4 x 128 (8 columns:
+// 1.16 ms against 0.99).
+template <typename T> struct ZRun { static constexpr int cols = 4, threads = 128; };
+template <> struct ZRun<float> { static constexpr int cols = 8, threads = 512; };
 
 
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
@@ -724,12 +730,11 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
     }
 }
 
-// Complex FFT along z of kZC consecutive kt columns of one r-plane.
-template <typename T>
+// Complex FFT along z of ZC consecutive kt columns of one r-plane.
+template <int ZC, typename T>
 __device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
                           int inv, int kt0, int kplane, typename V2<T>::type* smem) {
     typedef typename V2<T>::type C2;
-    constexpr int ZC = ZCols<T>::value;
     const int nz = pl.n, PH = d.PH;
     C2* a = smem;
     C2* b = smem + (size_t)ZC * nz;

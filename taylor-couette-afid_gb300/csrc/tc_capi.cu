@@ -329,6 +329,9 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     if (!make_plan(d.M, pth) || !make_plan(d.nz, pz)) {
         int r = fail(nullptr, 2003, "FFT length does not factor into 2, 3, 5"); tc_destroy(h); return r;
     }
+    if (zfft_smem_bytes(d.nz, h->mixed) > 200 * 1024) {
+        int r = fail(nullptr, 2003, "NZM too large for one z-FFT tile in shared memory"); tc_destroy(h); return r;
+    }
     h->pd.th = pth; h->pd.z = pz; h->pf.th = pth; h->pf.z = pz;
     ce = h->mixed ? upload_plans(h, h->pf) : upload_plans(h, h->pd);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "twiddle upload"); tc_destroy(h); return r; }

@@ -152,11 +152,11 @@ __global__ void __launch_bounds__(128) div_fft_kernel(Dims d, CoefT<T> c, T dxt,
 
 // Complex FFT along z of kZC consecutive kt columns of one r-plane.
 template <typename T>
-__global__ void __launch_bounds__(128) zfft_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
+__global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
                                                    const typename V2<T>::type* tw, int inv) {
     if (f.st->halt) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    zfft_tile(d, f, pl, tw, inv, blockIdx.x * ZCols<T>::value, blockIdx.y,
+    zfft_tile<ZRun<T>::cols>(d, f, pl, tw, inv, blockIdx.x * ZRun<T>::cols, blockIdx.y,
               reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
@@ -607,17 +607,22 @@ void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Cons
     TC_LAUNCH_CHECK();
 }
 
+size_t zfft_smem_bytes(int nz, bool mixed) {
+    return mixed ? (size_t)2 * ZRun<float>::cols * nz * sizeof(float2)
+                 : (size_t)2 * ZRun<double>::cols * nz * sizeof(double2);
+}
+
 template <typename T>
 void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p, bool inv) {
-    constexpr int ZC = ZCols<T>::value;
-    size_t sm = (size_t)2 * ZC * p.z.n * sizeof(typename V2<T>::type);
+    constexpr int ZC = ZRun<T>::cols;
+    const size_t sm = zfft_smem_bytes(p.z.n, std::is_same<T, float>::value);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
     dim3 g((d.PH + ZC - 1) / ZC, d.nr);
-    zfft_kernel<T><<<g, 128, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
+    zfft_kernel<T><<<g, ZRun<T>::threads, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
 

@@ -44,6 +44,9 @@ struct PlansT {
 
 int reduction_blocks();
 int theta_rows(int M);
+// Dynamic shared memory of a single-run z-FFT block for transforms of
+// length nz (at most 200 KB are granted).
+size_t zfft_smem_bytes(int nz, bool mixed);
 
 // Step control (precision independent).
 void launch_begin_step(cudaStream_t s, const Consts& k, StepState* st, int mode, double dt, double time);

@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
                 const int local = (int)(item - table(PH_ZFFT)[m]);
                 const int groups = (I.d.PH + ZC - 1) / ZC;
                 const int kplane = local / groups, g = local - kplane * groups;
-                zfft_tile(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, smem);
+                zfft_tile<ZC>(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, smem);
             }
             __syncthreads();
         }
