@@ -28,6 +28,20 @@ namespace tcgb {
 
 namespace {
 
+// Theta-FFT blocks of the single-run path: threads, and rows R per block
+// chosen as the largest power of two (<= 32) with R * M <= kThSpan.  On the
+// 512x512x128 grid 128 threads with R * M <= 512 measured fastest (FP32
+// divergence + FFT 0.158 ms a launch; 256 threads: 0.168-0.192; 512:
+// 0.207-0.243).
+constexpr int kThThreads = 128;
+constexpr int kThSpan = 512;
+static int theta_rows_run(int M) {
+    int R = 1;
+    while (R < 32 && (R * 2) * M <= kThSpan) R *= 2;
+    return R;
+}
+
+
 // --------------------------------------------------------------------------
 // Step control
 // --------------------------------------------------------------------------
@@ -141,7 +155,7 @@ __global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, FieldsT<T> f,
 // --------------------------------------------------------------------------
 
 template <bool FROM_PHI, int R, typename T>
-__global__ void __launch_bounds__(128) div_fft_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, FFTPlan pl,
+__global__ void __launch_bounds__(kThThreads) div_fft_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, FFTPlan pl,
                                                       const typename V2<T>::type* tw,
                                                       const typename V2<T>::type* twr, double fft_norm, int sub) {
     if (f.st->halt) return;
@@ -194,7 +208,7 @@ __global__ void pfactor_kernel(Dims d, Coef c, double* fl, double* fdi) {
 
 // Inverse real FFT along theta: spec rows -> phi rows.
 template <int R, typename T>
-__global__ void __launch_bounds__(128) theta_inv_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
+__global__ void __launch_bounds__(kThThreads) theta_inv_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
                                                         const typename V2<T>::type* tw,
                                                         const typename V2<T>::type* twr) {
     if (f.st->halt) return;
@@ -592,14 +606,14 @@ static void div_fft_R(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Co
         attr = true;
     }
     long long nrows = (long long)d.nr * d.nz;
-    div_fft_kernel<FP, R, T><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(
+    div_fft_kernel<FP, R, T><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(
         d, c, (T)k.dxt, (T)k.dxz, f, p.th, p.tw_th, p.twr, k.fft_norm, sub);
 }
 
 template <typename T>
 void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                     const PlansT<T>& p, int sub, bool from_phi) {
-    int R = theta_rows(p.th.n);
+    int R = theta_rows_run(p.th.n);
 #define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR, T>(s, d, c, k, f, p, sub); \
                            else div_fft_R<false, RR, T>(s, d, c, k, f, p, sub); break;
     switch (R) { TC_DF(1) TC_DF(2) TC_DF(4) TC_DF(8) TC_DF(16) TC_DF(32) }
@@ -643,12 +657,12 @@ static void theta_inv_R(cudaStream_t s, const Dims& d, const FieldsT<T>& f, cons
         attr = true;
     }
     long long nrows = (long long)d.nr * d.nz;
-    theta_inv_kernel<R, T><<<(unsigned)((nrows + R - 1) / R), 128, sm, s>>>(d, f, p.th, p.tw_th, p.twr);
+    theta_inv_kernel<R, T><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(d, f, p.th, p.tw_th, p.twr);
 }
 
 template <typename T>
 void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
-    int R = theta_rows(p.th.n);
+    int R = theta_rows_run(p.th.n);
     switch (R) {
         case 1: theta_inv_R<1, T>(s, d, f, p); break;
         case 2: theta_inv_R<2, T>(s, d, f, p); break;
