@@ -639,6 +639,77 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
     }
 }
 
+// lu_column without the round trip of the forward-elimination results
+// through memory: the forward sweep stores y only at every kRBr-th level (the
+// checkpoints, over the rhs entries there); the back substitution recomputes
+// the y of a batch from the checkpoint below it and the right-hand sides,
+// re-read, then substitutes down through the batch.  Per level the traffic
+// drops from 20 bytes (FP32: rhs read, y write, y read, q read and write) to
+// 16 bytes and 1/16.  Used where the sweep is bound by memory (FP32); the
+// recomputation doubles the forward arithmetic, which the FP64 sweeps, bound
+// by the FP64 pipe, cannot afford.
+template <bool EXTRA, typename T>
+__device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
+                                               const T* l, const T* di, const T* u, const T* sc, T extra) {
+    const T y0 = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
+    rhs[(size_t)k0 * P] = y0;
+    T y = y0;
+    // full batches [k0 + 1 + kRBr m, k0 + kRBr (m + 1)], checkpoint at their top
+    const int nb = (nr - 1 - k0) / kRBr;
+    int k = k0 + 1;
+    for (int m = 0; m < nb; ++m, k += kRBr) {
+        T r[kRBr];
+#pragma unroll
+        for (int b = 0; b < kRBr; ++b) r[b] = rhs[(size_t)(k + b) * P];
+#pragma unroll
+        for (int b = 0; b < kRBr; ++b) y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
+        rhs[(size_t)(k + kRBr - 1) * P] = y;
+    }
+    // tail levels: every y stored
+    for (; k < nr; ++k) {
+        y = rhs[(size_t)k * P] * ld(sc + k) - ld(l + k) * y;
+        rhs[(size_t)k * P] = y;
+    }
+    // back substitution: the tail from its stored y
+    T x = y * ld(di + nr - 1);
+    q[(size_t)(nr - 1) * P] += x;
+    const int ktop = k0 + nb * kRBr;          // top level of the last full batch
+    for (k = nr - 2; k > ktop; --k) {
+        x = (rhs[(size_t)k * P] - ld(u + k) * x) * ld(di + k);
+        q[(size_t)k * P] += x;
+    }
+    // full batches from the top: recompute y from the checkpoint below
+    for (int m = nb - 1; m >= 0; --m) {
+        const int kb = k0 + 1 + m * kRBr;     // lowest level of the batch
+        T yb[kRBr], v[kRBr];
+        T yc = rhs[(size_t)(kb - 1) * P];     // checkpoint (or y at k0)
+#pragma unroll
+        for (int b = 0; b < kRBr - 1; ++b) yb[b] = rhs[(size_t)(kb + b) * P];
+        yb[kRBr - 1] = rhs[(size_t)(kb + kRBr - 1) * P];
+#pragma unroll
+        for (int b = 0; b < kRBr; ++b) v[b] = q[(size_t)(kb + b) * P];
+#pragma unroll
+        for (int b = 0; b < kRBr - 1; ++b) {
+            yc = yb[b] * ld(sc + kb + b) - ld(l + kb + b) * yc;
+            yb[b] = yc;
+        }
+        // yb[kRBr - 1] is the stored checkpoint y of the batch's top level
+        const bool top_of_column = kb + kRBr - 1 == nr - 1;
+#pragma unroll
+        for (int b = kRBr - 1; b >= 0; --b) {
+            const int kk = kb + b;
+            if (b == kRBr - 1 && top_of_column) continue;   // substituted above
+            x = (yb[b] - ld(u + kk) * x) * ld(di + kk);
+            q[(size_t)kk * P] = v[b] + x;
+        }
+    }
+    // the first level (below every batch), unless it is also the last
+    if (k0 < nr - 1) {
+        x = (y0 - ld(u + k0) * x) * ld(di + k0);
+        q[(size_t)k0 * P] += x;
+    }
+}
+
 // SolveImpEqnUpdate_QT.F90:65-78 (comp 0), _QR.F90:136-150 (comp 1, faces
 // 1..nr-1), _QZ.F90:214-224 (comp 2) for the column `col`.  The three
 // components are independent, so each gets its own thread.
@@ -648,6 +719,18 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
     const size_t P = (size_t)d.P;
     const int v = (f.icyl && f.icyl[col] == 0) ? 1 : 0;
     const MomFactorsT<T>& F = f.F;
+    if constexpr (std::is_same<T, float>::value) {
+        if (comp == 0)
+            lu_column_ckpt<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v),
+                                 F.u(sub, 0, v), F.scale(sub, 0), *F.extra(sub));
+        else if (comp == 1)
+            lu_column_ckpt<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0),
+                                  F.u(sub, 1, 0), F.scale(sub, 1), (T)0);
+        else
+            lu_column_ckpt<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v),
+                                  F.u(sub, 2, v), F.scale(sub, 2), (T)0);
+        return;
+    }
     if (comp == 0)
         lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
                         F.scale(sub, 0), *F.extra(sub));

@@ -68,7 +68,11 @@ def test_mixed_routines(gpu_lib, oracle):
     dict(),
     dict(nthm=64, nzm=48, nrm=96, istr=6, str=20.0, sizepert=0.1, omegapert=0.5, romeg=0.1, ren=5000.0,
          dtmin=1e-5, dtmax=1e-3, limitCFL=1.2),
-], ids=["C1-64cubed", "cheb-variable-dt"])
+    # radial sweeps whose levels above the first fill whole 16-level batches
+    # (17 cells: theta and z components; 18: the radial faces)
+    dict(nthm=32, nzm=32, nrm=17),
+    dict(nthm=32, nzm=32, nrm=18),
+], ids=["C1-64cubed", "cheb-variable-dt", "nr17", "nr18"])
 def test_mixed_twenty_steps_vs_fp64(gpu_lib, oracle, case):
     bou = make_bou(**case)
     g, o = pair(oracle, bou)
