@@ -640,30 +640,36 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
 }
 
 // lu_column without the round trip of the forward-elimination results
-// through memory: the forward sweep stores y only at every kRBr-th level (the
+// through memory: the forward sweep stores y only at every kCkpt-th level (the
 // checkpoints, over the rhs entries there); the back substitution recomputes
 // the y of a batch from the checkpoint below it and the right-hand sides,
 // re-read, then substitutes down through the batch.  Per level the traffic
 // drops from 20 bytes (FP32: rhs read, y write, y read, q read and write) to
-// 16 bytes and 1/16.  Used where the sweep is bound by memory (FP32); the
+// 16 bytes and 1/kCkpt.  Used where the sweep is bound by memory (FP32); the
 // recomputation doubles the forward arithmetic, which the FP64 sweeps, bound
 // by the FP64 pipe, cannot afford.
+// Levels per checkpointed batch.  On the 512x512x128 grid (radial solve of
+// the three components, one launch): batches of 8 with 8 resident blocks
+// per SM 0.325 ms, of 16 with 6 blocks 0.372 ms, the plain sweep with 6
+// blocks 0.380 ms.
+constexpr int kCkpt = 8;
+
 template <bool EXTRA, typename T>
 __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
                                                const T* l, const T* di, const T* u, const T* sc, T extra) {
     const T y0 = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
     rhs[(size_t)k0 * P] = y0;
     T y = y0;
-    // full batches [k0 + 1 + kRBr m, k0 + kRBr (m + 1)], checkpoint at their top
-    const int nb = (nr - 1 - k0) / kRBr;
+    // full batches [k0 + 1 + kCkpt m, k0 + kCkpt (m + 1)], checkpoint at their top
+    const int nb = (nr - 1 - k0) / kCkpt;
     int k = k0 + 1;
-    for (int m = 0; m < nb; ++m, k += kRBr) {
-        T r[kRBr];
+    for (int m = 0; m < nb; ++m, k += kCkpt) {
+        T r[kCkpt];
 #pragma unroll
-        for (int b = 0; b < kRBr; ++b) r[b] = rhs[(size_t)(k + b) * P];
+        for (int b = 0; b < kCkpt; ++b) r[b] = rhs[(size_t)(k + b) * P];
 #pragma unroll
-        for (int b = 0; b < kRBr; ++b) y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
-        rhs[(size_t)(k + kRBr - 1) * P] = y;
+        for (int b = 0; b < kCkpt; ++b) y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
+        rhs[(size_t)(k + kCkpt - 1) * P] = y;
     }
     // tail levels: every y stored
     for (; k < nr; ++k) {
@@ -673,32 +679,32 @@ __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restric
     // back substitution: the tail from its stored y
     T x = y * ld(di + nr - 1);
     q[(size_t)(nr - 1) * P] += x;
-    const int ktop = k0 + nb * kRBr;          // top level of the last full batch
+    const int ktop = k0 + nb * kCkpt;          // top level of the last full batch
     for (k = nr - 2; k > ktop; --k) {
         x = (rhs[(size_t)k * P] - ld(u + k) * x) * ld(di + k);
         q[(size_t)k * P] += x;
     }
     // full batches from the top: recompute y from the checkpoint below
     for (int m = nb - 1; m >= 0; --m) {
-        const int kb = k0 + 1 + m * kRBr;     // lowest level of the batch
-        T yb[kRBr], v[kRBr];
+        const int kb = k0 + 1 + m * kCkpt;     // lowest level of the batch
+        T yb[kCkpt], v[kCkpt];
         T yc = rhs[(size_t)(kb - 1) * P];     // checkpoint (or y at k0)
 #pragma unroll
-        for (int b = 0; b < kRBr - 1; ++b) yb[b] = rhs[(size_t)(kb + b) * P];
-        yb[kRBr - 1] = rhs[(size_t)(kb + kRBr - 1) * P];
+        for (int b = 0; b < kCkpt - 1; ++b) yb[b] = rhs[(size_t)(kb + b) * P];
+        yb[kCkpt - 1] = rhs[(size_t)(kb + kCkpt - 1) * P];
 #pragma unroll
-        for (int b = 0; b < kRBr; ++b) v[b] = q[(size_t)(kb + b) * P];
+        for (int b = 0; b < kCkpt; ++b) v[b] = q[(size_t)(kb + b) * P];
 #pragma unroll
-        for (int b = 0; b < kRBr - 1; ++b) {
+        for (int b = 0; b < kCkpt - 1; ++b) {
             yc = yb[b] * ld(sc + kb + b) - ld(l + kb + b) * yc;
             yb[b] = yc;
         }
-        // yb[kRBr - 1] is the stored checkpoint y of the batch's top level
-        const bool top_of_column = kb + kRBr - 1 == nr - 1;
+        // yb[kCkpt - 1] is the stored checkpoint y of the batch's top level
+        const bool top_of_column = kb + kCkpt - 1 == nr - 1;
 #pragma unroll
-        for (int b = kRBr - 1; b >= 0; --b) {
+        for (int b = kCkpt - 1; b >= 0; --b) {
             const int kk = kb + b;
-            if (b == kRBr - 1 && top_of_column) continue;   // substituted above
+            if (b == kCkpt - 1 && top_of_column) continue;   // substituted above
             x = (yb[b] - ld(u + kk) * x) * ld(di + kk);
             q[(size_t)kk * P] = v[b] + x;
         }

@@ -141,8 +141,16 @@ __global__ void __launch_bounds__(128) momentum_march_kernel(Dims d, CoefT<T> c,
 // Radial implicit solves, one thread per (z, theta) column and component
 // --------------------------------------------------------------------------
 
+// Resident blocks per SM the radial kernel is compiled for (registers
+// capped to fit): the sweeps are bound by load latency, and more warps beat
+// the few values a thread would otherwise keep in flight (FP32 with 8-level
+// checkpoints: 8 blocks, 64 registers, 0.325 ms against 0.372 ms with 16
+// levels and 6 blocks; FP64: 6 blocks, 0.942 ms against 0.961 ms unbounded).
+template <typename T> struct RadialBlocks { static constexpr int value = 6; };
+template <> struct RadialBlocks<float> { static constexpr int value = 8; };
+
 template <typename T>
-__global__ void __launch_bounds__(128) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
+__global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= d.P) return;

@@ -68,7 +68,7 @@ def test_mixed_routines(gpu_lib, oracle):
     dict(),
     dict(nthm=64, nzm=48, nrm=96, istr=6, str=20.0, sizepert=0.1, omegapert=0.5, romeg=0.1, ren=5000.0,
          dtmin=1e-5, dtmax=1e-3, limitCFL=1.2),
-    # radial sweeps whose levels above the first fill whole 16-level batches
+    # radial sweeps whose levels above the first fill whole checkpoint batches
     # (17 cells: theta and z components; 18: the radial faces)
     dict(nthm=32, nzm=32, nrm=17),
     dict(nthm=32, nzm=32, nrm=18),

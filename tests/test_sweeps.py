@@ -3,7 +3,7 @@ csrc/tc_bodies.cuh) against the plain LU sweep (lu_column), compiled for the
 host from the same source text: same solution to 1e-12 (FP64 instantiation)
 for every column length from 2 to 399 levels and both first levels (0 for
 the theta and z components, 1 for the radial faces), which covers empty and
-partial tails and whole 16-level batches."""
+partial tails and whole batches (of 8 and 16 levels)."""
 import os
 import shutil
 import subprocess
@@ -23,6 +23,7 @@ HARNESS = r'''
 template <typename T> T ld(const T* p) { return *p; }
 constexpr int kRB = 8;
 constexpr int kRBr = 16;
+constexpr int kCkpt = CKPT;
 %s
 int main() {
     int bad = 0;
@@ -54,7 +55,8 @@ def _extract(src, start, end):
     return src[a:src.index(end, a)]
 
 
-def test_checkpointed_sweep_matches_plain_sweep(tmp_path):
+@pytest.mark.parametrize("batch", [8, 16])
+def test_checkpointed_sweep_matches_plain_sweep(tmp_path, batch):
     if shutil.which("g++") is None:
         pytest.skip("no host C++ compiler")
     src = open(BODIES).read()
@@ -65,6 +67,6 @@ def test_checkpointed_sweep_matches_plain_sweep(tmp_path):
     cpp = tmp_path / "sweeps.cpp"
     cpp.write_text(HARNESS % (plain + ckpt))
     exe = tmp_path / "sweeps"
-    subprocess.run(["g++", "-O1", "-std=c++17", str(cpp), "-o", str(exe)], check=True)
+    subprocess.run(["g++", "-O1", "-std=c++17", f"-DCKPT={batch}", str(cpp), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
