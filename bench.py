@@ -95,6 +95,13 @@ def algorithmic_bytes(cls: str, nt: int, nz: int, nr: int, rk_substep_mix: float
 # Compulsory HBM bytes of one ideally fused RK3 step per cell: q (3 fields)
 # read and written, pr read and written and one spectral round trip of phi per
 # substep, plus the RK memory ru (read in substeps 2-3, written in 1-2).
+# The FP64 fused momentum kernel measured by ncu on the 512x512x128 grid, one
+# RK3 step (profiles/momentum_kernel_fp64_P2.md): DRAM bytes per cell of a
+# launch averaged over the three substeps (79.6, 103.4, 103.4), and per cell
+# its FP64 instructions (54.85 DADD + 32.93 DMUL + 44.94 DFMA) and FLOPs.
+# Per-cell figures do not depend on the grid size.
+MOMENTUM_FP64_NCU = {"dram_bytes_per_cell": 95.47, "fp64_inst_per_cell": 132.72, "fp64_flops_per_cell": 177.66}
+
 STEP_BYTES = {"fp64": 3 * (6 + 2 + 2) * 8 + (2 * 3 + 2 * 3) * 8,
               "mixed": 3 * (6 * 4 + 2 * 8 + 2 * 4) + 12 * 4}
 
@@ -598,13 +605,22 @@ def main():
     bytes_launch = algorithmic_bytes(dom, nt, nz, nr, rk_mix)
     achieved = bytes_launch / (dom_ms / dom_n * 1e-3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            tj = json.load(f)
-        ent = tj.get(args.workload, {}).get(dom)
-        if ent:
-            traffic = ent.get("bytes_per_launch")
+    pipe = None
+    if dom == "momentum":
+        # DRAM bytes of a launch from the ncu capture, scaled by the cells;
+        # the kernel's real limit is the FP64 pipe: its FP64 instruction rate
+        # against the probe's (one DFMA = 2 FLOPs per instruction)
+        traffic = MOMENTUM_FP64_NCU["dram_bytes_per_cell"] * cells
+        t_launch = dom_ms / dom_n * 1e-3
+        inst_rate = MOMENTUM_FP64_NCU["fp64_inst_per_cell"] * cells / t_launch
+        peak_inst = fp64_peak * 1e12 / 2.0
+        pipe = {"bound": "fp64 pipe", "unit": "FP64 instructions/s", "achieved": inst_rate, "peak": peak_inst,
+                "frac": inst_rate / peak_inst,
+                "fp64_tflops": MOMENTUM_FP64_NCU["fp64_flops_per_cell"] * cells / t_launch / 1e12,
+                "peak_tflops": fp64_peak,
+                "per_cell": {"fp64_instructions": MOMENTUM_FP64_NCU["fp64_inst_per_cell"],
+                             "fp64_flops": MOMENTUM_FP64_NCU["fp64_flops_per_cell"]},
+                "note": "per-cell FP64 instruction counts from ncu; peak = the FP64 FMA probe of this run"}
     total_ms = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}
 
@@ -628,7 +644,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": achieved / peak_gbs, "peak_kind": f"{peak_kind} hbm_gbs",
                      "traffic": traffic, "algorithmic_bytes_per_launch": bytes_launch,
-                     "ms_per_launch": dom_ms / dom_n, "launches": dom_n},
+                     "ms_per_launch": dom_ms / dom_n, "launches": dom_n,
+                     "traffic_note": "ncu DRAM bytes per cell on the 512x512x128 grid x cells" if traffic else None,
+                     "compute": pipe},
         "step_roofline": {
             "bytes_per_cell_step": STEP_BYTES["fp64"], "achieved": value * 1e6 * STEP_BYTES["fp64"] / 1e9,
             "peak": peak_gbs, "unit": "GB/s", "frac": value * 1e6 * STEP_BYTES["fp64"] / 1e9 / peak_gbs,
