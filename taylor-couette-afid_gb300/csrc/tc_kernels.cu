@@ -183,7 +183,10 @@ __global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) ptri_kernel(Dims d, Coef c, FieldsT<T> f, double2* ws) {
+// Compiled for 8 resident blocks per SM (64 registers, a few spilled): on
+// the 512x512x128 grid 0.217 ms a launch (FP32 spectrum) and 0.234 ms (FP64)
+// against 0.246 and 0.245 ms with 122 and 96 registers.
+__global__ void __launch_bounds__(128, 8) ptri_kernel(Dims d, Coef c, FieldsT<T> f, double2* ws) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)d.nz * d.PH) return;
