@@ -158,7 +158,13 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, cons
         if (ch == 0) {
             corrd[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
             corrd[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
-            if (row == 0) corrd[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
+            if (row == 0) {
+                corrd[(s * 3 + 2) * (nr + 1)] = k.alm[s] * dt * k.dxz;
+                // factors of the momentum right-hand side (TimeMarcher.F90 gam, rom, alre times dt)
+                corrd[9 * (nr + 1) + s * 3 + 0] = k.gam[s] * dt;
+                corrd[9 * (nr + 1) + s * 3 + 1] = k.rom[s] * dt;
+                corrd[9 * (nr + 1) + s * 3 + 2] = k.alre[s] * dt;
+            }
         }
     }
     __syncthreads();
@@ -203,7 +209,7 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, cons
     // phase 4 (mixed path): round the factors into the FP32 copies
     if (!std::is_same<T, double>::value) {
         __syncthreads();
-        const int nF = (int)MomFactorsT<T>::count(F.stride), nC = 9 * (nr + 1);
+        const int nF = (int)MomFactorsT<T>::count(F.stride), nC = (int)kCorrCount(nr + 1);
         for (int t = threadIdx.x; t < nF; t += blockDim.x) F.base[t] = (T)Fd.base[t];
         for (int t = threadIdx.x; t < nC; t += blockDim.x) corr[t] = (T)corrd[t];
     }
@@ -245,6 +251,8 @@ struct MomArgs {
     T al, ga, ro, alre, dxt_al, dxz_al;
     T udxz, udxzq, q_romeg, virotint, virotext;
     T ac1j_fs0, am1j_fs0, ap1j_fs1, ac1j_fs1, ac3j_fs0, am3j_fs0, ap3j_fs1, ac3j_fs1;
+    const T* cf;            // this substep's pressure-gradient products dt al metric (per component, level)
+    const T* mr;            // gam dt, rom dt, alre dt of this substep
     int use_ru;
 };
 
@@ -352,7 +360,10 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
         if (k >= 1) hr = a.h_r[o];
         hz = a.h_z[o];
     }
-    const T dt = step_dt<T>(a.st), ga = a.ga, ro = a.ro, alre = a.alre;
+    // gam dt, rom dt, alre dt; the pressure terms use the per-level dt al
+    // metric products of the correction (a.cf), so no factor dt remains
+    const T gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
+    const int nrr = nr + 1;
     const T one = (T)1.0;
     const T fic = a.icyl ? (T)a.icyl[(size_t)j * d.nt + i] : one, foc = one;
     const T* pr = a.pr + o;
@@ -373,18 +384,16 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
         } else {
             d33 = ld(qt + P) * ld(c.ap1j + k) + ld(qt) * ld(c.ac1j + k) + ld(qt - P) * ld(c.am1j + k);
         }
-        T dpx11 = (p_c - ld(pr + S.dim)) * a.dxt_al * ld(c.usrm + k);
         T old = a.use_ru ? a.ru1[o] : (T)0;
-        a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
+        a.rhs_t[o] = gadt * ht + rodt * old + alredt * d33 - (p_c - ld(pr + S.dim)) * ld(a.cf + k);
         a.ru1[o] = ht;
     }
     // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
     if (k >= 1) {
         T d33 = ld(qr + P) * ld(c.ap2je + k) + ld(qr) * ld(c.ac2je + k) + ld(qr - P) * ld(c.am2je + k);
-        T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
-        T dpx22 = (p_c - ld(pr - P)) * udx2;
+        T dpx22 = (p_c - ld(pr - P)) * ld(a.cf + nrr + k);
         T old = a.use_ru ? a.ru2[o] : (T)0;
-        a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
+        a.rhs_r[o] = gadt * hr + rodt * old + alredt * d33 - dpx22;
         a.ru2[o] = hr;
     }
     // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
@@ -404,11 +413,11 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
         } else {
             d33 = ld(qz + P) * ld(c.ap3j + k) + ld(qz) * ld(c.ac3j + k) + ld(qz - P) * ld(c.am3j + k);
         }
-        T dpx33 = (p_c - ld(pr + S.djm)) * a.dxz_al;
+        T dpx33 = (p_c - ld(pr + S.djm)) * ld(a.cf + 2 * nrr);
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
         T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
-        a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
+        a.rhs_z[o] = gadt * hz + rodt * old + alredt * d33 - dpx33;
         a.ru3[o] = hz;
     }
 }
@@ -441,7 +450,10 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
     const int djm = j == 0 ? (nz - 1) * nt : -nt, djp = j == nz - 1 ? -(nz - 1) * nt : nt;
     const size_t col = (size_t)j * nt + i;
     const T one = (T)1.0, two = (T)2.0;
-    const T dt = step_dt<T>(a.st), ga = a.ga, ro = a.ro, alre = a.alre;
+    // gam dt, rom dt, alre dt; the pressure terms use the per-level dt al
+    // metric products of the correction (a.cf), so no factor dt remains
+    const T gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
+    const int nrr = nr + 1;
     const T fic = a.icyl ? (T)a.icyl[col] : one, foc = one;
     const T udxz = a.udxz, udxzq = a.udxzq;
 
@@ -546,18 +558,17 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
             } else {
                 d33 = qt_p * ld(c.ap1j + k) + qt_c * ld(c.ac1j + k) + qt_m * ld(c.am1j + k);
             }
-            const T dpx11 = (p_c - p_im) * a.dxt_al * ld(c.usrm + k);
+            const T dpx11 = (p_c - p_im) * ld(a.cf + k);
             const T old = a.use_ru ? a.ru1[o] : (T)0;
-            a.rhs_t[o] = (ga * ht + ro * old + alre * d33 - dpx11) * dt;
+            a.rhs_t[o] = gadt * ht + rodt * old + alredt * d33 - dpx11;
             a.ru1[o] = ht;
         }
         // ---- ImplicitAndUpdateQR, faces 1..nr-1
         if (k >= 1) {
             const T d33 = qr_p * ld(c.ap2je + k) + qr_c * ld(c.ac2je + k) + qr_m * ld(c.am2je + k);
-            const T udx2 = ld(c.rc + k) * a.al * ld(c.udx2c + k);
-            const T dpx22 = (p_c - pr_m) * udx2;
+            const T dpx22 = (p_c - pr_m) * ld(a.cf + nrr + k);
             const T old = a.use_ru ? a.ru2[o] : (T)0;
-            a.rhs_r[o] = (ga * hr + ro * old + alre * d33 - dpx22) * dt;
+            a.rhs_r[o] = gadt * hr + rodt * old + alredt * d33 - dpx22;
             a.ru2[o] = hr;
         }
         // ---- ImplicitAndUpdateQZ
@@ -575,10 +586,10 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
             } else {
                 d33 = qz_p * ld(c.ap3j + k) + qz_c * ld(c.ac3j + k) + qz_m * ld(c.am3j + k);
             }
-            const T dpx33 = (p_c - p_jm) * a.dxz_al;
+            const T dpx33 = (p_c - p_jm) * ld(a.cf + 2 * nrr);
             // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
             const T old = top ? hz : (a.use_ru ? a.ru3[o] : (T)0);
-            a.rhs_z[o] = (ga * hz + ro * old + alre * d33 - dpx33) * dt;
+            a.rhs_z[o] = gadt * hz + rodt * old + alredt * d33 - dpx33;
             a.ru3[o] = hz;
         }
         // march: level k becomes the lower neighbour of level k+1
@@ -1146,6 +1157,9 @@ inline MomArgs<T> make_mom_args(const Consts& k, const FieldsT<T>& f, int sub) {
     a.ac1j_fs0 = (T)k.ac1j_fs0; a.am1j_fs0 = (T)k.am1j_fs0; a.ap1j_fs1 = (T)k.ap1j_fs1; a.ac1j_fs1 = (T)k.ac1j_fs1;
     a.ac3j_fs0 = (T)k.ac3j_fs0; a.am3j_fs0 = (T)k.am3j_fs0; a.ap3j_fs1 = (T)k.ap3j_fs1; a.ac3j_fs1 = (T)k.ac3j_fs1;
     a.use_ru = k.rom[sub] != 0.0;
+    const int nrr = f.F.stride;
+    a.cf = f.corr + (size_t)sub * 3 * nrr;
+    a.mr = f.corr + (size_t)9 * nrr + sub * 3;
     return a;
 }
 

@@ -143,7 +143,7 @@ cudaError_t alloc_fields(tc_handle* h, FieldsT<T>& f) {
     AL(f.spec, (size_t)d.PS * nr);
     AL(f.F.base, MomFactorsT<T>::count(nrr));
     f.F.stride = nrr;
-    AL(f.corr, (size_t)9 * nrr);
+    AL(f.corr, kCorrCount(nrr));
     AL(f.scal, 8);
     AL(f.red, (size_t)6 * reduction_blocks());
     if (std::is_same<T, double>::value) f.prf = reinterpret_cast<T*>(f.pr);
@@ -156,7 +156,7 @@ cudaError_t alloc_fields(tc_handle* h, FieldsT<T>& f) {
     } else {
         AL(f.Fd.base, MomFactorsT<double>::count(nrr));
         f.Fd.stride = nrr;
-        AL(f.corrd, (size_t)9 * nrr);
+        AL(f.corrd, kCorrCount(nrr));
         AL(f.ws, (size_t)d.PS * nr);
     }
 #undef AL

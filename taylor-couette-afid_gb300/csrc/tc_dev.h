@@ -109,6 +109,14 @@ struct StepState {
     float dt_f, beta_f, vinner_f, pad_f;
 };
 
+// Per-step coefficients of one step (factors kernel), per substep s:
+// [ (s*3 + c)*(nr+1) + k ]  dt al(s) times the pressure-gradient metric of
+//                            component c at level k (CorrectVelocity.F90:
+//                            325-330; the momentum right-hand sides use the
+//                            same products for the pressure of the step),
+// [ 9*(nr+1) + s*3 + 0..2 ] gam(s) dt, rom(s) dt, alre(s) dt.
+__host__ __device__ inline size_t kCorrCount(int nrr) { return (size_t)9 * nrr + 9; }
+
 // Factors of the row-scaled momentum matrices of one step: for each substep
 // s (3), component c (0 = qt, 1 = qr, 2 = qz) and slip variant v (0 = no
 // slip at the inner wall, 1 = free slip), arrays of length nr+1:
