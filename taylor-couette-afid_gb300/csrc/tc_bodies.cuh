@@ -274,14 +274,15 @@ __device__ T explicit_qt(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     T h11 = ((t_ip + t_c) * (t_ip + t_c) - (t_c + t_im) * (t_c + t_im)) * udxt;
     const T rp2 = r_p + r_pim, rc2 = r_c + r_im;
     T h12d = (rp2 * (t_kp + t_c) - rc2 * (t_c + t_km)) * ld(c.q_udx2rm + k);
-    T h12n = t_c * ld(c.q_usrm + k) * (rp2 * usrcp + rc2 * usrc);
+    const T qrs = rp2 * usrcp + rc2 * usrc;          // shared by h12n and the Coriolis term
+    T h12n = t_c * ld(c.q_usrm + k) * qrs;
     T h13 = ((z_jp + z_jpim) * (t_jp + t_c) - (z_c + z_im) * (t_c + t_jm)) * A.udxz;
     T d11qt = (t_ip - two * t_c + t_im) * udxtq;
     T d22qt = (t_jp - two * t_c + t_jm) * A.udxzq;
     T qre = r_p * usrcp + r_c * usrc;
     T qrw = r_pim * usrcp + r_im * usrc;
     T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
-    T coriol = -(rc2 * usrc + rp2 * usrcp) * A.q_romeg;
+    T coriol = -qrs * A.q_romeg;
     return -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
 }
 
@@ -300,15 +301,17 @@ __device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
     const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp), usrcm = ld(c.usrc + km);
     const T two = (T)2.0;
-    T a = (t_ip + t_mip + t_c + t_m) * (T)0.25;
+    // theta-velocity sums of the two faces, shared by h11n, h21, d11qre and Coriolis
+    const T sa = t_ip + t_mip, sb = t_c + t_m, s4 = sa + sb;
+    T a = s4 * (T)0.25;
     T h11n = a * a;
-    T h21 = ((t_ip + t_mip) * (r_ip + r_c) - (t_c + t_m) * (r_c + r_im)) * udxt;
+    T h21 = (sa * (r_ip + r_c) - sb * (r_c + r_im)) * udxt;
     T h22 = ((r_p * usrcp + r_c * usrc) * (r_p + r_c) - (r_c * usrc + r_m * usrcm) * (r_c + r_m)) * ld(c.q_udx2c + k);
     T h23 = ((z_jp + z_mjp) * (r_jp + r_c) - (z_c + z_m) * (r_c + r_jm)) * A.udxz;
-    T d11qre = -((t_ip + t_mip) - (t_c + t_m)) * ld(c.udx1vis2 + k);
+    T d11qre = -(sa - sb) * ld(c.udx1vis2 + k);
     T d11qr = (r_ip - two * r_c + r_im) * udxtq;
     T d22qr = (r_jp - two * r_c + r_jm) * A.udxzq;
-    T coriol = (t_c + t_ip + t_m + t_mip) * ld(c.q_rc_romeg + k);
+    T coriol = s4 * ld(c.q_rc_romeg + k);
     return -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
 }
 
@@ -326,7 +329,8 @@ __device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     T r_c = ld(qr), r_jm = ld(qr + S.djm);
     const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
     const T two = (T)2.0;
-    T h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (t_c + t_jm) * (z_c + z_im)) * udxt;
+    // second product written as in explicit_qt's h13, so the two share it
+    T h31 = ((t_ip + t_jmip) * (z_ip + z_c) - (z_c + z_im) * (t_c + t_jm)) * udxt;
     T h32 = ((r_p + r_pjm) * (z_kp + z_c) - (r_c + r_jm) * (z_c + z_km)) * ld(c.q_udx2rm + k);
     T h33 = ((z_jp + z_c) * (z_jp + z_c) - (z_c + z_jm) * (z_c + z_jm)) * A.udxz;
     T dqz1 = (z_im - two * z_c + z_ip) * udxtq;
@@ -477,6 +481,9 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
     }
     for (int k = k0; k < k1; ++k, o += P) {
         const bool top = k == nr - 1;
+        // lower-face fluxes of this level: the theta-r product of h12d is also
+        // the second product of h21, the r-z product of h32 that of h23
+        const T U12lo = U12, Uzlo = Uz;
         const int kp = k + 1;
         // fresh loads of level k (neighbours) and k+1 (column)
         const T qt_ip = ld(a.qt + o + dip), qt_im = ld(a.qt + o + dim);
@@ -490,6 +497,8 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
         const T p_c = ld(a.pr + o), p_im = ld(a.pr + o + dim), p_jm = ld(a.pr + o + djm);
 
         const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
+        // (qz + qz(i-1)) (qt + qt(j-1)): the second product of h13 and of h31
+        const T tz_sw = (qz_c + qz_im) * (qt_c + qt_jm);
         // ---- ExplicitTermsQT (momentum_cell / explicit_qt)
         T ht;
         {
@@ -499,14 +508,15 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
             const T up = rp2 * (qt_p + qt_c);
             const T h12d = (up - U12) * ld(c.q_udx2rm + k);
             U12 = up;
-            const T h12n = qt_c * ld(c.q_usrm + k) * (rp2 * usrcp + rc2 * usrc);
-            const T h13 = ((qz_jp + qz_jpim) * (qt_jp + qt_c) - (qz_c + qz_im) * (qt_c + qt_jm)) * udxz;
+            const T qrs = rp2 * usrcp + rc2 * usrc;      // shared by h12n and the Coriolis term
+            const T h12n = qt_c * ld(c.q_usrm + k) * qrs;
+            const T h13 = ((qz_jp + qz_jpim) * (qt_jp + qt_c) - tz_sw) * udxz;
             const T d11qt = (qt_ip - two * qt_c + qt_im) * udxtq;
             const T d22qt = (qt_jp - two * qt_c + qt_jm) * udxzq;
             const T qre = qr_p * usrcp + qr_c * usrc;
             const T qrw = qr_pim * usrcp + qr_im * usrc;
             const T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
-            const T coriol = -(rc2 * usrc + rp2 * usrcp) * a.q_romeg;
+            const T coriol = -qrs * a.q_romeg;
             ht = -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
         }
         // ---- ExplicitTermsQR at face k (1 <= k)
@@ -516,15 +526,16 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
             if (k >= 1) {
                 const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
                 const T qr_im_ = qr_im;
-                const T aa = (qt_ip + qt_mip + qt_c + qt_m) * (T)0.25;
+                const T sa = qt_ip + qt_mip, sb = qt_c + qt_m, s4 = sa + sb;
+                const T aa = s4 * (T)0.25;
                 const T h11n = aa * aa;
-                const T h21 = ((qt_ip + qt_mip) * (qr_ip + qr_c) - (qt_c + qt_m) * (qr_c + qr_im_)) * udxt;
+                const T h21 = (sa * (qr_ip + qr_c) - U12lo) * udxt;
                 const T h22 = (rup - Gup) * ld(c.q_udx2c + k);
-                const T h23 = ((qz_jp + qz_mjp) * (qr_jp + qr_c) - (qz_c + qz_m) * (qr_c + qr_jm)) * udxz;
-                const T d11qre = -((qt_ip + qt_mip) - (qt_c + qt_m)) * ld(c.udx1vis2 + k);
+                const T h23 = ((qz_jp + qz_mjp) * (qr_jp + qr_c) - Uzlo) * udxz;
+                const T d11qre = -(sa - sb) * ld(c.udx1vis2 + k);
                 const T d11qr = (qr_ip - two * qr_c + qr_im_) * udxtq;
                 const T d22qr = (qr_jp - two * qr_c + qr_jm) * udxzq;
-                const T coriol = (qt_c + qt_ip + qt_m + qt_mip) * ld(c.q_rc_romeg + k);
+                const T coriol = s4 * ld(c.q_rc_romeg + k);
                 hr = -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
             }
             Gup = rup;
@@ -533,7 +544,7 @@ __device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c
         T hz;
         {
             const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-            const T h31 = ((qt_ip + qt_jmip) * (qz_ip + qz_c) - (qt_c + qt_jm) * (qz_c + qz_im)) * udxt;
+            const T h31 = ((qt_ip + qt_jmip) * (qz_ip + qz_c) - tz_sw) * udxt;
             const T upz = (qr_p + qr_pjm) * (qz_p + qz_c);
             const T h32 = (upz - Uz) * ld(c.q_udx2rm + k);
             Uz = upz;
