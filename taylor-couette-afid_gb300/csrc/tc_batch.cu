@@ -178,8 +178,7 @@ __global__ void __launch_bounds__(256) ens_ptri_kernel(const InstT<T>* inst, con
     if (I.f.st->halt) return;
     const long long t = (item - prefix[m]) * blockDim.x + threadIdx.x;
     if (t >= (long long)I.d.nz * I.d.PH) return;
-    double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(I.f.spec) : I.f.ws;
-    ptri_one(I.d, I.c, I.f, ws, t);
+    ptri_solve(I.d, I.c, I.f, t);
 }
 
 // row-wise FFT phases: item = R consecutive (k, j) rows

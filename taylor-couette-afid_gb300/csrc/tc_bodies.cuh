@@ -12,6 +12,7 @@
 
 #include "tc_convert.cuh"
 #include "tc_fft.cuh"
+#include "tc_ff.cuh"
 #include "tc_kernels.cuh"
 
 namespace tcgb {
@@ -869,106 +870,12 @@ __device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_f
 
 // SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
 // matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
-// right-hand side, with the precomputed LU factors, in FP64.  One thread per
-// pair of modes (kz, nzm-kz) that share a matrix.  The forward-sweep partial
-// results go to the FP64 array ws: the spectrum itself for the FP64 path, a
-// separate scratch for the mixed path, so the FP32 spectrum is rounded once.
-template <typename T>
-__device__ __forceinline__ void ptri_mode(const Dims& d, const Coef& c, const FieldsT<T>& f, double2* ws, long long t) {
-    typedef typename V2<T>::type C2;
-    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
-    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
-    const bool two = (kz != 0) && (2 * kz != d.nz);
-    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
-    const size_t o1 = (size_t)kz * PH + kt, o2 = (size_t)(two ? d.nz - kz : kz) * PH + kt;
-    C2* x1 = f.spec + o1;
-    C2* x2 = f.spec + o2;
-    double2* w1 = ws + o1;
-    double2* w2 = ws + o2;
-    const double* L = f.pf_l + t;
-    const double* DI = f.pf_dinv + t;
-    // forward sweep, planes loaded kRB at a time ahead of the recurrence
-    double2 y1 = to_d2(x1[0]), y2 = two ? to_d2(x2[0]) : make_double2(0.0, 0.0);
-    w1[0] = y1;
-    if (two) w2[0] = y2;
-    int k = 1;
-    for (; k + kRB <= nr; k += kRB) {
-        C2 b1[kRB], b2[kRB];
-        double l[kRB];
-#pragma unroll
-        for (int b = 0; b < kRB; ++b) {
-            l[b] = ld(L + (size_t)(k + b) * FS);
-            b1[b] = x1[(size_t)(k + b) * PS];
-            if (two) b2[b] = x2[(size_t)(k + b) * PS];
-        }
-#pragma unroll
-        for (int b = 0; b < kRB; ++b) {
-            const double2 v1 = to_d2(b1[b]);
-            y1 = make_double2(v1.x - l[b] * y1.x, v1.y - l[b] * y1.y);
-            w1[(size_t)(k + b) * PS] = y1;
-            if (two) {
-                const double2 v2 = to_d2(b2[b]);
-                y2 = make_double2(v2.x - l[b] * y2.x, v2.y - l[b] * y2.y);
-                w2[(size_t)(k + b) * PS] = y2;
-            }
-        }
-    }
-    for (; k < nr; ++k) {
-        const double l = ld(L + (size_t)k * FS);
-        double2 b1 = to_d2(x1[(size_t)k * PS]);
-        y1 = make_double2(b1.x - l * y1.x, b1.y - l * y1.y);
-        w1[(size_t)k * PS] = y1;
-        if (two) {
-            double2 b2 = to_d2(x2[(size_t)k * PS]);
-            y2 = make_double2(b2.x - l * y2.x, b2.y - l * y2.y);
-            w2[(size_t)k * PS] = y2;
-        }
-    }
-    // back substitution
-    double di = ld(DI + (size_t)(nr - 1) * FS);
-    double2 s1 = make_double2(y1.x * di, y1.y * di), s2 = make_double2(y2.x * di, y2.y * di);
-    st2(x1 + (size_t)(nr - 1) * PS, s1.x, s1.y);
-    if (two) st2(x2 + (size_t)(nr - 1) * PS, s2.x, s2.y);
-    k = nr - 2;
-    for (; k - (kRB - 1) >= 0; k -= kRB) {
-        double2 b1[kRB], b2[kRB];
-        double u[kRB], dv[kRB];
-#pragma unroll
-        for (int b = 0; b < kRB; ++b) {
-            u[b] = ld(c.apph + k - b);
-            dv[b] = ld(DI + (size_t)(k - b) * FS);
-            b1[b] = w1[(size_t)(k - b) * PS];
-            if (two) b2[b] = w2[(size_t)(k - b) * PS];
-        }
-#pragma unroll
-        for (int b = 0; b < kRB; ++b) {
-            s1 = make_double2((b1[b].x - u[b] * s1.x) * dv[b], (b1[b].y - u[b] * s1.y) * dv[b]);
-            st2(x1 + (size_t)(k - b) * PS, s1.x, s1.y);
-            if (two) {
-                s2 = make_double2((b2[b].x - u[b] * s2.x) * dv[b], (b2[b].y - u[b] * s2.y) * dv[b]);
-                st2(x2 + (size_t)(k - b) * PS, s2.x, s2.y);
-            }
-        }
-    }
-    for (; k >= 0; --k) {
-        const double u = ld(c.apph + k);
-        di = ld(DI + (size_t)k * FS);
-        double2 b1 = w1[(size_t)k * PS];
-        s1 = make_double2((b1.x - u * s1.x) * di, (b1.y - u * s1.y) * di);
-        st2(x1 + (size_t)k * PS, s1.x, s1.y);
-        if (two) {
-            double2 b2 = w2[(size_t)k * PS];
-            s2 = make_double2((b2.x - u * s2.x) * di, (b2.y - u * s2.y) * di);
-            st2(x2 + (size_t)k * PS, s2.x, s2.y);
-        }
-    }
-}
-
-// One mode (kz, kt) of the full spectrum, kz = 0..nzm-1: the solve of
-// ptri_mode for one member of a pair (the factors of mode kz and nzm-kz are
-// shared: index min(kz, nzm-kz)).  Twice the threads of the paired form
-// with half the registers each, which keeps more warps resident on the FP64
-// pipe; the arithmetic of each mode is ptri_mode's.
+// right-hand side, with the precomputed LU factors.  One thread per mode
+// (kz, kt) of the full spectrum, kz = 0..nzm-1; modes kz and nzm-kz share
+// their factors (index min(kz, nzm-kz)).
+//
+// FP64 path (ptri_one): FP64 arithmetic, the forward-sweep results kept in
+// the spectrum itself.
 template <typename T>
 __device__ __forceinline__ void ptri_one(const Dims& d, const Coef& c, const FieldsT<T>& f, double2* ws, long long t) {
     typedef typename V2<T>::type C2;
@@ -1031,6 +938,111 @@ __device__ __forceinline__ void ptri_one(const Dims& d, const Coef& c, const Fie
         s = make_double2((b.x - u * s.x) * di, (b.y - u * s.y) * di);
         st2(x + (size_t)k * PS, s.x, s.y);
     }
+}
+
+// Mixed path (ptri_ff): float-float arithmetic (tc_ff.cuh; the factors and
+// the super-diagonal were converted to float-float pairs once), which keeps
+// the low, nearly singular modes as accurate as FP64 on the FP32 pipes.  The
+// forward-sweep results are kept, as float-float complex values, only at
+// every kPtriCk-th level (and at every level of the tail above the last full
+// batch) in the scratch f.ws; the back substitution recomputes a batch from
+// the checkpoint below it and the spectrum, re-read.  The spectrum is
+// rounded to FP32 once, at the end.
+// (kPtriCk and ptri_slots: tc_dev.h)
+
+struct ffc {
+    ffv re, im;
+};
+__device__ __forceinline__ float4 ffc_pack(ffc v) { return make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo); }
+__device__ __forceinline__ ffc ffc_unpack(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ ffv ffv_ld(const float2* p) { const float2 v = ld(p); return {v.x, v.y}; }
+// y = x - l y
+__device__ __forceinline__ ffc ffc_fwd(float2 x, ffv l, ffc y) {
+    return {ff_sub(ff_from(x.x), ff_mul(l, y.re)), ff_sub(ff_from(x.y), ff_mul(l, y.im))};
+}
+// s = (y - u s) di
+__device__ __forceinline__ ffc ffc_back(ffc y, ffv u, ffv di, ffc s) {
+    return {ff_mul(ff_sub(y.re, ff_mul(u, s.re)), di), ff_mul(ff_sub(y.im, ff_mul(u, s.im)), di)};
+}
+__device__ __forceinline__ float2 ffc_round(ffc v) { return make_float2(ff_round(v.re), ff_round(v.im)); }
+
+__device__ __forceinline__ void ptri_ff(const Dims& d, const FieldsT<float>& f, long long t) {
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const int kf = kz < nzh ? kz : d.nz - kz;
+    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
+    const size_t o = (size_t)kz * PH + kt;
+    float2* x = f.spec + o;
+    float4* w = f.ws + o;                              // slot q at w[q * PS]
+    const float2* L = f.pl_ff + (size_t)kf * PH + kt;
+    const float2* DI = f.pdi_ff + (size_t)kf * PH + kt;
+    const float2* U = f.pu_ff;
+    const int nb = (nr - 1) / kPtriCk;
+    // forward elimination
+    const float2 x0 = x[0];
+    const ffc y0 = {ff_from(x0.x), ff_from(x0.y)};
+    w[0] = ffc_pack(y0);
+    ffc y = y0;
+    int k = 1;
+    for (int m = 0; m < nb; ++m, k += kPtriCk) {
+        float2 xv[kPtriCk], lv[kPtriCk];
+#pragma unroll
+        for (int b = 0; b < kPtriCk; ++b) {
+            xv[b] = x[(size_t)(k + b) * PS];
+            lv[b] = ld(L + (size_t)(k + b) * FS);
+        }
+#pragma unroll
+        for (int b = 0; b < kPtriCk; ++b) y = ffc_fwd(xv[b], {lv[b].x, lv[b].y}, y);
+        w[(size_t)(m + 1) * PS] = ffc_pack(y);
+    }
+    for (int q = nb + 1; k < nr; ++k, ++q) {
+        y = ffc_fwd(x[(size_t)k * PS], ffv_ld(L + (size_t)k * FS), y);
+        w[(size_t)q * PS] = ffc_pack(y);
+    }
+    // back substitution: the last level, then the tail from its stored y
+    ffc s = {ff_mul(y.re, ffv_ld(DI + (size_t)(nr - 1) * FS)), ff_mul(y.im, ffv_ld(DI + (size_t)(nr - 1) * FS))};
+    x[(size_t)(nr - 1) * PS] = ffc_round(s);
+    const int ktop = kPtriCk * nb;                     // top level of the last full batch
+    for (k = nr - 2; k > ktop; --k) {
+        const ffc yk = ffc_unpack(w[(size_t)(nb + 1 + (k - ktop - 1)) * PS]);
+        s = ffc_back(yk, ffv_ld(U + k), ffv_ld(DI + (size_t)k * FS), s);
+        x[(size_t)k * PS] = ffc_round(s);
+    }
+    // full batches from the top: recompute y from the checkpoint below
+    for (int m = nb - 1; m >= 0; --m) {
+        const int kb = 1 + m * kPtriCk;               // lowest level of the batch
+        ffc yb[kPtriCk];
+        ffc yc = ffc_unpack(w[(size_t)m * PS]);
+        float2 xv[kPtriCk - 1];
+#pragma unroll
+        for (int b = 0; b < kPtriCk - 1; ++b) xv[b] = x[(size_t)(kb + b) * PS];
+#pragma unroll
+        for (int b = 0; b < kPtriCk - 1; ++b) {
+            yc = ffc_fwd(xv[b], ffv_ld(L + (size_t)(kb + b) * FS), yc);
+            yb[b] = yc;
+        }
+        yb[kPtriCk - 1] = ffc_unpack(w[(size_t)(m + 1) * PS]);
+        const bool top_of_column = kb + kPtriCk - 1 == nr - 1;
+#pragma unroll
+        for (int b = kPtriCk - 1; b >= 0; --b) {
+            const int kk = kb + b;
+            if (b == kPtriCk - 1 && top_of_column) continue;   // substituted above
+            s = ffc_back(yb[b], ffv_ld(U + kk), ffv_ld(DI + (size_t)kk * FS), s);
+            x[(size_t)kk * PS] = ffc_round(s);
+        }
+    }
+    // level 0, unless it is also the last
+    if (nr > 1) {
+        s = ffc_back(y0, ffv_ld(U), ffv_ld(DI), s);
+        x[0] = ffc_round(s);
+    }
+}
+
+// The pressure tridiagonal of mode t in the path's arithmetic.
+template <typename T>
+__device__ __forceinline__ void ptri_solve(const Dims& d, const Coef& c, const FieldsT<T>& f, long long t) {
+    if constexpr (std::is_same<T, double>::value) ptri_one(d, c, f, reinterpret_cast<double2*>(f.spec), t);
+    else ptri_ff(d, f, t);
 }
 
 // Inverse real FFT along theta: spec rows -> phi rows.

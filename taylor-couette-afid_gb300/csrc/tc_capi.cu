@@ -157,7 +157,7 @@ cudaError_t alloc_fields(tc_handle* h, FieldsT<T>& f) {
         AL(f.Fd.base, MomFactorsT<double>::count(nrr));
         f.Fd.stride = nrr;
         AL(f.corrd, kCorrCount(nrr));
-        AL(f.ws, (size_t)d.PS * nr);
+        AL(f.ws, (size_t)d.PS * ptri_slots(nr));
     }
 #undef AL
     return ce;
@@ -341,6 +341,15 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     std::memset(h->st_host, 0, sizeof(StepState));
 
     launch_pressure_factors(h->stream, d, h->c, pl, pdv);
+    if (h->mixed) {
+        float2* pu = nullptr;
+        ce = dalloc(h, &pu, (size_t)nr);
+        if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "device allocation"); tc_destroy(h); return r; }
+        launch_pressure_factors_ff(h->stream, d, h->c, pl, pdv, pu);
+        h->ff.pl_ff = reinterpret_cast<const float2*>(pl);
+        h->ff.pdi_ff = reinterpret_cast<const float2*>(pdv);
+        h->ff.pu_ff = pu;
+    }
     ce = cudaStreamSynchronize(h->stream);
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pressure factors"); tc_destroy(h); return r; }
     *out = h;

@@ -109,6 +109,15 @@ struct StepState {
     float dt_f, beta_f, vinner_f, pad_f;
 };
 
+// Checkpointed forward sweep of the mixed path's pressure solve (ptri_ff):
+// levels per batch, and the checkpoint slots of a column of nr levels
+// (levels kPtriCk m, m = 0..nb, and the tail levels kPtriCk nb + 1 .. nr - 1).
+constexpr int kPtriCk = 8;
+__host__ __device__ inline int ptri_slots(int nr) {
+    const int nb = (nr - 1) / kPtriCk;
+    return nb + 1 + (nr - 1 - kPtriCk * nb);
+}
+
 // Per-step coefficients of one step (factors kernel), per substep s:
 // [ (s*3 + c)*(nr+1) + k ]  dt al(s) times the pressure-gradient metric of
 //                            component c at level k (CorrectVelocity.F90:

@@ -188,11 +188,11 @@ template <typename T>
 // Compiled for 8 resident blocks per SM (64 registers, a few spilled): on
 // the 512x512x128 grid 0.217 ms a launch (FP32 spectrum) and 0.234 ms (FP64)
 // against 0.246 and 0.245 ms with 122 and 96 registers.
-__global__ void __launch_bounds__(128, 8) ptri_kernel(Dims d, Coef c, FieldsT<T> f, double2* ws) {
+__global__ void __launch_bounds__(128, 8) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)d.nz * d.PH) return;
-    ptri_one(d, c, f, ws, t);
+    ptri_solve(d, c, f, t);
 }
 
 // LU factors of every pressure mode matrix (time independent): thread per
@@ -656,8 +656,7 @@ void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const Plans
 template <typename T>
 void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f) {
     long long n = (long long)d.nz * d.PH;      // one thread per mode
-    double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(f.spec) : f.ws;
-    ptri_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f, ws);
+    ptri_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f);
     TC_LAUNCH_CHECK();
 }
 
@@ -704,6 +703,31 @@ void launch_divergence(cudaStream_t s, const Dims& d, const CoefT<T>& c, const C
                        int sub) {
     long long n = (long long)d.nr * d.nz * (d.nt / 2);
     divergence_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, (T)k.dxt, (T)k.dxz, f, sub);
+    TC_LAUNCH_CHECK();
+}
+
+// The mixed path's pressure factors as float-float pairs, in place (each
+// double becomes the pair (hi, lo) in the same 8 bytes), and the
+// super-diagonal apph as pairs.
+__global__ void pfactor_ff_kernel(double* l, double* dinv, long long n, const double* apph, float2* u, int nr) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        const double a = l[t], b = dinv[t];
+        const float ah = __double2float_rn(a), bh = __double2float_rn(b);
+        reinterpret_cast<float2*>(l)[t] = make_float2(ah, __double2float_rn(a - (double)ah));
+        reinterpret_cast<float2*>(dinv)[t] = make_float2(bh, __double2float_rn(b - (double)bh));
+    }
+    if (t < nr) {
+        const double a = apph[t];
+        const float ah = __double2float_rn(a);
+        u[t] = make_float2(ah, __double2float_rn(a - (double)ah));
+    }
+}
+
+void launch_pressure_factors_ff(cudaStream_t s, const Dims& d, const Coef& c, double* l, double* dinv, float2* u) {
+    const long long n = (long long)d.nzh * d.PH * d.nr;
+    const long long m = n > d.nr ? n : d.nr;
+    pfactor_ff_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(l, dinv, n, c.apph, u, d.nr);
     TC_LAUNCH_CHECK();
 }
 

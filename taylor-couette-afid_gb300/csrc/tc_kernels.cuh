@@ -30,7 +30,11 @@ struct FieldsT {
     double* corrd;
     double* scal;                     // per substep: [s] usdt*fft_norm, [3+s] usdt
     double* red;                      // reduction partials
-    double2* ws;                      // FP64 forward-sweep scratch of the pressure solve (T = float)
+    // mixed path (T = float): the pressure factors and super-diagonal as
+    // float-float pairs (pl_ff, pdi_ff alias pf_l, pf_dinv, converted in
+    // place), and the checkpoint slots of the pressure solve's forward sweep
+    const float2 *pl_ff, *pdi_ff, *pu_ff;
+    float4* ws;
 };
 
 template <typename T>
@@ -77,6 +81,7 @@ void launch_divergence(cudaStream_t s, const Dims& d, const CoefT<T>& c, const C
 
 // One-time set-up.
 void launch_pressure_factors(cudaStream_t s, const Dims& d, const Coef& c, double* l, double* dinv);
+void launch_pressure_factors_ff(cudaStream_t s, const Dims& d, const Coef& c, double* l, double* dinv, float2* u);
 
 // Reductions (FP64 arithmetic; results land in StepState).
 template <typename T>

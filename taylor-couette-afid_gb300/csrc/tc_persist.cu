@@ -201,8 +201,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
             if (I.f.st->halt) continue;
             const long long t = (item - table(PH_PTRI)[m]) * kPersistThreads + threadIdx.x;
             if (t < (long long)I.d.nz * I.d.PH) {
-                double2* ws = std::is_same<T, double>::value ? reinterpret_cast<double2*>(I.f.spec) : I.f.ws;
-                ptri_one(I.d, I.c, I.f, ws, t);
+                ptri_solve(I.d, I.c, I.f, t);
             }
         }
         if (!grid_barrier(a)) return;
