@@ -114,11 +114,19 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
 
 // ---- grouped substep phases ---------------------------------------------------
 
+// Register targets of the heavier grouped kernels, as minimum resident
+// blocks of 256 threads (smaller tiles fit proportionally more): 4 blocks =
+// 64 registers, 3 = 80.  As for the single-run kernels, more resident warps
+// beat the few values a thread would otherwise keep in flight; the FP32
+// march keeps 80 (64 spills) and the FP64 radial sweep 80.
+template <typename T> struct EnsBlocks { static constexpr int momentum = 4, radial = 3, ptri = 4; };
+template <> struct EnsBlocks<float> { static constexpr int momentum = 3, radial = 4, ptri = 4; };
+
 // momentum: item = (chunk of kMomChunk radial levels, tile of TPB
 // consecutive (j, i) columns), each thread marching its column in r; for
 // FP64 (no marching) a chunk is one level and a thread one cell
 template <typename T>
-__global__ void __launch_bounds__(256) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+__global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
@@ -156,7 +164,7 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
 
 // column-wise: item = (component, TPB consecutive (z, theta) columns)
 template <typename T>
-__global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+__global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
@@ -171,7 +179,7 @@ __global__ void __launch_bounds__(256) ens_radial_kernel(const InstT<T>* inst, c
 
 // mode-wise: item = TPB consecutive (kz, kt) modes
 template <typename T>
-__global__ void __launch_bounds__(256) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
+__global__ void __launch_bounds__(256, EnsBlocks<T>::ptri) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
