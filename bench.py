@@ -95,12 +95,12 @@ def algorithmic_bytes(cls: str, nt: int, nz: int, nr: int, rk_substep_mix: float
 # Compulsory HBM bytes of one ideally fused RK3 step per cell: q (3 fields)
 # read and written, pr read and written and one spectral round trip of phi per
 # substep, plus the RK memory ru (read in substeps 2-3, written in 1-2).
-# The FP64 fused momentum kernel measured by ncu on the 512x512x128 grid, one
-# RK3 step (profiles/momentum_kernel_fp64_P2.md): DRAM bytes per cell of a
-# launch averaged over the three substeps (79.6, 103.4, 103.4), and per cell
-# its FP64 instructions (50.88 DADD + 26.95 DMUL + 44.94 DFMA) and FLOPs.
-# Per-cell figures do not depend on the grid size.
-MOMENTUM_FP64_NCU = {"dram_bytes_per_cell": 95.47, "fp64_inst_per_cell": 122.77, "fp64_flops_per_cell": 167.71}
+# The FP64 fused momentum kernel (two cells a thread) measured by ncu on the
+# 512x512x128 grid, one RK3 step (profiles/momentum_kernel_fp64_P2.md): DRAM
+# bytes per cell of a launch averaged over the three substeps (79.2, 102.9,
+# 102.8), and per cell its FP64 instructions (45.41 DADD + 20.98 DMUL +
+# 42.45 DFMA) and FLOPs.  Per-cell figures do not depend on the grid size.
+MOMENTUM_FP64_NCU = {"dram_bytes_per_cell": 94.98, "fp64_inst_per_cell": 108.84, "fp64_flops_per_cell": 151.29}
 
 STEP_BYTES = {"fp64": 3 * (6 + 2 + 2) * 8 + (2 * 3 + 2 * 3) * 8,
               "mixed": 3 * (6 * 4 + 2 * 8 + 2 * 4) + 12 * 4}

@@ -339,32 +339,17 @@ __device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     return -(h31 + h32 + h33) + dqz1 + dqz2;
 }
 
-template <int MODE, typename T>
-__device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
-                                              int k) {
+// ImplicitAndUpdateQT/QR/QZ for cell (i, j, k) of stencil S given its
+// explicit terms: the right-hand sides and the RK memory.
+template <typename T>
+__device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, const Stencil& S,
+                                              int i, int j, int k, T ht, T hr, T hz) {
     const int nr = d.nr;
-    const Stencil S = make_stencil(d, i, j, k);
     const size_t o = S.o;
     const int P = S.P;
     const T* qt = a.qt + o;
     const T* qr = a.qr + o;
     const T* qz = a.qz + o;
-    T ht = 0, hr = 0, hz = 0;
-    if (MODE != MODE_IMPLICIT) {
-        ht = explicit_qt(S, c, a, qt, qr, qz);
-        if (k >= 1) hr = explicit_qr(S, c, a, qt, qr, qz);
-        hz = explicit_qz(S, c, a, qt, qr, qz);
-        if (MODE == MODE_EXPLICIT) {
-            a.h_t[o] = ht;
-            if (k >= 1) a.h_r[o] = hr;
-            a.h_z[o] = hz;
-            return;
-        }
-    } else {
-        ht = a.h_t[o];
-        if (k >= 1) hr = a.h_r[o];
-        hz = a.h_z[o];
-    }
     // gam dt, rom dt, alre dt; the pressure terms use the per-level dt al
     // metric products of the correction (a.cf), so no factor dt remains
     const T gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
@@ -425,6 +410,173 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
         a.rhs_z[o] = gadt * hz + rodt * old + alredt * d33 - dpx33;
         a.ru3[o] = hz;
     }
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
+                                              int k) {
+    const int nr = d.nr;
+    const Stencil S = make_stencil(d, i, j, k);
+    const size_t o = S.o;
+    const int P = S.P;
+    const T* qt = a.qt + o;
+    const T* qr = a.qr + o;
+    const T* qz = a.qz + o;
+    T ht = 0, hr = 0, hz = 0;
+    if (MODE != MODE_IMPLICIT) {
+        ht = explicit_qt(S, c, a, qt, qr, qz);
+        if (k >= 1) hr = explicit_qr(S, c, a, qt, qr, qz);
+        hz = explicit_qz(S, c, a, qt, qr, qz);
+        if (MODE == MODE_EXPLICIT) {
+            a.h_t[o] = ht;
+            if (k >= 1) a.h_r[o] = hr;
+            a.h_z[o] = hz;
+            return;
+        }
+    } else {
+        ht = a.h_t[o];
+        if (k >= 1) hr = a.h_r[o];
+        hz = a.h_z[o];
+    }
+    implicit_cell(d, c, a, S, i, j, k, ht, hr, hz);
+}
+
+// The fused momentum work of momentum_cell (MODE_FUSED) for the two cells
+// (i, j, k) and (i+1, j, k), i even: the sums and products through the
+// theta face between them are formed once (h11 of qt, h31 of qz, h21 of qr,
+// the qr interpolation qre = qrw of d11qre), and within each cell the
+// products the radial and z terms share (h12d and h21; h23 and h32) are
+// formed once.  The FP64 path is bound by the FP64 pipe, so each shared
+// product or sum is a cycle saved.  Term by term the arithmetic is that of
+// explicit_qt/qr/qz; only the rounding order of a few sums differs.
+template <typename T>
+__device__ __forceinline__ void momentum_pair(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
+                                              int k) {
+    const Stencil Sa = make_stencil(d, i, j, k), Sb = make_stencil(d, i + 1, j, k);
+    const int P = Sa.P;
+    const T* qt = a.qt + Sa.o;
+    const T* qr = a.qr + Sa.o;
+    const T* qz = a.qz + Sa.o;
+    const int dimA = Sa.dim;                     // theta- of cell a (wraps at i = 0)
+    const int dipB = 1 + Sb.dip;                 // theta+ of cell b, from cell a (wraps at i + 1 = nt - 1)
+    const int djp = Sa.djp, djm = Sa.djm;
+    const int kP = (Sa.kpp - k) * P, kM = (Sa.kmm - k) * P;
+    const T two = (T)2.0;
+    // level k and the clamped radial neighbours
+    const T ta = ld(qt), tb = ld(qt + 1), tam = ld(qt + dimA), tbp = ld(qt + dipB);
+    const T ta_jp = ld(qt + djp), tb_jp = ld(qt + djp + 1), ta_jm = ld(qt + djm), tb_jm = ld(qt + djm + 1);
+    const T tbp_jm = ld(qt + djm + dipB);
+    const T ta_kp = ld(qt + kP), tb_kp = ld(qt + kP + 1), ta_km = ld(qt + kM), tb_km = ld(qt + kM + 1);
+    const T ra = ld(qr), rb = ld(qr + 1), ram = ld(qr + dimA);
+    const T ra_p = ld(qr + P), rb_p = ld(qr + P + 1), ram_p = ld(qr + P + dimA);
+    const T ra_jm = ld(qr + djm), rb_jm = ld(qr + djm + 1);
+    const T ra_pjm = ld(qr + P + djm), rb_pjm = ld(qr + P + djm + 1);
+    const T za = ld(qz), zb = ld(qz + 1), zam = ld(qz + dimA), zbp = ld(qz + dipB);
+    const T za_jp = ld(qz + djp), zb_jp = ld(qz + djp + 1), za_jm = ld(qz + djm), zb_jm = ld(qz + djm + 1);
+    const T zam_jp = ld(qz + djp + dimA);
+    const T za_kp = ld(qz + kP), zb_kp = ld(qz + kP + 1), za_km = ld(qz + kM), zb_km = ld(qz + kM + 1);
+    const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + k + 1);
+    // shared products
+    const T Sab = tb + ta, Sab2 = Sab * Sab;                 // theta face a|b of h11
+    const T rc2a = ra + ram, rp2a = ra_p + ram_p, rc2b = rb + ra, rp2b = rb_p + ra_p;
+    const T Xa = rc2a * (ta + ta_km);                         // lower radial face of h12d (a); h21 of a for k >= 1
+    const T Xb = rc2b * (tb + tb_km);                         // the same for b; = theta face a|b of h21 for k >= 1
+    const T x13a = (za + zam) * (ta + ta_jm);                 // second products of h13 (and h31)
+    const T x13b = (zb + za) * (tb + tb_jm);                  // = theta face a|b of h31
+    const T qrea = ra_p * usrcp + ra * usrc;                  // = qrw of b
+    const T qreb = rb_p * usrcp + rb * usrc;
+    const T qrwa = ram_p * usrcp + ram * usrc;
+    const T Ya = (ra + ra_jm) * (za + za_km);                 // lower radial face of h32 (a); h23 of a for k >= 1
+    const T Yb = (rb + rb_jm) * (zb + zb_km);
+    T ht[2], hr[2] = {(T)0, (T)0}, hz[2];
+    // ---- ExplicitTermsQT
+    {
+        const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
+        const T q2rm = ld(c.q_udx2rm + k), qusrm = ld(c.q_usrm + k), hv1 = ld(c.h_udx1vis1 + k);
+        {
+            const T B = ta + tam;
+            const T h11 = (Sab2 - B * B) * udxt;
+            const T h12d = (rp2a * (ta_kp + ta) - Xa) * q2rm;
+            const T qrs = rp2a * usrcp + rc2a * usrc;
+            const T h12n = ta * qusrm * qrs;
+            const T h13 = ((za_jp + zam_jp) * (ta_jp + ta) - x13a) * a.udxz;
+            const T d11qt = (tb - two * ta + tam) * udxtq;
+            const T d22qt = (ta_jp - two * ta + ta_jm) * a.udxzq;
+            const T d11qre = (qrea - qrwa) * hv1;
+            const T coriol = -qrs * a.q_romeg;
+            ht[0] = -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
+        }
+        {
+            const T A = tbp + tb;
+            const T h11 = (A * A - Sab2) * udxt;
+            const T h12d = (rp2b * (tb_kp + tb) - Xb) * q2rm;
+            const T qrs = rp2b * usrcp + rc2b * usrc;
+            const T h12n = tb * qusrm * qrs;
+            const T h13 = ((zb_jp + za_jp) * (tb_jp + tb) - x13b) * a.udxz;
+            const T d11qt = (tbp - two * tb + ta) * udxtq;
+            const T d22qt = (tb_jp - two * tb + tb_jm) * a.udxzq;
+            const T d11qre = (qreb - qrea) * hv1;
+            const T coriol = -qrs * a.q_romeg;
+            ht[1] = -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
+        }
+    }
+    // ---- ExplicitTermsQR at faces k >= 1 (kM = -P there)
+    if (k >= 1) {
+        const T rbp = ld(qr + dipB), ra_jp = ld(qr + djp), rb_jp = ld(qr + djp + 1);
+        const T ra_m = ld(qr - P), rb_m = ld(qr - P + 1);
+        const T tbp_m = ld(qt - P + dipB);
+        const T za_mjp = ld(qz - P + djp), zb_mjp = ld(qz - P + djp + 1);
+        const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k), usrcm = ld(c.usrc + k - 1);
+        const T q2c = ld(c.q_udx2c + k), v2 = ld(c.udx1vis2 + k), qrc = ld(c.q_rc_romeg + k);
+        const T sa0 = tb + tb_km, sb0 = ta + ta_km;           // cell a; sb of b = sa0
+        {
+            const T s4 = sa0 + sb0, aa = s4 * (T)0.25;
+            const T h11n = aa * aa;
+            const T h21 = (Xb - Xa) * udxt;
+            const T h22 = (qrea * (ra_p + ra) - (ra * usrc + ra_m * usrcm) * (ra + ra_m)) * q2c;
+            const T h23 = ((za_jp + za_mjp) * (ra_jp + ra) - Ya) * a.udxz;
+            const T d11qre = -(sa0 - sb0) * v2;
+            const T d11qr = (rb - two * ra + ram) * udxtq;
+            const T d22qr = (ra_jp - two * ra + ra_jm) * a.udxzq;
+            const T coriol = s4 * qrc;
+            hr[0] = -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
+        }
+        {
+            const T sa1 = tbp + tbp_m;
+            const T s4 = sa1 + sa0, aa = s4 * (T)0.25;
+            const T h11n = aa * aa;
+            const T h21 = (sa1 * (rbp + rb) - Xb) * udxt;
+            const T h22 = (qreb * (rb_p + rb) - (rb * usrc + rb_m * usrcm) * (rb + rb_m)) * q2c;
+            const T h23 = ((zb_jp + zb_mjp) * (rb_jp + rb) - Yb) * a.udxz;
+            const T d11qre = -(sa1 - sa0) * v2;
+            const T d11qr = (rbp - two * rb + ra) * udxtq;
+            const T d22qr = (rb_jp - two * rb + rb_jm) * a.udxzq;
+            const T coriol = s4 * qrc;
+            hr[1] = -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
+        }
+    }
+    // ---- ExplicitTermsQZ
+    {
+        const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k), q2rm = ld(c.q_udx2rm + k);
+        {
+            const T h31 = (x13b - x13a) * udxt;
+            const T h32 = ((ra_p + ra_pjm) * (za_kp + za) - Ya) * q2rm;
+            const T h33 = ((za_jp + za) * (za_jp + za) - (za + za_jm) * (za + za_jm)) * a.udxz;
+            const T dqz1 = (zam - two * za + zb) * udxtq;
+            const T dqz2 = (za_jm - two * za + za_jp) * a.udxzq;
+            hz[0] = -(h31 + h32 + h33) + dqz1 + dqz2;
+        }
+        {
+            const T h31 = ((tbp + tbp_jm) * (zbp + zb) - x13b) * udxt;
+            const T h32 = ((rb_p + rb_pjm) * (zb_kp + zb) - Yb) * q2rm;
+            const T h33 = ((zb_jp + zb) * (zb_jp + zb) - (zb + zb_jm) * (zb + zb_jm)) * a.udxz;
+            const T dqz1 = (za - two * zb + zbp) * udxtq;
+            const T dqz2 = (zb_jm - two * zb + zb_jp) * a.udxzq;
+            hz[1] = -(h31 + h32 + h33) + dqz1 + dqz2;
+        }
+    }
+    implicit_cell(d, c, a, Sa, i, j, k, ht[0], hr[0], hz[0]);
+    implicit_cell(d, c, a, Sb, i + 1, j, k, ht[1], hr[1], hz[1]);
 }
 
 // The fused momentum work (explicit terms and implicit right-hand sides of

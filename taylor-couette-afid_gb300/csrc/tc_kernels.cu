@@ -127,9 +127,20 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
 
 // The fused form: one thread per (theta, z) column and chunk of kMomChunk
 // radial levels, marching in r (momentum_column).
+// FP64 fused momentum, two theta-neighbouring cells per thread
+// (momentum_pair); one thread per pair (i even: nthm is even).
 template <typename T>
+__global__ void __launch_bounds__(128) momentum_pair_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
+    if (a.st->halt) return;
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.nt || j >= d.nz) return;
+    momentum_pair(d, c, a, i, j, blockIdx.z);
+}
+
 // Compiled for 8 resident blocks per SM: 64 registers without spills (the
 // unbounded allocation took 80, leaving 6 blocks, and ran 14 % slower).
+template <typename T>
 __global__ void __launch_bounds__(128, 8) momentum_march_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
     if (a.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -596,7 +607,10 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
         g.z = (d.nr + kMomChunk - 1) / kMomChunk;
         momentum_march_kernel<T><<<g, blk, 0, s>>>(d, c, a);
     } else if (mode == MODE_FUSED) {
-        momentum_kernel<MODE_FUSED, T><<<g, blk, 0, s>>>(d, c, a);
+        // two cells per thread along theta
+        const dim3 pblk(32, 4, 1);
+        const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
+        momentum_pair_kernel<T><<<pg, pblk, 0, s>>>(d, c, a);
     }
     else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
     else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
