@@ -116,15 +116,17 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
 
 // Register targets of the heavier grouped kernels, as minimum resident
 // blocks of 256 threads (smaller tiles fit proportionally more): 4 blocks =
-// 64 registers, 3 = 80.  As for the single-run kernels, more resident warps
-// beat the few values a thread would otherwise keep in flight; the FP32
-// march keeps 80 (64 spills) and the FP64 radial sweep 80.
-template <typename T> struct EnsBlocks { static constexpr int momentum = 4, radial = 3, ptri = 4; };
+// 64 registers, 3 = 80, 2 = 128.  As for the single-run kernels, more
+// resident warps beat the few values a thread would otherwise keep in
+// flight; the FP32 march keeps 80 (64 spills), the FP64 radial sweep 80 and
+// the FP64 two-cell momentum body 128.
+template <typename T> struct EnsBlocks { static constexpr int momentum = 2, radial = 3, ptri = 4; };
 template <> struct EnsBlocks<float> { static constexpr int momentum = 3, radial = 4, ptri = 4; };
 
 // momentum: item = (chunk of kMomChunk radial levels, tile of TPB
 // consecutive (j, i) columns), each thread marching its column in r; for
-// FP64 (no marching) a chunk is one level and a thread one cell
+// FP64 (no marching) a chunk is one level and a thread a theta-neighbouring
+// pair of cells (momentum_pair)
 template <typename T>
 __global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;
@@ -132,17 +134,14 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kern
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
-    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const long long units = mom_units<T>(I.d.P);
+    const int tiles = (int)((units + blockDim.x - 1) / blockDim.x);
     const int chunk = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)chunk * tiles) * blockDim.x + threadIdx.x;
-    if (flat >= I.d.P) return;
-    const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
-    if (MomMarch<T>::value) {
-        const int k0 = chunk * kMomChunk, k1 = min(k0 + kMomChunk, I.d.nr);
-        momentum_column(I.d, I.cv, I.ma[sub], i, j, k0, k1);
-    } else {
-        momentum_cell<MODE_FUSED>(I.d, I.cv, I.ma[sub], i, j, chunk);
-    }
+    if (flat >= units) return;
+    int i, j;
+    mom_unit_cell<T>((int)flat, I.d.nt, i, j);
+    mom_unit(I.d, I.cv, I.ma[sub], i, j, chunk);
 }
 
 // cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)
@@ -316,7 +315,8 @@ int rebuild(tc_ensemble* e) {
         const Dims& d = h->d;
         maxNz = std::max(maxNz, d.nz);
         long long cnt[PH_COUNT];
-        cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) * ceil_div(d.P, TPB);
+        cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) *
+                      ceil_div(mom_units<T>(d.P), TPB);
         cnt[PH_CORR] = (long long)d.nr * ceil_div(d.P, TPB);
         cnt[PH_RAD] = 3LL * ceil_div(d.P, TPB);
         cnt[PH_PTRI] = ceil_div((long long)d.nz * d.PH, TPB);

@@ -26,6 +26,36 @@ enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT,
 
 constexpr double kCflFloor = 0.00000001;   // CalcMaxCFL.F90 starts its maximum here
 
+// Momentum work units of one radial level (or chunk) of a member: columns
+// for the FP32 march, theta-neighbouring cell pairs for FP64 (momentum_pair).
+template <typename T>
+__host__ __device__ __forceinline__ long long mom_units(long long P) { return MomMarch<T>::value ? P : P / 2; }
+
+// Cell (i, j) of momentum unit u of a member with nt theta cells.
+template <typename T>
+__device__ __forceinline__ void mom_unit_cell(int u, int nt, int& i, int& j) {
+    if (MomMarch<T>::value) {
+        j = (int)((unsigned)u / (unsigned)nt);
+        i = u - j * nt;
+    } else {
+        const int half = nt / 2;
+        j = (int)((unsigned)u / (unsigned)half);
+        i = 2 * (u - j * half);
+    }
+}
+
+// The momentum work of unit (i, j) at level/chunk `outer` of substep args ma.
+template <typename T>
+__device__ __forceinline__ void mom_unit(const Dims& d, const CoefT<T>& cv, const MomArgs<T>& ma, int i, int j,
+                                         int outer) {
+    if constexpr (MomMarch<T>::value) {
+        const int k0 = outer * kMomChunk;
+        momentum_column(d, cv, ma, i, j, k0, min(k0 + kMomChunk, d.nr));
+    } else {
+        momentum_pair(d, cv, ma, i, j, outer);
+    }
+}
+
 __device__ __forceinline__ int find_member(const int* prefix, int n, long long item) {
     int lo = 0, hi = n;
     while (hi - lo > 1) {

@@ -143,20 +143,17 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         if (!grid_barrier(a)) return;
     }
     // momentum: (chunk of kMomChunk levels, tile of columns) marching in r;
-    // for FP64 (level, tile of cells)
+    // for FP64 (level, tile of theta-neighbouring cell pairs)
     for (long long item = blockIdx.x; item < a.items[PH_MOM]; item += gridDim.x) {
         const int m = find_member(table(PH_MOM), n, item);
         const InstT<T>& I = inst[m];
         if (I.f.st->halt) continue;
-        const CellItem ci = cell_item(item - table(PH_MOM)[m], I.d.P);
-        if (ci.flat < (long long)I.d.P) {
-            const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
-            if (MomMarch<T>::value) {
-                const int k0 = ci.outer * kMomChunk;
-                momentum_column(I.d, I.cv, I.ma[sub], i, j, k0, min(k0 + kMomChunk, I.d.nr));
-            } else {
-                momentum_cell<MODE_FUSED>(I.d, I.cv, I.ma[sub], i, j, ci.outer);
-            }
+        const long long units = mom_units<T>(I.d.P);
+        const CellItem ci = cell_item(item - table(PH_MOM)[m], (size_t)units);
+        if (ci.flat < units) {
+            int i, j;
+            mom_unit_cell<T>((int)ci.flat, I.d.nt, i, j);
+            mom_unit(I.d, I.cv, I.ma[sub], i, j, ci.outer);
         }
     }
     if (!grid_barrier(a)) return;
