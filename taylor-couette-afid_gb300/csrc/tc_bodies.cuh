@@ -13,6 +13,7 @@
 #include "tc_convert.cuh"
 #include "tc_fft.cuh"
 #include "tc_ff.cuh"
+#include "tc_f32x2.cuh"
 #include "tc_kernels.cuh"
 
 namespace tcgb {
@@ -577,6 +578,191 @@ __device__ __forceinline__ void momentum_pair(const Dims& d, const CoefT<T>& c, 
     }
     implicit_cell(d, c, a, Sa, i, j, k, ht[0], hr[0], hz[0]);
     implicit_cell(d, c, a, Sb, i + 1, j, k, ht[1], hr[1], hz[1]);
+}
+
+// momentum_column for the two theta-neighbouring columns (i, j) and
+// (i+1, j), i even, in packed FP32 (tc_f32x2.cuh): every F2 holds cell i in
+// its first lane and cell i+1 in its second, so one packed instruction does
+// the arithmetic of both cells; centre values load as float2, and the
+// theta neighbours are the other lane of the pair plus one scalar load each
+// side.  The terms are momentum_column's, with the multiply-adds written
+// out: (A^2 - B^2) of h11 and h33 as (A - B)(A + B).  FP32 mixed path only.
+__device__ __forceinline__ F2 ld_f2(const float* p) {
+    const float2 v = ld(reinterpret_cast<const float2*>(p));
+    return mkf2(v.x, v.y);
+}
+
+__device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
+                                                   int i, int j, int k0, int k1) {
+    const int nr = d.nr, nt = d.nt, nz = d.nz;
+    const int P = (int)d.P;
+    const int dimA = i == 0 ? nt - 1 : -1;             // q(i-1) from the pair's first cell
+    const int dipB = i + 2 == nt ? 2 - nt : 2;         // q(i+2)
+    const int djm = j == 0 ? (nz - 1) * nt : -nt, djp = j == nz - 1 ? -(nz - 1) * nt : nt;
+    const size_t col = (size_t)j * nt + i;
+    const F2 TWO = bc2(2.0f), MTWO = bc2(-2.0f), QUARTER = bc2(0.25f), ZERO = bc2(0.0f);
+    const float gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
+    const F2 GADT = bc2(gadt), RODT = bc2(rodt), ALREDT = bc2(alredt);
+    const int nrr = nr + 1;
+    const F2 FIC = a.icyl ? mkf2((float)a.icyl[col], (float)a.icyl[col + 1]) : bc2(1.0f);
+    const F2 UDXZ = bc2(a.udxz), UDXZQ = bc2(a.udxzq), NQROMEG = bc2(-a.q_romeg);
+    const F2 NCFZ = bc2(-ld(a.cf + 2 * nrr));
+    const float* qt = a.qt;
+    const float* qr = a.qr;
+    const float* qz = a.qz;
+    const float* pr = a.pr;
+
+    // level k0 and its lower neighbours
+    size_t o = (size_t)k0 * P + col;
+    const int km0 = k0 > 0 ? k0 - 1 : 0;
+    const size_t om = (size_t)km0 * P + col;
+    F2 tc = ld_f2(qt + o), tm = ld_f2(qt + om);
+    F2 tmip = mkf2(f2y(tm), ld(qt + om + dipB));
+    F2 rc = ld_f2(qr + o);
+    F2 rim = mkf2(ld(qr + o + dimA), f2x(rc));
+    F2 rjm = ld_f2(qr + o + djm);
+    F2 rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
+    F2 zc = ld_f2(qz + o), zm = ld_f2(qz + om), zmjp = ld_f2(qz + om + djp);
+    F2 prm = k0 > 0 ? ld_f2(pr + om) : ZERO;
+    F2 U12, Uz, Gup;
+    {
+        U12 = (rc + rim) * (tc + tm);
+        Uz = (rc + rjm) * (zc + zm);
+        const float usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : 0.0f;
+        Gup = fma2(rm, bc2(usrcm), rc * bc2(usrc)) * (rc + rm);
+    }
+    for (int k = k0; k < k1; ++k, o += P) {
+        const bool top = k == nr - 1;
+        const F2 U12lo = U12, Uzlo = Uz;
+        const int kp = k + 1;
+        // loads of level k (neighbours) and k+1 (column)
+        float tcx, tcy, rcx, rcy, zcx, zcy;
+        f2xy(tc, tcx, tcy);
+        f2xy(rc, rcx, rcy);
+        f2xy(zc, zcx, zcy);
+        const F2 tip = mkf2(tcy, ld(qt + o + dipB)), tim = mkf2(ld(qt + o + dimA), tcx);
+        const F2 tjp = ld_f2(qt + o + djp), tjm = ld_f2(qt + o + djm);
+        const F2 tjmip = mkf2(f2y(tjm), ld(qt + o + djm + dipB));
+        const F2 tp = top ? tc : ld_f2(qt + o + P);
+        const F2 rip = mkf2(rcy, ld(qr + o + dipB)), rjp = ld_f2(qr + o + djp);
+        const F2 rp = ld_f2(qr + o + P);
+        const F2 rpim = mkf2(ld(qr + o + P + dimA), f2x(rp)), rpjm = ld_f2(qr + o + P + djm);
+        const F2 zip = mkf2(zcy, ld(qz + o + dipB)), zim = mkf2(ld(qz + o + dimA), zcx);
+        const F2 zjp = ld_f2(qz + o + djp), zjm = ld_f2(qz + o + djm);
+        const F2 zjpim = mkf2(ld(qz + o + djp + dimA), f2x(zjp));
+        const F2 zp = top ? zc : ld_f2(qz + o + P);
+        const F2 pc = ld_f2(pr + o), pjm = ld_f2(pr + o + djm);
+        const F2 pim = mkf2(ld(pr + o + dimA), f2x(pc));
+
+        const F2 USRC = bc2(ld(c.usrc + k)), USRCP = bc2(ld(c.usrc + kp));
+        const F2 tz_sw = (zc + zim) * (tc + tjm);
+        const F2 qre = fma2(rp, USRCP, rc * USRC);
+        // ---- ExplicitTermsQT
+        F2 ht;
+        {
+            const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+            const F2 sth = tip + tim;
+            const F2 x11 = (tip - tim) * fma2(TWO, tc, sth);          // (tip+tc)^2 - (tc+tim)^2
+            const F2 rp2 = rp + rpim, rc2 = rc + rim;
+            const F2 up = rp2 * (tp + tc);
+            const F2 qrs = fma2(rp2, USRCP, rc2 * USRC);
+            const F2 h12n = tc * bc2(ld(c.q_usrm + k)) * qrs;
+            U12 = up;
+            F2 s = fma2(up - U12lo, bc2(ld(c.q_udx2rm + k)), h12n);  // h12d + h12n
+            s = fma2(x11, UDXT, s);                                   // + h11
+            s = fma2((zjp + zjpim) * (tjp + tc) - tz_sw, UDXZ, s);    // + h13
+            const F2 qrw = fma2(rpim, USRCP, rim * USRC);
+            F2 r = (qre - qrw) * bc2(ld(c.h_udx1vis1 + k));           // d11qre
+            r = fma2(fma2(MTWO, tc, tjp + tjm), UDXZQ, r);            // + d22qt
+            r = fma2(fma2(MTWO, tc, sth), UDXTQ, r);                  // + d11qt
+            ht = fma2(qrs, NQROMEG, r - s);                           // + Coriolis
+        }
+        // ---- ExplicitTermsQR at face k (1 <= k)
+        F2 hr = ZERO;
+        {
+            const F2 rup = qre * (rp + rc);
+            if (k >= 1) {
+                const F2 UDXT = bc2(ld(c.udxt_c + k)), UDXTQ = bc2(ld(c.udxtq_c + k));
+                const F2 sa = tip + tmip, sb = tc + tm, s4 = sa + sb;
+                const F2 aa = s4 * QUARTER;
+                F2 s = (sa * (rip + rc) - U12lo) * UDXT;                  // h21
+                s = fma2(rup - Gup, bc2(ld(c.q_udx2c + k)), s);           // + h22
+                s = fma2((zjp + zmjp) * (rjp + rc) - Uzlo, UDXZ, s);      // + h23
+                F2 r = fma2(aa, aa, (sb - sa) * bc2(ld(c.udx1vis2 + k))); // h11n + d11qre
+                r = fma2(fma2(MTWO, rc, rip + rim), UDXTQ, r);            // + d11qr
+                r = fma2(fma2(MTWO, rc, rjp + rjm), UDXZQ, r);            // + d22qr
+                r = fma2(s4, bc2(ld(c.q_rc_romeg + k)), r);               // + Coriolis
+                hr = r - s;
+            }
+            Gup = rup;
+        }
+        // ---- ExplicitTermsQZ
+        F2 hz;
+        {
+            const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+            const F2 upz = (rp + rpjm) * (zp + zc);
+            F2 s = (upz - Uzlo) * bc2(ld(c.q_udx2rm + k));                // h32
+            Uz = upz;
+            s = fma2((tip + tjmip) * (zip + zc) - tz_sw, UDXT, s);        // + h31
+            const F2 sjz = zjp + zjm;
+            s = fma2((zjp - zjm) * fma2(TWO, zc, sjz), UDXZ, s);          // + h33
+            F2 r = fma2(MTWO, zc, zim + zip) * UDXTQ;                     // dqz1
+            r = fma2(fma2(MTWO, zc, sjz), UDXZQ, r);                      // + dqz2
+            hz = r - s;
+        }
+        // ---- ImplicitAndUpdateQT
+        {
+            F2 d33;
+            if (k == 0) {
+                const F2 acc = fma2(bc2(ld(c.ac1j)), FIC, bc2(a.ac1j_fs0) * (bc2(1.0f) - FIC));
+                const F2 amm = fma2(bc2(ld(c.am1j)), FIC, bc2(a.am1j_fs0) * (bc2(1.0f) - FIC));
+                d33 = fma2(tp, bc2(ld(c.ap1j)), fma2(tc, acc, bc2(a.virotint + step_vinner<float>(a.st)) * amm));
+            } else if (top) {
+                const float app = ld(c.ap1j + k) * 1.0f + a.ap1j_fs1 * 0.0f;
+                const float acc = ld(c.ac1j + k) * 1.0f + a.ac1j_fs1 * 0.0f;
+                d33 = fma2(tc, bc2(acc), fma2(tm, bc2(ld(c.am1j + k)), bc2(a.virotext * app)));
+            } else {
+                d33 = fma2(tp, bc2(ld(c.ap1j + k)), fma2(tc, bc2(ld(c.ac1j + k)), tm * bc2(ld(c.am1j + k))));
+            }
+            const F2 old = a.use_ru ? ld_f2(a.ru1 + o) : ZERO;
+            const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old, GADT * ht)));
+            st_f2(a.rhs_t + o, rhs);
+            st_f2(a.ru1 + o, ht);
+        }
+        // ---- ImplicitAndUpdateQR, faces 1..nr-1
+        if (k >= 1) {
+            const F2 d33 = fma2(rp, bc2(ld(c.ap2je + k)), fma2(rc, bc2(ld(c.ac2je + k)), rm * bc2(ld(c.am2je + k))));
+            const F2 old = a.use_ru ? ld_f2(a.ru2 + o) : ZERO;
+            const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old, GADT * hr)));
+            st_f2(a.rhs_r + o, rhs);
+            st_f2(a.ru2 + o, hr);
+        }
+        // ---- ImplicitAndUpdateQZ
+        {
+            F2 d33;
+            if (k == 0) {
+                const F2 acc = fma2(bc2(ld(c.ac3j)), FIC, bc2(a.ac3j_fs0) * (bc2(1.0f) - FIC));
+                const F2 amm = fma2(bc2(ld(c.am3j)), FIC, bc2(a.am3j_fs0) * (bc2(1.0f) - FIC));
+                d33 = fma2(zp, bc2(ld(c.ap3j)), fma2(zc, acc, zc * amm));
+            } else if (top) {
+                const float app = ld(c.ap3j + k) * 1.0f + a.ap3j_fs1 * 0.0f;
+                const float acc = ld(c.ac3j + k) * 1.0f + a.ac3j_fs1 * 0.0f;
+                d33 = fma2(zc, bc2(app), fma2(zc, bc2(acc), zm * bc2(ld(c.am3j + k))));
+            } else {
+                d33 = fma2(zp, bc2(ld(c.ap3j + k)), fma2(zc, bc2(ld(c.ac3j + k)), zm * bc2(ld(c.am3j + k))));
+            }
+            // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
+            const F2 old = top ? hz : (a.use_ru ? ld_f2(a.ru3 + o) : ZERO);
+            const F2 rhs = fma2(pc - pjm, NCFZ, fma2(ALREDT, d33, fma2(RODT, old, GADT * hz)));
+            st_f2(a.rhs_z + o, rhs);
+            st_f2(a.ru3 + o, hz);
+        }
+        // march: level k becomes the lower neighbour of level k+1
+        tm = tc; tmip = tip; tc = tp;
+        rm = rc; rc = rp; rim = rpim; rjm = rpjm;
+        zm = zc; zmjp = zjp; zc = zp;
+        prm = pc;
+    }
 }
 
 // The fused momentum work (explicit terms and implicit right-hand sides of

@@ -138,6 +138,18 @@ __global__ void __launch_bounds__(128) momentum_pair_kernel(Dims d, CoefT<T> c, 
     momentum_pair(d, c, a, i, j, blockIdx.z);
 }
 
+// FP32 march of two theta-neighbouring columns a thread in packed FP32
+// (momentum_column_x2).  124 registers, 4 resident blocks per SM; capping
+// the registers (96 or 80, with spills) measured slower.
+__global__ void __launch_bounds__(128) momentum_march_x2_kernel(Dims d, CoefT<float> c, MomArgs<float> a) {
+    if (a.st->halt) return;
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.nt || j >= d.nz) return;
+    const int k0 = blockIdx.z * kMomChunk, k1 = min(k0 + kMomChunk, d.nr);
+    momentum_column_x2(d, c, a, i, j, k0, k1);
+}
+
 // Compiled for 8 resident blocks per SM: 64 registers without spills (the
 // unbounded allocation took 80, leaving 6 blocks, and ran 14 % slower).
 template <typename T>
@@ -604,8 +616,15 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
     dim3 blk;
     dim3 g = cell_grid(d, blk);
     if (mode == MODE_FUSED && MomMarch<T>::value) {
-        g.z = (d.nr + kMomChunk - 1) / kMomChunk;
-        momentum_march_kernel<T><<<g, blk, 0, s>>>(d, c, a);
+        if constexpr (std::is_same<T, float>::value) {
+            const dim3 pblk(32, 4, 1);
+            const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y,
+                          (d.nr + kMomChunk - 1) / kMomChunk);
+            momentum_march_x2_kernel<<<pg, pblk, 0, s>>>(d, c, a);
+        } else {
+            g.z = (d.nr + kMomChunk - 1) / kMomChunk;
+            momentum_march_kernel<T><<<g, blk, 0, s>>>(d, c, a);
+        }
     } else if (mode == MODE_FUSED) {
         // two cells per thread along theta
         const dim3 pblk(32, 4, 1);
