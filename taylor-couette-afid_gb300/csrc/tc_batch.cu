@@ -118,15 +118,15 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
 // blocks of 256 threads (smaller tiles fit proportionally more): 4 blocks =
 // 64 registers, 3 = 80, 2 = 128.  As for the single-run kernels, more
 // resident warps beat the few values a thread would otherwise keep in
-// flight; the FP32 march keeps 80 (64 spills), the FP64 radial sweep 80 and
-// the FP64 two-cell momentum body 128.
+// flight; the FP64 radial sweep keeps 80 and the two-cell momentum bodies
+// (FP64 and packed FP32) 128.
 template <typename T> struct EnsBlocks { static constexpr int momentum = 2, radial = 3, ptri = 4; };
-template <> struct EnsBlocks<float> { static constexpr int momentum = 3, radial = 4, ptri = 4; };
+template <> struct EnsBlocks<float> { static constexpr int momentum = 2, radial = 4, ptri = 4; };
 
-// momentum: item = (chunk of kMomChunk radial levels, tile of TPB
-// consecutive (j, i) columns), each thread marching its column in r; for
-// FP64 (no marching) a chunk is one level and a thread a theta-neighbouring
-// pair of cells (momentum_pair)
+// momentum: item = (chunk of kMomChunk radial levels, tile of TPB pairs of
+// theta-neighbouring columns), each thread marching its two columns in r in
+// packed FP32 (momentum_column_x2); for FP64 (no marching) a chunk is one
+// level and a thread a pair of cells (momentum_pair)
 template <typename T>
 __global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
     const long long item = blockIdx.x;

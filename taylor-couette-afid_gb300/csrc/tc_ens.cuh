@@ -26,22 +26,19 @@ enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT,
 
 constexpr double kCflFloor = 0.00000001;   // CalcMaxCFL.F90 starts its maximum here
 
-// Momentum work units of one radial level (or chunk) of a member: columns
-// for the FP32 march, theta-neighbouring cell pairs for FP64 (momentum_pair).
+// Momentum work units of one radial level (FP64) or chunk of kMomChunk
+// levels (FP32 march) of a member: theta-neighbouring cell pairs
+// (momentum_pair, momentum_column_x2).
 template <typename T>
-__host__ __device__ __forceinline__ long long mom_units(long long P) { return MomMarch<T>::value ? P : P / 2; }
+__host__ __device__ __forceinline__ long long mom_units(long long P) { return P / 2; }
 
-// Cell (i, j) of momentum unit u of a member with nt theta cells.
+// Cell (i, j) of the first cell of momentum unit u of a member with nt
+// theta cells (nt is even).
 template <typename T>
 __device__ __forceinline__ void mom_unit_cell(int u, int nt, int& i, int& j) {
-    if (MomMarch<T>::value) {
-        j = (int)((unsigned)u / (unsigned)nt);
-        i = u - j * nt;
-    } else {
-        const int half = nt / 2;
-        j = (int)((unsigned)u / (unsigned)half);
-        i = 2 * (u - j * half);
-    }
+    const int half = nt / 2;
+    j = (int)((unsigned)u / (unsigned)half);
+    i = 2 * (u - j * half);
 }
 
 // The momentum work of unit (i, j) at level/chunk `outer` of substep args ma.
@@ -50,7 +47,7 @@ __device__ __forceinline__ void mom_unit(const Dims& d, const CoefT<T>& cv, cons
                                          int outer) {
     if constexpr (MomMarch<T>::value) {
         const int k0 = outer * kMomChunk;
-        momentum_column(d, cv, ma, i, j, k0, min(k0 + kMomChunk, d.nr));
+        momentum_column_x2(d, cv, ma, i, j, k0, min(k0 + kMomChunk, d.nr));
     } else {
         momentum_pair(d, cv, ma, i, j, outer);
     }

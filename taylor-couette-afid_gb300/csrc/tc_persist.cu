@@ -142,8 +142,8 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         }
         if (!grid_barrier(a)) return;
     }
-    // momentum: (chunk of kMomChunk levels, tile of columns) marching in r;
-    // for FP64 (level, tile of theta-neighbouring cell pairs)
+    // momentum: (chunk of kMomChunk levels, tile of theta-neighbouring column
+    // pairs) marching in r; for FP64 (level, tile of cell pairs)
     for (long long item = blockIdx.x; item < a.items[PH_MOM]; item += gridDim.x) {
         const int m = find_member(table(PH_MOM), n, item);
         const InstT<T>& I = inst[m];
