@@ -591,6 +591,11 @@ __device__ __forceinline__ F2 ld_f2(const float* p) {
     const float2 v = ld(reinterpret_cast<const float2*>(p));
     return mkf2(v.x, v.y);
 }
+// arrays the kernel also writes (ordinary loads)
+__device__ __forceinline__ F2 ldp_f2(const float* p) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    return mkf2(v.x, v.y);
+}
 
 __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
                                                    int i, int j, int k0, int k1) {
@@ -653,6 +658,12 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
         const F2 zp = top ? zc : ld_f2(qz + o + P);
         const F2 pc = ld_f2(pr + o), pjm = ld_f2(pr + o + djm);
         const F2 pim = mkf2(ld(pr + o + dimA), f2x(pc));
+        // the RK memory of this level, loaded with the fields so that its
+        // latency overlaps the explicit terms (below, the compiler could not
+        // move these loads above the previous level's stores)
+        const F2 old_t = a.use_ru ? ldp_f2(a.ru1 + o) : ZERO;
+        const F2 old_r = (a.use_ru && k >= 1) ? ldp_f2(a.ru2 + o) : ZERO;
+        const F2 old_z = (a.use_ru && !top) ? ldp_f2(a.ru3 + o) : ZERO;
 
         const F2 USRC = bc2(ld(c.usrc + k)), USRCP = bc2(ld(c.usrc + kp));
         const F2 tz_sw = (zc + zim) * (tc + tjm);
@@ -724,16 +735,14 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
             } else {
                 d33 = fma2(tp, bc2(ld(c.ap1j + k)), fma2(tc, bc2(ld(c.ac1j + k)), tm * bc2(ld(c.am1j + k))));
             }
-            const F2 old = a.use_ru ? ld_f2(a.ru1 + o) : ZERO;
-            const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old, GADT * ht)));
+            const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old_t, GADT * ht)));
             st_f2(a.rhs_t + o, rhs);
             st_f2(a.ru1 + o, ht);
         }
         // ---- ImplicitAndUpdateQR, faces 1..nr-1
         if (k >= 1) {
             const F2 d33 = fma2(rp, bc2(ld(c.ap2je + k)), fma2(rc, bc2(ld(c.ac2je + k)), rm * bc2(ld(c.am2je + k))));
-            const F2 old = a.use_ru ? ld_f2(a.ru2 + o) : ZERO;
-            const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old, GADT * hr)));
+            const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old_r, GADT * hr)));
             st_f2(a.rhs_r + o, rhs);
             st_f2(a.ru2 + o, hr);
         }
@@ -752,7 +761,7 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
                 d33 = fma2(zp, bc2(ld(c.ap3j + k)), fma2(zc, bc2(ld(c.ac3j + k)), zm * bc2(ld(c.am3j + k))));
             }
             // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
-            const F2 old = top ? hz : (a.use_ru ? ld_f2(a.ru3 + o) : ZERO);
+            const F2 old = top ? hz : old_z;
             const F2 rhs = fma2(pc - pjm, NCFZ, fma2(ALREDT, d33, fma2(RODT, old, GADT * hz)));
             st_f2(a.rhs_z + o, rhs);
             st_f2(a.ru3 + o, hz);

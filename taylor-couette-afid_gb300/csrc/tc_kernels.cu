@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(128) momentum_pair_kernel(Dims d, CoefT<T> c, 
 }
 
 // FP32 march of two theta-neighbouring columns a thread in packed FP32
-// (momentum_column_x2).  124 registers, 4 resident blocks per SM; capping
-// the registers (96 or 80, with spills) measured slower.
-__global__ void __launch_bounds__(128) momentum_march_x2_kernel(Dims d, CoefT<float> c, MomArgs<float> a) {
+// (momentum_column_x2).  Compiled for 4 resident blocks per SM (128
+// registers, no spills; unbounded it takes 153 and fits 3); capping the
+// registers further (96 or 80, with spills) measured slower.
+__global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT<float> c, MomArgs<float> a) {
     if (a.st->halt) return;
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
