@@ -1303,9 +1303,9 @@ struct ffc {
 __device__ __forceinline__ float4 ffc_pack(ffc v) { return make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo); }
 __device__ __forceinline__ ffc ffc_unpack(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
 __device__ __forceinline__ ffv ffv_ld(const float2* p) { const float2 v = ld(p); return {v.x, v.y}; }
-// y = x - l y
+// y = x - l y (x exact in FP32)
 __device__ __forceinline__ ffc ffc_fwd(float2 x, ffv l, ffc y) {
-    return {ff_sub(ff_from(x.x), ff_mul(l, y.re)), ff_sub(ff_from(x.y), ff_mul(l, y.im))};
+    return {ff_add_f(ff_neg(ff_mul(l, y.re)), x.x), ff_add_f(ff_neg(ff_mul(l, y.im)), x.y)};
 }
 // s = (y - u s) di
 __device__ __forceinline__ ffc ffc_back(ffc y, ffv u, ffv di, ffc s) {

@@ -43,6 +43,13 @@ __device__ __forceinline__ ffv ff_add(ffv a, ffv b) {
     return ff_fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
 }
 
+// double-word plus float ("DWPlusFP" of the same paper): 10 operations
+// against 20 for two double words, relative error below 2 u^2
+__device__ __forceinline__ ffv ff_add_f(ffv a, float b) {
+    const ffv s = ff_two_sum(a.hi, b);
+    return ff_fast_two_sum(s.hi, __fadd_rn(a.lo, s.lo));
+}
+
 __device__ __forceinline__ ffv ff_neg(ffv a) { return {-a.hi, -a.lo}; }
 
 __device__ __forceinline__ ffv ff_sub(ffv a, ffv b) { return ff_add(a, ff_neg(b)); }

@@ -52,6 +52,9 @@ int main() {
         long double ea = (long double)val(a), eb = (long double)val(b);
         long double sa = ea + eb, pm = ea * eb;
         if (sa != 0) worst_add = std::fmax(worst_add, (double)fabsl(((long double)val(ff_add(a, b)) - sa) / sa));
+        float fb = (float)db;
+        long double sf = ea + (long double)fb;
+        if (sf != 0) worst_add = std::fmax(worst_add, (double)fabsl(((long double)val(ff_add_f(a, fb)) - sf) / sf));
         if (pm != 0) worst_mul = std::fmax(worst_mul, (double)fabsl(((long double)val(ff_mul(a, b)) - pm) / pm));
     }
     std::printf("add %.3e mul %.3e\n", worst_add, worst_mul);
@@ -74,7 +77,7 @@ int main() {
     // float-float (rhs given in FP32 as in the mixed path)
     static ffv yf[n];
     yf[0] = ff_from((float)r[0]);
-    for (int k = 1; k < n; ++k) yf[k] = ff_sub(ff_from((float)r[k]), ff_mul(to_ff(l[k]), yf[k - 1]));
+    for (int k = 1; k < n; ++k) yf[k] = ff_add_f(ff_neg(ff_mul(to_ff(l[k]), yf[k - 1])), (float)r[k]);
     ffv s = ff_mul(yf[n - 1], to_ff(dinv[n - 1]));
     double err_ff = 0, err_f = 0, xmax = 0;
     static double y32[n];
