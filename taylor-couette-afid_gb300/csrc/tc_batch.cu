@@ -211,16 +211,23 @@ __global__ void __launch_bounds__(128) ens_thinv_kernel(const InstT<T>* inst, co
                      reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
-// z FFT: item = (plane k, kZC consecutive kt columns)
+// z FFT: item = (plane k, ZEns::cols consecutive kt columns)
+// z-FFT block shape of the grouped kernels: columns per item and threads.
+// On the 96-member C4 ensemble (FP32, 7.10 ms a step) 8 columns of 128
+// threads beat 4 x 128 (7.33), 8 x 64 (7.14), 16 x 256 (7.18), 16 x 128
+// (7.23), 8 x 256 (7.42) and 8 x 512 (7.89); FP64 does not depend on it.
+template <typename T> struct ZEns { static constexpr int cols = 4, threads = 128; };
+template <> struct ZEns<float> { static constexpr int cols = 8, threads = 128; };
+
 template <typename T>
-__global__ void __launch_bounds__(128) ens_zfft_kernel(const InstT<T>* inst, const int* prefix, int n, int inv) {
+__global__ void __launch_bounds__(ZEns<T>::threads) ens_zfft_kernel(const InstT<T>* inst, const int* prefix, int n, int inv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const int local = (int)(item - prefix[m]);
-    constexpr int ZC = ZCols<T>::value;
+    constexpr int ZC = ZEns<T>::cols;
     const int groups = (I.d.PH + ZC - 1) / ZC;
     const int kplane = local / groups, g = local - kplane * groups;
     zfft_tile<ZC>(I.d, I.f, I.p.z, I.p.tw_z, inv, g * ZC, kplane, reinterpret_cast<typename V2<T>::type*>(smem_raw));
@@ -322,7 +329,7 @@ int rebuild(tc_ensemble* e) {
         cnt[PH_PTRI] = ceil_div((long long)d.nz * d.PH, TPB);
         cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
         cnt[PH_THINV] = cnt[PH_DIV];
-        cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, ZCols<T>::value);
+        cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, persistent ? ZCols<T>::value : ZEns<T>::cols);
         cnt[PH_FACT] = 1;
         cnt[PH_CFL] = I.vdt ? cnt[PH_CORR] : 0;
         for (int p = 0; p < PH_COUNT; ++p) {
@@ -334,7 +341,7 @@ int rebuild(tc_ensemble* e) {
     for (int p = 0; p < PH_COUNT; ++p) e->items[p] = prefix[(size_t)p * (n + 1) + n];
     typedef typename V2<T>::type C2;
     e->smem_div = (size_t)2 * R * maxM * sizeof(C2);
-    e->smem_z = (size_t)2 * ZCols<T>::value * maxNz * sizeof(C2);
+    e->smem_z = (size_t)2 * (persistent ? ZCols<T>::value : ZEns<T>::cols) * maxNz * sizeof(C2);
     if (e->smem_div > 200 * 1024 || e->smem_z > 200 * 1024) return efail(e, 2011, "ensemble FFT tile exceeds shared memory");
     cudaError_t c = cudaMalloc(&e->inst_dev, sizeof(InstT<T>) * n);
     if (c == cudaSuccess) c = cudaMalloc(&e->prefix_dev, sizeof(int) * prefix.size());
@@ -423,9 +430,9 @@ int enqueue_step(tc_ensemble* e) {
             case 16: launch_div<16, T>(e, I, P(PH_DIV), n, sub); break;
             default: launch_div<32, T>(e, I, P(PH_DIV), n, sub); break;
         }
-        ens_zfft_kernel<T><<<e->items[PH_ZFFT], 128, e->smem_z, s>>>(I, P(PH_ZFFT), n, 0);
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 0);
         ens_ptri_kernel<T><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
-        ens_zfft_kernel<T><<<e->items[PH_ZFFT], 128, e->smem_z, s>>>(I, P(PH_ZFFT), n, 1);
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 1);
         switch (e->rows_used) {
             case 1: launch_thinv<1, T>(e, I, P(PH_THINV), n); break;
             case 2: launch_thinv<2, T>(e, I, P(PH_THINV), n); break;
