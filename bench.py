@@ -171,9 +171,10 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_sample(workload: str, seconds: float, threads: int):
+def cpu_sample(workload: str, seconds: float, threads: int, nr_cap: int = 48):
     """Time the CPU oracle on a bounded sample of the workload: the same theta
-    x z plane with the radial extent cut so one step takes a second or so."""
+    x z plane with the radial extent cut (to nr_cap cells) so one step takes a
+    second or so."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import tc_ref
     import __graft_entry__ as entry
@@ -182,7 +183,7 @@ def cpu_sample(workload: str, seconds: float, threads: int):
     tc_ref.build()
     tc_ref.set_threads(threads)
     w = dict(WORKLOADS[workload])
-    nr_sample = min(w["nrm"], 48)
+    nr_sample = min(w["nrm"], nr_cap)
     w["nrm"] = nr_sample
     bou = base_bou(**w)
     st = ini.couette_noise(bou, seed=1234)
@@ -631,6 +632,11 @@ def main():
         cpu = {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
                "sample": f"{n} steps of a {sb['nthm']}x{sb['nzm']}x{sb['nrm']} slab of the workload "
                          f"({el:.1f} s, C++ oracle, OpenMP on all host cores)"}
+        # the same oracle on one core, on a thinner slab (serial baseline)
+        v1, n1, el1, sb1 = cpu_sample(args.workload, min(args.cpu_seconds, 6.0), 1, nr_cap=8)
+        cpu["serial"] = {"value": v1, "unit": "Mcell-steps/s", "cores": 1,
+                         "sample": f"{n1} steps of a {sb1['nthm']}x{sb1['nzm']}x{sb1['nrm']} slab "
+                                   f"({el1:.1f} s, C++ oracle, one thread)"}
 
     line = {
         "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
