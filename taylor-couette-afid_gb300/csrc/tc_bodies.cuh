@@ -580,13 +580,16 @@ __device__ __forceinline__ void momentum_pair(const Dims& d, const CoefT<T>& c, 
     implicit_cell(d, c, a, Sb, i + 1, j, k, ht[1], hr[1], hz[1]);
 }
 
-// momentum_column for the two theta-neighbouring columns (i, j) and
-// (i+1, j), i even, in packed FP32 (tc_f32x2.cuh): every F2 holds cell i in
-// its first lane and cell i+1 in its second, so one packed instruction does
-// the arithmetic of both cells; centre values load as float2, and the
-// theta neighbours are the other lane of the pair plus one scalar load each
-// side.  The terms are momentum_column's, with the multiply-adds written
-// out: (A^2 - B^2) of h11 and h33 as (A - B)(A + B).  FP32 mixed path only.
+// The fused momentum work (explicit terms and implicit right-hand sides of
+// all three components, as momentum_cell with MODE_FUSED) of the levels
+// k0 <= k < k1 of the two theta-neighbouring columns (i, j) and (i+1, j),
+// i even, marching outwards in r (see kMomChunk below), in packed FP32
+// (tc_f32x2.cuh): every F2 holds cell i in its first lane and cell i+1 in
+// its second, so one packed instruction does the arithmetic of both cells;
+// centre values load as float2, and the theta neighbours are the other lane
+// of the pair plus one scalar load each side.  The terms are those of
+// explicit_qt/qr/qz and implicit_cell with the multiply-adds written out:
+// (A^2 - B^2) of h11 and h33 as (A - B)(A + B).  FP32 mixed path only.
 __device__ __forceinline__ F2 ld_f2(const float* p) {
     const float2 v = ld(reinterpret_cast<const float2*>(p));
     return mkf2(v.x, v.y);
@@ -774,190 +777,19 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
     }
 }
 
-// The fused momentum work (explicit terms and implicit right-hand sides of
-// all three components, as momentum_cell with MODE_FUSED) for the cells
-// k0 <= k < k1 of column (i, j), marching outwards in r.  Values of planes
-// k-1 and k that the next level needs again stay in registers, and so do the
-// radial fluxes of the face between two levels: the lower-face flux of h12d,
-// h22 and h32 at level k is the upper-face flux of level k-1, the same
-// products of the same sums.  The arithmetic of every term is otherwise
-// momentum_cell's.
+// The FP32 fused momentum work marches in r: a thread takes a chunk of
+// kMomChunk radial levels of its columns, keeping the values of planes k-1
+// and k that the next level needs in registers, and the radial fluxes of the
+// face between two levels (the lower-face flux of h12d, h22 and h32 at level
+// k is the upper-face flux of level k-1).  It is bound by instruction issue
+// and gains from the marching (fewer loads and address computations) and
+// from packed FP32 (momentum_column_x2).  The FP64 kernels are bound by the
+// FP64 pipe: they keep one level a thread and share the face terms of two
+// theta-neighbouring cells instead (momentum_pair).
 constexpr int kMomChunk = 32;   // radial levels per thread
-
-// The fused momentum form each element type uses: the FP32 kernels are bound
-// by instruction issue and gain from the marching (fewer loads and address
-// computations); the FP64 kernels are bound by the FP64 pipe, and the
-// marching kernel's larger register footprint (128 vs 72) costs them more
-// occupancy than its few saved FP64 operations give back, so FP64 keeps one
-// thread per cell.
 template <typename T> struct MomMarch { static constexpr bool value = false; };
 template <> struct MomMarch<float> { static constexpr bool value = true; };
 
-template <typename T>
-__device__ __forceinline__ void momentum_column(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
-                                                int k0, int k1) {
-    const int nr = d.nr, nt = d.nt, nz = d.nz;
-    const int P = (int)d.P;
-    const int dim = i == 0 ? nt - 1 : -1, dip = i == nt - 1 ? 1 - nt : 1;
-    const int djm = j == 0 ? (nz - 1) * nt : -nt, djp = j == nz - 1 ? -(nz - 1) * nt : nt;
-    const size_t col = (size_t)j * nt + i;
-    const T one = (T)1.0, two = (T)2.0;
-    // gam dt, rom dt, alre dt; the pressure terms use the per-level dt al
-    // metric products of the correction (a.cf), so no factor dt remains
-    const T gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
-    const int nrr = nr + 1;
-    const T fic = a.icyl ? (T)a.icyl[col] : one, foc = one;
-    const T udxz = a.udxz, udxzq = a.udxzq;
-
-    // level k0 and its lower neighbours
-    size_t o = (size_t)k0 * P + col;
-    const int km0 = k0 > 0 ? k0 - 1 : 0;
-    const size_t om = (size_t)km0 * P + col;
-    T qt_c = ld(a.qt + o), qt_m = ld(a.qt + om), qt_mip = ld(a.qt + om + dip);
-    T qr_c = ld(a.qr + o), qr_im = ld(a.qr + o + dim), qr_jm = ld(a.qr + o + djm);
-    T qr_m = k0 > 0 ? ld(a.qr + om) : (T)0;
-    T qz_c = ld(a.qz + o), qz_m = ld(a.qz + om), qz_mjp = ld(a.qz + om + djp);
-    T pr_m = k0 > 0 ? ld(a.pr + om) : (T)0;
-    // fluxes through the lower face of level k0 (recomputed at a chunk start)
-    T U12, Uz, Gup;
-    {
-        const T rc2 = qr_c + qr_im;
-        U12 = rc2 * (qt_c + qt_m);                         // D12(k0): t_km = qt(kmm)
-        Uz = (qr_c + qr_jm) * (qz_c + qz_m);                // Dz(k0)
-        const T usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : (T)0;
-        Gup = (qr_c * usrc + qr_m * usrcm) * (qr_c + qr_m);   // Gdn(k0), used for k0 >= 1
-    }
-    for (int k = k0; k < k1; ++k, o += P) {
-        const bool top = k == nr - 1;
-        // lower-face fluxes of this level: the theta-r product of h12d is also
-        // the second product of h21, the r-z product of h32 that of h23
-        const T U12lo = U12, Uzlo = Uz;
-        const int kp = k + 1;
-        // fresh loads of level k (neighbours) and k+1 (column)
-        const T qt_ip = ld(a.qt + o + dip), qt_im = ld(a.qt + o + dim);
-        const T qt_jp = ld(a.qt + o + djp), qt_jm = ld(a.qt + o + djm), qt_jmip = ld(a.qt + o + djm + dip);
-        const T qt_p = top ? qt_c : ld(a.qt + o + P);
-        const T qr_ip = ld(a.qr + o + dip), qr_jp = ld(a.qr + o + djp);
-        const T qr_p = ld(a.qr + o + P), qr_pim = ld(a.qr + o + P + dim), qr_pjm = ld(a.qr + o + P + djm);
-        const T qz_ip = ld(a.qz + o + dip), qz_im = ld(a.qz + o + dim);
-        const T qz_jp = ld(a.qz + o + djp), qz_jm = ld(a.qz + o + djm), qz_jpim = ld(a.qz + o + djp + dim);
-        const T qz_p = top ? qz_c : ld(a.qz + o + P);
-        const T p_c = ld(a.pr + o), p_im = ld(a.pr + o + dim), p_jm = ld(a.pr + o + djm);
-
-        const T usrc = ld(c.usrc + k), usrcp = ld(c.usrc + kp);
-        // (qz + qz(i-1)) (qt + qt(j-1)): the second product of h13 and of h31
-        const T tz_sw = (qz_c + qz_im) * (qt_c + qt_jm);
-        // ---- ExplicitTermsQT (momentum_cell / explicit_qt)
-        T ht;
-        {
-            const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-            const T h11 = ((qt_ip + qt_c) * (qt_ip + qt_c) - (qt_c + qt_im) * (qt_c + qt_im)) * udxt;
-            const T rp2 = qr_p + qr_pim, rc2 = qr_c + qr_im;
-            const T up = rp2 * (qt_p + qt_c);
-            const T h12d = (up - U12) * ld(c.q_udx2rm + k);
-            U12 = up;
-            const T qrs = rp2 * usrcp + rc2 * usrc;      // shared by h12n and the Coriolis term
-            const T h12n = qt_c * ld(c.q_usrm + k) * qrs;
-            const T h13 = ((qz_jp + qz_jpim) * (qt_jp + qt_c) - tz_sw) * udxz;
-            const T d11qt = (qt_ip - two * qt_c + qt_im) * udxtq;
-            const T d22qt = (qt_jp - two * qt_c + qt_jm) * udxzq;
-            const T qre = qr_p * usrcp + qr_c * usrc;
-            const T qrw = qr_pim * usrcp + qr_im * usrc;
-            const T d11qre = (qre - qrw) * ld(c.h_udx1vis1 + k);
-            const T coriol = -qrs * a.q_romeg;
-            ht = -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
-        }
-        // ---- ExplicitTermsQR at face k (1 <= k)
-        T hr = 0;
-        {
-            const T rup = (qr_p * usrcp + qr_c * usrc) * (qr_p + qr_c);
-            if (k >= 1) {
-                const T udxt = ld(c.udxt_c + k), udxtq = ld(c.udxtq_c + k);
-                const T qr_im_ = qr_im;
-                const T sa = qt_ip + qt_mip, sb = qt_c + qt_m, s4 = sa + sb;
-                const T aa = s4 * (T)0.25;
-                const T h11n = aa * aa;
-                const T h21 = (sa * (qr_ip + qr_c) - U12lo) * udxt;
-                const T h22 = (rup - Gup) * ld(c.q_udx2c + k);
-                const T h23 = ((qz_jp + qz_mjp) * (qr_jp + qr_c) - Uzlo) * udxz;
-                const T d11qre = -(sa - sb) * ld(c.udx1vis2 + k);
-                const T d11qr = (qr_ip - two * qr_c + qr_im_) * udxtq;
-                const T d22qr = (qr_jp - two * qr_c + qr_jm) * udxzq;
-                const T coriol = s4 * ld(c.q_rc_romeg + k);
-                hr = -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
-            }
-            Gup = rup;
-        }
-        // ---- ExplicitTermsQZ
-        T hz;
-        {
-            const T udxt = ld(c.udxt_m + k), udxtq = ld(c.udxtq_m + k);
-            const T h31 = ((qt_ip + qt_jmip) * (qz_ip + qz_c) - tz_sw) * udxt;
-            const T upz = (qr_p + qr_pjm) * (qz_p + qz_c);
-            const T h32 = (upz - Uz) * ld(c.q_udx2rm + k);
-            Uz = upz;
-            const T h33 = ((qz_jp + qz_c) * (qz_jp + qz_c) - (qz_c + qz_jm) * (qz_c + qz_jm)) * udxz;
-            const T dqz1 = (qz_im - two * qz_c + qz_ip) * udxtq;
-            const T dqz2 = (qz_jm - two * qz_c + qz_jp) * udxzq;
-            hz = -(h31 + h32 + h33) + dqz1 + dqz2;
-        }
-        // ---- ImplicitAndUpdateQT
-        {
-            T d33;
-            if (k == 0) {
-                const T app = ld(c.ap1j);
-                const T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
-                const T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
-                d33 = qt_p * app + qt_c * acc + (a.virotint + step_vinner<T>(a.st)) * amm;
-            } else if (top) {
-                const T amm = ld(c.am1j + k);
-                const T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
-                const T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
-                d33 = a.virotext * app + qt_c * acc + qt_m * amm;
-            } else {
-                d33 = qt_p * ld(c.ap1j + k) + qt_c * ld(c.ac1j + k) + qt_m * ld(c.am1j + k);
-            }
-            const T dpx11 = (p_c - p_im) * ld(a.cf + k);
-            const T old = a.use_ru ? a.ru1[o] : (T)0;
-            a.rhs_t[o] = gadt * ht + rodt * old + alredt * d33 - dpx11;
-            a.ru1[o] = ht;
-        }
-        // ---- ImplicitAndUpdateQR, faces 1..nr-1
-        if (k >= 1) {
-            const T d33 = qr_p * ld(c.ap2je + k) + qr_c * ld(c.ac2je + k) + qr_m * ld(c.am2je + k);
-            const T dpx22 = (p_c - pr_m) * ld(a.cf + nrr + k);
-            const T old = a.use_ru ? a.ru2[o] : (T)0;
-            a.rhs_r[o] = gadt * hr + rodt * old + alredt * d33 - dpx22;
-            a.ru2[o] = hr;
-        }
-        // ---- ImplicitAndUpdateQZ
-        {
-            T d33;
-            if (k == 0) {
-                const T app = ld(c.ap3j);
-                const T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
-                const T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
-                d33 = qz_p * app + qz_c * acc + qz_c * amm;
-            } else if (top) {
-                const T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
-                const T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
-                d33 = qz_c * app + qz_c * acc + qz_m * ld(c.am3j + k);
-            } else {
-                d33 = qz_p * ld(c.ap3j + k) + qz_c * ld(c.ac3j + k) + qz_m * ld(c.am3j + k);
-            }
-            const T dpx33 = (p_c - p_jm) * ld(a.cf + 2 * nrr);
-            // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
-            const T old = top ? hz : (a.use_ru ? a.ru3[o] : (T)0);
-            a.rhs_z[o] = gadt * hz + rodt * old + alredt * d33 - dpx33;
-            a.ru3[o] = hz;
-        }
-        // march: level k becomes the lower neighbour of level k+1
-        qt_m = qt_c; qt_mip = qt_ip; qt_c = qt_p;
-        qr_m = qr_c; qr_c = qr_p; qr_im = qr_pim; qr_jm = qr_pjm;
-        qz_m = qz_c; qz_mjp = qz_jp; qz_c = qz_p;
-        pr_m = p_c;
-    }
-}
 
 // One LU-factored tridiagonal along r for one column: forward elimination
 // into rhs (y_k0 = (rhs_k0 + extra) sc_k0, y_k = rhs_k sc_k - l_k y_k-1),

@@ -151,17 +151,6 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
     momentum_column_x2(d, c, a, i, j, k0, k1);
 }
 
-// Compiled for 8 resident blocks per SM: 64 registers without spills (the
-// unbounded allocation took 80, leaving 6 blocks, and ran 14 % slower).
-template <typename T>
-__global__ void __launch_bounds__(128, 8) momentum_march_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
-    if (a.st->halt) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= d.nt || j >= d.nz) return;
-    const int k0 = blockIdx.z * kMomChunk, k1 = min(k0 + kMomChunk, d.nr);
-    momentum_column(d, c, a, i, j, k0, k1);
-}
 
 // --------------------------------------------------------------------------
 // Radial implicit solves, one thread per (z, theta) column and component
@@ -616,21 +605,17 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
     MomArgs<T> a = make_mom_args(k, f, sub);
     dim3 blk;
     dim3 g = cell_grid(d, blk);
-    if (mode == MODE_FUSED && MomMarch<T>::value) {
-        if constexpr (std::is_same<T, float>::value) {
-            const dim3 pblk(32, 4, 1);
+    if (mode == MODE_FUSED) {
+        // two theta-neighbouring cells (FP64) or columns (FP32 march) a thread
+        const dim3 pblk(32, 4, 1);
+        if constexpr (MomMarch<T>::value) {
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y,
                           (d.nr + kMomChunk - 1) / kMomChunk);
             momentum_march_x2_kernel<<<pg, pblk, 0, s>>>(d, c, a);
         } else {
-            g.z = (d.nr + kMomChunk - 1) / kMomChunk;
-            momentum_march_kernel<T><<<g, blk, 0, s>>>(d, c, a);
+            const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
+            momentum_pair_kernel<T><<<pg, pblk, 0, s>>>(d, c, a);
         }
-    } else if (mode == MODE_FUSED) {
-        // two cells per thread along theta
-        const dim3 pblk(32, 4, 1);
-        const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
-        momentum_pair_kernel<T><<<pg, pblk, 0, s>>>(d, c, a);
     }
     else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
     else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
