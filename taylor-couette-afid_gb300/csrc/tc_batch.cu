@@ -79,6 +79,7 @@ __global__ void ens_init_kernel(StepState* st, double dt, double time, int ntime
     st->halt = 0;
     st->errorcode = 0;
     st->instcfl = kCflFloor;
+    st->dt_factored = __longlong_as_double(0x7ff8000000000000LL);   // NaN: factor on the first step
 }
 
 // CalcMaxCFL of the variable-dt members: item = (k, tile of cells); block

@@ -122,12 +122,24 @@ template <> __device__ __forceinline__ float step_vinner<float>(const StepState*
 // FP64 (Fd, corrd); for the mixed path the results are then rounded into the
 // FP32 copies F, corr.  One block.
 template <typename T>
-__device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, const StepState* st,
+__device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, StepState* st,
                              const MomFactorsT<double>& Fd, double* corrd, double* scal, const MomFactorsT<T>& F,
                              T* corr) {
     const int nr = d.nr;
     const double beta = st->beta, dt = st->dt;
     const int nsub = k.nsst;
+    if (st->dt_factored == dt) {
+        // the factors, correction coefficients and scales depend on dt only:
+        // keep them, and update the inner-wall term of this step
+        // (SolveImpEqnUpdate_QT.F90:67), which follows dvinner_t
+        if (threadIdx.x < nsub) {
+            const int s = threadIdx.x;
+            const double ex = 0.5 * k.alm[s] * dt * st->dvinner_t * c.am1j[0] / k.ren;
+            *Fd.extra(s) = ex;
+            if (!std::is_same<T, double>::value) *F.extra(s) = (T)ex;
+        }
+        return;
+    }
     // phase 1: row entries (parallel over rows)
     for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
         int row = t % nr, chain = t / nr;        // chain: 0,1 = qt v0/v1; 2 = qr; 3,4 = qz v0/v1
@@ -183,7 +195,7 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, cons
         di[k0] = 1.0;
         if (cidx == 1) l[1] = 0.0;   // couples to the wall value qr(1) = 0
         for (int row = k0 + 1; row < nr; ++row) {
-            double fact = l[row] / dp;
+            const double fact = l[row] / dp;
             l[row] = fact;
             dp = 1.0 - fact * u[row - 1];
             di[row] = dp;
@@ -215,6 +227,8 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, cons
         for (int t = threadIdx.x; t < nF; t += blockDim.x) F.base[t] = (T)Fd.base[t];
         for (int t = threadIdx.x; t < nC; t += blockDim.x) corr[t] = (T)corrd[t];
     }
+    __syncthreads();
+    if (threadIdx.x == 0) st->dt_factored = dt;
 }
 
 // Neighbour offsets of cell (i, j, k) relative to its own index o, in

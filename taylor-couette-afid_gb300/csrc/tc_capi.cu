@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -339,6 +340,9 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     ce = cudaMallocHost((void**)&h->st_host, sizeof(StepState));
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "pinned allocation"); tc_destroy(h); return r; }
     std::memset(h->st_host, 0, sizeof(StepState));
+    h->st_host->dt_factored = std::numeric_limits<double>::quiet_NaN();   // no factors yet
+    ce = cudaMemcpy(h->st, h->st_host, sizeof(StepState), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "state upload"); tc_destroy(h); return r; }
 
     launch_pressure_factors(h->stream, d, h->c, pl, pdv);
     if (h->mixed) {

@@ -107,6 +107,9 @@ struct StepState {
     // dt, beta and vinner_t rounded once per step for the FP32 kernels of the
     // mixed path (so that they do not convert per cell)
     float dt_f, beta_f, vinner_f, pad_f;
+    // dt of the momentum factors now in place (the factors kernel skips the
+    // factorisation while dt does not change)
+    double dt_factored;
 };
 
 // Checkpointed forward sweep of the mixed path's pressure solve (ptri_ff):

@@ -166,6 +166,21 @@ def test_patterned_slip(gpu_lib, oracle):
     g.close()
 
 
+def test_dt_changes_between_steps(gpu_lib, oracle):
+    """The momentum factors are kept while dt repeats and rebuilt when it
+    changes; the inner-wall oscillation (SIZEPERT, OMEGAPERT) changes the
+    wall term of every step, cached factors or not."""
+    bou = make_bou(nthm=32, nzm=24, nrm=20, istr=4, str=3.0, sizepert=0.1, omegapert=0.5)
+    g, o, _ = pair(oracle, bou)
+    t = 0.0
+    for dt in (1e-3, 1e-3, 5e-4, 5e-4, 1e-3, 7e-4):
+        g.time_marcher(dt, t)
+        o.time_marcher(dt, t)
+        t += dt
+    compare_state(g, o, 1e-11, bou["nrm"])
+    g.close()
+
+
 def test_state_round_trip(gpu_lib):
     bou = make_bou(nthm=24, nzm=18, nrm=10)
     st = ini.couette_noise(bou, seed=3)
