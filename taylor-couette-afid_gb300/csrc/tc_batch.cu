@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
     const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
     if (flat >= I.d.P) return;
     const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
-    correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, k);
+    correct_cell<true, true, T>(I.d, I.f, sub, i, j, k);
 }
 
 // column-wise: item = (component, TPB consecutive (z, theta) columns)
@@ -319,7 +319,6 @@ int rebuild(tc_ensemble* e) {
         I.d = h->d; I.cv = MC<T>(h); I.c = h->c; I.k = h->k; I.f = MF<T>(h); I.p = MP<T>(h);
         for (int s = 0; s < 3; ++s) I.ma[s] = make_mom_args(h->k, I.f, s);
         I.vdt = e->vdt[e->active[a]];
-        I.dxzq_t = (T)h->k.dxzq;
         const Dims& d = h->d;
         maxNz = std::max(maxNz, d.nz);
         long long cnt[PH_COUNT];

@@ -179,6 +179,15 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
                 corrd[9 * (nr + 1) + s * 3 + 1] = k.rom[s] * dt;
                 corrd[9 * (nr + 1) + s * 3 + 2] = k.alre[s] * dt;
             }
+            if (s == 0) {
+                // CorrectPressure coefficients of the step (one set for all substeps)
+                double* pc = corrd + kPresCoef(nr + 1);
+                const double u = c.udx1qm[row];
+                pc[row] = beta * (2.0 * u + 2.0 * k.dxzq - c.acph[row]);
+                pc[(nr + 1) + row] = -beta * u;
+                pc[2 * (nr + 1) + row] = -beta * c.apph[row];
+                if (row == 0) pc[3 * (nr + 1)] = -beta * k.dxzq;
+            }
         }
     }
     __syncthreads();
@@ -219,6 +228,25 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
         if (cidx == 1 && row == 0) continue;
         double* di = Fd.dinv(s, cidx, v);
         di[row] = 1.0 / di[row];
+    }
+    __syncthreads();
+    // phase 3b: fold the row scales sc into the factors, so that the sweeps
+    // solve for y'_k = y_k / sc_k: y'_k = rhs_k - l'_k y'_k-1 and
+    // x_k = (y'_k - u'_k x_k+1) di'_k with l'_k = l_k sc_k-1 / sc_k,
+    // u'_k = u_k / sc_k, di'_k = di_k sc_k (one multiplication a level less)
+    for (int t = threadIdx.x; t < nsub * 5 * nr; t += blockDim.x) {
+        int row = t % nr, chain = t / nr;
+        int s = chain / 5, ch = chain % 5;
+        int cidx = ch < 2 ? 0 : (ch == 2 ? 1 : 2);
+        int v = (ch == 1 || ch == 4) ? 1 : 0;
+        const int k0 = (cidx == 1) ? 1 : 0;
+        if (row < k0) continue;
+        const double* sc = Fd.scale(s, cidx);
+        const double scr = sc[row];
+        double* l = Fd.l(s, cidx, v);
+        if (row > k0) l[row] = l[row] * sc[row - 1] / scr;
+        Fd.u(s, cidx, v)[row] = Fd.u(s, cidx, v)[row] / scr;
+        Fd.dinv(s, cidx, v)[row] = Fd.dinv(s, cidx, v)[row] * scr;
     }
     // phase 4 (mixed path): round the factors into the FP32 copies
     if (!std::is_same<T, double>::value) {
@@ -805,9 +833,10 @@ template <typename T> struct MomMarch { static constexpr bool value = false; };
 template <> struct MomMarch<float> { static constexpr bool value = true; };
 
 
-// One LU-factored tridiagonal along r for one column: forward elimination
-// into rhs (y_k0 = (rhs_k0 + extra) sc_k0, y_k = rhs_k sc_k - l_k y_k-1),
-// then back substitution adding the solution to q.  Planes are loaded in
+// One LU-factored tridiagonal along r for one column, with the row scales
+// folded into the factors: forward elimination into rhs (y_k0 = rhs_k0 +
+// extra, y_k = rhs_k - l_k y_k-1), then back substitution
+// (x_k = (y_k - u_k x_k+1) di_k) adding the solution to q.  Planes are loaded in
 // batches of kRB ahead of the dependent arithmetic, so that each thread keeps
 // several loads in flight (the recurrence itself is sequential).
 constexpr int kRB = 8;
@@ -815,8 +844,8 @@ constexpr int kRBr = 16;   // planes per batch in the radial momentum sweeps
 
 template <bool EXTRA, typename T>
 __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
-                                          const T* l, const T* di, const T* u, const T* sc, T extra) {
-    T y = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
+                                          const T* l, const T* di, const T* u, T extra) {
+    T y = EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P];
     rhs[(size_t)k0 * P] = y;
     int k = k0 + 1;
     for (; k + kRBr <= nr; k += kRBr) {
@@ -825,12 +854,12 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
         for (int b = 0; b < kRBr; ++b) r[b] = rhs[(size_t)(k + b) * P];
 #pragma unroll
         for (int b = 0; b < kRBr; ++b) {
-            y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
+            y = r[b] - ld(l + k + b) * y;
             rhs[(size_t)(k + b) * P] = y;
         }
     }
     for (; k < nr; ++k) {
-        y = rhs[(size_t)k * P] * ld(sc + k) - ld(l + k) * y;
+        y = rhs[(size_t)k * P] - ld(l + k) * y;
         rhs[(size_t)k * P] = y;
     }
     T x = y * ld(di + nr - 1);
@@ -872,8 +901,8 @@ constexpr int kCkpt = 8;
 
 template <bool EXTRA, typename T>
 __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
-                                               const T* l, const T* di, const T* u, const T* sc, T extra) {
-    const T y0 = (EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P]) * ld(sc + k0);
+                                               const T* l, const T* di, const T* u, T extra) {
+    const T y0 = EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P];
     rhs[(size_t)k0 * P] = y0;
     T y = y0;
     // full batches [k0 + 1 + kCkpt m, k0 + kCkpt (m + 1)], checkpoint at their top
@@ -884,12 +913,12 @@ __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restric
 #pragma unroll
         for (int b = 0; b < kCkpt; ++b) r[b] = rhs[(size_t)(k + b) * P];
 #pragma unroll
-        for (int b = 0; b < kCkpt; ++b) y = r[b] * ld(sc + k + b) - ld(l + k + b) * y;
+        for (int b = 0; b < kCkpt; ++b) y = r[b] - ld(l + k + b) * y;
         rhs[(size_t)(k + kCkpt - 1) * P] = y;
     }
     // tail levels: every y stored
     for (; k < nr; ++k) {
-        y = rhs[(size_t)k * P] * ld(sc + k) - ld(l + k) * y;
+        y = rhs[(size_t)k * P] - ld(l + k) * y;
         rhs[(size_t)k * P] = y;
     }
     // back substitution: the tail from its stored y
@@ -912,7 +941,7 @@ __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restric
         for (int b = 0; b < kCkpt; ++b) v[b] = q[(size_t)(kb + b) * P];
 #pragma unroll
         for (int b = 0; b < kCkpt - 1; ++b) {
-            yc = yb[b] * ld(sc + kb + b) - ld(l + kb + b) * yc;
+            yc = yb[b] - ld(l + kb + b) * yc;
             yb[b] = yc;
         }
         // yb[kCkpt - 1] is the stored checkpoint y of the batch's top level
@@ -944,24 +973,22 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
     if constexpr (std::is_same<T, float>::value) {
         if (comp == 0)
             lu_column_ckpt<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v),
-                                 F.u(sub, 0, v), F.scale(sub, 0), *F.extra(sub));
+                                 F.u(sub, 0, v), *F.extra(sub));
         else if (comp == 1)
             lu_column_ckpt<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0),
-                                  F.u(sub, 1, 0), F.scale(sub, 1), (T)0);
+                                  F.u(sub, 1, 0), (T)0);
         else
             lu_column_ckpt<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v),
-                                  F.u(sub, 2, v), F.scale(sub, 2), (T)0);
+                                  F.u(sub, 2, v), (T)0);
         return;
     }
     if (comp == 0)
         lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
-                        F.scale(sub, 0), *F.extra(sub));
+                        *F.extra(sub));
     else if (comp == 1)
-        lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0),
-                         F.scale(sub, 1), (T)0);
+        lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0), (T)0);
     else
-        lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v),
-                         F.scale(sub, 2), (T)0);
+        lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v), (T)0);
 }
 
 __device__ __forceinline__ double2 ld2(const double* p) { return ld(reinterpret_cast<const double2*>(p)); }
@@ -1274,8 +1301,7 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
 }
 
 template <bool VEL, bool PRES, typename T>
-__device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, const CoefT<T>& cv, double dxzq, T dxzq_t,
-                                             const FieldsT<T>& f, int sub, int i, int j, int k) {
+__device__ __forceinline__ void correct_cell(const Dims& d, const FieldsT<T>& f, int sub, int i, int j, int k) {
     const int nt = d.nt, nr = d.nr;
     const size_t P = (size_t)d.P;
     const int im = wm(i, nt), ip = wp(i, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
@@ -1293,30 +1319,25 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const Coef& c, const
         f.qz[o] -= (loc - pjm) * ld(cf + 2 * (nr + 1));
     }
     if (PRES) {
+        // CorrectPressure.F90:40-44 with the coefficients of the step
+        // (factors kernel): pr + phi - be lap(phi) = pr + phi + pe phi
+        // + pt (phi_ip + phi_im) + pz (phi_jp + phi_jm) + pq (phi_kp + phi_km),
+        // where the reference's amm = apph(kc) makes both radial neighbours
+        // share one coefficient
+        const T pip = ld(phi + (size_t)k * P + rowoff + ip);
+        const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
+        const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
+        const T* pc = f.corr + kPresCoef(nr + 1);
+        T inc = loc + ld(pc + k) * loc;
+        inc += ld(pc + (nr + 1) + k) * (pip + pim);
+        inc += ld(pc + 3 * (nr + 1)) * (pjp + pjm);
+        inc += ld(pc + 2 * (nr + 1) + k) * (pkp + pkm);
         if (std::is_same<T, double>::value) {
-            const double pip = ld(phi + (size_t)k * P + rowoff + ip);
-            const double pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
-            const double pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
-            const double l0 = loc, im_ = pim, jm_ = pjm, km_ = pkm;
-            const double be = f.st->beta;
-            const double app = ld(c.apph + k), acc = ld(c.acph + k), amm = app;   // amm = apph(kc)
-            f.pr[o] = f.pr[o] + l0 - be * ((pip - 2.0 * l0 + im_) * ld(c.udx1qm + k) +
-                                           (pjp - 2.0 * l0 + jm_) * dxzq +
-                                           (pkp * app + l0 * acc + km_ * amm));
+            f.pr[o] = f.pr[o] + (double)inc;
         } else {
-            // mixed path: the increment phi - beta lap(phi) from the FP32 phi in
-            // FP32, accumulated into the FP64 pressure; the FP32 copy used by
-            // the momentum rhs is refreshed from the FP64 sum
-            // (coefficients from the FP32 copies, conversions on the integer pipes)
-            const T pip = ld(phi + (size_t)k * P + rowoff + ip);
-            const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
-            const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
-            const float be = f.st->beta_f;
-            const T app = ld(cv.apph + k), acc = ld(cv.acph + k), amm = app;   // amm = apph(kc)
-            const T two = (T)2.0;
-            const T inc = loc - be * ((pip - two * loc + pim) * ld(cv.udx1qm + k) +
-                                      (pjp - two * loc + pjm) * dxzq_t +
-                                      (pkp * app + loc * acc + pkm * amm));
+            // mixed path: the increment from the FP32 phi in FP32, accumulated
+            // into the FP64 pressure; the FP32 copy used by the momentum rhs is
+            // refreshed from the FP64 sum (conversions on the integer pipes)
             const double p = f.pr[o] + f2d((float)inc);
             f.pr[o] = p;
             f.prf[o] = (T)d2f(p);

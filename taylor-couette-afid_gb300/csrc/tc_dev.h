@@ -126,8 +126,16 @@ __host__ __device__ inline int ptri_slots(int nr) {
 //                            component c at level k (CorrectVelocity.F90:
 //                            325-330; the momentum right-hand sides use the
 //                            same products for the pressure of the step),
-// [ 9*(nr+1) + s*3 + 0..2 ] gam(s) dt, rom(s) dt, alre(s) dt.
-__host__ __device__ inline size_t kCorrCount(int nrr) { return (size_t)9 * nrr + 9; }
+// [ 9*(nr+1) + s*3 + 0..2 ] gam(s) dt, rom(s) dt, alre(s) dt;
+// and for the pressure of the step (CorrectPressure.F90:40-44 regrouped as
+// pr + phi + pe phi + pt (phi_ip + phi_im) + pz (phi_jp + phi_jm)
+//    + pq (phi_kp + phi_km), be = beta):
+// [ kPresCoef(nr+1) + k ]              pe = be (2 udx1qm + 2 dxzq - acph)
+// [ kPresCoef(nr+1) + (nr+1) + k ]     pt = -be udx1qm
+// [ kPresCoef(nr+1) + 2 (nr+1) + k ]   pq = -be apph
+// [ kPresCoef(nr+1) + 3 (nr+1) ]       pz = -be dxzq
+__host__ __device__ inline size_t kPresCoef(int nrr) { return (size_t)9 * nrr + 9; }
+__host__ __device__ inline size_t kCorrCount(int nrr) { return (size_t)12 * nrr + 10; }
 
 // Factors of the row-scaled momentum matrices of one step: for each substep
 // s (3), component c (0 = qt, 1 = qr, 2 = qz) and slip variant v (0 = no

@@ -19,7 +19,6 @@ struct InstT {
     PlansT<T> p;
     MomArgs<T> ma[3];
     int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
-    T dxzq_t;         // dxzq in the element type
 };
 
 enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };

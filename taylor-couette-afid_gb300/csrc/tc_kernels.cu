@@ -244,18 +244,17 @@ __global__ void __launch_bounds__(kThThreads) theta_inv_kernel(Dims d, FieldsT<T
 
 // --------------------------------------------------------------------------
 // Projection: CorrectVelocity.F90:318-337 (element type T) and
-// CorrectPressure.F90:364-390 (FP64: pr += phi - beta lap(phi))
+// CorrectPressure.F90:40-44 (FP64: pr += phi - beta lap(phi))
 // --------------------------------------------------------------------------
 
 template <bool VEL, bool PRES, typename T>
-__global__ void __launch_bounds__(128) correct_kernel(Dims d, Coef c, CoefT<T> cv, double dxzq, T dxzq_t,
-                                                      FieldsT<T> f, int sub) {
+__global__ void __launch_bounds__(128) correct_kernel(Dims d, FieldsT<T> f, int sub) {
     if (f.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= d.nt || j >= d.nz) return;
-    correct_cell<VEL, PRES, T>(d, c, cv, dxzq, dxzq_t, f, sub, i, j, k);
+    correct_cell<VEL, PRES, T>(d, f, sub, i, j, k);
 }
 
 // CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
@@ -710,10 +709,9 @@ void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>
                     int sub, bool vel, bool pres) {
     dim3 blk;
     dim3 g = cell_grid(d, blk);
-    const T dxzq_t = (T)k.dxzq;
-    if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
-    else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
-    else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, c, cv, k.dxzq, dxzq_t, f, sub);
+    if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, f, sub);
+    else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, f, sub);
+    else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, f, sub);
     TC_LAUNCH_CHECK();
 }
 

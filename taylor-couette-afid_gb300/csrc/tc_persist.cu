@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         const CellItem ci = cell_item(item - table(PH_CORR)[m], I.d.P);
         if (ci.flat < (long long)I.d.P) {
             const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
-            correct_cell<true, true, T>(I.d, I.c, I.cv, I.k.dxzq, I.dxzq_t, I.f, sub, i, j, ci.outer);
+            correct_cell<true, true, T>(I.d, I.f, sub, i, j, ci.outer);
         }
     }
     if (a.flags & PF_END) {
