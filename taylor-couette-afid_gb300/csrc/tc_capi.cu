@@ -82,6 +82,32 @@ std::vector<C2> twiddles(int n, int count) {
     return w;
 }
 
+// The plain table of length n (padded to an even count) followed by the
+// factored forms of the same twiddles for the multiply-add butterflies of
+// tc_fft.cuh: n entries of exp(-2 pi i j / n), then n of exp(+2 pi i j / n),
+// each {g, fx, fy, swap} from the long double cosine and sine.
+template <typename C2>
+std::vector<C2> twiddles_with_factored(int n) {
+    typedef decltype(C2().x) R;
+    const int pad = (n + 1) & ~1;
+    std::vector<C2> w = twiddles<C2>(n, n);
+    w.resize((size_t)pad + 4 * (size_t)n);
+    FTw<R>* f = reinterpret_cast<FTw<R>*>(w.data() + pad);
+    const long double tpi = 6.283185307179586476925286766559L;
+    for (int dir = 0; dir < 2; ++dir)
+        for (int j = 0; j < n; ++j) {
+            const long double a = tpi * (long double)j / (long double)n;
+            const long double c = cosl(a), s = dir == 0 ? -sinl(a) : sinl(a);
+            FTw<R>& e = f[(size_t)dir * n + j];
+            if (fabsl(c) >= fabsl(s)) {
+                e.g = (R)(s / c); e.fx = (R)c; e.fy = (R)c; e.swap = (R)0;
+            } else {
+                e.g = (R)(c / s); e.fx = (R)(-s); e.fy = (R)s; e.swap = (R)1;
+            }
+        }
+    return w;
+}
+
 int check(tc_handle* h) {
     if (!h) return fail(nullptr, 2000, "null handle");
     return 0;
@@ -168,7 +194,8 @@ template <typename T>
 cudaError_t upload_plans(tc_handle* h, PlansT<T>& p) {
     typedef typename V2<T>::type C2;
     const Dims& d = h->d;
-    std::vector<C2> wt = twiddles<C2>(d.M, d.M), wz = twiddles<C2>(d.nz, d.nz), wr = twiddles<C2>(d.nt, d.M + 1);
+    std::vector<C2> wt = twiddles_with_factored<C2>(d.M), wz = twiddles_with_factored<C2>(d.nz),
+                    wr = twiddles<C2>(d.nt, d.M + 1);
     C2 *dwt = nullptr, *dwz = nullptr, *dwr = nullptr;
     cudaError_t ce = dalloc(h, &dwt, wt.size());
     if (ce == cudaSuccess) ce = dalloc(h, &dwz, wz.size());

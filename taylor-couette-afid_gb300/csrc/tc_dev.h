@@ -40,6 +40,13 @@ struct FFTPlan {
     unsigned mn = 0, mn1 = 0;
 };
 
+// A twiddle in the factored form of the FP64 multiply-add butterflies
+// (tc_fft.cuh): w y = (fx (z.x - g z.y), fy (z.y + g z.x)), z = y or, when
+// swap != 0, y with its parts swapped.
+template <typename R> struct FTw {
+    R g, fx, fy, swap;
+};
+
 inline unsigned div_magic(unsigned d) {
     return d <= 1 ? 0u : (unsigned)(((1ull << 32) + d - 1) / d);
 }

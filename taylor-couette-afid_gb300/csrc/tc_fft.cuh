@@ -12,6 +12,8 @@
 // SolvePressureCorrection.F90:61-98 plans use).
 #pragma once
 
+#include <type_traits>
+
 #include "tc_dev.h"
 
 namespace tcgb {
@@ -89,6 +91,84 @@ template <typename C2> __device__ __forceinline__ void dft5(C2* v, bool inv) {
     v[3] = inv ? w2 : w3;
 }
 
+// ---- butterflies in fused multiply-adds (FP64 path) ----------------------
+//
+// The FP64 transforms are bound by the FP64 pipe, so they count FP64
+// instructions.  A twiddle w = c + i s is stored factored (FTw): with
+// z = y, or y with its parts swapped,
+//     w y = (fx (z.x - g z.y), fy (z.y + g z.x)),
+// where |c| >= |s| gives g = s/c, fx = fy = c and no swap, and |s| > |c| gives
+// the swap, g = c/s, fx = -s, fy = s; so |g| <= 1.  The reduced product costs
+// two FMAs and its scale folds into the FMAs that add it to the other input
+// of the butterfly (x +- w y in four FMAs), against a complex product (four)
+// and two complex additions (four) -- the factoring of Linzer and Feig
+// (IBM J. Res. Dev. 1993) and Goedecker (SIAM J. Sci. Comput. 1997) for
+// multiply-add units.  The swap is a register select on the integer pipes.
+// A radix-4 butterfly as two levels of these radix-2 steps,
+//     p, m = a0 +- w^2 a2,  u, v = a1 +- w^2 a3,
+//     X0, X2 = p +- w u,    X1, X3 = m -+ i w v    (forward),
+// costs 24 FP64 instructions against 28.  s = 0 gives g = 0, fx = fy = 1,
+// which reproduces the plain sums exactly.
+template <typename C2> struct CRe;
+template <> struct CRe<double2> { typedef double type; };
+template <> struct CRe<float2> { typedef float type; };
+
+__device__ __forceinline__ FTw<double> ld_ftw(const FTw<double>* p) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ FTw<float> ld_ftw(const FTw<float>* p) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    return {a.x, a.y, a.z, a.w};
+}
+__device__ __forceinline__ bool ftw_swapped(double s) { return __double_as_longlong(s) != 0; }
+__device__ __forceinline__ bool ftw_swapped(float s) { return __float_as_int(s) != 0; }
+__device__ __forceinline__ double fmar(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmar(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// (z.x - g z.y, z.y + g z.x): w y = (fx r.x, fy r.y)
+template <typename C2, typename R>
+__device__ __forceinline__ C2 tw_reduce(C2 y, const FTw<R>& w) {
+    const bool sw = ftw_swapped(w.swap);
+    const R zx = sw ? y.y : y.x, zy = sw ? y.x : y.y;
+    return mk2(fmar(-w.g, zy, zx), fmar(w.g, zx, zy));
+}
+
+// v[0], v[1] = v[0] +- w v[1]
+template <typename C2, typename R>
+__device__ __forceinline__ void bfly2_fma(C2* v, const FTw<R>& w) {
+    const C2 y = tw_reduce(v[1], w);
+    const C2 x = v[0];
+    v[0] = mk2(fmar(w.fx, y.x, x.x), fmar(w.fy, y.y, x.y));
+    v[1] = mk2(fmar(-w.fx, y.x, x.x), fmar(-w.fy, y.y, x.y));
+}
+
+// radix-4 DIT butterfly with twiddles w1 = w, w2 = w^2 (table of the
+// transform's direction); inv selects the sign of i in the outputs
+template <typename C2, typename R>
+__device__ __forceinline__ void bfly4_fma(C2* v, const FTw<R>& w1, const FTw<R>& w2, bool inv) {
+    const C2 y2 = tw_reduce(v[2], w2), y3 = tw_reduce(v[3], w2);
+    const C2 p = mk2(fmar(w2.fx, y2.x, v[0].x), fmar(w2.fy, y2.y, v[0].y));
+    const C2 m = mk2(fmar(-w2.fx, y2.x, v[0].x), fmar(-w2.fy, y2.y, v[0].y));
+    const C2 u = mk2(fmar(w2.fx, y3.x, v[1].x), fmar(w2.fy, y3.y, v[1].y));
+    const C2 d = mk2(fmar(-w2.fx, y3.x, v[1].x), fmar(-w2.fy, y3.y, v[1].y));
+    const C2 yu = tw_reduce(u, w1), yd = tw_reduce(d, w1);
+    v[0] = mk2(fmar(w1.fx, yu.x, p.x), fmar(w1.fy, yu.y, p.y));
+    v[2] = mk2(fmar(-w1.fx, yu.x, p.x), fmar(-w1.fy, yu.y, p.y));
+    // w1 d = (fx yd.x, fy yd.y); -i (w1 d) = (fy yd.y, -fx yd.x)
+    const C2 mi = mk2(fmar(w1.fy, yd.y, m.x), fmar(-w1.fx, yd.x, m.y));   // m - i w1 d
+    const C2 pi = mk2(fmar(-w1.fy, yd.y, m.x), fmar(w1.fx, yd.x, m.y));   // m + i w1 d
+    v[1] = inv ? pi : mi;
+    v[3] = inv ? mi : pi;
+}
+
+// The factored tables of a transform of length n follow its plain table
+// (n entries, padded to an even count): n forward entries, then n inverse.
+template <typename C2>
+__device__ __forceinline__ const FTw<typename CRe<C2>::type>* ftw_table(const C2* tw, int n, bool inv) {
+    return reinterpret_cast<const FTw<typename CRe<C2>::type>*>(tw + ((n + 1) & ~1)) + (inv ? n : 0);
+}
+
 // One Stockham stage of radix p (compile time) over C interleaved lines:
 // sub-DFTs of length L become length L*p.
 // x / d with the plan's multiplier m (m = 0: d = 1).
@@ -97,6 +177,10 @@ __device__ __forceinline__ int fdiv(int x, unsigned m) { return m ? (int)__umulh
 template <int C, int p, typename C2>
 __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restrict__ b, int n, int L, int rp,
                                           unsigned mrp, const C2* __restrict__ tw, bool inv) {
+    typedef typename CRe<C2>::type R;
+    // FP64 radix-4 and radix-2 stages after the first: factored butterflies
+    constexpr bool kFused = std::is_same<R, double>::value && (p == 4 || p == 2);
+    const FTw<R>* ftw = ftw_table(tw, n, inv);
     const int r = rp * p;
     const int nb = (n / p) * C;
     const int istep = rp * C, ostep = rp * L * C;
@@ -108,6 +192,14 @@ __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restri
         C2 v[p];
 #pragma unroll
         for (int cc = 0; cc < p; ++cc) v[cc] = in[cc * istep];
+        if (kFused && L > 1) {
+            const FTw<R> w1 = ld_ftw(ftw + s * rp);
+            if constexpr (p == 4) bfly4_fma(v, w1, ld_ftw(ftw + 2 * s * rp), inv);
+            else bfly2_fma(v, w1);
+#pragma unroll
+            for (int u = 0; u < p; ++u) out[u * ostep] = v[u];
+            continue;
+        }
         if (s != 0) {
 #pragma unroll
             for (int cc = 1; cc < p; ++cc) v[cc] = cmul(v[cc], twiddle(tw, cc * s * rp, inv));
