@@ -1345,6 +1345,63 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const FieldsT<T>& f,
     }
 }
 
+// correct_cell<true, true, float> for the two cells (i, j, k) and (i+1, j, k),
+// i even (nthm is even): the pair's fields move as float2 (pressure as
+// double2), the theta neighbours inside the pair come from the pair itself,
+// so a thread issues half the loads of two single-cell threads.  Same
+// arithmetic, cell by cell, as correct_cell.
+__device__ __forceinline__ void correct_pair_f(const Dims& d, const FieldsT<float>& f, int sub, int i, int j, int k) {
+    const int nt = d.nt, nr = d.nr, nrr = nr + 1;
+    const size_t P = (size_t)d.P;
+    const int im = wm(i, nt), ip1 = wp(i + 1, nt), jm = wm(j, d.nz), jp = wp(j, d.nz);
+    const size_t rowoff = (size_t)j * nt;
+    const size_t o = (size_t)k * P + rowoff + i;
+    const float* phi = f.phi;
+    const float2 L = ld(reinterpret_cast<const float2*>(phi + o));
+    const float pim = ld(phi + (size_t)k * P + rowoff + im);
+    const float pip = ld(phi + (size_t)k * P + rowoff + ip1);
+    const float2 PJm = ld(reinterpret_cast<const float2*>(phi + (size_t)k * P + (size_t)jm * nt + i));
+    const float2 PJp = ld(reinterpret_cast<const float2*>(phi + (size_t)k * P + (size_t)jp * nt + i));
+    const float2 PKm = ld(reinterpret_cast<const float2*>(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i));
+    const float2 PKp = ld(reinterpret_cast<const float2*>(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i));
+    // CorrectVelocity.F90:318-337
+    const float* cf = f.corr + (size_t)sub * 3 * nrr;
+    const float cft = ld(cf + k), cfz = ld(cf + 2 * nrr);
+    float2* qt = reinterpret_cast<float2*>(f.qt + o);
+    float2* qz = reinterpret_cast<float2*>(f.qz + o);
+    float2 vt = *qt, vz = *qz;
+    vt.x -= (L.x - pim) * cft;
+    vt.y -= (L.y - L.x) * cft;
+    vz.x -= (L.x - PJm.x) * cfz;
+    vz.y -= (L.y - PJm.y) * cfz;
+    *qt = vt;
+    *qz = vz;
+    if (k >= 1) {
+        const float cfr = ld(cf + nrr + k);
+        float2* qr = reinterpret_cast<float2*>(f.qr + o);
+        float2 vr = *qr;
+        vr.x -= (L.x - PKm.x) * cfr;
+        vr.y -= (L.y - PKm.y) * cfr;
+        *qr = vr;
+    }
+    // CorrectPressure.F90:40-44 with the coefficients of the step
+    const float* pc = f.corr + kPresCoef(nrr);
+    const float pe = ld(pc + k), pt = ld(pc + nrr + k), pq = ld(pc + 2 * nrr + k), pz = ld(pc + 3 * nrr);
+    float ia = L.x + pe * L.x, ib = L.y + pe * L.y;
+    ia += pt * (L.y + pim);
+    ib += pt * (pip + L.x);
+    ia += pz * (PJp.x + PJm.x);
+    ib += pz * (PJp.y + PJm.y);
+    ia += pq * (PKp.x + PKm.x);
+    ib += pq * (PKp.y + PKm.y);
+    double2* pr = reinterpret_cast<double2*>(f.pr + o);
+    double2 p = *pr;
+    p.x += f2d(ia);
+    p.y += f2d(ib);
+    *pr = p;
+    *reinterpret_cast<float2*>(f.prf + o) = make_float2(d2f(p.x), d2f(p.y));
+}
+
 // CalcMaxCFL.F90:30-43 at cell (i, j, k), in the element type: FP32 on the
 // mixed path (a maximum is exact in any precision, so the reduction over
 // cells can stay in FP32 too).

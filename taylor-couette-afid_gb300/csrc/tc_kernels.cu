@@ -257,6 +257,16 @@ __global__ void __launch_bounds__(128) correct_kernel(Dims d, FieldsT<T> f, int 
     correct_cell<VEL, PRES, T>(d, f, sub, i, j, k);
 }
 
+// The fused projection of the mixed path, two theta-neighbouring cells a
+// thread (correct_pair_f).
+__global__ void __launch_bounds__(128) correct_pair_kernel(Dims d, FieldsT<float> f, int sub) {
+    if (f.st->halt) return;
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.nt || j >= d.nz) return;
+    correct_pair_f(d, f, sub, i, j, blockIdx.z);
+}
+
 // CalcLocalDivergence.F90:19-40 into phi (per-routine entry point only).
 template <typename T>
 __global__ void __launch_bounds__(128) divergence_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, int sub) {
@@ -709,6 +719,15 @@ void launch_correct(cudaStream_t s, const Dims& d, const Coef& c, const CoefT<T>
                     int sub, bool vel, bool pres) {
     dim3 blk;
     dim3 g = cell_grid(d, blk);
+    if constexpr (std::is_same<T, float>::value) {
+        if (vel && pres) {
+            const dim3 pblk(32, 4, 1);
+            const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
+            correct_pair_kernel<<<pg, pblk, 0, s>>>(d, f, sub);
+            TC_LAUNCH_CHECK();
+            return;
+        }
+    }
     if (vel && pres) correct_kernel<true, true, T><<<g, blk, 0, s>>>(d, f, sub);
     else if (vel) correct_kernel<true, false, T><<<g, blk, 0, s>>>(d, f, sub);
     else correct_kernel<false, true, T><<<g, blk, 0, s>>>(d, f, sub);
