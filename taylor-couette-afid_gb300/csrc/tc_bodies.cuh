@@ -899,49 +899,61 @@ __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q
 // blocks 0.380 ms.
 constexpr int kCkpt = 8;
 
-template <bool EXTRA, typename T>
+// Lane operations of the checkpointed sweep: V = T, one column a thread, or
+// V = F2 (FP32 path), two neighbouring columns a thread in packed FP32.
+template <typename V, typename T> struct SweepV;
+template <typename T> struct SweepV<T, T> {
+    static __device__ __forceinline__ T load(const T* p) { return *p; }
+    static __device__ __forceinline__ void store(T* p, T v) { *p = v; }
+    static __device__ __forceinline__ T fnma(T s, T a, T b) { return b - s * a; }   // b - s a
+    static __device__ __forceinline__ T mul(T a, T s) { return a * s; }
+    static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+    static __device__ __forceinline__ T adds(T a, T s) { return a + s; }
+};
+
+template <bool EXTRA, typename T, typename V = T>
 __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
                                                const T* l, const T* di, const T* u, T extra) {
-    const T y0 = EXTRA ? rhs[(size_t)k0 * P] + extra : rhs[(size_t)k0 * P];
-    rhs[(size_t)k0 * P] = y0;
-    T y = y0;
+    typedef SweepV<V, T> O;
+    const V y0 = EXTRA ? O::adds(O::load(rhs + (size_t)k0 * P), extra) : O::load(rhs + (size_t)k0 * P);
+    O::store(rhs + (size_t)k0 * P, y0);
+    V y = y0;
     // full batches [k0 + 1 + kCkpt m, k0 + kCkpt (m + 1)], checkpoint at their top
     const int nb = (nr - 1 - k0) / kCkpt;
     int k = k0 + 1;
     for (int m = 0; m < nb; ++m, k += kCkpt) {
-        T r[kCkpt];
+        V r[kCkpt];
 #pragma unroll
-        for (int b = 0; b < kCkpt; ++b) r[b] = rhs[(size_t)(k + b) * P];
+        for (int b = 0; b < kCkpt; ++b) r[b] = O::load(rhs + (size_t)(k + b) * P);
 #pragma unroll
-        for (int b = 0; b < kCkpt; ++b) y = r[b] - ld(l + k + b) * y;
-        rhs[(size_t)(k + kCkpt - 1) * P] = y;
+        for (int b = 0; b < kCkpt; ++b) y = O::fnma(ld(l + k + b), y, r[b]);
+        O::store(rhs + (size_t)(k + kCkpt - 1) * P, y);
     }
     // tail levels: every y stored
     for (; k < nr; ++k) {
-        y = rhs[(size_t)k * P] - ld(l + k) * y;
-        rhs[(size_t)k * P] = y;
+        y = O::fnma(ld(l + k), y, O::load(rhs + (size_t)k * P));
+        O::store(rhs + (size_t)k * P, y);
     }
     // back substitution: the tail from its stored y
-    T x = y * ld(di + nr - 1);
-    q[(size_t)(nr - 1) * P] += x;
+    V x = O::mul(y, ld(di + nr - 1));
+    O::store(q + (size_t)(nr - 1) * P, O::add(O::load(q + (size_t)(nr - 1) * P), x));
     const int ktop = k0 + nb * kCkpt;          // top level of the last full batch
     for (k = nr - 2; k > ktop; --k) {
-        x = (rhs[(size_t)k * P] - ld(u + k) * x) * ld(di + k);
-        q[(size_t)k * P] += x;
+        x = O::mul(O::fnma(ld(u + k), x, O::load(rhs + (size_t)k * P)), ld(di + k));
+        O::store(q + (size_t)k * P, O::add(O::load(q + (size_t)k * P), x));
     }
     // full batches from the top: recompute y from the checkpoint below
     for (int m = nb - 1; m >= 0; --m) {
         const int kb = k0 + 1 + m * kCkpt;     // lowest level of the batch
-        T yb[kCkpt], v[kCkpt];
-        T yc = rhs[(size_t)(kb - 1) * P];     // checkpoint (or y at k0)
+        V yb[kCkpt], v[kCkpt];
+        V yc = O::load(rhs + (size_t)(kb - 1) * P);     // checkpoint (or y at k0)
 #pragma unroll
-        for (int b = 0; b < kCkpt - 1; ++b) yb[b] = rhs[(size_t)(kb + b) * P];
-        yb[kCkpt - 1] = rhs[(size_t)(kb + kCkpt - 1) * P];
+        for (int b = 0; b < kCkpt; ++b) yb[b] = O::load(rhs + (size_t)(kb + b) * P);
 #pragma unroll
-        for (int b = 0; b < kCkpt; ++b) v[b] = q[(size_t)(kb + b) * P];
+        for (int b = 0; b < kCkpt; ++b) v[b] = O::load(q + (size_t)(kb + b) * P);
 #pragma unroll
         for (int b = 0; b < kCkpt - 1; ++b) {
-            yc = yb[b] - ld(l + kb + b) * yc;
+            yc = O::fnma(ld(l + kb + b), yc, yb[b]);
             yb[b] = yc;
         }
         // yb[kCkpt - 1] is the stored checkpoint y of the batch's top level
@@ -950,16 +962,31 @@ __device__ __forceinline__ void lu_column_ckpt(T* __restrict__ rhs, T* __restric
         for (int b = kCkpt - 1; b >= 0; --b) {
             const int kk = kb + b;
             if (b == kCkpt - 1 && top_of_column) continue;   // substituted above
-            x = (yb[b] - ld(u + kk) * x) * ld(di + kk);
-            q[(size_t)kk * P] = v[b] + x;
+            x = O::mul(O::fnma(ld(u + kk), x, yb[b]), ld(di + kk));
+            O::store(q + (size_t)kk * P, O::add(v[b], x));
         }
     }
     // the first level (below every batch), unless it is also the last
     if (k0 < nr - 1) {
-        x = (y0 - ld(u + k0) * x) * ld(di + k0);
-        q[(size_t)k0 * P] += x;
+        x = O::mul(O::fnma(ld(u + k0), x, y0), ld(di + k0));
+        O::store(q + (size_t)k0 * P, O::add(O::load(q + (size_t)k0 * P), x));
     }
 }
+
+// Two neighbouring columns in packed FP32 (the loads and stores move both
+// columns' entries as one 8-byte word; the factors are the same for both).
+template <> struct SweepV<F2, float> {
+    static __device__ __forceinline__ F2 load(const float* p) {
+        F2 r;
+        r.v = *reinterpret_cast<const unsigned long long*>(p);
+        return r;
+    }
+    static __device__ __forceinline__ void store(float* p, F2 v) { *reinterpret_cast<unsigned long long*>(p) = v.v; }
+    static __device__ __forceinline__ F2 fnma(float s, F2 a, F2 b) { return fma2(bc2(-s), a, b); }
+    static __device__ __forceinline__ F2 mul(F2 a, float s) { return a * bc2(s); }
+    static __device__ __forceinline__ F2 add(F2 a, F2 b) { return a + b; }
+    static __device__ __forceinline__ F2 adds(F2 a, float s) { return a + bc2(s); }
+};
 
 // SolveImpEqnUpdate_QT.F90:65-78 (comp 0), _QR.F90:136-150 (comp 1, faces
 // 1..nr-1), _QZ.F90:214-224 (comp 2) for the column `col`.  The three
@@ -989,6 +1016,31 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
         lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0), (T)0);
     else
         lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v), (T)0);
+}
+
+// radial_column of the FP32 path for the columns col and col+1 (col even)
+// in packed FP32; columns whose inner-wall slip variants differ (patterned
+// free slip) are solved one after the other.
+__device__ __forceinline__ void radial_column_pair(const Dims& d, const FieldsT<float>& f, int sub, long long col,
+                                                   int comp) {
+    const int nr = d.nr;
+    const size_t P = (size_t)d.P;
+    const int va = (f.icyl && f.icyl[col] == 0) ? 1 : 0, vb = (f.icyl && f.icyl[col + 1] == 0) ? 1 : 0;
+    if (va != vb) {
+        radial_column(d, f, sub, col, comp);
+        radial_column(d, f, sub, col + 1, comp);
+        return;
+    }
+    const MomFactorsT<float>& F = f.F;
+    if (comp == 0)
+        lu_column_ckpt<true, float, F2>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, va), F.dinv(sub, 0, va),
+                                        F.u(sub, 0, va), *F.extra(sub));
+    else if (comp == 1)
+        lu_column_ckpt<false, float, F2>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0),
+                                         F.u(sub, 1, 0), 0.0f);
+    else
+        lu_column_ckpt<false, float, F2>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, va), F.dinv(sub, 2, va),
+                                         F.u(sub, 2, va), 0.0f);
 }
 
 __device__ __forceinline__ double2 ld2(const double* p) { return ld(reinterpret_cast<const double2*>(p)); }

@@ -163,6 +163,10 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
 // levels and 6 blocks; FP64: 6 blocks, 0.942 ms against 0.961 ms unbounded).
 template <typename T> struct RadialBlocks { static constexpr int value = 6; };
 template <> struct RadialBlocks<float> { static constexpr int value = 8; };
+#ifndef TC_RADIAL_PAIR_BLOCKS
+#define TC_RADIAL_PAIR_BLOCKS 6
+#endif
+constexpr int kRadialPairBlocks = TC_RADIAL_PAIR_BLOCKS;
 
 template <typename T>
 __global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
@@ -170,6 +174,14 @@ __global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kern
     const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= d.P) return;
     radial_column(d, f, sub, col, blockIdx.y);
+}
+
+// FP32 path: two neighbouring columns a thread (radial_column_pair).
+__global__ void __launch_bounds__(128, kRadialPairBlocks) radial_pair_kernel(Dims d, FieldsT<float> f, int sub) {
+    if (f.st->halt) return;
+    const long long col = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (col >= d.P) return;
+    radial_column_pair(d, f, sub, col, blockIdx.y);
 }
 
 // --------------------------------------------------------------------------
@@ -633,7 +645,10 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
 
 template <typename T>
 void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub) {
-    radial_solve_kernel<T><<<dim3((unsigned)((d.P + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
+    if constexpr (std::is_same<T, float>::value)
+        radial_pair_kernel<<<dim3((unsigned)((d.P / 2 + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
+    else
+        radial_solve_kernel<T><<<dim3((unsigned)((d.P + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
     TC_LAUNCH_CHECK();
 }
 

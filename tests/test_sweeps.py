@@ -82,8 +82,8 @@ def test_checkpointed_sweep_matches_plain_sweep(tmp_path, batch):
     src = open(BODIES).read()
     plain = _extract(src, "template <bool EXTRA, typename T>\n__device__ __forceinline__ void lu_column(",
                      "// lu_column without the round trip")
-    ckpt = _extract(src, "template <bool EXTRA, typename T>\n__device__ __forceinline__ void lu_column_ckpt(",
-                    "// SolveImpEqnUpdate_QT.F90:65-78")
+    ckpt = _extract(src, "// Lane operations of the checkpointed sweep",
+                    "// Two neighbouring columns in packed FP32")
     cpp = tmp_path / "sweeps.cpp"
     cpp.write_text(HARNESS % (plain + ckpt))
     exe = tmp_path / "sweeps"
