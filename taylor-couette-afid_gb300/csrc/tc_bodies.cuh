@@ -64,6 +64,9 @@ __device__ __forceinline__ void stage_tile(C2* a, int n, G get, A at) {
     for (; t < n; t += bd) a[at(t)] = get(t);
 }
 
+// L2 prefetch of the line holding p (a hint: no data returns, nothing waits)
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // --------------------------------------------------------------------------
 // Step control
 // --------------------------------------------------------------------------
@@ -642,6 +645,11 @@ __device__ __forceinline__ F2 ldp_f2(const float* p) {
     return mkf2(v.x, v.y);
 }
 
+// Levels ahead of the march whose entries are prefetched into L2.  On the
+// 512x512x128 grid (mixed, one launch, mean over the substeps): none
+// 0.486 ms, 1 level 0.404 ms, 2 levels 0.383 ms, 3 levels 0.387 ms.
+constexpr int kMomPrefetch = 2;
+
 __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
                                                    int i, int j, int k0, int k1) {
     const int nr = d.nr, nt = d.nt, nz = d.nz;
@@ -685,6 +693,20 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
         const bool top = k == nr - 1;
         const F2 U12lo = U12, Uzlo = Uz;
         const int kp = k + 1;
+        // bring the pair's entries of level k + kMomPrefetch into L2 ahead of
+        // their loads
+        if (k + kMomPrefetch < nr) {
+            const size_t of = o + (size_t)kMomPrefetch * P;
+            prefetch_l2(qt + of);
+            prefetch_l2(qr + of);
+            prefetch_l2(qz + of);
+            prefetch_l2(pr + of);
+            if (a.use_ru) {
+                prefetch_l2(a.ru1 + of);
+                prefetch_l2(a.ru2 + of);
+                prefetch_l2(a.ru3 + of);
+            }
+        }
         // loads of level k (neighbours) and k+1 (column)
         float tcx, tcy, rcx, rcy, zcx, zcy;
         f2xy(tc, tcx, tcy);

@@ -156,17 +156,15 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
 // Radial implicit solves, one thread per (z, theta) column and component
 // --------------------------------------------------------------------------
 
-// Resident blocks per SM the radial kernel is compiled for (registers
+// Resident blocks per SM the radial kernels are compiled for (registers
 // capped to fit): the sweeps are bound by load latency, and more warps beat
-// the few values a thread would otherwise keep in flight (FP32 with 8-level
-// checkpoints: 8 blocks, 64 registers, 0.325 ms against 0.372 ms with 16
-// levels and 6 blocks; FP64: 6 blocks, 0.942 ms against 0.961 ms unbounded).
+// the few values a thread would otherwise keep in flight (FP64: 6 blocks,
+// 0.942 ms against 0.961 ms unbounded on the 512x512x128 grid).  The FP32
+// pair sweep (two columns a thread, 8-level checkpoints) fits 6 blocks in
+// 80 registers without spills (8 blocks spill); on the 512x512x384 grid it
+// runs 0.76 ms a launch against 0.91 ms for one column a thread (8 blocks).
 template <typename T> struct RadialBlocks { static constexpr int value = 6; };
-template <> struct RadialBlocks<float> { static constexpr int value = 8; };
-#ifndef TC_RADIAL_PAIR_BLOCKS
-#define TC_RADIAL_PAIR_BLOCKS 6
-#endif
-constexpr int kRadialPairBlocks = TC_RADIAL_PAIR_BLOCKS;
+constexpr int kRadialPairBlocks = 6;
 
 template <typename T>
 __global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
