@@ -119,10 +119,10 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
 // blocks of 256 threads (smaller tiles fit proportionally more): 4 blocks =
 // 64 registers, 3 = 80, 2 = 128.  As for the single-run kernels, more
 // resident warps beat the few values a thread would otherwise keep in
-// flight; the FP64 radial sweep keeps 80 and the two-cell momentum bodies
-// (FP64 and packed FP32) 128.
+// flight; the radial sweeps (FP64; FP32 two columns a thread) keep 80
+// and the two-cell momentum bodies (FP64 and packed FP32) 128.
 template <typename T> struct EnsBlocks { static constexpr int momentum = 2, radial = 3, ptri = 4; };
-template <> struct EnsBlocks<float> { static constexpr int momentum = 2, radial = 4, ptri = 4; };
+template <> struct EnsBlocks<float> { static constexpr int momentum = 2, radial = 3, ptri = 4; };
 
 // momentum: item = (chunk of kMomChunk radial levels, tile of TPB pairs of
 // theta-neighbouring columns), each thread marching its two columns in r in
@@ -154,12 +154,12 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
-    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const long long units = cell_units<T>(I.d.P);
+    const int tiles = (int)((units + blockDim.x - 1) / blockDim.x);
     const int k = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
-    if (flat >= I.d.P) return;
-    const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
-    correct_cell<true, true, T>(I.d, I.f, sub, i, j, k);
+    if (flat >= units) return;
+    corr_unit(I.d, I.f, sub, (int)flat, k);
 }
 
 // column-wise: item = (component, TPB consecutive (z, theta) columns)
@@ -170,11 +170,12 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(c
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
-    const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
+    const long long units = cell_units<T>(I.d.P);
+    const int tiles = (int)((units + blockDim.x - 1) / blockDim.x);
     const int comp = (int)((unsigned)local / (unsigned)tiles);
-    const long long col = (local - (long long)comp * tiles) * blockDim.x + threadIdx.x;
-    if (col >= I.d.P) return;
-    radial_column(I.d, I.f, sub, col, comp);
+    const long long u = (local - (long long)comp * tiles) * blockDim.x + threadIdx.x;
+    if (u >= units) return;
+    rad_unit(I.d, I.f, sub, u, comp);
 }
 
 // mode-wise: item = TPB consecutive (kz, kt) modes
@@ -324,14 +325,14 @@ int rebuild(tc_ensemble* e) {
         long long cnt[PH_COUNT];
         cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) *
                       ceil_div(mom_units<T>(d.P), TPB);
-        cnt[PH_CORR] = (long long)d.nr * ceil_div(d.P, TPB);
-        cnt[PH_RAD] = 3LL * ceil_div(d.P, TPB);
+        cnt[PH_CORR] = (long long)d.nr * ceil_div(cell_units<T>(d.P), TPB);
+        cnt[PH_RAD] = 3LL * ceil_div(cell_units<T>(d.P), TPB);
         cnt[PH_PTRI] = ceil_div((long long)d.nz * d.PH, TPB);
         cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
         cnt[PH_THINV] = cnt[PH_DIV];
         cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, persistent ? ZCols<T>::value : ZEns<T>::cols);
         cnt[PH_FACT] = 1;
-        cnt[PH_CFL] = I.vdt ? cnt[PH_CORR] : 0;
+        cnt[PH_CFL] = I.vdt ? (long long)d.nr * ceil_div(d.P, TPB) : 0;   // (level, tile of cells)
         for (int p = 0; p < PH_COUNT; ++p) {
             long long v = (long long)prefix[(size_t)p * (n + 1) + a] + cnt[p];
             if (v > 2000000000LL) return efail(e, 2010, "ensemble work list exceeds 2^31 items");

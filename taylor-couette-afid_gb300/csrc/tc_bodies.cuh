@@ -862,7 +862,7 @@ template <> struct MomMarch<float> { static constexpr bool value = true; };
 // batches of kRB ahead of the dependent arithmetic, so that each thread keeps
 // several loads in flight (the recurrence itself is sequential).
 constexpr int kRB = 8;
-constexpr int kRBr = 16;   // planes per batch in the radial momentum sweeps
+constexpr int kRBr = 8;   // planes per batch in the radial momentum sweeps
 
 template <bool EXTRA, typename T>
 __device__ __forceinline__ void lu_column(T* __restrict__ rhs, T* __restrict__ q, size_t P, int k0, int nr,
@@ -1130,9 +1130,9 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
         C2 zk = Z[k1 * R + r], zc = cconj(Z[k2 * R + r]);
         C2 e = cadd(zk, zc), o = csub(zk, zc);
         C2 w = __ldg(twr + kt);
-        C2 wo = cmul(w, o);
-        // - i * wo = (wo.y, -wo.x)
-        f.spec[(size_t)row * PH + kt] = mk2(e.x + wo.y, e.y - wo.x);
+        // e - i w o = (e.x + w.x o.y + w.y o.x, e.y - w.x o.x + w.y o.y), in
+        // multiply-adds (the product w o is never rounded on its own)
+        f.spec[(size_t)row * PH + kt] = mk2(fmar(w.x, o.y, fmar(w.y, o.x, e.x)), fmar(-w.x, o.x, fmar(w.y, o.y, e.y)));
     }
 }
 
@@ -1358,10 +1358,9 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
             if (kt == 0) { xk.y = 0; xm.y = 0; }   // imaginary parts of the 0 and Nyquist bins
             C2 xc = cconj(xm);
             C2 e = cadd(xk, xc), o = csub(xk, xc);
-            C2 w = cconj(__ldg(twr + kt));
-            C2 wo = cmul(w, o);
-            // Z = e + i wo
-            z = mk2(e.x - wo.y, e.y + wo.x);
+            C2 w = __ldg(twr + kt);
+            // Z = e + i conj(w) o = (e.x - w.x o.y + w.y o.x, e.y + w.x o.x + w.y o.y)
+            z = mk2(fmar(-w.x, o.y, fmar(w.y, o.x, e.x)), fmar(w.x, o.x, fmar(w.y, o.y, e.y)));
         }
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });

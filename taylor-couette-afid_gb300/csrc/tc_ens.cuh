@@ -52,6 +52,34 @@ __device__ __forceinline__ void mom_unit(const Dims& d, const CoefT<T>& cv, cons
     }
 }
 
+// Work units of one radial level of the projection and of one component of
+// the radial sweeps: FP32 two theta-neighbouring cells / columns
+// (correct_pair_f, radial_column_pair), FP64 one.
+template <typename T>
+__host__ __device__ __forceinline__ long long cell_units(long long P) {
+    return std::is_same<T, float>::value ? P / 2 : P;
+}
+
+// The projection of unit u at level k.
+template <typename T>
+__device__ __forceinline__ void corr_unit(const Dims& d, const FieldsT<T>& f, int sub, int u, int k) {
+    if constexpr (std::is_same<T, float>::value) {
+        int i, j;
+        mom_unit_cell<T>(u, d.nt, i, j);
+        correct_pair_f(d, f, sub, i, j, k);
+    } else {
+        const int j = (int)((unsigned)u / (unsigned)d.nt), i = u - j * d.nt;
+        correct_cell<true, true, T>(d, f, sub, i, j, k);
+    }
+}
+
+// The radial sweep of unit u for component comp.
+template <typename T>
+__device__ __forceinline__ void rad_unit(const Dims& d, const FieldsT<T>& f, int sub, long long u, int comp) {
+    if constexpr (std::is_same<T, float>::value) radial_column_pair(d, f, sub, 2 * u, comp);
+    else radial_column(d, f, sub, u, comp);
+}
+
 __device__ __forceinline__ int find_member(const int* prefix, int n, long long item) {
     int lo = 0, hi = n;
     while (hi - lo > 1) {

@@ -157,13 +157,16 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
 // --------------------------------------------------------------------------
 
 // Resident blocks per SM the radial kernels are compiled for (registers
-// capped to fit): the sweeps are bound by load latency, and more warps beat
-// the few values a thread would otherwise keep in flight (FP64: 6 blocks,
-// 0.942 ms against 0.961 ms unbounded on the 512x512x128 grid).  The FP32
+// capped to fit): more resident warps beat the few values a thread would
+// otherwise keep in flight.  FP64 on the 512x512x128 grid (batches of kRBr
+// levels): 8 blocks with batches of 8 (64 registers) 0.748 ms, 8 blocks with
+// batches of 4 0.751 ms, 10 blocks 0.764 ms, 6 blocks with batches of 16
+// (80 registers, spilling) 0.834 ms, 4 blocks with batches of 16 0.891 ms.
+// The FP32
 // pair sweep (two columns a thread, 8-level checkpoints) fits 6 blocks in
 // 80 registers without spills (8 blocks spill); on the 512x512x384 grid it
 // runs 0.76 ms a launch against 0.91 ms for one column a thread (8 blocks).
-template <typename T> struct RadialBlocks { static constexpr int value = 6; };
+template <typename T> struct RadialBlocks { static constexpr int value = 8; };
 constexpr int kRadialPairBlocks = 6;
 
 template <typename T>

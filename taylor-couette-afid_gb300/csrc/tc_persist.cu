@@ -162,8 +162,9 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         const int m = find_member(table(PH_RAD), n, item);
         const InstT<T>& I = inst[m];
         if (I.f.st->halt) continue;
-        const CellItem ci = cell_item(item - table(PH_RAD)[m], I.d.P);
-        if (ci.flat < (long long)I.d.P) radial_column(I.d, I.f, sub, ci.flat, ci.outer);
+        const long long units = cell_units<T>(I.d.P);
+        const CellItem ci = cell_item(item - table(PH_RAD)[m], (size_t)units);
+        if (ci.flat < units) rad_unit(I.d, I.f, sub, ci.flat, ci.outer);
     }
     if (!grid_barrier(a)) return;
     // divergence + theta FFT: R rows per item
@@ -217,11 +218,9 @@ __global__ void __launch_bounds__(kPersistThreads) persist_kernel(const InstT<T>
         const int m = find_member(table(PH_CORR), n, item);
         const InstT<T>& I = inst[m];
         if (I.f.st->halt) continue;
-        const CellItem ci = cell_item(item - table(PH_CORR)[m], I.d.P);
-        if (ci.flat < (long long)I.d.P) {
-            const int j = (int)((unsigned)ci.flat / (unsigned)I.d.nt), i = (int)ci.flat - j * I.d.nt;
-            correct_cell<true, true, T>(I.d, I.f, sub, i, j, ci.outer);
-        }
+        const long long units = cell_units<T>(I.d.P);
+        const CellItem ci = cell_item(item - table(PH_CORR)[m], (size_t)units);
+        if (ci.flat < units) corr_unit(I.d, I.f, sub, (int)ci.flat, ci.outer);
     }
     if (a.flags & PF_END) {
         if (!grid_barrier(a)) return;
