@@ -360,8 +360,17 @@ class TaylorCouette:
                 raise ValueError(f"expected shape {self.halo_shape}, got {p.shape}")
         self._ck(self.L.tc_set_state(self.h, *[_dptr(a) for a in arrs], _dptr(p) if p is not None else None))
 
-    def get_state(self):
-        out = [np.empty(self.halo_shape) for _ in range(4)]
+    def get_state(self, out=None):
+        """WriteFlowField's fields (reference layout with halos).  `out`: four
+        C-contiguous float64 arrays of the halo shape to fill (for example in
+        pinned memory), else new arrays."""
+        if out is None:
+            out = [np.empty(self.halo_shape) for _ in range(4)]
+        else:
+            out = list(out)
+            for a in out:
+                if a.shape != self.halo_shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"expected C-contiguous float64 arrays of shape {self.halo_shape}")
         self._ck(self.L.tc_get_state(self.h, *[_dptr(a) for a in out]))
         return tuple(out)
 

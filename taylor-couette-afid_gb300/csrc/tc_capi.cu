@@ -46,12 +46,21 @@ cudaError_t dalloc(tc_handle* h, T** p, size_t count) {
     return e;
 }
 
-// Radix plan: radix-4 stages first, then 2, 3, 5.
-bool make_plan(int n, FFTPlan& P) {
+// Radix plan: radix-8 stages first when r8 (the FP32 transforms, bound by
+// instruction issue: fewer passes through shared memory), then 4, 2, 3, 5.
+// The FP64 transforms keep radix-4 stages, whose factored multiply-add
+// butterflies cost the same FP64 instructions a point and level.
+bool make_plan(int n, FFTPlan& P, bool r8) {
     if (n < 1 || n > 65536) return false;
     P.n = n;
     P.nstages = 0;
     int m = n;
+    if (r8)
+        while (m % 8 == 0 && m > 1) {
+            if (P.nstages >= kMaxStages) return false;
+            P.radix[P.nstages++] = 8;
+            m /= 8;
+        }
     for (int r : {4, 2, 3, 5})
         while (m % r == 0 && m > 1) {
             if (P.nstages >= kMaxStages) return false;
@@ -354,7 +363,7 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
 
     // FFT plans and twiddles
     FFTPlan pth, pz;
-    if (!make_plan(d.M, pth) || !make_plan(d.nz, pz)) {
+    if (!make_plan(d.M, pth, h->mixed) || !make_plan(d.nz, pz, h->mixed)) {
         int r = fail(nullptr, 2003, "FFT length does not factor into 2, 3, 5"); tc_destroy(h); return r;
     }
     if (zfft_smem_bytes(d.nz, h->mixed) > 200 * 1024) {

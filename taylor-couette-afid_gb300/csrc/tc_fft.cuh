@@ -91,6 +91,30 @@ template <typename C2> __device__ __forceinline__ void dft5(C2* v, bool inv) {
     v[3] = inv ? w2 : w3;
 }
 
+// 8-point DFT as two 4-point DFTs of the even and odd inputs joined by
+// W8^k = exp(-+ i pi k / 4): 52 additions and 4 multiplications.
+template <typename C2> __device__ __forceinline__ void dft8(C2* v, bool inv) {
+    typedef decltype(v[0].x) R;
+    const R h = (R)0.70710678118654752440;   // 1/sqrt(2)
+    C2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    dft4(e, inv);
+    dft4(o, inv);
+    // o1 W8, o2 W8^2, o3 W8^3; forward W8 = (1 - i) h, inverse (1 + i) h
+    const C2 t1 = inv ? mk2((o[1].x - o[1].y) * h, (o[1].y + o[1].x) * h)
+                      : mk2((o[1].x + o[1].y) * h, (o[1].y - o[1].x) * h);
+    const C2 t2 = inv ? mk2(-o[2].y, o[2].x) : mk2(o[2].y, -o[2].x);
+    const C2 t3 = inv ? mk2(-(o[3].x + o[3].y) * h, (o[3].x - o[3].y) * h)
+                      : mk2((o[3].y - o[3].x) * h, -(o[3].x + o[3].y) * h);
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], t1);
+    v[5] = csub(e[1], t1);
+    v[2] = cadd(e[2], t2);
+    v[6] = csub(e[2], t2);
+    v[3] = cadd(e[3], t3);
+    v[7] = csub(e[3], t3);
+}
+
 // ---- butterflies in fused multiply-adds (FP64 path) ----------------------
 //
 // The FP64 transforms are bound by the FP64 pipe, so they count FP64
@@ -204,7 +228,8 @@ __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restri
 #pragma unroll
             for (int cc = 1; cc < p; ++cc) v[cc] = cmul(v[cc], twiddle(tw, cc * s * rp, inv));
         }
-        if (p == 4) dft4(v, inv);
+        if constexpr (p == 8) dft8(v, inv);
+        else if (p == 4) dft4(v, inv);
         else if (p == 2) dft2(v);
         else if (p == 3) dft3(v, inv);
         else dft5(v, inv);
@@ -223,7 +248,8 @@ __device__ C2* fft_lines(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv)
     for (int st = 0; st < P.nstages; ++st) {
         const int p = P.radix[st], rp = P.rp[st];
         const unsigned m = P.mrp[st];
-        if (p == 4) fft_stage<C, 4>(a, b, n, L, rp, m, tw, inv);
+        if (p == 8) fft_stage<C, 8>(a, b, n, L, rp, m, tw, inv);
+        else if (p == 4) fft_stage<C, 4>(a, b, n, L, rp, m, tw, inv);
         else if (p == 2) fft_stage<C, 2>(a, b, n, L, rp, m, tw, inv);
         else if (p == 3) fft_stage<C, 3>(a, b, n, L, rp, m, tw, inv);
         else fft_stage<C, 5>(a, b, n, L, rp, m, tw, inv);
