@@ -1498,26 +1498,6 @@ __device__ __forceinline__ T cfl_value(const Dims& d, const Coef& c, const CoefT
                fabs((z1 + z0) * 0.5 * dxz));
 }
 
-// cfl_value<float> of the cells (i, j, k) and (i+1, j, k), i even, with the
-// pair's fields loaded as float2: the larger of the two.
-__device__ __forceinline__ float cfl_pair_f(const Dims& d, const CoefT<float>& cv, double dxt, double dxz,
-                                            const FieldsT<float>& f, int i, int j, int k) {
-    const size_t P = (size_t)d.P;
-    const int ip1 = wp(i + 1, d.nt), jp = wp(j, d.nz);
-    const size_t row = (size_t)k * P + (size_t)j * d.nt;
-    const size_t o = row + i;
-    const float h = 0.5f, fdxt = (float)dxt, fdxz = (float)dxz;
-    const float usrm = ld(cv.usrm + k), udx2rm = ld(cv.udx2rm + k);
-    const float2 t = ld(reinterpret_cast<const float2*>(f.qt + o));
-    const float t2 = ld(f.qt + row + ip1);
-    const float2 r0 = ld(reinterpret_cast<const float2*>(f.qr + o)), r1 = ld(reinterpret_cast<const float2*>(f.qr + o + P));
-    const float2 z0 = ld(reinterpret_cast<const float2*>(f.qz + o));
-    const float2 z1 = ld(reinterpret_cast<const float2*>(f.qz + (size_t)k * P + (size_t)jp * d.nt + i));
-    const float va = fabsf((t.y + t.x) * h * fdxt * usrm) + fabsf((r1.x + r0.x) * h * udx2rm) + fabsf((z1.x + z0.x) * h * fdxz);
-    const float vb = fabsf((t2 + t.y) * h * fdxt * usrm) + fabsf((r1.y + r0.y) * h * udx2rm) + fabsf((z1.y + z0.y) * h * fdxz);
-    return fmaxf(va, vb);
-}
-
 __device__ __forceinline__ double to_double(double v) { return v; }
 __device__ __forceinline__ double to_double(float v) { return f2d(v); }
 

@@ -337,19 +337,6 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Co
     A best = WHICH == 0 ? (A)0.00000001 : (A)0.0;
     const size_t P = (size_t)d.P;
     const int nt = d.nt, Pi = (int)d.P;
-    if constexpr (WHICH == 0 && std::is_same<T, float>::value) {
-        // two theta-neighbouring cells a thread (nthm is even)
-        const int half = nt / 2, units = Pi / 2;
-        for (int k = blockIdx.y; k < d.nr; k += gridDim.y)
-            for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < units; u += gridDim.x * blockDim.x) {
-                const int j = (int)((unsigned)u / (unsigned)half), i = 2 * (u - j * half);
-                best = fmaxf(best, cfl_pair_f(d, cv, dxt, dxz, f, i, j, k));
-            }
-        double b = to_double(best);
-        b = block_reduce<true>(b, sh);
-        if (threadIdx.x == 0) f.red[blockIdx.y * gridDim.x + blockIdx.x] = b;
-        return;
-    }
     for (int k = blockIdx.y; k < d.nr; k += gridDim.y) {
         for (int flat = blockIdx.x * blockDim.x + threadIdx.x; flat < Pi; flat += gridDim.x * blockDim.x) {
             const int j = (int)((unsigned)flat / (unsigned)nt), i = flat - j * nt;
