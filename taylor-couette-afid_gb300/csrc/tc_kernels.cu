@@ -629,12 +629,14 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
     dim3 g = cell_grid(d, blk);
     if (mode == MODE_FUSED) {
         // two theta-neighbouring cells (FP64) or columns (FP32 march) a thread
-        const dim3 pblk(32, 4, 1);
+        // blocks of 32 x 4 threads; 16 x 8 and 64 x 2 measured the same or slower
         if constexpr (MomMarch<T>::value) {
+            const dim3 pblk(32, 4, 1);
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y,
                           (d.nr + kMomChunk - 1) / kMomChunk);
             momentum_march_x2_kernel<<<pg, pblk, 0, s>>>(d, c, a);
         } else {
+            const dim3 pblk(32, 4, 1);
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
             momentum_pair_kernel<T><<<pg, pblk, 0, s>>>(d, c, a);
         }
