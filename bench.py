@@ -523,20 +523,26 @@ def main():
     e2e = None
     if not args.no_e2e:
         barrier()
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         g.set_state(*pinned)
+        ea.record(stream)
         nt2, t2 = 0, 0.0
         for _ in range(args.steps):
             code, nt2, t2, _ = g.run(1, nt2, t2)
+        eb.record(stream)
         qt_o, qr_o, qz_o, pr_o = g.get_state(out=pinned_out)
         e1.record(stream)
         barrier()
         ms_e2e = max_over_ranks(e0.elapsed_time(e1))
+        e2e_parts = {"set_state_ms": round(e0.elapsed_time(ea), 2), "steps_ms": round(ea.elapsed_time(eb), 2),
+                     "get_state_ms": round(eb.elapsed_time(e1), 2)}
         h2d = sum(a.nbytes for a in pinned)
         d2h = h2d
         e2e = {"value": world * cells * args.steps / (ms_e2e * 1e-3) / 1e6, "unit": "Mcell-steps/s",
                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
                "ms_per_step": ms_e2e / args.steps,
+               "parts": e2e_parts,
                "note": "state in (tc_set_state) and out (tc_get_state) once per timed run, from and into "
                        "pinned host buffers, amortised per step; dt/time read back every step"}
         ref_state = tuple(a.copy() for a in (qt_o, qr_o, qz_o))
