@@ -1487,18 +1487,19 @@ __device__ __forceinline__ T cfl_value(const Dims& d, const Coef& c, const CoefT
     const size_t P = (size_t)d.P;
     const int ip = wp(i, d.nt), jp = wp(j, d.nz);
     const size_t o = (size_t)k * P + (size_t)j * d.nt + i;
+    // (a + b) 0.5 x equals (a + b) (0.5 x) exactly; the theta term uses the
+    // product 0.5 dxt usrm(k), rounded once
     if (!std::is_same<T, double>::value) {
-        const T h = (T)0.5;
-        const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * h * (T)dxt * ld(cv.usrm + k)));
-        const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * h * ld(cv.udx2rm + k)));
-        const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * h * (T)dxz));
+        const T vt = fabsf((float)((ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip) + ld(f.qt + o)) * ld(cv.h_dxt_usrm + k)));
+        const T vr = fabsf((float)((ld(f.qr + o + P) + ld(f.qr + o)) * ld(cv.h_udx2rm + k)));
+        const T vz = fabsf((float)((ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i) + ld(f.qz + o)) * (T)(0.5 * dxz)));
         return vt + vr + vz;
     }
     const double t0 = ld(f.qt + o), t1 = ld(f.qt + (size_t)k * P + (size_t)j * d.nt + ip);
     const double r0 = ld(f.qr + o), r1 = ld(f.qr + o + P);
     const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * d.nt + i);
-    return (T)(fabs((t1 + t0) * 0.5 * dxt * ld(c.usrm + k)) + fabs((r1 + r0) * 0.5 * ld(c.udx2rm + k)) +
-               fabs((z1 + z0) * 0.5 * dxz));
+    return (T)(fabs((t1 + t0) * ld(c.h_dxt_usrm + k)) + fabs((r1 + r0) * ld(c.h_udx2rm + k)) +
+               fabs((z1 + z0) * (0.5 * dxz)));
 }
 
 __device__ __forceinline__ double to_double(double v) { return v; }

@@ -224,7 +224,7 @@ void set_coef_ptrs(CoefT<T>& c, const T* base, int lenK) {
                       &c.ap3j, &c.ac3j, &c.am3j, &c.ap2j, &c.ac2j, &c.am2j,
                       &c.udx2m, &c.rudx2c, &c.udx1qm, &c.apph, &c.acph, &c.amph,
                       &c.usrm2, &c.q_udx2rm, &c.q_usrm, &c.h_udx1vis1, &c.q_udx2c,
-                      &c.q_rc_romeg, &c.rm, &c.udx2mm, &c.udx2cc, &c.pvol};
+                      &c.q_rc_romeg, &c.rm, &c.udx2mm, &c.udx2cc, &c.pvol, &c.h_dxt_usrm, &c.h_udx2rm};
     for (int a = 0; a < kCoefArrays; ++a) *cp[a] = base + (size_t)a * lenK;
     c.ak1 = base + (size_t)kCoefArrays * lenK;
     c.ak3 = base + (size_t)(kCoefArrays + 1) * lenK;
@@ -305,7 +305,7 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
         &g.ap2j, &g.ac2j, &g.am2j,
         &g.udx2m, &g.rudx2c, &g.udx1qm, &g.apph, &g.acph, &g.amph, nullptr,
         nullptr, nullptr, nullptr, nullptr, nullptr,
-        &g.rm, &g.udx2mm, &g.udx2cc, &g.pvol};
+        &g.rm, &g.udx2mm, &g.udx2cc, &g.pvol, nullptr, nullptr};
     const int lenK = std::max(std::max(nrr, d.nt), d.nz) + 1;
     std::vector<double> host((size_t)(kCoefArrays + 2) * lenK, 0.0);
     for (int a = 0; a < kCoefArrays; ++a) {
@@ -324,6 +324,8 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
         host[(size_t)32 * lenK + m] = 0.5 * g.udx1vis1[m];
         host[(size_t)33 * lenK + m] = 0.25 * g.udx2c[m];
         host[(size_t)34 * lenK + m] = 0.25 * g.rc[m] * cfg->romeg;
+        host[(size_t)39 * lenK + m] = m < nr ? 0.5 * g.dxt * g.usrm[m] : 0.0;                 // h_dxt_usrm
+        host[(size_t)40 * lenK + m] = 0.5 * g.udx2rm[m];                                       // h_udx2rm
     }
     for (int i = 0; i < d.nt; ++i) host[(size_t)kCoefArrays * lenK + i] = g.ak1[i];
     for (int j = 0; j < d.nz; ++j) host[(size_t)(kCoefArrays + 1) * lenK + j] = g.ak3[j];

@@ -73,10 +73,13 @@ struct CoefT {
     const T *q_udx2rm, *q_usrm, *h_udx1vis1, *q_udx2c, *q_rc_romeg;
     // statistics metrics (CreateGrid.F90:136-173)
     const T *rm, *udx2mm, *udx2cc, *pvol;
+    // 0.5 dxt usrm and 0.5 udx2rm: the theta and radial terms of CalcMaxCFL
+    // in one product each
+    const T *h_dxt_usrm, *h_udx2rm;
     const T *ak1, *ak3;
 };
 typedef CoefT<double> Coef;
-constexpr int kCoefArrays = 39;   // arrays before ak1, ak3
+constexpr int kCoefArrays = 41;   // arrays before ak1, ak3
 
 // Scalars of the configuration (param.F90).
 struct Consts {
