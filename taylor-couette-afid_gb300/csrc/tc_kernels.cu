@@ -125,10 +125,11 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
     momentum_cell<MODE>(d, c, a, i, j, k);
 }
 
-// The fused form: one thread per (theta, z) column and chunk of kMomChunk
-// radial levels, marching in r (momentum_column).
 // FP64 fused momentum, two theta-neighbouring cells per thread
-// (momentum_pair); one thread per pair (i even: nthm is even).
+// (momentum_pair); one thread per pair (i even: nthm is even).  Unbounded
+// (124 registers, 4 blocks per SM): capped at 5 blocks (96 registers)
+// 6.78 ms and at 6 (80, spilling) 6.78 ms against 6.63 ms on the
+// 512x512x128 grid.
 template <typename T>
 __global__ void __launch_bounds__(128) momentum_pair_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
     if (a.st->halt) return;
