@@ -191,6 +191,16 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
                 pc[2 * (nr + 1) + row] = -beta * c.apph[row];
                 if (row == 0) pc[3 * (nr + 1)] = -beta * k.dxzq;
             }
+            {
+                // divergence coefficients of substep s (usdt and the FFT
+                // normalisation folded in)
+                double* dc = corrd + kDivCoef(nr + 1);
+                const double sc = k.fft_norm / (k.alm[s] * dt);
+                const double us = c.usrm[row] * sc;
+                dc[s * 2 * (nr + 1) + row] = k.dxt * us;
+                dc[s * 2 * (nr + 1) + (nr + 1) + row] = c.udx2m[row] * us;
+                if (row == 0) dc[6 * (nr + 1) + s] = k.dxz * sc;
+            }
         }
     }
     __syncthreads();
@@ -1093,6 +1103,33 @@ __device__ __forceinline__ typename V2<T>::type div_pair(const Dims& d, const Co
     return mk2(a, b);
 }
 
+// div_pair times usdt and the FFT normalisation, from the per-dt coefficients
+// of substep `sub`: each term (q_+ - q) times one product (the rounding
+// order differs from div_pair's by the folding).
+template <typename T>
+__device__ __forceinline__ typename V2<T>::type div_pair_scaled(const Dims& d, const FieldsT<T>& f, int sub, int k,
+                                                                int j, int m) {
+    const size_t P = (size_t)d.P;
+    const int nt = d.nt, nrr = d.nr + 1;
+    const size_t row = (size_t)k * P + (size_t)j * nt;
+    const int i0 = 2 * m, i2 = (2 * m + 2 == nt) ? 0 : 2 * m + 2;
+    const T* qt = f.qt;
+    const T* qr = f.qr;
+    const T* qz = f.qz;
+    auto t01 = ld2(qt + row + i0);
+    T t2 = ld(qt + row + i2);
+    auto r0 = ld2(qr + row + i0);
+    auto r1 = ld2(qr + row + P + i0);
+    const int jp = wp(j, d.nz);
+    auto z0 = ld2(qz + row + i0);
+    auto z1 = ld2(qz + (size_t)k * P + (size_t)jp * nt + i0);
+    const T* dc = f.corr + kDivCoef(nrr);
+    const T ct = ld(dc + sub * 2 * nrr + k), cr = ld(dc + sub * 2 * nrr + nrr + k), cz = ld(dc + 6 * nrr + sub);
+    T a = (t01.y - t01.x) * ct + (r1.x - r0.x) * cr + (z1.x - z0.x) * cz;
+    T b = (t2 - t01.y) * ct + (r1.y - r0.y) * cr + (z1.y - z0.y) * cz;
+    return mk2(a, b);
+}
+
 // Forward transform of R rows.  FROM_PHI: the rows come from the phi array
 // (CalcLocalDivergence already ran); otherwise the divergence is computed on
 // the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
@@ -1114,10 +1151,13 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
         if (row < nrows) {
             const int k = d.mnz ? fdiv((int)row, d.mnz) : (int)(row / d.nz);
             const int j = (int)(row - (long long)k * d.nz);
-            if (FROM_PHI) z = ld2(f.phi + (size_t)row * d.nt + 2 * m);
-            else z = div_pair(d, c, dxt, dxz, f.qt, f.qr, f.qz, k, j, m);
-            z.x *= scl;
-            z.y *= scl;
+            if (FROM_PHI) {
+                z = ld2(f.phi + (size_t)row * d.nt + 2 * m);
+                z.x *= scl;
+                z.y *= scl;
+            } else {
+                z = div_pair_scaled(d, f, sub, k, j, m);
+            }
         }
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });

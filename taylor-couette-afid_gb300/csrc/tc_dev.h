@@ -144,8 +144,14 @@ __host__ __device__ inline int ptri_slots(int nr) {
 // [ kPresCoef(nr+1) + (nr+1) + k ]     pt = -be udx1qm
 // [ kPresCoef(nr+1) + 2 (nr+1) + k ]   pq = -be apph
 // [ kPresCoef(nr+1) + 3 (nr+1) ]       pz = -be dxzq
+// and for the divergence of substep s, with usdt(s) = 1/(al(s) dt) and the
+// FFT normalisation f folded in (CalcLocalDivergence.F90:27-40 times usdt f):
+// [ kDivCoef(nr+1) + s*2*(nr+1) + k ]          dt_k = dxt usrm(k) usdt f
+// [ kDivCoef(nr+1) + s*2*(nr+1) + (nr+1) + k ] dr_k = udx2m(k) usrm(k) usdt f
+// [ kDivCoef(nr+1) + 6*(nr+1) + s ]            dz = dxz usdt f
 __host__ __device__ inline size_t kPresCoef(int nrr) { return (size_t)9 * nrr + 9; }
-__host__ __device__ inline size_t kCorrCount(int nrr) { return (size_t)12 * nrr + 10; }
+__host__ __device__ inline size_t kDivCoef(int nrr) { return kPresCoef(nrr) + (size_t)3 * nrr + 1; }
+__host__ __device__ inline size_t kCorrCount(int nrr) { return kDivCoef(nrr) + (size_t)6 * nrr + 3; }
 
 // Factors of the row-scaled momentum matrices of one step: for each substep
 // s (3), component c (0 = qt, 1 = qr, 2 = qz) and slip variant v (0 = no
