@@ -100,7 +100,7 @@ def algorithmic_bytes(cls: str, nt: int, nz: int, nr: int, rk_substep_mix: float
 # bytes per cell of a launch averaged over the three substeps (79.2, 102.9,
 # 102.8), and per cell its FP64 instructions (45.41 DADD + 20.98 DMUL +
 # 42.45 DFMA) and FLOPs.  Per-cell figures do not depend on the grid size.
-MOMENTUM_FP64_NCU = {"dram_bytes_per_cell": 94.98, "fp64_inst_per_cell": 108.84, "fp64_flops_per_cell": 151.29}
+MOMENTUM_FP64_NCU = {"dram_bytes_per_cell": 95.04, "fp64_inst_per_cell": 103.23, "fp64_flops_per_cell": 147.0}
 
 STEP_BYTES = {"fp64": 3 * (6 + 2 + 2) * 8 + (2 * 3 + 2 * 3) * 8,
               "mixed": 3 * (6 * 4 + 2 * 8 + 2 * 4) + 12 * 4}

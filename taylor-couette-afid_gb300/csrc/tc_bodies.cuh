@@ -201,6 +201,14 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
                 dc[s * 2 * (nr + 1) + (nr + 1) + row] = c.udx2m[row] * us;
                 if (row == 0) dc[6 * (nr + 1) + s] = k.dxz * sc;
             }
+            {
+                // alre dt times the radial coefficients of the momentum rhs
+                double* ic = corrd + kImpCoef(nr + 1) + (size_t)s * 9 * (nr + 1);
+                const double ad = k.alre[s] * dt;
+                const double* src[9] = {c.ap1j, c.ac1j, c.am1j, c.ap2je, c.ac2je, c.am2je, c.ap3j, c.ac3j, c.am3j};
+#pragma unroll
+                for (int e = 0; e < 9; ++e) ic[e * (nr + 1) + row] = ad * src[e][row];
+            }
         }
     }
     __syncthreads();
@@ -310,6 +318,7 @@ struct MomArgs {
     T ac1j_fs0, am1j_fs0, ap1j_fs1, ac1j_fs1, ac3j_fs0, am3j_fs0, ap3j_fs1, ac3j_fs1;
     const T* cf;            // this substep's pressure-gradient products dt al metric (per component, level)
     const T* mr;            // gam dt, rom dt, alre dt of this substep
+    const T* ic;            // alre dt times the radial coefficients of this substep (9 arrays)
     int use_ru;
 };
 
@@ -396,8 +405,11 @@ __device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
 }
 
 // ImplicitAndUpdateQT/QR/QZ for cell (i, j, k) of stencil S given its
-// explicit terms: the right-hand sides and the RK memory.
-template <typename T>
+// explicit terms: the right-hand sides and the RK memory.  RU: whether the
+// substep reads the RK memory (rom != 0), at compile time (0, 1) or read from
+// a.use_ru (-1).  Interior levels take alre dt times the radial coefficients
+// from a.ic; the wall levels form their coefficients here, as the reference.
+template <typename T, int RU = -1>
 __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, const Stencil& S,
                                               int i, int j, int k, T ht, T hr, T hz) {
     const int nr = d.nr;
@@ -409,61 +421,69 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
     // gam dt, rom dt, alre dt; the pressure terms use the per-level dt al
     // metric products of the correction (a.cf), so no factor dt remains
     const T gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
+    const bool use_ru = RU < 0 ? (a.use_ru != 0) : (RU != 0);
     const int nrr = nr + 1;
+    const T* ic = a.ic;
     const T one = (T)1.0;
     const T fic = a.icyl ? (T)a.icyl[(size_t)j * d.nt + i] : one, foc = one;
     const T* pr = a.pr + o;
     const T p_c = ld(pr);
     // ---- qt (ImplicitAndUpdateQT.F90:45-115)
     {
-        T d33;
+        T rhs = gadt * ht;
+        if (use_ru) rhs += rodt * a.ru1[o];
         if (k == 0) {
             T app = ld(c.ap1j);
             T acc = ld(c.ac1j) * fic + a.ac1j_fs0 * (one - fic);
             T amm = ld(c.am1j) * fic + a.am1j_fs0 * (one - fic);
-            d33 = ld(qt + P) * app + ld(qt) * acc + (a.virotint + step_vinner<T>(a.st)) * amm;
+            rhs += alredt * (ld(qt + P) * app + ld(qt) * acc + (a.virotint + step_vinner<T>(a.st)) * amm);
         } else if (k == nr - 1) {
             T amm = ld(c.am1j + k);
             T app = ld(c.ap1j + k) * foc + a.ap1j_fs1 * (one - foc);
             T acc = ld(c.ac1j + k) * foc + a.ac1j_fs1 * (one - foc);
-            d33 = a.virotext * app + ld(qt) * acc + ld(qt - P) * amm;
+            rhs += alredt * (a.virotext * app + ld(qt) * acc + ld(qt - P) * amm);
         } else {
-            d33 = ld(qt + P) * ld(c.ap1j + k) + ld(qt) * ld(c.ac1j + k) + ld(qt - P) * ld(c.am1j + k);
+            rhs += ld(ic + k) * ld(qt + P);
+            rhs += ld(ic + nrr + k) * ld(qt);
+            rhs += ld(ic + 2 * nrr + k) * ld(qt - P);
         }
-        T old = a.use_ru ? a.ru1[o] : (T)0;
-        a.rhs_t[o] = gadt * ht + rodt * old + alredt * d33 - (p_c - ld(pr + S.dim)) * ld(a.cf + k);
+        a.rhs_t[o] = rhs - (p_c - ld(pr + S.dim)) * ld(a.cf + k);
         a.ru1[o] = ht;
     }
     // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
     if (k >= 1) {
-        T d33 = ld(qr + P) * ld(c.ap2je + k) + ld(qr) * ld(c.ac2je + k) + ld(qr - P) * ld(c.am2je + k);
-        T dpx22 = (p_c - ld(pr - P)) * ld(a.cf + nrr + k);
-        T old = a.use_ru ? a.ru2[o] : (T)0;
-        a.rhs_r[o] = gadt * hr + rodt * old + alredt * d33 - dpx22;
+        T rhs = gadt * hr;
+        if (use_ru) rhs += rodt * a.ru2[o];
+        rhs += ld(ic + 3 * nrr + k) * ld(qr + P);
+        rhs += ld(ic + 4 * nrr + k) * ld(qr);
+        rhs += ld(ic + 5 * nrr + k) * ld(qr - P);
+        a.rhs_r[o] = rhs - (p_c - ld(pr - P)) * ld(a.cf + nrr + k);
         a.ru2[o] = hr;
     }
     // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
     {
-        T d33;
+        T rhs = gadt * hz;
+        // At the outer wall the reference has already replaced ru3(nrm) by
+        // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
+        if (k == nr - 1) rhs += rodt * hz;
+        else if (use_ru) rhs += rodt * a.ru3[o];
         if (k == 0) {
             T app = ld(c.ap3j);
             T acc = ld(c.ac3j) * fic + a.ac3j_fs0 * (one - fic);
             T amm = ld(c.am3j) * fic + a.am3j_fs0 * (one - fic);
             T q0 = ld(qz);
-            d33 = ld(qz + P) * app + q0 * acc + q0 * amm;
+            rhs += alredt * (ld(qz + P) * app + q0 * acc + q0 * amm);
         } else if (k == nr - 1) {
             T app = ld(c.ap3j + k) * foc + a.ap3j_fs1 * (one - foc);
             T acc = ld(c.ac3j + k) * foc + a.ac3j_fs1 * (one - foc);
             T q0 = ld(qz);
-            d33 = q0 * app + q0 * acc + ld(qz - P) * ld(c.am3j + k);
+            rhs += alredt * (q0 * app + q0 * acc + ld(qz - P) * ld(c.am3j + k));
         } else {
-            d33 = ld(qz + P) * ld(c.ap3j + k) + ld(qz) * ld(c.ac3j + k) + ld(qz - P) * ld(c.am3j + k);
+            rhs += ld(ic + 6 * nrr + k) * ld(qz + P);
+            rhs += ld(ic + 7 * nrr + k) * ld(qz);
+            rhs += ld(ic + 8 * nrr + k) * ld(qz - P);
         }
-        T dpx33 = (p_c - ld(pr + S.djm)) * ld(a.cf + 2 * nrr);
-        // At the outer wall the reference has already replaced ru3(nrm) by
-        // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
-        T old = (k == nr - 1) ? hz : (a.use_ru ? a.ru3[o] : (T)0);
-        a.rhs_z[o] = gadt * hz + rodt * old + alredt * d33 - dpx33;
+        a.rhs_z[o] = rhs - (p_c - ld(pr + S.djm)) * ld(a.cf + 2 * nrr);
         a.ru3[o] = hz;
     }
 }
@@ -504,8 +524,9 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
 // products the radial and z terms share (h12d and h21; h23 and h32) are
 // formed once.  The FP64 path is bound by the FP64 pipe, so each shared
 // product or sum is a cycle saved.  Term by term the arithmetic is that of
-// explicit_qt/qr/qz; only the rounding order of a few sums differs.
-template <typename T>
+// explicit_qt/qr/qz; only the rounding order of a few sums differs.  RU as
+// for implicit_cell.
+template <typename T, int RU = -1>
 __device__ __forceinline__ void momentum_pair(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
                                               int k) {
     const Stencil Sa = make_stencil(d, i, j, k), Sb = make_stencil(d, i + 1, j, k);
@@ -631,8 +652,8 @@ __device__ __forceinline__ void momentum_pair(const Dims& d, const CoefT<T>& c, 
             hz[1] = -(h31 + h32 + h33) + dqz1 + dqz2;
         }
     }
-    implicit_cell(d, c, a, Sa, i, j, k, ht[0], hr[0], hz[0]);
-    implicit_cell(d, c, a, Sb, i + 1, j, k, ht[1], hr[1], hz[1]);
+    implicit_cell<T, RU>(d, c, a, Sa, i, j, k, ht[0], hr[0], hz[0]);
+    implicit_cell<T, RU>(d, c, a, Sb, i + 1, j, k, ht[1], hr[1], hz[1]);
 }
 
 // The fused momentum work (explicit terms and implicit right-hand sides of
@@ -1571,6 +1592,7 @@ inline MomArgs<T> make_mom_args(const Consts& k, const FieldsT<T>& f, int sub) {
     const int nrr = f.F.stride;
     a.cf = f.corr + (size_t)sub * 3 * nrr;
     a.mr = f.corr + (size_t)9 * nrr + sub * 3;
+    a.ic = f.corr + kImpCoef(nrr) + (size_t)sub * 9 * nrr;
     return a;
 }
 

@@ -151,7 +151,13 @@ __host__ __device__ inline int ptri_slots(int nr) {
 // [ kDivCoef(nr+1) + 6*(nr+1) + s ]            dz = dxz usdt f
 __host__ __device__ inline size_t kPresCoef(int nrr) { return (size_t)9 * nrr + 9; }
 __host__ __device__ inline size_t kDivCoef(int nrr) { return kPresCoef(nrr) + (size_t)3 * nrr + 1; }
-__host__ __device__ inline size_t kCorrCount(int nrr) { return kDivCoef(nrr) + (size_t)6 * nrr + 3; }
+// and for the momentum right-hand sides of substep s, alre(s) dt times the
+// radial coefficients of component c (0 = qt: ap1j, ac1j, am1j; 1 = qr:
+// ap2je, ac2je, am2je; 2 = qz: ap3j, ac3j, am3j), coefficient e (0 = ap,
+// 1 = ac, 2 = am):
+// [ kImpCoef(nr+1) + ((s*3 + c)*3 + e)*(nr+1) + k ]
+__host__ __device__ inline size_t kImpCoef(int nrr) { return kDivCoef(nrr) + (size_t)6 * nrr + 3; }
+__host__ __device__ inline size_t kCorrCount(int nrr) { return kImpCoef(nrr) + (size_t)27 * nrr; }
 
 // Factors of the row-scaled momentum matrices of one step: for each substep
 // s (3), component c (0 = qt, 1 = qr, 2 = qz) and slip variant v (0 = no

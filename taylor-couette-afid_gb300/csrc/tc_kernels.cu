@@ -130,13 +130,14 @@ __global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomAr
 // (124 registers, 4 blocks per SM): capped at 5 blocks (96 registers)
 // 6.78 ms and at 6 (80, spilling) 6.78 ms against 6.63 ms on the
 // 512x512x128 grid.
-template <typename T>
+// RU: whether the substep reads the RK memory (compiled both ways).
+template <typename T, int RU>
 __global__ void __launch_bounds__(128) momentum_pair_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
     if (a.st->halt) return;
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.nt || j >= d.nz) return;
-    momentum_pair(d, c, a, i, j, blockIdx.z);
+    momentum_pair<T, RU>(d, c, a, i, j, blockIdx.z);
 }
 
 // FP32 march of two theta-neighbouring columns a thread in packed FP32
@@ -639,7 +640,8 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
         } else {
             const dim3 pblk(32, 4, 1);
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);
-            momentum_pair_kernel<T><<<pg, pblk, 0, s>>>(d, c, a);
+            if (a.use_ru) momentum_pair_kernel<T, 1><<<pg, pblk, 0, s>>>(d, c, a);
+            else momentum_pair_kernel<T, 0><<<pg, pblk, 0, s>>>(d, c, a);
         }
     }
     else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
