@@ -29,15 +29,17 @@ namespace tcgb {
 namespace {
 
 // Theta-FFT blocks of the single-run path: threads, and rows R per block
-// chosen as the largest power of two (<= 32) with R * M <= kThSpan.  On the
-// 512x512x128 grid 128 threads with R * M <= 512 measured fastest (FP32
-// divergence + FFT 0.158 ms a launch; 256 threads: 0.168-0.192; 512:
-// 0.207-0.243).
+// chosen as the largest power of two (<= 32) with R * M <= the span.  On the
+// 512x512x128 grid (M = 256, radix-8 FP32 stages), 128 threads: divergence +
+// forward FFT with spans 512 / 1024 / 2048 0.150 / 0.158 / 0.233 ms (FP32)
+// and 1.237 / 1.232 / 1.259 ms (FP64); inverse FFT 0.107 / 0.100 / 0.146 ms
+// (FP32) and 0.897 / 0.898 / 0.921 ms (FP64); 64 or 256 threads no faster.
 constexpr int kThThreads = 128;
-constexpr int kThSpan = 512;
-static int theta_rows_run(int M) {
+constexpr int kThSpan = 512;       // divergence + forward transform
+constexpr int kThSpanInv = 1024;   // inverse transform
+static int theta_rows_run(int M, int span = kThSpan) {
     int R = 1;
-    while (R < 32 && (R * 2) * M <= kThSpan) R *= 2;
+    while (R < 32 && (R * 2) * M <= span) R *= 2;
     return R;
 }
 
@@ -723,7 +725,7 @@ static void theta_inv_R(cudaStream_t s, const Dims& d, const FieldsT<T>& f, cons
 
 template <typename T>
 void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
-    int R = theta_rows_run(p.th.n);
+    int R = theta_rows_run(p.th.n, kThSpanInv);
     switch (R) {
         case 1: theta_inv_R<1, T>(s, d, f, p); break;
         case 2: theta_inv_R<2, T>(s, d, f, p); break;
