@@ -214,11 +214,12 @@ __global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<
               reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
+// Compiled for 7 resident blocks per SM (73 registers): on the 512x512x128
+// grid the float-float solve of the mixed path takes 0.133 ms a launch
+// against 0.140 ms with 8 blocks (64 registers, a few spilled), 0.156 ms with
+// 10 and 0.183 ms with 6; the FP64 solve 0.230 ms with 7 or 8.
 template <typename T>
-// Compiled for 8 resident blocks per SM (64 registers, a few spilled): on
-// the 512x512x128 grid 0.217 ms a launch (FP32 spectrum) and 0.234 ms (FP64)
-// against 0.246 and 0.245 ms with 122 and 96 registers.
-__global__ void __launch_bounds__(128, 8) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {
+__global__ void __launch_bounds__(128, 7) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)d.nz * d.PH) return;
