@@ -187,6 +187,7 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
                 double* pc = corrd + kPresCoef(nr + 1);
                 const double u = c.udx1qm[row];
                 pc[row] = beta * (2.0 * u + 2.0 * k.dxzq - c.acph[row]);
+                pc[3 * (nr + 1) + 1 + row] = 1.0 + pc[row];
                 pc[(nr + 1) + row] = -beta * u;
                 pc[2 * (nr + 1) + row] = -beta * c.apph[row];
                 if (row == 0) pc[3 * (nr + 1)] = -beta * k.dxzq;
@@ -1465,13 +1466,19 @@ __device__ __forceinline__ void correct_cell(const Dims& d, const FieldsT<T>& f,
         const T pjp = ld(phi + (size_t)k * P + (size_t)jp * nt + i);
         const T pkp = ld(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i);
         const T* pc = f.corr + kPresCoef(nr + 1);
-        T inc = loc + ld(pc + k) * loc;
-        inc += ld(pc + (nr + 1) + k) * (pip + pim);
-        inc += ld(pc + 3 * (nr + 1)) * (pjp + pjm);
-        inc += ld(pc + 2 * (nr + 1) + k) * (pkp + pkm);
-        if (std::is_same<T, double>::value) {
-            f.pr[o] = f.pr[o] + (double)inc;
+        if constexpr (std::is_same<T, double>::value) {
+            // pr + (1 + pe) phi + ...: the sum starts from pr
+            double p = f.pr[o];
+            p += ld(pc + 3 * (nr + 1) + 1 + k) * loc;
+            p += ld(pc + (nr + 1) + k) * (pip + pim);
+            p += ld(pc + 3 * (nr + 1)) * (pjp + pjm);
+            p += ld(pc + 2 * (nr + 1) + k) * (pkp + pkm);
+            f.pr[o] = p;
         } else {
+            T inc = loc + ld(pc + k) * loc;
+            inc += ld(pc + (nr + 1) + k) * (pip + pim);
+            inc += ld(pc + 3 * (nr + 1)) * (pjp + pjm);
+            inc += ld(pc + 2 * (nr + 1) + k) * (pkp + pkm);
             // mixed path: the increment from the FP32 phi in FP32, accumulated
             // into the FP64 pressure; the FP32 copy used by the momentum rhs is
             // refreshed from the FP64 sum (conversions on the integer pipes)

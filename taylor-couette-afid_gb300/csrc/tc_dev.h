@@ -144,13 +144,15 @@ __host__ __device__ inline int ptri_slots(int nr) {
 // [ kPresCoef(nr+1) + (nr+1) + k ]     pt = -be udx1qm
 // [ kPresCoef(nr+1) + 2 (nr+1) + k ]   pq = -be apph
 // [ kPresCoef(nr+1) + 3 (nr+1) ]       pz = -be dxzq
+// [ kPresCoef(nr+1) + 3 (nr+1) + 1 + k ] 1 + pe (the FP64 update starts
+//                                        from pr + (1 + pe) phi)
 // and for the divergence of substep s, with usdt(s) = 1/(al(s) dt) and the
 // FFT normalisation f folded in (CalcLocalDivergence.F90:27-40 times usdt f):
 // [ kDivCoef(nr+1) + s*2*(nr+1) + k ]          dt_k = dxt usrm(k) usdt f
 // [ kDivCoef(nr+1) + s*2*(nr+1) + (nr+1) + k ] dr_k = udx2m(k) usrm(k) usdt f
 // [ kDivCoef(nr+1) + 6*(nr+1) + s ]            dz = dxz usdt f
 __host__ __device__ inline size_t kPresCoef(int nrr) { return (size_t)9 * nrr + 9; }
-__host__ __device__ inline size_t kDivCoef(int nrr) { return kPresCoef(nrr) + (size_t)3 * nrr + 1; }
+__host__ __device__ inline size_t kDivCoef(int nrr) { return kPresCoef(nrr) + (size_t)4 * nrr + 1; }
 // and for the momentum right-hand sides of substep s, alre(s) dt times the
 // radial coefficients of component c (0 = qt: ap1j, ac1j, am1j; 1 = qr:
 // ap2je, ac2je, am2je; 2 = qz: ap3j, ac3j, am3j), coefficient e (0 = ap,
