@@ -96,7 +96,7 @@ def algorithmic_bytes(cls: str, nt: int, nz: int, nr: int, rk_substep_mix: float
 # read and written, pr read and written and one spectral round trip of phi per
 # substep, plus the RK memory ru (read in substeps 2-3, written in 1-2).
 # The FP64 fused momentum kernel (two cells a thread) measured by ncu on the
-# 512x512x128 grid, one RK3 step (profiles/momentum_kernel_fp64_P2.md): DRAM
+# 512x512x128 grid, one RK3 step (ncu --set full, one launch per substep): DRAM
 # bytes per cell of a launch averaged over the three substeps (79.2, 102.9,
 # 102.8), and per cell its FP64 instructions (45.41 DADD + 20.98 DMUL +
 # 42.45 DFMA) and FLOPs.  Per-cell figures do not depend on the grid size.

@@ -5,8 +5,8 @@
  * reference has no plugin API: its routines take no arguments and talk
  * through the Fortran modules `param` and `local_arrays` (param.F90:4-102).
  * Each entry point below replaces the reference routine(s) named in its
- * comment; a Fortran host binds them with ISO_C_BINDING (see INTEGRATION.md
- * and taylor-couette-afid_gb300/fortran/tc_gpu_mod.F90).
+ * comment; a Fortran host binds them with ISO_C_BINDING through the module
+ * taylor-couette-afid_gb300/fortran/tc_gpu_mod.F90.
  *
  * Conventions
  *  - Every function returns an int status: 0 = OK.  165, 166, 169, 266, 333
@@ -52,10 +52,12 @@ typedef struct tc_ensemble tc_ensemble;
 /* Precision of a handle.  TC_PREC_FP64: the plain path, every operation in
  * IEEE FP64 (the drop-in).  TC_PREC_MIXED: velocity fields, explicit terms,
  * implicit momentum sweeps and FFTs in FP32 with FP32 accumulation; the
- * radial pressure tridiagonals, the pressure accumulation of CorrectPressure
- * and the CFL/divergence/torque reductions in FP64.  Host arrays are FP64
- * in both. */
-enum tc_precision_mode { TC_PREC_FP64 = 0, TC_PREC_MIXED = 1 };
+ * radial pressure tridiagonals (on the FP32 spectrum, widened), the pressure
+ * accumulation of CorrectPressure and the CFL/divergence/torque reductions
+ * in FP64.  TC_PREC_MIXED_FF: TC_PREC_MIXED with the pressure tridiagonals
+ * in float-float arithmetic (about 48 significant bits, on the FP32 pipes)
+ * instead of FP64.  Host arrays are FP64 in all three. */
+enum tc_precision_mode { TC_PREC_FP64 = 0, TC_PREC_MIXED = 1, TC_PREC_MIXED_FF = 2 };
 
 /* 1-D grid/coefficient arrays, 0-based (entry m = reference index m+1). */
 enum tc_grid_array {
@@ -87,7 +89,7 @@ enum tc_field {
  * (malformed).  err (may be NULL) receives a message. */
 int tc_read_bou(const char* path, tc_bou* out, char* err, int errlen);
 
-/* CreateGrid.F90:24-324 and InitPressureSolver.F90:22-110 on the host:
+/* CreateGrid.F90:24-324 and InitPressureSolver.F90:22-66 on the host:
  * writes grid array `which` (enum tc_grid_array) into out[0..len-1] and
  * returns its length, or a negative status on bad input. */
 int tc_grid_array(const tc_bou* cfg, int which, double* out, int len);
@@ -214,28 +216,50 @@ int tc_run(tc_handle* h, int nsteps, int* ntime, double* time, double* dt);
  * (1-based) is selected with tc_set_substep. */
 int tc_begin_step(tc_handle* h, double dt, double time);
 int tc_set_substep(tc_handle* h, int ns);
-/* ExplicitTermsQT/QR/QZ (ExplicitTermsQT.F90:22-129, ExplicitTermsQR.F90:159-280,
- * ExplicitTermsQZ.F90:311-390): explicit terms into DQ, HR, QCAP. */
+/* One routine each, as TimeMarcher.F90:31-37 calls them (the per-substep
+ * coefficients al, ga, ro of the substep chosen with tc_set_substep).
+ * ExplicitTermsQT.F90:22-129: explicit terms of qt into DQ. */
+int tc_explicit_terms_qt(tc_handle* h);
+/* ExplicitTermsQR.F90:25-149: explicit terms of qr (faces k = 2..nrm) into
+ * HR (the reference keeps them in dph). */
+int tc_explicit_terms_qr(tc_handle* h);
+/* ExplicitTermsQZ.F90:23-106: explicit terms of qz into QCAP. */
+int tc_explicit_terms_qz(tc_handle* h);
+/* ImplicitAndUpdateQT.F90:26-117: rhs and ru1 from DQ, then
+ * SolveImpEqnUpdate_QT (SolveImpEqnUpdate_QT.F90:22-80): the radial solve
+ * with the inner-wall term of the oscillating cylinder, qt += dq. */
+int tc_implicit_and_update_qt(tc_handle* h);
+/* ImplicitAndUpdateQR.F90:28-71: rhs and ru2 from HR, then
+ * SolveImpEqnUpdate_QR (SolveImpEqnUpdate_QR.F90:25-67), qr += dq, and qr
+ * set to 0 on both walls. */
+int tc_implicit_and_update_qr(tc_handle* h);
+/* ImplicitAndUpdateQZ.F90:24-119: rhs and ru3 from QCAP (outer-wall row
+ * with the reference's overwritten ru3(nrm)), then SolveImpEqnUpdate_QZ
+ * (SolveImpEqnUpdate_QZ.F90:21-70), qz += dq. */
+int tc_implicit_and_update_qz(tc_handle* h);
+/* SolveImpEqnUpdate_QT/QR/QZ alone, each on its RHS_T/R/Z array. */
+int tc_solve_imp_eqn_update_qt(tc_handle* h);
+int tc_solve_imp_eqn_update_qr(tc_handle* h);
+int tc_solve_imp_eqn_update_qz(tc_handle* h);
+/* The three components in one launch each (what the fused time step runs):
+ * tc_explicit_terms = ExplicitTermsQT + QR + QZ; tc_implicit_and_update =
+ * ImplicitAndUpdateQT + QR + QZ with their solves; tc_solve_imp_eqn_update
+ * = the three solves. */
 int tc_explicit_terms(tc_handle* h);
-/* ImplicitAndUpdateQT/QR/QZ (ImplicitAndUpdateQT.F90:26-117,
- * ImplicitAndUpdateQR.F90:152-195, ImplicitAndUpdateQZ.F90:223-312) with
- * SolveImpEqnUpdate_QT/QR/QZ (SolveImpEqnUpdate_QT.F90:22-80,
- * _QR.F90:109-151, _QZ.F90:177-225): rhs and ru from DQ/HR/QCAP, radial
- * implicit solve, q += dq, qr walls reset. */
 int tc_implicit_and_update(tc_handle* h);
-/* Explicit terms fused with the rhs and ru update (no DQ/HR/QCAP arrays);
- * equivalent to the explicit half of the two calls above. */
-int tc_explicit_and_rhs(tc_handle* h);
-/* SolveImpEqnUpdate_QT/QR/QZ alone, on the RHS_T/R/Z arrays. */
 int tc_solve_imp_eqn_update(tc_handle* h);
+/* Explicit terms fused with the rhs and ru update (no DQ/HR/QCAP arrays);
+ * equivalent to tc_explicit_terms followed by the rhs half of
+ * tc_implicit_and_update. */
+int tc_explicit_and_rhs(tc_handle* h);
 /* CalcLocalDivergence.F90:19-40: DPH = div(q)/(al*dt). */
 int tc_calc_local_divergence(tc_handle* h);
-/* SolvePressureCorrection.F90:129-290: DPH <- phi.  The singular
+/* SolvePressureCorrection.F90:100-163: DPH <- phi.  The singular
  * k_theta = k_z = 0 mode is solved with phi(nrm) = 0 (its last equation is
  * the dependent one); LAPACK in the reference divides by a roundoff pivot
  * there instead, which only moves phi by a radially constant offset. */
 int tc_solve_pressure_correction(tc_handle* h);
-/* CorrectVelocity.F90:302-340 and CorrectPressure.F90:352-393. */
+/* CorrectVelocity.F90:28-47 and CorrectPressure.F90:23-49. */
 int tc_correct_velocity(tc_handle* h);
 int tc_correct_pressure(tc_handle* h);
 
@@ -243,14 +267,16 @@ int tc_correct_pressure(tc_handle* h);
 
 /* CalcMaxCFL.F90:12-49 */
 int tc_calc_max_cfl(tc_handle* h, double* cflm);
-/* CheckDivergence.F90:60-95 */
+/* CheckDivergence.F90:21-43.  A NaN in the fields makes *qmax NaN and the
+ * status 169 (the reference's divergence error code): Fortran's MAX would
+ * skip the NaN and report a finite divergence. */
 int tc_check_divergence(tc_handle* h, double* qmax);
-/* CalcTorque.F90:107-157 (the host writes torquenu.out itself). */
+/* CalcTorque.F90:26-57 (the host writes torquenu.out itself). */
 int tc_calc_torque(tc_handle* h, double* inner, double* outer);
 /* CalcVelocityStats.F90:11-68: vmax(3) and the three rms values. */
 int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3);
 
-/* CheckDivergence.F90:60-95 on velocity arrays the caller keeps on the
+/* CheckDivergence.F90:28-43 on velocity arrays the caller keeps on the
  * current CUDA device, without a handle and without allocating device
  * memory.  No counterpart in the reference.
  *  - qt, qr, qz: device arrays in the reference layout
@@ -260,7 +286,11 @@ int tc_calc_velocity_stats(tc_handle* h, double* vmax3, double* rms3);
  *    (tc_grid_array TC_G_UDX2M, TC_G_USRM); dxt = nthm*LAMB/(2 pi),
  *    dxz = nzm/ALX3 (dx1, dx3 of CreateGrid.F90:28-34).
  *  - stream: cudaStream_t the work is ordered on (NULL = legacy default);
- *    the call synchronises it and returns the maximum |div| in *qmax.
+ *    the call synchronises it and returns the maximum |div| in *qmax.  A NaN
+ *    in the fields makes *qmax NaN and the status 169, as tc_check_divergence.
+ *    The call copies the coefficients from pageable host memory and waits
+ *    for the stream, so it cannot run inside a stream capture: on a stream
+ *    that is being captured it returns 2018 and enqueues nothing.
  * Its scratch (coefficients, per-block maxima, result) is one static
  * 130 KB device array per device, not memory of the caller's: nrm above
  * 8192 is rejected with 2016.  Nothing in it must start at zero; every

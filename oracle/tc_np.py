@@ -5,7 +5,7 @@ TEST INFRASTRUCTURE ONLY: used by tests/ to cross-check the C++ oracle
 
 Unlike the C++ oracle this one is vectorised with NumPy, calls the real LAPACK
 ``dgttrf/dgttrs/zgttrf/zgttrs`` through ``scipy.linalg.lapack`` (the routines the
-reference links, SolveImpEqnUpdate_QT.F90:63,74, SolvePressureCorrection.F90:256,258)
+reference links, SolveImpEqnUpdate_QT.F90:63,74, SolvePressureCorrection.F90:139,141)
 and ``numpy.fft`` (pocketfft) in place of FFTW.  Arrays use the reference memory
 layout: a NumPy array of shape (nthm+2, nzm+2, nr) in C order is the Fortran
 array q(1:nr, 0:nzm+1, 0:nthm+1); index [i, j, k-1].
@@ -123,7 +123,7 @@ class NpOracle:
         self.kpv = np.array([0] + [min(kc + 1, nrm) for kc in range(1, nr + 1)])
         self.kmv[nr] = 0
         self.kpv[nr] = 0
-        # q1 coefficients (:194-238)
+        # q1 coefficients (CreateGrid.F90:191-238)
         ap1j, am1j, ac1j = z(), z(), z()
         for kc in range(2, nrm):
             a22 = dxrq / g2rm[kc] / rm[kc]
@@ -141,7 +141,7 @@ class NpOracle:
         self.ap1j_fs = [0.0, rc[2] ** 3 / (rm[1] ** 2 * rm[2]) * dxrq * urpp, 0.0]
         self.ac1j_fs = [0.0, -rc[2] ** 3 / rm[1] ** 3 * dxrq * urpp, 0.0]
         self.am1j_fs = [0.0, 0.0, 0.0]
-        # q2 (:244-276)
+        # q2 (CreateGrid.F90:241-276)
         ap2j, am2j, ac2j, ap2je, am2je, ac2je = (z() for _ in range(6))
         ac2j[1] = 1.0
         ac2j[nr] = 1.0
@@ -154,7 +154,7 @@ class NpOracle:
             b22m = rm[kc - 1] / (rc[kc - 1] * g2rm[kc - 1])
             b22 = (rm[kc] / g2rm[kc] + rm[kc - 1] / g2rm[kc - 1]) / rc[kc]
             ap2je[kc], am2je[kc], ac2je[kc] = b22p * ugmm, b22m * ugmm, -b22 * ugmm - 1.0 / rc[kc] ** 2
-        # q3 (:281-322)
+        # q3 (CreateGrid.F90:279-322)
         ap3j, am3j, ac3j = z(), z(), z()
         for kc in range(2, nrm):
             a22 = dxrq / g2rm[kc] / rm[kc]
@@ -319,7 +319,7 @@ class NpOracle:
         f[..., 0] = (rhs[..., 0] + 0.5 * al * dt * self.dvinner_t * self.am1j[1] / b["ren"]) * ackl_b[0]
         x = self._solve_cols(amk[1:], np.ones(nrm), apk[:-1], f.reshape(-1, nrm).T)
         qt[I, J, :nrm] += x.T.reshape(nthm, nzm, nrm)
-        # ---- QR: ImplicitAndUpdateQR.F90:152-195 + SolveImpEqnUpdate_QR.F90:109-151
+        # ---- QR: ImplicitAndUpdateQR.F90:39-71 + SolveImpEqnUpdate_QR.F90:25-67
         qr = self.qr
         kr = np.arange(2, nrm + 1)
         d33 = qr[I, J, 2:nr] * self.ap2je[kr] + qr[I, J, 1:nrm] * self.ac2je[kr] + qr[I, J, 0:nrm - 1] * self.am2je[kr]
@@ -337,7 +337,7 @@ class NpOracle:
         qr[I, J, 1:nrm] += x.T.reshape(nthm, nzm, nr)[..., 1:nrm]
         qr[..., 0] = 0.0
         qr[..., nr - 1] = 0.0
-        # ---- QZ: ImplicitAndUpdateQZ.F90:235-312 + SolveImpEqnUpdate_QZ.F90:188-225
+        # ---- QZ: ImplicitAndUpdateQZ.F90:36-117 + SolveImpEqnUpdate_QZ.F90:32-70
         qz = self.qz
         ap, ac, am = self.ap3j[kc].copy(), self.ac3j[kc].copy(), self.am3j[kc].copy()
         d33 = np.empty((nthm, nzm, nrm))
@@ -371,7 +371,7 @@ class NpOracle:
              * self.usrm[kc] + (qz[I, Jp, :nrm] - qz[I, J, :nrm]) * self.dxz)
         return d
 
-    # SolvePressureCorrection.F90:217-280
+    # SolvePressureCorrection.F90:100-163
     def solve_pressure(self, div):
         nrm, nthm, nzm = self.nrm, self.nthm, self.nzm
         rhs = div / (self.al * self.dt)                      # [i, j, k]
@@ -397,7 +397,7 @@ class NpOracle:
         phi = np.fft.irfft(p, n=nzm, axis=1) * nzm
         return phi
 
-    # CorrectVelocity.F90:318-337 and CorrectPressure.F90:364-390
+    # CorrectVelocity.F90:28-47 and CorrectPressure.F90:31-49
     def correct(self, phi):
         nrm, nthm, nzm, nr = self.nrm, self.nthm, self.nzm, self.nr
         d = self.dph

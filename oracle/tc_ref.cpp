@@ -292,7 +292,7 @@ void TCRef::create_grid() {
         udx2cc[k] = dxr / g2rcc[k];
     }
 
-    // coefficients for q1, inner points (:194-203)
+    // coefficients for q1, inner points (CreateGrid.F90:194-203)
     for (int kc = 2; kc <= nrm - 1; ++kc) {
         int kp = kc + 1;
         double a22 = dxrq / g2rm[kc] / rm[kc];
@@ -301,7 +301,7 @@ void TCRef::create_grid() {
         ap1j[kc] = a22p; am1j[kc] = a22m;
         ac1j[kc] = -(a22p + a22m) - 1.0 / sq(rm[kc]);
     }
-    {   // external bc (:209-220)
+    {   // external bc (CreateGrid.F90:209-220)
         int kc = nrm, kp = kc + 1;
         double a22 = dxrq / (g2rm[kc] * rm[kc]);
         double apjjc = a22 * rc[kp] / g2rc[kp];
@@ -311,7 +311,7 @@ void TCRef::create_grid() {
         am1j[kc] = amjjc;
         ap1j_fs[1] = 0.0; ac1j_fs[1] = -amjjc; am1j_fs[1] = amjjc;
     }
-    {   // internal bc (:226-238); overwrites the *_fs(1) entries set above
+    {   // internal bc (CreateGrid.F90:226-238); overwrites the *_fs(1) entries set above
         int kc = 1, kp = kc + 1;
         double urpp = 1.0 / (g2rm[kc] * g2rc[kp]);
         double a22 = dxrq / g2rm[kc] / rm[kc];
@@ -324,7 +324,7 @@ void TCRef::create_grid() {
         ac1j_fs[1] = -std::pow(rc[kp], 3) / std::pow(rm[kc], 3) * dxrq * urpp;
         am1j_fs[1] = 0.0;
     }
-    // q2 (:244-259)
+    // q2 (CreateGrid.F90:244-259)
     am2j[1] = 0.0; ap2j[1] = 0.0; ac2j[1] = 1.0;
     for (int kc = 2; kc <= nrm; ++kc) {
         int km = kc - 1;
@@ -335,7 +335,7 @@ void TCRef::create_grid() {
         ac2j[kc] = -(a22 * a22p + a22 * a22m);
     }
     am2j[nr] = 0.0; ap2j[nr] = 0.0; ac2j[nr] = 1.0;
-    // q2 explicit part (:266-276)
+    // q2 explicit part (CreateGrid.F90:266-276)
     for (int kc = 2; kc <= nrm; ++kc) {
         int km = kc - 1, kp = kc + 1;
         double ugmm = dxrq / g2rc[kc];
@@ -345,7 +345,7 @@ void TCRef::create_grid() {
         ap2je[kc] = a22p * ugmm; am2je[kc] = a22m * ugmm;
         ac2je[kc] = -a22 * ugmm - 1.0 / sq(rc[kc]);
     }
-    // q3 inner (:281-290)
+    // q3 inner (CreateGrid.F90:281-290)
     for (int kc = 2; kc <= nrm - 1; ++kc) {
         int kp = kc + 1;
         double a22 = dxrq / g2rm[kc] / rm[kc];
@@ -353,7 +353,7 @@ void TCRef::create_grid() {
         double a22m = +a22 * rc[kc] / g2rc[kc];
         ap3j[kc] = a22p; am3j[kc] = a22m; ac3j[kc] = -(a22p + a22m);
     }
-    {   // q3 internal bc (:296-306)
+    {   // q3 internal bc (CreateGrid.F90:296-306)
         int kc = 1, kp = kc + 1;
         double a22 = dxrq / g2rm[kc] / rm[kc];
         double a22p = +a22 * rc[kp] / g2rc[kp];
@@ -361,7 +361,7 @@ void TCRef::create_grid() {
         am3j[kc] = 0.0; ap3j[kc] = a22p; ac3j[kc] = -(a22p + 2.0 * a22m);
         am3j_fs[1] = 0.0; ap3j_fs[1] = a22p; ac3j_fs[1] = -(a22p);
     }
-    {   // q3 external bc (:311-322)
+    {   // q3 external bc (CreateGrid.F90:311-322)
         int kc = nrm, kp = kc + 1;
         double a22 = dxrq / g2rm[kc] / rm[kc];
         double a22m = +a22 * rc[kc] / g2rc[kc];
@@ -392,7 +392,7 @@ void TCRef::slip_bcs() {
         if (thdispl[i] == 0) thdispl[i] = nthm;
     }
     if (ntot != 0) {
-        // The reference divides integers by ntott and ntotz here (:523-524);
+        // The reference divides integers by ntott and ntotz here (SlipBCs.F90:58-59);
         // with either being zero that is an integer division by zero.  Such
         // inputs are rejected before this point (tcref_create returns NULL).
         for (auto& v : icylsl) v = 0;
@@ -616,7 +616,7 @@ void tcref_explicit_terms_qt(void* h) {
     }
 }
 
-// ExplicitTermsQR.F90:159-280 (writes dph for kc = 2..nrm)
+// ExplicitTermsQR.F90:40-149 (writes dph for kc = 2..nrm)
 void tcref_explicit_terms_qr(void* h) {
     TCRef& R = *(TCRef*)h;
     const double udxzq = R.dxzq / R.b.ren, udxz = R.dxz * 0.25;
@@ -650,7 +650,7 @@ void tcref_explicit_terms_qr(void* h) {
     }
 }
 
-// ExplicitTermsQZ.F90:311-390
+// ExplicitTermsQZ.F90:34-106
 void tcref_explicit_terms_qz(void* h) {
     TCRef& R = *(TCRef*)h;
     const double udxz = R.dxz * 0.25, udxzq = R.dxzq / R.b.ren;
@@ -689,7 +689,7 @@ void tcref_implicit_rhs_qt(void* h) {
         int imm = ic - 1;
         for (int jc = 1; jc <= R.nzm; ++jc) {
             double fic = (double)R.icylsl[R.S(jc, ic)], foc = (double)R.ocylsl[R.S(jc, ic)];
-            // inner cylinder (:45-68)
+            // inner cylinder (ImplicitAndUpdateQT.F90:44-68)
             int kc = 1, kpp = 2;
             double app = R.ap1j[kc];
             double acc = (R.ac1j[kc] * fic + R.ac1j_fs[1] * (1 - fic));
@@ -699,7 +699,7 @@ void tcref_implicit_rhs_qt(void* h) {
             size_t n = R.N(kc, jc, ic);
             R.rhs[n] = (R.ga * R.dq[n] + R.ro * R.ru1[n] + alre * d33qt - dpx11) * R.dt;
             R.ru1[n] = R.dq[n];
-            // inner points (:71-90)
+            // inner points (ImplicitAndUpdateQT.F90:70-90)
             for (kc = 2; kc <= nrm - 1; ++kc) {
                 int kmm = kc - 1; kpp = kc + 1;
                 amm = R.am1j[kc]; acc = R.ac1j[kc]; app = R.ap1j[kc];
@@ -709,7 +709,7 @@ void tcref_implicit_rhs_qt(void* h) {
                 R.rhs[n] = (R.ga * R.dq[n] + R.ro * R.ru1[n] + alre * d33qt - dpx11) * R.dt;
                 R.ru1[n] = R.dq[n];
             }
-            // outer cylinder (:95-115)
+            // outer cylinder (ImplicitAndUpdateQT.F90:93-115)
             kc = nrm;
             int kmm = nrm - 1;
             amm = R.am1j[kc];
@@ -770,7 +770,7 @@ void tcref_solve_imp_eqn_update_qt(void* h) {
     }
 }
 
-// ImplicitAndUpdateQR.F90:152-187 (rhs and ru2 only)
+// ImplicitAndUpdateQR.F90:39-66 (rhs and ru2 only)
 void tcref_implicit_rhs_qr(void* h) {
     TCRef& R = *(TCRef*)h;
     const double alre = R.al / R.b.ren;
@@ -791,7 +791,7 @@ void tcref_implicit_rhs_qr(void* h) {
     }
 }
 
-// SolveImpEqnUpdate_QR.F90:109-151 plus the wall reset of ImplicitAndUpdateQR.F90:194-195
+// SolveImpEqnUpdate_QR.F90:25-67 plus the wall reset of ImplicitAndUpdateQR.F90:70-71
 void tcref_solve_imp_eqn_update_qr(void* h) {
     TCRef& R = *(TCRef*)h;
     const int nrm = R.nrm, nr = R.nr;
@@ -831,7 +831,7 @@ void tcref_solve_imp_eqn_update_qr(void* h) {
         for (int j = 0; j <= R.nzm + 1; ++j) { R.qr[R.H(1, j, i)] = 0.0; R.qr[R.H(nr, j, i)] = 0.0; }
 }
 
-// ImplicitAndUpdateQZ.F90:223-312 (rhs and ru3 only; serial semantics:
+// ImplicitAndUpdateQZ.F90:36-117 (rhs and ru3 only; serial semantics:
 // udxz = dxz*al and ocylsl is the module array).  At kc = nrm the interior
 // loop has already replaced ru3(nrm) by qcap(nrm) when the wall block
 // recomputes rhs(nrm), and amm is left at am3j(nrm) by that loop.
@@ -875,7 +875,7 @@ void tcref_implicit_rhs_qz(void* h) {
     }
 }
 
-// SolveImpEqnUpdate_QZ.F90:177-225
+// SolveImpEqnUpdate_QZ.F90:21-70
 void tcref_solve_imp_eqn_update_qz(void* h) {
     TCRef& R = *(TCRef*)h;
     const int nrm = R.nrm;
@@ -957,7 +957,7 @@ void tcref_calc_local_divergence(void* h) {
     }
 }
 
-// SolvePressureCorrection.F90:166-280: r2c along z, c2c forward along
+// SolvePressureCorrection.F90:100-163: r2c along z, c2c forward along
 // theta, divide by nthm*nzm, per-mode zgttrf/zgttrs in r, c2c backward
 // along theta, c2r along z.  The decomp_2d transposes only move data.
 void tcref_solve_pressure_correction(void* h) {
@@ -975,7 +975,7 @@ void tcref_solve_pressure_correction(void* h) {
                 R.plan_z.exec(a.data(), o.data(), -1);
                 for (int j = 1; j <= nzmh; ++j) sp[R.P(k, j, i)] = o[j - 1];
             }
-        // forward c2c along theta for each (k, j), then normalise (:230)
+        // forward c2c along theta for each (k, j), then normalise (SolvePressureCorrection.F90:113)
 #pragma omp for schedule(static)
         for (int j = 1; j <= nzmh; ++j)
             for (int k = 1; k <= nrm; ++k) {
@@ -985,7 +985,7 @@ void tcref_solve_pressure_correction(void* h) {
                 for (int i = 1; i <= nthm; ++i) sp[R.P(k, j, i)] = cd(o[i - 1].real() / den, o[i - 1].imag() / den);
             }
     }
-    // per-mode radial tridiagonal (:244-265)
+    // per-mode radial tridiagonal (SolvePressureCorrection.F90:127-148)
 #pragma omp parallel
     {
         std::vector<double> dl(nrm), d(nrm), du(nrm), du2(nrm), xr(nrm), xi(nrm);
@@ -1034,7 +1034,7 @@ void tcref_solve_pressure_correction(void* h) {
     }
 }
 
-// CorrectVelocity.F90:318-337
+// CorrectVelocity.F90:28-47
 void tcref_correct_velocity(void* h) {
     TCRef& R = *(TCRef*)h;
 #pragma omp parallel for schedule(static)
@@ -1055,7 +1055,7 @@ void tcref_correct_velocity(void* h) {
         for (int j = 0; j <= R.nzm + 1; ++j) { R.qr[R.H(1, j, i)] = 0.0; R.qr[R.H(R.nr, j, i)] = 0.0; }
 }
 
-// CorrectPressure.F90:364-390 (amm = apph(kc), as in the reference)
+// CorrectPressure.F90:31-49 (amm = apph(kc), as in the reference)
 void tcref_correct_pressure(void* h) {
     TCRef& R = *(TCRef*)h;
     const double be = R.beta;
@@ -1128,7 +1128,7 @@ double tcref_calc_max_cfl(void* h) {
     return cflm;
 }
 
-// CheckDivergence.F90:70-90
+// CheckDivergence.F90:21-43
 double tcref_check_divergence(void* h) {
     TCRef& R = *(TCRef*)h;
     double qmax = 0.0;
@@ -1149,7 +1149,7 @@ double tcref_check_divergence(void* h) {
     return qmax;
 }
 
-// CalcTorque.F90:121-150
+// CalcTorque.F90:26-55
 void tcref_calc_torque(void* h, double* inner, double* outer) {
     TCRef& R = *(TCRef*)h;
     const int nr = R.nr, nrm = R.nrm;

@@ -39,8 +39,8 @@ typedef struct tcref_bou {
 } tcref_bou;
 
 /* Treatment of the singular k_theta = k_z = 0 pressure mode
- * (SolvePressureCorrection.F90:244-265 with the zero-flux rows of
- * InitPressureSolver.F90:66-76). */
+ * (SolvePressureCorrection.F90:127-148 with the zero-flux rows of
+ * InitPressureSolver.F90:22-32). */
 enum {
     TCREF_MODE00_LAPACK = 0,  /* LAPACK ?gttrs arithmetic: divides by the roundoff pivot */
     TCREF_MODE00_PIN = 1      /* drop the last (dependent) row: phi(nrm) = 0 for that mode */

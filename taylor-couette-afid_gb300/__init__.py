@@ -104,6 +104,8 @@ SIGNATURES = {
     "tc_implicit_and_update": (ctypes.c_int, [_vp]),
     "tc_explicit_and_rhs": (ctypes.c_int, [_vp]),
     "tc_solve_imp_eqn_update": (ctypes.c_int, [_vp]),
+    **{f"tc_{r}_{c}": (ctypes.c_int, [_vp]) for r in ("explicit_terms", "implicit_and_update", "solve_imp_eqn_update")
+       for c in ("qt", "qr", "qz")},
     "tc_calc_local_divergence": (ctypes.c_int, [_vp]),
     "tc_solve_pressure_correction": (ctypes.c_int, [_vp]),
     "tc_correct_velocity": (ctypes.c_int, [_vp]),
@@ -215,7 +217,10 @@ def check_divergence_noalloc(qt: int, qr: int, qz: int, nthm: int, nzm: int, nrm
     """CheckDivergence on caller-owned device arrays (addresses of FP64
     arrays in the reference layout, periodic halos current) with no handle
     and no device allocation; udx2m and usrm are host arrays of nrm
-    entries.  Calls on one device must not overlap."""
+    entries.  Calls on one device must not overlap.  A NaN in the fields
+    raises TCError 169 (the reference's divergence error code)."""
+    if len(udx2m) < nrm or len(usrm) < nrm:
+        raise ValueError(f"udx2m and usrm need nrm = {nrm} entries, got {len(udx2m)} and {len(usrm)}")
     u = np.ascontiguousarray(udx2m[:nrm], dtype=np.float64)
     m = np.ascontiguousarray(usrm[:nrm], dtype=np.float64)
     v = ctypes.c_double()
@@ -295,28 +300,30 @@ def h5_write_grid_info(bou: dict, directory: str = "."):
         raise TCError(rc, lib().tc_last_error(None).decode())
 
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_FF = 0, 1, 2
+# precision names of the Python mirror -> enum tc_precision_mode
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-ff": PREC_MIXED_FF}
 
 
 class TaylorCouette:
     """One simulation instance resident on the current CUDA device.
 
-    precision: "fp64" (plain path, the drop-in) or "mixed" (FP32 velocities,
-    explicit terms, momentum sweeps and FFTs; FP64 pressure solve, pressure
-    accumulation and reductions)."""
+    precision: "fp64" (plain path, the drop-in), "mixed" (FP32 velocities,
+    explicit terms, momentum sweeps and FFTs; FP64 pressure tridiagonals,
+    pressure accumulation and reductions) or "mixed-ff" ("mixed" with the
+    pressure tridiagonals in float-float arithmetic)."""
 
     def __init__(self, bou: dict, precision: str = "fp64", _handle=None):
         self.L = lib()
         self.bou = dict(bou)
         self._b = Bou.from_dict(bou)
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         self.precision = precision
         self._owned = _handle is None
         if _handle is None:
             h = ctypes.c_void_p()
-            rc = self.L.tc_create_ex(ctypes.byref(self._b), PREC_MIXED if precision == "mixed" else PREC_FP64,
-                                     ctypes.byref(h))
+            rc = self.L.tc_create_ex(ctypes.byref(self._b), PRECISIONS[precision], ctypes.byref(h))
             if rc != 0:
                 raise TCError(rc, self.L.tc_last_error(None).decode())
         else:
@@ -469,6 +476,34 @@ class TaylorCouette:
     def solve_imp_eqn_update(self):
         self._ck(self.L.tc_solve_imp_eqn_update(self.h))
 
+    # one component each, as TimeMarcher.F90:31-37 calls them
+    def explicit_terms_qt(self):
+        self._ck(self.L.tc_explicit_terms_qt(self.h))
+
+    def explicit_terms_qr(self):
+        self._ck(self.L.tc_explicit_terms_qr(self.h))
+
+    def explicit_terms_qz(self):
+        self._ck(self.L.tc_explicit_terms_qz(self.h))
+
+    def implicit_and_update_qt(self):
+        self._ck(self.L.tc_implicit_and_update_qt(self.h))
+
+    def implicit_and_update_qr(self):
+        self._ck(self.L.tc_implicit_and_update_qr(self.h))
+
+    def implicit_and_update_qz(self):
+        self._ck(self.L.tc_implicit_and_update_qz(self.h))
+
+    def solve_imp_eqn_update_qt(self):
+        self._ck(self.L.tc_solve_imp_eqn_update_qt(self.h))
+
+    def solve_imp_eqn_update_qr(self):
+        self._ck(self.L.tc_solve_imp_eqn_update_qr(self.h))
+
+    def solve_imp_eqn_update_qz(self):
+        self._ck(self.L.tc_solve_imp_eqn_update_qz(self.h))
+
     def calc_local_divergence(self):
         self._ck(self.L.tc_calc_local_divergence(self.h))
 
@@ -544,15 +579,15 @@ class Ensemble:
     cooperative launch per RK substep).  Members are admitted and retired
     between steps; each keeps the single-run arithmetic.
 
-    precision: "fp64" or "mixed" for every member."""
+    precision: "fp64", "mixed" or "mixed-ff" for every member."""
 
     def __init__(self, precision: str = "mixed"):
         self.L = lib()
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         self.precision = precision
         e = ctypes.c_void_p()
-        rc = self.L.tc_ensemble_create(PREC_MIXED if precision == "mixed" else PREC_FP64, ctypes.byref(e))
+        rc = self.L.tc_ensemble_create(PRECISIONS[precision], ctypes.byref(e))
         if rc != 0:
             raise TCError(rc, "tc_ensemble_create")
         self.e = e

@@ -179,15 +179,16 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(c
 }
 
 // mode-wise: item = TPB consecutive (kz, kt) modes
-template <typename T>
-__global__ void __launch_bounds__(256, EnsBlocks<T>::ptri) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
+// FF: the members' pressure solve (ptri_solve); one precision per ensemble
+template <typename T, int FF>
+__global__ void __launch_bounds__(256, (std::is_same<T, float>::value && FF == 0) ? 3 : EnsBlocks<T>::ptri) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
     const long long item = blockIdx.x;
     const int m = find_member(prefix, n, item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long t = (item - prefix[m]) * blockDim.x + threadIdx.x;
     if (t >= (long long)I.d.nz * I.d.PH) return;
-    ptri_solve(I.d, I.c, I.f, t);
+    ptri_solve<T, FF>(I.d, I.c, I.f, t);
 }
 
 // row-wise FFT phases: item = R consecutive (k, j) rows
@@ -242,6 +243,7 @@ int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 struct tc_ensemble {
     int mixed = 0;
+    int precision = TC_PREC_FP64;   // of every member (enum tc_precision_mode)
     cudaStream_t stream = nullptr;
     std::vector<tc_handle*> members;     // slot -> member (nullptr = free)
     std::vector<int> target;             // requested step count per slot (informational)
@@ -432,7 +434,8 @@ int enqueue_step(tc_ensemble* e) {
             default: launch_div<32, T>(e, I, P(PH_DIV), n, sub); break;
         }
         ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 0);
-        ens_ptri_kernel<T><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
+        if (e->precision == TC_PREC_MIXED_FF) ens_ptri_kernel<T, 1><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
+        else ens_ptri_kernel<T, 0><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
         ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 1);
         switch (e->rows_used) {
             case 1: launch_thinv<1, T>(e, I, P(PH_THINV), n); break;
@@ -508,9 +511,10 @@ using namespace tcgb::ens;
 
 int tc_ensemble_create(int precision, tc_ensemble** out) {
     if (!out) return 2000;
-    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED) return 2007;
+    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED && precision != TC_PREC_MIXED_FF) return 2007;
     tc_ensemble* e = new tc_ensemble();
-    e->mixed = precision == TC_PREC_MIXED;
+    e->mixed = precision != TC_PREC_FP64;
+    e->precision = precision;
     *out = e;
     return 0;
 }
@@ -546,7 +550,7 @@ int tc_ensemble_add(tc_ensemble* e, const tc_bou* cfg, double dt, const double* 
         if (e->members[s]->k.nsst != cfg->nsst)
             return efail(e, 2012, "every member of an ensemble needs the same NSST");
     tc_handle* h = nullptr;
-    int r = tc_create_ex(cfg, e->mixed ? TC_PREC_MIXED : TC_PREC_FP64, &h);
+    int r = tc_create_ex(cfg, e->precision, &h);
     if (r) return efail(e, r, tc_last_error(nullptr));
     tc_set_stream(h, e->stream);
     r = tc_set_state(h, qt, qr, qz, pr);

@@ -171,7 +171,7 @@ __device__ void factors_body(const Dims& d, const Coef& c, const Consts& k, Step
             Fd.u(s, 1, 0)[row] = row >= 1 ? -c.ap2j[row] * betadx * ackl_b : 0.0;
             Fd.scale(s, 1)[row] = ackl_b;
         }
-        // CorrectVelocity.F90:325-330 coefficients
+        // CorrectVelocity.F90:35-40 coefficients
         if (ch == 0) {
             corrd[(s * 3 + 0) * (nr + 1) + row] = dt * k.alm[s] * k.dxt * c.usrm[row];
             corrd[(s * 3 + 1) * (nr + 1) + row] = dt * k.alm[s] * c.rudx2c[row];
@@ -353,7 +353,7 @@ __device__ T explicit_qt(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     return -(h11 + (h12d + h12n) + h13) + d11qre + d22qt + d11qt + coriol;
 }
 
-// ExplicitTermsQR.F90:180-280 at face (i, j, k), 1 <= k <= nr-1
+// ExplicitTermsQR.F90:46-146 at face (i, j, k), 1 <= k <= nr-1
 template <typename T>
 __device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A, const T* qt, const T* qr,
                          const T* qz) {
@@ -382,7 +382,7 @@ __device__ T explicit_qr(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
     return -(h21 + h22 + h23) + h11n + d11qr + d22qr + d11qre + coriol;
 }
 
-// ExplicitTermsQZ.F90:328-390 at cell (i, j, k)
+// ExplicitTermsQZ.F90:40-102 at cell (i, j, k)
 template <typename T>
 __device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& A, const T* qt, const T* qr,
                          const T* qz) {
@@ -410,9 +410,11 @@ __device__ T explicit_qz(const Stencil& S, const CoefT<T>& c, const MomArgs<T>& 
 // substep reads the RK memory (rom != 0), at compile time (0, 1) or read from
 // a.use_ru (-1).  Interior levels take alre dt times the radial coefficients
 // from a.ic; the wall levels form their coefficients here, as the reference.
+// mask selects the components (1 qt, 2 qr, 4 qz; the per-routine entry
+// points run one at a time, the fused kernels all three).
 template <typename T, int RU = -1>
 __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, const Stencil& S,
-                                              int i, int j, int k, T ht, T hr, T hz) {
+                                              int i, int j, int k, T ht, T hr, T hz, int mask = 7) {
     const int nr = d.nr;
     const size_t o = S.o;
     const int P = S.P;
@@ -430,7 +432,7 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
     const T* pr = a.pr + o;
     const T p_c = ld(pr);
     // ---- qt (ImplicitAndUpdateQT.F90:45-115)
-    {
+    if (mask & 1) {
         T rhs = gadt * ht;
         if (use_ru) rhs += rodt * a.ru1[o];
         if (k == 0) {
@@ -451,8 +453,8 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
         a.rhs_t[o] = rhs - (p_c - ld(pr + S.dim)) * ld(a.cf + k);
         a.ru1[o] = ht;
     }
-    // ---- qr (ImplicitAndUpdateQR.F90:165-187), faces 1..nr-1
-    if (k >= 1) {
+    // ---- qr (ImplicitAndUpdateQR.F90:41-63), faces 1..nr-1
+    if ((mask & 2) && k >= 1) {
         T rhs = gadt * hr;
         if (use_ru) rhs += rodt * a.ru2[o];
         rhs += ld(ic + 3 * nrr + k) * ld(qr + P);
@@ -461,8 +463,8 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
         a.rhs_r[o] = rhs - (p_c - ld(pr - P)) * ld(a.cf + nrr + k);
         a.ru2[o] = hr;
     }
-    // ---- qz (ImplicitAndUpdateQZ.F90:241-312)
-    {
+    // ---- qz (ImplicitAndUpdateQZ.F90:42-113)
+    if (mask & 4) {
         T rhs = gadt * hz;
         // At the outer wall the reference has already replaced ru3(nrm) by
         // qcap(nrm) when it builds rhs(nrm) (ImplicitAndUpdateQZ.F90:86,110).
@@ -489,9 +491,10 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
     }
 }
 
+// mask: components to compute (1 qt, 2 qr, 4 qz), as implicit_cell.
 template <int MODE, typename T>
 __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
-                                              int k) {
+                                              int k, int mask = 7) {
     const int nr = d.nr;
     const Stencil S = make_stencil(d, i, j, k);
     const size_t o = S.o;
@@ -501,21 +504,21 @@ __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, 
     const T* qz = a.qz + o;
     T ht = 0, hr = 0, hz = 0;
     if (MODE != MODE_IMPLICIT) {
-        ht = explicit_qt(S, c, a, qt, qr, qz);
-        if (k >= 1) hr = explicit_qr(S, c, a, qt, qr, qz);
-        hz = explicit_qz(S, c, a, qt, qr, qz);
+        if (mask & 1) ht = explicit_qt(S, c, a, qt, qr, qz);
+        if ((mask & 2) && k >= 1) hr = explicit_qr(S, c, a, qt, qr, qz);
+        if (mask & 4) hz = explicit_qz(S, c, a, qt, qr, qz);
         if (MODE == MODE_EXPLICIT) {
-            a.h_t[o] = ht;
-            if (k >= 1) a.h_r[o] = hr;
-            a.h_z[o] = hz;
+            if (mask & 1) a.h_t[o] = ht;
+            if ((mask & 2) && k >= 1) a.h_r[o] = hr;
+            if (mask & 4) a.h_z[o] = hz;
             return;
         }
     } else {
-        ht = a.h_t[o];
-        if (k >= 1) hr = a.h_r[o];
-        hz = a.h_z[o];
+        if (mask & 1) ht = a.h_t[o];
+        if ((mask & 2) && k >= 1) hr = a.h_r[o];
+        if (mask & 4) hz = a.h_z[o];
     }
-    implicit_cell(d, c, a, S, i, j, k, ht, hr, hz);
+    implicit_cell(d, c, a, S, i, j, k, ht, hr, hz, mask);
 }
 
 // The fused momentum work of momentum_cell (MODE_FUSED) for the two cells
@@ -1045,8 +1048,8 @@ template <> struct SweepV<F2, float> {
     static __device__ __forceinline__ F2 adds(F2 a, float s) { return a + bc2(s); }
 };
 
-// SolveImpEqnUpdate_QT.F90:65-78 (comp 0), _QR.F90:136-150 (comp 1, faces
-// 1..nr-1), _QZ.F90:214-224 (comp 2) for the column `col`.  The three
+// SolveImpEqnUpdate_QT.F90:65-78 (comp 0), SolveImpEqnUpdate_QR.F90:54-65 (comp 1, faces
+// 1..nr-1), SolveImpEqnUpdate_QZ.F90:59-68 (comp 2) for the column `col`.  The three
 // components are independent, so each gets its own thread.
 template <typename T>
 __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f, int sub, long long col, int comp) {
@@ -1227,7 +1230,7 @@ __device__ __forceinline__ double2 to_d2(float2 v) { return f2d(v); }
 __device__ __forceinline__ void st2(double2* p, double x, double y) { *p = make_double2(x, y); }
 __device__ __forceinline__ void st2(float2* p, double x, double y) { *p = make_float2(d2f(x), d2f(y)); }
 
-// SolvePressureCorrection.F90:244-265: per mode (kt, kz) the real radial
+// SolvePressureCorrection.F90:127-148: per mode (kt, kz) the real radial
 // matrix (amph, acph - ak3 - ak1/rm^2, apph) applied to the complex
 // right-hand side, with the precomputed LU factors.  One thread per mode
 // (kz, kt) of the full spectrum, kz = 0..nzm-1; modes kz and nzm-kz share
@@ -1397,11 +1400,98 @@ __device__ __forceinline__ void ptri_ff(const Dims& d, const FieldsT<float>& f, 
     }
 }
 
-// The pressure tridiagonal of mode t in the path's arithmetic.
-template <typename T>
+// Mixed path in FP64 arithmetic (ptri_d64, the default of the mixed form):
+// the checkpointed structure of ptri_ff with the FP64 LU factors and FP64
+// complex values in the checkpoint slots; the FP32 spectrum is widened on
+// load and rounded once, on the final store.
+__device__ __forceinline__ double2 d64_fwd(float2 x, double l, double2 y) {
+    const double2 v = f2d(x);
+    return make_double2(v.x - l * y.x, v.y - l * y.y);
+}
+__device__ __forceinline__ double2 d64_back(double2 y, double u, double di, double2 s) {
+    return make_double2((y.x - u * s.x) * di, (y.y - u * s.y) * di);
+}
+
+__device__ __forceinline__ void ptri_d64(const Dims& d, const Coef& c, const FieldsT<float>& f, long long t) {
+    const int PH = d.PH, nzh = d.nzh, nr = d.nr;
+    const int kz = (int)(t / PH), kt = (int)(t - (long long)kz * PH);
+    const int kf = kz < nzh ? kz : d.nz - kz;
+    const size_t PS = (size_t)d.PS, FS = (size_t)nzh * PH;
+    const size_t o = (size_t)kz * PH + kt;
+    float2* x = f.spec + o;
+    double2* w = reinterpret_cast<double2*>(f.ws) + o;     // slot q at w[q * PS]
+    const double* L = f.pf_l + (size_t)kf * PH + kt;
+    const double* DI = f.pf_dinv + (size_t)kf * PH + kt;
+    const double* U = c.apph;
+    const int nb = (nr - 1) / kPtriCk;
+    // forward elimination
+    const double2 y0 = f2d(x[0]);
+    w[0] = y0;
+    double2 y = y0;
+    int k = 1;
+    for (int m = 0; m < nb; ++m, k += kPtriCk) {
+        float2 xv[kPtriCk];
+        double lv[kPtriCk];
+#pragma unroll
+        for (int b = 0; b < kPtriCk; ++b) {
+            xv[b] = x[(size_t)(k + b) * PS];
+            lv[b] = ld(L + (size_t)(k + b) * FS);
+        }
+#pragma unroll
+        for (int b = 0; b < kPtriCk; ++b) y = d64_fwd(xv[b], lv[b], y);
+        w[(size_t)(m + 1) * PS] = y;
+    }
+    for (int q = nb + 1; k < nr; ++k, ++q) {
+        y = d64_fwd(x[(size_t)k * PS], ld(L + (size_t)k * FS), y);
+        w[(size_t)q * PS] = y;
+    }
+    // back substitution: the last level, then the tail from its stored y
+    const double dl = ld(DI + (size_t)(nr - 1) * FS);
+    double2 s = make_double2(y.x * dl, y.y * dl);
+    st2(x + (size_t)(nr - 1) * PS, s.x, s.y);
+    const int ktop = kPtriCk * nb;
+    for (k = nr - 2; k > ktop; --k) {
+        s = d64_back(w[(size_t)(nb + 1 + (k - ktop - 1)) * PS], ld(U + k), ld(DI + (size_t)k * FS), s);
+        st2(x + (size_t)k * PS, s.x, s.y);
+    }
+    // full batches from the top: recompute y from the checkpoint below
+    for (int m = nb - 1; m >= 0; --m) {
+        const int kb = 1 + m * kPtriCk;
+        double2 yb[kPtriCk];
+        double2 yc = w[(size_t)m * PS];
+        float2 xv[kPtriCk - 1];
+#pragma unroll
+        for (int b = 0; b < kPtriCk - 1; ++b) xv[b] = x[(size_t)(kb + b) * PS];
+#pragma unroll
+        for (int b = 0; b < kPtriCk - 1; ++b) {
+            yc = d64_fwd(xv[b], ld(L + (size_t)(kb + b) * FS), yc);
+            yb[b] = yc;
+        }
+        yb[kPtriCk - 1] = w[(size_t)(m + 1) * PS];
+        const bool top_of_column = kb + kPtriCk - 1 == nr - 1;
+#pragma unroll
+        for (int b = kPtriCk - 1; b >= 0; --b) {
+            const int kk = kb + b;
+            if (b == kPtriCk - 1 && top_of_column) continue;
+            s = d64_back(yb[b], ld(U + kk), ld(DI + (size_t)kk * FS), s);
+            st2(x + (size_t)kk * PS, s.x, s.y);
+        }
+    }
+    if (nr > 1) {
+        s = d64_back(y0, ld(U), ld(DI), s);
+        st2(x, s.x, s.y);
+    }
+}
+
+// The pressure tridiagonal of mode t in the path's arithmetic.  FF (mixed
+// path only): 0 FP64, 1 float-float, -1 as f.ptri_ff says (kernels that
+// know the mode at launch compile one variant each: both in one kernel take
+// more registers than either).
+template <typename T, int FF = -1>
 __device__ __forceinline__ void ptri_solve(const Dims& d, const Coef& c, const FieldsT<T>& f, long long t) {
     if constexpr (std::is_same<T, double>::value) ptri_one(d, c, f, reinterpret_cast<double2*>(f.spec), t);
-    else ptri_ff(d, f, t);
+    else if (FF == 1 || (FF < 0 && f.ptri_ff)) ptri_ff(d, f, t);
+    else ptri_d64(d, c, f, t);
 }
 
 // Inverse real FFT along theta: spec rows -> phi rows.
@@ -1508,7 +1598,7 @@ __device__ __forceinline__ void correct_pair_f(const Dims& d, const FieldsT<floa
     const float2 PJp = ld(reinterpret_cast<const float2*>(phi + (size_t)k * P + (size_t)jp * nt + i));
     const float2 PKm = ld(reinterpret_cast<const float2*>(phi + (size_t)(k > 0 ? k - 1 : 0) * P + rowoff + i));
     const float2 PKp = ld(reinterpret_cast<const float2*>(phi + (size_t)(k < nr - 1 ? k + 1 : nr - 1) * P + rowoff + i));
-    // CorrectVelocity.F90:318-337
+    // CorrectVelocity.F90:28-47
     const float* cf = f.corr + (size_t)sub * 3 * nrr;
     const float cft = ld(cf + k), cfz = ld(cf + 2 * nrr);
     float2* qt = reinterpret_cast<float2*>(f.qt + o);

@@ -251,11 +251,13 @@ const char* tc_last_error(const tc_handle* h) {
 
 int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     if (!cfg || !out) return fail(nullptr, 2000, "null argument");
-    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED) return fail(nullptr, 2007, "unknown precision");
+    if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED && precision != TC_PREC_MIXED_FF)
+        return fail(nullptr, 2007, "unknown precision");
     *out = nullptr;
     tc_handle* h = new tc_handle();
     h->bou = *cfg;
-    h->mixed = precision == TC_PREC_MIXED;
+    h->mixed = precision != TC_PREC_FP64;
+    h->ptri_ff = precision == TC_PREC_MIXED_FF;
     std::string e = build_grid(*cfg, h->g);
     if (!e.empty()) { int r = fail(nullptr, 2003, e); delete h; return r; }
     int dev = 0;
@@ -383,7 +385,8 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "state upload"); tc_destroy(h); return r; }
 
     launch_pressure_factors(h->stream, d, h->c, pl, pdv);
-    if (h->mixed) {
+    h->ff.ptri_ff = h->ptri_ff;
+    if (h->ptri_ff) {
         float2* pu = nullptr;
         ce = dalloc(h, &pu, (size_t)nr);
         if (ce != cudaSuccess) { int r = cuda_fail(nullptr, ce, "device allocation"); tc_destroy(h); return r; }
@@ -406,7 +409,9 @@ int tc_get_bou(const tc_handle* h, tc_bou* out) {
     return 0;
 }
 
-int tc_precision(const tc_handle* h) { return h ? (h->mixed ? TC_PREC_MIXED : TC_PREC_FP64) : -1; }
+int tc_precision(const tc_handle* h) {
+    return h ? (h->ptri_ff ? TC_PREC_MIXED_FF : h->mixed ? TC_PREC_MIXED : TC_PREC_FP64) : -1;
+}
 
 void tc_destroy(tc_handle* h) {
     if (!h) return;
@@ -656,9 +661,12 @@ static int ensure_h(tc_handle* h) {
     return 0;
 }
 
+// comp: -1 all three components, else 0 (qt), 1 (qr) or 2 (qz) alone.
 template <typename T>
-static int routine(tc_handle* h, int which) {
+static int routine(tc_handle* h, int which, int comp) {
     cudaStream_t s = h->stream;
+    const int mask = comp < 0 ? 7 : (1 << comp);
+    const int comp0 = comp < 0 ? 0 : comp, ncomp = comp < 0 ? 3 : 1;
     if (which <= 1) {
         if (int r = ensure_h<T>(h)) return r;
     }
@@ -668,17 +676,17 @@ static int routine(tc_handle* h, int which) {
     const int sub = h->sub;
     switch (which) {
         case 0:  // ExplicitTermsQT/QR/QZ
-            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_EXPLICIT, h->d, cv, h->k, f, sub); });
+            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_EXPLICIT, h->d, cv, h->k, f, sub, mask); });
             break;
         case 1:  // ImplicitAndUpdateQ* with SolveImpEqnUpdate_Q*
-            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_IMPLICIT, h->d, cv, h->k, f, sub); });
-            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub); });
+            L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_IMPLICIT, h->d, cv, h->k, f, sub, mask); });
+            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub, comp0, ncomp); });
             break;
         case 2:
             L(h, K_MOMENTUM, 1, [&] { launch_momentum(s, MODE_FUSED, h->d, cv, h->k, f, sub); });
             break;
         case 3:
-            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub); });
+            L(h, K_RADIAL, 1, [&] { launch_radial_solve(s, h->d, f, sub, comp0, ncomp); });
             break;
         case 4:
             L(h, K_DIVFFT, 1, [&] { launch_divergence(s, h->d, cv, h->k, f, sub); });
@@ -700,15 +708,24 @@ static int routine(tc_handle* h, int which) {
     return 0;
 }
 
-static int run_routine(tc_handle* h, int which) {
+static int run_routine(tc_handle* h, int which, int comp = -1) {
     if (int r = check(h)) return r;
-    return h->mixed ? routine<float>(h, which) : routine<double>(h, which);
+    return h->mixed ? routine<float>(h, which, comp) : routine<double>(h, which, comp);
 }
 
 int tc_explicit_terms(tc_handle* h) { return run_routine(h, 0); }
 int tc_implicit_and_update(tc_handle* h) { return run_routine(h, 1); }
 int tc_explicit_and_rhs(tc_handle* h) { return run_routine(h, 2); }
 int tc_solve_imp_eqn_update(tc_handle* h) { return run_routine(h, 3); }
+int tc_explicit_terms_qt(tc_handle* h) { return run_routine(h, 0, 0); }
+int tc_explicit_terms_qr(tc_handle* h) { return run_routine(h, 0, 1); }
+int tc_explicit_terms_qz(tc_handle* h) { return run_routine(h, 0, 2); }
+int tc_implicit_and_update_qt(tc_handle* h) { return run_routine(h, 1, 0); }
+int tc_implicit_and_update_qr(tc_handle* h) { return run_routine(h, 1, 1); }
+int tc_implicit_and_update_qz(tc_handle* h) { return run_routine(h, 1, 2); }
+int tc_solve_imp_eqn_update_qt(tc_handle* h) { return run_routine(h, 3, 0); }
+int tc_solve_imp_eqn_update_qr(tc_handle* h) { return run_routine(h, 3, 1); }
+int tc_solve_imp_eqn_update_qz(tc_handle* h) { return run_routine(h, 3, 2); }
 int tc_calc_local_divergence(tc_handle* h) { return run_routine(h, 4); }
 int tc_solve_pressure_correction(tc_handle* h) { return run_routine(h, 5); }
 int tc_correct_velocity(tc_handle* h) { return run_routine(h, 6); }
@@ -743,7 +760,9 @@ int tc_calc_max_cfl(tc_handle* h, double* cflm) {
 
 int tc_check_divergence(tc_handle* h, double* qmax) {
     if (int r = reduce(h, 1)) return r;
-    if (qmax) *qmax = h->st_host->dmax;
+    const double v = h->st_host->dmax;
+    if (qmax) *qmax = v;
+    if (v != v) return fail(h, 169, "tc_check_divergence: the velocity field holds a NaN");
     return 0;
 }
 

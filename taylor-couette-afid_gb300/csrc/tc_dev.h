@@ -96,7 +96,7 @@ struct Consts {
     double dxz_al[3], dxt_al[3]; // dxz*al, dxt*al per substep
     double fft_norm;             // 0.5/(nthm*nzm): FFT normalisation and real-unpacking 1/2
     int nsst, idtv, ntst;
-    int patterned;          // patterned slip active (SlipBCs.F90:520)
+    int patterned;          // patterned slip active (SlipBCs.F90:55-56)
     int minstrt, minstrz, multmin;
 };
 
@@ -133,9 +133,10 @@ __host__ __device__ inline int ptri_slots(int nr) {
 
 // Per-step coefficients of one step (factors kernel), per substep s:
 // [ (s*3 + c)*(nr+1) + k ]  dt al(s) times the pressure-gradient metric of
-//                            component c at level k (CorrectVelocity.F90:
-//                            325-330; the momentum right-hand sides use the
-//                            same products for the pressure of the step),
+//                            component c at level k
+//                            (CorrectVelocity.F90:35-40; the momentum
+//                            right-hand sides use the same products for the
+//                            pressure of the step),
 // [ 9*(nr+1) + s*3 + 0..2 ] gam(s) dt, rom(s) dt, alre(s) dt;
 // and for the pressure of the step (CorrectPressure.F90:40-44 regrouped as
 // pr + phi + pe phi + pt (phi_ip + phi_im) + pz (phi_jp + phi_jm)

@@ -24,7 +24,7 @@ struct Grid {
     // free-slip variants of the wall rows, index 0 = inner, 1 = outer
     double ap1j_fs[2] = {0, 0}, ac1j_fs[2] = {0, 0}, am1j_fs[2] = {0, 0};
     double ap3j_fs[2] = {0, 0}, ac3j_fs[2] = {0, 0}, am3j_fs[2] = {0, 0};
-    // pressure operator (InitPressureSolver.F90:66-76), length nr
+    // pressure operator (InitPressureSolver.F90:22-32), length nr
     std::vector<double> apph, amph, acph;
     // modified wavenumbers, lengths nthm and nzm
     std::vector<double> ak1, ak3;

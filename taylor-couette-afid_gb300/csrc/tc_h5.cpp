@@ -642,17 +642,17 @@ void interp_field(const std::vector<double>& old, int ntho, int nzo, int nro, in
     for (int i = 1; i <= nthom; ++i)
         for (int j = 1; j <= nzom; ++j)
             for (int k = 1; k <= nro; ++k) A(k, j, i) = old[(size_t)(k - 1) + (size_t)nro * ((size_t)(j - 1) + (size_t)nzom * (i - 1))];
-    for (int i = 1; i <= nthom; ++i)                     // interp.F90:99-104
+    for (int i = 1; i <= nthom; ++i)                     // interp.F90:109-114
         for (int j = 1; j <= nzom; ++j) {
             A(0, j, i) = 2.0 * A(1, j, i) - A(2, j, i);
             A(nro + 1, j, i) = 2.0 * A(nro, j, i) - A(nro - 1, j, i);
         }
-    for (int j = 1; j <= nzom; ++j)                      // :105-110
+    for (int j = 1; j <= nzom; ++j)                      // interp.F90:116-121
         for (int k = 1; k <= nro; ++k) {
             A(k, j, 0) = 2.0 * A(k, j, 1) - A(k, j, 2);
             A(k, j, nthom + 1) = 2.0 * A(k, j, nthom) - A(k, j, nthom - 1);
         }
-    for (int i = 1; i <= nthom; ++i)                     // :111-116
+    for (int i = 1; i <= nthom; ++i)                     // interp.F90:123-128
         for (int k = 1; k <= nro; ++k) {
             A(k, 0, i) = 2.0 * A(k, 1, i) - A(k, 2, i);
             A(k, nzom + 1, i) = 2.0 * A(k, nzom, i) - A(k, nzom - 1, i);

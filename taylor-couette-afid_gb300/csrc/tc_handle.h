@@ -11,6 +11,7 @@
 struct tc_handle {
     tc_bou bou;
     int mixed = 0;          // 0: plain FP64, 1: mixed FP32/FP64
+    int ptri_ff = 0;        // mixed: pressure tridiagonals in float-float instead of FP64
     tcgb::Grid g;
     tcgb::Dims d;
     tcgb::Consts k;

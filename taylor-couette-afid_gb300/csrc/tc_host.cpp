@@ -102,7 +102,7 @@ std::string validate(const tc_bou& b) {
     int ntott = b.minstrt * b.multmin, ntotz = b.minstrz * b.multmin;
     if (ntott + ntotz != 0 && (ntott == 0 || ntotz == 0))
         return "patterned slip needs MINSTRT*MULTMIN and MINSTRZ*MULTMIN both non-zero "
-               "(SlipBCs.F90:523-524 divides by each)";
+               "(SlipBCs.F90:58-59 divides by each)";
     long long cells = (long long)b.nthm * b.nzm * b.nrm;
     if (cells > (1LL << 31) - 1) return "more than 2^31-1 cells";
     return "";
@@ -134,23 +134,23 @@ std::string build_grid(const tc_bou& b, Grid& g) {
     auto R = [](std::vector<double>& a, int k) -> double& { return a[k - 1]; };
 
     g.pi = 2.0 * std::asin(1.0);                                  // CreateGrid.F90:24
-    g.dxt = ((double)nthm * b.lamb) / (2.0 * g.pi);               // :28-34
+    g.dxt = ((double)nthm * b.lamb) / (2.0 * g.pi);               // CreateGrid.F90:28-34
     g.dxz = (double)nzm / b.alx3;
     g.dxr = (double)nrm / 1.0;
     g.dxtq = g.dxt * g.dxt; g.dxzq = g.dxz * g.dxz; g.dxrq = g.dxr * g.dxr;
     const double dxr = g.dxr, dxrq = g.dxrq;
 
     auto& rc = g.rc;
-    if (b.istr == 0) {                                            // :85-90
+    if (b.istr == 0) {                                            // CreateGrid.F90:85-90
         for (int k = 1; k <= nr; ++k) R(rc, k) = (b.rext - b.rint) * ((double)(k - 1) / (double)nrm) + b.rint;
-    } else if (b.istr == 4) {                                     // :99-105
+    } else if (b.istr == 4) {                                     // CreateGrid.F90:99-105
         double tstr = std::tanh(b.str);
         R(rc, 1) = b.rint;
         for (int k = 2; k <= nr; ++k) {
             double z2dp = (double)(2 * k - nr - 1) / (double)nrm;
             R(rc, k) = (1.0 + std::tanh(b.str * z2dp) / tstr) * 0.5 * (b.rext - b.rint) + b.rint;
         }
-    } else {                                                      // :109-128
+    } else {                                                      // CreateGrid.F90:109-128
         int nclip = (int)b.str, nrmo = nr + 2 * nclip;
         std::vector<double> etaz(nr + 1);
         for (int k = 1; k <= nr; ++k)
@@ -161,14 +161,14 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         for (int k = 2; k <= nrm; ++k) R(rc, k) = (b.rext - b.rint) * (1.0 - etaz[k]) * 0.5 + b.rint;
         R(rc, nr) = b.rext;
     }
-    for (int k = 1; k <= nrm; ++k) {                              // :136-139
+    for (int k = 1; k <= nrm; ++k) {                              // CreateGrid.F90:136-139
         R(g.rm, k) = (R(rc, k) + R(rc, k + 1)) * 0.5;
         R(g.g2rm, k) = (R(rc, k + 1) - R(rc, k)) * dxr;
     }
-    R(g.g2rc, 1) = (R(rc, 2) - R(rc, 1)) * dxr;                   // :141-151
+    R(g.g2rc, 1) = (R(rc, 2) - R(rc, 1)) * dxr;                   // CreateGrid.F90:141-151
     for (int k = 2; k <= nrm; ++k) R(g.g2rc, k) = (R(rc, k + 1) - R(rc, k - 1)) * dxr * 0.5;
     R(g.g2rc, nr) = (R(rc, nr) - R(rc, nrm)) * dxr;
-    for (int k = 1; k <= nrm; ++k) {                              // :156-166
+    for (int k = 1; k <= nrm; ++k) {                              // CreateGrid.F90:156-166
         R(g.udx1vis1, k) = 2.0 * g.dxt / (sq(R(g.rm, k)) * b.ren);
         R(g.udx2rm, k) = dxr / (R(g.g2rm, k) * R(g.rm, k));
         R(g.udx2m, k) = dxr / R(g.g2rm, k);
@@ -178,8 +178,8 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         R(g.udx1qm, k) = g.dxtq / sq(R(g.rm, k));
         R(g.pvol, k) = sq(R(rc, k + 1)) - sq(R(rc, k));
     }
-    R(g.udx2c, nr) = dxr / R(g.g2rc, nr);                         // :167
-    {   // :141-153,160,173: g2rmm and g2rcc (statistics only).  rm(nr) is never
+    R(g.udx2c, nr) = dxr / R(g.g2rc, nr);                         // CreateGrid.F90:167
+    {   // CreateGrid.F90:141-153,160,173: g2rmm and g2rcc (statistics only).  rm(nr) is never
         // set by CreateGrid and stays 0, so g2rmm(nrm) and udx2mm(nrm) use it.
         std::vector<double> g2rmm(nr, 0.0), g2rcc(nr, 0.0);
         R(g2rmm, 1) = (R(g.rm, 2) - R(g.rm, 1)) * dxr;
@@ -193,12 +193,12 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         for (int k = 1; k <= nrm; ++k) R(g.udx2mm, k) = dxr / R(g2rmm, k);
         for (int k = 1; k <= nr; ++k) R(g.udx2cc, k) = dxr / R(g2rcc, k);
     }
-    for (int k = 1; k <= nr; ++k) {                               // :169-174
+    for (int k = 1; k <= nr; ++k) {                               // CreateGrid.F90:169-174
         R(g.udx1vis2, k) = g.dxt / (R(rc, k) * b.ren);
         R(g.usrc, k) = 1.0 / R(rc, k);
     }
     auto& rm = g.rm; auto& g2rm = g.g2rm; auto& g2rc = g.g2rc;
-    // q1 (:194-238)
+    // q1 (CreateGrid.F90:191-238)
     for (int kc = 2; kc <= nrm - 1; ++kc) {
         double a22 = dxrq / R(g2rm, kc) / R(rm, kc);
         double a22p = +a22 * R(rc, kc + 1) / R(g2rc, kc + 1);
@@ -231,7 +231,7 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         g.am1j_fs[0] = 0.0;
         g.ap1j_fs[1] = g.ac1j_fs[1] = g.am1j_fs[1] = 0.0;
     }
-    // q2 (:244-276)
+    // q2 (CreateGrid.F90:241-276)
     R(g.ac2j, 1) = 1.0; R(g.ac2j, nr) = 1.0;
     for (int kc = 2; kc <= nrm; ++kc) {
         int km = kc - 1, kp = kc + 1;
@@ -247,7 +247,7 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         R(g.ap2je, kc) = e22p * ugmm; R(g.am2je, kc) = e22m * ugmm;
         R(g.ac2je, kc) = -e22 * ugmm - 1.0 / sq(R(rc, kc));
     }
-    // q3 (:281-322)
+    // q3 (CreateGrid.F90:279-322)
     for (int kc = 2; kc <= nrm - 1; ++kc) {
         double a22 = dxrq / R(g2rm, kc) / R(rm, kc);
         double a22p = +a22 * R(rc, kc + 1) / R(g2rc, kc + 1);
@@ -269,7 +269,7 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         R(g.am3j, kc) = a22m; R(g.ap3j, kc) = 0.0; R(g.ac3j, kc) = -(a22m + 2.0 * a22p);
         g.am3j_fs[1] = a22m; g.ap3j_fs[1] = 0.0; g.ac3j_fs[1] = -(a22m);
     }
-    // pressure operator (InitPressureSolver.F90:66-76); kmc(1) = kpc(nrm) = 0
+    // pressure operator (InitPressureSolver.F90:22-32); kmc(1) = kpc(nrm) = 0
     for (int kc = 1; kc <= nrm; ++kc) {
         int kmc = (kc == 1) ? 0 : 1, kpc = (kc == nrm) ? 0 : 1;
         int kp = kc + kpc;
@@ -281,7 +281,7 @@ std::string build_grid(const tc_bou& b, Grid& g) {
         R(g.apph, kc) = a22icp * ugmmm;
         R(g.acph, kc) = ac2 * ugmmm;
     }
-    // modified wavenumbers (:85-110), with the negative-frequency form above
+    // modified wavenumbers (InitPressureSolver.F90:41-66), with the negative-frequency form above
     // nzm/2+1 and nthm/2+1
     g.ak3.assign(nzm, 0.0);
     for (int j = 1; j <= nzm; ++j) {

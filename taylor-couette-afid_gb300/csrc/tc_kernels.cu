@@ -70,7 +70,7 @@ __global__ void finish_step_kernel(Consts k, StepState* st) {
     int err = st->errorcode;
     if (st->output) {
         if (st->vmax[0] > k.limitVel && st->vmax[1] > k.limitVel) err = 266;
-        if (fabs(st->dmax) > k.resid) err = 169;
+        if (!(fabs(st->dmax) <= k.resid)) err = 169;   // a NaN divergence fails too
     }
     if (st->time > k.tmax) err = 333;
     if (st->ntime == k.ntst) err = 555;
@@ -79,7 +79,7 @@ __global__ void finish_step_kernel(Consts k, StepState* st) {
     if (err != 0) st->halt = 1;
 }
 
-// SlipBCs.F90:495-555 for the rotated slip pattern (only launched when
+// SlipBCs.F90:55-88 for the rotated slip pattern (only launched when
 // MINSTRT*MULTMIN and MINSTRZ*MULTMIN are both non-zero).  One thread per
 // (z, theta) column decides whether any band covers it.
 __global__ void slip_kernel(Dims d, Consts k, StepState* st, signed char* icyl) {
@@ -117,14 +117,15 @@ __global__ void factors_kernel(Dims d, Coef c, Consts k, StepState* st, MomFacto
 // Momentum: explicit terms and implicit right-hand sides
 // --------------------------------------------------------------------------
 
+// mask: components (1 qt, 2 qr, 4 qz) of the per-routine entry points.
 template <int MODE, typename T>
-__global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomArgs<T> a) {
+__global__ void __launch_bounds__(128) momentum_kernel(Dims d, CoefT<T> c, MomArgs<T> a, int mask) {
     if (a.st->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= d.nt || j >= d.nz) return;
-    momentum_cell<MODE>(d, c, a, i, j, k);
+    momentum_cell<MODE>(d, c, a, i, j, k, mask);
 }
 
 // FP64 fused momentum, two theta-neighbouring cells per thread
@@ -174,19 +175,20 @@ template <typename T> struct RadialBlocks { static constexpr int value = 8; };
 constexpr int kRadialPairBlocks = 6;
 
 template <typename T>
-__global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kernel(Dims d, FieldsT<T> f, int sub) {
+__global__ void __launch_bounds__(128, RadialBlocks<T>::value) radial_solve_kernel(Dims d, FieldsT<T> f, int sub,
+                                                                                     int comp0) {
     if (f.st->halt) return;
     const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= d.P) return;
-    radial_column(d, f, sub, col, blockIdx.y);
+    radial_column(d, f, sub, col, comp0 + (int)blockIdx.y);
 }
 
 // FP32 path: two neighbouring columns a thread (radial_column_pair).
-__global__ void __launch_bounds__(128, kRadialPairBlocks) radial_pair_kernel(Dims d, FieldsT<float> f, int sub) {
+__global__ void __launch_bounds__(128, kRadialPairBlocks) radial_pair_kernel(Dims d, FieldsT<float> f, int sub, int comp0) {
     if (f.st->halt) return;
     const long long col = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (col >= d.P) return;
-    radial_column_pair(d, f, sub, col, blockIdx.y);
+    radial_column_pair(d, f, sub, col, comp0 + (int)blockIdx.y);
 }
 
 // --------------------------------------------------------------------------
@@ -218,12 +220,17 @@ __global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<
 // grid the float-float solve of the mixed path takes 0.133 ms a launch
 // against 0.140 ms with 8 blocks (64 registers, a few spilled), 0.156 ms with
 // 10 and 0.183 ms with 6; the FP64 solve 0.230 ms with 7 or 8.
-template <typename T>
-__global__ void __launch_bounds__(128, 7) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {
+// The FP64 solve of the mixed path keeps a batch of FP64 complex values
+// (32 registers) and is compiled for 5 blocks (6 spill).
+template <typename T, int FF> struct PtriBlocks { static constexpr int value = 7; };
+template <> struct PtriBlocks<float, 0> { static constexpr int value = 5; };
+
+template <typename T, int FF>
+__global__ void __launch_bounds__(128, PtriBlocks<T, FF>::value) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {
     if (f.st->halt) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)d.nz * d.PH) return;
-    ptri_solve(d, c, f, t);
+    ptri_solve<T, FF>(d, c, f, t);
 }
 
 // LU factors of every pressure mode matrix (time independent): thread per
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(kThThreads) theta_inv_kernel(Dims d, FieldsT<T
 }
 
 // --------------------------------------------------------------------------
-// Projection: CorrectVelocity.F90:318-337 (element type T) and
+// Projection: CorrectVelocity.F90:28-47 (element type T) and
 // CorrectPressure.F90:40-44 (FP64: pr += phi - beta lap(phi))
 // --------------------------------------------------------------------------
 
@@ -310,13 +317,20 @@ __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
+// Maximum that keeps a NaN (fmax drops it): the divergence check must see a
+// field that has blown up.
+__device__ __forceinline__ double nan_max(double a, double b) { return (b != b || b > a) ? b : a; }
+__device__ __forceinline__ double warp_nan_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-template <bool MAX>
+template <bool MAX, bool NANMAX = false>
 __device__ double block_reduce(double v, double* sh) {
-    v = MAX ? warp_max(v) : warp_sum(v);
+    v = MAX ? (NANMAX ? warp_nan_max(v) : warp_max(v)) : warp_sum(v);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
     if (l == 0) sh[w] = v;
@@ -324,15 +338,16 @@ __device__ double block_reduce(double v, double* sh) {
     const int nw = blockDim.x >> 5;
     if (w == 0) {
         v = (l < nw) ? sh[l] : (MAX ? -1.0e300 : 0.0);
-        v = MAX ? warp_max(v) : warp_sum(v);
+        v = MAX ? (NANMAX ? warp_nan_max(v) : warp_max(v)) : warp_sum(v);
     }
     return v;
 }
 
-// CalcMaxCFL.F90:30-43 (WHICH = 0) and CheckDivergence.F90:77-89 (WHICH = 1):
+// CalcMaxCFL.F90:30-43 (WHICH = 0) and CheckDivergence.F90:28-40 (WHICH = 1):
 // blockIdx.y strides over radial levels, the x blocks over the cells of a
 // level (32-bit index arithmetic).  The CFL maximum is kept in the element
-// type (exact); the divergence in FP64.
+// type (exact); the divergence in FP64, and a NaN anywhere makes it NaN (so
+// that the check raises 169 on a field that has blown up).
 template <int WHICH, typename T>
 __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, CoefT<T> cv, double dxt, double dxz,
                                                                FieldsT<T> f, int only_on_output) {
@@ -355,12 +370,12 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_kernel(Dims d, Coef c, Co
                 const double z0 = ld(f.qz + o), z1 = ld(f.qz + (size_t)k * P + (size_t)jp * nt + i);
                 const double v = fabs(((t1 - t0) * dxt + (r1 - r0) * ld(c.udx2m + k)) * ld(c.usrm + k) +
                                       (z1 - z0) * dxz);
-                best = fmax(best, (A)v);
+                best = nan_max(best, v);
             }
         }
     }
     double b = to_double(best);
-    b = block_reduce<true>(b, sh);
+    b = block_reduce<true, WHICH == 1>(b, sh);
     if (threadIdx.x == 0) f.red[blockIdx.y * gridDim.x + blockIdx.x] = b;
 }
 
@@ -379,8 +394,13 @@ __global__ void __launch_bounds__(kRedThreads) cellmax_finish(const double* red,
     __shared__ double sh[32];
     if (only_on_output && (st->halt || !st->output)) return;
     double best = which == 0 ? 0.00000001 : 0.0;
-    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = fmax(best, red[t]);
-    best = block_reduce<true>(best, sh);
+    if (which == 0) {
+        for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = fmax(best, red[t]);
+        best = block_reduce<true>(best, sh);
+    } else {
+        for (int t = threadIdx.x; t < nblocks; t += blockDim.x) best = nan_max(best, red[t]);
+        best = block_reduce<true, true>(best, sh);
+    }
     if (threadIdx.x == 0) {
         if (which == 0) st->instcfl = best;
         else st->dmax = best;
@@ -440,7 +460,7 @@ __global__ void __launch_bounds__(kRedThreads) vstats_finish(const double* red, 
     }
 }
 
-// CalcTorque.F90:131-150: wall sums over (z, theta) columns.
+// CalcTorque.F90:36-48: wall sums over (z, theta) columns.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) torque_kernel(Dims d, Coef c, double virotint, double virotext,
                                                               FieldsT<T> f) {
@@ -628,7 +648,7 @@ static dim3 cell_grid(const Dims& d, dim3& blk) {
 
 template <typename T>
 void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c, const Consts& k,
-                     const FieldsT<T>& f, int sub) {
+                     const FieldsT<T>& f, int sub, int mask) {
     MomArgs<T> a = make_mom_args(k, f, sub);
     dim3 blk;
     dim3 g = cell_grid(d, blk);
@@ -647,17 +667,17 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
             else momentum_pair_kernel<T, 0><<<pg, pblk, 0, s>>>(d, c, a);
         }
     }
-    else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
-    else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a);
+    else if (mode == MODE_EXPLICIT) momentum_kernel<MODE_EXPLICIT, T><<<g, blk, 0, s>>>(d, c, a, mask);
+    else momentum_kernel<MODE_IMPLICIT, T><<<g, blk, 0, s>>>(d, c, a, mask);
     TC_LAUNCH_CHECK();
 }
 
 template <typename T>
-void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub) {
+void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub, int comp0, int ncomp) {
     if constexpr (std::is_same<T, float>::value)
-        radial_pair_kernel<<<dim3((unsigned)((d.P / 2 + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
+        radial_pair_kernel<<<dim3((unsigned)((d.P / 2 + 127) / 128), ncomp), 128, 0, s>>>(d, f, sub, comp0);
     else
-        radial_solve_kernel<T><<<dim3((unsigned)((d.P + 127) / 128), 3), 128, 0, s>>>(d, f, sub);
+        radial_solve_kernel<T><<<dim3((unsigned)((d.P + 127) / 128), ncomp), 128, 0, s>>>(d, f, sub, comp0);
     TC_LAUNCH_CHECK();
 }
 
@@ -708,7 +728,9 @@ void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const Plans
 template <typename T>
 void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const FieldsT<T>& f) {
     long long n = (long long)d.nz * d.PH;      // one thread per mode
-    ptri_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, c, f);
+    const unsigned g = (unsigned)((n + 127) / 128);
+    if (std::is_same<T, float>::value && f.ptri_ff) ptri_kernel<T, 1><<<g, 128, 0, s>>>(d, c, f);
+    else ptri_kernel<T, 0><<<g, 128, 0, s>>>(d, c, f);
     TC_LAUNCH_CHECK();
 }
 
@@ -846,8 +868,8 @@ void launch_to_host(cudaStream_t s, const Dims& d, const T* src, double* stage, 
     template void launch_slip<T>(cudaStream_t, const Dims&, const Consts&, const FieldsT<T>&);                 \
     template void launch_factors<T>(cudaStream_t, const Dims&, const Coef&, const Consts&, const FieldsT<T>&); \
     template void launch_momentum<T>(cudaStream_t, int, const Dims&, const CoefT<T>&, const Consts&,           \
-                                     const FieldsT<T>&, int);                                                 \
-    template void launch_radial_solve<T>(cudaStream_t, const Dims&, const FieldsT<T>&, int);                  \
+                                     const FieldsT<T>&, int, int);                                            \
+    template void launch_radial_solve<T>(cudaStream_t, const Dims&, const FieldsT<T>&, int, int, int);        \
     template void launch_div_fft<T>(cudaStream_t, const Dims&, const CoefT<T>&, const Consts&,                \
                                     const FieldsT<T>&, const PlansT<T>&, int, bool);                          \
     template void launch_zfft<T>(cudaStream_t, const Dims&, const FieldsT<T>&, const PlansT<T>&, bool);       \

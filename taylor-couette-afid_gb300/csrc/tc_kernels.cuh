@@ -30,11 +30,14 @@ struct FieldsT {
     double* corrd;
     double* scal;                     // per substep: [s] usdt*fft_norm, [3+s] usdt
     double* red;                      // reduction partials
-    // mixed path (T = float): the pressure factors and super-diagonal as
+    // mixed path (T = float): the checkpoint slots of the pressure solve's
+    // forward sweep (16 bytes each: an FP64 complex value, or a float-float
+    // one); with ptri_ff set the pressure factors and the super-diagonal are
     // float-float pairs (pl_ff, pdi_ff alias pf_l, pf_dinv, converted in
-    // place), and the checkpoint slots of the pressure solve's forward sweep
+    // place) and the solve runs in float-float, else in FP64 on pf_l, pf_dinv
     const float2 *pl_ff, *pdi_ff, *pu_ff;
     float4* ws;
+    int ptri_ff;
 };
 
 template <typename T>
@@ -61,10 +64,13 @@ template <typename T>
 void launch_factors(cudaStream_t s, const Dims& d, const Coef& c, const Consts& k, const FieldsT<T>& f);
 
 // Substep kernels.
+// mask (MODE_EXPLICIT, MODE_IMPLICIT): components 1 qt, 2 qr, 4 qz.
 template <typename T>
 void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c, const Consts& k,
-                     const FieldsT<T>& f, int sub);
-template <typename T> void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub);
+                     const FieldsT<T>& f, int sub, int mask = 7);
+// Components comp0 .. comp0 + ncomp - 1 (0 qt, 1 qr, 2 qz).
+template <typename T>
+void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int sub, int comp0 = 0, int ncomp = 3);
 template <typename T>
 void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                     const PlansT<T>& p, int sub, bool from_phi);

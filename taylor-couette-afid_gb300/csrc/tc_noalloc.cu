@@ -1,4 +1,4 @@
-// tc_noalloc.cu -- tc_check_divergence_noalloc: CheckDivergence.F90:60-95 on
+// tc_noalloc.cu -- tc_check_divergence_noalloc: CheckDivergence.F90:28-43 on
 // velocity arrays the caller keeps on the device, in the reference layout,
 // without allocating anything.
 //
@@ -14,6 +14,7 @@
 // reads them.  Its address is looked up once per device with
 // cudaGetSymbolAddress, by the first call made with that device current.
 // All calls on one device share the array, so calls must not overlap.
+// A NaN anywhere in the fields makes the result NaN and the status 169.
 
 #include <cmath>
 #include <mutex>
@@ -40,8 +41,12 @@ static __device__ __align__(256) double g_noalloc_scratch[kNaWords];
 std::mutex g_na_mutex;
 double* g_na_addr[kNaMaxDevices] = {nullptr};
 
+// A maximum that keeps a NaN (fmax would drop it), so that a field that has
+// blown up reports NaN instead of the largest finite divergence.
+__device__ __forceinline__ double na_max(double a, double b) { return (b != b || b > a) ? b : a; }
+
 __device__ __forceinline__ double na_warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = na_max(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
 
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(kNaThreads) na_divmax_kernel(const double* __r
         const double r0 = __ldg(qr + o), r1 = __ldg(qr + o + 1);
         const double z0 = __ldg(qz + o), z1 = __ldg(qz + o + sj);
         const double v = fabs(((t1 - t0) * dxt + (r1 - r0) * udx2m[k]) * usrm[k] + (z1 - z0) * dxz);
-        best = fmax(best, v);
+        best = na_max(best, v);
     }
     best = na_block_max(best);
     if (threadIdx.x == 0) scratch[2 * kNaMaxR + blockIdx.x] = best;
@@ -89,7 +94,7 @@ __global__ void __launch_bounds__(kNaThreads) na_divmax_kernel(const double* __r
 
 __global__ void __launch_bounds__(kNaThreads) na_finish_kernel(double* scratch) {
     double best = 0.0;
-    for (int t = threadIdx.x; t < kNaBlocks; t += blockDim.x) best = fmax(best, scratch[2 * kNaMaxR + t]);
+    for (int t = threadIdx.x; t < kNaBlocks; t += blockDim.x) best = na_max(best, scratch[2 * kNaMaxR + t]);
     best = na_block_max(best);
     if (threadIdx.x == 0) scratch[2 * kNaMaxR + kNaBlocks] = best;
 }
@@ -132,6 +137,13 @@ int tc_check_divergence_noalloc(const double* qt, const double* qr, const double
         scratch = g_na_addr[dev];
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The call copies from pageable host memory and synchronises the stream,
+    // neither of which a stream capture allows: refuse before enqueueing.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    c = cudaStreamIsCapturing(s, &cap);
+    if (c != cudaSuccess) return na_cuda(c, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone)
+        return na_fail(2018, "tc_check_divergence_noalloc: the stream is being captured; call it outside capture");
     const size_t cb = sizeof(double) * (size_t)nrm;
     c = cudaMemcpyAsync(scratch, udx2m, cb, cudaMemcpyHostToDevice, s);
     if (c == cudaSuccess) c = cudaMemcpyAsync(scratch + kNaMaxR, usrm, cb, cudaMemcpyHostToDevice, s);
@@ -145,5 +157,6 @@ int tc_check_divergence_noalloc(const double* qt, const double* qr, const double
     if (c == cudaSuccess) c = cudaStreamSynchronize(s);
     if (c != cudaSuccess) return na_cuda(c, "result read");
     *qmax = v;
+    if (v != v) return na_fail(169, "tc_check_divergence_noalloc: the velocity field holds a NaN");
     return 0;
 }

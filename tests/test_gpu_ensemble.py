@@ -48,7 +48,7 @@ def run_members(precision, bous, seeds, nsteps, dts, tune=None):
     return out, stat
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-ff"])
 def test_alone_and_in_the_mix_are_identical(gpu_lib, precision):
     dt = 2e-3
     alone, st_alone = run_members(precision, [PROBE], [7], 6, [dt])
@@ -65,7 +65,7 @@ def test_alone_and_in_the_mix_are_identical(gpu_lib, precision):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-ff"])
 def test_members_match_the_single_run_path(gpu_lib, precision):
     bous = [PROBE] + MIX
     seeds = [7, 1, 2, 3, 4, 5]

@@ -12,9 +12,9 @@ import tc_gb300.initial as ini
 pytestmark = pytest.mark.gpu
 
 
-def pair(oracle, bou, seed=5):
+def pair(oracle, bou, seed=5, precision="mixed"):
     st = ini.couette_noise(bou, seed=seed)
-    g = tc.TaylorCouette(bou, precision="mixed")
+    g = tc.TaylorCouette(bou, precision=precision)
     g.set_state(*st)
     o = oracle.CppOracle(bou)
     o.set_state(*st)
@@ -73,9 +73,12 @@ def test_mixed_routines(gpu_lib, oracle):
     dict(nthm=32, nzm=32, nrm=17),
     dict(nthm=32, nzm=32, nrm=18),
 ], ids=["C1-64cubed", "cheb-variable-dt", "nr17", "nr18"])
-def test_mixed_twenty_steps_vs_fp64(gpu_lib, oracle, case):
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
+def test_mixed_twenty_steps_vs_fp64(gpu_lib, oracle, case, precision):
+    """Both pressure-solve options: FP64 (the default) and float-float."""
     bou = make_bou(**case)
-    g, o = pair(oracle, bou)
+    g, o = pair(oracle, bou, precision=precision)
+    assert g.L.tc_precision(g.h) == {"mixed": 1, "mixed-ff": 2}[precision]
     code_g, n_g, t_g, _ = g.run(20, 0, 0.0)
     code_o, t_o, _ = o.run(0, 20, 0.0)
     assert code_g == code_o == 0
@@ -86,7 +89,7 @@ def test_mixed_twenty_steps_vs_fp64(gpu_lib, oracle, case):
     ti_o, to_o = o.calc_torque()
     terr = max(abs(ti_g - ti_o) / abs(ti_o), abs(to_g - to_o) / abs(to_o))
     div = g.check_divergence()
-    print(case, "velocity", errs, "torque", terr, "div", div)
+    print(precision, case, "velocity", errs, "torque", terr, "div", div)
     assert max(errs) < 1e-3
     assert terr < 1e-4
     assert div < 1e-3 * bou["resid"]

@@ -99,6 +99,75 @@ def test_routines_one_substep(gpu_lib, oracle, case):
     g.close()
 
 
+@pytest.mark.parametrize("case", [
+    dict(nthm=32, nzm=40, nrm=28),
+    dict(nthm=48, nzm=40, nrm=24, istr=4, str=3.0, sizepert=0.1, omegapert=0.5, romeg=0.1, dtmin=1e-4, dtmax=1e-4),
+    dict(nthm=40, nzm=24, nrm=20, istr=6, str=3.0, minstrt=2, minstrz=1, multmin=2),
+], ids=["uniform", "tanh-osc-rot", "cheb-patterned-slip"])
+def test_routines_one_component_at_a_time(gpu_lib, oracle, case):
+    """The per-component entry points in TimeMarcher.F90:31-37 order, each
+    checked against the oracle's routine of the same name right after it
+    runs, for two substeps; then the three-component entry points on the
+    same input give the same fields."""
+    bou = make_bou(**case)
+    g, o, st = pair(oracle, bou)
+    dt, nrm = bou["dtmax"], bou["nrm"]
+    g.begin_step(dt, 0.21)
+    o.call("begin_step", dt, 0.21)
+    for ns in (1, 2):
+        g.set_substep(ns)
+        o.call("set_substep", ns)
+        g.explicit_terms_qt()
+        o.call("explicit_terms_qt")
+        assert rel_err(g.get_field("dq"), o.get(oracle.DQ), interior=False, nk=nrm) < TOL_ROUTINE
+        g.explicit_terms_qr()
+        o.call("explicit_terms_qr")
+        hr_o = o.get(oracle.DPH)[1:-1, 1:-1, 1:nrm]
+        assert rel_err(g.get_field("hr")[..., 1:nrm], hr_o, interior=False) < TOL_ROUTINE
+        g.explicit_terms_qz()
+        o.call("explicit_terms_qz")
+        assert rel_err(g.get_field("qcap"), o.get(oracle.QCAP), interior=False, nk=nrm) < TOL_ROUTINE
+        for comp, ru, w, nk in (("qt", "ru1", oracle.QT, nrm), ("qr", "ru2", oracle.QR, nrm + 1),
+                                ("qz", "ru3", oracle.QZ, nrm)):
+            getattr(g, "implicit_and_update_" + comp)()
+            o.call("implicit_rhs_" + comp)
+            o.call("solve_imp_eqn_update_" + comp)
+            o.call("update_halo", w)
+            lo = 1 if comp == "qr" else 0
+            wr = {"ru1": oracle.RU1, "ru2": oracle.RU2, "ru3": oracle.RU3}[ru]
+            assert rel_err(g.get_field(ru)[..., lo:nrm], o.get(wr)[..., lo:nrm], interior=False) < TOL_ROUTINE, ru
+            got = g.get_state()[("qt", "qr", "qz").index(comp)]
+            assert rel_err(got, o.get(w), nk=nk) < TOL_ROUTINE, comp
+        g.calc_local_divergence()
+        o.call("calc_local_divergence")
+        g.solve_pressure_correction()
+        o.call("solve_pressure_correction")
+        o.call("update_halo", oracle.DPH)
+        g.correct_velocity()
+        o.call("correct_velocity")
+        g.correct_pressure()
+        o.call("correct_pressure")
+        for w in (oracle.QT, oracle.QR, oracle.QZ, oracle.PR):
+            o.call("update_halo", w)
+        compare_state(g, o, TOL_ROUTINE, nrm)
+    # the grouped entry points run the same arithmetic per component
+    h = tc.TaylorCouette(bou)
+    for x in (g, h):
+        x.set_state(*st)
+        x.begin_step(dt, 0.21)
+        x.set_substep(1)
+    for comp in ("qt", "qr", "qz"):
+        getattr(g, "explicit_terms_" + comp)()
+    for comp in ("qt", "qr", "qz"):
+        getattr(g, "implicit_and_update_" + comp)()
+    h.explicit_terms()
+    h.implicit_and_update()
+    for a, b in zip(g.get_state()[:3], h.get_state()[:3]):
+        np.testing.assert_array_equal(a, b)
+    g.close()
+    h.close()
+
+
 def test_fused_step_matches_routines(gpu_lib, oracle):
     """tc_time_marcher (fused kernels) equals the oracle's TimeMarcher."""
     bou = make_bou(nthm=32, nzm=48, nrm=32)

@@ -38,7 +38,7 @@ def run(precision, schedule, bous, seeds, dts, nsteps, rows=0, blocks_per_sm=0):
     return out, stat, info
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-ff"])
 def test_persistent_matches_grouped(gpu_lib, precision):
     bous = MIX[:2] + [PROBE, VAR] + MIX[2:]
     seeds = [1, 2, 7, 11, 3, 4, 5]

@@ -120,3 +120,12 @@ def test_initial_field_is_seeded_and_periodic():
     np.testing.assert_array_equal(qt[:, 0], qt[:, -2])
     noise = qz[1:-1, 1:-1, :5]
     assert 0.004 < noise.std() < 0.007 and np.abs(noise).max() <= 0.01
+
+
+def test_noalloc_wrapper_checks_coefficient_lengths():
+    """The Python mirror refuses coefficient arrays shorter than nrm before
+    anything reaches the library (the C side would read nrm entries)."""
+    with pytest.raises(ValueError):
+        tc.check_divergence_noalloc(0, 0, 0, 8, 8, 16, np.ones(15), np.ones(16), 1.0, 1.0)
+    with pytest.raises(ValueError):
+        tc.check_divergence_noalloc(0, 0, 0, 8, 8, 16, np.ones(16), np.ones(3), 1.0, 1.0)

@@ -62,7 +62,7 @@ def test_mode00_only_moves_pressure(oracle):
 def test_laminar_couette_torque(oracle):
     """CalcTorque normalises by the laminar torque: circular Couette flow gives
     torque -> 1 at both walls as the radial grid is refined (the wall gradient
-    of CalcTorque.F90:133-137 is first-order accurate)."""
+    of CalcTorque.F90:38-42 is first-order accurate)."""
     errs = []
     for nrm in (32, 64, 128):
         bou = make_bou(nthm=8, nzm=8, nrm=nrm)

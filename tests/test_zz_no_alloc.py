@@ -56,6 +56,42 @@ def test_noalloc_divergence_matches_handle(gpu_lib, case):
     g.close()
 
 
+def test_noalloc_on_a_side_stream_and_with_a_nan(gpu_lib):
+    """The same result on a non-default stream; a NaN in the field gives
+    status 169 on both paths instead of a finite maximum."""
+    import torch
+    bou = make_bou(nthm=32, nzm=24, nrm=20, istr=6, str=3.0)
+    g = tc.TaylorCouette(bou)
+    g.set_state(*ini.couette_noise(bou, seed=5, amp=0.3))
+    want = g.check_divergence()
+    qt, qr, qz, pr = g.get_state()
+    nthm, nzm, nrm = bou["nthm"], bou["nzm"], bou["nrm"]
+    udx2m, usrm = tc.grid_array(bou, "udx2m"), tc.grid_array(bou, "usrm")
+    dxt = nthm * bou["lamb"] / (2.0 * math.pi)
+    dxz = nzm / bou["alx3"]
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        dq = [_device_copy(a) for a in (qt, qr, qz)]
+    side.synchronize()
+    got = [tc.check_divergence_noalloc(dq[0].data_ptr(), dq[1].data_ptr(), dq[2].data_ptr(), nthm, nzm, nrm,
+                                       udx2m, usrm, dxt, dxz, stream=side.cuda_stream) for _ in range(2)]
+    for v in got:
+        assert abs(v - want) <= 1e-12 * want
+    qt_nan = qt.copy()
+    qt_nan[5, 7, 3] = np.nan                  # an interior cell (theta 5, z 7, r 3)
+    g.set_state(qt_nan, qr, qz, pr)
+    with pytest.raises(tc.TCError) as e:
+        g.check_divergence()
+    assert e.value.code == 169
+    dn = _device_copy(qt_nan)
+    torch.cuda.synchronize()
+    with pytest.raises(tc.TCError) as e:
+        tc.check_divergence_noalloc(dn.data_ptr(), dq[1].data_ptr(), dq[2].data_ptr(), nthm, nzm, nrm,
+                                    udx2m, usrm, dxt, dxz)
+    assert e.value.code == 169
+    g.close()
+
+
 def test_noalloc_rejects_too_many_radial_cells(gpu_lib):
     import torch
     buf = torch.zeros(16, dtype=torch.float64, device="cuda:0")
