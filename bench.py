@@ -1,15 +1,15 @@
 #!/usr/bin/env python
 """Throughput of the Taylor-Couette time step on GB300, in Mcell-steps/s.
 
-Workload (default, "C2"): 512 x 512 x 384 (theta x z x r) cells, radial
+Workload (default, "C3"): 1024 x 768 x 512 (theta x z x r) cells, radial
 clustering at both walls with the reference's own bou.in grid (ISTR=6,
 STR3=20: the configuration's ISTR=1 is undefined in the reference grid
-generator, and the tanh grid ISTR=4 with STR3=4 is numerically unstable in the
-reference algorithm at 384 radial cells), RINT=1, REXT=1.4, ALX3D=2*pi,
-1/NU=5000, inner cylinder oscillating (VIROTINT=1, AMPL_PERT=0.1,
-FREQ_PERT=0.5), RK3, variable dt (CFLMAX=1.2, DTMIN=1e-5, DTMAX=3e-4), seeded
+generator), RINT=1, REXT=1.4, ALX3D=2*pi, rotating frame ROTP=0.1,
+1/NU=2e4, RK3, variable dt (CFLMAX=1.2, DTMIN=1e-5, DTMAX=1.8e-4), seeded
 Couette-plus-noise start (amplitude 0.01).  One "step" is one full RK3 time
 step (three substeps) with the dt rule of main.F90, FP64 throughout.
+"C2" (512 x 512 x 384, oscillating inner cylinder, DTMAX 3e-4) is the
+production-size case of the same path; "C1" the small CPU-runnable one.
 
   value  : steps with the state resident in HBM (tc_run, one host sync)
   e2e    : through the C ABI with host buffers: tc_set_state from pinned host
@@ -19,11 +19,17 @@ step (three substeps) with the dt rule of main.F90, FP64 throughout.
            algorithmic HBM bytes per launch / its mean CUDA-event duration
   cpu_baseline: the CPU oracle (C++ restatement of the reference's serial
            algorithm) on the host cores, on a bounded sample of the workload
+  mixed  : the same workload in the mixed FP32/FP64 form (FP64 pressure
+           tridiagonals; the float-float variant beside it), with its error
+           against the FP64 run after the same steps
+  ensemble: the batched ensemble of 96 drawn instances, FP64 and mixed
+  serving: continuous batching of Poisson arrivals at two rates, p50/p99
 
 Under torchrun (N > 1) every rank advances its own replica (the time step of
 one run does not shard without the reference's halo and transpose exchanges),
 so scaling is weak and value sums the replicas.
-``--impl reference`` times the CPU oracle alone on rank 0.
+``--impl reference`` times the CPU oracle alone on rank 0, on the full grid
+of the same workload.
 """
 from __future__ import annotations
 
@@ -203,9 +209,21 @@ def cpu_sample(workload: str, seconds: float, threads: int, nr_cap: int = 48):
     return cells * n / el / 1e6, n, el, bou
 
 
+def arm_config(workload: str, world: int) -> dict:
+    """The `config` of the bench line; both arms print the same one."""
+    w = WORKLOADS[workload]
+    nt, nz, nr = w["nthm"], w["nzm"], w["nrm"]
+    cells = nt * nz * nr
+    return {"workload": f"{workload}: {DESCR[workload]}", "grid": [nt, nz, nr], "cells": cells,
+            "precision": "FP64 plain", "parallelism": f"replicas x{world}",
+            "l2": f"inputs larger than L2: every field is {cells * 8 / 1e6:.0f} MB, 12 fields resident"}
+
+
 def run_reference(args, rank: int):
-    """--impl reference: the CPU restatement of the reference's serial algorithm
-    (the Fortran reference itself cannot be built here) on the host cores."""
+    """--impl reference: the CPU restatement of the reference's serial
+    algorithm (the Fortran reference itself cannot be built: no Fortran
+    compiler, MPI, FFTW or LAPACK here or on the GPU host) on every host
+    core, on the full grid of the workload, one full RK3 step per step."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
@@ -216,12 +234,11 @@ def run_reference(args, rank: int):
     import tc_gb300.initial as ini
     tc_ref.build()
     tc_ref.set_threads(threads)
-    w = dict(WORKLOADS[args.workload])
-    w["nrm"] = min(w["nrm"], 48)
-    bou = base_bou(**w)
+    bou = base_bou(**WORKLOADS[args.workload])
     st = ini.couette_noise(bou, seed=1234)
     o = tc_ref.CppOracle(bou)
     o.set_state(*st)
+    del st
     cells = bou["nthm"] * bou["nzm"] * bou["nrm"]
     ntime, tsim = 0, 0.0
     for _ in range(args.warmup):
@@ -233,14 +250,14 @@ def run_reference(args, rank: int):
         ntime += 1
     el = time.perf_counter() - t0
     v = cells * args.steps / el / 1e6
-    sample = (f"{bou['nthm']}x{bou['nzm']}x{bou['nrm']} slab of the {args.workload} workload "
-              f"(radial extent cut from {WORKLOADS[args.workload]['nrm']} to {bou['nrm']}), "
-              f"{args.steps} steps after {args.warmup} warm-up")
+    sample = (f"the full {bou['nthm']}x{bou['nzm']}x{bou['nrm']} grid of the {args.workload} workload, "
+              f"{args.steps} RK3 steps with the dt rule after {args.warmup} warm-up steps, C++ restatement "
+              f"of the reference's serial algorithm, OpenMP on {threads} host cores")
     line = {"impl": "reference", "metric": "Mcell-steps/s", "value": v, "unit": "Mcell-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {DESCR[args.workload]}", "cells_sample": cells},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Couette+noise start)",
+            "config": arm_config(args.workload, args.gpus),
             "cpu_baseline": {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -342,24 +359,17 @@ def ensemble_legs(tc, torch, stream, steps: int, warmup: int, n_inst: int = 96, 
     return out
 
 
-def run_serving(args):
+def serving_leg(tc, torch, n: int, rates: list, chunk: int, hbm_budget: float, matched_runs: int = 6,
+                with_clocks: bool = True) -> dict:
     """The serving workload: seeded Poisson arrivals swept over rates, runs of
     64^3 .. 256x256x128 cells and 100..2000 RK3 steps (variable dt, CFLMAX
-    0.8), admitted against a 150 GB HBM budget into one mixed-precision
-    ensemble (continuous batching).  Beside it: the same runs one after
-    another on the plain FP64 single-run path (tc_run), for the aggregate
-    throughput and each run's torque."""
-    import torch
-    torch.cuda.set_device(0)
-    import __graft_entry__ as entry
-    tc = entry.load()
-    import tc_gb300.build as tb
-    tb.build()
+    0.8), admitted against an HBM budget into one mixed-precision ensemble
+    (continuous batching).  Beside it: the same runs one after another on
+    the plain FP64 single-run path (tc_run), for the aggregate throughput
+    and each run's torque."""
     import tc_gb300.autotune as at
     import tc_gb300.initial as ini
     import tc_gb300.serving as sv
-    n = args.requests
-    rates = [float(x) for x in args.rates.split(",")]
     base = sv.draw_requests(n, rates[0], seed=7)
     states = {r.rid: ini.couette_noise(r.bou, seed=r.seed) for r in base}
     # sequential plain FP64 (the drop-in path), one run at a time
@@ -377,10 +387,10 @@ def run_serving(args):
            "note": "same runs, one after another, tc_run on the plain FP64 path, host states in, torque out"}
     tile, _ = at.tune("mixed", [r.bou for r in base[:8]], [states[r.rid] for r in base[:8]], steps=2)
     sweep = []
-    clocks = Clocks(0)
+    clocks = Clocks(0) if with_clocks else None
     for rate in rates:
         reqs = sv.with_rate(base, rate, seed=7)
-        srv = sv.Server("mixed", hbm_budget=args.hbm_budget, chunk=args.chunk, tune=tile)
+        srv = sv.Server("mixed", hbm_budget=hbm_budget, chunk=chunk, tune=tile)
         res, stats = srv.run(reqs, lambda r: states[r.rid])
         lat = [x.latency for x in res]
         terr = []
@@ -394,26 +404,42 @@ def run_serving(args):
                       "peak_bytes": stats["peak_bytes"],
                       "torque_err_vs_fp64": {"max": max(terr), "median": statistics.median(terr)},
                       "errorcodes_nonzero": sum(1 for x in res if x.errorcode)})
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
     # precision error alone on the first runs, on the FP64 form's time grid
-    nchk = min(200, min(r.nsteps for r in base[:6]))
-    errs = matched_torque_errors(tc, torch.cuda.current_stream(), [r.bou for r in base[:6]],
-                                 [states[r.rid] for r in base[:6]], nchk)
-    matched = {"runs": 6, "steps": nchk, "max": max(errs), "median": statistics.median(errs), "dt": MATCHED_DT}
+    mr = min(matched_runs, len(base))
+    nchk = min(200, min(r.nsteps for r in base[:mr]))
+    errs = matched_torque_errors(tc, torch.cuda.current_stream(), [r.bou for r in base[:mr]],
+                                 [states[r.rid] for r in base[:mr]], nchk)
+    matched = {"runs": mr, "steps": nchk, "max": max(errs), "median": statistics.median(errs), "dt": MATCHED_DT}
     best = max(sweep, key=lambda x: x["value"])
-    line = {"metric": "Mcell-steps/s", "value": best["value"], "unit": "Mcell-steps/s", "n_gpus": 1,
-            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32/f64 mixed", "data": "synthetic (seeded Couette+noise starts, seeded Poisson arrivals)",
-            "config": {"workload": "C5: serving loop, Poisson arrivals, grids 64^3..256x256x128, 100..2000 RK3 "
-                                   "steps, radius ratio 0.5..0.9, 1/NU 500..1e4, variable dt CFLMAX 0.8, "
-                                   f"{args.hbm_budget / 1e9:.0f} GB HBM budget, chunk {args.chunk} steps",
-                       "requests_per_rate": n, "tile": {"threads": tile[0], "rows": tile[1]}},
-            "serving": sweep, "sequential_fp64": seq, "torque_err_mixed_vs_fp64_matched_dt": matched,
+    return {"workload": "C5: serving loop, Poisson arrivals, grids 64^3..256x256x128, 100..2000 RK3 steps, "
+                        "radius ratio 0.5..0.9, 1/NU 500..1e4, variable dt CFLMAX 0.8, "
+                        f"{hbm_budget / 1e9:.0f} GB HBM budget, chunk {chunk} steps",
+            "requests_per_rate": n, "tile": {"threads": tile[0], "rows": tile[1]},
+            "serving": sweep, "best_value": best["value"], "sequential_fp64": seq,
+            "torque_err_mixed_vs_fp64_matched_dt": matched,
             "torque_err_note": "torque_err_vs_fp64 in each sweep entry compares every served run at its end with "
                                "the FP64 run of the same request, each on its own CFL-driven dt sequence over up "
                                "to 2000 steps of a developing (at high Re, turbulent) flow; the matched-dt figure "
                                "isolates the precision error",
             "speedup_served_mixed_vs_sequential_fp64": best["value"] / seq["value"], "clocks": clk}
+
+
+def run_serving(args):
+    """--workload C5: the full serving sweep as its own bench line."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as entry
+    tc = entry.load()
+    import tc_gb300.build as tb
+    tb.build()
+    rates = [float(x) for x in args.rates.split(",")]
+    leg = serving_leg(tc, torch, args.requests, rates, args.chunk, args.hbm_budget)
+    line = {"metric": "Mcell-steps/s", "value": leg["best_value"], "unit": "Mcell-steps/s", "n_gpus": 1,
+            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/f64 mixed", "data": "synthetic (seeded Couette+noise starts, seeded Poisson arrivals)",
+            "config": {"workload": leg["workload"], "requests_per_rate": args.requests, "tile": leg["tile"]},
+            **{k: v for k, v in leg.items() if k not in ("workload", "tile", "requests_per_rate", "best_value")}}
     print(json.dumps(line), flush=True)
 
 
@@ -423,7 +449,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="C2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="C3", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -435,6 +461,9 @@ def main():
     ap.add_argument("--rates", default="0.5,1,2,5,10,20", help="C5: arrival rates, runs/s")
     ap.add_argument("--chunk", type=int, default=25, help="C5: steps between admissions")
     ap.add_argument("--hbm-budget", type=float, default=150e9)
+    ap.add_argument("--no-serving", action="store_true", help="skip the short serving leg of the default run")
+    ap.add_argument("--serve-requests", type=int, default=8, help="serving leg: runs per arrival rate")
+    ap.add_argument("--serve-rates", default="2,20", help="serving leg: arrival rates, runs/s")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -548,57 +577,72 @@ def main():
         ref_state = tuple(a.copy() for a in (qt_o, qr_o, qz_o))
         ref_torque = g.calc_torque()
 
-    # ---- the mixed FP32/FP64 form on the same start ---------------------------
+    # ---- the mixed FP32/FP64 forms on the same start ---------------------------
+    # "mixed": FP64 pressure tridiagonals (the split of the specification);
+    # "mixed-ff": the same with float-float pressure tridiagonals
     mixed = None
     if not args.no_mixed:
-        gm = tc.TaylorCouette(bou, precision="mixed")
-        gm.set_stream(stream.cuda_stream)
-        gm.set_state(*pinned)
-        code_m, ntm, tm, _ = gm.run(args.warmup, 0, 0.0)
-        gm.profile(True)
-        barrier()
-        e0.record(stream)
-        code_m, ntm, tm, _ = gm.run(args.steps, ntm, tm)
-        e1.record(stream)
-        barrier()
-        ms_m = max_over_ranks(e0.elapsed_time(e1))
-        prof_m = gm.profile_read()
-        gm.profile(False)
-        mixed = {"value": world * cells * args.steps / (ms_m * 1e-3) / 1e6, "unit": "Mcell-steps/s",
-                 "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m, "status": code_m}
-        tot_m = sum(v[0] for v in prof_m.values())
-        mixed["kernel_shares"] = {k: round(v[0] / tot_m, 4) for k, v in prof_m.items() if v[1]}
-        if e2e is not None:
+        forms = {}
+        for prec in ("mixed", "mixed-ff"):
+            gm = tc.TaylorCouette(bou, precision=prec)
+            gm.set_stream(stream.cuda_stream)
+            gm.set_state(*pinned)
+            code_m, ntm, tm, _ = gm.run(args.warmup, 0, 0.0)
+            gm.profile(True)
             barrier()
             e0.record(stream)
-            gm.set_state(*pinned)
-            nt3, t3 = 0, 0.0
-            for _ in range(args.steps):
-                code_m, nt3, t3, _ = gm.run(1, nt3, t3)
-            mstate = gm.get_state(out=pinned_out)
+            code_m, ntm, tm, _ = gm.run(args.steps, ntm, tm)
             e1.record(stream)
             barrier()
-            ms_me = max_over_ranks(e0.elapsed_time(e1))
-            mixed["e2e"] = {"value": world * cells * args.steps / (ms_me * 1e-3) / 1e6, "unit": "Mcell-steps/s",
-                            "ms_per_step": ms_me / args.steps}
-            # error against the FP64 path after the same K steps from the same start
-            errs = {}
-            for name, a, b, nk in zip(("qt", "qr", "qz"), mstate[:3], ref_state, (nr, nr + 1, nr)):
-                a, b = a[1:-1, 1:-1, :nk], b[1:-1, 1:-1, :nk]
-                errs[name] = float(np.abs(a - b).max() / np.abs(b).max())
-            ti, to = gm.calc_torque()
-            errs["torque_inner"] = abs(ti - ref_torque[0]) / abs(ref_torque[0])
-            errs["torque_outer"] = abs(to - ref_torque[1]) / abs(ref_torque[1])
-            errs["max_divergence"] = gm.check_divergence()
-            errs["steps"] = args.steps
-            mixed["err_vs_fp64"] = errs
-        gm.close()
+            ms_m = max_over_ranks(e0.elapsed_time(e1))
+            prof_m = gm.profile_read()
+            gm.profile(False)
+            leg = {"value": world * cells * args.steps / (ms_m * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                   "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m, "status": code_m,
+                   "pressure_tridiagonals": "FP64" if prec == "mixed" else "float-float"}
+            tot_m = sum(v[0] for v in prof_m.values())
+            leg["kernel_shares"] = {k: round(v[0] / tot_m, 4) for k, v in prof_m.items() if v[1]}
+            leg["ms_per_step_by_kernel"] = {k: round(v[0] / args.steps, 3) for k, v in prof_m.items() if v[1]}
+            if e2e is not None:
+                barrier()
+                e0.record(stream)
+                gm.set_state(*pinned)
+                nt3, t3 = 0, 0.0
+                for _ in range(args.steps):
+                    code_m, nt3, t3, _ = gm.run(1, nt3, t3)
+                mstate = gm.get_state(out=pinned_out)
+                e1.record(stream)
+                barrier()
+                ms_me = max_over_ranks(e0.elapsed_time(e1))
+                leg["e2e"] = {"value": world * cells * args.steps / (ms_me * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                              "ms_per_step": ms_me / args.steps}
+                # error against the FP64 path after the same K steps from the same start
+                errs = {}
+                for name, a, b, nk in zip(("qt", "qr", "qz"), mstate[:3], ref_state, (nr, nr + 1, nr)):
+                    a, b = a[1:-1, 1:-1, :nk], b[1:-1, 1:-1, :nk]
+                    errs[name] = float(np.abs(a - b).max() / np.abs(b).max())
+                ti, to = gm.calc_torque()
+                errs["torque_inner"] = abs(ti - ref_torque[0]) / abs(ref_torque[0])
+                errs["torque_outer"] = abs(to - ref_torque[1]) / abs(ref_torque[1])
+                errs["max_divergence"] = gm.check_divergence()
+                errs["steps"] = args.steps
+                leg["err_vs_fp64"] = errs
+            gm.close()
+            forms[prec] = leg
+        mixed = dict(forms["mixed"])
+        mixed["float_float_pressure"] = forms["mixed-ff"]
 
     # ---- batched ensembles (FP64 and mixed) ----------------------------------
     ensemble = None
     if not args.no_ensemble:
         ensemble = ensemble_legs(tc, torch, stream, args.ens_steps, args.warmup, args.ens_instances)
         ensemble["speedup_mixed_ensemble_vs_plain_fp64"] = ensemble["mixed"]["value"] / value
+
+    # ---- serving (continuous batching), a short sweep of two arrival rates ------
+    serving = None
+    if not args.no_serving and rank == 0:
+        serving = serving_leg(tc, torch, args.serve_requests, [float(x) for x in args.serve_rates.split(",")],
+                              args.chunk, args.hbm_budget, matched_runs=4, with_clocks=False)
 
     if rank != 0:
         if dist is not None:
@@ -651,10 +695,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Couette+noise start)",
-        "config": {"workload": f"{args.workload}: {DESCR[args.workload]}", "grid": [nt, nz, nr],
-                   "cells": cells, "precision": "FP64 plain", "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2: every field is "
-                         f"{cells * 8 / 1e6:.0f} MB, 12 fields resident"},
+        "config": arm_config(args.workload, world),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": achieved / peak_gbs, "peak_kind": f"{peak_kind} hbm_gbs",
                      "traffic": traffic, "algorithmic_bytes_per_launch": bytes_launch,
@@ -675,6 +716,7 @@ def main():
         "e2e": e2e,
         "mixed": mixed,
         "ensemble": ensemble,
+        "serving": serving,
         "gpu_launches": launches,
         "clocks": clk,
         "sim": {"time": tsim, "last_dt": dt},

@@ -89,6 +89,7 @@ SIGNATURES = {
     "tc_create": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.POINTER(_vp)]),
     "tc_create_ex": (ctypes.c_int, [ctypes.POINTER(Bou), ctypes.c_int, ctypes.POINTER(_vp)]),
     "tc_precision": (ctypes.c_int, [_vp]),
+    "tc_use_tma": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tc_destroy": (None, [_vp]),
     "tc_last_error": (ctypes.c_char_p, [_vp]),
     "tc_set_stream": (ctypes.c_int, [_vp, _vp]),
@@ -456,6 +457,10 @@ class TaylorCouette:
         if rc != 0 and rc not in ERRORS:
             raise TCError(rc, self.L.tc_last_error(self.h).decode())
         return rc, n.value, t.value, d.value
+
+    def use_tma(self, enable: bool = True):
+        """Mixed path: TMA-staged momentum march (default where the grid allows) or not."""
+        self._ck(self.L.tc_use_tma(self.h, 1 if enable else 0))
 
     # per-routine entry points (parity bisection)
     def begin_step(self, dt: float, time: float):

@@ -495,10 +495,8 @@ __device__ __forceinline__ void implicit_cell(const Dims& d, const CoefT<T>& c, 
 template <int MODE, typename T>
 __device__ __forceinline__ void momentum_cell(const Dims& d, const CoefT<T>& c, const MomArgs<T>& a, int i, int j,
                                               int k, int mask = 7) {
-    const int nr = d.nr;
     const Stencil S = make_stencil(d, i, j, k);
     const size_t o = S.o;
-    const int P = S.P;
     const T* qt = a.qt + o;
     const T* qr = a.qr + o;
     const T* qz = a.qz + o;
@@ -685,6 +683,173 @@ __device__ __forceinline__ F2 ldp_f2(const float* p) {
 // 0.486 ms, 1 level 0.404 ms, 2 levels 0.383 ms, 3 levels 0.387 ms.
 constexpr int kMomPrefetch = 2;
 
+// Values the march reads at level k: the pair (i, i+1) and its theta, z
+// neighbours at level k, the pair at level k+1 (suffix p), the RK memory.
+struct MarchIn {
+    F2 tip, tim, tjp, tjm, tjmip, tp;
+    F2 rip, rjp, rp, rpim, rpjm;
+    F2 zip, zim, zjp, zjm, zjpim, zp;
+    F2 pc, pjm, pim;
+    F2 old_t, old_r, old_z;
+};
+
+// Values carried from level k-1 to level k: the pair at levels k (c) and
+// k-1 (m), the neighbours of level k-1 the next level still needs, and the
+// radial fluxes through the face between the two levels.
+struct MarchCarry {
+    F2 tc, tm, tmip, rc, rim, rjm, rm, zc, zm, zmjp, prm;
+    F2 U12, Uz, Gup;
+};
+
+// Per-thread constants of the march.
+struct MarchK {
+    F2 TWO, MTWO, QUARTER, ZERO, GADT, RODT, ALREDT, FIC, UDXZ, UDXZQ, NQROMEG, NCFZ;
+};
+
+__device__ __forceinline__ MarchK march_consts(const Dims& d, const MomArgs<float>& a, size_t col) {
+    MarchK K;
+    K.TWO = bc2(2.0f); K.MTWO = bc2(-2.0f); K.QUARTER = bc2(0.25f); K.ZERO = bc2(0.0f);
+    K.GADT = bc2(ld(a.mr)); K.RODT = bc2(ld(a.mr + 1)); K.ALREDT = bc2(ld(a.mr + 2));
+    K.FIC = a.icyl ? mkf2((float)a.icyl[col], (float)a.icyl[col + 1]) : bc2(1.0f);
+    K.UDXZ = bc2(a.udxz); K.UDXZQ = bc2(a.udxzq); K.NQROMEG = bc2(-a.q_romeg);
+    K.NCFZ = bc2(-ld(a.cf + 2 * (d.nr + 1)));
+    return K;
+}
+
+// The arithmetic of one level k of the march (explicit terms and the
+// implicit right-hand sides of the three components) from the carried
+// values and the level's loads; stores rhs and ru at offset o, then moves
+// the carry up one level.  Shared by the global-load march
+// (momentum_column_x2) and the TMA-staged one (momentum_march_tma_kernel),
+// so both compute the same bits.
+__device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
+                                            const MarchK& K, int k, size_t o, MarchCarry& C, const MarchIn& L) {
+    const int nr = d.nr, nrr = nr + 1;
+    const bool top = k == nr - 1;
+    const int kp = k + 1;
+    const F2 TWO = K.TWO, MTWO = K.MTWO, QUARTER = K.QUARTER, ZERO = K.ZERO;
+    const F2 GADT = K.GADT, RODT = K.RODT, ALREDT = K.ALREDT, FIC = K.FIC;
+    const F2 UDXZ = K.UDXZ, UDXZQ = K.UDXZQ, NQROMEG = K.NQROMEG, NCFZ = K.NCFZ;
+    const F2 U12lo = C.U12, Uzlo = C.Uz;
+    F2& U12 = C.U12;
+    F2& Uz = C.Uz;
+    F2& Gup = C.Gup;
+    const F2 tc = C.tc, tm = C.tm, tmip = C.tmip, rc = C.rc, rim = C.rim, rjm = C.rjm, rm = C.rm;
+    const F2 zc = C.zc, zm = C.zm, zmjp = C.zmjp, prm = C.prm;
+    const F2 tip = L.tip, tim = L.tim, tjp = L.tjp, tjm = L.tjm, tjmip = L.tjmip, tp = L.tp;
+    const F2 rip = L.rip, rjp = L.rjp, rp = L.rp, rpim = L.rpim, rpjm = L.rpjm;
+    const F2 zip = L.zip, zim = L.zim, zjp = L.zjp, zjm = L.zjm, zjpim = L.zjpim, zp = L.zp;
+    const F2 pc = L.pc, pjm = L.pjm, pim = L.pim;
+    const F2 old_t = L.old_t, old_r = L.old_r, old_z = L.old_z;
+    (void)ZERO; (void)nrr;
+    const F2 USRC = bc2(ld(c.usrc + k)), USRCP = bc2(ld(c.usrc + kp));
+    const F2 tz_sw = (zc + zim) * (tc + tjm);
+    const F2 qre = fma2(rp, USRCP, rc * USRC);
+    // ---- ExplicitTermsQT
+    F2 ht;
+    {
+        const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+        const F2 sth = tip + tim;
+        const F2 x11 = (tip - tim) * fma2(TWO, tc, sth);          // (tip+tc)^2 - (tc+tim)^2
+        const F2 rp2 = rp + rpim, rc2 = rc + rim;
+        const F2 up = rp2 * (tp + tc);
+        const F2 qrs = fma2(rp2, USRCP, rc2 * USRC);
+        const F2 h12n = tc * bc2(ld(c.q_usrm + k)) * qrs;
+        U12 = up;
+        F2 s = fma2(up - U12lo, bc2(ld(c.q_udx2rm + k)), h12n);  // h12d + h12n
+        s = fma2(x11, UDXT, s);                                   // + h11
+        s = fma2((zjp + zjpim) * (tjp + tc) - tz_sw, UDXZ, s);    // + h13
+        const F2 qrw = fma2(rpim, USRCP, rim * USRC);
+        F2 r = (qre - qrw) * bc2(ld(c.h_udx1vis1 + k));           // d11qre
+        r = fma2(fma2(MTWO, tc, tjp + tjm), UDXZQ, r);            // + d22qt
+        r = fma2(fma2(MTWO, tc, sth), UDXTQ, r);                  // + d11qt
+        ht = fma2(qrs, NQROMEG, r - s);                           // + Coriolis
+    }
+    // ---- ExplicitTermsQR at face k (1 <= k)
+    F2 hr = ZERO;
+    {
+        const F2 rup = qre * (rp + rc);
+        if (k >= 1) {
+            const F2 UDXT = bc2(ld(c.udxt_c + k)), UDXTQ = bc2(ld(c.udxtq_c + k));
+            const F2 sa = tip + tmip, sb = tc + tm, s4 = sa + sb;
+            const F2 aa = s4 * QUARTER;
+            F2 s = (sa * (rip + rc) - U12lo) * UDXT;                  // h21
+            s = fma2(rup - Gup, bc2(ld(c.q_udx2c + k)), s);           // + h22
+            s = fma2((zjp + zmjp) * (rjp + rc) - Uzlo, UDXZ, s);      // + h23
+            F2 r = fma2(aa, aa, (sb - sa) * bc2(ld(c.udx1vis2 + k))); // h11n + d11qre
+            r = fma2(fma2(MTWO, rc, rip + rim), UDXTQ, r);            // + d11qr
+            r = fma2(fma2(MTWO, rc, rjp + rjm), UDXZQ, r);            // + d22qr
+            r = fma2(s4, bc2(ld(c.q_rc_romeg + k)), r);               // + Coriolis
+            hr = r - s;
+        }
+        Gup = rup;
+    }
+    // ---- ExplicitTermsQZ
+    F2 hz;
+    {
+        const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+        const F2 upz = (rp + rpjm) * (zp + zc);
+        F2 s = (upz - Uzlo) * bc2(ld(c.q_udx2rm + k));                // h32
+        Uz = upz;
+        s = fma2((tip + tjmip) * (zip + zc) - tz_sw, UDXT, s);        // + h31
+        const F2 sjz = zjp + zjm;
+        s = fma2((zjp - zjm) * fma2(TWO, zc, sjz), UDXZ, s);          // + h33
+        F2 r = fma2(MTWO, zc, zim + zip) * UDXTQ;                     // dqz1
+        r = fma2(fma2(MTWO, zc, sjz), UDXZQ, r);                      // + dqz2
+        hz = r - s;
+    }
+    // ---- ImplicitAndUpdateQT
+    {
+        F2 d33;
+        if (k == 0) {
+            const F2 acc = fma2(bc2(ld(c.ac1j)), FIC, bc2(a.ac1j_fs0) * (bc2(1.0f) - FIC));
+            const F2 amm = fma2(bc2(ld(c.am1j)), FIC, bc2(a.am1j_fs0) * (bc2(1.0f) - FIC));
+            d33 = fma2(tp, bc2(ld(c.ap1j)), fma2(tc, acc, bc2(a.virotint + step_vinner<float>(a.st)) * amm));
+        } else if (top) {
+            const float app = ld(c.ap1j + k) * 1.0f + a.ap1j_fs1 * 0.0f;
+            const float acc = ld(c.ac1j + k) * 1.0f + a.ac1j_fs1 * 0.0f;
+            d33 = fma2(tc, bc2(acc), fma2(tm, bc2(ld(c.am1j + k)), bc2(a.virotext * app)));
+        } else {
+            d33 = fma2(tp, bc2(ld(c.ap1j + k)), fma2(tc, bc2(ld(c.ac1j + k)), tm * bc2(ld(c.am1j + k))));
+        }
+        const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old_t, GADT * ht)));
+        st_f2(a.rhs_t + o, rhs);
+        st_f2(a.ru1 + o, ht);
+    }
+    // ---- ImplicitAndUpdateQR, faces 1..nr-1
+    if (k >= 1) {
+        const F2 d33 = fma2(rp, bc2(ld(c.ap2je + k)), fma2(rc, bc2(ld(c.ac2je + k)), rm * bc2(ld(c.am2je + k))));
+        const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old_r, GADT * hr)));
+        st_f2(a.rhs_r + o, rhs);
+        st_f2(a.ru2 + o, hr);
+    }
+    // ---- ImplicitAndUpdateQZ
+    {
+        F2 d33;
+        if (k == 0) {
+            const F2 acc = fma2(bc2(ld(c.ac3j)), FIC, bc2(a.ac3j_fs0) * (bc2(1.0f) - FIC));
+            const F2 amm = fma2(bc2(ld(c.am3j)), FIC, bc2(a.am3j_fs0) * (bc2(1.0f) - FIC));
+            d33 = fma2(zp, bc2(ld(c.ap3j)), fma2(zc, acc, zc * amm));
+        } else if (top) {
+            const float app = ld(c.ap3j + k) * 1.0f + a.ap3j_fs1 * 0.0f;
+            const float acc = ld(c.ac3j + k) * 1.0f + a.ac3j_fs1 * 0.0f;
+            d33 = fma2(zc, bc2(app), fma2(zc, bc2(acc), zm * bc2(ld(c.am3j + k))));
+        } else {
+            d33 = fma2(zp, bc2(ld(c.ap3j + k)), fma2(zc, bc2(ld(c.ac3j + k)), zm * bc2(ld(c.am3j + k))));
+        }
+        // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
+        const F2 old = top ? hz : old_z;
+        const F2 rhs = fma2(pc - pjm, NCFZ, fma2(ALREDT, d33, fma2(RODT, old, GADT * hz)));
+        st_f2(a.rhs_z + o, rhs);
+        st_f2(a.ru3 + o, hz);
+    }
+    // march: level k becomes the lower neighbour of level k+1
+    C.tm = tc; C.tmip = tip; C.tc = tp;
+    C.rm = rc; C.rc = rp; C.rim = rpim; C.rjm = rpjm;
+    C.zm = zc; C.zmjp = zjp; C.zc = zp;
+    C.prm = pc;
+}
+
 __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
                                                    int i, int j, int k0, int k1) {
     const int nr = d.nr, nt = d.nt, nz = d.nz;
@@ -693,13 +858,8 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
     const int dipB = i + 2 == nt ? 2 - nt : 2;         // q(i+2)
     const int djm = j == 0 ? (nz - 1) * nt : -nt, djp = j == nz - 1 ? -(nz - 1) * nt : nt;
     const size_t col = (size_t)j * nt + i;
-    const F2 TWO = bc2(2.0f), MTWO = bc2(-2.0f), QUARTER = bc2(0.25f), ZERO = bc2(0.0f);
-    const float gadt = ld(a.mr), rodt = ld(a.mr + 1), alredt = ld(a.mr + 2);
-    const F2 GADT = bc2(gadt), RODT = bc2(rodt), ALREDT = bc2(alredt);
-    const int nrr = nr + 1;
-    const F2 FIC = a.icyl ? mkf2((float)a.icyl[col], (float)a.icyl[col + 1]) : bc2(1.0f);
-    const F2 UDXZ = bc2(a.udxz), UDXZQ = bc2(a.udxzq), NQROMEG = bc2(-a.q_romeg);
-    const F2 NCFZ = bc2(-ld(a.cf + 2 * nrr));
+    const MarchK K = march_consts(d, a, col);
+    const F2 ZERO = K.ZERO;
     const float* qt = a.qt;
     const float* qr = a.qr;
     const float* qz = a.qz;
@@ -709,25 +869,23 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
     size_t o = (size_t)k0 * P + col;
     const int km0 = k0 > 0 ? k0 - 1 : 0;
     const size_t om = (size_t)km0 * P + col;
-    F2 tc = ld_f2(qt + o), tm = ld_f2(qt + om);
-    F2 tmip = mkf2(f2y(tm), ld(qt + om + dipB));
-    F2 rc = ld_f2(qr + o);
-    F2 rim = mkf2(ld(qr + o + dimA), f2x(rc));
-    F2 rjm = ld_f2(qr + o + djm);
-    F2 rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
-    F2 zc = ld_f2(qz + o), zm = ld_f2(qz + om), zmjp = ld_f2(qz + om + djp);
-    F2 prm = k0 > 0 ? ld_f2(pr + om) : ZERO;
-    F2 U12, Uz, Gup;
+    MarchCarry C;
+    C.tc = ld_f2(qt + o); C.tm = ld_f2(qt + om);
+    C.tmip = mkf2(f2y(C.tm), ld(qt + om + dipB));
+    C.rc = ld_f2(qr + o);
+    C.rim = mkf2(ld(qr + o + dimA), f2x(C.rc));
+    C.rjm = ld_f2(qr + o + djm);
+    C.rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
+    C.zc = ld_f2(qz + o); C.zm = ld_f2(qz + om); C.zmjp = ld_f2(qz + om + djp);
+    C.prm = k0 > 0 ? ld_f2(pr + om) : ZERO;
     {
-        U12 = (rc + rim) * (tc + tm);
-        Uz = (rc + rjm) * (zc + zm);
+        C.U12 = (C.rc + C.rim) * (C.tc + C.tm);
+        C.Uz = (C.rc + C.rjm) * (C.zc + C.zm);
         const float usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : 0.0f;
-        Gup = fma2(rm, bc2(usrcm), rc * bc2(usrc)) * (rc + rm);
+        C.Gup = fma2(C.rm, bc2(usrcm), C.rc * bc2(usrc)) * (C.rc + C.rm);
     }
     for (int k = k0; k < k1; ++k, o += P) {
         const bool top = k == nr - 1;
-        const F2 U12lo = U12, Uzlo = Uz;
-        const int kp = k + 1;
         // bring the pair's entries of level k + kMomPrefetch into L2 ahead of
         // their loads
         if (k + kMomPrefetch < nr) {
@@ -743,136 +901,31 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
             }
         }
         // loads of level k (neighbours) and k+1 (column)
+        MarchIn L;
         float tcx, tcy, rcx, rcy, zcx, zcy;
-        f2xy(tc, tcx, tcy);
-        f2xy(rc, rcx, rcy);
-        f2xy(zc, zcx, zcy);
-        const F2 tip = mkf2(tcy, ld(qt + o + dipB)), tim = mkf2(ld(qt + o + dimA), tcx);
-        const F2 tjp = ld_f2(qt + o + djp), tjm = ld_f2(qt + o + djm);
-        const F2 tjmip = mkf2(f2y(tjm), ld(qt + o + djm + dipB));
-        const F2 tp = top ? tc : ld_f2(qt + o + P);
-        const F2 rip = mkf2(rcy, ld(qr + o + dipB)), rjp = ld_f2(qr + o + djp);
-        const F2 rp = ld_f2(qr + o + P);
-        const F2 rpim = mkf2(ld(qr + o + P + dimA), f2x(rp)), rpjm = ld_f2(qr + o + P + djm);
-        const F2 zip = mkf2(zcy, ld(qz + o + dipB)), zim = mkf2(ld(qz + o + dimA), zcx);
-        const F2 zjp = ld_f2(qz + o + djp), zjm = ld_f2(qz + o + djm);
-        const F2 zjpim = mkf2(ld(qz + o + djp + dimA), f2x(zjp));
-        const F2 zp = top ? zc : ld_f2(qz + o + P);
-        const F2 pc = ld_f2(pr + o), pjm = ld_f2(pr + o + djm);
-        const F2 pim = mkf2(ld(pr + o + dimA), f2x(pc));
+        f2xy(C.tc, tcx, tcy);
+        f2xy(C.rc, rcx, rcy);
+        f2xy(C.zc, zcx, zcy);
+        L.tip = mkf2(tcy, ld(qt + o + dipB)); L.tim = mkf2(ld(qt + o + dimA), tcx);
+        L.tjp = ld_f2(qt + o + djp); L.tjm = ld_f2(qt + o + djm);
+        L.tjmip = mkf2(f2y(L.tjm), ld(qt + o + djm + dipB));
+        L.tp = top ? C.tc : ld_f2(qt + o + P);
+        L.rip = mkf2(rcy, ld(qr + o + dipB)); L.rjp = ld_f2(qr + o + djp);
+        L.rp = ld_f2(qr + o + P);
+        L.rpim = mkf2(ld(qr + o + P + dimA), f2x(L.rp)); L.rpjm = ld_f2(qr + o + P + djm);
+        L.zip = mkf2(zcy, ld(qz + o + dipB)); L.zim = mkf2(ld(qz + o + dimA), zcx);
+        L.zjp = ld_f2(qz + o + djp); L.zjm = ld_f2(qz + o + djm);
+        L.zjpim = mkf2(ld(qz + o + djp + dimA), f2x(L.zjp));
+        L.zp = top ? C.zc : ld_f2(qz + o + P);
+        L.pc = ld_f2(pr + o); L.pjm = ld_f2(pr + o + djm);
+        L.pim = mkf2(ld(pr + o + dimA), f2x(L.pc));
         // the RK memory of this level, loaded with the fields so that its
         // latency overlaps the explicit terms (below, the compiler could not
         // move these loads above the previous level's stores)
-        const F2 old_t = a.use_ru ? ldp_f2(a.ru1 + o) : ZERO;
-        const F2 old_r = (a.use_ru && k >= 1) ? ldp_f2(a.ru2 + o) : ZERO;
-        const F2 old_z = (a.use_ru && !top) ? ldp_f2(a.ru3 + o) : ZERO;
-
-        const F2 USRC = bc2(ld(c.usrc + k)), USRCP = bc2(ld(c.usrc + kp));
-        const F2 tz_sw = (zc + zim) * (tc + tjm);
-        const F2 qre = fma2(rp, USRCP, rc * USRC);
-        // ---- ExplicitTermsQT
-        F2 ht;
-        {
-            const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
-            const F2 sth = tip + tim;
-            const F2 x11 = (tip - tim) * fma2(TWO, tc, sth);          // (tip+tc)^2 - (tc+tim)^2
-            const F2 rp2 = rp + rpim, rc2 = rc + rim;
-            const F2 up = rp2 * (tp + tc);
-            const F2 qrs = fma2(rp2, USRCP, rc2 * USRC);
-            const F2 h12n = tc * bc2(ld(c.q_usrm + k)) * qrs;
-            U12 = up;
-            F2 s = fma2(up - U12lo, bc2(ld(c.q_udx2rm + k)), h12n);  // h12d + h12n
-            s = fma2(x11, UDXT, s);                                   // + h11
-            s = fma2((zjp + zjpim) * (tjp + tc) - tz_sw, UDXZ, s);    // + h13
-            const F2 qrw = fma2(rpim, USRCP, rim * USRC);
-            F2 r = (qre - qrw) * bc2(ld(c.h_udx1vis1 + k));           // d11qre
-            r = fma2(fma2(MTWO, tc, tjp + tjm), UDXZQ, r);            // + d22qt
-            r = fma2(fma2(MTWO, tc, sth), UDXTQ, r);                  // + d11qt
-            ht = fma2(qrs, NQROMEG, r - s);                           // + Coriolis
-        }
-        // ---- ExplicitTermsQR at face k (1 <= k)
-        F2 hr = ZERO;
-        {
-            const F2 rup = qre * (rp + rc);
-            if (k >= 1) {
-                const F2 UDXT = bc2(ld(c.udxt_c + k)), UDXTQ = bc2(ld(c.udxtq_c + k));
-                const F2 sa = tip + tmip, sb = tc + tm, s4 = sa + sb;
-                const F2 aa = s4 * QUARTER;
-                F2 s = (sa * (rip + rc) - U12lo) * UDXT;                  // h21
-                s = fma2(rup - Gup, bc2(ld(c.q_udx2c + k)), s);           // + h22
-                s = fma2((zjp + zmjp) * (rjp + rc) - Uzlo, UDXZ, s);      // + h23
-                F2 r = fma2(aa, aa, (sb - sa) * bc2(ld(c.udx1vis2 + k))); // h11n + d11qre
-                r = fma2(fma2(MTWO, rc, rip + rim), UDXTQ, r);            // + d11qr
-                r = fma2(fma2(MTWO, rc, rjp + rjm), UDXZQ, r);            // + d22qr
-                r = fma2(s4, bc2(ld(c.q_rc_romeg + k)), r);               // + Coriolis
-                hr = r - s;
-            }
-            Gup = rup;
-        }
-        // ---- ExplicitTermsQZ
-        F2 hz;
-        {
-            const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
-            const F2 upz = (rp + rpjm) * (zp + zc);
-            F2 s = (upz - Uzlo) * bc2(ld(c.q_udx2rm + k));                // h32
-            Uz = upz;
-            s = fma2((tip + tjmip) * (zip + zc) - tz_sw, UDXT, s);        // + h31
-            const F2 sjz = zjp + zjm;
-            s = fma2((zjp - zjm) * fma2(TWO, zc, sjz), UDXZ, s);          // + h33
-            F2 r = fma2(MTWO, zc, zim + zip) * UDXTQ;                     // dqz1
-            r = fma2(fma2(MTWO, zc, sjz), UDXZQ, r);                      // + dqz2
-            hz = r - s;
-        }
-        // ---- ImplicitAndUpdateQT
-        {
-            F2 d33;
-            if (k == 0) {
-                const F2 acc = fma2(bc2(ld(c.ac1j)), FIC, bc2(a.ac1j_fs0) * (bc2(1.0f) - FIC));
-                const F2 amm = fma2(bc2(ld(c.am1j)), FIC, bc2(a.am1j_fs0) * (bc2(1.0f) - FIC));
-                d33 = fma2(tp, bc2(ld(c.ap1j)), fma2(tc, acc, bc2(a.virotint + step_vinner<float>(a.st)) * amm));
-            } else if (top) {
-                const float app = ld(c.ap1j + k) * 1.0f + a.ap1j_fs1 * 0.0f;
-                const float acc = ld(c.ac1j + k) * 1.0f + a.ac1j_fs1 * 0.0f;
-                d33 = fma2(tc, bc2(acc), fma2(tm, bc2(ld(c.am1j + k)), bc2(a.virotext * app)));
-            } else {
-                d33 = fma2(tp, bc2(ld(c.ap1j + k)), fma2(tc, bc2(ld(c.ac1j + k)), tm * bc2(ld(c.am1j + k))));
-            }
-            const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old_t, GADT * ht)));
-            st_f2(a.rhs_t + o, rhs);
-            st_f2(a.ru1 + o, ht);
-        }
-        // ---- ImplicitAndUpdateQR, faces 1..nr-1
-        if (k >= 1) {
-            const F2 d33 = fma2(rp, bc2(ld(c.ap2je + k)), fma2(rc, bc2(ld(c.ac2je + k)), rm * bc2(ld(c.am2je + k))));
-            const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old_r, GADT * hr)));
-            st_f2(a.rhs_r + o, rhs);
-            st_f2(a.ru2 + o, hr);
-        }
-        // ---- ImplicitAndUpdateQZ
-        {
-            F2 d33;
-            if (k == 0) {
-                const F2 acc = fma2(bc2(ld(c.ac3j)), FIC, bc2(a.ac3j_fs0) * (bc2(1.0f) - FIC));
-                const F2 amm = fma2(bc2(ld(c.am3j)), FIC, bc2(a.am3j_fs0) * (bc2(1.0f) - FIC));
-                d33 = fma2(zp, bc2(ld(c.ap3j)), fma2(zc, acc, zc * amm));
-            } else if (top) {
-                const float app = ld(c.ap3j + k) * 1.0f + a.ap3j_fs1 * 0.0f;
-                const float acc = ld(c.ac3j + k) * 1.0f + a.ac3j_fs1 * 0.0f;
-                d33 = fma2(zc, bc2(app), fma2(zc, bc2(acc), zm * bc2(ld(c.am3j + k))));
-            } else {
-                d33 = fma2(zp, bc2(ld(c.ap3j + k)), fma2(zc, bc2(ld(c.ac3j + k)), zm * bc2(ld(c.am3j + k))));
-            }
-            // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
-            const F2 old = top ? hz : old_z;
-            const F2 rhs = fma2(pc - pjm, NCFZ, fma2(ALREDT, d33, fma2(RODT, old, GADT * hz)));
-            st_f2(a.rhs_z + o, rhs);
-            st_f2(a.ru3 + o, hz);
-        }
-        // march: level k becomes the lower neighbour of level k+1
-        tm = tc; tmip = tip; tc = tp;
-        rm = rc; rc = rp; rim = rpim; rjm = rpjm;
-        zm = zc; zmjp = zjp; zc = zp;
-        prm = pc;
+        L.old_t = a.use_ru ? ldp_f2(a.ru1 + o) : ZERO;
+        L.old_r = (a.use_ru && k >= 1) ? ldp_f2(a.ru2 + o) : ZERO;
+        L.old_z = (a.use_ru && !top) ? ldp_f2(a.ru3 + o) : ZERO;
+        march_level(d, c, a, K, k, o, C, L);
     }
 }
 

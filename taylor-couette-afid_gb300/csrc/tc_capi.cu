@@ -249,6 +249,53 @@ const char* tc_last_error(const tc_handle* h) {
     return g_last_error.c_str();
 }
 
+// cuTensorMapEncodeTiled of the driver, looked up through the runtime (the
+// library links the runtime only).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// A 3-D descriptor of an FP32 array [nplanes][nz][nt] with a box of one
+// 72-float row (the march's staged rows).
+static bool march_map(CUtensorMap* m, const float* base, int nt, int nz, int nplanes) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nt, (cuuint64_t)nz, (cuuint64_t)nplanes};
+    const cuuint64_t strides[2] = {(cuuint64_t)nt * 4, (cuuint64_t)nt * nz * 4};
+    const cuuint32_t box[3] = {72, 1, 1}, estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Descriptors of the mixed march for grids whose rows meet the TMA rules
+// (nthm a multiple of 4, so rows start on 16-byte boundaries; nthm >= 64).
+static bool make_march_maps(tc_handle* h) {
+    const Dims& d = h->d;
+    if (!h->mixed || d.nt % 4 != 0 || d.nt < 64) return false;
+    const FieldsT<float>& f = h->ff;
+    MarchMaps& M = h->maps;
+    return march_map(&M.qt, f.qt, d.nt, d.nz, d.nr) && march_map(&M.qr, f.qr, d.nt, d.nz, d.nr + 1) &&
+           march_map(&M.qz, f.qz, d.nt, d.nz, d.nr) && march_map(&M.pr, f.prf, d.nt, d.nz, d.nr) &&
+           march_map(&M.ru1, f.ru1, d.nt, d.nz, d.nr) && march_map(&M.ru2, f.ru2, d.nt, d.nz, d.nr + 1) &&
+           march_map(&M.ru3, f.ru3, d.nt, d.nz, d.nr);
+}
+
 int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     if (!cfg || !out) return fail(nullptr, 2000, "null argument");
     if (precision != TC_PREC_FP64 && precision != TC_PREC_MIXED && precision != TC_PREC_MIXED_FF)
@@ -386,6 +433,10 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
 
     launch_pressure_factors(h->stream, d, h->c, pl, pdv);
     h->ff.ptri_ff = h->ptri_ff;
+    h->ff.tma = nullptr;
+    h->fd.tma = nullptr;
+    h->maps_ok = make_march_maps(h);
+    if (h->maps_ok) h->ff.tma = &h->maps;
     if (h->ptri_ff) {
         float2* pu = nullptr;
         ce = dalloc(h, &pu, (size_t)nr);
@@ -406,6 +457,14 @@ int tc_create(const tc_bou* cfg, tc_handle** out) { return tc_create_ex(cfg, TC_
 int tc_get_bou(const tc_handle* h, tc_bou* out) {
     if (!h || !out) return 2000;
     *out = h->bou;
+    return 0;
+}
+
+int tc_use_tma(tc_handle* h, int enable) {
+    if (int r = check(h)) return r;
+    if (enable && !h->maps_ok) return fail(h, 2019, "no TMA descriptors for this handle (FP64, or nthm not a "
+                                                   "multiple of 4 or below 64)");
+    h->ff.tma = enable ? &h->maps : nullptr;
     return 0;
 }
 
@@ -431,22 +490,53 @@ int tc_set_stream(tc_handle* h, void* s) {
 
 // ---- state transfer --------------------------------------------------------
 
+// The device address of a host array of n doubles when all of it is pinned
+// (page-locked and mapped: cudaHostAlloc, cudaHostRegister) memory, else
+// null.  The first and the last element are both checked, so an array that
+// runs out of its pinned allocation takes the staged path.
+static double* pinned_view(const void* p, size_t n) {
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    const char* last = static_cast<const char*>(p) + (n - 1) * sizeof(double);
+    if (cudaPointerGetAttributes(&a1, last) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if (static_cast<char*>(a1.devicePointer) - static_cast<char*>(a0.devicePointer) !=
+        (ptrdiff_t)((n - 1) * sizeof(double)))
+        return nullptr;
+    return static_cast<double*>(a0.devicePointer);
+}
+
+// Host array (reference layout) -> device field.  From pinned host memory the
+// transpose kernel reads the host array itself over the CPU-GPU link (one
+// pass, no staging copy); from pageable memory the array is first copied
+// into the staging buffer.
 template <typename T>
 static int upload(tc_handle* h, const double* src, T* dst, int nk, int halo) {
     const Dims& d = h->d;
     size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
-    CK(cudaMemcpyAsync(h->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, h->stream), "H2D copy");
-    L(h, K_LAYOUT, 1, [&] { launch_to_device(h->stream, d, (const double*)h->stage, dst, nk, halo); });
+    const double* view = pinned_view(src, n);
+    if (!view) {
+        CK(cudaMemcpyAsync(h->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, h->stream), "H2D copy");
+        view = h->stage;
+    }
+    L(h, K_LAYOUT, 1, [&] { launch_to_device(h->stream, d, view, dst, nk, halo); });
     return 0;
 }
 
+// Device field -> host array.  Asynchronous: the caller synchronises the
+// stream once after its last download (stream order keeps the staging
+// buffer's copies apart).
 template <typename T>
 static int download(tc_handle* h, const T* src, double* dst, int nk, int halo) {
     const Dims& d = h->d;
     size_t n = (size_t)(d.nr + 1) * (d.nz + 2 * halo) * (d.nt + 2 * halo);
+    if (double* view = pinned_view(dst, n)) {
+        L(h, K_LAYOUT, 1, [&] { launch_to_host(h->stream, d, src, view, nk, halo); });
+        return 0;
+    }
     L(h, K_LAYOUT, 1, [&] { launch_to_host(h->stream, d, src, h->stage, nk, halo); });
     CK(cudaMemcpyAsync(dst, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H copy");
-    CK(cudaStreamSynchronize(h->stream), "D2H sync");
     return 0;
 }
 
@@ -491,6 +581,7 @@ static int get_state_t(tc_handle* h, double* qt, double* qr, double* qz, double*
     if (qr) if (int r = download(h, (const T*)f.qr, qr, d.nr + 1, 1)) return r;
     if (qz) if (int r = download(h, (const T*)f.qz, qz, d.nr, 1)) return r;
     if (pr) if (int r = download(h, (const double*)f.pr, pr, d.nr, 1)) return r;
+    CK(cudaStreamSynchronize(h->stream), "get_state sync");
     return 0;
 }
 
@@ -524,7 +615,12 @@ static int field_io(tc_handle* h, int which, double* out, const double* in) {
         default: return fail(h, 2004, "unknown field id");
     }
     if (!p && !pp) return fail(h, 2005, "field not allocated (call tc_explicit_terms first)");
-    if (out) return pp ? download(h, (const double*)pp, out, nk, halo) : download(h, (const T*)p, out, nk, halo);
+    if (out) {
+        int r = pp ? download(h, (const double*)pp, out, nk, halo) : download(h, (const T*)p, out, nk, halo);
+        if (r) return r;
+        CK(cudaStreamSynchronize(h->stream), "get_field sync");
+        return 0;
+    }
     int r = pp ? upload(h, in, pp, nk, halo) : upload(h, in, p, nk, halo);
     if (r) return r;
     if (pp) refresh_prf(h, f);

@@ -21,6 +21,8 @@ struct tc_handle {
     tcgb::FieldsT<float> ff;      // mixed path state
     tcgb::PlansT<double> pd;
     tcgb::PlansT<float> pf;
+    tcgb::MarchMaps maps;         // TMA descriptors of the mixed march (ff.tma points here when in use)
+    bool maps_ok = false;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     double* stage = nullptr;

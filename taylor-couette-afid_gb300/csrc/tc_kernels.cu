@@ -23,6 +23,7 @@
 #include <type_traits>
 
 #include "tc_bodies.cuh"
+#include "tc_tma.cuh"
 
 namespace tcgb {
 
@@ -156,6 +157,190 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
     momentum_column_x2(d, c, a, i, j, k0, k1);
 }
 
+
+// --------------------------------------------------------------------------
+// The FP32 march with its input planes staged in shared memory by the TMA
+// unit.  A block of 32 x 4 threads owns a 64 (theta) x 4 (z) tile of
+// columns and marches kMomChunk radial levels; each radial plane p of its
+// inputs is one stage: for qt, qr, qz the rows j0-1 .. j0+4 of the tile, for
+// the FP32 pressure j0-1 .. j0+3 and for the RK memory j0 .. j0+3, every row
+// theta i0-4 .. i0+67 (one 72-float TMA box a row, z wrapped periodically
+// when the row is chosen; the theta halo outside 0..nthm-1 reads as zero and
+// the two edge columns of the domain take their periodic neighbour from
+// global memory instead).  kTmaStages planes are in flight: while level k
+// reads planes k and k+1, planes k+2 .. k+kTmaStages-1 load.  The
+// arithmetic is march_level, as in momentum_march_x2_kernel.  Every wait on
+// an mbarrier is bounded (kTmaWaitNs); a wait that gives up makes the block
+// wait for its loads still in flight (bounded again), raise error 3001 with
+// the step halted, and return.
+// --------------------------------------------------------------------------
+
+constexpr int kTmaW = 72;                  // floats of one staged row
+constexpr int kTmaRowB = 384;              // bytes of a row slot (128-byte aligned)
+constexpr int kTmaStages = 4;
+constexpr int kRowQt = 0, kRowQr = 6, kRowQz = 12, kRowPr = 18, kRowRu = 23;
+constexpr int kRowsNoRu = 23, kRowsRu = 35;
+constexpr int kTmaStageB = kRowsRu * kTmaRowB;
+constexpr size_t kTmaSmem = (size_t)kTmaStages * kTmaStageB + 128;
+constexpr unsigned long long kTmaWaitNs = 1000000000ull;       // 1 s
+constexpr unsigned long long kTmaDrainNs = 100000000ull;       // 0.1 s per plane
+
+__global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, CoefT<float> c, MomArgs<float> a,
+                                                                    const __grid_constant__ MarchMaps maps) {
+    if (a.st->halt) return;
+    __shared__ __align__(8) unsigned long long bars[kTmaStages];
+    extern __shared__ unsigned char tma_dyn[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(tma_dyn) + 127) & ~(size_t)127);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nr = d.nr, nt = d.nt, nz = d.nz;
+    const int P = (int)d.P;
+    const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 4;
+    const int k0 = blockIdx.z * kMomChunk, k1 = min(k0 + kMomChunk, nr);
+    const int i = i0 + 2 * tx, j = j0 + ty;
+    const bool active = i < nt && j < nz;
+    const int nrows = a.use_ru ? kRowsRu : kRowsNoRu;
+    const unsigned sbase = smem_u32(sm), bbase = smem_u32(bars);
+
+    if (tx == 0 && ty == 0) {
+        for (int q = 0; q < kTmaStages; ++q) mbar_init(bbase + 8 * q, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    // plane p of the chunk into stage (p - k0) % kTmaStages; warp 0 posts
+    // the byte count, then each lane issues its rows
+    auto issue = [&](int p) {
+        if (ty != 0) return;
+        const int q = (p - k0) % kTmaStages;
+        const unsigned bar = bbase + 8 * q, dst = sbase + q * kTmaStageB;
+        if (tx == 0) mbar_arrive_expect_tx(bar, (unsigned)(nrows * kTmaW * 4));
+        __syncwarp();
+        for (int r = tx; r < nrows; r += 32) {
+            const CUtensorMap* m;
+            int dz;
+            if (r < kRowQr) { m = &maps.qt; dz = r - kRowQt - 1; }
+            else if (r < kRowQz) { m = &maps.qr; dz = r - kRowQr - 1; }
+            else if (r < kRowPr) { m = &maps.qz; dz = r - kRowQz - 1; }
+            else if (r < kRowRu) { m = &maps.pr; dz = r - kRowPr - 1; }
+            else {
+                const int u = r - kRowRu;
+                m = u < 4 ? &maps.ru1 : (u < 8 ? &maps.ru2 : &maps.ru3);
+                dz = u & 3;
+            }
+            const int zr = ((j0 + dz) % nz + nz) % nz;
+            tma_load_3d(dst + r * kTmaRowB, m, i0 - 4, zr, p, bar);
+        }
+    };
+    int issued = k0 - 1;
+    for (int p = k0; p <= k1 && p < k0 + kTmaStages; ++p) { issue(p); issued = p; }
+
+    auto stage_row = [&](int p, int row) -> const float* {
+        return reinterpret_cast<const float*>(sm + ((p - k0) % kTmaStages) * kTmaStageB + row * kTmaRowB);
+    };
+    auto parity = [&](int p) -> unsigned { return (unsigned)(((p - k0) / kTmaStages) & 1); };
+    auto bar_of = [&](int p) -> unsigned { return bbase + 8 * ((p - k0) % kTmaStages); };
+    const int xi = 4 + 2 * tx;                       // the pair's first cell in a staged row
+    auto pair = [&](const float* row) -> F2 {
+        const float2 v = *reinterpret_cast<const float2*>(row + xi);
+        return mkf2(v.x, v.y);
+    };
+    // rows of this thread: z rows j-1, j, j+1 of the 6-row fields
+    const int rjm = ty, rj = ty + 1, rjp = ty + 2;
+
+    bool fail = !mbar_wait(bar_of(k0), parity(k0), kTmaWaitNs);
+    int pend = fail ? k0 : k0 + 1;                   // lowest plane not yet consumed
+
+    const bool eL = i == 0, eR = i + 2 == nt;        // the domain's periodic theta edges
+    const int dimA = eL ? nt - 1 : -1, dipB = eR ? 2 - nt : 2;
+    const int jj = j < nz ? j : nz - 1;
+    const int djm = jj == 0 ? (nz - 1) * nt : -nt, djp = jj == nz - 1 ? -(nz - 1) * nt : nt;
+    const size_t col = (size_t)jj * nt + (i < nt ? i : 0);
+    const MarchK K = march_consts(d, a, col);
+    const F2 ZERO = K.ZERO;
+    const float* qt = a.qt;
+    const float* qr = a.qr;
+    const float* qz = a.qz;
+    const float* pr = a.pr;
+    size_t o = (size_t)k0 * P + col;
+    MarchCarry C;
+    if (active) {
+        const int km0 = k0 > 0 ? k0 - 1 : 0;
+        const size_t om = (size_t)km0 * P + col;
+        C.tc = pair(stage_row(k0, kRowQt + rj));
+        C.tm = ld_f2(qt + om);
+        C.tmip = mkf2(f2y(C.tm), ld(qt + om + dipB));
+        C.rc = pair(stage_row(k0, kRowQr + rj));
+        C.rim = mkf2(eL ? ld(qr + o + dimA) : stage_row(k0, kRowQr + rj)[xi - 1], f2x(C.rc));
+        C.rjm = pair(stage_row(k0, kRowQr + rjm));
+        C.rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
+        C.zc = pair(stage_row(k0, kRowQz + rj));
+        C.zm = ld_f2(qz + om);
+        C.zmjp = ld_f2(qz + om + djp);
+        C.prm = k0 > 0 ? ld_f2(pr + om) : ZERO;
+        C.U12 = (C.rc + C.rim) * (C.tc + C.tm);
+        C.Uz = (C.rc + C.rjm) * (C.zc + C.zm);
+        const float usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : 0.0f;
+        C.Gup = fma2(C.rm, bc2(usrcm), C.rc * bc2(usrc)) * (C.rc + C.rm);
+    }
+    for (int k = k0; k < k1; ++k, o += P) {
+        const int kn = k + 1;
+        if (!fail) {
+            fail = !mbar_wait(bar_of(kn), parity(kn), kTmaWaitNs);
+            if (!fail) pend = kn + 1;
+        }
+        if (active && !fail) {
+            const bool top = k == nr - 1;
+            const float* Tj = stage_row(k, kRowQt + rj);
+            const float* Tjm = stage_row(k, kRowQt + rjm);
+            const float* Rj = stage_row(k, kRowQr + rj);
+            const float* Zj = stage_row(k, kRowQz + rj);
+            const float* Zjp = stage_row(k, kRowQz + rjp);
+            const float* Pj = stage_row(k, kRowPr + rj);
+            MarchIn L;
+            float tcx, tcy, rcx, rcy, zcx, zcy;
+            f2xy(C.tc, tcx, tcy);
+            f2xy(C.rc, rcx, rcy);
+            f2xy(C.zc, zcx, zcy);
+            L.tip = mkf2(tcy, eR ? ld(qt + o + dipB) : Tj[xi + 2]);
+            L.tim = mkf2(eL ? ld(qt + o + dimA) : Tj[xi - 1], tcx);
+            L.tjp = pair(stage_row(k, kRowQt + rjp));
+            L.tjm = pair(Tjm);
+            L.tjmip = mkf2(f2y(L.tjm), eR ? ld(qt + o + djm + dipB) : Tjm[xi + 2]);
+            L.tp = top ? C.tc : pair(stage_row(kn, kRowQt + rj));
+            L.rip = mkf2(rcy, eR ? ld(qr + o + dipB) : Rj[xi + 2]);
+            L.rjp = pair(stage_row(k, kRowQr + rjp));
+            const float* Rpj = stage_row(kn, kRowQr + rj);
+            L.rp = pair(Rpj);
+            L.rpim = mkf2(eL ? ld(qr + o + P + dimA) : Rpj[xi - 1], f2x(L.rp));
+            L.rpjm = pair(stage_row(kn, kRowQr + rjm));
+            L.zip = mkf2(zcy, eR ? ld(qz + o + dipB) : Zj[xi + 2]);
+            L.zim = mkf2(eL ? ld(qz + o + dimA) : Zj[xi - 1], zcx);
+            L.zjp = pair(Zjp);
+            L.zjm = pair(stage_row(k, kRowQz + rjm));
+            L.zjpim = mkf2(eL ? ld(qz + o + djp + dimA) : Zjp[xi - 1], f2x(L.zjp));
+            L.zp = top ? C.zc : pair(stage_row(kn, kRowQz + rj));
+            L.pc = pair(Pj);
+            L.pjm = pair(stage_row(k, kRowPr + rjm));
+            L.pim = mkf2(eL ? ld(pr + o + dimA) : Pj[xi - 1], f2x(L.pc));
+            L.old_t = a.use_ru ? pair(stage_row(k, kRowRu + ty)) : ZERO;
+            L.old_r = (a.use_ru && k >= 1) ? pair(stage_row(k, kRowRu + 4 + ty)) : ZERO;
+            L.old_z = (a.use_ru && !top) ? pair(stage_row(k, kRowRu + 8 + ty)) : ZERO;
+            march_level(d, c, a, K, k, o, C, L);
+        }
+        // every thread is done with plane k: its stage takes plane k + kTmaStages
+        if (__syncthreads_or(fail)) {
+            for (int p = pend; p <= issued; ++p) mbar_wait(bar_of(p), parity(p), kTmaDrainNs);
+            if (tx == 0 && ty == 0) {
+                StepState* st = const_cast<StepState*>(a.st);
+                atomicExch(&st->errorcode, 3001);
+                atomicExch(&st->halt, 1);
+            }
+            return;
+        }
+        const int pn = k + kTmaStages;
+        if (pn <= k1) { issue(pn); issued = pn; }
+    }
+}
 
 // --------------------------------------------------------------------------
 // Radial implicit solves, one thread per (z, theta) column and component
@@ -659,7 +844,17 @@ void launch_momentum(cudaStream_t s, int mode, const Dims& d, const CoefT<T>& c,
             const dim3 pblk(32, 4, 1);
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y,
                           (d.nr + kMomChunk - 1) / kMomChunk);
-            momentum_march_x2_kernel<<<pg, pblk, 0, s>>>(d, c, a);
+            if (f.tma) {
+                static bool attr = false;
+                if (!attr) {
+                    cudaFuncSetAttribute(momentum_march_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kTmaSmem);
+                    attr = true;
+                }
+                momentum_march_tma_kernel<<<pg, pblk, kTmaSmem, s>>>(d, c, a, *f.tma);
+            } else {
+                momentum_march_x2_kernel<<<pg, pblk, 0, s>>>(d, c, a);
+            }
         } else {
             const dim3 pblk(32, 4, 1);
             const dim3 pg((d.nt / 2 + pblk.x - 1) / pblk.x, (d.nz + pblk.y - 1) / pblk.y, d.nr);

@@ -5,11 +5,19 @@
 // both.
 #pragma once
 
+#include <cuda.h>   // CUtensorMap
+
 #include "tc_dev.h"
 
 namespace tcgb {
 
 enum { MODE_FUSED = 0, MODE_EXPLICIT = 1, MODE_IMPLICIT = 2 };
+
+// TMA descriptors of the mixed path's march inputs (FP32 arrays [k][j][i],
+// box of 72 x 1 x 1 elements), made once per handle.
+struct MarchMaps {
+    CUtensorMap qt, qr, qz, pr, ru1, ru2, ru3;
+};
 
 template <typename T>
 struct FieldsT {
@@ -38,6 +46,9 @@ struct FieldsT {
     const float2 *pl_ff, *pdi_ff, *pu_ff;
     float4* ws;
     int ptri_ff;
+    // host pointer to the handle's march descriptors (mixed path, single
+    // runs; null: the march loads through the read-only cache instead)
+    const MarchMaps* tma;
 };
 
 template <typename T>

@@ -96,6 +96,40 @@ def test_mixed_twenty_steps_vs_fp64(gpu_lib, oracle, case, precision):
     g.close()
 
 
+@pytest.mark.parametrize("case", [
+    dict(nthm=64, nzm=64, nrm=40, istr=6, str=3.0),                    # one theta tile: both periodic edges
+    dict(nthm=192, nzm=30, nrm=37, istr=4, str=2.0, romeg=0.1,          # 3 tiles, z and r not multiples of
+         sizepert=0.1, omegapert=0.5, dtmin=2e-4, dtmax=2e-4),           # the tile, rotating, oscillating wall
+    dict(nthm=96, nzm=20, nrm=17, minstrt=2, minstrz=1, multmin=2),      # partial theta tile, patterned slip
+], ids=["64x64x40", "192x30x37-rot", "96x20x17-slip"])
+def test_tma_march_equals_cached_march(gpu_lib, case):
+    """The TMA-staged march and the march that loads through the read-only
+    cache run the same arithmetic on the same values: identical bits after
+    several steps (all three RK substeps, the wall rows and the edges)."""
+    bou = make_bou(**case)
+    st = ini.couette_noise(bou, seed=21, amp=0.05)
+    out = []
+    for tma in (True, False):
+        g = tc.TaylorCouette(bou, precision="mixed")
+        g.use_tma(tma)
+        g.set_state(*st)
+        code, n, t, _ = g.run(4, 0, 0.0)
+        assert code == 0
+        out.append(g.get_state())
+        g.close()
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_tma_unavailable_is_reported(gpu_lib):
+    g = tc.TaylorCouette(make_bou(nthm=30, nzm=16, nrm=8), precision="mixed")
+    with pytest.raises(tc.TCError) as e:
+        g.use_tma(True)
+    assert e.value.code == 2019
+    g.use_tma(False)
+    g.close()
+
+
 def test_mixed_state_round_trip_is_fp32(gpu_lib):
     bou = make_bou(nthm=24, nzm=18, nrm=10)
     st = ini.couette_noise(bou, seed=3)
