@@ -459,7 +459,8 @@ class TaylorCouette:
         return rc, n.value, t.value, d.value
 
     def use_tma(self, enable: bool = True):
-        """Mixed path: TMA-staged momentum march (default where the grid allows) or not."""
+        """Mixed path: the TMA-staged momentum march (True) or the march that
+        loads through the read-only cache (False, the default)."""
         self._ck(self.L.tc_use_tma(self.h, 1 if enable else 0))
 
     # per-routine entry points (parity bisection)

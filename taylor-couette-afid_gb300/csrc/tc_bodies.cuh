@@ -716,14 +716,115 @@ __device__ __forceinline__ MarchK march_consts(const Dims& d, const MomArgs<floa
     return K;
 }
 
+// The coefficients march_level reads at level k (the grid metrics of
+// CreateGrid.F90 in FP32, and the substep's pressure-gradient products),
+// gathered so that a kernel can stage a chunk's table in shared memory.
+struct alignas(16) MarchCoef {
+    float usrc, usrcp, udxt_m, udxtq_m, q_usrm, q_udx2rm, h_udx1vis1, udxt_c;
+    float udxtq_c, q_udx2c, udx1vis2, q_rc_romeg, ap1j, ac1j, am1j, ap2je;
+    float ac2je, am2je, ap3j, ac3j, am3j, cf_t, cf_r, pad;
+};
+constexpr int kMarchCoefN = 24;   // floats of a MarchCoef
+
+// Coefficient q (MarchCoef order) of level k, from global memory.
+__device__ __forceinline__ float march_coef_entry(const CoefT<float>& c, const MomArgs<float>& a, int nrr, int k,
+                                                  int q) {
+    switch (q) {
+        case 0: return ld(c.usrc + k);
+        case 1: return ld(c.usrc + k + 1);
+        case 2: return ld(c.udxt_m + k);
+        case 3: return ld(c.udxtq_m + k);
+        case 4: return ld(c.q_usrm + k);
+        case 5: return ld(c.q_udx2rm + k);
+        case 6: return ld(c.h_udx1vis1 + k);
+        case 7: return ld(c.udxt_c + k);
+        case 8: return ld(c.udxtq_c + k);
+        case 9: return ld(c.q_udx2c + k);
+        case 10: return ld(c.udx1vis2 + k);
+        case 11: return ld(c.q_rc_romeg + k);
+        case 12: return ld(c.ap1j + k);
+        case 13: return ld(c.ac1j + k);
+        case 14: return ld(c.am1j + k);
+        case 15: return ld(c.ap2je + k);
+        case 16: return ld(c.ac2je + k);
+        case 17: return ld(c.am2je + k);
+        case 18: return ld(c.ap3j + k);
+        case 19: return ld(c.ac3j + k);
+        case 20: return ld(c.am3j + k);
+        case 21: return ld(a.cf + k);
+        case 22: return ld(a.cf + nrr + k);
+        default: return 0.0f;
+    }
+}
+
+// Sources of march_level's coefficients: read from global memory where they
+// are used (the cached march; loading them all up front would cost
+// registers), or from a MarchCoef record (the TMA march's shared table).
+struct MarchCoefGlobal {
+    const CoefT<float>& c;
+    const MomArgs<float>& a;
+    int nrr, k;
+    __device__ __forceinline__ float usrc() const { return ld(c.usrc + k); }
+    __device__ __forceinline__ float usrcp() const { return ld(c.usrc + k + 1); }
+    __device__ __forceinline__ float udxt_m() const { return ld(c.udxt_m + k); }
+    __device__ __forceinline__ float udxtq_m() const { return ld(c.udxtq_m + k); }
+    __device__ __forceinline__ float q_usrm() const { return ld(c.q_usrm + k); }
+    __device__ __forceinline__ float q_udx2rm() const { return ld(c.q_udx2rm + k); }
+    __device__ __forceinline__ float h_udx1vis1() const { return ld(c.h_udx1vis1 + k); }
+    __device__ __forceinline__ float udxt_c() const { return ld(c.udxt_c + k); }
+    __device__ __forceinline__ float udxtq_c() const { return ld(c.udxtq_c + k); }
+    __device__ __forceinline__ float q_udx2c() const { return ld(c.q_udx2c + k); }
+    __device__ __forceinline__ float udx1vis2() const { return ld(c.udx1vis2 + k); }
+    __device__ __forceinline__ float q_rc_romeg() const { return ld(c.q_rc_romeg + k); }
+    __device__ __forceinline__ float ap1j() const { return ld(c.ap1j + k); }
+    __device__ __forceinline__ float ac1j() const { return ld(c.ac1j + k); }
+    __device__ __forceinline__ float am1j() const { return ld(c.am1j + k); }
+    __device__ __forceinline__ float ap2je() const { return ld(c.ap2je + k); }
+    __device__ __forceinline__ float ac2je() const { return ld(c.ac2je + k); }
+    __device__ __forceinline__ float am2je() const { return ld(c.am2je + k); }
+    __device__ __forceinline__ float ap3j() const { return ld(c.ap3j + k); }
+    __device__ __forceinline__ float ac3j() const { return ld(c.ac3j + k); }
+    __device__ __forceinline__ float am3j() const { return ld(c.am3j + k); }
+    __device__ __forceinline__ float cf_t() const { return ld(a.cf + k); }
+    __device__ __forceinline__ float cf_r() const { return ld(a.cf + nrr + k); }
+};
+struct MarchCoefTable {
+    const MarchCoef& q;
+    __device__ __forceinline__ float usrc() const { return q.usrc; }
+    __device__ __forceinline__ float usrcp() const { return q.usrcp; }
+    __device__ __forceinline__ float udxt_m() const { return q.udxt_m; }
+    __device__ __forceinline__ float udxtq_m() const { return q.udxtq_m; }
+    __device__ __forceinline__ float q_usrm() const { return q.q_usrm; }
+    __device__ __forceinline__ float q_udx2rm() const { return q.q_udx2rm; }
+    __device__ __forceinline__ float h_udx1vis1() const { return q.h_udx1vis1; }
+    __device__ __forceinline__ float udxt_c() const { return q.udxt_c; }
+    __device__ __forceinline__ float udxtq_c() const { return q.udxtq_c; }
+    __device__ __forceinline__ float q_udx2c() const { return q.q_udx2c; }
+    __device__ __forceinline__ float udx1vis2() const { return q.udx1vis2; }
+    __device__ __forceinline__ float q_rc_romeg() const { return q.q_rc_romeg; }
+    __device__ __forceinline__ float ap1j() const { return q.ap1j; }
+    __device__ __forceinline__ float ac1j() const { return q.ac1j; }
+    __device__ __forceinline__ float am1j() const { return q.am1j; }
+    __device__ __forceinline__ float ap2je() const { return q.ap2je; }
+    __device__ __forceinline__ float ac2je() const { return q.ac2je; }
+    __device__ __forceinline__ float am2je() const { return q.am2je; }
+    __device__ __forceinline__ float ap3j() const { return q.ap3j; }
+    __device__ __forceinline__ float ac3j() const { return q.ac3j; }
+    __device__ __forceinline__ float am3j() const { return q.am3j; }
+    __device__ __forceinline__ float cf_t() const { return q.cf_t; }
+    __device__ __forceinline__ float cf_r() const { return q.cf_r; }
+};
+
 // The arithmetic of one level k of the march (explicit terms and the
 // implicit right-hand sides of the three components) from the carried
 // values and the level's loads; stores rhs and ru at offset o, then moves
 // the carry up one level.  Shared by the global-load march
 // (momentum_column_x2) and the TMA-staged one (momentum_march_tma_kernel),
 // so both compute the same bits.
+template <typename CQ>
 __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
-                                            const MarchK& K, int k, size_t o, MarchCarry& C, const MarchIn& L) {
+                                            const MarchK& K, const CQ& Q, int k, size_t o, MarchCarry& C,
+                                            const MarchIn& L) {
     const int nr = d.nr, nrr = nr + 1;
     const bool top = k == nr - 1;
     const int kp = k + 1;
@@ -742,25 +843,25 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     const F2 pc = L.pc, pjm = L.pjm, pim = L.pim;
     const F2 old_t = L.old_t, old_r = L.old_r, old_z = L.old_z;
     (void)ZERO; (void)nrr;
-    const F2 USRC = bc2(ld(c.usrc + k)), USRCP = bc2(ld(c.usrc + kp));
+    const F2 USRC = bc2(Q.usrc()), USRCP = bc2(Q.usrcp());
     const F2 tz_sw = (zc + zim) * (tc + tjm);
     const F2 qre = fma2(rp, USRCP, rc * USRC);
     // ---- ExplicitTermsQT
     F2 ht;
     {
-        const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+        const F2 UDXT = bc2(Q.udxt_m()), UDXTQ = bc2(Q.udxtq_m());
         const F2 sth = tip + tim;
         const F2 x11 = (tip - tim) * fma2(TWO, tc, sth);          // (tip+tc)^2 - (tc+tim)^2
         const F2 rp2 = rp + rpim, rc2 = rc + rim;
         const F2 up = rp2 * (tp + tc);
         const F2 qrs = fma2(rp2, USRCP, rc2 * USRC);
-        const F2 h12n = tc * bc2(ld(c.q_usrm + k)) * qrs;
+        const F2 h12n = tc * bc2(Q.q_usrm()) * qrs;
         U12 = up;
-        F2 s = fma2(up - U12lo, bc2(ld(c.q_udx2rm + k)), h12n);  // h12d + h12n
+        F2 s = fma2(up - U12lo, bc2(Q.q_udx2rm()), h12n);  // h12d + h12n
         s = fma2(x11, UDXT, s);                                   // + h11
         s = fma2((zjp + zjpim) * (tjp + tc) - tz_sw, UDXZ, s);    // + h13
         const F2 qrw = fma2(rpim, USRCP, rim * USRC);
-        F2 r = (qre - qrw) * bc2(ld(c.h_udx1vis1 + k));           // d11qre
+        F2 r = (qre - qrw) * bc2(Q.h_udx1vis1());           // d11qre
         r = fma2(fma2(MTWO, tc, tjp + tjm), UDXZQ, r);            // + d22qt
         r = fma2(fma2(MTWO, tc, sth), UDXTQ, r);                  // + d11qt
         ht = fma2(qrs, NQROMEG, r - s);                           // + Coriolis
@@ -770,16 +871,16 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     {
         const F2 rup = qre * (rp + rc);
         if (k >= 1) {
-            const F2 UDXT = bc2(ld(c.udxt_c + k)), UDXTQ = bc2(ld(c.udxtq_c + k));
+            const F2 UDXT = bc2(Q.udxt_c()), UDXTQ = bc2(Q.udxtq_c());
             const F2 sa = tip + tmip, sb = tc + tm, s4 = sa + sb;
             const F2 aa = s4 * QUARTER;
             F2 s = (sa * (rip + rc) - U12lo) * UDXT;                  // h21
-            s = fma2(rup - Gup, bc2(ld(c.q_udx2c + k)), s);           // + h22
+            s = fma2(rup - Gup, bc2(Q.q_udx2c()), s);           // + h22
             s = fma2((zjp + zmjp) * (rjp + rc) - Uzlo, UDXZ, s);      // + h23
-            F2 r = fma2(aa, aa, (sb - sa) * bc2(ld(c.udx1vis2 + k))); // h11n + d11qre
+            F2 r = fma2(aa, aa, (sb - sa) * bc2(Q.udx1vis2())); // h11n + d11qre
             r = fma2(fma2(MTWO, rc, rip + rim), UDXTQ, r);            // + d11qr
             r = fma2(fma2(MTWO, rc, rjp + rjm), UDXZQ, r);            // + d22qr
-            r = fma2(s4, bc2(ld(c.q_rc_romeg + k)), r);               // + Coriolis
+            r = fma2(s4, bc2(Q.q_rc_romeg()), r);               // + Coriolis
             hr = r - s;
         }
         Gup = rup;
@@ -787,9 +888,9 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     // ---- ExplicitTermsQZ
     F2 hz;
     {
-        const F2 UDXT = bc2(ld(c.udxt_m + k)), UDXTQ = bc2(ld(c.udxtq_m + k));
+        const F2 UDXT = bc2(Q.udxt_m()), UDXTQ = bc2(Q.udxtq_m());
         const F2 upz = (rp + rpjm) * (zp + zc);
-        F2 s = (upz - Uzlo) * bc2(ld(c.q_udx2rm + k));                // h32
+        F2 s = (upz - Uzlo) * bc2(Q.q_udx2rm());                // h32
         Uz = upz;
         s = fma2((tip + tjmip) * (zip + zc) - tz_sw, UDXT, s);        // + h31
         const F2 sjz = zjp + zjm;
@@ -802,24 +903,24 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     {
         F2 d33;
         if (k == 0) {
-            const F2 acc = fma2(bc2(ld(c.ac1j)), FIC, bc2(a.ac1j_fs0) * (bc2(1.0f) - FIC));
-            const F2 amm = fma2(bc2(ld(c.am1j)), FIC, bc2(a.am1j_fs0) * (bc2(1.0f) - FIC));
-            d33 = fma2(tp, bc2(ld(c.ap1j)), fma2(tc, acc, bc2(a.virotint + step_vinner<float>(a.st)) * amm));
+            const F2 acc = fma2(bc2(Q.ac1j()), FIC, bc2(a.ac1j_fs0) * (bc2(1.0f) - FIC));
+            const F2 amm = fma2(bc2(Q.am1j()), FIC, bc2(a.am1j_fs0) * (bc2(1.0f) - FIC));
+            d33 = fma2(tp, bc2(Q.ap1j()), fma2(tc, acc, bc2(a.virotint + step_vinner<float>(a.st)) * amm));
         } else if (top) {
-            const float app = ld(c.ap1j + k) * 1.0f + a.ap1j_fs1 * 0.0f;
-            const float acc = ld(c.ac1j + k) * 1.0f + a.ac1j_fs1 * 0.0f;
-            d33 = fma2(tc, bc2(acc), fma2(tm, bc2(ld(c.am1j + k)), bc2(a.virotext * app)));
+            const float app = Q.ap1j() * 1.0f + a.ap1j_fs1 * 0.0f;
+            const float acc = Q.ac1j() * 1.0f + a.ac1j_fs1 * 0.0f;
+            d33 = fma2(tc, bc2(acc), fma2(tm, bc2(Q.am1j()), bc2(a.virotext * app)));
         } else {
-            d33 = fma2(tp, bc2(ld(c.ap1j + k)), fma2(tc, bc2(ld(c.ac1j + k)), tm * bc2(ld(c.am1j + k))));
+            d33 = fma2(tp, bc2(Q.ap1j()), fma2(tc, bc2(Q.ac1j()), tm * bc2(Q.am1j())));
         }
-        const F2 rhs = fma2(pc - pim, bc2(-ld(a.cf + k)), fma2(ALREDT, d33, fma2(RODT, old_t, GADT * ht)));
+        const F2 rhs = fma2(pc - pim, bc2(-Q.cf_t()), fma2(ALREDT, d33, fma2(RODT, old_t, GADT * ht)));
         st_f2(a.rhs_t + o, rhs);
         st_f2(a.ru1 + o, ht);
     }
     // ---- ImplicitAndUpdateQR, faces 1..nr-1
     if (k >= 1) {
-        const F2 d33 = fma2(rp, bc2(ld(c.ap2je + k)), fma2(rc, bc2(ld(c.ac2je + k)), rm * bc2(ld(c.am2je + k))));
-        const F2 rhs = fma2(pc - prm, bc2(-ld(a.cf + nrr + k)), fma2(ALREDT, d33, fma2(RODT, old_r, GADT * hr)));
+        const F2 d33 = fma2(rp, bc2(Q.ap2je()), fma2(rc, bc2(Q.ac2je()), rm * bc2(Q.am2je())));
+        const F2 rhs = fma2(pc - prm, bc2(-Q.cf_r()), fma2(ALREDT, d33, fma2(RODT, old_r, GADT * hr)));
         st_f2(a.rhs_r + o, rhs);
         st_f2(a.ru2 + o, hr);
     }
@@ -827,15 +928,15 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     {
         F2 d33;
         if (k == 0) {
-            const F2 acc = fma2(bc2(ld(c.ac3j)), FIC, bc2(a.ac3j_fs0) * (bc2(1.0f) - FIC));
-            const F2 amm = fma2(bc2(ld(c.am3j)), FIC, bc2(a.am3j_fs0) * (bc2(1.0f) - FIC));
-            d33 = fma2(zp, bc2(ld(c.ap3j)), fma2(zc, acc, zc * amm));
+            const F2 acc = fma2(bc2(Q.ac3j()), FIC, bc2(a.ac3j_fs0) * (bc2(1.0f) - FIC));
+            const F2 amm = fma2(bc2(Q.am3j()), FIC, bc2(a.am3j_fs0) * (bc2(1.0f) - FIC));
+            d33 = fma2(zp, bc2(Q.ap3j()), fma2(zc, acc, zc * amm));
         } else if (top) {
-            const float app = ld(c.ap3j + k) * 1.0f + a.ap3j_fs1 * 0.0f;
-            const float acc = ld(c.ac3j + k) * 1.0f + a.ac3j_fs1 * 0.0f;
-            d33 = fma2(zc, bc2(app), fma2(zc, bc2(acc), zm * bc2(ld(c.am3j + k))));
+            const float app = Q.ap3j() * 1.0f + a.ap3j_fs1 * 0.0f;
+            const float acc = Q.ac3j() * 1.0f + a.ac3j_fs1 * 0.0f;
+            d33 = fma2(zc, bc2(app), fma2(zc, bc2(acc), zm * bc2(Q.am3j())));
         } else {
-            d33 = fma2(zp, bc2(ld(c.ap3j + k)), fma2(zc, bc2(ld(c.ac3j + k)), zm * bc2(ld(c.am3j + k))));
+            d33 = fma2(zp, bc2(Q.ap3j()), fma2(zc, bc2(Q.ac3j()), zm * bc2(Q.am3j())));
         }
         // outer wall: ru3(nrm) already replaced by qcap(nrm) (ImplicitAndUpdateQZ.F90:86,110)
         const F2 old = top ? hz : old_z;
@@ -925,7 +1026,7 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
         L.old_t = a.use_ru ? ldp_f2(a.ru1 + o) : ZERO;
         L.old_r = (a.use_ru && k >= 1) ? ldp_f2(a.ru2 + o) : ZERO;
         L.old_z = (a.use_ru && !top) ? ldp_f2(a.ru3 + o) : ZERO;
-        march_level(d, c, a, K, k, o, C, L);
+        march_level(d, c, a, K, MarchCoefGlobal{c, a, nr + 1, k}, k, o, C, L);
     }
 }
 

@@ -270,14 +270,14 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// A 3-D descriptor of an FP32 array [nplanes][nz][nt] with a box of one
-// 72-float row (the march's staged rows).
-static bool march_map(CUtensorMap* m, const float* base, int nt, int nz, int nplanes) {
+// A 3-D descriptor of an FP32 array [nplanes][nz][nt] with a box of `rows`
+// z rows of 72 floats (the march's staged rows).
+static bool march_map(CUtensorMap* m, const float* base, int nt, int nz, int nplanes, int rows) {
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)nt, (cuuint64_t)nz, (cuuint64_t)nplanes};
     const cuuint64_t strides[2] = {(cuuint64_t)nt * 4, (cuuint64_t)nt * nz * 4};
-    const cuuint32_t box[3] = {72, 1, 1}, estr[3] = {1, 1, 1};
+    const cuuint32_t box[3] = {72, (cuuint32_t)rows, 1}, estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -290,10 +290,16 @@ static bool make_march_maps(tc_handle* h) {
     if (!h->mixed || d.nt % 4 != 0 || d.nt < 64) return false;
     const FieldsT<float>& f = h->ff;
     MarchMaps& M = h->maps;
-    return march_map(&M.qt, f.qt, d.nt, d.nz, d.nr) && march_map(&M.qr, f.qr, d.nt, d.nz, d.nr + 1) &&
-           march_map(&M.qz, f.qz, d.nt, d.nz, d.nr) && march_map(&M.pr, f.prf, d.nt, d.nz, d.nr) &&
-           march_map(&M.ru1, f.ru1, d.nt, d.nz, d.nr) && march_map(&M.ru2, f.ru2, d.nt, d.nz, d.nr + 1) &&
-           march_map(&M.ru3, f.ru3, d.nt, d.nz, d.nr);
+    const float* q[4] = {f.qt, f.qr, f.qz, f.prf};
+    const int nq[4] = {d.nr, d.nr + 1, d.nr, d.nr};
+    const float* ru[3] = {f.ru1, f.ru2, f.ru3};
+    const int nru[3] = {d.nr, d.nr + 1, d.nr};
+    for (int c = 0; c < 4; ++c)
+        if (!march_map(&M.q6[c], q[c], d.nt, d.nz, nq[c], 6) || !march_map(&M.q1[c], q[c], d.nt, d.nz, nq[c], 1))
+            return false;
+    for (int c = 0; c < 3; ++c)
+        if (!march_map(&M.ru[c], ru[c], d.nt, d.nz, nru[c], 4)) return false;
+    return true;
 }
 
 int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
@@ -435,8 +441,7 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     h->ff.ptri_ff = h->ptri_ff;
     h->ff.tma = nullptr;
     h->fd.tma = nullptr;
-    h->maps_ok = make_march_maps(h);
-    if (h->maps_ok) h->ff.tma = &h->maps;
+    h->maps_ok = make_march_maps(h);   // built, but the cached march is the default (tc_use_tma)
     if (h->ptri_ff) {
         float2* pu = nullptr;
         ce = dalloc(h, &pu, (size_t)nr);

@@ -162,33 +162,55 @@ __global__ void __launch_bounds__(128, 4) momentum_march_x2_kernel(Dims d, CoefT
 // The FP32 march with its input planes staged in shared memory by the TMA
 // unit.  A block of 32 x 4 threads owns a 64 (theta) x 4 (z) tile of
 // columns and marches kMomChunk radial levels; each radial plane p of its
-// inputs is one stage: for qt, qr, qz the rows j0-1 .. j0+4 of the tile, for
-// the FP32 pressure j0-1 .. j0+3 and for the RK memory j0 .. j0+3, every row
-// theta i0-4 .. i0+67 (one 72-float TMA box a row, z wrapped periodically
-// when the row is chosen; the theta halo outside 0..nthm-1 reads as zero and
-// the two edge columns of the domain take their periodic neighbour from
-// global memory instead).  kTmaStages planes are in flight: while level k
-// reads planes k and k+1, planes k+2 .. k+kTmaStages-1 load.  The
-// arithmetic is march_level, as in momentum_march_x2_kernel.  Every wait on
-// an mbarrier is bounded (kTmaWaitNs); a wait that gives up makes the block
-// wait for its loads still in flight (bounded again), raise error 3001 with
-// the step halted, and return.
+// inputs is one pipeline stage: for qt, qr, qz and the FP32 pressure the z
+// rows j0-1 .. j0+4 of the tile, for the RK memory j0 .. j0+3, every row
+// theta i0-4 .. i0+67 (72 floats).  A tile whose rows do not wrap in z takes
+// each array's rows in one box (7 copies a plane); a tile at the periodic z
+// ends takes the q rows one at a time with z wrapped (27 copies).  The theta
+// halo outside 0..nthm-1 reads as zero: the two edge columns of the domain
+// take their periodic neighbour from global memory instead (predicated
+// loads, no branch).  The per-level coefficients of the chunk are staged
+// in shared memory once.
+//
+// Pipeline: warp 0 is the producer; kTmaStages planes are in flight (while
+// level k reads planes k and k+1, planes up to k+kTmaStages-1 load).  Each
+// stage has a "full" barrier (the producer posts the byte count, the TMA
+// unit completes it) and an "empty" barrier that every warp arrives on when
+// it is done with the plane; the producer reuses a stage only after all four
+// warps released it, so no block-wide barrier stands in the march.
+// The arithmetic is march_level, as in momentum_march_x2_kernel, so both
+// give the same bits.  Every wait is bounded (kTmaWaitNs); one that runs out
+// sets the block's abort flag, the others give up on seeing it, and the
+// block waits for its copies still in flight (bounded again), raises 3001
+// with the step halted and returns.
 // --------------------------------------------------------------------------
 
-constexpr int kTmaW = 72;                  // floats of one staged row
-constexpr int kTmaRowB = 384;              // bytes of a row slot (128-byte aligned)
+// v if !p, else the read-only load *ptr: a predicated load, so that the few
+// edge threads that need a global value cost the others no branch.
+__device__ __forceinline__ float ld_pred(bool p, const float* ptr, float v) {
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.f32 %0, [%1];\n\t}"
+        : "+f"(v)
+        : "l"(ptr), "r"((int)p));
+    return v;
+}
+
+constexpr int kTmaW = 72;                          // floats of one staged row
+constexpr int kTmaRowD = kTmaW * 4;                // bytes of a row inside a multi-row box
+constexpr int kTmaRowP = 384;                      // bytes of a row slot of a single-row box (128-aligned)
+constexpr int kTmaQB = 6 * kTmaRowP;               // one q array's rows in a stage
+constexpr int kTmaRuB = 4 * kTmaRowD;              // one RK-memory array's rows (1152 = 9 x 128)
+constexpr int kTmaStageB = 4 * kTmaQB + 3 * kTmaRuB;
 constexpr int kTmaStages = 4;
-constexpr int kRowQt = 0, kRowQr = 6, kRowQz = 12, kRowPr = 18, kRowRu = 23;
-constexpr int kRowsNoRu = 23, kRowsRu = 35;
-constexpr int kTmaStageB = kRowsRu * kTmaRowB;
 constexpr size_t kTmaSmem = (size_t)kTmaStages * kTmaStageB + 128;
 constexpr unsigned long long kTmaWaitNs = 1000000000ull;       // 1 s
-constexpr unsigned long long kTmaDrainNs = 100000000ull;       // 0.1 s per plane
+constexpr unsigned long long kTmaDrainNs = 100000000ull;       // 0.1 s a plane
 
 __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, CoefT<float> c, MomArgs<float> a,
                                                                     const __grid_constant__ MarchMaps maps) {
     if (a.st->halt) return;
-    __shared__ __align__(8) unsigned long long bars[kTmaStages];
+    __shared__ __align__(8) unsigned long long full_bar[kTmaStages], empty_bar[kTmaStages];
+    __shared__ int abort_flag;
+    __shared__ MarchCoef ctab[kMomChunk];            // the chunk's per-level coefficients
     extern __shared__ unsigned char tma_dyn[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(tma_dyn) + 127) & ~(size_t)127);
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -198,57 +220,62 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
     const int k0 = blockIdx.z * kMomChunk, k1 = min(k0 + kMomChunk, nr);
     const int i = i0 + 2 * tx, j = j0 + ty;
     const bool active = i < nt && j < nz;
-    const int nrows = a.use_ru ? kRowsRu : kRowsNoRu;
-    const unsigned sbase = smem_u32(sm), bbase = smem_u32(bars);
+    const bool zwrap = j0 == 0 || j0 + 5 > nz;       // q rows j0-1 .. j0+4 leave 0..nzm-1
+    const int rs = zwrap ? kTmaRowP : kTmaRowD;       // row stride of the q rows in a stage
+    const unsigned sbase = smem_u32(sm);
+    volatile int* abort = &abort_flag;
 
     if (tx == 0 && ty == 0) {
-        for (int q = 0; q < kTmaStages; ++q) mbar_init(bbase + 8 * q, 1);
+        for (int q = 0; q < kTmaStages; ++q) {
+            mbar_init(smem_u32(&full_bar[q]), 1);
+            mbar_init(smem_u32(&empty_bar[q]), 4);
+        }
+        abort_flag = 0;
         mbar_init_fence();
     }
+    for (int e = ty * 32 + tx; e < (k1 - k0) * kMarchCoefN; e += 128)
+        reinterpret_cast<float*>(ctab)[e] = march_coef_entry(c, a, nr + 1, k0 + e / kMarchCoefN, e % kMarchCoefN);
     __syncthreads();
 
-    // plane p of the chunk into stage (p - k0) % kTmaStages; warp 0 posts
-    // the byte count, then each lane issues its rows
-    auto issue = [&](int p) {
-        if (ty != 0) return;
-        const int q = (p - k0) % kTmaStages;
-        const unsigned bar = bbase + 8 * q, dst = sbase + q * kTmaStageB;
-        if (tx == 0) mbar_arrive_expect_tx(bar, (unsigned)(nrows * kTmaW * 4));
-        __syncwarp();
-        for (int r = tx; r < nrows; r += 32) {
-            const CUtensorMap* m;
-            int dz;
-            if (r < kRowQr) { m = &maps.qt; dz = r - kRowQt - 1; }
-            else if (r < kRowQz) { m = &maps.qr; dz = r - kRowQr - 1; }
-            else if (r < kRowPr) { m = &maps.qz; dz = r - kRowQz - 1; }
-            else if (r < kRowRu) { m = &maps.pr; dz = r - kRowPr - 1; }
-            else {
-                const int u = r - kRowRu;
-                m = u < 4 ? &maps.ru1 : (u < 8 ? &maps.ru2 : &maps.ru3);
-                dz = u & 3;
-            }
-            const int zr = ((j0 + dz) % nz + nz) % nz;
-            tma_load_3d(dst + r * kTmaRowB, m, i0 - 4, zr, p, bar);
-        }
-    };
+    auto slot = [&](int p) { return (p - k0) & (kTmaStages - 1); };
+    auto par = [&](int p) { return (unsigned)(((p - k0) / kTmaStages) & 1); };
+    // producer (warp 0): plane p into its stage, once the stage's previous
+    // plane has been released by all warps
     int issued = k0 - 1;
-    for (int p = k0; p <= k1 && p < k0 + kTmaStages; ++p) { issue(p); issued = p; }
-
-    auto stage_row = [&](int p, int row) -> const float* {
-        return reinterpret_cast<const float*>(sm + ((p - k0) % kTmaStages) * kTmaStageB + row * kTmaRowB);
+    auto produce = [&](int p) -> bool {
+        const int q = slot(p);
+        bool free = true;
+        if (p >= k0 + kTmaStages) free = mbar_wait_or_abort(smem_u32(&empty_bar[q]), par(p) ^ 1, kTmaWaitNs, abort);
+        if (!__all_sync(0xffffffffu, free)) return false;     // the whole warp agrees (a failed wait set abort)
+        const unsigned fb = smem_u32(&full_bar[q]), dst = sbase + q * kTmaStageB;
+        const unsigned bytes = (unsigned)((4 * 6 + (a.use_ru ? 3 * 4 : 0)) * kTmaRowD);
+        if (tx == 0) mbar_arrive_expect_tx(fb, bytes);
+        __syncwarp();
+        if (!zwrap) {
+            if (tx < 4) tma_load_3d(dst + tx * kTmaQB, &maps.q6[tx], i0 - 4, j0 - 1, p, fb);
+        } else if (tx < 24) {
+            const int f = tx / 6, r = tx - 6 * f;
+            const int zr = ((j0 - 1 + r) % nz + nz) % nz;
+            tma_load_3d(dst + f * kTmaQB + r * kTmaRowP, &maps.q1[f], i0 - 4, zr, p, fb);
+        }
+        if (a.use_ru && tx >= 24 && tx < 27)
+            tma_load_3d(dst + 4 * kTmaQB + (tx - 24) * kTmaRuB, &maps.ru[tx - 24], i0 - 4, j0, p, fb);
+        issued = p;
+        return true;
     };
-    auto parity = [&](int p) -> unsigned { return (unsigned)(((p - k0) / kTmaStages) & 1); };
-    auto bar_of = [&](int p) -> unsigned { return bbase + 8 * ((p - k0) % kTmaStages); };
-    const int xi = 4 + 2 * tx;                       // the pair's first cell in a staged row
-    auto pair = [&](const float* row) -> F2 {
-        const float2 v = *reinterpret_cast<const float2*>(row + xi);
+    bool ok = true;
+    if (ty == 0)
+        for (int p = k0; p <= k1 && p < k0 + kTmaStages && ok; ++p) ok = produce(p);
+
+    const int xb = (4 + 2 * tx) * 4;                 // the pair's byte offset in a staged row
+    auto pair = [&](const unsigned char* row) -> F2 {
+        const float2 v = *reinterpret_cast<const float2*>(row + xb);
         return mkf2(v.x, v.y);
     };
-    // rows of this thread: z rows j-1, j, j+1 of the 6-row fields
-    const int rjm = ty, rj = ty + 1, rjp = ty + 2;
-
-    bool fail = !mbar_wait(bar_of(k0), parity(k0), kTmaWaitNs);
-    int pend = fail ? k0 : k0 + 1;                   // lowest plane not yet consumed
+    auto left = [&](const unsigned char* row) -> float { return *reinterpret_cast<const float*>(row + xb - 4); };
+    auto right = [&](const unsigned char* row) -> float { return *reinterpret_cast<const float*>(row + xb + 8); };
+    // q array f, z row j + dz of this thread, in the stage at base
+    auto qrow = [&](const unsigned char* base, int f, int dz) { return base + f * kTmaQB + (ty + 1 + dz) * rs; };
 
     const bool eL = i == 0, eR = i + 2 == nt;        // the domain's periodic theta edges
     const int dimA = eL ? nt - 1 : -1, dipB = eR ? 2 - nt : 2;
@@ -263,17 +290,20 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
     const float* pr = a.pr;
     size_t o = (size_t)k0 * P + col;
     MarchCarry C;
-    if (active) {
+    if (ok) ok = mbar_wait_or_abort(smem_u32(&full_bar[slot(k0)]), par(k0), kTmaWaitNs, abort);
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok && active) {
+        const unsigned char* S0 = sm + slot(k0) * kTmaStageB;
         const int km0 = k0 > 0 ? k0 - 1 : 0;
         const size_t om = (size_t)km0 * P + col;
-        C.tc = pair(stage_row(k0, kRowQt + rj));
+        C.tc = pair(qrow(S0, 0, 0));
         C.tm = ld_f2(qt + om);
         C.tmip = mkf2(f2y(C.tm), ld(qt + om + dipB));
-        C.rc = pair(stage_row(k0, kRowQr + rj));
-        C.rim = mkf2(eL ? ld(qr + o + dimA) : stage_row(k0, kRowQr + rj)[xi - 1], f2x(C.rc));
-        C.rjm = pair(stage_row(k0, kRowQr + rjm));
+        C.rc = pair(qrow(S0, 1, 0));
+        C.rim = mkf2(ld_pred(eL, qr + o + dimA, left(qrow(S0, 1, 0))), f2x(C.rc));
+        C.rjm = pair(qrow(S0, 1, -1));
         C.rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
-        C.zc = pair(stage_row(k0, kRowQz + rj));
+        C.zc = pair(qrow(S0, 2, 0));
         C.zm = ld_f2(qz + om);
         C.zmjp = ld_f2(qz + om + djp);
         C.prm = k0 > 0 ? ld_f2(pr + om) : ZERO;
@@ -282,63 +312,67 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
         const float usrc = ld(c.usrc + k0), usrcm = k0 > 0 ? ld(c.usrc + k0 - 1) : 0.0f;
         C.Gup = fma2(C.rm, bc2(usrcm), C.rc * bc2(usrc)) * (C.rc + C.rm);
     }
-    for (int k = k0; k < k1; ++k, o += P) {
+    for (int k = k0; k < k1 && ok; ++k, o += P) {
         const int kn = k + 1;
-        if (!fail) {
-            fail = !mbar_wait(bar_of(kn), parity(kn), kTmaWaitNs);
-            if (!fail) pend = kn + 1;
-        }
-        if (active && !fail) {
+        const bool got = mbar_wait_or_abort(smem_u32(&full_bar[slot(kn)]), par(kn), kTmaWaitNs, abort);
+        if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
+        if (active) {
             const bool top = k == nr - 1;
-            const float* Tj = stage_row(k, kRowQt + rj);
-            const float* Tjm = stage_row(k, kRowQt + rjm);
-            const float* Rj = stage_row(k, kRowQr + rj);
-            const float* Zj = stage_row(k, kRowQz + rj);
-            const float* Zjp = stage_row(k, kRowQz + rjp);
-            const float* Pj = stage_row(k, kRowPr + rj);
+            const unsigned char* S = sm + slot(k) * kTmaStageB;     // plane k
+            const unsigned char* N = sm + slot(kn) * kTmaStageB;    // plane k+1
+            const unsigned char* Tj = qrow(S, 0, 0);
+            const unsigned char* Tjm = qrow(S, 0, -1);
+            const unsigned char* Rj = qrow(S, 1, 0);
+            const unsigned char* Zj = qrow(S, 2, 0);
+            const unsigned char* Zjp = qrow(S, 2, 1);
+            const unsigned char* Pj = qrow(S, 3, 0);
+            const unsigned char* Rpj = qrow(N, 1, 0);
+            const unsigned char* RU = S + 4 * kTmaQB + ty * kTmaRowD;
             MarchIn L;
             float tcx, tcy, rcx, rcy, zcx, zcy;
             f2xy(C.tc, tcx, tcy);
             f2xy(C.rc, rcx, rcy);
             f2xy(C.zc, zcx, zcy);
-            L.tip = mkf2(tcy, eR ? ld(qt + o + dipB) : Tj[xi + 2]);
-            L.tim = mkf2(eL ? ld(qt + o + dimA) : Tj[xi - 1], tcx);
-            L.tjp = pair(stage_row(k, kRowQt + rjp));
+            L.tip = mkf2(tcy, ld_pred(eR, qt + o + dipB, right(Tj)));
+            L.tim = mkf2(ld_pred(eL, qt + o + dimA, left(Tj)), tcx);
+            L.tjp = pair(qrow(S, 0, 1));
             L.tjm = pair(Tjm);
-            L.tjmip = mkf2(f2y(L.tjm), eR ? ld(qt + o + djm + dipB) : Tjm[xi + 2]);
-            L.tp = top ? C.tc : pair(stage_row(kn, kRowQt + rj));
-            L.rip = mkf2(rcy, eR ? ld(qr + o + dipB) : Rj[xi + 2]);
-            L.rjp = pair(stage_row(k, kRowQr + rjp));
-            const float* Rpj = stage_row(kn, kRowQr + rj);
+            L.tjmip = mkf2(f2y(L.tjm), ld_pred(eR, qt + o + djm + dipB, right(Tjm)));
+            L.tp = top ? C.tc : pair(qrow(N, 0, 0));
+            L.rip = mkf2(rcy, ld_pred(eR, qr + o + dipB, right(Rj)));
+            L.rjp = pair(qrow(S, 1, 1));
             L.rp = pair(Rpj);
-            L.rpim = mkf2(eL ? ld(qr + o + P + dimA) : Rpj[xi - 1], f2x(L.rp));
-            L.rpjm = pair(stage_row(kn, kRowQr + rjm));
-            L.zip = mkf2(zcy, eR ? ld(qz + o + dipB) : Zj[xi + 2]);
-            L.zim = mkf2(eL ? ld(qz + o + dimA) : Zj[xi - 1], zcx);
+            L.rpim = mkf2(ld_pred(eL, qr + o + P + dimA, left(Rpj)), f2x(L.rp));
+            L.rpjm = pair(qrow(N, 1, -1));
+            L.zip = mkf2(zcy, ld_pred(eR, qz + o + dipB, right(Zj)));
+            L.zim = mkf2(ld_pred(eL, qz + o + dimA, left(Zj)), zcx);
             L.zjp = pair(Zjp);
-            L.zjm = pair(stage_row(k, kRowQz + rjm));
-            L.zjpim = mkf2(eL ? ld(qz + o + djp + dimA) : Zjp[xi - 1], f2x(L.zjp));
-            L.zp = top ? C.zc : pair(stage_row(kn, kRowQz + rj));
+            L.zjm = pair(qrow(S, 2, -1));
+            L.zjpim = mkf2(ld_pred(eL, qz + o + djp + dimA, left(Zjp)), f2x(L.zjp));
+            L.zp = top ? C.zc : pair(qrow(N, 2, 0));
             L.pc = pair(Pj);
-            L.pjm = pair(stage_row(k, kRowPr + rjm));
-            L.pim = mkf2(eL ? ld(pr + o + dimA) : Pj[xi - 1], f2x(L.pc));
-            L.old_t = a.use_ru ? pair(stage_row(k, kRowRu + ty)) : ZERO;
-            L.old_r = (a.use_ru && k >= 1) ? pair(stage_row(k, kRowRu + 4 + ty)) : ZERO;
-            L.old_z = (a.use_ru && !top) ? pair(stage_row(k, kRowRu + 8 + ty)) : ZERO;
-            march_level(d, c, a, K, k, o, C, L);
+            L.pjm = pair(qrow(S, 3, -1));
+            L.pim = mkf2(ld_pred(eL, pr + o + dimA, left(Pj)), f2x(L.pc));
+            L.old_t = a.use_ru ? pair(RU) : ZERO;
+            L.old_r = (a.use_ru && k >= 1) ? pair(RU + kTmaRuB) : ZERO;
+            L.old_z = (a.use_ru && !top) ? pair(RU + 2 * kTmaRuB) : ZERO;
+            (void)rcx;
+            march_level(d, c, a, K, MarchCoefTable{ctab[k - k0]}, k, o, C, L);
         }
-        // every thread is done with plane k: its stage takes plane k + kTmaStages
-        if (__syncthreads_or(fail)) {
-            for (int p = pend; p <= issued; ++p) mbar_wait(bar_of(p), parity(p), kTmaDrainNs);
-            if (tx == 0 && ty == 0) {
-                StepState* st = const_cast<StepState*>(a.st);
-                atomicExch(&st->errorcode, 3001);
-                atomicExch(&st->halt, 1);
-            }
-            return;
-        }
+        // this warp is done with plane k
+        __syncwarp();
+        if (tx == 0) mbar_arrive(smem_u32(&empty_bar[slot(k)]));
         const int pn = k + kTmaStages;
-        if (pn <= k1) { issue(pn); issued = pn; }
+        if (ty == 0 && pn <= k1 && !produce(pn)) { ok = false; break; }
+    }
+    if (__syncthreads_or(*abort)) {
+        if (tx == 0 && ty == 0) {
+            for (int p = max(issued - kTmaStages + 1, k0); p <= issued; ++p)
+                mbar_wait(smem_u32(&full_bar[slot(p)]), par(p), kTmaDrainNs);
+            StepState* st = const_cast<StepState*>(a.st);
+            atomicExch(&st->errorcode, 3001);
+            atomicExch(&st->halt, 1);
+        }
     }
 }
 

@@ -13,10 +13,12 @@ namespace tcgb {
 
 enum { MODE_FUSED = 0, MODE_EXPLICIT = 1, MODE_IMPLICIT = 2 };
 
-// TMA descriptors of the mixed path's march inputs (FP32 arrays [k][j][i],
-// box of 72 x 1 x 1 elements), made once per handle.
+// TMA descriptors of the mixed path's march inputs (FP32 arrays [k][j][i]),
+// made once per handle: q6 (qt, qr, qz, pr) with boxes of 72 x 6 x 1
+// elements (theta x z x r), q1 the same arrays with single-row boxes (for
+// the tiles whose z rows wrap), ru the RK memory with 72 x 4 x 1 boxes.
 struct MarchMaps {
-    CUtensorMap qt, qr, qz, pr, ru1, ru2, ru3;
+    CUtensorMap q6[4], q1[4], ru[3];
 };
 
 template <typename T>

@@ -57,6 +57,28 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigne
     return true;
 }
 
+// Arrive once on the barrier (release: the thread's earlier reads of the
+// buffer the barrier guards are done).
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// mbar_wait that also gives up as soon as *abort is set (by a thread of
+// the block whose own wait ran out); sets *abort when it runs out itself.
+__device__ __forceinline__ bool mbar_wait_or_abort(unsigned bar, unsigned parity, unsigned long long limit_ns,
+                                                   volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = tma_now_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort) return false;
+        if (tma_now_ns() - t0 > limit_ns) {
+            *abort = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
 // Tiled 3-D load of the tensor map's box at element coordinates (x, y, z)
 // into shared memory at dst (128-byte aligned), completing on bar.
 // Coordinates outside the tensor read as zero; x must be a multiple of
