@@ -82,9 +82,14 @@ __global__ void ens_init_kernel(StepState* st, double dt, double time, int ntime
     st->dt_factored = __longlong_as_double(0x7ff8000000000000LL);   // NaN: factor on the first step
 }
 
-// CalcMaxCFL of the variable-dt members: item = (k, tile of cells); block
-// maximum, then an atomic maximum on the bits of the member's instcfl (the
-// order of non-negative doubles is the order of their bit patterns).
+// CalcMaxCFL of the variable-dt members: item = (k, kCflTiles consecutive
+// tiles of blockDim.x cells); block maximum, then an atomic maximum on the
+// bits of the member's instcfl (the order of non-negative doubles is the
+// order of their bit patterns).  A block reduces up to kCflTiles tiles
+// before its one atomic: with one tile an item the atomics on the few
+// members' instcfl were the bottleneck of the phase.
+constexpr int kCflTiles = 8;
+
 template <typename T>
 __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, const int* prefix, int n) {
     __shared__ double sh[32];
@@ -94,12 +99,17 @@ __global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, cons
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
     const int tiles = (int)((I.d.P + blockDim.x - 1) / blockDim.x);
-    const int k = (int)((unsigned)local / (unsigned)tiles);
-    const long long flat = (local - (long long)k * tiles) * blockDim.x + threadIdx.x;
+    const int chunks = (tiles + kCflTiles - 1) / kCflTiles;
+    const int k = (int)((unsigned)local / (unsigned)chunks);
+    const int ch = (int)(local - (long long)k * chunks);
+    const int t1 = min(tiles, (ch + 1) * kCflTiles);
     double v = 0.0;
-    if (flat < I.d.P) {
-        const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
-        v = cfl_cell(I.d, I.c, I.cv, I.k.dxt, I.k.dxz, I.f, i, j, k);
+    for (int tt = ch * kCflTiles; tt < t1; ++tt) {
+        const long long flat = (long long)tt * blockDim.x + threadIdx.x;
+        if (flat < I.d.P) {
+            const int j = (int)((unsigned)flat / (unsigned)I.d.nt), i = (int)flat - j * I.d.nt;
+            v = fmax(v, cfl_cell(I.d, I.c, I.cv, I.k.dxt, I.k.dxz, I.f, i, j, k));
+        }
     }
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -334,7 +344,9 @@ int rebuild(tc_ensemble* e) {
         cnt[PH_THINV] = cnt[PH_DIV];
         cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, persistent ? ZCols<T>::value : ZEns<T>::cols);
         cnt[PH_FACT] = 1;
-        cnt[PH_CFL] = I.vdt ? (long long)d.nr * ceil_div(d.P, TPB) : 0;   // (level, tile of cells)
+        // (level, tile of cells) for the persistent kernel; (level, kCflTiles tiles) grouped
+        cnt[PH_CFL] = !I.vdt ? 0
+                      : (long long)d.nr * (persistent ? ceil_div(d.P, TPB) : ceil_div(ceil_div(d.P, TPB), kCflTiles));
         for (int p = 0; p < PH_COUNT; ++p) {
             long long v = (long long)prefix[(size_t)p * (n + 1) + a] + cnt[p];
             if (v > 2000000000LL) return efail(e, 2010, "ensemble work list exceeds 2^31 items");
