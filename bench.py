@@ -462,6 +462,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=25, help="C5: steps between admissions")
     ap.add_argument("--hbm-budget", type=float, default=150e9)
     ap.add_argument("--no-serving", action="store_true", help="skip the short serving leg of the default run")
+    ap.add_argument("--mixed-tma", action="store_true",
+                    help="mixed legs: the TMA-staged momentum march instead of the cached one (the default)")
     ap.add_argument("--serve-requests", type=int, default=8, help="serving leg: runs per arrival rate")
     ap.add_argument("--serve-rates", default="2,20", help="serving leg: arrival rates, runs/s")
     args = ap.parse_args()
@@ -586,6 +588,8 @@ def main():
         for prec in ("mixed", "mixed-ff"):
             gm = tc.TaylorCouette(bou, precision=prec)
             gm.set_stream(stream.cuda_stream)
+            if args.mixed_tma:
+                gm.use_tma(True)
             gm.set_state(*pinned)
             code_m, ntm, tm, _ = gm.run(args.warmup, 0, 0.0)
             gm.profile(True)
@@ -599,7 +603,8 @@ def main():
             gm.profile(False)
             leg = {"value": world * cells * args.steps / (ms_m * 1e-3) / 1e6, "unit": "Mcell-steps/s",
                    "ms_per_step": ms_m / args.steps, "speedup_vs_fp64": ms / ms_m, "status": code_m,
-                   "pressure_tridiagonals": "FP64" if prec == "mixed" else "float-float"}
+                   "pressure_tridiagonals": "FP64" if prec == "mixed" else "float-float",
+                   "momentum_march": "TMA-staged" if args.mixed_tma else "cached"}
             tot_m = sum(v[0] for v in prof_m.values())
             leg["kernel_shares"] = {k: round(v[0] / tot_m, 4) for k, v in prof_m.items() if v[1]}
             leg["ms_per_step_by_kernel"] = {k: round(v[0] / args.steps, 3) for k, v in prof_m.items() if v[1]}
