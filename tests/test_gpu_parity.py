@@ -264,8 +264,8 @@ def test_state_round_trip(gpu_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_state_transfer_from_pinned_memory(gpu_lib, precision):
-    """Pinned host arrays are read and written by the layout kernels in place
-    (no staging copy); the result equals the pageable (staged) path's."""
+    """State transfer from and into pinned host arrays (copy-engine copies at
+    the link rate) gives the same fields as from pageable arrays."""
     import torch
     bou = make_bou(nthm=40, nzm=36, nrm=22, istr=6, str=3.0)
     st = ini.couette_noise(bou, seed=9)
