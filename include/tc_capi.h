@@ -112,7 +112,7 @@ int tc_precision(const tc_handle* h);
 /* Mixed handles: stage the momentum march's input planes in shared memory
  * with TMA loads (1; the grid needs nthm a multiple of 4 and at least 64) or
  * load them through the read-only cache (0, the default: on GB300 it runs
- * the march about 9 % faster).  Both compute the same bits.  2019 when the
+ * the march about 5 % faster).  Both compute the same bits.  2019 when the
  * handle has no TMA descriptors.  No counterpart in the reference. */
 int tc_use_tma(tc_handle* h, int enable);
 /* The configuration the handle was created with. */

@@ -205,14 +205,14 @@ constexpr size_t kTmaSmem = (size_t)kTmaStages * kTmaStageB + 128;
 constexpr unsigned long long kTmaWaitNs = 1000000000ull;       // 1 s
 constexpr unsigned long long kTmaDrainNs = 100000000ull;       // 0.1 s a plane
 
-__global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, CoefT<float> c, MomArgs<float> a,
-                                                                    const __grid_constant__ MarchMaps maps) {
-    if (a.st->halt) return;
-    __shared__ __align__(8) unsigned long long full_bar[kTmaStages], empty_bar[kTmaStages];
-    __shared__ int abort_flag;
-    __shared__ MarchCoef ctab[kMomChunk];            // the chunk's per-level coefficients
-    extern __shared__ unsigned char tma_dyn[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(tma_dyn) + 127) & ~(size_t)127);
+// EDGE: the block's tile holds one of the domain's periodic theta edges
+// (the first or the last tile of a row), whose threads read the wrapped
+// neighbour from global memory; the other blocks compile without that code.
+template <bool EDGE>
+__device__ __forceinline__ void march_tma_block(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
+                                                const MarchMaps& maps, unsigned long long* full_bar,
+                                                unsigned long long* empty_bar, int& abort_flag, MarchCoef* ctab,
+                                                unsigned char* sm) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nr = d.nr, nt = d.nt, nz = d.nz;
     const int P = (int)d.P;
@@ -272,12 +272,13 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
         const float2 v = *reinterpret_cast<const float2*>(row + xb);
         return mkf2(v.x, v.y);
     };
+    auto edge = [&](bool p, const float* ptr, float v) -> float { return EDGE ? ld_pred(p, ptr, v) : v; };
     auto left = [&](const unsigned char* row) -> float { return *reinterpret_cast<const float*>(row + xb - 4); };
     auto right = [&](const unsigned char* row) -> float { return *reinterpret_cast<const float*>(row + xb + 8); };
     // q array f, z row j + dz of this thread, in the stage at base
     auto qrow = [&](const unsigned char* base, int f, int dz) { return base + f * kTmaQB + (ty + 1 + dz) * rs; };
 
-    const bool eL = i == 0, eR = i + 2 == nt;        // the domain's periodic theta edges
+    const bool eL = EDGE && i == 0, eR = EDGE && i + 2 == nt;   // the domain's periodic theta edges
     const int dimA = eL ? nt - 1 : -1, dipB = eR ? 2 - nt : 2;
     const int jj = j < nz ? j : nz - 1;
     const int djm = jj == 0 ? (nz - 1) * nt : -nt, djp = jj == nz - 1 ? -(nz - 1) * nt : nt;
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
         C.tm = ld_f2(qt + om);
         C.tmip = mkf2(f2y(C.tm), ld(qt + om + dipB));
         C.rc = pair(qrow(S0, 1, 0));
-        C.rim = mkf2(ld_pred(eL, qr + o + dimA, left(qrow(S0, 1, 0))), f2x(C.rc));
+        C.rim = mkf2(edge(eL, qr + o + dimA, left(qrow(S0, 1, 0))), f2x(C.rc));
         C.rjm = pair(qrow(S0, 1, -1));
         C.rm = k0 > 0 ? ld_f2(qr + om) : ZERO;
         C.zc = pair(qrow(S0, 2, 0));
@@ -333,26 +334,26 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
             f2xy(C.tc, tcx, tcy);
             f2xy(C.rc, rcx, rcy);
             f2xy(C.zc, zcx, zcy);
-            L.tip = mkf2(tcy, ld_pred(eR, qt + o + dipB, right(Tj)));
-            L.tim = mkf2(ld_pred(eL, qt + o + dimA, left(Tj)), tcx);
+            L.tip = mkf2(tcy, edge(eR, qt + o + dipB, right(Tj)));
+            L.tim = mkf2(edge(eL, qt + o + dimA, left(Tj)), tcx);
             L.tjp = pair(qrow(S, 0, 1));
             L.tjm = pair(Tjm);
-            L.tjmip = mkf2(f2y(L.tjm), ld_pred(eR, qt + o + djm + dipB, right(Tjm)));
+            L.tjmip = mkf2(f2y(L.tjm), edge(eR, qt + o + djm + dipB, right(Tjm)));
             L.tp = top ? C.tc : pair(qrow(N, 0, 0));
-            L.rip = mkf2(rcy, ld_pred(eR, qr + o + dipB, right(Rj)));
+            L.rip = mkf2(rcy, edge(eR, qr + o + dipB, right(Rj)));
             L.rjp = pair(qrow(S, 1, 1));
             L.rp = pair(Rpj);
-            L.rpim = mkf2(ld_pred(eL, qr + o + P + dimA, left(Rpj)), f2x(L.rp));
+            L.rpim = mkf2(edge(eL, qr + o + P + dimA, left(Rpj)), f2x(L.rp));
             L.rpjm = pair(qrow(N, 1, -1));
-            L.zip = mkf2(zcy, ld_pred(eR, qz + o + dipB, right(Zj)));
-            L.zim = mkf2(ld_pred(eL, qz + o + dimA, left(Zj)), zcx);
+            L.zip = mkf2(zcy, edge(eR, qz + o + dipB, right(Zj)));
+            L.zim = mkf2(edge(eL, qz + o + dimA, left(Zj)), zcx);
             L.zjp = pair(Zjp);
             L.zjm = pair(qrow(S, 2, -1));
-            L.zjpim = mkf2(ld_pred(eL, qz + o + djp + dimA, left(Zjp)), f2x(L.zjp));
+            L.zjpim = mkf2(edge(eL, qz + o + djp + dimA, left(Zjp)), f2x(L.zjp));
             L.zp = top ? C.zc : pair(qrow(N, 2, 0));
             L.pc = pair(Pj);
             L.pjm = pair(qrow(S, 3, -1));
-            L.pim = mkf2(ld_pred(eL, pr + o + dimA, left(Pj)), f2x(L.pc));
+            L.pim = mkf2(edge(eL, pr + o + dimA, left(Pj)), f2x(L.pc));
             L.old_t = a.use_ru ? pair(RU) : ZERO;
             L.old_r = (a.use_ru && k >= 1) ? pair(RU + kTmaRuB) : ZERO;
             L.old_z = (a.use_ru && !top) ? pair(RU + 2 * kTmaRuB) : ZERO;
@@ -374,6 +375,20 @@ __global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, Coef
             atomicExch(&st->halt, 1);
         }
     }
+}
+
+__global__ void __launch_bounds__(128, 4) momentum_march_tma_kernel(Dims d, CoefT<float> c, MomArgs<float> a,
+                                                                    const __grid_constant__ MarchMaps maps) {
+    if (a.st->halt) return;
+    __shared__ __align__(8) unsigned long long full_bar[kTmaStages], empty_bar[kTmaStages];
+    __shared__ int abort_flag;
+    __shared__ MarchCoef ctab[kMomChunk];            // the chunk's per-level coefficients
+    extern __shared__ unsigned char tma_dyn[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(tma_dyn) + 127) & ~(size_t)127);
+    if (blockIdx.x == 0 || blockIdx.x == gridDim.x - 1)
+        march_tma_block<true>(d, c, a, maps, full_bar, empty_bar, abort_flag, ctab, sm);
+    else
+        march_tma_block<false>(d, c, a, maps, full_bar, empty_bar, abort_flag, ctab, sm);
 }
 
 // --------------------------------------------------------------------------
