@@ -149,10 +149,32 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kern
     const int tiles = (int)((units + blockDim.x - 1) / blockDim.x);
     const int chunk = (int)((unsigned)local / (unsigned)tiles);
     const long long flat = (local - (long long)chunk * tiles) * blockDim.x + threadIdx.x;
-    if (flat >= units) return;
-    int i, j;
-    mom_unit_cell<T>((int)flat, I.d.nt, i, j);
-    mom_unit(I.d, I.cv, I.ma[sub], i, j, chunk);
+    if constexpr (MomMarch<T>::value) {
+        // The block's member and chunk are one: its arguments and the chunk's
+        // per-level coefficients are copied to shared memory once, so that the
+        // march reads them there instead of chasing the member's pointers in
+        // global memory at every level (two dependent loads a coefficient).
+        __shared__ MarchCoef ctab[kMomChunk];
+        __shared__ MomArgs<float> sma;
+        const int k0 = chunk * kMomChunk, k1 = min(k0 + kMomChunk, I.d.nr);
+        constexpr int kWords = (int)(sizeof(MomArgs<float>) / sizeof(int));
+        static_assert(sizeof(MomArgs<float>) % sizeof(int) == 0, "MomArgs copied as ints");
+        for (int w = threadIdx.x; w < kWords; w += blockDim.x)
+            reinterpret_cast<int*>(&sma)[w] = reinterpret_cast<const int*>(&I.ma[sub])[w];
+        for (int e = threadIdx.x; e < (k1 - k0) * kMarchCoefN; e += blockDim.x)
+            reinterpret_cast<float*>(ctab)[e] =
+                march_coef_entry(I.cv, I.ma[sub], I.d.nr + 1, k0 + e / kMarchCoefN, e % kMarchCoefN);
+        __syncthreads();
+        if (flat >= units) return;
+        int i, j;
+        mom_unit_cell<T>((int)flat, I.d.nt, i, j);
+        momentum_column_x2<true>(I.d, I.cv, sma, i, j, k0, k1, ctab);
+    } else {
+        if (flat >= units) return;
+        int i, j;
+        mom_unit_cell<T>((int)flat, I.d.nt, i, j);
+        mom_unit(I.d, I.cv, I.ma[sub], i, j, chunk);
+    }
 }
 
 // cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)

@@ -951,8 +951,12 @@ __device__ __forceinline__ void march_level(const Dims& d, const CoefT<float>& c
     C.prm = pc;
 }
 
+// TAB: the per-level coefficients come from ctab (ctab[k - k0], a table the
+// caller staged in shared memory) instead of the coefficient arrays.
+template <bool TAB = false>
 __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<float>& c, const MomArgs<float>& a,
-                                                   int i, int j, int k0, int k1) {
+                                                   int i, int j, int k0, int k1,
+                                                   const MarchCoef* ctab = nullptr) {
     const int nr = d.nr, nt = d.nt, nz = d.nz;
     const int P = (int)d.P;
     const int dimA = i == 0 ? nt - 1 : -1;             // q(i-1) from the pair's first cell
@@ -1026,7 +1030,8 @@ __device__ __forceinline__ void momentum_column_x2(const Dims& d, const CoefT<fl
         L.old_t = a.use_ru ? ldp_f2(a.ru1 + o) : ZERO;
         L.old_r = (a.use_ru && k >= 1) ? ldp_f2(a.ru2 + o) : ZERO;
         L.old_z = (a.use_ru && !top) ? ldp_f2(a.ru3 + o) : ZERO;
-        march_level(d, c, a, K, MarchCoefGlobal{c, a, nr + 1, k}, k, o, C, L);
+        if constexpr (TAB) march_level(d, c, a, K, MarchCoefTable{ctab[k - k0]}, k, o, C, L);
+        else march_level(d, c, a, K, MarchCoefGlobal{c, a, nr + 1, k}, k, o, C, L);
     }
 }
 
