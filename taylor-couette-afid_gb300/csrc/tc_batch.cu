@@ -5,8 +5,9 @@
 // and coefficients are reused as they are.  One step of the ensemble is a
 // fixed sequence of grouped launches, each covering every active member: the
 // launch's blocks form a flat work list of (member, tile) items, a block
-// finds its member by binary search in a prefix table of item counts and then
-// runs the same device body as the single-instance kernel (tc_bodies.cuh), so
+// reads its member from an owner table (the member of every item), its first
+// item from a prefix table of item counts, and then runs the same device
+// body as the single-instance kernel (tc_bodies.cuh), so
 // a member's arithmetic is identical alone and in the mix.  Per step:
 //   begin (dt, beta, inner-wall forcing per member), factors (one block per
 //   member), then per RK substep: momentum, radial solve, divergence + theta
@@ -91,10 +92,10 @@ __global__ void ens_init_kernel(StepState* st, double dt, double time, int ntime
 constexpr int kCflTiles = 8;
 
 template <typename T>
-__global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, const int* prefix, int n) {
+__global__ void __launch_bounds__(256) ens_cfl_kernel(const InstT<T>* inst, const int* prefix, const int* owner) {
     __shared__ double sh[32];
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
@@ -139,9 +140,9 @@ template <> struct EnsBlocks<float> { static constexpr int momentum = 2, radial 
 // packed FP32 (momentum_column_x2); for FP64 (no marching) a chunk is one
 // level and a thread a pair of cells (momentum_pair)
 template <typename T>
-__global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+__global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kernel(const InstT<T>* inst, const int* prefix, const int* owner, int sub) {
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
@@ -180,9 +181,9 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::momentum) ens_momentum_kern
 // cell-wise phases: item = (k, tile of TPB consecutive (j, i) cells)
 
 template <typename T>
-__global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+__global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, const int* prefix, const int* owner, int sub) {
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
@@ -196,9 +197,9 @@ __global__ void __launch_bounds__(256) ens_correct_kernel(const InstT<T>* inst, 
 
 // column-wise: item = (component, TPB consecutive (z, theta) columns)
 template <typename T>
-__global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+__global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(const InstT<T>* inst, const int* prefix, const int* owner, int sub) {
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long local = item - prefix[m];
@@ -213,9 +214,9 @@ __global__ void __launch_bounds__(256, EnsBlocks<T>::radial) ens_radial_kernel(c
 // mode-wise: item = TPB consecutive (kz, kt) modes
 // FF: the members' pressure solve (ptri_solve); one precision per ensemble
 template <typename T, int FF>
-__global__ void __launch_bounds__(256, (std::is_same<T, float>::value && FF == 0) ? 3 : EnsBlocks<T>::ptri) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, int n) {
+__global__ void __launch_bounds__(256, (std::is_same<T, float>::value && FF == 0) ? 3 : EnsBlocks<T>::ptri) ens_ptri_kernel(const InstT<T>* inst, const int* prefix, const int* owner) {
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const long long t = (item - prefix[m]) * blockDim.x + threadIdx.x;
@@ -223,27 +224,39 @@ __global__ void __launch_bounds__(256, (std::is_same<T, float>::value && FF == 0
     ptri_solve<T, FF>(I.d, I.c, I.f, t);
 }
 
-// row-wise FFT phases: item = R consecutive (k, j) rows
-template <int R, typename T>
-__global__ void __launch_bounds__(128) ens_divfft_kernel(const InstT<T>* inst, const int* prefix, int n, int sub) {
+// row-wise FFT phases: item = I.rows (I.rows_inv) consecutive (k, j) rows of
+// the item's member, so that a block holds about as many points for a short
+// theta line as for a long one
+template <typename T>
+__global__ void __launch_bounds__(128) ens_divfft_kernel(const InstT<T>* inst, const int* prefix, const int* owner, int sub) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
-    div_fft_rows<false, R, T>(I.d, I.cv, (T)I.k.dxt, (T)I.k.dxz, I.f, I.p.th, I.p.tw_th, I.p.twr, I.k.fft_norm, sub,
-                              (item - prefix[m]) * R, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    div_fft_rows_n<false, T>(I.d, I.cv, (T)I.k.dxt, (T)I.k.dxz, I.f, I.p.th, I.p.tw_th, I.p.twr, I.k.fft_norm, sub,
+                             (item - prefix[m]) * I.rows, reinterpret_cast<typename V2<T>::type*>(smem_raw),
+                             I.rows, I.lg_rows);
 }
 
-template <int R, typename T>
-__global__ void __launch_bounds__(128) ens_thinv_kernel(const InstT<T>* inst, const int* prefix, int n) {
+template <typename T>
+__global__ void __launch_bounds__(128) ens_thinv_kernel(const InstT<T>* inst, const int* prefix, const int* owner) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
-    thinv_rows<R, T>(I.d, I.f, I.p.th, I.p.tw_th, I.p.twr, (item - prefix[m]) * R,
-                     reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    thinv_rows_n<T>(I.d, I.f, I.p.th, I.p.tw_th, I.p.twr, (item - prefix[m]) * I.rows_inv,
+                    reinterpret_cast<typename V2<T>::type*>(smem_raw), I.rows_inv, I.lg_rows_inv);
+}
+
+// Rows per theta-FFT block of a member with M-point half lines: the largest
+// power of two up to 32 with rows * M <= span points (the single-run kernels'
+// rule: 512 for the divergence + forward FFT, 1024 for the inverse).
+int rows_for(int M, int span) {
+    int R = 1;
+    while (R < 32 && (R * 2) * M <= span) R *= 2;
+    return R;
 }
 
 // z FFT: item = (plane k, ZEns::cols consecutive kt columns)
@@ -255,10 +268,10 @@ template <typename T> struct ZEns { static constexpr int cols = 4, threads = 128
 template <> struct ZEns<float> { static constexpr int cols = 8, threads = 128; };
 
 template <typename T>
-__global__ void __launch_bounds__(ZEns<T>::threads) ens_zfft_kernel(const InstT<T>* inst, const int* prefix, int n, int inv) {
+__global__ void __launch_bounds__(ZEns<T>::threads) ens_zfft_kernel(const InstT<T>* inst, const int* prefix, const int* owner, int inv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const long long item = blockIdx.x;
-    const int m = find_member(prefix, n, item);
+    const int m = __ldg(owner + item);
     const InstT<T>& I = inst[m];
     if (I.f.st->halt) return;
     const int local = (int)(item - prefix[m]);
@@ -283,10 +296,12 @@ struct tc_ensemble {
     std::vector<int> active;             // slots in the current work list
     void* inst_dev = nullptr;            // InstT<T>[active]
     int* prefix_dev = nullptr;           // PH_COUNT tables of (n+1) ints
+    int* owner_dev = nullptr;            // grouped schedule: the member of every work item, phase by phase
+    long long owner_off[tcgb::ens::PH_COUNT] = {0};
     int threads = 128;                   // threads per cell/column/mode tile
-    int rows = 0;                        // rows per theta-FFT block (0: from the largest member)
-    int rows_used = 0;
-    size_t smem_div = 0, smem_z = 0;
+    int rows = 0;                        // rows per theta-FFT block (0: per member, from its line length)
+    int rows_used = 0;                   // persistent schedule: rows of every member
+    size_t smem_div = 0, smem_inv = 0, smem_z = 0;
     int items[tcgb::ens::PH_COUNT] = {0};
     int schedule = TC_SCHED_GROUPED;
     int persist_blocks = 0;              // resident blocks of the persistent kernel
@@ -324,11 +339,6 @@ template <typename T> const PlansT<T>& MP(tc_handle* h);
 template <> const PlansT<double>& MP<double>(tc_handle* h) { return h->pd; }
 template <> const PlansT<float>& MP<float>(tc_handle* h) { return h->pf; }
 
-template <int R, typename T>
-void set_smem_attrs() {
-    cudaFuncSetAttribute(ens_divfft_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(ens_thinv_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-}
 
 template <typename T>
 int rebuild(tc_ensemble* e) {
@@ -337,11 +347,13 @@ int rebuild(tc_ensemble* e) {
     if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
     if (e->inst_dev) { cudaFree(e->inst_dev); e->inst_dev = nullptr; }
     if (e->prefix_dev) { cudaFree(e->prefix_dev); e->prefix_dev = nullptr; }
+    if (e->owner_dev) { cudaFree(e->owner_dev); e->owner_dev = nullptr; }
     e->dirty = false;
     if (n == 0) return 0;
     std::vector<InstT<T>> inst(n);
     std::vector<int> prefix((size_t)PH_COUNT * (n + 1), 0);
     int maxM = 1, maxNz = 1;
+    long long maxDiv = 1, maxInv = 1;    // points of the largest theta-FFT tiles
     for (int a = 0; a < n; ++a) maxM = std::max(maxM, e->members[e->active[a]]->d.M);
     const bool persistent = e->schedule == TC_SCHED_PERSISTENT;
     int R = e->rows > 0 ? e->rows : theta_rows(maxM);
@@ -355,6 +367,12 @@ int rebuild(tc_ensemble* e) {
         for (int s = 0; s < 3; ++s) I.ma[s] = make_mom_args(h->k, I.f, s);
         I.vdt = e->vdt[e->active[a]];
         const Dims& d = h->d;
+        I.rows = persistent ? R : e->rows > 0 ? e->rows : rows_for(d.M, 512);
+        I.rows_inv = persistent ? R : e->rows > 0 ? e->rows : rows_for(d.M, 1024);
+        I.lg_rows = lines_log2(I.rows);
+        I.lg_rows_inv = lines_log2(I.rows_inv);
+        maxDiv = std::max(maxDiv, (long long)I.rows * d.M);
+        maxInv = std::max(maxInv, (long long)I.rows_inv * d.M);
         maxNz = std::max(maxNz, d.nz);
         long long cnt[PH_COUNT];
         cnt[PH_MOM] = (long long)(MomMarch<T>::value ? ceil_div(d.nr, kMomChunk) : d.nr) *
@@ -362,8 +380,8 @@ int rebuild(tc_ensemble* e) {
         cnt[PH_CORR] = (long long)d.nr * ceil_div(cell_units<T>(d.P), TPB);
         cnt[PH_RAD] = 3LL * ceil_div(cell_units<T>(d.P), TPB);
         cnt[PH_PTRI] = ceil_div((long long)d.nz * d.PH, TPB);
-        cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, R);
-        cnt[PH_THINV] = cnt[PH_DIV];
+        cnt[PH_DIV] = ceil_div((long long)d.nr * d.nz, I.rows);
+        cnt[PH_THINV] = ceil_div((long long)d.nr * d.nz, I.rows_inv);
         cnt[PH_ZFFT] = (long long)d.nr * ceil_div(d.PH, persistent ? ZCols<T>::value : ZEns<T>::cols);
         cnt[PH_FACT] = 1;
         // (level, tile of cells) for the persistent kernel; (level, kCflTiles tiles) grouped
@@ -377,9 +395,11 @@ int rebuild(tc_ensemble* e) {
     }
     for (int p = 0; p < PH_COUNT; ++p) e->items[p] = prefix[(size_t)p * (n + 1) + n];
     typedef typename V2<T>::type C2;
-    e->smem_div = (size_t)2 * R * maxM * sizeof(C2);
+    e->smem_div = (size_t)2 * maxDiv * sizeof(C2);
+    e->smem_inv = (size_t)2 * maxInv * sizeof(C2);
     e->smem_z = (size_t)2 * (persistent ? ZCols<T>::value : ZEns<T>::cols) * maxNz * sizeof(C2);
-    if (e->smem_div > 200 * 1024 || e->smem_z > 200 * 1024) return efail(e, 2011, "ensemble FFT tile exceeds shared memory");
+    if (e->smem_div > 200 * 1024 || e->smem_inv > 200 * 1024 || e->smem_z > 200 * 1024)
+        return efail(e, 2011, "ensemble FFT tile exceeds shared memory");
     cudaError_t c = cudaMalloc(&e->inst_dev, sizeof(InstT<T>) * n);
     if (c == cudaSuccess) c = cudaMalloc(&e->prefix_dev, sizeof(int) * prefix.size());
     if (c == cudaSuccess) c = cudaMemcpy(e->inst_dev, inst.data(), sizeof(InstT<T>) * n, cudaMemcpyHostToDevice);
@@ -396,25 +416,24 @@ int rebuild(tc_ensemble* e) {
         if (c != cudaSuccess) return ecuda(e, c, "persistent kernel setup");
         return 0;
     }
-    switch (R) {
-        case 1: set_smem_attrs<1, T>(); break;
-        case 2: set_smem_attrs<2, T>(); break;
-        case 4: set_smem_attrs<4, T>(); break;
-        case 8: set_smem_attrs<8, T>(); break;
-        case 16: set_smem_attrs<16, T>(); break;
-        default: set_smem_attrs<32, T>(); break;
-    }
+    cudaFuncSetAttribute(ens_divfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(ens_thinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(ens_zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    // A grouped block reads its member from the owner table (one load)
+    // instead of searching the prefix table (about log2(n) dependent loads
+    // that the streamed data evicts from L1, ahead of the member's struct,
+    // its halt flag and only then its data).
+    long long total = 0;
+    for (int p = 0; p < PH_COUNT; ++p) { e->owner_off[p] = total; total += e->items[p]; }
+    std::vector<int> owner((size_t)std::max(total, 1LL));
+    for (int p = 0; p < PH_COUNT; ++p)
+        for (int a = 0; a < n; ++a)
+            std::fill(owner.begin() + e->owner_off[p] + prefix[(size_t)p * (n + 1) + a],
+                      owner.begin() + e->owner_off[p] + prefix[(size_t)p * (n + 1) + a + 1], a);
+    c = cudaMalloc(&e->owner_dev, sizeof(int) * owner.size());
+    if (c == cudaSuccess) c = cudaMemcpy(e->owner_dev, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice);
+    if (c != cudaSuccess) return ecuda(e, c, "ensemble owner table");
     return 0;
-}
-
-template <int R, typename T>
-void launch_div(tc_ensemble* e, const InstT<T>* I, const int* pre, int n, int sub) {
-    ens_divfft_kernel<R, T><<<e->items[PH_DIV], 128, e->smem_div, e->stream>>>(I, pre, n, sub);
-}
-template <int R, typename T>
-void launch_thinv(tc_ensemble* e, const InstT<T>* I, const int* pre, int n) {
-    ens_thinv_kernel<R, T><<<e->items[PH_THINV], 128, e->smem_div, e->stream>>>(I, pre, n);
 }
 
 // Enqueue one step of every active member on e->stream.
@@ -424,6 +443,7 @@ int enqueue_step(tc_ensemble* e) {
     const InstT<T>* I = (const InstT<T>*)e->inst_dev;
     const int* pre = e->prefix_dev;
     auto P = [&](int p) { return pre + (size_t)p * (n + 1); };
+    auto O = [&](int p) { return e->owner_dev + e->owner_off[p]; };
     cudaStream_t s = e->stream;
     const int nsst = e->members[e->active[0]]->k.nsst;
     if (e->schedule == TC_SCHED_PERSISTENT) {
@@ -451,35 +471,21 @@ int enqueue_step(tc_ensemble* e) {
     const int TPB = e->threads;
     int count = 0;
     if (e->items[PH_CFL] > 0) {
-        ens_cfl_kernel<T><<<e->items[PH_CFL], TPB, 0, s>>>(I, P(PH_CFL), n);
+        ens_cfl_kernel<T><<<e->items[PH_CFL], TPB, 0, s>>>(I, P(PH_CFL), O(PH_CFL));
         ++count;
     }
     ens_begin_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(I, n); ++count;
     ens_factors_kernel<T><<<n, 256, 0, s>>>(I); ++count;
     for (int sub = 0; sub < nsst; ++sub) {
-        ens_momentum_kernel<T><<<e->items[PH_MOM], TPB, 0, s>>>(I, P(PH_MOM), n, sub);
-        ens_radial_kernel<T><<<e->items[PH_RAD], TPB, 0, s>>>(I, P(PH_RAD), n, sub);
-        switch (e->rows_used) {
-            case 1: launch_div<1, T>(e, I, P(PH_DIV), n, sub); break;
-            case 2: launch_div<2, T>(e, I, P(PH_DIV), n, sub); break;
-            case 4: launch_div<4, T>(e, I, P(PH_DIV), n, sub); break;
-            case 8: launch_div<8, T>(e, I, P(PH_DIV), n, sub); break;
-            case 16: launch_div<16, T>(e, I, P(PH_DIV), n, sub); break;
-            default: launch_div<32, T>(e, I, P(PH_DIV), n, sub); break;
-        }
-        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 0);
-        if (e->precision == TC_PREC_MIXED_FF) ens_ptri_kernel<T, 1><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
-        else ens_ptri_kernel<T, 0><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), n);
-        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), n, 1);
-        switch (e->rows_used) {
-            case 1: launch_thinv<1, T>(e, I, P(PH_THINV), n); break;
-            case 2: launch_thinv<2, T>(e, I, P(PH_THINV), n); break;
-            case 4: launch_thinv<4, T>(e, I, P(PH_THINV), n); break;
-            case 8: launch_thinv<8, T>(e, I, P(PH_THINV), n); break;
-            case 16: launch_thinv<16, T>(e, I, P(PH_THINV), n); break;
-            default: launch_thinv<32, T>(e, I, P(PH_THINV), n); break;
-        }
-        ens_correct_kernel<T><<<e->items[PH_CORR], TPB, 0, s>>>(I, P(PH_CORR), n, sub);
+        ens_momentum_kernel<T><<<e->items[PH_MOM], TPB, 0, s>>>(I, P(PH_MOM), O(PH_MOM), sub);
+        ens_radial_kernel<T><<<e->items[PH_RAD], TPB, 0, s>>>(I, P(PH_RAD), O(PH_RAD), sub);
+        ens_divfft_kernel<T><<<e->items[PH_DIV], 128, e->smem_div, s>>>(I, P(PH_DIV), O(PH_DIV), sub);
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), O(PH_ZFFT), 0);
+        if (e->precision == TC_PREC_MIXED_FF) ens_ptri_kernel<T, 1><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), O(PH_PTRI));
+        else ens_ptri_kernel<T, 0><<<e->items[PH_PTRI], TPB, 0, s>>>(I, P(PH_PTRI), O(PH_PTRI));
+        ens_zfft_kernel<T><<<e->items[PH_ZFFT], ZEns<T>::threads, e->smem_z, s>>>(I, P(PH_ZFFT), O(PH_ZFFT), 1);
+        ens_thinv_kernel<T><<<e->items[PH_THINV], 128, e->smem_inv, s>>>(I, P(PH_THINV), O(PH_THINV));
+        ens_correct_kernel<T><<<e->items[PH_CORR], TPB, 0, s>>>(I, P(PH_CORR), O(PH_CORR), sub);
         count += 8;
     }
     ens_end_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(I, n); ++count;
@@ -561,6 +567,7 @@ void tc_ensemble_destroy(tc_ensemble* e) {
     if (e->graph) cudaGraphDestroy(e->graph);
     if (e->inst_dev) cudaFree(e->inst_dev);
     if (e->prefix_dev) cudaFree(e->prefix_dev);
+    if (e->owner_dev) cudaFree(e->owner_dev);
     if (e->bar) cudaFree(e->bar);
     for (tc_handle* h : e->members) if (h) tc_destroy(h);
     delete e;

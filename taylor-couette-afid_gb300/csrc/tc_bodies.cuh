@@ -1317,11 +1317,16 @@ __device__ __forceinline__ typename V2<T>::type div_pair_scaled(const Dims& d, c
 // Forward transform of R rows.  FROM_PHI: the rows come from the phi array
 // (CalcLocalDivergence already ran); otherwise the divergence is computed on
 // the fly.  Output: spec[row][kt], kt = 0..M, scaled by usdt/(nthm*nzm).
-template <bool FROM_PHI, int R, typename T>
-__device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f, const FFTPlan& pl,
-                             const typename V2<T>::type* tw, const typename V2<T>::type* twr, double fft_norm,
-                             int sub, long long row0, typename V2<T>::type* smem) {
+// RT > 0: R = RT rows at compile time (div_fft_rows); RT = 0: R = 2^lgR
+// rows known at run time (div_fft_rows_n, the ensembles' per-member row
+// counts).  The arithmetic does not depend on R.
+template <bool FROM_PHI, int RT, typename T>
+__device__ __forceinline__ void div_fft_rows_impl(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f,
+                                                  const FFTPlan& pl, const typename V2<T>::type* tw,
+                                                  const typename V2<T>::type* twr, double fft_norm, int sub,
+                                                  long long row0, typename V2<T>::type* smem, int Rrt, int lgR) {
     typedef typename V2<T>::type C2;
+    const int R = RT > 0 ? RT : Rrt;
     const int M = pl.n;
     C2* a = smem;
     C2* b = smem + (size_t)R * M;
@@ -1346,7 +1351,7 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
-    const C2* Z = fft_lines<R>(a, b, pl, tw, false);
+    const C2* Z = RT > 0 ? fft_lines<RT>(a, b, pl, tw, false) : fft_lines_n(a, b, pl, tw, false, R, lgR);
     // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
     const int PH = M + 1;
     for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
@@ -1361,6 +1366,21 @@ __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, con
         // multiply-adds (the product w o is never rounded on its own)
         f.spec[(size_t)row * PH + kt] = mk2(fmar(w.x, o.y, fmar(w.y, o.x, e.x)), fmar(-w.x, o.x, fmar(w.y, o.y, e.y)));
     }
+}
+
+template <bool FROM_PHI, int R, typename T>
+__device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f, const FFTPlan& pl,
+                             const typename V2<T>::type* tw, const typename V2<T>::type* twr, double fft_norm,
+                             int sub, long long row0, typename V2<T>::type* smem) {
+    div_fft_rows_impl<FROM_PHI, R, T>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, row0, smem, R, 0);
+}
+
+template <bool FROM_PHI, typename T>
+__device__ __forceinline__ void div_fft_rows_n(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f,
+                                               const FFTPlan& pl, const typename V2<T>::type* tw,
+                                               const typename V2<T>::type* twr, double fft_norm, int sub,
+                                               long long row0, typename V2<T>::type* smem, int R, int lgR) {
+    div_fft_rows_impl<FROM_PHI, 0, T>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, row0, smem, R, lgR);
 }
 
 // Complex FFT along z of ZC consecutive kt columns of one r-plane.
@@ -1653,11 +1673,14 @@ __device__ __forceinline__ void ptri_solve(const Dims& d, const Coef& c, const F
     else ptri_d64(d, c, f, t);
 }
 
-// Inverse real FFT along theta: spec rows -> phi rows.
-template <int R, typename T>
-__device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
-                           const typename V2<T>::type* twr, long long row0, typename V2<T>::type* smem) {
+// Inverse real FFT along theta: spec rows -> phi rows, R rows a block (RT
+// at compile time, thinv_rows; or 2^lgR at run time, thinv_rows_n).
+template <int RT, typename T>
+__device__ __forceinline__ void thinv_rows_impl(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl,
+                                                const typename V2<T>::type* tw, const typename V2<T>::type* twr,
+                                                long long row0, typename V2<T>::type* smem, int Rrt, int lgR) {
     typedef typename V2<T>::type C2;
+    const int R = RT > 0 ? RT : Rrt;
     const int M = pl.n, PH = M + 1;
     C2* a = smem;
     C2* b = smem + (size_t)R * M;
@@ -1679,12 +1702,25 @@ __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
-    const C2* Z = fft_lines<R>(a, b, pl, tw, true);
+    const C2* Z = RT > 0 ? fft_lines<RT>(a, b, pl, tw, true) : fft_lines_n(a, b, pl, tw, true, R, lgR);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = fdiv(t, pl.mn), m = t - r * M;
         const long long row = row0 + r;
         if (row < nrows) *reinterpret_cast<C2*>(f.phi + (size_t)row * d.nt + 2 * m) = Z[m * R + r];
     }
+}
+
+template <int R, typename T>
+__device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
+                           const typename V2<T>::type* twr, long long row0, typename V2<T>::type* smem) {
+    thinv_rows_impl<R, T>(d, f, pl, tw, twr, row0, smem, R, 0);
+}
+
+template <typename T>
+__device__ __forceinline__ void thinv_rows_n(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl,
+                                             const typename V2<T>::type* tw, const typename V2<T>::type* twr,
+                                             long long row0, typename V2<T>::type* smem, int R, int lgR) {
+    thinv_rows_impl<0, T>(d, f, pl, tw, twr, row0, smem, R, lgR);
 }
 
 template <bool VEL, bool PRES, typename T>

@@ -19,6 +19,9 @@ struct InstT {
     PlansT<T> p;
     MomArgs<T> ma[3];
     int vdt;          // 1: dt from the CFL number every step (main.F90:156-174); 0: fixed dt
+    // grouped schedule: theta rows per block of the divergence + forward FFT
+    // (rows = 2^lg_rows) and of the inverse FFT, per member
+    int rows, lg_rows, rows_inv, lg_rows_inv;
 };
 
 enum { PH_MOM = 0, PH_RAD, PH_DIV, PH_ZFFT, PH_PTRI, PH_THINV, PH_CORR, PH_FACT, PH_CFL, PH_COUNT };

@@ -194,13 +194,15 @@ __device__ __forceinline__ const FTw<typename CRe<C2>::type>* ftw_table(const C2
 }
 
 // One Stockham stage of radix p (compile time) over C interleaved lines:
-// sub-DFTs of length L become length L*p.
+// sub-DFTs of length L become length L*p.  CT > 0: C = CT at compile time;
+// CT = 0: C = 2^lgC known at run time.
 // x / d with the plan's multiplier m (m = 0: d = 1).
 __device__ __forceinline__ int fdiv(int x, unsigned m) { return m ? (int)__umulhi((unsigned)x, m) : x; }
 
-template <int C, int p, typename C2>
+template <int CT, int p, typename C2>
 __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restrict__ b, int n, int L, int rp,
-                                          unsigned mrp, const C2* __restrict__ tw, bool inv) {
+                                          unsigned mrp, const C2* __restrict__ tw, bool inv, int Crt, int lgC) {
+    const int C = CT > 0 ? CT : Crt;
     typedef typename CRe<C2>::type R;
     // FP64 radix-4 and radix-2 stages after the first: factored butterflies
     constexpr bool kFused = std::is_same<R, double>::value && (p == 4 || p == 2);
@@ -209,7 +211,7 @@ __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restri
     const int nb = (n / p) * C;
     const int istep = rp * C, ostep = rp * L * C;
     for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-        const int c = t % C, bf = t / C;
+        const int c = CT > 0 ? t % CT : t & (C - 1), bf = CT > 0 ? t / CT : t >> lgC;
         const int s = fdiv(bf, mrp), q = bf - s * rp;
         const C2* in = a + (size_t)(q + r * s) * C + c;
         C2* out = b + (size_t)(q + rp * s) * C + c;
@@ -241,23 +243,37 @@ __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restri
 // Transform C interleaved lines of length P.n held in `a`; `b` is scratch of
 // the same size.  All threads of the block must call it.  Returns the buffer
 // that holds the result (a or b).
-template <int C, typename C2>
-__device__ C2* fft_lines(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv) {
+// fft_lines<C>: C lines, C known at compile time; fft_lines_n: C = 2^lgC
+// lines known only at run time.  The arithmetic does not depend on C.
+template <int CT, typename C2>
+__device__ __forceinline__ C2* fft_lines_impl(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv, int C, int lgC) {
     const int n = P.n;
     int L = 1;
     for (int st = 0; st < P.nstages; ++st) {
         const int p = P.radix[st], rp = P.rp[st];
         const unsigned m = P.mrp[st];
-        if (p == 8) fft_stage<C, 8>(a, b, n, L, rp, m, tw, inv);
-        else if (p == 4) fft_stage<C, 4>(a, b, n, L, rp, m, tw, inv);
-        else if (p == 2) fft_stage<C, 2>(a, b, n, L, rp, m, tw, inv);
-        else if (p == 3) fft_stage<C, 3>(a, b, n, L, rp, m, tw, inv);
-        else fft_stage<C, 5>(a, b, n, L, rp, m, tw, inv);
+        if (p == 8) fft_stage<CT, 8>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 4) fft_stage<CT, 4>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 2) fft_stage<CT, 2>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 3) fft_stage<CT, 3>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else fft_stage<CT, 5>(a, b, n, L, rp, m, tw, inv, C, lgC);
         __syncthreads();
         C2* t = a; a = b; b = t;
         L *= p;
     }
     return a;
+}
+
+constexpr int lines_log2(int c) { return c <= 1 ? 0 : 1 + lines_log2(c >> 1); }
+
+template <int C, typename C2>
+__device__ C2* fft_lines(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv) {
+    return fft_lines_impl<C>(a, b, P, tw, inv, C, 0);
+}
+
+template <typename C2>
+__device__ __forceinline__ C2* fft_lines_n(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv, int C, int lgC) {
+    return fft_lines_impl<0>(a, b, P, tw, inv, C, lgC);
 }
 
 }  // namespace tcgb
