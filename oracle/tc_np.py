@@ -10,7 +10,9 @@ and ``numpy.fft`` (pocketfft) in place of FFTW.  Arrays use the reference memory
 layout: a NumPy array of shape (nthm+2, nzm+2, nr) in C order is the Fortran
 array q(1:nr, 0:nzm+1, 0:nthm+1); index [i, j, k-1].
 
-Parity status: unpinned (the reference has no golden vectors).
+Parity status: the C++ oracle it cross-checks is pinned to runs of the
+reference's own source (tests/golden/reference_runs.npz, made by
+tests/golden/make_reference_runs.py).
 """
 from __future__ import annotations
 

@@ -8,13 +8,17 @@
  * baseline leg use it, always as the checker or the timed CPU baseline, never
  * as part of the product path.
  *
- * Parity status: UNPINNED.  The reference ships no tests, golden vectors or
- * known-answer fixtures, and its Fortran/MPI/FFTW/HDF5 build cannot be
- * compiled here (no Fortran compiler, MPI, FFTW or LAPACK libraries).  The
- * restatement is cross-checked against an independent NumPy/SciPy restatement
- * (oracle/tc_np.py) that calls the real LAPACK ?gttrf/?gttrs, and against
- * physics known-answer tests (laminar Couette torque, divergence-free
- * projection, FFT round trips).
+ * Parity status: pinned to runs of the reference's own source.  The
+ * reference ships no tests or golden vectors, and its Fortran/MPI/FFTW/HDF5
+ * build cannot be compiled here (no Fortran compiler, MPI, FFTW or LAPACK
+ * libraries).  Its main program and time-step routines were instead executed
+ * on one rank by a translator of the Fortran subset they use
+ * (tests/golden/fortran_subset.py; LAPACK through SciPy, FFTW through
+ * numpy.fft), and the runs are committed as fixtures
+ * (tests/golden/reference_runs.npz) that tests/test_reference_runs.py checks
+ * this restatement against.  It is also cross-checked against an independent
+ * NumPy/SciPy restatement (oracle/tc_np.py) and physics known-answer tests
+ * (laminar Couette torque, divergence-free projection, FFT round trips).
  */
 #ifndef TC_REF_H
 #define TC_REF_H

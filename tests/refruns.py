@@ -1,0 +1,160 @@
+"""The golden runs of the reference's own Fortran source and how a
+simulation is compared with them.
+
+tests/golden/reference_runs.npz / .json hold runs of the reference's main
+program (main.F90 and every routine of its time step, executed on one rank
+by tests/golden/fortran_subset.py; see tests/golden/make_reference_runs.py):
+for each case its bou.in values and seed, the final fields, the dt sequence,
+the CFL number behind each dt, the CalcTorque records of the output steps,
+the CheckDivergence maxima, the stop code and the final diagnostics.
+
+The mode kθ = kz = 0 of the pressure equation is singular; the reference
+solves it with LAPACK's roundoff pivot, which adds an arbitrary constant to
+φ of that mode every substep (SolvePressureCorrection.F90:137-141).  Through
+CorrectPressure (`amm = apph(kc)`, CorrectPressure.F90:40) that constant
+reaches pr only as a function of the radial index.  The pressure is
+therefore compared with the θ-z mean of every radial level removed; the
+velocities do not see the constant (only differences of φ enter them).
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load():
+    with open(os.path.join(GOLDEN, "reference_runs.json")) as f:
+        meta = json.load(f)
+    z = np.load(os.path.join(GOLDEN, "reference_runs.npz"))
+    return meta["cases"], {k: z[k] for k in z.files}
+
+
+CASES, DATA = load()
+CASE_NAMES = [c["name"] for c in CASES]
+
+
+def case(name):
+    return next(c for c in CASES if c["name"] == name)
+
+
+def ref(name, key):
+    return DATA[f"{name}/{key}"]
+
+
+def start(c):
+    import tc_gb300.initial as ini
+    return ini.couette_noise(c["bou"], seed=c["seed"], amp=c["amp"])
+
+
+def is_output_step(ntime, time, dt, tout):
+    """main.F90:184: the step of index ntime ends in an output block."""
+    return ntime == 1 or math.fmod(time, tout) < dt
+
+
+def march(step, cfl, torque, c):
+    """Advance a simulation as main.F90:152-226 does, one step at a time.
+
+    step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
+    cfl() and torque() are CalcMaxCFL and CalcTorque of the current state.
+    Returns the per-step dt, time and CFL, the torques of the output steps,
+    the stop code and the index of the last step."""
+    bou = c["bou"]
+    ntst = int(bou["ntst"])
+    t, dt = 0.0, 0.0
+    rec = dict(dt=[], time=[], cfl=[], torque=[])
+    code, ntime = 0, 0
+    for ntime in range(0, ntst + 1):
+        rec["cfl"].append(cfl())
+        code, t, dt = step(ntime, t, dt)
+        rec["dt"].append(dt)
+        rec["time"].append(t)
+        if is_output_step(ntime, t, dt, bou["tout"]):
+            rec["torque"].append((t,) + tuple(torque()))
+        if code != 0:
+            break
+    rec["code"], rec["ntime"] = code, ntime
+    return rec
+
+
+def relmax(a, b):
+    den = float(np.abs(b).max())
+    return float(np.abs(a - b).max()) / (den if den > 0 else 1.0)
+
+
+def pressure_fluct(p, nrm):
+    """Interior pr without the θ-z mean of each radial level."""
+    a = p[1:-1, 1:-1, :nrm]
+    return a - a.mean(axis=(0, 1), keepdims=True)
+
+
+def field_errors(c, state):
+    """Relative errors of (qt, qr, qz, pr) against the reference run: the
+    interior cells (qt, qz, pr: nrm radial levels; qr: nr faces), each
+    divided by the reference field's maximum; pr with the radial profile
+    removed and divided by max |pr| of the reference.  Cases that keep
+    only some theta planes compare those planes and the whole-field sums."""
+    name = c["name"]
+    nrm = int(c["bou"]["nrm"])
+    planes = c.get("planes")
+    out = {}
+    for k, a, nk in zip(("qt", "qr", "qz", "pr"), state, (nrm, nrm + 1, nrm, nrm)):
+        if planes is None:
+            b = ref(name, k)
+            full_b = b
+        else:
+            b = ref(name, k + "_planes")
+            a_full = a
+            a = a[planes]
+            full_b = None
+        if k == "pr":
+            scale = float(np.abs(b[1:-1, 1:-1, :nrm]).max()) if planes is None else float(np.abs(b[:, 1:-1, :nrm]).max())
+            if planes is None:
+                err = float(np.abs(pressure_fluct(a, nrm) - pressure_fluct(b, nrm)).max()) / scale
+            else:
+                # planes keep the radial profile: compare sums of the full field instead
+                err = 0.0
+        else:
+            if planes is None:
+                ai, bi = a[1:-1, 1:-1, :nk], b[1:-1, 1:-1, :nk]
+            else:
+                ai, bi = a[:, 1:-1, :nk], b[:, 1:-1, :nk]
+            err = relmax(ai, bi)
+        if planes is not None:
+            sums = _field_sums(k, a_full)
+            for s, v in sums.items():
+                rv = float(ref(name, s))
+                err = max(err, abs(v - rv) / max(abs(rv), 1e-300) if s.endswith("sumsq") else
+                          abs(v - rv) / float(ref(name, k + "_sumsq")) ** 0.5 / math.sqrt(a_full[1:-1, 1:-1].size))
+        out[k] = err
+    return out
+
+
+def _field_sums(k, v):
+    import tc_gb300.initial as ini
+    a = v[1:-1, 1:-1, :]
+    if k == "pr":
+        a = a[..., :-1]
+        a = a - a.mean(axis=(0, 1), keepdims=True)
+    w = ini.uniform(99, 7, a.shape[0], a.shape[1], a.shape[2])
+    return {k + "_sum": float(a.sum()), k + "_sumsq": float((a * a).sum()), k + "_wsum": float((a * w).sum())}
+
+
+def scalar_errors(c, rec):
+    """Relative errors of the dt sequence, the step times, the CFL numbers
+    behind dt and the output-step torques against the reference run."""
+    name = c["name"]
+    rdt, rtime, rcfl = ref(name, "step_dt"), ref(name, "step_time"), ref(name, "step_cfl")
+    rtq = ref(name, "out_torque")
+    n = len(rdt)
+    assert len(rec["dt"]) == n, (len(rec["dt"]), n)
+    e = dict(dt=relmax(np.array(rec["dt"]), rdt), time=relmax(np.array(rec["time"]), rtime),
+             cfl=relmax(np.array(rec["cfl"]), rcfl))
+    tq = np.array(rec["torque"]).reshape(-1, 3)
+    assert tq.shape == rtq.shape, (tq.shape, rtq.shape)
+    e["torque"] = max(relmax(tq[:, 1], rtq[:, 1]), relmax(tq[:, 2], rtq[:, 2])) if len(tq) else 0.0
+    return e

@@ -1,0 +1,116 @@
+"""The CUDA path against runs of the reference's own Fortran source.
+
+Every case of tests/golden/reference_runs.npz (tests/refruns.py) is run on
+the GPU through the C ABI (tc_run one step at a time, as main.F90:152-226
+runs the loop) from the same seeded start and bou.in values:
+
+* FP64 (the drop-in): velocities and pressure (radial profile of the
+  singular mode removed) within 1e-10 of the reference's, the dt sequence,
+  step times, CFL numbers and output-step torques within 1e-10 relative,
+  the same stop code at the same step;
+* the mixed forms (FP32 velocity side; FP64 or float-float pressure
+  tridiagonals) on the production-like cases: velocities within 1e-3 of the
+  velocity scale and torques within 1e-4 relative, each error printed;
+* an ensemble holding every case that runs to NTST (grouped launches, FP64
+  members of different shapes): each member within 1e-10 of its reference
+  run.
+"""
+import numpy as np
+import pytest
+
+from conftest import tc
+
+import refruns as R
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+TOL_MIXED_Q = 1e-3
+TOL_MIXED_TORQUE = 1e-4
+
+
+def gpu_march(c, precision="fp64"):
+    g = tc.TaylorCouette(c["bou"], precision=precision)
+    g.set_state(*R.start(c))
+
+    def step(ntime, t, dt):
+        code, _, t, dt = g.run(1, ntime, t, dt)
+        return code, t, dt
+
+    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c)
+    return g, rec
+
+
+@pytest.mark.parametrize("name", R.CASE_NAMES)
+def test_fp64_matches_reference_run(gpu_lib, name):
+    c = R.case(name)
+    g, rec = gpu_march(c)
+    assert rec["code"] == int(R.ref(name, "errorcode"))
+    assert rec["ntime"] == int(R.ref(name, "ntime"))
+    se = R.scalar_errors(c, rec)
+    fe = R.field_errors(c, g.get_state())
+    print(name, {k: f"{v:.1e}" for k, v in {**fe, **se}.items()})
+    for k, v in {**fe, **se}.items():
+        assert v <= TOL, (k, v)
+    ti, to = g.calc_torque()
+    rt = R.ref(name, "final_torque")
+    assert abs(ti - rt[1]) <= TOL * abs(rt[1]) and abs(to - rt[2]) <= TOL * abs(rt[2])
+    assert g.check_divergence() < c["bou"]["resid"]
+    g.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
+@pytest.mark.parametrize("name", ["production_oscillating_32x24x32", "rotating_32x24x32",
+                                  "chebyshev_rk3_rotating"])
+def test_mixed_against_reference_run(gpu_lib, name, precision):
+    """The mixed forms on the reference's own time grid: the dt sequence of
+    the reference run is imposed (each form's own CFL rule would pick a
+    slightly different dt), so the difference is the precision alone."""
+    c = R.case(name)
+    g = tc.TaylorCouette(c["bou"], precision=precision)
+    g.set_state(*R.start(c))
+    times = np.concatenate([[0.0], R.ref(name, "step_time")[:-1]])
+    for dt, t in zip(R.ref(name, "step_dt"), times):
+        g.time_marcher(float(dt), float(t))
+    st = g.get_state()
+    nrm = int(c["bou"]["nrm"])
+    scale = max(float(np.abs(R.ref(name, "qt")[1:-1, 1:-1, :nrm]).max()), 1.0)
+    err = {k: float(np.abs(a[1:-1, 1:-1, :nk] - R.ref(name, k)[1:-1, 1:-1, :nk]).max()) / scale
+           for k, a, nk in zip(("qt", "qr", "qz"), st[:3], (nrm, nrm + 1, nrm))}
+    ti, to = g.calc_torque()
+    rt = R.ref(name, "final_torque")
+    terr = max(abs(ti - rt[1]) / abs(rt[1]), abs(to - rt[2]) / abs(rt[2]))
+    print(name, precision, {k: f"{v:.1e}" for k, v in err.items()}, f"torque {terr:.1e}",
+          f"div {g.check_divergence():.1e}")
+    assert max(err.values()) <= TOL_MIXED_Q
+    assert terr <= TOL_MIXED_TORQUE
+    assert g.check_divergence() < c["bou"]["resid"]
+    g.close()
+
+
+def test_ensemble_members_match_reference_runs(gpu_lib):
+    """Grouped launches over members of different shapes, radial grids and
+    dt rules: every member lands on its reference run.  (An ensemble runs
+    one time scheme and no patterned slip, so the AB2 and slip cases stay
+    out.)"""
+    names = [n for n in R.CASE_NAMES if int(R.ref(n, "errorcode")) == 555 and R.case(n).get("planes") is None
+             and int(R.case(n)["bou"]["nsst"]) == 3 and int(R.case(n)["bou"]["minstrt"]) == 0]
+    assert len(names) >= 5
+    ens = tc.Ensemble("fp64")
+    slots = {}
+    for n in names:
+        c = R.case(n)
+        slots[n] = ens.add(c["bou"], R.start(c), nsteps=int(c["bou"]["ntst"]) + 1, dt=0.0)
+    steps = max(int(R.case(n)["bou"]["ntst"]) + 1 for n in names)
+    ens.step(steps)
+    ens.sync()
+    for n in names:
+        c = R.case(n)
+        done, t, dt, code = ens.status_full(slots[n])
+        assert done == int(c["bou"]["ntst"]) + 1
+        assert abs(t - float(R.ref(n, "final_time"))) <= TOL * float(R.ref(n, "final_time"))
+        fe = R.field_errors(c, ens.member(slots[n]).get_state())
+        print(n, {k: f"{v:.1e}" for k, v in fe.items()})
+        for k, v in fe.items():
+            assert v <= TOL, (n, k, v)
+    ens.close()
