@@ -113,7 +113,7 @@ CASES = [
          bou=base_bou(nthm=16, nzm=16, nrm=8, minstrt=2, minstrz=2, multmin=1, ntst=9, virotint=1.0,
                       rext=1.5, lamb=1.0, alx3=2.0)),
     dict(name="aspect_lamb_virotext", seed=16, amp=0.03,
-         bou=base_bou(nthm=10, nzm=14, nrm=9, istr=6, str=2.0, lamb=3.0, alx3=1.7, rint=0.8, rext=1.3,
+         bou=base_bou(nthm=10, nzm=10, nrm=9, istr=6, str=2.0, lamb=3.0, alx3=1.7, rint=0.8, rext=1.3,
                       virotext=0.3, virotint=0.9, idtv=1, limitCFL=0.9, dtmin=1e-5, dtmax=3e-3, tout=1e-2)),
     dict(name="stops_at_tmax", seed=17, amp=0.01,
          bou=base_bou(nthm=8, nzm=8, nrm=6, tmax=4.5e-3, ntst=100)),
