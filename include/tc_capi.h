@@ -102,7 +102,10 @@ const char* tc_version(void);
 /* InitTimeMarchScheme + InitVariables + CreateGrid + InitPressureSolver
  * (main.F90:70-94): validate cfg, build the grid and coefficients, allocate
  * all device state on the current CUDA device, zero it.  Fields start at zero
- * and time at 0; load a start with tc_set_state. */
+ * and time at 0; load a start with tc_set_state.  The transform lengths
+ * NTM/2 (theta, real transform of NTM points) and NZM may have no prime
+ * factor above 13 (status 2003 otherwise; the reference's FFTW plans take
+ * any length). */
 int tc_create(const tc_bou* cfg, tc_handle** out);
 /* tc_create with a precision (enum tc_precision_mode); tc_create is
  * tc_create_ex(cfg, TC_PREC_FP64, out).  No counterpart in the reference,

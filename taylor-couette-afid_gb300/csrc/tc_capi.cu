@@ -47,7 +47,8 @@ cudaError_t dalloc(tc_handle* h, T** p, size_t count) {
 }
 
 // Radix plan: radix-8 stages first when r8 (the FP32 transforms, bound by
-// instruction issue: fewer passes through shared memory), then 4, 2, 3, 5.
+// instruction issue: fewer passes through shared memory), then 4, 2, 3, 5,
+// and the primes 7, 11, 13.
 // The FP64 transforms keep radix-4 stages, whose factored multiply-add
 // butterflies cost the same FP64 instructions a point and level.
 bool make_plan(int n, FFTPlan& P, bool r8) {
@@ -61,7 +62,7 @@ bool make_plan(int n, FFTPlan& P, bool r8) {
             P.radix[P.nstages++] = 8;
             m /= 8;
         }
-    for (int r : {4, 2, 3, 5})
+    for (int r : {4, 2, 3, 5, 7, 11, 13})
         while (m % r == 0 && m > 1) {
             if (P.nstages >= kMaxStages) return false;
             P.radix[P.nstages++] = r;
@@ -421,7 +422,7 @@ int tc_create_ex(const tc_bou* cfg, int precision, tc_handle** out) {
     // FFT plans and twiddles
     FFTPlan pth, pz;
     if (!make_plan(d.M, pth, h->mixed) || !make_plan(d.nz, pz, h->mixed)) {
-        int r = fail(nullptr, 2003, "FFT length does not factor into 2, 3, 5"); tc_destroy(h); return r;
+        int r = fail(nullptr, 2003, "FFT length has a prime factor above 13"); tc_destroy(h); return r;
     }
     if (zfft_smem_bytes(d.nz, h->mixed) > 200 * 1024) {
         int r = fail(nullptr, 2003, "NZM too large for one z-FFT tile in shared memory"); tc_destroy(h); return r;

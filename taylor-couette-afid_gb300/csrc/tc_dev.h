@@ -26,7 +26,8 @@ template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 type; };
 template <> struct V2<float> { typedef float2 type; };
 
-// Radix plan of one complex transform length (radices 2, 3, 4, 5), with the
+// Radix plan of one complex transform length (radices 2, 3, 4, 5, 7, 8, 11,
+// 13), with the
 // stride rp = n / (L p) of every Stockham stage and the multipliers that turn
 // the kernels' divisions by rp, n and n + 1 into a multiply-high:
 // x / d = umulhi(x, ceil(2^32 / d)) exactly when x * d < 2^32 (n <= 65536);

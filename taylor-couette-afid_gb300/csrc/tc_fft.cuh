@@ -1,6 +1,6 @@
-// tc_fft.cuh -- shared-memory mixed-radix complex FFT (radix 2, 3, 4, 5),
-// generic over the element type (double2 for the FP64 path, float2 for the
-// mixed path).
+// tc_fft.cuh -- shared-memory mixed-radix complex FFT (radix 2, 3, 4, 5, 7,
+// 8, 11, 13), generic over the element type (double2 for the FP64 path,
+// float2 for the mixed path).
 //
 // Stockham autosort, decimation in time, out of place between two
 // shared-memory buffers.  C independent lines are stored interleaved: element
@@ -240,6 +240,42 @@ __device__ __forceinline__ void fft_stage(const C2* __restrict__ a, C2* __restri
     }
 }
 
+// A Stockham stage of an odd prime radix P (7, 11, 13): every butterfly as a
+// direct DFT that keeps one output in registers at a time.  For output k the
+// P inputs are read again from shared memory, twiddled by w^(j s rp) and
+// multiplied by exp(-+ 2 pi i jk / P) = entry (jk mod P) n/P of the
+// transform's table.  These radices are rare; a stage of its own, out of
+// line (rather than P values in registers in fft_stage), leaves the code and
+// the register count of the common stages as they are.  Arguments as
+// fft_stage.
+template <int CT, int P, typename C2>
+__device__ __noinline__ void fft_stage_prime(const C2* __restrict__ a, C2* __restrict__ b, int n, int L, int rp,
+                                             unsigned mrp, const C2* __restrict__ tw, bool inv, int Crt, int lgC) {
+    const int C = CT > 0 ? CT : Crt;
+    const int r = rp * P, step = n / P;
+    const int nb = (n / P) * C;
+    const int istep = rp * C, ostep = rp * L * C;
+#pragma unroll 1
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+        const int c = CT > 0 ? t % CT : t & (C - 1), bf = CT > 0 ? t / CT : t >> lgC;
+        const int s = fdiv(bf, mrp), q = bf - s * rp;
+        const C2* in = a + (size_t)(q + r * s) * C + c;
+        C2* out = b + (size_t)(q + rp * s) * C + c;
+        const int srp = L > 1 ? s * rp : 0;
+#pragma unroll 1
+        for (int k = 0; k < P; ++k) {
+            C2 acc = in[0];
+#pragma unroll 1
+            for (int j = 1; j < P; ++j) {
+                C2 x = in[j * istep];
+                if (srp != 0) x = cmul(x, twiddle(tw, j * srp, inv));
+                acc = cadd(acc, cmul(x, twiddle(tw, ((j * k) % P) * step, inv)));
+            }
+            out[k * ostep] = acc;
+        }
+    }
+}
+
 // Transform C interleaved lines of length P.n held in `a`; `b` is scratch of
 // the same size.  All threads of the block must call it.  Returns the buffer
 // that holds the result (a or b).
@@ -256,7 +292,10 @@ __device__ __forceinline__ C2* fft_lines_impl(C2* a, C2* b, const FFTPlan& P, co
         else if (p == 4) fft_stage<CT, 4>(a, b, n, L, rp, m, tw, inv, C, lgC);
         else if (p == 2) fft_stage<CT, 2>(a, b, n, L, rp, m, tw, inv, C, lgC);
         else if (p == 3) fft_stage<CT, 3>(a, b, n, L, rp, m, tw, inv, C, lgC);
-        else fft_stage<CT, 5>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 5) fft_stage<CT, 5>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 7) fft_stage_prime<CT, 7>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (p == 11) fft_stage_prime<CT, 11>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else fft_stage_prime<CT, 13>(a, b, n, L, rp, m, tw, inv, C, lgC);
         __syncthreads();
         C2* t = a; a = b; b = t;
         L *= p;

@@ -73,9 +73,11 @@ bool list_read(const std::vector<std::string>& recs, size_t& line, std::vector<I
 
 inline double sq(double x) { return x * x; }
 
-bool factor235(int n) {
+// The FFT engine's radices: every prime factor of a transform length must
+// be one of these.
+bool fft_length_ok(int n) {
     if (n < 1) return false;
-    for (int p : {2, 3, 5}) while (n % p == 0) n /= p;
+    for (int p : {2, 3, 5, 7, 11, 13}) while (n % p == 0) n /= p;
     return n == 1;
 }
 
@@ -86,8 +88,8 @@ std::string validate(const tc_bou& b) {
     if (b.nrm < 3) return "NRM must be at least 3";
     if (b.nthm < 4 || b.nthm % 2) return "NTM must be even and at least 4";
     if (b.nzm < 2 || b.nzm % 2) return "NZM must be even and at least 2";
-    if (!factor235(b.nthm / 2) || !factor235(b.nzm)) {
-        std::snprintf(buf, sizeof buf, "NTM/2=%d and NZM=%d must factor into 2, 3 and 5", b.nthm / 2, b.nzm);
+    if (!fft_length_ok(b.nthm / 2) || !fft_length_ok(b.nzm)) {
+        std::snprintf(buf, sizeof buf, "NTM/2=%d and NZM=%d must have no prime factor above 13", b.nthm / 2, b.nzm);
         return buf;
     }
     if (b.nthm > 4096 || b.nzm > 1536 || b.nrm > 4096)

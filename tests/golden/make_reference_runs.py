@@ -121,6 +121,12 @@ CASES = [
          bou=base_bou(nthm=8, nzm=8, nrm=6, idtv=1, limitCFL=1e-4, dtmin=1e-3, dtmax=2e-3, ntst=10)),
     dict(name="output_every_step", seed=19, amp=0.05,
          bou=base_bou(nthm=12, nzm=10, nrm=10, istr=6, str=5.0, tout=1e-3, ntst=14)),
+    # transform lengths with the prime factors 7, 13 (theta 14 -> 7 complex
+    # points, z 26) and 11 (theta 22, z 22)
+    dict(name="prime_lengths_7_13", seed=20, amp=0.02,
+         bou=base_bou(nthm=14, nzm=26, nrm=8, istr=6, str=3.0, ntst=9)),
+    dict(name="prime_lengths_11", seed=21, amp=0.02,
+         bou=base_bou(nthm=22, nzm=22, nrm=7, ntst=9, idtv=1, limitCFL=1.0, dtmin=1e-5, dtmax=2e-3)),
     # the production case (512x512x384, ISTR=6, STR3=20, 1/NU=5000,
     # oscillating inner cylinder, CFLMAX 1.2, DTMAX 3e-4) on a smaller grid
     dict(name="production_oscillating_32x24x32", seed=1234, amp=0.01,

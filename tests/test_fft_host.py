@@ -1,8 +1,9 @@
 """The shared-memory FFT engine (csrc/tc_fft.cuh) and its plans and twiddle
 tables (csrc/tc_capi.cu), compiled for the host from the same source text
 with single-thread shims for the CUDA built-ins, against a direct DFT in long
-double: every radix (2, 3, 4, 5, 8), the factored multiply-add butterflies of
-the FP64 stages, both directions, FP64 and FP32, lengths from 2 to 1536.
+double: every radix (2, 3, 4, 5, 7, 8, 11, 13), the factored multiply-add
+butterflies of the FP64 stages, both directions, FP64 and FP32, lengths from
+2 to 1536.
 Relative max error below 1e-13 (FP64) and 2e-6 (FP32)."""
 import os
 import shutil
@@ -23,11 +24,13 @@ SHIMS = r'''
 #define __device__
 #define __host__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 #define __restrict__
 struct double2 { double x, y; };
 struct float2 { float x, y; };
 struct float4 { float x, y, z, w; };
 inline double2 make_double2(double a, double b) { return {a, b}; }
+inline float4 make_float4(float a, float b, float c, float d) { return {a, b, c, d}; }
 inline float2 make_float2(float a, float b) { return {a, b}; }
 template <typename T> inline T __ldg(const T* p) { return *p; }
 inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
@@ -47,7 +50,7 @@ using namespace tcgb;
 
 template <typename C2>
 double run(int n, bool r8, bool inv, unsigned seed) {
-    constexpr int C = 2;
+    constexpr int C = 4;
     FFTPlan P;
     if (!make_plan(n, P, r8)) { std::printf("no plan for %%d\n", n); std::exit(2); }
     std::vector<C2> tw = twiddles_with_factored<C2>(n);
@@ -81,7 +84,8 @@ double run(int n, bool r8, bool inv, unsigned seed) {
 }
 
 int main() {
-    const int sizes[] = {2, 3, 4, 5, 6, 8, 10, 12, 16, 30, 40, 48, 64, 96, 128, 160, 256, 384, 512, 768, 1536};
+    const int sizes[] = {2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 14, 16, 22, 26, 30, 40, 48, 56, 64, 77, 91, 96, 128,
+                         143, 160, 168, 256, 384, 448, 512, 768, 1001, 1536};
     int bad = 0;
     for (int n : sizes)
         for (int r8 = 0; r8 < 2; ++r8)

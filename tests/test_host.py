@@ -96,7 +96,7 @@ def test_host_grid_matches_oracle(gpu_lib, oracle, case):
         np.testing.assert_allclose(a[:n], b[:n], rtol=1e-14, atol=1e-300, err_msg=name)
 
 
-@pytest.mark.parametrize("bad,code", [(dict(nthm=15), 2003), (dict(nzm=14), 2003), (dict(nthm=14), 2003),
+@pytest.mark.parametrize("bad,code", [(dict(nthm=15), 2003), (dict(nzm=34), 2003), (dict(nthm=34), 2003),
                                       (dict(istr=1), 2003), (dict(rext=0.5), 2003),
                                       (dict(minstrt=1, multmin=1), 2003), (dict(nrm=2), 2003)])
 def test_invalid_configurations(gpu_lib, bad, code):
