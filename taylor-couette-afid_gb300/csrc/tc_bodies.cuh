@@ -1611,6 +1611,16 @@ __device__ __forceinline__ void ptri_d64(const Dims& d, const Coef& c, const Fie
     for (int m = 0; m < nb; ++m, k += kPtriCk) {
         float2 xv[kPtriCk];
         double lv[kPtriCk];
+        // the batch two ahead into L2 (the sweep is bound by load latency)
+        if (m + 2 < nb) {
+            const float2* px = x + (size_t)(k + 2 * kPtriCk) * PS;
+            const double* pl = L + (size_t)(k + 2 * kPtriCk) * FS;
+#pragma unroll 1
+            for (int b = 0; b < kPtriCk; ++b, px += PS, pl += FS) {
+                prefetch_l2(px);
+                prefetch_l2(pl);
+            }
+        }
 #pragma unroll
         for (int b = 0; b < kPtriCk; ++b) {
             xv[b] = x[(size_t)(k + b) * PS];
@@ -1636,6 +1646,18 @@ __device__ __forceinline__ void ptri_d64(const Dims& d, const Coef& c, const Fie
     // full batches from the top: recompute y from the checkpoint below
     for (int m = nb - 1; m >= 0; --m) {
         const int kb = 1 + m * kPtriCk;
+        if (m >= 2) {
+            const int kp = kb - 2 * kPtriCk;
+            const float2* px = x + (size_t)kp * PS;
+            const double* pl = L + (size_t)kp * FS;
+            const double* pd = DI + (size_t)kp * FS;
+#pragma unroll 1
+            for (int b = 0; b < kPtriCk; ++b, px += PS, pl += FS, pd += FS) {
+                prefetch_l2(px);
+                prefetch_l2(pl);
+                prefetch_l2(pd);
+            }
+        }
         double2 yb[kPtriCk];
         double2 yc = w[(size_t)m * PS];
         float2 xv[kPtriCk - 1];

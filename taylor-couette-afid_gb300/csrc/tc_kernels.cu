@@ -454,10 +454,12 @@ __global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<
 // grid the float-float solve of the mixed path takes 0.133 ms a launch
 // against 0.140 ms with 8 blocks (64 registers, a few spilled), 0.156 ms with
 // 10 and 0.183 ms with 6; the FP64 solve 0.230 ms with 7 or 8.
-// The FP64 solve of the mixed path keeps a batch of FP64 complex values
-// (32 registers) and is compiled for 5 blocks (6 spill).
+// The FP64 solve of the mixed path keeps a batch of FP64 complex values (32
+// registers); with the L2 prefetch of the batches two ahead it is bound by
+// load latency, not by registers: on the same grid 0.267 ms a launch for 7
+// blocks (69 registers, 32 bytes spilled), 0.264 for 8 (64), 0.338 for 6
+// and 0.325 for 5 (94, none spilled).
 template <typename T, int FF> struct PtriBlocks { static constexpr int value = 7; };
-template <> struct PtriBlocks<float, 0> { static constexpr int value = 5; };
 
 template <typename T, int FF>
 __global__ void __launch_bounds__(128, PtriBlocks<T, FF>::value) ptri_kernel(Dims d, Coef c, FieldsT<T> f) {

@@ -61,7 +61,7 @@ def test_fp64_matches_reference_run(gpu_lib, name):
 
 @pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
 @pytest.mark.parametrize("name", ["production_oscillating_32x24x32", "rotating_32x24x32",
-                                  "chebyshev_rk3_rotating"])
+                                  "chebyshev_rk3_rotating", "prime_lengths_7_13"])
 def test_mixed_against_reference_run(gpu_lib, name, precision):
     """The mixed forms on the reference's own time grid: the dt sequence of
     the reference run is imposed (each form's own CFL rule would pick a
