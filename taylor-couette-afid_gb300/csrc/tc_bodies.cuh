@@ -1320,7 +1320,7 @@ __device__ __forceinline__ typename V2<T>::type div_pair_scaled(const Dims& d, c
 // RT > 0: R = RT rows at compile time (div_fft_rows); RT = 0: R = 2^lgR
 // rows known at run time (div_fft_rows_n, the ensembles' per-member row
 // counts).  The arithmetic does not depend on R.
-template <bool FROM_PHI, int RT, typename T>
+template <bool FROM_PHI, int RT, typename T, bool PRIME = true>
 __device__ __forceinline__ void div_fft_rows_impl(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f,
                                                   const FFTPlan& pl, const typename V2<T>::type* tw,
                                                   const typename V2<T>::type* twr, double fft_norm, int sub,
@@ -1351,7 +1351,7 @@ __device__ __forceinline__ void div_fft_rows_impl(const Dims& d, const CoefT<T>&
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
-    const C2* Z = RT > 0 ? fft_lines<RT>(a, b, pl, tw, false) : fft_lines_n(a, b, pl, tw, false, R, lgR);
+    const C2* Z = RT > 0 ? fft_lines<RT, PRIME>(a, b, pl, tw, false) : fft_lines_n<PRIME>(a, b, pl, tw, false, R, lgR);
     // X[k] = (Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i / nthm)
     const int PH = M + 1;
     for (int t = threadIdx.x; t < R * PH; t += blockDim.x) {
@@ -1368,11 +1368,11 @@ __device__ __forceinline__ void div_fft_rows_impl(const Dims& d, const CoefT<T>&
     }
 }
 
-template <bool FROM_PHI, int R, typename T>
+template <bool FROM_PHI, int R, typename T, bool PRIME = true>
 __device__ void div_fft_rows(const Dims& d, const CoefT<T>& c, T dxt, T dxz, const FieldsT<T>& f, const FFTPlan& pl,
                              const typename V2<T>::type* tw, const typename V2<T>::type* twr, double fft_norm,
                              int sub, long long row0, typename V2<T>::type* smem) {
-    div_fft_rows_impl<FROM_PHI, R, T>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, row0, smem, R, 0);
+    div_fft_rows_impl<FROM_PHI, R, T, PRIME>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, row0, smem, R, 0);
 }
 
 template <bool FROM_PHI, typename T>
@@ -1383,8 +1383,9 @@ __device__ __forceinline__ void div_fft_rows_n(const Dims& d, const CoefT<T>& c,
     div_fft_rows_impl<FROM_PHI, 0, T>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, row0, smem, R, lgR);
 }
 
-// Complex FFT along z of ZC consecutive kt columns of one r-plane.
-template <int ZC, typename T>
+// Complex FFT along z of ZC consecutive kt columns of one r-plane.  PRIME:
+// with the stages of radix 7, 11 and 13 (fft_lines_impl).
+template <int ZC, typename T, bool PRIME = true>
 __device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
                           int inv, int kt0, int kplane, typename V2<T>::type* smem) {
     typedef typename V2<T>::type C2;
@@ -1397,7 +1398,7 @@ __device__ void zfft_tile(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl,
         return (kt0 + c < PH) ? plane[(size_t)j * PH + kt0 + c] : mk2((T)0, (T)0);
     }, [](int t) { return t; });
     __syncthreads();
-    const C2* Z = fft_lines<ZC>(a, b, pl, tw, inv != 0);
+    const C2* Z = fft_lines<ZC, PRIME>(a, b, pl, tw, inv != 0);
     for (int t = threadIdx.x; t < ZC * nz; t += blockDim.x) {
         const int c = t % ZC, j = t / ZC;
         if (kt0 + c < PH) plane[(size_t)j * PH + kt0 + c] = Z[t];
@@ -1697,7 +1698,7 @@ __device__ __forceinline__ void ptri_solve(const Dims& d, const Coef& c, const F
 
 // Inverse real FFT along theta: spec rows -> phi rows, R rows a block (RT
 // at compile time, thinv_rows; or 2^lgR at run time, thinv_rows_n).
-template <int RT, typename T>
+template <int RT, typename T, bool PRIME = true>
 __device__ __forceinline__ void thinv_rows_impl(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl,
                                                 const typename V2<T>::type* tw, const typename V2<T>::type* twr,
                                                 long long row0, typename V2<T>::type* smem, int Rrt, int lgR) {
@@ -1724,7 +1725,7 @@ __device__ __forceinline__ void thinv_rows_impl(const Dims& d, const FieldsT<T>&
         return z;
     }, [&](int t) { const int r = fdiv(t, pl.mn); return (t - r * M) * R + r; });
     __syncthreads();
-    const C2* Z = RT > 0 ? fft_lines<RT>(a, b, pl, tw, true) : fft_lines_n(a, b, pl, tw, true, R, lgR);
+    const C2* Z = RT > 0 ? fft_lines<RT, PRIME>(a, b, pl, tw, true) : fft_lines_n<PRIME>(a, b, pl, tw, true, R, lgR);
     for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
         const int r = fdiv(t, pl.mn), m = t - r * M;
         const long long row = row0 + r;
@@ -1732,10 +1733,10 @@ __device__ __forceinline__ void thinv_rows_impl(const Dims& d, const FieldsT<T>&
     }
 }
 
-template <int R, typename T>
+template <int R, typename T, bool PRIME = true>
 __device__ void thinv_rows(const Dims& d, const FieldsT<T>& f, const FFTPlan& pl, const typename V2<T>::type* tw,
                            const typename V2<T>::type* twr, long long row0, typename V2<T>::type* smem) {
-    thinv_rows_impl<R, T>(d, f, pl, tw, twr, row0, smem, R, 0);
+    thinv_rows_impl<R, T, PRIME>(d, f, pl, tw, twr, row0, smem, R, 0);
 }
 
 template <typename T>

@@ -281,7 +281,10 @@ __device__ __noinline__ void fft_stage_prime(const C2* __restrict__ a, C2* __res
 // that holds the result (a or b).
 // fft_lines<C>: C lines, C known at compile time; fft_lines_n: C = 2^lgC
 // lines known only at run time.  The arithmetic does not depend on C.
-template <int CT, typename C2>
+// PRIME: the stages of the radices 7, 11 and 13 are compiled in (kernels
+// instantiated without them keep the code of the common stages exactly as
+// it is; the launchers pick the instance with them for plans that need it).
+template <int CT, bool PRIME, typename C2>
 __device__ __forceinline__ C2* fft_lines_impl(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv, int C, int lgC) {
     const int n = P.n;
     int L = 1;
@@ -292,10 +295,12 @@ __device__ __forceinline__ C2* fft_lines_impl(C2* a, C2* b, const FFTPlan& P, co
         else if (p == 4) fft_stage<CT, 4>(a, b, n, L, rp, m, tw, inv, C, lgC);
         else if (p == 2) fft_stage<CT, 2>(a, b, n, L, rp, m, tw, inv, C, lgC);
         else if (p == 3) fft_stage<CT, 3>(a, b, n, L, rp, m, tw, inv, C, lgC);
-        else if (p == 5) fft_stage<CT, 5>(a, b, n, L, rp, m, tw, inv, C, lgC);
-        else if (p == 7) fft_stage_prime<CT, 7>(a, b, n, L, rp, m, tw, inv, C, lgC);
-        else if (p == 11) fft_stage_prime<CT, 11>(a, b, n, L, rp, m, tw, inv, C, lgC);
-        else fft_stage_prime<CT, 13>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if (!PRIME || p == 5) fft_stage<CT, 5>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        else if constexpr (PRIME) {
+            if (p == 7) fft_stage_prime<CT, 7>(a, b, n, L, rp, m, tw, inv, C, lgC);
+            else if (p == 11) fft_stage_prime<CT, 11>(a, b, n, L, rp, m, tw, inv, C, lgC);
+            else fft_stage_prime<CT, 13>(a, b, n, L, rp, m, tw, inv, C, lgC);
+        }
         __syncthreads();
         C2* t = a; a = b; b = t;
         L *= p;
@@ -305,14 +310,21 @@ __device__ __forceinline__ C2* fft_lines_impl(C2* a, C2* b, const FFTPlan& P, co
 
 constexpr int lines_log2(int c) { return c <= 1 ? 0 : 1 + lines_log2(c >> 1); }
 
-template <int C, typename C2>
+template <int C, bool PRIME = true, typename C2>
 __device__ C2* fft_lines(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv) {
-    return fft_lines_impl<C>(a, b, P, tw, inv, C, 0);
+    return fft_lines_impl<C, PRIME>(a, b, P, tw, inv, C, 0);
 }
 
-template <typename C2>
+template <bool PRIME = true, typename C2>
 __device__ __forceinline__ C2* fft_lines_n(C2* a, C2* b, const FFTPlan& P, const C2* tw, bool inv, int C, int lgC) {
-    return fft_lines_impl<0>(a, b, P, tw, inv, C, lgC);
+    return fft_lines_impl<0, PRIME>(a, b, P, tw, inv, C, lgC);
+}
+
+// Whether a plan has a stage of radix 7, 11 or 13 (host and device).
+__host__ __device__ inline bool plan_has_prime(const FFTPlan& P) {
+    for (int st = 0; st < P.nstages; ++st)
+        if (P.radix[st] > 5 && P.radix[st] != 8) return true;
+    return false;
 }
 
 }  // namespace tcgb

@@ -430,23 +430,26 @@ __global__ void __launch_bounds__(128, kRadialPairBlocks) radial_pair_kernel(Dim
 // (row = k*nzm + j) of nthm reals packed as nthm/2 complex values.
 // --------------------------------------------------------------------------
 
-template <bool FROM_PHI, int R, typename T>
+// PRIME (kernels below too): compiled with the FFT stages of radix 7, 11 and
+// 13; the launchers take that instance (one row a block) only for plans with
+// such a stage.
+template <bool FROM_PHI, int R, typename T, bool PRIME>
 __global__ void __launch_bounds__(kThThreads) div_fft_kernel(Dims d, CoefT<T> c, T dxt, T dxz, FieldsT<T> f, FFTPlan pl,
                                                       const typename V2<T>::type* tw,
                                                       const typename V2<T>::type* twr, double fft_norm, int sub) {
     if (f.st->halt) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    div_fft_rows<FROM_PHI, R, T>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, (long long)blockIdx.x * R,
+    div_fft_rows<FROM_PHI, R, T, PRIME>(d, c, dxt, dxz, f, pl, tw, twr, fft_norm, sub, (long long)blockIdx.x * R,
                                  reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
 // Complex FFT along z of kZC consecutive kt columns of one r-plane.
-template <typename T>
+template <typename T, bool PRIME>
 __global__ void __launch_bounds__(ZRun<T>::threads) zfft_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
                                                    const typename V2<T>::type* tw, int inv) {
     if (f.st->halt) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    zfft_tile<ZRun<T>::cols>(d, f, pl, tw, inv, blockIdx.x * ZRun<T>::cols, blockIdx.y,
+    zfft_tile<ZRun<T>::cols, T, PRIME>(d, f, pl, tw, inv, blockIdx.x * ZRun<T>::cols, blockIdx.y,
               reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
@@ -494,13 +497,14 @@ __global__ void pfactor_kernel(Dims d, Coef c, double* fl, double* fdi) {
 }
 
 // Inverse real FFT along theta: spec rows -> phi rows.
-template <int R, typename T>
+template <int R, typename T, bool PRIME>
 __global__ void __launch_bounds__(kThThreads) theta_inv_kernel(Dims d, FieldsT<T> f, FFTPlan pl,
                                                         const typename V2<T>::type* tw,
                                                         const typename V2<T>::type* twr) {
     if (f.st->halt) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    thinv_rows<R, T>(d, f, pl, tw, twr, (long long)blockIdx.x * R, reinterpret_cast<typename V2<T>::type*>(smem_raw));
+    thinv_rows<R, T, PRIME>(d, f, pl, tw, twr, (long long)blockIdx.x * R,
+                            reinterpret_cast<typename V2<T>::type*>(smem_raw));
 }
 
 // --------------------------------------------------------------------------
@@ -927,23 +931,30 @@ void launch_radial_solve(cudaStream_t s, const Dims& d, const FieldsT<T>& f, int
     TC_LAUNCH_CHECK();
 }
 
-template <bool FP, int R, typename T>
+template <bool FP, int R, typename T, bool PRIME = false>
 static void div_fft_R(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                       const PlansT<T>& p, int sub) {
     size_t sm = (size_t)2 * R * p.th.n * sizeof(typename V2<T>::type);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(div_fft_kernel<FP, R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(div_fft_kernel<FP, R, T, PRIME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
         attr = true;
     }
     long long nrows = (long long)d.nr * d.nz;
-    div_fft_kernel<FP, R, T><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(
+    div_fft_kernel<FP, R, T, PRIME><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(
         d, c, (T)k.dxt, (T)k.dxz, f, p.th, p.tw_th, p.twr, k.fft_norm, sub);
 }
 
 template <typename T>
 void launch_div_fft(cudaStream_t s, const Dims& d, const CoefT<T>& c, const Consts& k, const FieldsT<T>& f,
                     const PlansT<T>& p, int sub, bool from_phi) {
+    if (plan_has_prime(p.th)) {
+        if (from_phi) div_fft_R<true, 1, T, true>(s, d, c, k, f, p, sub);
+        else div_fft_R<false, 1, T, true>(s, d, c, k, f, p, sub);
+        TC_LAUNCH_CHECK();
+        return;
+    }
     int R = theta_rows_run(p.th.n);
 #define TC_DF(RR) case RR: if (from_phi) div_fft_R<true, RR, T>(s, d, c, k, f, p, sub); \
                            else div_fft_R<false, RR, T>(s, d, c, k, f, p, sub); break;
@@ -963,11 +974,13 @@ void launch_zfft(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const Plans
     const size_t sm = zfft_smem_bytes(p.z.n, std::is_same<T, float>::value);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(zfft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(zfft_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(zfft_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
     dim3 g((d.PH + ZC - 1) / ZC, d.nr);
-    zfft_kernel<T><<<g, ZRun<T>::threads, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
+    if (plan_has_prime(p.z)) zfft_kernel<T, true><<<g, ZRun<T>::threads, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
+    else zfft_kernel<T, false><<<g, ZRun<T>::threads, sm, s>>>(d, f, p.z, p.tw_z, inv ? 1 : 0);
     TC_LAUNCH_CHECK();
 }
 
@@ -980,20 +993,25 @@ void launch_pressure_tridiag(cudaStream_t s, const Dims& d, const Coef& c, const
     TC_LAUNCH_CHECK();
 }
 
-template <int R, typename T>
+template <int R, typename T, bool PRIME = false>
 static void theta_inv_R(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
     size_t sm = (size_t)2 * R * p.th.n * sizeof(typename V2<T>::type);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(theta_inv_kernel<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(theta_inv_kernel<R, T, PRIME>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
     long long nrows = (long long)d.nr * d.nz;
-    theta_inv_kernel<R, T><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(d, f, p.th, p.tw_th, p.twr);
+    theta_inv_kernel<R, T, PRIME><<<(unsigned)((nrows + R - 1) / R), kThThreads, sm, s>>>(d, f, p.th, p.tw_th, p.twr);
 }
 
 template <typename T>
 void launch_theta_inverse(cudaStream_t s, const Dims& d, const FieldsT<T>& f, const PlansT<T>& p) {
+    if (plan_has_prime(p.th)) {
+        theta_inv_R<1, T, true>(s, d, f, p);
+        TC_LAUNCH_CHECK();
+        return;
+    }
     int R = theta_rows_run(p.th.n, kThSpanInv);
     switch (R) {
         case 1: theta_inv_R<1, T>(s, d, f, p); break;
