@@ -1334,6 +1334,20 @@ class Gen:
             return k + 1
         m = re.match(r"^do\s+(\w+)\s*=\s*(.*)$", text)
         if m:
+            # a GOTO inside the loop to the CONTINUE labelled right after its
+            # END DO leaves the loop (an EXIT): remember that label
+            depth, e = 0, i + 1
+            while e < len(stmts):
+                t_e = stmts[e][2]
+                if re.match(r"^do\b", t_e):
+                    depth += 1
+                elif re.match(r"^(end\s*do|enddo)$", t_e):
+                    if depth == 0:
+                        break
+                    depth -= 1
+                e += 1
+            after = stmts[e + 1] if e + 1 < len(stmts) else None
+            self.loops.append(after[1] if after is not None and after[2] == "continue" else None)
             var = m.group(1)
             b = [self.ex(parse_expr(x))[0] for x in _split_top(m.group(2))]
             step = b[2] if len(b) > 2 else "1"
@@ -1349,6 +1363,7 @@ class Gen:
             self.ind -= 1
             self.emit("else:")
             self.emit(f"    {target} = {rng}.start + len({rng}) * {rng}.step")
+            self.loops.pop()
             return k + 1
         m = re.match(r"^select\s+case\s*\((.*)\)$", text)
         if m:
@@ -1375,6 +1390,13 @@ class Gen:
                 self.body_or_pass(n0)
                 self.ind -= 1
         if text in ("exit",):
+            self.emit("break")
+            return i + 1
+        m = re.match(r"^go\s*to\s+(\d+)$", text)
+        if m:
+            if not self.loops or self.loops[-1] != int(m.group(1)):
+                raise SyntaxError(f"{self.u.file}:{line}: only a GOTO to the CONTINUE after the enclosing loop is "
+                                  f"supported: {text}")
             self.emit("break")
             return i + 1
         if text == "cycle":
@@ -1506,12 +1528,13 @@ class Gen:
         body = self.lines
         self.lines = []
         self.ind = 1
+        # module arrays first: the bounds of dummy and local arrays may use them
+        mod_arrays = [nm for nm in sorted(self.arrays) if self.var(nm)[1] == "module"]
+        for nm in mod_arrays:
+            self.emit(f"a_{nm} = G.{nm}")
+        self.rebind(mod_arrays)
         for p in pre:
             self.emit(p)
-        for nm in sorted(self.arrays):
-            v, where = self.var(nm)
-            if where == "module":
-                self.emit(f"a_{nm} = G.{nm}")
         self.rebind()
         out = [head] + self.lines + body
         out.append("    return " + self.ret_tuple())
@@ -1698,7 +1721,7 @@ class OneRank:
             mpimaxrealscalar=self.ident, mpiallmaxrealscalar=self.ident, mpiminrealscalar=self.ident,
             mpisumreal1d=self.ident, mpiallsumreal1d=self.ident, mpiabort=self.abort,
             hdfstart=self.none, hdfclose=self.none, openlogs=self.none, writegridinfo=self.none,
-            initstats=self.none, initdumprcuts=self.none, hdfserialreadintscalar=self.read_scalar,
+            initdumprcuts=self.none, hdfserialreadintscalar=self.read_scalar,
             hdfserialreadrealscalar=self.read_scalar, hdfreadcontinua=self.read_continua,
             quitroutine=self.quit, mpi_wtime=lambda: 0.0)
         for name, fn in stubs.items():
@@ -1838,11 +1861,13 @@ class OneRank:
 
     def read_continua(self, n1o, n2o, n3o, xs2, xe2, xs3, xe3, intvar, qua):
         """HdfReadContinua: the file's (nr, nz-1, nth-1) values into
-        qua(1:n3o, xs2:xe2, xs3:xe3)."""
+        qua(1:n3o, xs2:xe2, xs3:xe3), the dummy being declared
+        qua(1:n3o, xs2-lvlhalo:xe2+lvlhalo, xs3-lvlhalo:xe3+lvlhalo)
+        (HdfReadContinua.F90:32-33) whatever the bounds of the actual."""
         name = {1: "qt", 2: "qr", 3: "qz"}[int(intvar)]
         src = self.continua[name]
         d = qua.d
-        o = qua.o
+        o = (1, xs2 - 1, xs3 - 1)
         d[1 - o[0]:n3o + 1 - o[0], xs2 - o[1]:xe2 + 1 - o[1], xs3 - o[2]:xe3 + 1 - o[2]] = src
         return None
 

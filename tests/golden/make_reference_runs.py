@@ -54,7 +54,10 @@ FILES = ["main.F90", "ReadInputFile.F90", "InitTimeMarchScheme.F90", "InitVariab
          "ImplicitAndUpdateQT.F90", "ImplicitAndUpdateQR.F90", "ImplicitAndUpdateQZ.F90",
          "SolveImpEqnUpdate_QT.F90", "SolveImpEqnUpdate_QR.F90", "SolveImpEqnUpdate_QZ.F90",
          "CalcLocalDivergence.F90", "SolvePressureCorrection.F90", "CorrectVelocity.F90", "CorrectPressure.F90",
-         "CalcVelocityStats.F90", "CalcTorque.F90", "AuxiliaryRoutines.F90"]
+         "CalcVelocityStats.F90", "CalcTorque.F90", "AuxiliaryRoutines.F90", "StatRoutines.F90",
+         "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90"]
+STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
+              "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 MODULE_FILES = ["param.F90"]
 
 BOU_ORDER = [
@@ -142,10 +145,43 @@ CASES = [
     # kept on four theta planes plus whole-field sums
     dict(name="c1_64cubed_5_steps", seed=2024, amp=0.01, planes=[1, 17, 33, 64],
          bou=base_bou(nthm=64, nzm=64, nrm=64, ntst=4)),
+    # statistics on (TSTA = 0): main.F90 calls CalcStats (with
+    # CalcVorticity) and CalcDissipation at every output step
+    dict(name="statistics_every_2_steps", seed=22, amp=0.05, stats=True,
+         bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9)),
+    # a restart from continua files of a coarser grid: ReadFlowField
+    # interpolates them (interp.F90) onto the run's grid; the start is kept
+    dict(name="restart_interpolated_from_coarser_grid", seed=23, amp=0.05,
+         old_grid=dict(nthm=8, nzm=8, nrm=6),
+         bou=base_bou(nthm=12, nzm=14, nrm=9, istr=0, ntst=4)),
 ]
 
 
-def run_case(ref_dir, case, verbose=False):
+class _Started(Exception):
+    """Raised after ReadFlowField in the restart cases: only the start is kept."""
+
+
+def run_restart(ref_dir, case):
+    """The interpolated start of a restart from a coarser grid, twice: with
+    undefined values as NaN (the mask of points that depend on memory the
+    reference never sets: interp.F90 reads corner halos of the old field
+    that nothing fills) and as zeros (the values)."""
+    out = {}
+    for nan_fill in (True, False):
+        try:
+            run_case(ref_dir, case, stop_after_read=True, nan_fill=nan_fill)
+        except _Started as st:
+            for k, a in st.args[0].items():
+                if nan_fill:
+                    out["start_defined_" + k] = np.isfinite(a)
+                else:
+                    out["start_" + k] = a
+    return out
+
+
+def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True):
+    if case.get("old_grid") and not stop_after_read:
+        return run_restart(ref_dir, case)
     bou = dict(case["bou"])
     qt, qr, qz, pr = ini.couette_noise(bou, seed=case["seed"], amp=case["amp"])
     nrm = int(bou["nrm"])
@@ -157,9 +193,27 @@ def run_case(ref_dir, case, verbose=False):
 
     continua = {"qt": interior(qt), "qr": interior(qr), "qz": interior(qz), "nth": nth, "nr": nr, "nz": nz,
                 "time": 0.0, "istr": int(bou["istr"]), "str": float(bou["str"])}
+    if case.get("old_grid"):
+        # the continua files hold the same seeded start on a coarser grid
+        obou = dict(bou, **case["old_grid"])
+        oq = ini.couette_noise(obou, seed=case["seed"], amp=case["amp"])
+        continua.update(qt=interior(oq[0]), qr=interior(oq[1]), qz=interior(oq[2]), nth=int(obou["nthm"]) + 1,
+                        nr=int(obou["nrm"]) + 1, nz=int(obou["nzm"]) + 1)
     rt = fs.OneRank({"bou.in": bou_text(bou), "continua_master.h5": ""}, continua)
-    w = fs.World(ref_dir, FILES, MODULE_FILES, rt)
+    w = fs.World(ref_dir, FILES, MODULE_FILES, rt, capture_units=(97, 92), nan_fill=nan_fill)
     F, G = w.F, w.G
+    start = {}
+    orig_read = F.readflowfield
+
+    def readflowfield(*a):
+        r = orig_read(*a)
+        for k in ("qt", "qr", "qz"):
+            start[k] = np.ascontiguousarray(getattr(G, k).d.transpose(2, 1, 0)).copy()
+        if stop_after_read:
+            raise _Started(start)
+        return r
+
+    F.readflowfield = readflowfield
     rec = {"cfl": [], "time": [], "dt": [], "dmax": [], "vmax": [], "step_cfl": []}
     orig = {n: getattr(F, n) for n in ("timemarcher", "calcmaxcfl", "checkdivergence", "calcvelocitystats")}
 
@@ -198,6 +252,9 @@ def run_case(ref_dir, case, verbose=False):
     except fs.Quit as q:
         code = q.errorcode
     torques_out = [list(map(float, r)) for r in rt.written.get(97, [])]
+    nutes = [list(map(float, r)) for r in rt.written.get(92, [])]
+    stats = {n: np.ascontiguousarray(getattr(G, n).d.T) for n in STAT_NAMES} if case.get("stats") else {}
+    nsamples = int(G.nstatsamples)
     F.checkdivergence, F.calcmaxcfl = orig["checkdivergence"], orig["calcmaxcfl"]
     final_dmax = float(F.checkdivergence(0.0)[0])
     final_cfl = float(F.calcmaxcfl(0.0)[0])
@@ -224,6 +281,12 @@ def run_case(ref_dir, case, verbose=False):
                out_vmax=np.array(rec["vmax"]).reshape(-1, 3), errorcode=np.array(code), ntime=np.array(G.ntime),
                final_time=np.array(G.time), final_dmax=np.array(final_dmax), final_cfl=np.array(final_cfl),
                final_torque=np.array(final_torque)))
+    if case.get("stats"):
+        out["stat_samples"] = np.array(nsamples)
+        out["out_nute"] = np.array(nutes).reshape(-1, 2)
+        for n, a in stats.items():
+            out["stat_" + n] = a
+
     if verbose:
         print(f"{case['name']}: code {code}, ntime {G.ntime}, {len(rec['dt'])} steps, {time.time() - t0:.1f} s")
     return out
@@ -265,7 +328,8 @@ def main():
             arrays[f"{case['name']}/{k}"] = v
         meta = [m for m in meta if m["name"] != case["name"]]
         meta.append(dict(name=case["name"], seed=case["seed"], amp=case["amp"], bou=case["bou"],
-                         planes=case.get("planes")))
+                         planes=case.get("planes"), stats=bool(case.get("stats")),
+                         old_grid=case.get("old_grid")))
     order = [c["name"] for c in CASES]
     meta.sort(key=lambda m: order.index(m["name"]))
     np.savez_compressed(args.out + ".npz", **arrays)

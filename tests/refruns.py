@@ -35,7 +35,14 @@ def load():
 
 
 CASES, DATA = load()
-CASE_NAMES = [c["name"] for c in CASES]
+# runs of the main loop (the restart cases keep only their interpolated start)
+CASE_NAMES = [c["name"] for c in CASES if not c.get("old_grid")]
+STATS_CASES = [c["name"] for c in CASES if c.get("stats")]
+RESTART_CASES = [c["name"] for c in CASES if c.get("old_grid")]
+# statistics in the order of the fixture (StatRoutines.F90 names) and of
+# the library's STATS list
+STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
+              "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 
 
 def case(name):
@@ -56,17 +63,19 @@ def is_output_step(ntime, time, dt, tout):
     return ntime == 1 or math.fmod(time, tout) < dt
 
 
-def march(step, cfl, torque, c):
+def march(step, cfl, torque, c, stats=None):
     """Advance a simulation as main.F90:152-226 does, one step at a time.
 
     step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
-    cfl() and torque() are CalcMaxCFL and CalcTorque of the current state.
+    cfl() and torque() are CalcMaxCFL and CalcTorque of the current state;
+    stats(), when given, is CalcStats + CalcDissipation of an output step
+    after TSTA (main.F90:188-190), returning the dissipation number.
     Returns the per-step dt, time and CFL, the torques of the output steps,
-    the stop code and the index of the last step."""
+    the dissipation numbers, the stop code and the index of the last step."""
     bou = c["bou"]
     ntst = int(bou["ntst"])
     t, dt = 0.0, 0.0
-    rec = dict(dt=[], time=[], cfl=[], torque=[])
+    rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[])
     code, ntime = 0, 0
     for ntime in range(0, ntst + 1):
         rec["cfl"].append(cfl())
@@ -75,6 +84,8 @@ def march(step, cfl, torque, c):
         rec["time"].append(t)
         if is_output_step(ntime, t, dt, bou["tout"]):
             rec["torque"].append((t,) + tuple(torque()))
+            if stats is not None and t > bou["tsta"]:
+                rec["nute"].append((t, stats()))
         if code != 0:
             break
     rec["code"], rec["ntime"] = code, ntime
@@ -158,3 +169,29 @@ def scalar_errors(c, rec):
     assert tq.shape == rtq.shape, (tq.shape, rtq.shape)
     e["torque"] = max(relmax(tq[:, 1], rtq[:, 1]), relmax(tq[:, 2], rtq[:, 2])) if len(tq) else 0.0
     return e
+
+
+def stat_errors(c, stat, samples, rec):
+    """Relative errors of the accumulated statistics (stat(name) -> (nzm,
+    nrm) array in the library's naming), the sample count and the
+    dissipation records against the reference run.  pr_mean is compared
+    with the z-mean of every radial level removed (the singular mode's
+    offset depends on the radial index only); pr_rms, which squares that
+    offset into the field, is not compared."""
+    import tc_gb300 as tcg
+    name = c["name"]
+    assert samples == int(ref(name, "stat_samples")), (samples, int(ref(name, "stat_samples")))
+    out = {}
+    for lib_name, fname in zip(tcg.STATS, STAT_NAMES):
+        if fname == "pr_rms":
+            continue
+        a, b = stat(lib_name), ref(name, "stat_" + fname)
+        if fname == "pr_me":
+            a = a - a.mean(axis=0, keepdims=True)
+            b = b - b.mean(axis=0, keepdims=True)
+        out[lib_name] = relmax(a, b)
+    rn = ref(name, "out_nute")
+    nu = np.array(rec["nute"]).reshape(-1, 2)
+    assert nu.shape == rn.shape, (nu.shape, rn.shape)
+    out["nute"] = relmax(nu[:, 1], rn[:, 1])
+    return out

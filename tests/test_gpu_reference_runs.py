@@ -11,6 +11,8 @@ runs the loop) from the same seeded start and bou.in values:
 * the mixed forms (FP32 velocity side; FP64 or float-float pressure
   tridiagonals) on the production-like cases: velocities within 1e-3 of the
   velocity scale and torques within 1e-4 relative, each error printed;
+* the statistics case: CalcStats / CalcDissipation accumulations within
+  1e-10 of the reference's;
 * an ensemble holding every case that runs to NTST (grouped launches, FP64
   members of different shapes): each member within 1e-10 of its reference
   run.
@@ -56,6 +58,32 @@ def test_fp64_matches_reference_run(gpu_lib, name):
     rt = R.ref(name, "final_torque")
     assert abs(ti - rt[1]) <= TOL * abs(rt[1]) and abs(to - rt[2]) <= TOL * abs(rt[2])
     assert g.check_divergence() < c["bou"]["resid"]
+    g.close()
+
+
+@pytest.mark.parametrize("name", R.STATS_CASES)
+def test_fp64_statistics_match_reference_run(gpu_lib, name):
+    """CalcStats + CalcDissipation on the GPU at the output steps after TSTA
+    (main.F90:188-190): the accumulated theta averages, the sample count and
+    the dissipation numbers within 1e-10 of the reference's."""
+    c = R.case(name)
+    g = tc.TaylorCouette(c["bou"])
+    g.set_state(*R.start(c))
+
+    def step(ntime, t, dt):
+        code, _, t, dt = g.run(1, ntime, t, dt)
+        return code, t, dt
+
+    def stats():
+        g.calc_stats()
+        return g.calc_dissipation()
+
+    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, stats=stats)
+    assert rec["code"] == int(R.ref(name, "errorcode"))
+    err = R.stat_errors(c, g.stat, g.stat_samples, rec)
+    print(name, {k: f"{v:.1e}" for k, v in err.items()})
+    for k, v in err.items():
+        assert v <= TOL, (k, v)
     g.close()
 
 

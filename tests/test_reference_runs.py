@@ -61,6 +61,69 @@ def test_oracle_matches_reference_run(oracle, name):
     assert abs(o.calc_max_cfl() - float(R.ref(name, "final_cfl"))) <= TOL_S * float(R.ref(name, "final_cfl"))
 
 
+@pytest.mark.parametrize("name", R.STATS_CASES)
+def test_oracle_statistics_match_reference_run(oracle, name):
+    """CalcStats + CalcDissipation at the output steps after TSTA
+    (main.F90:188-190): the accumulated theta averages, the sample count and
+    the dissipation numbers within 1e-12 of the reference's (pr_mean, radial
+    profile removed, within the pressure tolerance)."""
+    import tc_gb300 as tcg
+    c = R.case(name)
+    o = oracle.CppOracle(c["bou"])
+    o.set_state(*R.start(c))
+
+    def step(ntime, t, dt):
+        return o.run(ntime, 1, t, dt)
+
+    def stats():
+        o.calc_stats()
+        return o.calc_dissipation()
+
+    rec = R.march(step, o.calc_max_cfl, o.calc_torque, c, stats=stats)
+    assert rec["code"] == int(R.ref(name, "errorcode"))
+    err = R.stat_errors(c, lambda n: o.stat(tcg.STATS.index(n)), o.stat_samples(), rec)
+    print(name, {k: f"{v:.1e}" for k, v in err.items()})
+    for k, v in err.items():
+        assert v <= (TOL_P if k == "pr_mean" else TOL_Q), (k, v)
+
+
+def write_old_continua(directory, c):
+    """The restart files of the restart case: the seeded start on the old
+    grid written as continua_*.h5 (interior cells, C order)."""
+    import tc_gb300 as tcg
+    import tc_gb300.initial as ini
+    obou = dict(c["bou"], **c["old_grid"])
+    oq = ini.couette_noise(obou, seed=c["seed"], amp=c["amp"])
+    nthm, nzm, nrm = obou["nthm"], obou["nzm"], obou["nrm"]
+    tcg.h5_write_scalars(os.path.join(directory, "continua_master.h5"),
+                         dict(nr=nrm + 1, nth=nthm + 1, nz=nzm + 1, time=0.0, rint=obou["rint"],
+                              rext=obou["rext"], istr=obou["istr"], str=obou["str"], alx3=obou["alx3"],
+                              lamb=obou["lamb"]), ints=("nr", "nth", "nz", "istr"))
+    for k, a in zip(("qt", "qr", "qz"), oq[:3]):
+        tcg.h5_write(os.path.join(directory, f"continua_{k}.h5"), "var", np.ascontiguousarray(a[1:-1, 1:-1, :]))
+
+
+@pytest.mark.parametrize("name", R.RESTART_CASES)
+def test_restart_interpolation_matches_reference_run(tmp_path, name):
+    """ReadFlowField + interp.F90 onto a finer grid (the reference's run read
+    continua files of the coarser grid): the library's loader gives the
+    reference's start bit for bit at every point the reference defines.
+    Where the reference's interpolation reads unset halo corners of the old
+    field (its value there depends on uninitialised memory) the fixture
+    holds a second run with those corners zeroed, and the loader matches
+    that run bit for bit too."""
+    from conftest import tc
+    c = R.case(name)
+    write_old_continua(str(tmp_path), c)
+    q = tc.h5_load_continua(c["bou"], str(tmp_path))[:3]
+    for k, a in zip(("qt", "qr", "qz"), q):
+        b, m = R.ref(name, "start_" + k), R.ref(name, "start_defined_" + k)
+        ai, bi, mi = a[1:-1, 1:-1], b[1:-1, 1:-1], m[1:-1, 1:-1]
+        assert mi.sum() > 0.9 * mi.size
+        np.testing.assert_array_equal(ai[mi], bi[mi], err_msg=k)
+        np.testing.assert_array_equal(ai[~mi], bi[~mi], err_msg=k)
+
+
 def test_cases_cover_the_stop_codes_and_forms():
     """The fixtures hold runs that end with 555 (NTST reached), 333 (TMAX)
     and 166 (dt below DTMIN), RK3 and AB2, the three radial grids, fixed and
@@ -74,6 +137,7 @@ def test_cases_cover_the_stop_codes_and_forms():
     assert any(b["minstrt"] * b["multmin"] != 0 for b in bous)
     assert any(b["dtmin"] < b["dtmax"] for b in bous) and any(b["dtmin"] == b["dtmax"] for b in bous)
     assert any((b["nthm"], b["nzm"], b["nrm"]) == (64, 64, 64) for b in bous)
+    assert R.STATS_CASES and R.RESTART_CASES
 
 
 REF_DIR = os.environ.get("TC_REFERENCE_DIR", "/root/reference")
