@@ -63,19 +63,25 @@ def is_output_step(ntime, time, dt, tout):
     return ntime == 1 or math.fmod(time, tout) < dt
 
 
-def march(step, cfl, torque, c, stats=None):
+def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
     """Advance a simulation as main.F90:152-226 does, one step at a time.
 
     step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
     cfl() and torque() are CalcMaxCFL and CalcTorque of the current state;
     stats(), when given, is CalcStats + CalcDissipation of an output step
-    after TSTA (main.F90:188-190), returning the dissipation number.
+    after TSTA (main.F90:188-190), returning the dissipation number;
+    vmax() and div(), when given, are the vmax of CalcVelocityStats and
+    CheckDivergence, recorded before the loop (div, main.F90:125) and at
+    every output step (main.F90:181,185).
     Returns the per-step dt, time and CFL, the torques of the output steps,
-    the dissipation numbers, the stop code and the index of the last step."""
+    the dissipation numbers, vmax and divergence records, the stop code and
+    the index of the last step."""
     bou = c["bou"]
     ntst = int(bou["ntst"])
     t, dt = 0.0, 0.0
-    rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[])
+    rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[], vmax=[], dmax=[])
+    if div is not None:
+        rec["dmax"].append(div())
     code, ntime = 0, 0
     for ntime in range(0, ntst + 1):
         rec["cfl"].append(cfl())
@@ -83,6 +89,10 @@ def march(step, cfl, torque, c, stats=None):
         rec["dt"].append(dt)
         rec["time"].append(t)
         if is_output_step(ntime, t, dt, bou["tout"]):
+            if vmax is not None:
+                rec["vmax"].append(tuple(vmax()))
+            if div is not None:
+                rec["dmax"].append(div())
             rec["torque"].append((t,) + tuple(torque()))
             if stats is not None and t > bou["tsta"]:
                 rec["nute"].append((t, stats()))
@@ -168,6 +178,17 @@ def scalar_errors(c, rec):
     tq = np.array(rec["torque"]).reshape(-1, 3)
     assert tq.shape == rtq.shape, (tq.shape, rtq.shape)
     e["torque"] = max(relmax(tq[:, 1], rtq[:, 1]), relmax(tq[:, 2], rtq[:, 2])) if len(tq) else 0.0
+    if rec["vmax"]:
+        vm, rvm = np.array(rec["vmax"]), ref(name, "out_vmax")
+        assert vm.shape == rvm.shape, (vm.shape, rvm.shape)
+        e["vmax"] = max(relmax(vm[:, i], rvm[:, i]) for i in range(3))
+    if rec["dmax"]:
+        # the start's divergence (O(1) for the seeded noise) relative; after
+        # the projection both sides hold roundoff, compared against the
+        # start's value
+        dm, rdm = np.array(rec["dmax"]), ref(name, "out_dmax")
+        assert dm.shape == rdm.shape, (dm.shape, rdm.shape)
+        e["dmax"] = float(np.abs(dm - rdm).max()) / float(rdm[0])
     return e
 
 

@@ -6,7 +6,8 @@ runs the loop) from the same seeded start and bou.in values:
 
 * FP64 (the drop-in): velocities and pressure (radial profile of the
   singular mode removed) within 1e-10 of the reference's, the dt sequence,
-  step times, CFL numbers and output-step torques within 1e-10 relative,
+  step times, CFL numbers, output-step torques, CalcVelocityStats maxima
+  and CheckDivergence maxima within 1e-10 relative,
   the same stop code at the same step;
 * the mixed forms (FP32 velocity side; FP64 or float-float pressure
   tridiagonals) on the production-like cases: velocities within 1e-3 of the
@@ -39,7 +40,8 @@ def gpu_march(c, precision="fp64"):
         code, _, t, dt = g.run(1, ntime, t, dt)
         return code, t, dt
 
-    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c)
+    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, vmax=lambda: g.velocity_stats()[0],
+                  div=g.check_divergence)
     return g, rec
 
 

@@ -8,8 +8,10 @@ compared with what the reference computed:
 * velocities: 1e-12 of each field's maximum (measured: below 3e-14);
 * pressure with the radial profile of the singular mode removed: 1e-11 of
   max |pr| (measured: below 2e-13);
-* the dt sequence, the step times, the CFL numbers behind dt and the
-  CalcTorque records of the output steps: 1e-12 relative;
+* the dt sequence, the step times, the CFL numbers behind dt, the
+  CalcTorque records and the CalcVelocityStats maxima of the output steps:
+  1e-12 relative; the CheckDivergence maxima (the start's and, after the
+  projection, the output steps' roundoff) within 1e-12 of the start's;
 * the stop code and the index of the last step: equal;
 * the final CheckDivergence below RESID in both.
 
@@ -35,7 +37,8 @@ def oracle_march(oracle, c):
     def step(ntime, t, dt):
         return o.run(ntime, 1, t, dt)
 
-    rec = R.march(step, o.calc_max_cfl, o.calc_torque, c)
+    rec = R.march(step, o.calc_max_cfl, o.calc_torque, c, vmax=lambda: o.velocity_stats()[0],
+                  div=o.check_divergence)
     return o, rec
 
 
