@@ -1221,6 +1221,13 @@ class Gen:
         fmt = cparts[1].strip() if len(cparts) > 1 else "*"
         its = [x.strip() for x in _split_top(items) if x.strip()] if items else []
         if kind == "write":
+            if re.fullmatch(r"[a-z_]\w*", unit) and self.vtype(unit) == "s":
+                # internal WRITE into a character variable
+                vals = [self.ex(parse_expr(x))[0] for x in its]
+                tmp = self.newtmp()
+                self.emit(f"{tmp} = R.internal_write({self.format_text(fmt)!r}, [{', '.join(vals)}])")
+                self.assign_target(parse_expr(unit), (tmp, "s", 0))
+                return
             if unit.isdigit() and int(unit) in self.w.capture_units:
                 vals = []
                 for x in its:
@@ -1232,6 +1239,26 @@ class Gen:
                 self.emit("pass")
             return
         if kind == "read":
+            if len(its) == 1 and its[0].startswith("(") and _top_assign(its[0][1:-1]) >= 0:
+                # one implied-DO list: (target, var = lo, hi)
+                parts = [x.strip() for x in _split_top(its[0][1:-1])]
+                if len(parts) != 3:
+                    raise SyntaxError(f"{self.u.name}: implied-DO list {its[0]}")
+                tnode = parse_expr(parts[0])
+                var, lo = [x.strip() for x in parts[1].split("=", 1)]
+                hi = self.ex(parse_expr(parts[2]))[0]
+                lo = self.ex(parse_expr(lo))[0]
+                nm = tnode[1] if tnode[0] == "name" else tnode[1][1]
+                rng, vals, k = self.newtmp(), self.newtmp(), self.newtmp()
+                _, where = self.var(var)
+                loopv = f"G.{var}" if where == "module" else f"v_{var}"
+                self.emit(f"{rng} = _frange({lo}, {hi}, 1)")
+                self.emit(f"{vals} = R.read({unit}, {fmt!r}, [{self.vtype(nm)!r}] * len({rng}))")
+                self.emit(f"for {k}, {loopv} in enumerate({rng}):")
+                self.ind += 1
+                self.assign_target(tnode, (f"{vals}[{k}]", None, 0))
+                self.ind -= 1
+                return
             targets = [parse_expr(x) for x in its]
             tmp = self.newtmp()
             types_ = []
@@ -1243,6 +1270,18 @@ class Gen:
                 self.assign_target(tnode, (f"{tmp}[{i}]", None, 0))
             return
         self.emit("pass")
+
+    def format_text(self, fmt):
+        """The edit descriptors of a WRITE: a FORMAT statement of this unit
+        by its label, or a character constant."""
+        if fmt.isdigit():
+            for _, label, text in self.u.body:
+                if label == int(fmt) and re.match(r"^format\s*\(", text):
+                    return text[text.index("("):].strip()
+            raise SyntaxError(f"{self.u.name}: no FORMAT labelled {fmt}")
+        if fmt[:1] in "'\"" and fmt[-1:] == fmt[:1]:
+            return fmt[1:-1]
+        raise SyntaxError(f"{self.u.name}: format {fmt}")
 
     def gen_allocate(self, text, dealloc=False):
         inner = text[text.index("(") + 1:text.rindex(")")]
@@ -1437,7 +1476,7 @@ class Gen:
                     kw[a.strip()] = self.ex(parse_expr(b))[0]
             self.emit(f"R.open({kw.get('unit', '0')}, {kw.get('file', repr(''))})")
             return i + 1
-        if re.match(r"^close\s*\(", text):
+        if re.match(r"^(close|rewind)\s*\(", text):
             self.emit("pass")
             return i + 1
         m = re.match(r"^inquire\s*\((.*)\)$", text)
@@ -1678,6 +1717,7 @@ class OneRank:
         self.continua = continua        # 'qt'/'qr'/'qz' -> (nr, nzm, nthm) arrays; 'time' etc.
         self.units = {}
         self.written = {}
+        self.h5 = {}                    # file name -> {dataset: C-order array}, what the run wrote
         self.world = None
 
     # ---- declarations the translated code sees as module variables
@@ -1723,7 +1763,11 @@ class OneRank:
             hdfstart=self.none, hdfclose=self.none, openlogs=self.none, writegridinfo=self.none,
             initdumprcuts=self.none, hdfserialreadintscalar=self.read_scalar,
             hdfserialreadrealscalar=self.read_scalar, hdfreadcontinua=self.read_continua,
+            hdfcreateblankfile=self.h5_blank, hdfserialwriterealscalar=self.h5_scalar,
+            hdfserialwriteintscalar=self.h5_int_scalar, hdfserialwritereal1d=self.h5_1d,
+            hdfwritereal2d=self.h5_2d_slab, hdfwriteserialreal2d=self.h5_2d, hdfwriterealhalo3d=self.h5_halo_3d,
             quitroutine=self.quit, mpi_wtime=lambda: 0.0)
+        self.F = F
         for name, fn in stubs.items():
             if not hasattr(F, name):
                 setattr(F, name, fn)
@@ -1740,6 +1784,12 @@ class OneRank:
         raise FortranStop("MpiAbort")
 
     def quit(self, tin, normalexit, errorcode):
+        """QuitRoutine.F90:10-43: a normal exit writes the statistics and the
+        continuation files (WriteStats, WriteFlowField) before the stop."""
+        if int(errorcode) != 100 and normalexit:
+            for name in ("writestats", "writeflowfield"):
+                if hasattr(self.F, name):
+                    getattr(self.F, name)()
         raise Quit(errorcode, normalexit)
 
     # ---- 2DECOMP&FFT
@@ -1871,7 +1921,77 @@ class OneRank:
         d[1 - o[0]:n3o + 1 - o[0], xs2 - o[1]:xe2 + 1 - o[1], xs3 - o[2]:xe3 + 1 - o[2]] = src
         return None
 
+    # ---- HDF5 output files: the datasets each write leaves in its file
+    # (HdfRoutines.F90), C order (the reverse of the Fortran dims), copied
+    # (the written arrays are often locals that the next call reuses)
+    @staticmethod
+    def _h5_name(filename):
+        return os.path.normpath(str(filename).strip())
+
+    def _h5_open(self, filename):
+        """h5fopen_f(H5F_ACC_RDWR_F): the file must exist."""
+        name = self._h5_name(filename)
+        if name not in self.h5:
+            raise RuntimeError(f"HDF5 file {name} opened for writing before it was created")
+        return self.h5[name]
+
+    def _h5_create(self, filename):
+        """h5fcreate_f(H5F_ACC_TRUNC_F): a new, empty file."""
+        self.h5[self._h5_name(filename)] = {}
+        return self.h5[self._h5_name(filename)]
+
+    def h5_blank(self, filename):
+        """HdfCreateBlankFile (HdfRoutines.F90:11-22)."""
+        self._h5_create(filename)
+
+    def h5_scalar(self, dsetname, filename, n):
+        """HdfSerialWriteRealScalar (HdfRoutines.F90:25-59): dims (1)."""
+        self._h5_open(filename)[str(dsetname).strip()] = np.array([float(n)])
+
+    def h5_int_scalar(self, dsetname, filename, n):
+        """HdfSerialWriteIntScalar (HdfRoutines.F90:62-96): dims (1), integer."""
+        self._h5_open(filename)[str(dsetname).strip()] = np.array([int(n)], dtype=np.int32)
+
+    def h5_1d(self, dsetname, filename, var, sz):
+        """HdfSerialWriteReal1D (HdfRoutines.F90:99-137): var(1:sz)."""
+        self._h5_open(filename)[str(dsetname).strip()] = np.array(var.d.reshape(-1, order="F")[:int(sz)], copy=True)
+
+    def h5_2d_slab(self, dsetname, filename, var):
+        """HdfWriteReal2D (HdfRoutines.F90:139-214): a new file holding
+        var(xstart(2):xend(2), xstart(3):xend(3)), dims (nzm, nthm)."""
+        self._h5_create(filename)[str(dsetname).strip()] = np.array(var.d.T, order="C", copy=True)
+
+    def h5_2d(self, filename, dsetname, ndx, ndy, var):
+        """HdfWriteSerialReal2D (HdfRoutines.F90:533-566): a new file
+        holding var(ndx, ndy)."""
+        a = var.d.reshape(-1, order="F")[:int(ndx) * int(ndy)].reshape((int(ndx), int(ndy)), order="F")
+        self._h5_create(filename)[str(dsetname).strip()] = np.array(a.T, order="C", copy=True)
+
+    def h5_halo_3d(self, filnam1, qua):
+        """HdfWriteRealHalo3D (HdfRoutines.F90:388-477): a new file holding
+        dataset 'var' = qua(1:nr, xstart(2):xend(2), xstart(3):xend(3)) of
+        the haloed array (1:nr, 0:nzm+1, 0:nthm+1)."""
+        self._h5_create(filnam1)["var"] = np.array(qua.d[:, 1:-1, 1:-1].transpose(2, 1, 0), order="C", copy=True)
+
     # ---- formatted I/O
+    @staticmethod
+    def internal_write(fmt, values):
+        """WRITE into a character variable with I edit descriptors only
+        (Iw, Iw.m: right-justified in w columns, at least m digits)."""
+        descs = [d.strip() for d in fmt.strip()[1:-1].split(",")]
+        if len(descs) != len(values):
+            raise RuntimeError(f"internal WRITE {fmt} of {len(values)} values")
+        out = []
+        for d, v in zip(descs, values):
+            m = re.fullmatch(r"i(\d+)(?:\.(\d+))?", d)
+            if not m:
+                raise RuntimeError(f"internal WRITE: edit descriptor {d}")
+            w, mn = int(m.group(1)), int(m.group(2) or 1)
+            digits = str(abs(int(v))).rjust(mn, "0")
+            txt = ("-" if int(v) < 0 else "") + digits
+            out.append("*" * w if len(txt) > w else txt.rjust(w))
+        return "".join(out)
+
     def open(self, unit, name):
         """OPEN: a file the caller supplied is read; any other name opens
         an output unit (what is written to it is dropped unless its unit

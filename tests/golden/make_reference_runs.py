@@ -55,7 +55,8 @@ FILES = ["main.F90", "ReadInputFile.F90", "InitTimeMarchScheme.F90", "InitVariab
          "SolveImpEqnUpdate_QT.F90", "SolveImpEqnUpdate_QR.F90", "SolveImpEqnUpdate_QZ.F90",
          "CalcLocalDivergence.F90", "SolvePressureCorrection.F90", "CorrectVelocity.F90", "CorrectPressure.F90",
          "CalcVelocityStats.F90", "CalcTorque.F90", "AuxiliaryRoutines.F90", "StatRoutines.F90",
-         "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90"]
+         "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90", "StatReadReduceWrite.F90", "WriteFlowField.F90",
+         "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90"]
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
               "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 MODULE_FILES = ["param.F90"]
@@ -147,8 +148,12 @@ CASES = [
          bou=base_bou(nthm=64, nzm=64, nrm=64, ntst=4)),
     # statistics on (TSTA = 0): main.F90 calls CalcStats (with
     # CalcVorticity) and CalcDissipation at every output step
-    dict(name="statistics_every_2_steps", seed=22, amp=0.05, stats=True,
-         bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9)),
+    # statistics every output step, radial/theta/streamwise-average slabs
+    # every other one, full-field dumps every third; the files the run
+    # writes (dumps, WriteStats and WriteFlowField at the stop) are kept
+    dict(name="statistics_and_dumps", seed=22, amp=0.05, stats=True, files=True, rcuts=[1.05, 1.23],
+         bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
+                      nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
     # a restart from continua files of a coarser grid: ReadFlowField
     # interpolates them (interp.F90) onto the run's grid; the start is kept
     dict(name="restart_interpolated_from_coarser_grid", seed=23, amp=0.05,
@@ -199,7 +204,11 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         oq = ini.couette_noise(obou, seed=case["seed"], amp=case["amp"])
         continua.update(qt=interior(oq[0]), qr=interior(oq[1]), qz=interior(oq[2]), nth=int(obou["nthm"]) + 1,
                         nr=int(obou["nrm"]) + 1, nz=int(obou["nzm"]) + 1)
-    rt = fs.OneRank({"bou.in": bou_text(bou), "continua_master.h5": ""}, continua)
+    files = {"bou.in": bou_text(bou), "continua_master.h5": ""}
+    if case.get("rcuts"):
+        # rcuts.in: a header record, then the radii of the slabs (InitDumpRCuts)
+        files["rcuts.in"] = " RCUT\n  " + "   ".join(repr(float(r)) for r in case["rcuts"]) + "\n"
+    rt = fs.OneRank(files, continua)
     w = fs.World(ref_dir, FILES, MODULE_FILES, rt, capture_units=(97, 92), nan_fill=nan_fill)
     F, G = w.F, w.G
     start = {}
@@ -281,6 +290,10 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
                out_vmax=np.array(rec["vmax"]).reshape(-1, 3), errorcode=np.array(code), ntime=np.array(G.ntime),
                final_time=np.array(G.time), final_dmax=np.array(final_dmax), final_cfl=np.array(final_cfl),
                final_torque=np.array(final_torque)))
+    if case.get("files"):
+        for fname, dsets in sorted(rt.h5.items()):
+            for dname, a in dsets.items():
+                out[f"h5:{fname}:{dname}"] = a
     if case.get("stats"):
         out["stat_samples"] = np.array(nsamples)
         out["out_nute"] = np.array(nutes).reshape(-1, 2)
@@ -319,7 +332,11 @@ def main():
             old = {k: z[k] for k in z.files}
         with open(args.out + ".json") as f:
             meta = [m for m in json.load(f)["cases"] if m["name"] != args.only]
-    arrays.update(old)
+    # keep the other cases of the committed fixture (no stale keys of cases
+    # that are gone or of the case being rerun)
+    names = [c["name"] for c in CASES]
+    arrays.update({k: v for k, v in old.items() if k.split("/")[0] in names and k.split("/")[0] != args.only})
+    meta = [m for m in meta if m["name"] in names]
     for case in CASES:
         if args.only and case["name"] != args.only:
             continue
@@ -329,7 +346,7 @@ def main():
         meta = [m for m in meta if m["name"] != case["name"]]
         meta.append(dict(name=case["name"], seed=case["seed"], amp=case["amp"], bou=case["bou"],
                          planes=case.get("planes"), stats=bool(case.get("stats")),
-                         old_grid=case.get("old_grid")))
+                         files=bool(case.get("files")), rcuts=case.get("rcuts"), old_grid=case.get("old_grid")))
     order = [c["name"] for c in CASES]
     meta.sort(key=lambda m: order.index(m["name"]))
     np.savez_compressed(args.out + ".npz", **arrays)

@@ -39,6 +39,7 @@ CASES, DATA = load()
 CASE_NAMES = [c["name"] for c in CASES if not c.get("old_grid")]
 STATS_CASES = [c["name"] for c in CASES if c.get("stats")]
 RESTART_CASES = [c["name"] for c in CASES if c.get("old_grid")]
+FILES_CASES = [c["name"] for c in CASES if c.get("files")]
 # statistics in the order of the fixture (StatRoutines.F90 names) and of
 # the library's STATS list
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
@@ -68,8 +69,9 @@ def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
 
     step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
     cfl() and torque() are CalcMaxCFL and CalcTorque of the current state;
-    stats(), when given, is CalcStats + CalcDissipation of an output step
-    after TSTA (main.F90:188-190), returning the dissipation number;
+    stats(time, dt), when given, is what an output step after TSTA runs
+    (main.F90:188-198: CalcStats, CalcDissipation and the dumps due at
+    that time), returning the dissipation number;
     vmax() and div(), when given, are the vmax of CalcVelocityStats and
     CheckDivergence, recorded before the loop (div, main.F90:125) and at
     every output step (main.F90:181,185).
@@ -95,7 +97,7 @@ def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
                 rec["dmax"].append(div())
             rec["torque"].append((t,) + tuple(torque()))
             if stats is not None and t > bou["tsta"]:
-                rec["nute"].append((t, stats()))
+                rec["nute"].append((t, stats(t, dt)))
         if code != 0:
             break
     rec["code"], rec["ntime"] = code, ntime
@@ -215,4 +217,16 @@ def stat_errors(c, stat, samples, rec):
     nu = np.array(rec["nute"]).reshape(-1, 2)
     assert nu.shape == rn.shape, (nu.shape, rn.shape)
     out["nute"] = relmax(nu[:, 1], rn[:, 1])
+    return out
+
+
+def h5_files(name):
+    """The HDF5 files the reference run wrote: path (relative to the run's
+    directory) -> {dataset: array}."""
+    out = {}
+    pre = f"{name}/h5:"
+    for k, v in DATA.items():
+        if k.startswith(pre):
+            path, dset = k[len(pre):].rsplit(":", 1)
+            out.setdefault(path, {})[dset] = v
     return out

@@ -13,7 +13,9 @@ runs the loop) from the same seeded start and bou.in values:
   tridiagonals) on the production-like cases: velocities within 1e-3 of the
   velocity scale and torques within 1e-4 relative, each error printed;
 * the statistics case: CalcStats / CalcDissipation accumulations within
-  1e-10 of the reference's;
+  1e-10 of the reference's, and every HDF5 file the reference run wrote
+  (slab and full-field dumps, statistics, continuation files) written
+  by the library with the same names, datasets and values;
 * an ensemble holding every case that runs to NTST (grouped launches, FP64
   members of different shapes): each member within 1e-10 of its reference
   run.
@@ -76,7 +78,7 @@ def test_fp64_statistics_match_reference_run(gpu_lib, name):
         code, _, t, dt = g.run(1, ntime, t, dt)
         return code, t, dt
 
-    def stats():
+    def stats(t, dt):
         g.calc_stats()
         return g.calc_dissipation()
 
@@ -87,6 +89,75 @@ def test_fp64_statistics_match_reference_run(gpu_lib, name):
     for k, v in err.items():
         assert v <= TOL, (k, v)
     g.close()
+
+
+@pytest.mark.parametrize("name", R.FILES_CASES)
+def test_output_files_match_reference_run(gpu_lib, tmp_path, name):
+    """The HDF5 files of the reference run, written by the library from the
+    GPU run at the same points of the loop: the radial, theta and
+    streamwise-average slabs every TFRAME2D and the full fields every
+    TFRAME3D of the output steps after TSTA (main.F90:188-198: DumpRCuts,
+    DumpThCuts, DumpStreamwiseAvg, DumpFlowField), and WriteStats and
+    WriteFlowField at the stop (QuitRoutine.F90:27-30).  The same file
+    names, the same datasets in each file with the same shapes and types
+    (32-bit integers, 64-bit reals), integers equal, reals within 1e-10 of each dataset's maximum (pr_mean with the
+    z-mean of every radial level removed, as for the pressure; pr_rms,
+    which squares the singular mode's offset in, is compared by shape)."""
+    import math
+    import os
+    from test_h5 import walk
+    c = R.case(name)
+    bou = c["bou"]
+    g = tc.TaylorCouette(bou)
+    g.set_state(*R.start(c))
+    d = str(tmp_path)
+    sub = {k: os.path.join(d, k) for k in ("rcuts", "thcut", "stave", "fullff", "stats")}
+    for v in sub.values():
+        os.makedirs(v)
+
+    def step(ntime, t, dt):
+        code, _, t, dt = g.run(1, ntime, t, dt)
+        return code, t, dt
+
+    def stats(t, dt):
+        g.calc_stats()
+        nute = g.calc_dissipation()
+        if math.fmod(t, bou["tframe2d"]) < dt:
+            g.dump_rcuts(sub["rcuts"], t, c["rcuts"])
+            g.dump_thcuts(sub["thcut"], t)
+            g.dump_streamwise_avg(sub["stave"], t)
+        if math.fmod(t, bou["tframe3d"]) < dt:
+            g.dump_flow_field(sub["fullff"], t)
+        return nute
+
+    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, stats=stats)
+    assert rec["code"] == int(R.ref(name, "errorcode")) == 555
+    g.write_stats(sub["stats"])
+    g.write_continua(d, rec["time"][-1])
+    g.close()
+    want = R.h5_files(name)
+    got = {os.path.relpath(os.path.join(r, f), d) for r, _, fs in os.walk(d) for f in fs if f.endswith(".h5")}
+    assert got == set(want), (sorted(got ^ set(want)))
+    worst = {}
+    for path, dsets in want.items():
+        mine = walk(os.path.join(d, path))
+        assert set(mine) == set(dsets), (path, sorted(mine), sorted(dsets))
+        for k, b in dsets.items():
+            a = mine[k][2]
+            assert a.shape == b.shape, (path, k, a.shape, b.shape)
+            assert mine[k][1] == ("<i4" if b.dtype.kind == "i" else "<f8"), (path, k, mine[k][1])
+            if b.dtype.kind == "i":
+                assert np.array_equal(a, b), (path, k, a, b)
+                continue
+            if k == "pr_rms":
+                continue
+            if k == "pr_mean":
+                a = a - a.mean(axis=0, keepdims=True)
+                b = b - b.mean(axis=0, keepdims=True)
+            worst[f"{path}:{k}"] = R.relmax(a, b)
+    print(name, len(want), "files;", "worst", max(worst.items(), key=lambda kv: kv[1]))
+    for k, v in worst.items():
+        assert v <= TOL, (k, v)
 
 
 @pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])

@@ -78,7 +78,7 @@ def test_oracle_statistics_match_reference_run(oracle, name):
     def step(ntime, t, dt):
         return o.run(ntime, 1, t, dt)
 
-    def stats():
+    def stats(t, dt):
         o.calc_stats()
         return o.calc_dissipation()
 
