@@ -13,7 +13,8 @@ continua path (pressure zero), and runs until the reference's QuitRoutine
 * per step: time and dt after the step, and the CFL number of the
   CalcMaxCFL call at the top of the step (the one its dt rule used);
 * per output step (main.F90: ntime = 1 or mod(time, tout) < dt): the
-  CalcTorque record (time, inner, outer) and vmax of CalcVelocityStats;
+  CalcTorque record (time, inner, outer) and vmax of CalcVelocityStats
+  and its rms_vel.out record (time, qt, qr, qz rms);
   the CheckDivergence maxima (the first one is the check before the loop);
 * the error code and ntime of the stop;
 * after the stop: CalcTorque, CheckDivergence and CalcMaxCFL of the final
@@ -56,7 +57,7 @@ FILES = ["main.F90", "ReadInputFile.F90", "InitTimeMarchScheme.F90", "InitVariab
          "CalcLocalDivergence.F90", "SolvePressureCorrection.F90", "CorrectVelocity.F90", "CorrectPressure.F90",
          "CalcVelocityStats.F90", "CalcTorque.F90", "AuxiliaryRoutines.F90", "StatRoutines.F90",
          "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90", "StatReadReduceWrite.F90", "WriteFlowField.F90",
-         "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90"]
+         "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90", "WriteGridInfo.F90"]
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
               "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 MODULE_FILES = ["param.F90"]
@@ -209,7 +210,7 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         # rcuts.in: a header record, then the radii of the slabs (InitDumpRCuts)
         files["rcuts.in"] = " RCUT\n  " + "   ".join(repr(float(r)) for r in case["rcuts"]) + "\n"
     rt = fs.OneRank(files, continua)
-    w = fs.World(ref_dir, FILES, MODULE_FILES, rt, capture_units=(97, 92), nan_fill=nan_fill)
+    w = fs.World(ref_dir, FILES, MODULE_FILES, rt, capture_units=(97, 92, 98), nan_fill=nan_fill)
     F, G = w.F, w.G
     start = {}
     orig_read = F.readflowfield
@@ -287,7 +288,8 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
             out.update(field_sums(k, v))
     out.update(dict(step_time=np.array(rec["time"]), step_dt=np.array(rec["dt"]), step_cfl=np.array(rec["step_cfl"]),
                out_torque=np.array(torques_out).reshape(-1, 3), out_dmax=np.array(rec["dmax"]),
-               out_vmax=np.array(rec["vmax"]).reshape(-1, 3), errorcode=np.array(code), ntime=np.array(G.ntime),
+               out_vmax=np.array(rec["vmax"]).reshape(-1, 3),
+               out_rms=np.array([list(map(float, r)) for r in rt.written.get(98, [])]).reshape(-1, 4), errorcode=np.array(code), ntime=np.array(G.ntime),
                final_time=np.array(G.time), final_dmax=np.array(final_dmax), final_cfl=np.array(final_cfl),
                final_torque=np.array(final_torque)))
     if case.get("files"):

@@ -64,7 +64,7 @@ def is_output_step(ntime, time, dt, tout):
     return ntime == 1 or math.fmod(time, tout) < dt
 
 
-def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
+def march(step, cfl, torque, c, stats=None, vstats=None, div=None):
     """Advance a simulation as main.F90:152-226 does, one step at a time.
 
     step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
@@ -72,16 +72,16 @@ def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
     stats(time, dt), when given, is what an output step after TSTA runs
     (main.F90:188-198: CalcStats, CalcDissipation and the dumps due at
     that time), returning the dissipation number;
-    vmax() and div(), when given, are the vmax of CalcVelocityStats and
-    CheckDivergence, recorded before the loop (div, main.F90:125) and at
-    every output step (main.F90:181,185).
+    vstats() and div(), when given, are CalcVelocityStats (vmax, rms) and
+    CheckDivergence, recorded at every output step (main.F90:181,185) and,
+    for div, before the loop (main.F90:125).
     Returns the per-step dt, time and CFL, the torques of the output steps,
     the dissipation numbers, vmax and divergence records, the stop code and
     the index of the last step."""
     bou = c["bou"]
     ntst = int(bou["ntst"])
     t, dt = 0.0, 0.0
-    rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[], vmax=[], dmax=[])
+    rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[], vmax=[], rms=[], dmax=[])
     if div is not None:
         rec["dmax"].append(div())
     code, ntime = 0, 0
@@ -91,8 +91,10 @@ def march(step, cfl, torque, c, stats=None, vmax=None, div=None):
         rec["dt"].append(dt)
         rec["time"].append(t)
         if is_output_step(ntime, t, dt, bou["tout"]):
-            if vmax is not None:
-                rec["vmax"].append(tuple(vmax()))
+            if vstats is not None:
+                vm, rms = vstats()
+                rec["vmax"].append(tuple(vm))
+                rec["rms"].append((t,) + tuple(rms))
             if div is not None:
                 rec["dmax"].append(div())
             rec["torque"].append((t,) + tuple(torque()))
@@ -184,6 +186,10 @@ def scalar_errors(c, rec):
         vm, rvm = np.array(rec["vmax"]), ref(name, "out_vmax")
         assert vm.shape == rvm.shape, (vm.shape, rvm.shape)
         e["vmax"] = max(relmax(vm[:, i], rvm[:, i]) for i in range(3))
+        rr, rrr = np.array(rec["rms"]), ref(name, "out_rms")
+        assert rr.shape == rrr.shape, (rr.shape, rrr.shape)
+        # (the values the reference wrote to rms_vel.out, before formatting)
+        e["rms"] = max(relmax(rr[:, i], rrr[:, i]) for i in range(1, 4))
     if rec["dmax"]:
         # the start's divergence (O(1) for the seeded noise) relative; after
         # the projection both sides hold roundoff, compared against the

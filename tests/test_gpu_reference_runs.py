@@ -42,7 +42,7 @@ def gpu_march(c, precision="fp64"):
         code, _, t, dt = g.run(1, ntime, t, dt)
         return code, t, dt
 
-    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, vmax=lambda: g.velocity_stats()[0],
+    rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, vstats=g.velocity_stats,
                   div=g.check_divergence)
     return g, rec
 
@@ -97,8 +97,9 @@ def test_output_files_match_reference_run(gpu_lib, tmp_path, name):
     GPU run at the same points of the loop: the radial, theta and
     streamwise-average slabs every TFRAME2D and the full fields every
     TFRAME3D of the output steps after TSTA (main.F90:188-198: DumpRCuts,
-    DumpThCuts, DumpStreamwiseAvg, DumpFlowField), and WriteStats and
-    WriteFlowField at the stop (QuitRoutine.F90:27-30).  The same file
+    DumpThCuts, DumpStreamwiseAvg, DumpFlowField), WriteStats and
+    WriteFlowField at the stop (QuitRoutine.F90:27-30), and the grid file
+    of WriteGridInfo.  The same file
     names, the same datasets in each file with the same shapes and types
     (32-bit integers, 64-bit reals), integers equal, reals within 1e-10 of each dataset's maximum (pr_mean with the
     z-mean of every radial level removed, as for the pressure; pr_rms,
@@ -134,6 +135,7 @@ def test_output_files_match_reference_run(gpu_lib, tmp_path, name):
     assert rec["code"] == int(R.ref(name, "errorcode")) == 555
     g.write_stats(sub["stats"])
     g.write_continua(d, rec["time"][-1])
+    tc.h5_write_grid_info(bou, d)
     g.close()
     want = R.h5_files(name)
     got = {os.path.relpath(os.path.join(r, f), d) for r, _, fs in os.walk(d) for f in fs if f.endswith(".h5")}

@@ -37,7 +37,7 @@ def oracle_march(oracle, c):
     def step(ntime, t, dt):
         return o.run(ntime, 1, t, dt)
 
-    rec = R.march(step, o.calc_max_cfl, o.calc_torque, c, vmax=lambda: o.velocity_stats()[0],
+    rec = R.march(step, o.calc_max_cfl, o.calc_torque, c, vstats=o.velocity_stats,
                   div=o.check_divergence)
     return o, rec
 
@@ -125,6 +125,22 @@ def test_restart_interpolation_matches_reference_run(tmp_path, name):
         assert mi.sum() > 0.9 * mi.size
         np.testing.assert_array_equal(ai[mi], bi[mi], err_msg=k)
         np.testing.assert_array_equal(ai[~mi], bi[~mi], err_msg=k)
+
+
+@pytest.mark.parametrize("name", R.FILES_CASES)
+def test_grid_info_file_matches_reference_run(tmp_path, name):
+    """WriteGridInfo (cordin_info.h5: rm, rc, tm, zm of CreateGrid) as the
+    reference run wrote it: the same datasets, bit for bit."""
+    from conftest import tc
+    from test_h5 import walk
+    c = R.case(name)
+    tc.h5_write_grid_info(c["bou"], str(tmp_path))
+    mine = walk(str(tmp_path / "cordin_info.h5"))
+    want = R.h5_files(name)["cordin_info.h5"]
+    assert set(mine) == set(want)
+    for k, b in want.items():
+        assert mine[k][1] == "<f8"
+        np.testing.assert_array_equal(mine[k][2], b, err_msg=k)
 
 
 def test_cases_cover_the_stop_codes_and_forms():
