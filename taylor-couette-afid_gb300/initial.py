@@ -1,9 +1,10 @@
 """Seeded Couette-plus-noise initial fields in the reference layout.
 
 The reference has no random initial condition (CreateInitialConditions.F90:26-43
-builds deterministic sinusoids with qt = 0); it reads other starts through the
-NREAD=1 continuation path (ReadFlowField.F90:135-140) with the pressure left at
-zero.  This module builds such a start:
+builds deterministic sinusoids with qt = 0, restated here by
+create_initial_conditions); it reads other starts through the NREAD=1
+continuation path (ReadFlowField.F90:135-140) with the pressure left at zero.
+couette_noise builds such a start:
 
 * qt = A*rm_k + B/rm_k + amp*U, with A, B the laminar circular-Couette
   coefficients the reference computes at CreateInitialConditions.F90:21-23;
@@ -77,6 +78,44 @@ def fill_halo(a: np.ndarray) -> None:
     a[:, 0, :] = a[:, -2, :]
     a[-1, :, :] = a[1, :, :]
     a[0, :, :] = a[-2, :, :]
+
+
+def create_initial_conditions(bou: dict):
+    """The reference's own start for NREAD = 0 (CreateInitialConditions.F90:18-43
+    with the halo update of main.F90:120-123), (qt, qr, qz, pr) with halos:
+
+    * qt = 0 (the laminar profile is computed there but not used);
+    * qr = eps*(sin 2πy + sin 4πy + sin 8πy + sin 6πy), y = zm/ALX3D, at the
+      radial faces k = 1..nrm, the inner wall's included; the outer wall
+      face k = nr stays 0;
+    * qz = Σ over m = 2, 4, 6, 8 of sin(2πx)(1 - |sin mπy|) sin(mπy) eps,
+      x = (rm - rint)/(rext - rint), for k = 1..nrm;
+    * pr = 0; eps = 0.1.
+
+    The arithmetic follows the reference's order of operations."""
+    import math
+    nthm, nzm, nrm = int(bou["nthm"]), int(bou["nzm"]), int(bou["nrm"])
+    nr = nrm + 1
+    alx3, rint, rext = float(bou["alx3"]), float(bou["rint"]), float(bou["rext"])
+    pi = 2.0 * math.asin(1.0)
+    dxz = float(nzm) / alx3
+    zm = (np.arange(nzm, dtype=np.float64) + 0.5) / dxz
+    _, rm = radial_grid(bou)
+    eps = 0.1
+    y = (zm / alx3)[:, None]
+    x = ((rm - rint) / (rext - rint))[None, :]
+    s2, s4, s6, s8 = (np.sin(y * m * pi) for m in (2, 4, 6, 8))
+    sx = np.sin(x * 2 * pi)
+    qr_jk = np.broadcast_to(eps * (s2 + s4 + s8 + s6), (nzm, nrm))
+    qz_jk = (sx * (1 - np.abs(s2)) * s2 * eps + sx * (1 - np.abs(s4)) * s4 * eps
+             + sx * (1 - np.abs(s6)) * s6 * eps + sx * (1 - np.abs(s8)) * s8 * eps)
+    shp = (nthm + 2, nzm + 2, nr)
+    qt, qr, qz, pr = (np.zeros(shp) for _ in range(4))
+    qr[1:-1, 1:-1, :nrm] = qr_jk
+    qz[1:-1, 1:-1, :nrm] = qz_jk
+    for a in (qr, qz):
+        fill_halo(a)
+    return qt, qr, qz, pr
 
 
 def couette_noise(bou: dict, seed: int = 1234, amp: float = 0.01):

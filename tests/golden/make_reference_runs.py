@@ -57,7 +57,8 @@ FILES = ["main.F90", "ReadInputFile.F90", "InitTimeMarchScheme.F90", "InitVariab
          "CalcLocalDivergence.F90", "SolvePressureCorrection.F90", "CorrectVelocity.F90", "CorrectPressure.F90",
          "CalcVelocityStats.F90", "CalcTorque.F90", "AuxiliaryRoutines.F90", "StatRoutines.F90",
          "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90", "StatReadReduceWrite.F90", "WriteFlowField.F90",
-         "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90", "WriteGridInfo.F90"]
+         "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90", "WriteGridInfo.F90",
+         "CreateInitialConditions.F90"]
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
               "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 MODULE_FILES = ["param.F90"]
@@ -155,6 +156,10 @@ CASES = [
     dict(name="statistics_and_dumps", seed=22, amp=0.05, stats=True, files=True, rcuts=[1.05, 1.23],
          bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
                       nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
+    # the reference's own initial condition (NREAD = 0: CreateInitialConditions)
+    dict(name="created_initial_conditions", seed=0, amp=0.0,
+         bou=base_bou(nthm=16, nzm=12, nrm=10, nread=0, istr=4, str=2.0, ren=800.0, ntst=14, tout=4e-3,
+                      dtmin=1e-4, dtmax=1e-2, limitCFL=2e-3)),
     # a restart from continua files of a coarser grid: ReadFlowField
     # interpolates them (interp.F90) onto the run's grid; the start is kept
     dict(name="restart_interpolated_from_coarser_grid", seed=23, amp=0.05,
@@ -224,6 +229,15 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         return r
 
     F.readflowfield = readflowfield
+    orig_create = F.createinitialconditions
+
+    def createinitialconditions(*a):
+        r = orig_create(*a)
+        for k in ("qt", "qr", "qz"):
+            start[k] = np.ascontiguousarray(getattr(G, k).d.transpose(2, 1, 0)).copy()
+        return r
+
+    F.createinitialconditions = createinitialconditions
     rec = {"cfl": [], "time": [], "dt": [], "dmax": [], "vmax": [], "step_cfl": []}
     orig = {n: getattr(F, n) for n in ("timemarcher", "calcmaxcfl", "checkdivergence", "calcvelocitystats")}
 
@@ -292,6 +306,10 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
                out_rms=np.array([list(map(float, r)) for r in rt.written.get(98, [])]).reshape(-1, 4), errorcode=np.array(code), ntime=np.array(G.ntime),
                final_time=np.array(G.time), final_dmax=np.array(final_dmax), final_cfl=np.array(final_cfl),
                final_torque=np.array(final_torque)))
+    if int(bou["nread"]) == 0:
+        # the reference's own start (before the halo update of main.F90:120)
+        for k, a in start.items():
+            out["start_" + k] = a
     if case.get("files"):
         for fname, dsets in sorted(rt.h5.items()):
             for dname, a in dsets.items():

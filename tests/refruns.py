@@ -39,6 +39,7 @@ CASES, DATA = load()
 CASE_NAMES = [c["name"] for c in CASES if not c.get("old_grid")]
 STATS_CASES = [c["name"] for c in CASES if c.get("stats")]
 RESTART_CASES = [c["name"] for c in CASES if c.get("old_grid")]
+CREATED_START_CASES = [c["name"] for c in CASES if int(c["bou"]["nread"]) == 0]
 FILES_CASES = [c["name"] for c in CASES if c.get("files")]
 # statistics in the order of the fixture (StatRoutines.F90 names) and of
 # the library's STATS list
@@ -55,7 +56,11 @@ def ref(name, key):
 
 
 def start(c):
+    """The start of a case: the reference's own initial condition for
+    NREAD = 0, else the seeded field its continua files held."""
     import tc_gb300.initial as ini
+    if int(c["bou"]["nread"]) == 0:
+        return ini.create_initial_conditions(c["bou"])
     return ini.couette_noise(c["bou"], seed=c["seed"], amp=c["amp"])
 
 

@@ -90,6 +90,17 @@ def test_oracle_statistics_match_reference_run(oracle, name):
         assert v <= (TOL_P if k == "pr_mean" else TOL_Q), (k, v)
 
 
+@pytest.mark.parametrize("name", R.CREATED_START_CASES)
+def test_created_initial_conditions_match_reference_run(name):
+    """NREAD = 0: the start CreateInitialConditions built in the reference
+    run (qt = 0, sinusoidal qr and qz, the inner-wall face of qr included)
+    and the host restatement agree bit for bit on the interior."""
+    import tc_gb300.initial as ini
+    c = R.case(name)
+    for k, a in zip(("qt", "qr", "qz"), ini.create_initial_conditions(c["bou"])[:3]):
+        np.testing.assert_array_equal(a[1:-1, 1:-1], R.ref(name, "start_" + k)[1:-1, 1:-1], err_msg=k)
+
+
 def write_old_continua(directory, c):
     """The restart files of the restart case: the seeded start on the old
     grid written as continua_*.h5 (interior cells, C order)."""
@@ -156,7 +167,7 @@ def test_cases_cover_the_stop_codes_and_forms():
     assert any(b["minstrt"] * b["multmin"] != 0 for b in bous)
     assert any(b["dtmin"] < b["dtmax"] for b in bous) and any(b["dtmin"] == b["dtmax"] for b in bous)
     assert any((b["nthm"], b["nzm"], b["nrm"]) == (64, 64, 64) for b in bous)
-    assert R.STATS_CASES and R.RESTART_CASES
+    assert R.STATS_CASES and R.RESTART_CASES and R.FILES_CASES and R.CREATED_START_CASES
 
 
 REF_DIR = os.environ.get("TC_REFERENCE_DIR", "/root/reference")
