@@ -1766,6 +1766,7 @@ class OneRank:
             hdfcreateblankfile=self.h5_blank, hdfserialwriterealscalar=self.h5_scalar,
             hdfserialwriteintscalar=self.h5_int_scalar, hdfserialwritereal1d=self.h5_1d,
             hdfwritereal2d=self.h5_2d_slab, hdfwriteserialreal2d=self.h5_2d, hdfwriterealhalo3d=self.h5_halo_3d,
+            hdfreadserialreal2d=self.h5_read_2d,
             quitroutine=self.quit, mpi_wtime=lambda: 0.0)
         self.F = F
         for name, fn in stubs.items():
@@ -1907,7 +1908,20 @@ class OneRank:
 
     # ---- HDF5 continua files
     def read_scalar(self, dsetname, filnam, var):
+        """HdfSerialReadIntScalar / HdfSerialReadRealScalar
+        (HdfRoutines.F90:217-269): from a file the run holds (written by it
+        or given before it), else from the continua master scalars."""
+        name = self._h5_name(filnam)
+        if name in self.h5:
+            v = self.h5[name][str(dsetname).strip()][0]
+            return (dsetname, filnam, int(v) if np.asarray(v).dtype.kind == "i" else float(v))
         return (dsetname, filnam, self.continua[dsetname.strip()])
+
+    def h5_read_2d(self, filename, dsetname, ndx, ndy, var):
+        """HdfReadSerialReal2D (HdfRoutines.F90:501-529): var(ndx, ndy) from
+        a file the run holds."""
+        a = self.h5[self._h5_name(filename)][str(dsetname).strip()]
+        var.d[:int(ndx), :int(ndy)] = a.T
 
     def read_continua(self, n1o, n2o, n3o, xs2, xe2, xs3, xe3, intvar, qua):
         """HdfReadContinua: the file's (nr, nz-1, nth-1) values into
@@ -2000,7 +2014,10 @@ class OneRank:
         self.units[int(unit)] = [ln for ln in text.split("\n")]
 
     def exists(self, name):
-        return str(name).strip().lstrip("./") in {k.lstrip("./") for k in self.files}
+        """INQUIRE(EXIST=): a file the caller supplied, or an HDF5 file the
+        run holds."""
+        return (str(name).strip().lstrip("./") in {k.lstrip("./") for k in self.files}
+                or self._h5_name(name) in self.h5)
 
     def read(self, unit, fmt, types_):
         """One READ statement: list-directed (fmt '*') takes values from as

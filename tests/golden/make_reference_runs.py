@@ -156,6 +156,10 @@ CASES = [
     dict(name="statistics_and_dumps", seed=22, amp=0.05, stats=True, files=True, rcuts=[1.05, 1.23],
          bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
                       nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
+    # STAREAD = 1: statistics files of an earlier run are read and added to
+    # this run's at the stop (StatReadReduceWrite)
+    dict(name="statistics_read_and_added", seed=24, amp=0.05, stats=True, files=True, stats_in=7,
+         bou=base_bou(nthm=12, nzm=10, nrm=8, istr=4, str=2.0, tsta=0.0, tout=3e-3, ntst=7, starea=1)),
     # the reference's own initial condition (NREAD = 0: CreateInitialConditions)
     dict(name="created_initial_conditions", seed=0, amp=0.0,
          bou=base_bou(nthm=16, nzm=12, nrm=10, nread=0, istr=4, str=2.0, ren=800.0, ntst=14, tout=4e-3,
@@ -215,6 +219,9 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         # rcuts.in: a header record, then the radii of the slabs (InitDumpRCuts)
         files["rcuts.in"] = " RCUT\n  " + "   ".join(repr(float(r)) for r in case["rcuts"]) + "\n"
     rt = fs.OneRank(files, continua)
+    h5_in = stats_files_in(bou, case["stats_in"]) if case.get("stats_in") is not None else {}
+    for fname, dsets in h5_in.items():
+        rt.h5[fname] = {k: v.copy() for k, v in dsets.items()}
     w = fs.World(ref_dir, FILES, MODULE_FILES, rt, capture_units=(97, 92, 98), nan_fill=nan_fill)
     F, G = w.F, w.G
     start = {}
@@ -238,6 +245,15 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         return r
 
     F.createinitialconditions = createinitialconditions
+    orig_ws = F.writestats
+    samples = []
+
+    def writestats(*a):
+        # the run's own sample count (WriteStats adds a read file's to it)
+        samples.append(int(G.nstatsamples))
+        return orig_ws(*a)
+
+    F.writestats = writestats
     rec = {"cfl": [], "time": [], "dt": [], "dmax": [], "vmax": [], "step_cfl": []}
     orig = {n: getattr(F, n) for n in ("timemarcher", "calcmaxcfl", "checkdivergence", "calcvelocitystats")}
 
@@ -278,7 +294,7 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
     torques_out = [list(map(float, r)) for r in rt.written.get(97, [])]
     nutes = [list(map(float, r)) for r in rt.written.get(92, [])]
     stats = {n: np.ascontiguousarray(getattr(G, n).d.T) for n in STAT_NAMES} if case.get("stats") else {}
-    nsamples = int(G.nstatsamples)
+    nsamples = samples[0] if samples else int(G.nstatsamples)
     F.checkdivergence, F.calcmaxcfl = orig["checkdivergence"], orig["calcmaxcfl"]
     final_dmax = float(F.checkdivergence(0.0)[0])
     final_cfl = float(F.calcmaxcfl(0.0)[0])
@@ -310,6 +326,9 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         # the reference's own start (before the halo update of main.F90:120)
         for k, a in start.items():
             out["start_" + k] = a
+    for fname, dsets in sorted(h5_in.items()):
+        for dname, a in dsets.items():
+            out[f"h5in:{fname}:{dname}"] = a
     if case.get("files"):
         for fname, dsets in sorted(rt.h5.items()):
             for dname, a in dsets.items():
@@ -322,6 +341,21 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
 
     if verbose:
         print(f"{case['name']}: code {code}, ntime {G.ntime}, {len(rec['dt'])} steps, {time.time() - t0:.1f} s")
+    return out
+
+
+STAT_FILES = ["vt_mean", "vr_mean", "vz_mean", "wt_mean", "wr_mean", "wz_mean", "vt_rms", "vr_rms", "vz_rms",
+              "wt_rms", "wr_rms", "wz_rms", "vtvr_mean", "vtvz_mean", "vrvz_mean", "pr_mean", "pr_rms", "disste"]
+
+
+def stats_files_in(bou, seed):
+    """Statistics files of an earlier run (stats/<name>.h5 with dataset
+    <name>, C order (nzm, nrm); stats/stafield_master.h5 with its sample
+    count): seeded values."""
+    nzm, nrm = int(bou["nzm"]), int(bou["nrm"])
+    out = {"stats/stafield_master.h5": {"averaging_time": np.array([3], dtype=np.int32)}}
+    for i, n in enumerate(STAT_FILES):
+        out[f"stats/{n}.h5"] = {n: ini.uniform(seed, 10 + i, 1, nzm, nrm)[0]}
     return out
 
 
@@ -366,7 +400,8 @@ def main():
         meta = [m for m in meta if m["name"] != case["name"]]
         meta.append(dict(name=case["name"], seed=case["seed"], amp=case["amp"], bou=case["bou"],
                          planes=case.get("planes"), stats=bool(case.get("stats")),
-                         files=bool(case.get("files")), rcuts=case.get("rcuts"), old_grid=case.get("old_grid")))
+                         files=bool(case.get("files")), rcuts=case.get("rcuts"), old_grid=case.get("old_grid"),
+                         stats_in=case.get("stats_in")))
     order = [c["name"] for c in CASES]
     meta.sort(key=lambda m: order.index(m["name"]))
     np.savez_compressed(args.out + ".npz", **arrays)

@@ -231,11 +231,12 @@ def stat_errors(c, stat, samples, rec):
     return out
 
 
-def h5_files(name):
-    """The HDF5 files the reference run wrote: path (relative to the run's
-    directory) -> {dataset: array}."""
+def h5_files(name, kind="h5"):
+    """The HDF5 files the reference run wrote (kind "h5") or was given
+    before it started (kind "h5in"): path (relative to the run's directory)
+    -> {dataset: array}."""
     out = {}
-    pre = f"{name}/h5:"
+    pre = f"{name}/{kind}:"
     for k, v in DATA.items():
         if k.startswith(pre):
             path, dset = k[len(pre):].rsplit(":", 1)
