@@ -156,6 +156,12 @@ CASES = [
     dict(name="statistics_and_dumps", seed=22, amp=0.05, stats=True, files=True, rcuts=[1.05, 1.23],
          bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
                       nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
+    # stops at the first output step: velocities above VMAX (266), and the
+    # divergence above RESID (169)
+    dict(name="velocities_above_vmax", seed=25, amp=0.05,
+         bou=base_bou(nthm=12, nzm=10, nrm=8, limitVel=4e-3)),
+    dict(name="divergence_above_resid", seed=26, amp=0.05,
+         bou=base_bou(nthm=12, nzm=10, nrm=8, resid=1e-30)),
     # STAREAD = 1: statistics files of an earlier run are read and added to
     # this run's at the stop (StatReadReduceWrite)
     dict(name="statistics_read_and_added", seed=24, amp=0.05, stats=True, files=True, stats_in=7,

@@ -60,7 +60,8 @@ def test_oracle_matches_reference_run(oracle, name):
     rt = R.ref(name, "final_torque")
     assert abs(ti - rt[1]) <= TOL_S * abs(rt[1]) and abs(to - rt[2]) <= TOL_S * abs(rt[2])
     resid = c["bou"]["resid"]
-    assert o.check_divergence() < resid and float(R.ref(name, "final_dmax")) < resid
+    if rec["code"] != 169:
+        assert o.check_divergence() < resid and float(R.ref(name, "final_dmax")) < resid
     assert abs(o.calc_max_cfl() - float(R.ref(name, "final_cfl"))) <= TOL_S * float(R.ref(name, "final_cfl"))
 
 
@@ -156,10 +157,11 @@ def test_grid_info_file_matches_reference_run(tmp_path, name):
 
 def test_cases_cover_the_stop_codes_and_forms():
     """The fixtures hold runs that end with 555 (NTST reached), 333 (TMAX)
-    and 166 (dt below DTMIN), RK3 and AB2, the three radial grids, fixed and
+    166 (dt below DTMIN), 266 (velocities above VMAX) and 169 (divergence
+    above RESID), RK3 and AB2, the three radial grids, fixed and
     variable dt, rotation, the oscillating cylinder and patterned slip."""
     codes = {int(R.ref(n, "errorcode")) for n in R.CASE_NAMES}
-    assert {555, 333, 166} <= codes
+    assert {555, 333, 166, 266, 169} <= codes
     bous = [c["bou"] for c in R.CASES]
     assert {0, 4, 6} <= {int(b["istr"]) for b in bous}
     assert {1, 3} <= {int(b["nsst"]) for b in bous}
