@@ -131,8 +131,10 @@ int tc_set_stream(tc_handle* h, void* cuda_stream);
 
 /* Copy a start into the handle: host arrays in the reference layout; halo
  * entries are ignored (the device keeps the fields periodic by index wrap).
- * qr(1,:,:) and qr(nr,:,:) are forced to 0 (wall values).  pr may be NULL
- * (zero pressure, as ReadFlowField leaves it).  Also zeroes ru1..ru3. */
+ * The wall faces qr(1,:,:) and qr(nr,:,:) are kept as given: the
+ * reference reads them until ImplicitAndUpdateQR sets them to 0 in the
+ * first substep (CreateInitialConditions leaves qr(1) non-zero).  pr may be
+ * NULL (zero pressure, as ReadFlowField leaves it).  Also zeroes ru1..ru3. */
 int tc_set_state(tc_handle* h, const double* qt, const double* qr,
                  const double* qz, const double* pr);
 /* Copy the state back into host arrays in the reference layout with the

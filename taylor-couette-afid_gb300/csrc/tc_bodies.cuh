@@ -1207,6 +1207,16 @@ template <> struct SweepV<F2, float> {
     static __device__ __forceinline__ F2 adds(F2 a, float s) { return a + bc2(s); }
 };
 
+// ImplicitAndUpdateQR.F90:70-71: after the update both wall faces of qr are
+// zero.  A start may hold other wall values (CreateInitialConditions.F90:30
+// sets the inner one); the reference reads them until the first update, and
+// so does the device.
+template <typename T>
+__device__ __forceinline__ void qr_walls_zero(T* q, size_t P, int nr) {
+    q[0] = (T)0;
+    q[(size_t)nr * P] = (T)0;
+}
+
 // SolveImpEqnUpdate_QT.F90:65-78 (comp 0), SolveImpEqnUpdate_QR.F90:54-65 (comp 1, faces
 // 1..nr-1), SolveImpEqnUpdate_QZ.F90:59-68 (comp 2) for the column `col`.  The three
 // components are independent, so each gets its own thread.
@@ -1220,10 +1230,11 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
         if (comp == 0)
             lu_column_ckpt<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v),
                                  F.u(sub, 0, v), *F.extra(sub));
-        else if (comp == 1)
+        else if (comp == 1) {
             lu_column_ckpt<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0),
                                   F.u(sub, 1, 0), (T)0);
-        else
+            qr_walls_zero(f.qr + col, P, nr);
+        } else
             lu_column_ckpt<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v),
                                   F.u(sub, 2, v), (T)0);
         return;
@@ -1231,9 +1242,10 @@ __device__ __forceinline__ void radial_column(const Dims& d, const FieldsT<T>& f
     if (comp == 0)
         lu_column<true>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, v), F.dinv(sub, 0, v), F.u(sub, 0, v),
                         *F.extra(sub));
-    else if (comp == 1)
+    else if (comp == 1) {
         lu_column<false>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0), F.u(sub, 1, 0), (T)0);
-    else
+        qr_walls_zero(f.qr + col, P, nr);
+    } else
         lu_column<false>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, v), F.dinv(sub, 2, v), F.u(sub, 2, v), (T)0);
 }
 
@@ -1254,10 +1266,12 @@ __device__ __forceinline__ void radial_column_pair(const Dims& d, const FieldsT<
     if (comp == 0)
         lu_column_ckpt<true, float, F2>(f.rhs_t + col, f.qt + col, P, 0, nr, F.l(sub, 0, va), F.dinv(sub, 0, va),
                                         F.u(sub, 0, va), *F.extra(sub));
-    else if (comp == 1)
+    else if (comp == 1) {
         lu_column_ckpt<false, float, F2>(f.rhs_r + col, f.qr + col, P, 1, nr, F.l(sub, 1, 0), F.dinv(sub, 1, 0),
                                          F.u(sub, 1, 0), 0.0f);
-    else
+        *reinterpret_cast<float2*>(f.qr + col) = make_float2(0.0f, 0.0f);
+        *reinterpret_cast<float2*>(f.qr + col + (size_t)nr * P) = make_float2(0.0f, 0.0f);
+    } else
         lu_column_ckpt<false, float, F2>(f.rhs_z + col, f.qz + col, P, 0, nr, F.l(sub, 2, va), F.dinv(sub, 2, va),
                                          F.u(sub, 2, va), 0.0f);
 }

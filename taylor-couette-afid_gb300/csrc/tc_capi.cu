@@ -539,8 +539,6 @@ static int set_state_t(tc_handle* h, const double* qt, const double* qr, const d
     if (int r = upload(h, qz, f.qz, d.nr, 1)) return r;
     if (pr) { if (int r = upload(h, pr, f.pr, d.nr, 1)) return r; }
     else CK(cudaMemsetAsync(f.pr, 0, cells * sizeof(double), h->stream), "memset");
-    CK(cudaMemsetAsync(f.qr, 0, (size_t)d.P * sizeof(T), h->stream), "memset");
-    CK(cudaMemsetAsync(f.qr + (size_t)d.nr * d.P, 0, (size_t)d.P * sizeof(T), h->stream), "memset");
     CK(cudaMemsetAsync(f.ru1, 0, cells * sizeof(T), h->stream), "memset");
     CK(cudaMemsetAsync(f.ru2, 0, faces * sizeof(T), h->stream), "memset");
     CK(cudaMemsetAsync(f.ru3, 0, cells * sizeof(T), h->stream), "memset");

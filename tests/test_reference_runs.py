@@ -58,7 +58,7 @@ def test_oracle_matches_reference_run(oracle, name):
         assert v <= TOL_S, (k, v)
     ti, to = o.calc_torque()
     rt = R.ref(name, "final_torque")
-    assert abs(ti - rt[1]) <= TOL_S * abs(rt[1]) and abs(to - rt[2]) <= TOL_S * abs(rt[2])
+    assert R.torque_error(ti, to, rt[1], rt[2]) <= TOL_S
     resid = c["bou"]["resid"]
     if rec["code"] != 169:
         assert o.check_divergence() < resid and float(R.ref(name, "final_dmax")) < resid
