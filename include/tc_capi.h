@@ -118,8 +118,13 @@ int tc_precision(const tc_handle* h);
  * the march about 5 % faster).  Both compute the same bits.  2019 when the
  * handle has no TMA descriptors.  No counterpart in the reference. */
 int tc_use_tma(tc_handle* h, int enable);
-/* The configuration the handle was created with. */
+/* The configuration the handle was created with (TMAX as tc_set_tmax or a
+ * restart left it). */
 int tc_get_bou(const tc_handle* h, tc_bou* out);
+/* TMAX of the stop test 333 (main.F90:206).  ReadFlowField.F90:149 adds the
+ * restart time to it; tc_h5_read_continua does the same through this call,
+ * and a host that reads the continuation files itself sets it here. */
+int tc_set_tmax(tc_handle* h, double tmax);
 void tc_destroy(tc_handle* h);
 const char* tc_last_error(const tc_handle* h);   /* h may be NULL */
 
@@ -159,7 +164,8 @@ int tc_set_field(tc_handle* h, int which, const double* in);
 /* WriteFlowField.F90:17-47: the state of h at simulated time `time`. */
 int tc_h5_write_continua(tc_handle* h, const char* dir, double time);
 /* ReadFlowField.F90:31-149: load the files into h (tc_set_state; pr = 0)
- * and return their time.  Files of another grid (nth, nz, nr, istr or str
+ * and return their time (0 when IRESET = 1, ReadFlowField.F90:144); h's
+ * TMAX becomes TMAX + that time (ReadFlowField.F90:149).  Files of another grid (nth, nz, nr, istr or str
  * differ) are interpolated onto h's grid as interp.F90 does (its quirks
  * kept: the old field's halos are linear extrapolations, qr and qz are
  * placed at (tm, zc, rm) and (tm, zm, rc), the radial direction takes the
@@ -168,7 +174,8 @@ int tc_h5_write_continua(tc_handle* h, const char* dir, double time);
  * 2024. */
 int tc_h5_read_continua(tc_handle* h, const char* dir, double* time);
 /* The same as host arrays, without a handle (no GPU): qt, qr, qz receive
- * the fields in the reference layout of cfg's grid (halos 0). */
+ * the fields in the reference layout of cfg's grid (halos 0); the time is
+ * 0 when IRESET = 1, and TMAX is the caller's to extend. */
 int tc_h5_load_continua(const tc_bou* cfg, const char* dir, double* qt, double* qr, double* qz,
                         double* time);
 /* Scalar datasets (int32 where is_int[i], else float64) in a new file, as

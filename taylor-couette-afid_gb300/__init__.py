@@ -93,6 +93,7 @@ SIGNATURES = {
     "tc_destroy": (None, [_vp]),
     "tc_last_error": (ctypes.c_char_p, [_vp]),
     "tc_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "tc_set_tmax": (ctypes.c_int, [_vp, ctypes.c_double]),
     "tc_set_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "tc_get_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "tc_get_field": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
@@ -355,6 +356,12 @@ class TaylorCouette:
     def set_stream(self, stream_ptr: int):
         self._ck(self.L.tc_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
 
+    def set_tmax(self, tmax: float):
+        """TMAX of the stop test 333; a restart adds its time to it
+        (ReadFlowField.F90:149), which read_continua does."""
+        self._ck(self.L.tc_set_tmax(self.h, float(tmax)))
+        self.bou["tmax"] = float(tmax)
+
     def set_state(self, qt, qr, qz, pr=None):
         """ReadFlowField: load a start (reference layout, halos ignored)."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (qt, qr, qz)]
@@ -429,9 +436,12 @@ class TaylorCouette:
         self._ck(self.L.tc_h5_write_continua(self.h, directory.encode(), float(time)))
 
     def read_continua(self, directory: str = ".") -> float:
-        """ReadFlowField (same grid): load the continuation files, return their time."""
+        """ReadFlowField: load the continuation files (interpolated when they
+        hold another grid) and return their time (0 with IRESET = 1); TMAX
+        grows by that time, as ReadFlowField.F90:149 does."""
         t = ctypes.c_double()
         self._ck(self.L.tc_h5_read_continua(self.h, directory.encode(), ctypes.byref(t)))
+        self.bou["tmax"] = float(self.bou["tmax"]) + t.value
         return t.value
 
     def get_field(self, name: str) -> np.ndarray:

@@ -488,6 +488,13 @@ void tc_destroy(tc_handle* h) {
     delete h;
 }
 
+int tc_set_tmax(tc_handle* h, double tmax) {
+    if (int r = check(h)) return r;
+    h->bou.tmax = tmax;
+    h->k.tmax = tmax;
+    return 0;
+}
+
 int tc_set_stream(tc_handle* h, void* s) {
     if (int r = check(h)) return r;
     h->stream = (cudaStream_t)s;

@@ -739,7 +739,8 @@ int tc_h5_load_continua(const tc_bou* cfg, const char* dir, double* qt, double* 
                 std::memcpy(&q[c][((size_t)(i + 1) * (nzm + 2) + (j + 1)) * nr], &v[((size_t)i * nzm + j) * nr],
                             sizeof(double) * nr);
     }
-    if (time) *time = s[3];
+    // ReadFlowField.F90:144: IRESET = 1 starts the clock again at 0
+    if (time) *time = cfg->ireset ? 0.0 : s[3];
     return 0;
 }
 
@@ -749,9 +750,13 @@ int tc_h5_read_continua(tc_handle* h, const char* dir, double* time) {
     const size_t halo = (size_t)(b.nthm + 2) * (b.nzm + 2) * (b.nrm + 1);
     std::vector<double> q[3];
     for (auto& a : q) a.resize(halo);
-    if (int r = tc_h5_load_continua(&b, dir, q[0].data(), q[1].data(), q[2].data(), time))
+    double t = 0.0;
+    if (int r = tc_h5_load_continua(&b, dir, q[0].data(), q[1].data(), q[2].data(), &t))
         return hfail(h, r, tc_last_error(nullptr));
-    return tc_set_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr);
+    if (int r = tc_set_state(h, q[0].data(), q[1].data(), q[2].data(), nullptr)) return r;
+    if (time) *time = t;
+    // ReadFlowField.F90:149: TMAX counts from the time the run restarts at
+    return tc_set_tmax(h, b.tmax + t);
 }
 
 int tc_h5_write_scalars(const char* path, int n, const char* const* names, const double* values, const int* is_int) {

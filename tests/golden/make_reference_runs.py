@@ -156,6 +156,11 @@ CASES = [
     dict(name="statistics_and_dumps", seed=22, amp=0.05, stats=True, files=True, rcuts=[1.05, 1.23],
          bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
                       nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
+    # a restart whose continua files hold time 1.2345: the run goes on from
+    # that time (the oscillating wall's phase, the output steps, TMAX)
+    dict(name="restart_at_a_later_time", seed=27, amp=0.03, start_time=1.2345,
+         bou=base_bou(nthm=12, nzm=10, nrm=8, istr=4, str=1.5, sizepert=0.2, omegapert=0.7, tout=3e-3,
+                      tmax=1.2405, ntst=100)),
     # stops at the first output step: velocities above VMAX (266), and the
     # divergence above RESID (169)
     dict(name="velocities_above_vmax", seed=25, amp=0.05,
@@ -213,7 +218,7 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         return np.asfortranarray(a[1:-1, 1:-1, :].transpose(2, 1, 0))
 
     continua = {"qt": interior(qt), "qr": interior(qr), "qz": interior(qz), "nth": nth, "nr": nr, "nz": nz,
-                "time": 0.0, "istr": int(bou["istr"]), "str": float(bou["str"])}
+                "time": float(case.get("start_time", 0.0)), "istr": int(bou["istr"]), "str": float(bou["str"])}
     if case.get("old_grid"):
         # the continua files hold the same seeded start on a coarser grid
         obou = dict(bou, **case["old_grid"])
@@ -407,7 +412,7 @@ def main():
         meta.append(dict(name=case["name"], seed=case["seed"], amp=case["amp"], bou=case["bou"],
                          planes=case.get("planes"), stats=bool(case.get("stats")),
                          files=bool(case.get("files")), rcuts=case.get("rcuts"), old_grid=case.get("old_grid"),
-                         stats_in=case.get("stats_in")))
+                         stats_in=case.get("stats_in"), start_time=case.get("start_time", 0.0)))
     order = [c["name"] for c in CASES]
     meta.sort(key=lambda m: order.index(m["name"]))
     np.savez_compressed(args.out + ".npz", **arrays)

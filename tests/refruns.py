@@ -55,6 +55,32 @@ def ref(name, key):
     return DATA[f"{name}/{key}"]
 
 
+def start_time(c):
+    """The time a case's run starts at: its continua files' time, or 0 with
+    IRESET = 1 (ReadFlowField.F90:144)."""
+    return 0.0 if int(c["bou"]["ireset"]) else float(c.get("start_time", 0.0))
+
+
+def run_bou(c):
+    """bou of a case as the run sees it after ReadFlowField: TMAX counts from
+    the restart time (ReadFlowField.F90:149)."""
+    return dict(c["bou"], tmax=float(c["bou"]["tmax"]) + start_time(c))
+
+
+def write_continua(directory, c, state, time):
+    """continua_q*.h5 and continua_master.h5 of `state` on c's grid at
+    `time` (the files WriteFlowField writes)."""
+    import tc_gb300 as tcg
+    bou = c["bou"]
+    nthm, nzm, nrm = int(bou["nthm"]), int(bou["nzm"]), int(bou["nrm"])
+    tcg.h5_write_scalars(os.path.join(directory, "continua_master.h5"),
+                         dict(nr=nrm + 1, nth=nthm + 1, nz=nzm + 1, time=time, rint=bou["rint"], rext=bou["rext"],
+                              istr=bou["istr"], str=bou["str"], alx3=bou["alx3"], lamb=bou["lamb"]),
+                         ints=("nr", "nth", "nz", "istr"))
+    for k, a in zip(("qt", "qr", "qz"), state[:3]):
+        tcg.h5_write(os.path.join(directory, f"continua_{k}.h5"), "var", np.ascontiguousarray(a[1:-1, 1:-1, :]))
+
+
 def start(c):
     """The start of a case: the reference's own initial condition for
     NREAD = 0, else the seeded field its continua files held."""
@@ -69,7 +95,7 @@ def is_output_step(ntime, time, dt, tout):
     return ntime == 1 or math.fmod(time, tout) < dt
 
 
-def march(step, cfl, torque, c, stats=None, vstats=None, div=None):
+def march(step, cfl, torque, c, stats=None, vstats=None, div=None, t0=0.0):
     """Advance a simulation as main.F90:152-226 does, one step at a time.
 
     step(ntime, time, dt) -> (code, time, dt) runs the step of index ntime;
@@ -80,12 +106,13 @@ def march(step, cfl, torque, c, stats=None, vstats=None, div=None):
     vstats() and div(), when given, are CalcVelocityStats (vmax, rms) and
     CheckDivergence, recorded at every output step (main.F90:181,185) and,
     for div, before the loop (main.F90:125).
+    t0 is the time the run starts at (a restart's, ReadFlowField.F90:144).
     Returns the per-step dt, time and CFL, the torques of the output steps,
     the dissipation numbers, vmax and divergence records, the stop code and
     the index of the last step."""
     bou = c["bou"]
     ntst = int(bou["ntst"])
-    t, dt = 0.0, 0.0
+    t, dt = float(t0), 0.0
     rec = dict(dt=[], time=[], cfl=[], torque=[], nute=[], vmax=[], rms=[], dmax=[])
     if div is not None:
         rec["dmax"].append(div())

@@ -36,14 +36,28 @@ TOL_MIXED_TORQUE = 1e-4
 
 def gpu_march(c, precision="fp64"):
     g = tc.TaylorCouette(c["bou"], precision=precision)
-    g.set_state(*R.start(c))
+    t0 = 0.0
+    if c.get("start_time"):
+        # a restart: the library reads the continuation files, takes their
+        # time and extends TMAX by it (ReadFlowField.F90:144-149)
+        import shutil
+        import tempfile
+        d = tempfile.mkdtemp()
+        try:
+            R.write_continua(d, c, R.start(c), c["start_time"])
+            t0 = g.read_continua(d)
+        finally:
+            shutil.rmtree(d)
+        assert t0 == R.start_time(c) and g.bou["tmax"] == R.run_bou(c)["tmax"]
+    else:
+        g.set_state(*R.start(c))
 
     def step(ntime, t, dt):
         code, _, t, dt = g.run(1, ntime, t, dt)
         return code, t, dt
 
     rec = R.march(step, g.calc_max_cfl, g.calc_torque, c, vstats=g.velocity_stats,
-                  div=g.check_divergence)
+                  div=g.check_divergence, t0=t0)
     return g, rec
 
 
@@ -212,7 +226,8 @@ def test_ensemble_members_match_reference_runs(gpu_lib):
     one time scheme and no patterned slip, so the AB2 and slip cases stay
     out.)"""
     names = [n for n in R.CASE_NAMES if int(R.ref(n, "errorcode")) == 555 and R.case(n).get("planes") is None
-             and int(R.case(n)["bou"]["nsst"]) == 3 and int(R.case(n)["bou"]["minstrt"]) == 0]
+             and int(R.case(n)["bou"]["nsst"]) == 3 and int(R.case(n)["bou"]["minstrt"]) == 0
+             and not R.case(n).get("start_time")]
     assert len(names) >= 5
     ens = tc.Ensemble("fp64")
     slots, left = {}, {}

@@ -229,6 +229,8 @@ def test_continua_load_same_grid(tmp_path):
     assert t == 0.75
     for a, b in zip((qt, qr, qz), f):
         assert np.array_equal(a[1:-1, 1:-1, :], b)
+    # IRESET = 1 starts the clock again (ReadFlowField.F90:144)
+    assert tc.h5_load_continua(dict(bou, ireset=1), str(tmp_path))[3] == 0.0
 
 
 def test_continua_interpolated_onto_a_finer_grid(tmp_path):

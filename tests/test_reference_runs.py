@@ -31,14 +31,14 @@ TOL_S = 1e-12
 
 
 def oracle_march(oracle, c):
-    o = oracle.CppOracle(c["bou"])
+    o = oracle.CppOracle(R.run_bou(c))
     o.set_state(*R.start(c))
 
     def step(ntime, t, dt):
         return o.run(ntime, 1, t, dt)
 
     rec = R.march(step, o.calc_max_cfl, o.calc_torque, c, vstats=o.velocity_stats,
-                  div=o.check_divergence)
+                  div=o.check_divergence, t0=R.start_time(c))
     return o, rec
 
 
