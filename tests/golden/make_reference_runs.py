@@ -157,10 +157,11 @@ CASES = [
          bou=base_bou(nthm=16, nzm=12, nrm=10, istr=6, str=3.0, romeg=0.15, tsta=0.0, tout=2e-3, ntst=9,
                       nslabr=2, dpthcut=1, dpstave=1, tframe2d=4e-3, dpfullf=1, tframe3d=6e-3)),
     # a restart whose continua files hold time 1.2345: the run goes on from
-    # that time (the oscillating wall's phase, the output steps, TMAX)
+    # that time (the oscillating wall's phase, the output steps) and TMAX
+    # counts from it (stop 333 after time 1.2345 + 0.0601)
     dict(name="restart_at_a_later_time", seed=27, amp=0.03, start_time=1.2345,
          bou=base_bou(nthm=12, nzm=10, nrm=8, istr=4, str=1.5, sizepert=0.2, omegapert=0.7, tout=3e-3,
-                      tmax=1.2405, ntst=100)),
+                      tmax=0.0601, ntst=100)),
     # stops at the first output step: velocities above VMAX (266), and the
     # divergence above RESID (169)
     dict(name="velocities_above_vmax", seed=25, amp=0.05,
