@@ -193,7 +193,7 @@ def test_output_files_match_reference_run(gpu_lib, tmp_path, name):
 
 @pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
 @pytest.mark.parametrize("name", ["production_oscillating_32x24x32", "rotating_32x24x32",
-                                  "chebyshev_rk3_rotating", "prime_lengths_7_13"])
+                                  "chebyshev_rk3_rotating", "prime_lengths_7_13", "created_initial_conditions"])
 def test_mixed_against_reference_run(gpu_lib, name, precision):
     """The mixed forms on the reference's own time grid: the dt sequence of
     the reference run is imposed (each form's own CFL rule would pick a
