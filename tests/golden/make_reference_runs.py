@@ -162,6 +162,12 @@ CASES = [
     dict(name="restart_at_a_later_time", seed=27, amp=0.03, start_time=1.2345,
          bou=base_bou(nthm=12, nzm=10, nrm=8, istr=4, str=1.5, sizepert=0.2, omegapert=0.7, tout=3e-3,
                       tmax=0.0601, ntst=100)),
+    # one step on a tanh grid with rotation, the oscillating wall (from time
+    # 0.37) and patterned slip: every routine's output of its three
+    # substeps is kept
+    dict(name="routine_outputs_of_one_step", seed=28, amp=0.05, start_time=0.37, routines=True,
+         bou=base_bou(nthm=16, nzm=16, nrm=8, istr=4, str=2.0, romeg=0.1, sizepert=0.1, omegapert=0.5,
+                      minstrt=2, minstrz=2, multmin=1, ntst=0, rext=1.5, alx3=2.0)),
     # stops at the first output step: velocities above VMAX (266), and the
     # divergence above RESID (169)
     dict(name="velocities_above_vmax", seed=25, amp=0.05,
@@ -297,6 +303,30 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
 
     F.timemarcher, F.calcmaxcfl, F.checkdivergence, F.calcvelocitystats = (
         timemarcher, calcmaxcfl, checkdivergence, calcvelocitystats)
+    routines = {}
+    if case.get("routines"):
+        # what every routine of the first step's substeps leaves in the
+        # arrays it writes (TimeMarcher.F90:31-54), C order
+        writes = {"explicittermsqt": ("dq",), "explicittermsqr": ("dph",), "explicittermsqz": ("qcap",),
+                  "implicitandupdateqt": ("qt", "ru1"), "implicitandupdateqr": ("qr", "ru2"),
+                  "implicitandupdateqz": ("qz", "ru3"), "calclocaldivergence": ("dph",),
+                  "solvepressurecorrection": ("dph",), "correctvelocity": ("qt", "qr", "qz"),
+                  "correctpressure": ("pr",)}
+        counts = {}
+
+        def recorder(name, fn):
+            def wrapped(*a):
+                r = fn(*a)
+                if not rec["time"]:            # inside the first TimeMarcher
+                    ns = counts[name] = counts.get(name, 0) + 1
+                    for arr in writes[name]:
+                        routines[f"routine:{ns}:{name}:{arr}"] = np.ascontiguousarray(
+                            getattr(G, arr).d.transpose(2, 1, 0)).copy()
+                return r
+            return wrapped
+
+        for name in writes:
+            setattr(F, name, recorder(name, getattr(F, name)))
     t0 = time.time()
     code = None
     try:
@@ -338,6 +368,7 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         # the reference's own start (before the halo update of main.F90:120)
         for k, a in start.items():
             out["start_" + k] = a
+    out.update(routines)
     for fname, dsets in sorted(h5_in.items()):
         for dname, a in dsets.items():
             out[f"h5in:{fname}:{dname}"] = a

@@ -41,6 +41,7 @@ STATS_CASES = [c["name"] for c in CASES if c.get("stats")]
 RESTART_CASES = [c["name"] for c in CASES if c.get("old_grid")]
 CREATED_START_CASES = [c["name"] for c in CASES if int(c["bou"]["nread"]) == 0]
 FILES_CASES = [c["name"] for c in CASES if c.get("files")]
+ROUTINE_CASES = [n for n in CASE_NAMES if any(k.startswith(f"{n}/routine:") for k in DATA)]
 # statistics in the order of the fixture (StatRoutines.F90 names) and of
 # the library's STATS list
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
@@ -283,3 +284,49 @@ def h5_files(name, kind="h5"):
             path, dset = k[len(pre):].rsplit(":", 1)
             out.setdefault(path, {})[dset] = v
     return out
+
+
+# The routines of a substep in TimeMarcher.F90:31-54 order, with the arrays
+# each one writes (the names of the reference's arrays; "hr" is dph as
+# ExplicitTermsQR leaves it, "phi" dph after SolvePressureCorrection).
+ROUTINES = [("explicittermsqt", ("dq",)), ("explicittermsqr", ("hr",)), ("explicittermsqz", ("qcap",)),
+            ("implicitandupdateqt", ("qt", "ru1")), ("implicitandupdateqr", ("qr", "ru2")),
+            ("implicitandupdateqz", ("qz", "ru3")), ("calclocaldivergence", ("div",)),
+            ("solvepressurecorrection", ("phi",)), ("correctvelocity", ("qt", "qr", "qz")),
+            ("correctpressure", ("pr",))]
+_REF_ARRAY = {"hr": "dph", "div": "dph", "phi": "dph"}
+
+
+def routine_error(name, ns, routine, arr, mine, nrm):
+    """Relative error of one routine's output in substep ns against the
+    reference run.  `mine` is in the library's layout: haloed
+    (nthm+2, nzm+2, nr) for qt, qr, qz, pr and dph (div, phi), plain
+    (nthm, nzm, nr) for dq, qcap, ru1..ru3 and hr.  Compared are the
+    levels the routine defines; phi and pr without the theta-z mean of each
+    radial level (the singular mode's offset), against max |reference|.
+    From substep 2 on that offset has entered pr, and the radial pressure
+    gradient of ImplicitAndUpdateQR (ImplicitAndUpdateQR.F90:58) carries its
+    radial differences into the theta-z mean of qr and of the divergence of
+    that qr (the projection then takes it out again: CorrectVelocity leaves
+    the same qr); those two are compared without their theta-z mean of each
+    level too."""
+    ref_ = ref(name, f"routine:{ns}:{routine}:{_REF_ARRAY.get(arr, arr)}")
+    if ns >= 2 and (routine, arr) in (("implicitandupdateqr", "qr"), ("calclocaldivergence", "div")):
+        nk = nrm + 1 if arr == "qr" else nrm
+        a, b = mine[1:-1, 1:-1, :nk], ref_[1:-1, 1:-1, :nk]
+        scale = float(np.abs(b).max())
+        return float(np.abs((a - a.mean(axis=(0, 1))) - (b - b.mean(axis=(0, 1)))).max()) / scale
+    if arr in ("dq", "qcap", "ru1", "ru3"):
+        a, b = mine[..., :nrm], ref_[..., :nrm]
+    elif arr == "ru2":
+        a, b = mine[..., 1:nrm], ref_[..., 1:nrm]
+    elif arr == "hr":
+        a, b = mine[..., 1:nrm], ref_[1:-1, 1:-1, 1:nrm]
+    elif arr == "qr":
+        a, b = mine[1:-1, 1:-1, :nrm + 1], ref_[1:-1, 1:-1, :nrm + 1]
+    elif arr in ("phi", "pr"):
+        scale = float(np.abs(ref_[1:-1, 1:-1, :nrm]).max())
+        return float(np.abs(pressure_fluct(mine, nrm) - pressure_fluct(ref_, nrm)).max()) / scale
+    else:
+        a, b = mine[1:-1, 1:-1, :nrm], ref_[1:-1, 1:-1, :nrm]
+    return relmax(a, b)

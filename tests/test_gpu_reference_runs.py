@@ -12,6 +12,8 @@ runs the loop) from the same seeded start and bou.in values:
 * the mixed forms (FP32 velocity side; FP64 or float-float pressure
   tridiagonals) on the production-like cases: velocities within 1e-3 of the
   velocity scale and torques within 1e-4 relative, each error printed;
+* every routine of a step's three substeps through the per-component
+  entry points, each against what the reference's routine left;
 * the statistics case: CalcStats / CalcDissipation accumulations within
   1e-10 of the reference's, and every HDF5 file the reference run wrote
   (slab and full-field dumps, statistics, continuation files) written
@@ -77,6 +79,38 @@ def test_fp64_matches_reference_run(gpu_lib, name):
     assert R.torque_error(ti, to, rt[1], rt[2]) <= TOL
     if rec["code"] != 169:
         assert g.check_divergence() < c["bou"]["resid"]
+    g.close()
+
+
+@pytest.mark.parametrize("name", R.ROUTINE_CASES)
+def test_fp64_routines_match_reference_run(gpu_lib, name):
+    """The per-component entry points, each right after it runs, against
+    what the reference's routine of the same name left in the first step
+    of the reference run (TimeMarcher.F90:31-54, three substeps): within
+    1e-10 (the divergence, phi and pr compared as refruns.routine_error
+    says)."""
+    c = R.case(name)
+    bou = R.run_bou(c)
+    nrm = int(bou["nrm"])
+    g = tc.TaylorCouette(bou)
+    g.set_state(*R.start(c))
+    g.begin_step(float(bou["dtmin"]), R.start_time(c))
+    calls = {"explicittermsqt": g.explicit_terms_qt, "explicittermsqr": g.explicit_terms_qr,
+             "explicittermsqz": g.explicit_terms_qz, "implicitandupdateqt": g.implicit_and_update_qt,
+             "implicitandupdateqr": g.implicit_and_update_qr, "implicitandupdateqz": g.implicit_and_update_qz,
+             "calclocaldivergence": g.calc_local_divergence, "solvepressurecorrection": g.solve_pressure_correction,
+             "correctvelocity": g.correct_velocity, "correctpressure": g.correct_pressure}
+    field = {"div": "dph", "phi": "dph"}
+    worst = {}
+    for ns in range(1, int(bou["nsst"]) + 1):
+        g.set_substep(ns)
+        for routine, arrays in R.ROUTINES:
+            calls[routine]()
+            for arr in arrays:
+                e = R.routine_error(name, ns, routine, arr, g.get_field(field.get(arr, arr)), nrm)
+                worst[f"{ns}:{routine}:{arr}"] = e
+                assert e <= TOL, (ns, routine, arr, e)
+    print(name, "worst", max(worst.items(), key=lambda kv: kv[1]))
     g.close()
 
 
