@@ -224,14 +224,17 @@ REF_DIR = os.environ.get("TC_REFERENCE_DIR", "/root/reference")
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF_DIR, "TimeMarcher.F90")),
                     reason="the reference tree is not on this machine")
-def test_fixture_reproduces_from_the_reference_source():
-    """Re-run the smallest case through the Fortran translator and get the
-    committed fixture back bit for bit."""
+@pytest.mark.parametrize("name", ["stops_at_tmax", "routine_outputs_of_one_step", "statistics_and_dumps",
+                                  "restart_interpolated_from_coarser_grid"])
+def test_fixture_reproduces_from_the_reference_source(name):
+    """Re-run small cases through the Fortran translator and get the
+    committed fixture back bit for bit (every key of the case)."""
     pytest.importorskip("scipy")
     import sys
     sys.path.insert(0, R.GOLDEN)
     import make_reference_runs as M
-    c = next(x for x in M.CASES if x["name"] == "stops_at_tmax")
+    c = next(x for x in M.CASES if x["name"] == name)
     out = M.run_case(REF_DIR, c)
+    assert set(out) == {k.split("/", 1)[1] for k in R.DATA if k.startswith(name + "/")}
     for k, v in out.items():
         np.testing.assert_array_equal(v, R.ref(c["name"], k), err_msg=k)
