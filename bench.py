@@ -12,9 +12,10 @@ step (three substeps) with the dt rule of main.F90, FP64 throughout.
 production-size case of the same path; "C1" the small CPU-runnable one.
 
   value  : steps with the state resident in HBM (tc_run, one host sync)
-  e2e    : through the C ABI with host buffers: tc_set_state from pinned host
-           memory, one tc_run(1) per step (the host reads dt/time back each
-           step, as the reference's host loop does), tc_get_state at the end
+  e2e    : through the C ABI with host buffers: tc_set_state from page-locked
+           host memory on huge pages (tc_host_alloc), one tc_run(1) per step
+           (the host reads dt/time back each step, as the reference's host
+           loop does), tc_get_state into the same kind of buffers at the end
   roofline: the kernel class with the largest share of the timed region,
            algorithmic HBM bytes per launch / its mean CUDA-event duration
   cpu_baseline: the CPU oracle (C++ restatement of the reference's serial
@@ -514,16 +515,16 @@ def main():
     g = tc.TaylorCouette(bou)
     g.set_stream(stream.cuda_stream)
 
-    # seeded start in pinned host memory (reference layout)
+    # seeded start in page-locked host memory on huge pages (reference layout)
     st = ini.couette_noise(bou, seed=1234 + rank)
     pinned = []
     for a in st:
-        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
-        t.numpy()[...] = a
-        pinned.append(t.numpy())
+        t = tc.host_array(a.shape)
+        t[...] = a
+        pinned.append(t)
     del st
-    # pinned host buffers for the end-to-end run's result
-    pinned_out = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy() for a in pinned]
+    # host buffers of the same kind for the end-to-end run's result
+    pinned_out = [tc.host_array(a.shape) for a in pinned]
     g.set_state(*pinned)
 
     # warm-up
@@ -580,7 +581,8 @@ def main():
                "ms_per_step": ms_e2e / args.steps,
                "parts": e2e_parts,
                "note": "state in (tc_set_state) and out (tc_get_state) once per timed run, from and into "
-                       "pinned host buffers, amortised per step; dt/time read back every step; one untimed "
+                       "page-locked host buffers on huge pages (tc_host_alloc), amortised per step; dt/time "
+                       "read back every step; one untimed "
                        "warm-up pass of the same calls on the same buffers before"}
         ref_state = tuple(a.copy() for a in (qt_o, qr_o, qz_o))
         ref_torque = g.calc_torque()

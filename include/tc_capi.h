@@ -28,6 +28,8 @@
 #ifndef TC_CAPI_H
 #define TC_CAPI_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -131,6 +133,18 @@ const char* tc_last_error(const tc_handle* h);   /* h may be NULL */
 /* Order all later work of h on this CUDA stream (cudaStream_t, NULL = the
  * legacy default stream). */
 int tc_set_stream(tc_handle* h, void* cuda_stream);
+
+/* Host memory for tc_set_state / tc_get_state and the other host arrays:
+ * `bytes` of zeroed, page-locked memory on transparent huge pages (aligned
+ * to the huge-page size), registered with the CUDA driver.  Copies from and
+ * into it keep the CPU-GPU link rate however long the GPU has been busy,
+ * which copies through memory of 64 KiB pages did not on the GB300 host.
+ * 1002 when the mapping fails, 1000 + cudaError_t when the registration
+ * does.  No counterpart in the reference (its arrays are Fortran
+ * allocatables). */
+int tc_host_alloc(size_t bytes, void** ptr);
+/* Unregister and unmap a tc_host_alloc buffer (2000 for any other pointer). */
+int tc_host_free(void* ptr);
 
 /* ---- state transfer (ReadFlowField.F90:135-140 / WriteFlowField) -------- */
 

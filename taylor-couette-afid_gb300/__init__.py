@@ -94,6 +94,8 @@ SIGNATURES = {
     "tc_last_error": (ctypes.c_char_p, [_vp]),
     "tc_set_stream": (ctypes.c_int, [_vp, _vp]),
     "tc_set_tmax": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "tc_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "tc_host_free": (ctypes.c_int, [_vp]),
     "tc_set_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "tc_get_state": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "tc_get_field": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
@@ -242,6 +244,24 @@ def selftest_conversions(n: int = 1 << 24) -> int:
     if rc != 0:
         raise TCError(rc, "tc_selftest_conversions")
     return v.value
+
+
+def host_array(shape, dtype=np.float64) -> np.ndarray:
+    """A zeroed host array in page-locked memory on transparent huge pages
+    (tc_host_alloc), for state transfers (set_state / get_state(out=...)):
+    they keep the CPU-GPU link rate however long the GPU has been busy.  The
+    memory is released when the array and every view of it are gone."""
+    import weakref
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    L = lib()
+    p = ctypes.c_void_p()
+    rc = L.tc_host_alloc(max(nbytes, 1), ctypes.byref(p))
+    if rc != 0:
+        raise TCError(rc, L.tc_last_error(None).decode())
+    buf = (ctypes.c_char * max(nbytes, 1)).from_address(p.value)
+    weakref.finalize(buf, L.tc_host_free, ctypes.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
 
 
 def h5_write(path: str, name: str, data: np.ndarray):

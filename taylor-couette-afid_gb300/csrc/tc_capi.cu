@@ -2,11 +2,16 @@
 // step sequence and the per-routine entry points, for the plain FP64 path
 // and the mixed FP32/FP64 path.
 
+#include <sys/mman.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -486,6 +491,67 @@ void tc_destroy(tc_handle* h) {
     for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     if (h->st_host) cudaFreeHost(h->st_host);
     delete h;
+}
+
+// ---- host buffers for state transfers -------------------------------------
+//
+// Page-locked host memory on transparent huge pages.  On the GB300 host
+// (64 KiB base pages, 512 MiB huge pages) a 13 GB state copy from or into
+// cudaHostAlloc'd memory ran at 190 GB/s right after allocation but slowed
+// to 25-60 GB/s once the GPU had run kernels for seconds in between
+// (tc_set_state of the 1024x768x512 state: 145, 531, 725 ms in three
+// rounds of 20 steps), while the same copies from anonymous memory on huge
+// pages registered with cudaHostRegister stayed at 68 ms in every round.
+
+namespace {
+std::mutex g_host_mu;
+std::map<void*, std::pair<void*, size_t>> g_host;   // buffer -> (mapping, length)
+
+size_t huge_page_bytes() {
+    size_t hp = 0;
+    if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+        unsigned long long v = 0;
+        if (std::fscanf(f, "%llu", &v) == 1) hp = (size_t)v;
+        std::fclose(f);
+    }
+    return hp >= 4096 && hp <= (size_t(1) << 30) ? hp : (size_t(2) << 20);
+}
+}  // namespace
+
+int tc_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr || bytes == 0) return fail(nullptr, 2000, "tc_host_alloc: null pointer or zero size");
+    *ptr = nullptr;
+    const size_t hp = huge_page_bytes();
+    const size_t span = (bytes + hp - 1) / hp * hp;
+    const size_t len = span + hp;                                      // room to align the start
+    void* base = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (base == MAP_FAILED) return fail(nullptr, 1002, "tc_host_alloc: mmap failed");
+    void* p = (void*)(((uintptr_t)base + hp - 1) / hp * hp);
+    madvise(p, span, MADV_HUGEPAGE);          // advisory: without huge pages the buffer still works
+    std::memset(p, 0, bytes);                 // fault the pages in before they are locked
+    cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        munmap(base, len);
+        return cuda_fail(nullptr, e, "tc_host_alloc: cudaHostRegister");
+    }
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    g_host[p] = {base, len};
+    *ptr = p;
+    return 0;
+}
+
+int tc_host_free(void* ptr) {
+    std::pair<void*, size_t> m;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        auto it = g_host.find(ptr);
+        if (it == g_host.end()) return fail(nullptr, 2000, "tc_host_free: not a tc_host_alloc buffer");
+        m = it->second;
+        g_host.erase(it);
+    }
+    cudaError_t e = cudaHostUnregister(ptr);
+    munmap(m.first, m.second);
+    return e == cudaSuccess ? 0 : cuda_fail(nullptr, e, "tc_host_free: cudaHostUnregister");
 }
 
 int tc_set_tmax(tc_handle* h, double tmax) {

@@ -291,6 +291,39 @@ def test_state_transfer_from_pinned_memory(gpu_lib, precision):
     h.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_state_transfer_through_host_arrays(gpu_lib, precision):
+    """tc_host_alloc buffers (page-locked, on huge pages) in and out give the
+    same fields as pageable arrays; the memory goes back when the arrays
+    do."""
+    import gc
+    bou = make_bou(nthm=40, nzm=36, nrm=22, istr=6, str=3.0)
+    st = ini.couette_noise(bou, seed=10)
+    ins = [tc.host_array(a.shape) for a in st]
+    outs = [tc.host_array(a.shape) for a in st]
+    for a, b in zip(ins, st):
+        assert not a.any() and a.ctypes.data % 4096 == 0
+        a[...] = b
+    g = tc.TaylorCouette(bou, precision=precision)
+    g.set_state(*ins)
+    g.time_marcher(1e-3, 0.0)
+    g.get_state(out=outs)
+    h = tc.TaylorCouette(bou, precision=precision)
+    h.set_state(*st)
+    h.time_marcher(1e-3, 0.0)
+    for a, b in zip(h.get_state(), outs):
+        np.testing.assert_array_equal(a, b)
+    g.close()
+    h.close()
+    del ins, outs, a, b
+    gc.collect()
+    for _ in range(3):                        # allocate and release again
+        x = tc.host_array((1 << 20,))
+        x[-1] = 1.0
+        del x
+        gc.collect()
+
+
 def test_error_codes(gpu_lib, oracle):
     """main.F90 exits: 166 (dt < DTMIN), 333 (time > TMAX), 555 (NTST)."""
     cases = [dict(dtmin=1e-2, dtmax=1e-3, nthm=16, nzm=16, nrm=12),

@@ -45,6 +45,15 @@ def test_library_exports_every_declared_symbol(gpu_lib):
     assert set(tc.SIGNATURES) == names
 
 
+def test_host_alloc_rejects_bad_arguments(gpu_lib):
+    """tc_host_alloc / tc_host_free argument checks (no GPU needed)."""
+    L = gpu_lib
+    p = ctypes.c_void_p()
+    assert L.tc_host_alloc(0, ctypes.byref(p)) == 2000
+    assert L.tc_host_alloc(16, None) == 2000
+    assert L.tc_host_free(ctypes.c_void_p(4096)) == 2000
+
+
 def test_read_bou(gpu_lib, tmp_path):
     p = tmp_path / "bou.in"
     p.write_text(BOU_TEXT)
