@@ -16,9 +16,18 @@ reference tree:
   ``halo_common.f90`` (the in-memory copies of its periodic planes);
 * MPI on one rank: broadcasts and reductions are identities;
 * HDF5: the continua fields that ``ReadFlowField`` reads come from arrays the
-  caller supplies; other file routines do nothing;
-* list-directed ``read`` from a ``bou.in`` text the caller supplies; records
-  written to chosen units (97: ``CalcTorque``) are kept.
+  caller supplies; the ``HdfRoutines.F90`` writers (``HdfCreateBlankFile``,
+  the serial scalar, 1-D and 2-D writers, ``HdfWriteReal2D``,
+  ``HdfWriteRealHalo3D``) record the datasets they leave in each file, with
+  the files' create-or-open semantics, and the readers of scalars and 2-D
+  arrays read those files back (statistics read at a restart);
+* ``QuitRoutine`` on a normal exit runs the reference's ``WriteStats`` and
+  ``WriteFlowField`` before the stop;
+* list-directed ``read`` from texts the caller supplies (``bou.in``,
+  ``rcuts.in``; a single implied-DO list is expanded), internal ``write``
+  with I edit descriptors (the time tags of the dump file names); records
+  written to chosen units (97: ``CalcTorque``, 92: ``CalcDissipation``, 98:
+  the velocity rms of ``CalcVelocityStats``) are kept.
 
 Arithmetic follows gfortran's x86-64 code for ``-O3 -fdefault-real-8``
 (no FMA contraction on that target): every real is a binary64, expressions

@@ -18,7 +18,13 @@ continua path (pressure zero), and runs until the reference's QuitRoutine
   the CheckDivergence maxima (the first one is the check before the loop);
 * the error code and ntime of the stop;
 * after the stop: CalcTorque, CheckDivergence and CalcMaxCFL of the final
-  state, called directly.
+  state, called directly;
+* where a case asks for them: the statistics accumulations, sample count
+  and dissipation records; every HDF5 file the run wrote (dumps, and
+  WriteStats / WriteFlowField / WriteGridInfo) and the files it was given;
+  what every routine of the first step's substeps wrote; the start that
+  CreateInitialConditions (NREAD = 0) or ReadFlowField's interpolation from
+  another grid built.
 
 Usage (needs the reference tree; SciPy for LAPACK):
 
