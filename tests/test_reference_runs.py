@@ -149,6 +149,21 @@ def test_created_initial_conditions_match_reference_run(name):
         np.testing.assert_array_equal(a[1:-1, 1:-1], R.ref(name, "start_" + k)[1:-1, 1:-1], err_msg=k)
 
 
+def test_bou_in_of_every_case_reads_back(tmp_path):
+    """The bou.in text each reference run read (ReadInputFile.F90), parsed
+    by the library's reader, gives the case's values exactly."""
+    from conftest import tc
+    import sys
+    sys.path.insert(0, R.GOLDEN)
+    import make_reference_runs as M
+    for c in R.CASES:
+        p = tmp_path / f"{c['name']}.in"
+        p.write_text(M.bou_text(c["bou"]))
+        got = tc.read_bou(str(p))
+        for k, v in c["bou"].items():
+            assert got[k] == v, (c["name"], k, got[k], v)
+
+
 def write_old_continua(directory, c):
     """The restart files of the restart case: the seeded start on the old
     grid written as continua_*.h5 (interior cells, C order)."""
