@@ -19,6 +19,7 @@ continua path (pressure zero), and runs until the reference's QuitRoutine
 * the error code and ntime of the stop;
 * after the stop: CalcTorque, CheckDivergence and CalcMaxCFL of the final
   state, called directly;
+* the 1-D grid and coefficient arrays of CreateGrid and InitPressureSolver;
 * where a case asks for them: the statistics accumulations, sample count
   and dissipation records; every HDF5 file the run wrote (dumps, and
   WriteStats / WriteFlowField / WriteGridInfo) and the files it was given;
@@ -65,6 +66,10 @@ FILES = ["main.F90", "ReadInputFile.F90", "InitTimeMarchScheme.F90", "InitVariab
          "CalcVorticity.F90", "CalcDissipation.F90", "interp.F90", "StatReadReduceWrite.F90", "WriteFlowField.F90",
          "DumpRCuts.F90", "DumpThCuts.F90", "DumpStreamwiseAvg.F90", "DumpFlowField.F90", "WriteGridInfo.F90",
          "CreateInitialConditions.F90"]
+# the 1-D arrays of CreateGrid and InitPressureSolver (module param)
+GRID_NAMES = ["rc", "rm", "g2rc", "g2rm", "usrc", "usrm", "udx1vis1", "udx1vis2", "udx1qm", "udx2c", "udx2m",
+              "rudx2c", "udx2rm", "ap1j", "am1j", "ac1j", "ap2j", "am2j", "ac2j", "ap2je", "am2je", "ac2je", "ap3j",
+              "am3j", "ac3j", "apph", "amph", "acph", "pvol", "udx2mm", "udx2cc", "ak1", "ak3"]
 STAT_NAMES = ["vt_me", "vr_me", "vz_me", "wt_me", "wr_me", "wz_me", "vt_rms", "vr_rms", "vz_rms", "wt_rms", "wr_rms",
               "wz_rms", "vtvr_me", "vtvz_me", "vrvz_me", "pr_me", "pr_rms", "disste"]
 MODULE_FILES = ["param.F90"]
@@ -375,6 +380,8 @@ def run_case(ref_dir, case, verbose=False, stop_after_read=False, nan_fill=True)
         for k, a in start.items():
             out["start_" + k] = a
     out.update(routines)
+    for n in GRID_NAMES:
+        out["grid_" + n] = np.array(getattr(G, n).d, dtype=np.float64).reshape(-1).copy()
     for fname, dsets in sorted(h5_in.items()):
         for dname, a in dsets.items():
             out[f"h5in:{fname}:{dname}"] = a

@@ -149,6 +149,21 @@ def test_created_initial_conditions_match_reference_run(name):
         np.testing.assert_array_equal(a[1:-1, 1:-1], R.ref(name, "start_" + k)[1:-1, 1:-1], err_msg=k)
 
 
+def test_grid_arrays_match_reference_runs():
+    """The library's CreateGrid / InitPressureSolver arrays (host code, the
+    same the device uses) equal the reference's, bit for bit, for every
+    case's grid (ISTR 0, 4, 6, several STR3, NRM, NTM, NZM, RINT/REXT, LAMB,
+    ALX3D); ak1 and ak3 over the entries the reference sets."""
+    from conftest import tc
+    for name in R.CASE_NAMES:
+        bou = R.case(name)["bou"]
+        for g in tc.GRID_ARRAYS:
+            a, b = tc.grid_array(bou, g), R.ref(name, "grid_" + g)
+            m = {"ak1": int(bou["nthm"]), "ak3": int(bou["nzm"])}.get(g, len(b))
+            assert len(a) >= m, (name, g, len(a), m)
+            np.testing.assert_array_equal(a[:m], b[:m], err_msg=f"{name} {g}")
+
+
 def test_bou_in_of_every_case_reads_back(tmp_path):
     """The bou.in text each reference run read (ReadInputFile.F90), parsed
     by the library's reader, gives the case's values exactly."""
