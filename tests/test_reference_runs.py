@@ -112,6 +112,35 @@ def test_oracle_routines_match_reference_run(oracle, name):
     print(name, "worst", max(worst.items(), key=lambda kv: kv[1]))
 
 
+NP_CASES = [n for n in R.CASE_NAMES
+            if R.case(n)["bou"]["minstrt"] * R.case(n)["bou"]["multmin"] == 0 and R.case(n).get("planes") is None
+            and int(R.case(n)["bou"]["nthm"]) * int(R.case(n)["bou"]["nzm"]) * int(R.case(n)["bou"]["nrm"]) <= 4096
+            and not R.case(n).get("start_time")]
+
+
+@pytest.mark.parametrize("name", NP_CASES)
+def test_numpy_oracle_matches_reference_run(name):
+    """The second restatement (oracle/tc_np.py: whole-array NumPy, LAPACK
+    through SciPy with the reference's roundoff pivot of the singular mode)
+    on the reference's own dt sequence: velocities within 1e-12 of the
+    reference run's, the pressure (radial profile removed) within 1e-10."""
+    pytest.importorskip("scipy")
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(R.GOLDEN), "..", "oracle"))
+    import tc_np
+    c = R.case(name)
+    n = tc_np.NpOracle(c["bou"], pin_mode00=False)
+    n.set_state(*R.start(c))
+    times = np.concatenate([[0.0], R.ref(name, "step_time")[:-1]])
+    for dt, t in zip(R.ref(name, "step_dt"), times):
+        n.time_marcher(float(dt), float(t))
+    fe = R.field_errors(c, (n.qt, n.qr, n.qz, n.pr))
+    print(name, {k: f"{v:.1e}" for k, v in fe.items()})
+    for k in ("qt", "qr", "qz"):
+        assert fe[k] <= TOL_Q, (k, fe[k])
+    assert fe["pr"] <= 1e-10, fe["pr"]
+
+
 @pytest.mark.parametrize("name", R.STATS_CASES)
 def test_oracle_statistics_match_reference_run(oracle, name):
     """CalcStats + CalcDissipation at the output steps after TSTA
