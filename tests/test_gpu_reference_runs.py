@@ -10,8 +10,9 @@ runs the loop) from the same seeded start and bou.in values:
   and CheckDivergence maxima within 1e-10 relative,
   the same stop code at the same step;
 * the mixed forms (FP32 velocity side; FP64 or float-float pressure
-  tridiagonals) on the production-like cases: velocities within 1e-3 of the
-  velocity scale and torques within 1e-4 relative, each error printed;
+  tridiagonals) on every case that keeps its whole fields: velocities within
+  1e-3 of the velocity scale and torques within 1e-4 relative, each error
+  printed;
 * every routine of a step's three substeps through the per-component
   entry points, each against what the reference's routine left;
 * the statistics case: CalcStats / CalcDissipation accumulations within
@@ -225,9 +226,11 @@ def test_output_files_match_reference_run(gpu_lib, tmp_path, name):
         assert v <= TOL, (k, v)
 
 
+MIXED_CASES = [n for n in R.CASE_NAMES if R.case(n).get("planes") is None and not R.case(n).get("start_time")]
+
+
 @pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
-@pytest.mark.parametrize("name", ["production_oscillating_32x24x32", "rotating_32x24x32",
-                                  "chebyshev_rk3_rotating", "prime_lengths_7_13", "created_initial_conditions"])
+@pytest.mark.parametrize("name", MIXED_CASES)
 def test_mixed_against_reference_run(gpu_lib, name, precision):
     """The mixed forms on the reference's own time grid: the dt sequence of
     the reference run is imposed (each form's own CFL rule would pick a
@@ -245,12 +248,13 @@ def test_mixed_against_reference_run(gpu_lib, name, precision):
            for k, a, nk in zip(("qt", "qr", "qz"), st[:3], (nrm, nrm + 1, nrm))}
     ti, to = g.calc_torque()
     rt = R.ref(name, "final_torque")
-    terr = max(abs(ti - rt[1]) / abs(rt[1]), abs(to - rt[2]) / abs(rt[2]))
+    terr = R.torque_error(ti, to, rt[1], rt[2])
     print(name, precision, {k: f"{v:.1e}" for k, v in err.items()}, f"torque {terr:.1e}",
           f"div {g.check_divergence():.1e}")
     assert max(err.values()) <= TOL_MIXED_Q
     assert terr <= TOL_MIXED_TORQUE
-    assert g.check_divergence() < c["bou"]["resid"]
+    if int(R.ref(name, "errorcode")) != 169:
+        assert g.check_divergence() < c["bou"]["resid"]
     g.close()
 
 
