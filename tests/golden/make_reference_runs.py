@@ -159,6 +159,12 @@ CASES = [
     # kept on four theta planes plus whole-field sums
     dict(name="c1_64cubed_5_steps", seed=2024, amp=0.01, planes=[1, 17, 33, 64],
          bou=base_bou(nthm=64, nzm=64, nrm=64, ntst=4)),
+    # the parameters of the 1024x768x512 benchmark (wall-clustered grid
+    # ISTR=6 STR3=20, ROTP=0.1, 1/NU=2e4, variable dt with CFLMAX=1.2 and
+    # DTMAX=1.8e-4) on a 128x96x64 grid, 5 steps; some theta planes kept
+    dict(name="c3_parameters_128x96x64_5_steps", seed=1234, amp=0.01, planes=[1, 33, 65, 128],
+         bou=base_bou(nthm=128, nzm=96, nrm=64, istr=6, str=20.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
+                      dtmin=1e-5, dtmax=1.8e-4, ntst=4)),
     # statistics on (TSTA = 0): main.F90 calls CalcStats (with
     # CalcVorticity) and CalcDissipation at every output step
     # statistics every output step, radial/theta/streamwise-average slabs
