@@ -165,6 +165,11 @@ CASES = [
     dict(name="c3_parameters_128x96x64_5_steps", seed=1234, amp=0.01, planes=[1, 33, 65, 128],
          bou=base_bou(nthm=128, nzm=96, nrm=64, istr=6, str=20.0, ren=2e4, romeg=0.1, idtv=1, limitCFL=1.2,
                       dtmin=1e-5, dtmax=1.8e-4, ntst=4)),
+    # the parameters of the 512x512x384 production case (ISTR=6 STR3=20,
+    # 1/NU=5000, the oscillating inner cylinder, DTMAX=3e-4) on 96x128x48
+    dict(name="c2_parameters_96x128x48_5_steps", seed=1234, amp=0.01, planes=[1, 25, 49, 96],
+         bou=base_bou(nthm=96, nzm=128, nrm=48, istr=6, str=20.0, ren=5000.0, sizepert=0.1, omegapert=0.5,
+                      idtv=1, limitCFL=1.2, dtmin=1e-5, dtmax=3e-4, ntst=4)),
     # statistics on (TSTA = 0): main.F90 calls CalcStats (with
     # CalcVorticity) and CalcDissipation at every output step
     # statistics every output step, radial/theta/streamwise-average slabs
