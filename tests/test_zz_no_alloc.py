@@ -100,3 +100,30 @@ def test_noalloc_rejects_too_many_radial_cells(gpu_lib):
         tc.check_divergence_noalloc(buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), 4, 4, 8193, coef, coef,
                                     1.0, 1.0)
     assert e.value.code == 2016 and "8192" in str(e.value)
+
+
+def test_noalloc_divergence_matches_reference_runs(gpu_lib):
+    """On the start and on the final fields of every reference run that
+    keeps its whole fields: the reference's CheckDivergence before the loop
+    (main.F90:125; O(1) for these starts) within 1e-13 relative, and after
+    the run (roundoff) within 1e-13 absolute."""
+    import torch
+    import refruns as R
+    for name in R.CASE_NAMES:
+        c = R.case(name)
+        if c.get("planes") is not None:
+            continue
+        bou = c["bou"]
+        nthm, nzm, nrm = int(bou["nthm"]), int(bou["nzm"]), int(bou["nrm"])
+        udx2m, usrm = tc.grid_array(bou, "udx2m"), tc.grid_array(bou, "usrm")
+        dxt = nthm * bou["lamb"] / (2.0 * math.pi)
+        dxz = nzm / bou["alx3"]
+        for fields, want, rel in ((R.start(c)[:3], float(R.ref(name, "out_dmax")[0]), True),
+                                  ([R.ref(name, k) for k in ("qt", "qr", "qz")], float(R.ref(name, "final_dmax")),
+                                   False)):
+            dq = [_device_copy(a) for a in fields]
+            torch.cuda.synchronize()
+            got = tc.check_divergence_noalloc(dq[0].data_ptr(), dq[1].data_ptr(), dq[2].data_ptr(), nthm, nzm, nrm,
+                                              udx2m, usrm, dxt, dxz)
+            err = abs(got - want) / (want if rel else 1.0)
+            assert err <= 1e-13, (name, rel, got, want)
