@@ -126,6 +126,17 @@ CASES = [
                       dtmin=1e-5, dtmax=1.8e-3, tout=5e-3)),
     dict(name="uniform_ab2", seed=14, amp=0.01,
          bou=base_bou(nthm=12, nzm=12, nrm=8, nsst=1, dtmin=5e-4, dtmax=5e-4)),
+    # AB2 with the dt rule: the multistep weights stay those of a constant
+    # step while dt changes (InitTimeMarchScheme.F90)
+    dict(name="ab2_variable_dt_tanh", seed=29, amp=0.03,
+         bou=base_bou(nthm=16, nzm=12, nrm=10, nsst=1, istr=4, str=2.0, idtv=1, limitCFL=0.4, dtmin=1e-4,
+                      dtmax=2e-3, ntst=14, tout=3e-3)),
+    # patterned slip on the oscillating, rotating inner cylinder over many
+    # steps (the slip pattern moves with the wall, SlipBCs.F90)
+    dict(name="patterned_slip_oscillating_rotating", seed=30, amp=0.02,
+         bou=base_bou(nthm=16, nzm=16, nrm=8, minstrt=2, minstrz=2, multmin=1, rext=1.5, alx3=2.0, istr=6,
+                      str=3.0, sizepert=0.15, omegapert=2.0, romeg=0.1, ntst=14, dtmin=2e-3, dtmax=2e-3,
+                      tout=6e-3)),
     dict(name="patterned_slip", seed=15, amp=0.01,
          bou=base_bou(nthm=16, nzm=16, nrm=8, minstrt=2, minstrz=2, multmin=1, ntst=9, virotint=1.0,
                       rext=1.5, lamb=1.0, alx3=2.0)),
