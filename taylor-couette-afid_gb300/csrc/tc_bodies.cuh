@@ -1208,7 +1208,7 @@ template <> struct SweepV<F2, float> {
 };
 
 // ImplicitAndUpdateQR.F90:70-71: after the update both wall faces of qr are
-// zero.  A start may hold other wall values (CreateInitialConditions.F90:30
+// zero.  A start may hold other wall values (CreateInitialConditions.F90:33-34
 // sets the inner one); the reference reads them until the first update, and
 // so does the device.
 template <typename T>
